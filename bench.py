@@ -1,0 +1,433 @@
+#!/usr/bin/env python
+"""Benchmark of the HAL-CPP hot path on one GB300 (or N replicas).
+
+Headline workload (one "step"): 200 ADI ticks of a 2048x2048 FP32 field at
+D*dt/dx^2 = 5.0, decay 0.01, a constant source field, zero-flux edges
+(f' = ADI(f) - 0.01 f + s per tick, PDEGrid2D semantics).  The metric is
+cell-updates per second over all GPUs.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+* value      -- device time of the resident run (inputs already in HBM),
+                L2 flushed between steps (a 512 MB write), CUDA events on the
+                handle's stream.
+* e2e        -- the same ticks through hal_cuda_adi_run_ticks_host: field and
+                source copied in from pinned host memory and the field copied
+                back, inside the timed region, every step.
+* roofline   -- the dominant kernel's algorithmic bytes per launch over its
+                CUDA-event launch time (hal_cuda_adi_profile), against the
+                measured HBM copy bandwidth.
+* cpu_baseline -- the CPU oracle (a C restatement of the reference's FP64 CPU
+                backend, 1 thread as the reference ships) on a bounded sample.
+* secondary  -- the explicit 2048^2 tick and the 1M-agent force pass.
+
+--impl reference times the CPU oracle alone (all host threads) on the same
+workload, one bounded sample per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "hal-cpp_gb300"))
+
+N = 2048
+TICKS = 200
+RATE = 5.0
+DECAY = 0.01
+CELLS = N * N
+ADI_COL_BYTES = 8    # x-sweep: read f, write w (FP32)
+ADI_ROW_BYTES = 16   # y-sweep: read w, f, src; write f'
+EXPLICIT_BYTES = 8   # fused tick: read f, write f'
+FLUSH_BYTES = 512 << 20
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    return rank, local, world
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join("/tmp", f"hal_bench_clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-i", str(self.device), "-lms", "100"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        with open(self.path) as fh:
+            for line in fh:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for name, val in zip(names[1:], parts[5:9]):
+                    if val.lower().startswith("active"):
+                        reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def profile_traffic(kernel):
+    """DRAM bytes per launch recorded by an ncu capture under profiles/
+    ("traffic_bytes_per_launch <kernel> <value>" lines), or None."""
+    pdir = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(pdir):
+        return None
+    for name in sorted(os.listdir(pdir)):
+        if not name.endswith((".md", ".txt")):
+            continue
+        with open(os.path.join(pdir, name)) as fh:
+            for line in fh:
+                parts = line.replace("`", " ").split()
+                if len(parts) >= 3 and parts[0] == "traffic_bytes_per_launch" and parts[1] == kernel:
+                    try:
+                        return float(parts[2])
+                    except ValueError:
+                        pass
+    return None
+
+
+def cpu_baseline_adi(threads, min_seconds=8.0, max_ticks=40):
+    """The oracle's FP64 ADI tick on the full 2048^2 workload, timed on the
+    host; returns (cell-updates/s, ticks timed)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    from halcuda import workloads
+
+    pyoracle.build(ref=False)
+    w = workloads.adi_inputs(N, seed=2)
+    f = w["field"].copy()
+    src = w["src"]
+    # one untimed tick to page everything in
+    f = pyoracle.Oracle.run_ticks(1, f, N, N, RATE, decay=DECAY, src_dense=src, ticks=1,
+                                  threads=threads)
+    ticks = 0
+    t0 = time.perf_counter()
+    while ticks < max_ticks:
+        f = pyoracle.Oracle.run_ticks(1, f, N, N, RATE, decay=DECAY, src_dense=src, ticks=1,
+                                      threads=threads)
+        ticks += 1
+        if time.perf_counter() - t0 >= min_seconds and ticks >= 2:
+            break
+    dt = time.perf_counter() - t0
+    return ticks * CELLS / dt, ticks, dt
+
+
+def run_reference(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    from halcuda import workloads
+
+    pyoracle.build(ref=False)
+    w = workloads.adi_inputs(N, seed=2)
+    f = w["field"].copy()
+    ticks_per_sample = 4
+    for _ in range(args.warmup):
+        f = pyoracle.Oracle.run_ticks(1, f, N, N, RATE, decay=DECAY, src_dense=w["src"],
+                                      ticks=ticks_per_sample, threads=threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        f = pyoracle.Oracle.run_ticks(1, f, N, N, RATE, decay=DECAY, src_dense=w["src"],
+                                      ticks=ticks_per_sample, threads=threads)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = ticks_per_sample * CELLS * len(times) / total
+    sample = (f"{ticks_per_sample} FP64 ADI ticks of the 2048x2048 workload per step "
+              f"(oracle C restatement, {threads} threads)")
+    line = {
+        "impl": "reference", "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / len(times), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_block(world),
+        "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def config_block(world):
+    return {"workload": f"adi-{N}x{N}-r{RATE:g}-decay{DECAY:g}-source-zeroflux-{TICKS}ticks",
+            "grid": [N, N], "ticks_per_step": TICKS, "diffRate": RATE, "decay": DECAY,
+            "boundaries": "zero-flux", "precision": "fp32 device, fp64 plan",
+            "l2": "flushed between steps (512 MB write)",
+            "parallelism": f"replicas x{world}"}
+
+
+def secondary_explicit(hal, torch, stream, warm=5, iters=50):
+    from halcuda import workloads
+
+    w = workloads.explicit_inputs(N, seed=1)
+    with hal.Diffusion(N, N) as d:
+        d.set_stream(stream.cuda_stream)
+        d.set_field(w["field"])
+        d.set_point_sources(w["src_idx"], w["src_val"])
+        d.run_ticks(warm * 10, 0.2, 0.001)
+        d.sync()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ticks = 100
+        times = []
+        for _ in range(iters // 10 or 1):
+            ev0.record(stream)
+            d.run_ticks(ticks, 0.2, 0.001)
+            ev1.record(stream)
+            ev1.synchronize()
+            times.append(ev0.elapsed_time(ev1))
+        ms_tick = min(times) / ticks
+        ms_launch = d.profile(iters, 0.2, 0.001)
+    peak, _ = peaks()
+    ach = EXPLICIT_BYTES * CELLS / (ms_launch * 1e-3) / 1e9
+    return {"workload": "explicit-2048x2048-r0.2-decay0.001-64sources-zeroflux",
+            "value": CELLS / (ms_tick * 1e-3), "unit": "cell-updates/s",
+            "ms_per_tick_graph": ms_tick,
+            "roofline": {"kernel": "TickKernel", "bound": "hbm", "achieved": ach, "peak": peak,
+                         "unit": "GB/s", "frac": ach / peak,
+                         "traffic": profile_traffic("TickKernel")},
+            "note": "100-tick graph replays; 33.5 MB ping-pong set is L2-resident"}
+
+
+def secondary_agents(hal, stream, iters=20):
+    from halcuda import workloads
+
+    w = workloads.agent_inputs(1_000_000, N, seed=3)
+    n = w["radii"].size
+    with hal.Agents(N, N, n) as ag:
+        ag.set_stream(stream.cuda_stream)
+        ag.upload(w["positions"], w["radii"])
+        ag.profile(3, 1.0, 0.1)
+        ms = ag.profile(iters, 1.0, 0.1)
+    # algorithmic bytes of the whole dispatch: 28 B/agent + 16 B/bin
+    bytes_tick = 28 * n + 16 * CELLS
+    peak, _ = peaks()
+    ach = bytes_tick / (ms[5] * 1e-3) / 1e9
+    return {"workload": "agents-1M-in-2048x2048-R1-k0.1-walls",
+            "value": n / (ms[5] * 1e-3), "unit": "agents/s",
+            "ms_per_dispatch": ms[5],
+            "ms_by_stage": {"count": ms[0], "scan": ms[1], "scatter": ms[2], "stabilize": ms[3],
+                            "forces": ms[4]},
+            "roofline": {"kernel": "whole dispatch", "bound": "hbm", "achieved": ach,
+                         "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "traffic": None}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-secondary", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    import halcuda as hal
+    from halcuda import workloads
+
+    rank, local, world = dist_env()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    if hal.lib().hal_cuda_set_device(local) != 0:
+        raise RuntimeError(hal.last_error())
+
+    w = workloads.adi_inputs(N, seed=2)
+    field = torch.from_numpy(w["field"].astype(np.float32)).pin_memory()
+    src = torch.from_numpy(w["src"].astype(np.float32)).pin_memory()
+    field_np = field.numpy()
+    src_np = src.numpy()
+    stream = torch.cuda.Stream()
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    adi = hal.Adi(N, N)
+    adi.set_stream(stream.cuda_stream)
+    adi.set_field(field_np)
+    adi.set_source(src_np)
+
+    def one_step():
+        adi.run_ticks(TICKS, RATE, DECAY)
+
+    # warm-up (also captures the graph)
+    for _ in range(args.warmup):
+        one_step()
+    adi.sync()
+
+    ev_s = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev_e = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = Clocks(local)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = hal.launch_count()
+    clocks.start()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        ev_s[k].record(stream)
+        one_step()
+        ev_e[k].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = hal.launch_count() - launches0
+    if dist is not None:
+        dist.barrier()
+    total_ms = sum(s.elapsed_time(e) for s, e in zip(ev_s, ev_e))
+    if dist is not None:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_step = total_ms / args.steps
+    value = world * CELLS * TICKS / (ms_step * 1e-3)
+
+    # per-kernel launch times (CUDA events around each launch, same data)
+    adi.profile(5, RATE, DECAY)
+    ms_col, ms_row = adi.profile(50, RATE, DECAY)
+    col_gbs = ADI_COL_BYTES * CELLS / (ms_col * 1e-3) / 1e9
+    row_gbs = ADI_ROW_BYTES * CELLS / (ms_row * 1e-3) / 1e9
+    if ms_row >= ms_col:
+        dom, dom_gbs, dom_bytes = "AdiRowSweep", row_gbs, ADI_ROW_BYTES
+    else:
+        dom, dom_gbs, dom_bytes = "AdiColumnSweep", col_gbs, ADI_COL_BYTES
+    peak, peak_kind = peaks()
+    tick_gbs = (ADI_COL_BYTES + ADI_ROW_BYTES) * CELLS / ((ms_col + ms_row) * 1e-3) / 1e9
+
+    # end to end through the host-buffer C-ABI call
+    out_host = torch.empty_like(field).pin_memory()
+    out_np = out_host.numpy()
+    for _ in range(2):
+        adi.run_ticks_host(field_np, src_np, TICKS, RATE, DECAY, out=out_np)
+    e2e_ms = []
+    for _ in range(max(3, min(args.steps, 10))):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        adi.run_ticks_host(field_np, src_np, TICKS, RATE, DECAY, out=out_np)
+        t1.record(stream)
+        t1.synchronize()
+        e2e_ms.append(t0.elapsed_time(t1))
+    e2e_step = statistics.median(e2e_ms)
+    if dist is not None:
+        t = torch.tensor([e2e_step], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_step = float(t.item())
+    e2e_value = world * CELLS * TICKS / (e2e_step * 1e-3)
+
+    secondary = None
+    if not args.no_secondary and rank == 0:
+        secondary = {"explicit": secondary_explicit(hal, torch, stream),
+                     "agents": secondary_agents(hal, stream)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, ticks, dt = cpu_baseline_adi(threads=1)
+        cpu = {"value": v, "unit": "cell-updates/s", "cores": 1, "kind": "port",
+               "sample": f"{ticks} FP64 ticks of the same 2048x2048 ADI workload "
+                         f"({dt:.1f} s, 1 thread, as the reference CPU backend ships)"}
+
+    adi.close()
+    if rank == 0:
+        line = {
+            "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: 200 seeded Gaussian blobs, U[0,0.01) source (numpy PCG64)",
+            "config": config_block(world),
+            "roofline": {"kernel": dom, "bound": "hbm", "achieved": dom_gbs, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": dom_gbs / peak,
+                         "traffic": profile_traffic(dom),
+                         "bytes_per_launch": dom_bytes * CELLS,
+                         "launch_ms": {"AdiColumnSweep": ms_col, "AdiRowSweep": ms_row},
+                         "achieved_by_kernel": {"AdiColumnSweep": col_gbs, "AdiRowSweep": row_gbs},
+                         "tick_achieved": tick_gbs,
+                         "note": "working set (3 x 16.8 MB + scratch) stays in the 126 MB L2 "
+                                 "across the ticks of a step"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "cell-updates/s",
+                    "h2d_bytes_per_step": 2 * CELLS * 4, "d2h_bytes_per_step": CELLS * 4,
+                    "ms_per_step": e2e_step,
+                    "call": "hal_cuda_adi_run_ticks_host (pinned host field + source in, field out)"},
+            "gpu_launches": int(launches),
+            "clocks": clk,
+            "secondary": secondary,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,707 @@
+// agents.cu -- cell-bucket agent forces (IAgentForceBackend2D) on sm_103a.
+//
+// The CPU backend (src/Agents/CpuAgentForceBackend2D.cpp:66-176) runs four
+// serial passes: count agents per cell, exclusive prefix into offsets, stable
+// scatter of agent indices, and a per-agent scan of the surrounding cells
+// summing a linear spring force.  Here each pass is data-parallel:
+//   BinCount     one thread per agent: clamped cell, atomic count, arrival rank
+//   scan         reduce-then-scan over the cells (three launches, no spin waits)
+//   Scatter      agent -> offsets[cell] + arrival rank (order within a cell is
+//                the atomic arrival order, not yet the CPU's)
+//   Stabilize    each agent counts the lower-indexed agents of its cell, which
+//                gives exactly the CPU's slot; it writes the final bucket and a
+//                cell-sorted copy of positions and radii
+//   Forces       one thread per sorted slot walks the cell window x-major then
+//                y, and each cell's slots in order -- the CPU's summation
+//                order -- and writes the agent's velocity delta.
+// The binning is integer work and matches the CPU bit for bit (positions are
+// float32 on the device; the CPU fed the same float32 values bins
+// identically).  The force sum runs in FP32 on the resident path and in FP64
+// with IEEE round-to-nearest operations (no contraction) on the FP64
+// interface path, where it matches the CPU backend bit for bit for float32
+// positions.
+#include "common.cuh"
+
+#include <cmath>
+
+namespace halcuda
+{
+    namespace
+    {
+        constexpr int kScanThreads = 1024;
+        constexpr int kScanItems = 4;
+        constexpr int kScanTile = kScanThreads * kScanItems;
+
+        // AgentForceCellCoord (CpuAgentForceBackend2D.cpp:14-27).
+        __device__ __forceinline__ int32_t CellCoord(float v, int32_t dim)
+        {
+            int32_t c = static_cast<int32_t>(floorf(v));
+            c = (c < 0) ? 0 : c;
+            c = (c >= dim) ? dim - 1 : c;
+            return c;
+        }
+
+        template <typename TP>
+        __global__ void BinCount(const TP *__restrict__ pos, int32_t n, int32_t xDim, int32_t yDim,
+                                 float2 *__restrict__ posF, int32_t *__restrict__ cellOf,
+                                 int32_t *__restrict__ arrival, int32_t *__restrict__ counts)
+        {
+            int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+            if (i >= n)
+            {
+                return;
+            }
+            float px = static_cast<float>(pos[2 * static_cast<int64_t>(i)]);
+            float py = static_cast<float>(pos[2 * static_cast<int64_t>(i) + 1]);
+            posF[i] = make_float2(px, py);
+            int32_t c = CellCoord(px, xDim) * yDim + CellCoord(py, yDim);
+            cellOf[i] = c;
+            arrival[i] = atomicAdd(counts + c, 1);
+        }
+
+        // Inclusive warp scan.
+        __device__ __forceinline__ int32_t WarpScan(int32_t v, int lane)
+        {
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1)
+            {
+                int32_t t = __shfl_up_sync(0xffffffffu, v, d);
+                if (lane >= d)
+                {
+                    v += t;
+                }
+            }
+            return v;
+        }
+
+        // Exclusive block scan of one value per thread; returns the block total.
+        __device__ __forceinline__ int32_t BlockExclusiveScan(int32_t v, int32_t &excl)
+        {
+            __shared__ int32_t warpSums[32];
+            const int lane = threadIdx.x & 31;
+            const int warp = threadIdx.x >> 5;
+            const int nwarps = blockDim.x >> 5;
+            int32_t inc = WarpScan(v, lane);
+            if (lane == 31)
+            {
+                warpSums[warp] = inc;
+            }
+            __syncthreads();
+            if (warp == 0)
+            {
+                int32_t s = (lane < nwarps) ? warpSums[lane] : 0;
+                int32_t si = WarpScan(s, lane);
+                if (lane < nwarps)
+                {
+                    warpSums[lane] = si - s;  // exclusive prefix of the warp sums
+                }
+            }
+            __syncthreads();
+            excl = inc - v + warpSums[warp];
+            __shared__ int32_t s_total;
+            if (threadIdx.x == blockDim.x - 1)
+            {
+                s_total = excl + v;
+            }
+            __syncthreads();
+            const int32_t total = s_total;
+            __syncthreads();
+            return total;
+        }
+
+        // Pass 1 of the scan: per-tile sums.
+        __global__ void __launch_bounds__(kScanThreads) ScanReduce(const int32_t *__restrict__ counts, int64_t C,
+                                                                   int32_t *__restrict__ tileSums)
+        {
+            int64_t base = static_cast<int64_t>(blockIdx.x) * kScanTile + threadIdx.x * kScanItems;
+            int32_t s = 0;
+#pragma unroll
+            for (int q = 0; q < kScanItems; q++)
+            {
+                if (base + q < C)
+                {
+                    s += counts[base + q];
+                }
+            }
+            int32_t excl;
+            int32_t total = BlockExclusiveScan(s, excl);
+            if (threadIdx.x == 0)
+            {
+                tileSums[blockIdx.x] = total;
+            }
+        }
+
+        // Pass 2: exclusive scan of the tile sums by one CTA (looping over
+        // chunks of kScanThreads).
+        __global__ void __launch_bounds__(kScanThreads) ScanTiles(int32_t *__restrict__ tileSums, int32_t nTiles)
+        {
+            int32_t carry = 0;
+            for (int32_t base = 0; base < nTiles; base += kScanThreads)
+            {
+                int32_t idx = base + threadIdx.x;
+                int32_t v = (idx < nTiles) ? tileSums[idx] : 0;
+                int32_t excl;
+                int32_t total = BlockExclusiveScan(v, excl);
+                if (idx < nTiles)
+                {
+                    tileSums[idx] = carry + excl;
+                }
+                carry += total;
+            }
+        }
+
+        // Pass 3: tile-local exclusive scan plus the tile prefix -> offsets.
+        __global__ void __launch_bounds__(kScanThreads) ScanApply(const int32_t *__restrict__ counts, int64_t C,
+                                                                  const int32_t *__restrict__ tilePrefix,
+                                                                  int32_t *__restrict__ offsets, int32_t n)
+        {
+            int64_t base = static_cast<int64_t>(blockIdx.x) * kScanTile + threadIdx.x * kScanItems;
+            int32_t v[kScanItems];
+            int32_t s = 0;
+#pragma unroll
+            for (int q = 0; q < kScanItems; q++)
+            {
+                v[q] = (base + q < C) ? counts[base + q] : 0;
+                s += v[q];
+            }
+            int32_t excl;
+            BlockExclusiveScan(s, excl);
+            int32_t run = tilePrefix[blockIdx.x] + excl;
+#pragma unroll
+            for (int q = 0; q < kScanItems; q++)
+            {
+                if (base + q < C)
+                {
+                    offsets[base + q] = run;
+                }
+                run += v[q];
+            }
+            if (blockIdx.x == 0 && threadIdx.x == 0)
+            {
+                offsets[C] = n;
+            }
+        }
+
+        __global__ void Scatter(const int32_t *__restrict__ cellOf, const int32_t *__restrict__ arrival,
+                                const int32_t *__restrict__ offsets, int32_t n, int32_t *__restrict__ bucketTmp)
+        {
+            int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+            if (i >= n)
+            {
+                return;
+            }
+            bucketTmp[offsets[cellOf[i]] + arrival[i]] = i;
+        }
+
+        // The CPU scatters in agent-index order (CpuAgentForceBackend2D.cpp:
+        // 100-109), so an agent's slot within its cell is the number of
+        // lower-indexed agents in the same cell.
+        template <typename TR>
+        __global__ void Stabilize(const int32_t *__restrict__ cellOf, const int32_t *__restrict__ offsets,
+                                  const int32_t *__restrict__ bucketTmp, const float2 *__restrict__ posF,
+                                  const TR *__restrict__ rad, int32_t n, int32_t *__restrict__ bucket,
+                                  float2 *__restrict__ sPos, TR *__restrict__ sRad)
+        {
+            int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+            if (i >= n)
+            {
+                return;
+            }
+            int32_t c = cellOf[i];
+            int32_t s = offsets[c];
+            int32_t e = offsets[c + 1];
+            int32_t rank = 0;
+            for (int32_t q = s; q < e; q++)
+            {
+                rank += (bucketTmp[q] < i) ? 1 : 0;
+            }
+            int32_t slot = s + rank;
+            bucket[slot] = i;
+            sPos[slot] = posF[i];
+            sRad[slot] = rad[i];
+        }
+
+        // IEEE-exact FP64 helpers (no contraction) and their FP32 twins.
+        __device__ __forceinline__ double Add(double a, double b) { return __dadd_rn(a, b); }
+        __device__ __forceinline__ double Sub(double a, double b) { return __dsub_rn(a, b); }
+        __device__ __forceinline__ double Mul(double a, double b) { return __dmul_rn(a, b); }
+        __device__ __forceinline__ double Div(double a, double b) { return __ddiv_rn(a, b); }
+        __device__ __forceinline__ double Sqrt(double a) { return __dsqrt_rn(a); }
+        __device__ __forceinline__ float Add(float a, float b) { return __fadd_rn(a, b); }
+        __device__ __forceinline__ float Sub(float a, float b) { return __fsub_rn(a, b); }
+        __device__ __forceinline__ float Mul(float a, float b) { return __fmul_rn(a, b); }
+        __device__ __forceinline__ float Div(float a, float b) { return __fdiv_rn(a, b); }
+        __device__ __forceinline__ float Sqrt(float a) { return __fsqrt_rn(a); }
+        __device__ __forceinline__ double Abs(double a) { return fabs(a); }
+        __device__ __forceinline__ float Abs(float a) { return fabsf(a); }
+
+        // AgentForceDisp (CpuAgentForceBackend2D.cpp:30-45).
+        template <typename T>
+        __device__ __forceinline__ T Disp(T a, T b, T dimF, bool wrap)
+        {
+            T d = Sub(b, a);
+            if (wrap && Abs(d) > Mul(dimF, T(0.5)))
+            {
+                d = (a > b) ? Add(d, dimF) : Sub(d, dimF);
+            }
+            return d;
+        }
+
+        // Pass 4 (CpuAgentForceBackend2D.cpp:112-175) over cell-sorted slots.
+        template <typename T, typename TV>
+        __global__ void Forces(const int32_t *__restrict__ bucket, const int32_t *__restrict__ offsets,
+                               const float2 *__restrict__ sPos, const T *__restrict__ sRad, int32_t n,
+                               double interactionRad, T R, T k, int32_t xDim, int32_t yDim, int32_t wrapX,
+                               int32_t wrapY, TV *__restrict__ vel)
+        {
+            int32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+            if (slot >= n)
+            {
+                return;
+            }
+            const int32_t i = bucket[slot];
+            const float2 pf = sPos[slot];
+            const T px = static_cast<T>(pf.x);
+            const T py = static_cast<T>(pf.y);
+            const T rad = sRad[slot];
+            // window bounds in FP64, as the CPU computes them
+            int32_t xStart = static_cast<int32_t>(floor(static_cast<double>(pf.x) - interactionRad));
+            int32_t xEnd = static_cast<int32_t>(ceil(static_cast<double>(pf.x) + interactionRad));
+            int32_t yStart = static_cast<int32_t>(floor(static_cast<double>(pf.y) - interactionRad));
+            int32_t yEnd = static_cast<int32_t>(ceil(static_cast<double>(pf.y) + interactionRad));
+            // off-grid cells of a non-wrapped axis are skipped anyway
+            if (!wrapX)
+            {
+                xStart = max(xStart, 0);
+                xEnd = min(xEnd, xDim);
+            }
+            if (!wrapY)
+            {
+                yStart = max(yStart, 0);
+                yEnd = min(yEnd, yDim);
+            }
+            const T xDimF = static_cast<T>(xDim);
+            const T yDimF = static_cast<T>(yDim);
+            T vx = T(0), vy = T(0);
+            for (int32_t xSq = xStart; xSq < xEnd; xSq++)
+            {
+                int32_t retX = xSq;
+                const bool inX = (retX >= 0) && (retX < xDim);
+                if (!inX)
+                {
+                    if (!wrapX)
+                    {
+                        continue;
+                    }
+                    retX %= xDim;
+                    retX = (retX < 0) ? retX + xDim : retX;
+                }
+                for (int32_t ySq = yStart; ySq < yEnd; ySq++)
+                {
+                    int32_t retY = ySq;
+                    const bool inY = (retY >= 0) && (retY < yDim);
+                    if (!inY)
+                    {
+                        if (!wrapY)
+                        {
+                            continue;
+                        }
+                        retY %= yDim;
+                        retY = (retY < 0) ? retY + yDim : retY;
+                    }
+                    const int32_t cell = retX * yDim + retY;
+                    const int32_t s = __ldg(offsets + cell);
+                    const int32_t e = __ldg(offsets + cell + 1);
+                    for (int32_t q = s; q < e; q++)
+                    {
+                        if (q == slot)
+                        {
+                            continue;
+                        }
+                        const float2 pj = sPos[q];
+                        const T xComp = Disp(px, static_cast<T>(pj.x), xDimF, wrapX != 0);
+                        const T yComp = Disp(py, static_cast<T>(pj.y), yDimF, wrapY != 0);
+                        const T dist = Sqrt(Add(Mul(xComp, xComp), Mul(yComp, yComp)));
+                        if ((dist < R) && (dist > T(0)))
+                        {
+                            const T touchDist = Sub(Add(rad, sRad[q]), dist);
+                            const T force = Mul(k, touchDist);
+                            vx = Sub(vx, Mul(Div(xComp, dist), force));
+                            vy = Sub(vy, Mul(Div(yComp, dist), force));
+                        }
+                    }
+                }
+            }
+            vel[2 * static_cast<int64_t>(i)] = static_cast<TV>(vx);
+            vel[2 * static_cast<int64_t>(i) + 1] = static_cast<TV>(vy);
+        }
+    }
+
+    struct Agents
+    {
+        int32_t xDim = 0, yDim = 0, maxAgents = 0;
+        int64_t C = 0;
+        int32_t n = 0;          // agents of the last upload
+        int device = 0;
+        StreamSlot stream;
+        DevBuf<float> pos32, rad32, vel32;
+        DevBuf<double> pos64, rad64, vel64;
+        DevBuf<float2> posF, sPos;
+        DevBuf<float> sRad32;
+        DevBuf<double> sRad64;
+        DevBuf<int32_t> cellOf, arrival, counts, offsets, tileSums, bucketTmp, bucket;
+        int32_t nTiles = 0;
+
+        int Init(int32_t x, int32_t y, int32_t maxN)
+        {
+            xDim = x;
+            yDim = y;
+            maxAgents = maxN;
+            C = static_cast<int64_t>(x) * y;
+            device = CurrentDevice();
+            HAL_TRY(CudaStatus(cudaSetDevice(device), "cudaSetDevice"));
+            HAL_TRY(stream.Create("cudaStreamCreate"));
+            size_t m = static_cast<size_t>(maxN > 0 ? maxN : 1);
+            HAL_TRY(pos32.Alloc(2 * m, "cudaMalloc(agents)"));
+            HAL_TRY(rad32.Alloc(m, "cudaMalloc(agents)"));
+            HAL_TRY(vel32.Alloc(2 * m, "cudaMalloc(agents)"));
+            HAL_TRY(posF.Alloc(m, "cudaMalloc(agents)"));
+            HAL_TRY(sPos.Alloc(m, "cudaMalloc(agents)"));
+            HAL_TRY(sRad32.Alloc(m, "cudaMalloc(agents)"));
+            HAL_TRY(cellOf.Alloc(m, "cudaMalloc(agents)"));
+            HAL_TRY(arrival.Alloc(m, "cudaMalloc(agents)"));
+            HAL_TRY(bucketTmp.Alloc(m, "cudaMalloc(agents)"));
+            HAL_TRY(bucket.Alloc(m, "cudaMalloc(agents)"));
+            HAL_TRY(counts.Alloc(static_cast<size_t>(C), "cudaMalloc(bins)"));
+            HAL_TRY(offsets.Alloc(static_cast<size_t>(C) + 1, "cudaMalloc(bins)"));
+            nTiles = static_cast<int32_t>((C + kScanTile - 1) / kScanTile);
+            HAL_TRY(tileSums.Alloc(static_cast<size_t>(nTiles), "cudaMalloc(bins)"));
+            HAL_TRY(CudaStatus(cudaMemset(offsets.p, 0, (static_cast<size_t>(C) + 1) * sizeof(int32_t)), "cudaMemset"));
+            return HAL_CUDA_OK;
+        }
+
+        // Bins n agents (positions of type TP, interleaved x,y) and sorts
+        // radii of type TR alongside.
+        // Bins n agents (positions of type TP, interleaved x,y) and sorts
+        // radii of type TR alongside.  With ev != nullptr, records an event
+        // after each stage (count, scan, scatter, stabilize) for profiling.
+        template <typename TP, typename TR>
+        int Bin(const TP *pos, const TR *rad, TR *sRad, cudaStream_t s, cudaEvent_t *ev = nullptr)
+        {
+            HAL_TRY(CudaStatus(cudaMemsetAsync(counts.p, 0, static_cast<size_t>(C) * sizeof(int32_t), s),
+                               "cudaMemsetAsync(counts)"));
+            const int T = 256;
+            unsigned ablocks = static_cast<unsigned>((n + T - 1) / T);
+            if (n > 0)
+            {
+                BinCount<TP><<<ablocks, T, 0, s>>>(pos, n, xDim, yDim, posF.p, cellOf.p, arrival.p, counts.p);
+                CountLaunch();
+            }
+            if (ev)
+            {
+                cudaEventRecord(ev[0], s);
+            }
+            ScanReduce<<<nTiles, kScanThreads, 0, s>>>(counts.p, C, tileSums.p);
+            ScanTiles<<<1, kScanThreads, 0, s>>>(tileSums.p, nTiles);
+            ScanApply<<<nTiles, kScanThreads, 0, s>>>(counts.p, C, tileSums.p, offsets.p, n);
+            CountLaunch(3);
+            if (ev)
+            {
+                cudaEventRecord(ev[1], s);
+            }
+            if (n > 0)
+            {
+                Scatter<<<ablocks, T, 0, s>>>(cellOf.p, arrival.p, offsets.p, n, bucketTmp.p);
+                CountLaunch();
+            }
+            if (ev)
+            {
+                cudaEventRecord(ev[2], s);
+            }
+            if (n > 0)
+            {
+                Stabilize<TR><<<ablocks, T, 0, s>>>(cellOf.p, offsets.p, bucketTmp.p, posF.p, rad, n, bucket.p,
+                                                    sPos.p, sRad);
+                CountLaunch();
+            }
+            if (ev)
+            {
+                cudaEventRecord(ev[3], s);
+            }
+            return LaunchStatus("agent binning");
+        }
+
+        template <typename T, typename TV>
+        int Force(const T *sRad, double R, double k, bool wrapX, bool wrapY, TV *vel, cudaStream_t s)
+        {
+            if (n == 0)
+            {
+                return HAL_CUDA_OK;
+            }
+            const int T_ = 128;
+            unsigned blocks = static_cast<unsigned>((n + T_ - 1) / T_);
+            Forces<T, TV><<<blocks, T_, 0, s>>>(bucket.p, offsets.p, sPos.p, sRad, n, R, static_cast<T>(R),
+                                                static_cast<T>(k), xDim, yDim, wrapX, wrapY, vel);
+            CountLaunch();
+            return LaunchStatus("agent forces");
+        }
+    };
+
+    const int32_t *AgentsCellOffsets(const hal_cuda_agents *a, int32_t *xDim, int32_t *yDim);
+}
+
+using halcuda::Agents;
+
+struct hal_cuda_agents : public Agents
+{
+};
+
+namespace halcuda
+{
+    const int32_t *AgentsCellOffsets(const hal_cuda_agents *a, int32_t *xDim, int32_t *yDim)
+    {
+        *xDim = a->xDim;
+        *yDim = a->yDim;
+        return a->offsets.p;
+    }
+}
+
+extern "C" int hal_cuda_agents_create(int32_t xDim, int32_t yDim, int32_t maxAgents, hal_cuda_agents **out)
+{
+    HAL_REQUIRE(out != nullptr, "hal_cuda_agents_create: out is NULL");
+    *out = nullptr;
+    HAL_REQUIRE(xDim > 0 && yDim > 0, "hal_cuda_agents_create: dimensions must be positive");
+    HAL_REQUIRE(static_cast<int64_t>(xDim) * yDim < (int64_t(1) << 31) - 1,
+                "hal_cuda_agents_create: xDim*yDim exceeds int32");
+    HAL_REQUIRE(maxAgents >= 0, "hal_cuda_agents_create: negative capacity");
+    hal_cuda_agents *h = new (std::nothrow) hal_cuda_agents();
+    if (h == nullptr)
+    {
+        halcuda::SetError("hal_cuda_agents_create: out of host memory");
+        return HAL_CUDA_ENOMEM;
+    }
+    int rc = h->Init(xDim, yDim, maxAgents);
+    if (rc != HAL_CUDA_OK)
+    {
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return HAL_CUDA_OK;
+}
+
+extern "C" int hal_cuda_agents_destroy(hal_cuda_agents *h)
+{
+    if (h != nullptr)
+    {
+        cudaSetDevice(h->device);
+        cudaStreamSynchronize(h->stream.Get());
+        delete h;
+    }
+    return HAL_CUDA_OK;
+}
+
+namespace
+{
+    // The cell window spans about 2R cells per axis; a wrapped axis walks all
+    // of it, so the radius is bounded to keep every launch short.
+    constexpr double kMaxInteractionRad = 1048576.0;
+
+    bool RadiusOk(double r)
+    {
+        return std::isfinite(r) && r >= 0.0 && r <= kMaxInteractionRad;
+    }
+}
+
+extern "C" int hal_cuda_accumulate_forces(hal_cuda_agents *h, const double *positions, int64_t posLen,
+                                          const double *radii, int64_t radLen, double *velocityDeltas,
+                                          double interactionRad, double springConstant, int32_t xDim, int32_t yDim,
+                                          int32_t wrapX, int32_t wrapY)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_accumulate_forces: handle is NULL");
+    HAL_REQUIRE(xDim == h->xDim && yDim == h->yDim,
+                "CudaAgentForceBackend2D::AccumulateForces called with dimensions differing from construction");
+    HAL_REQUIRE(posLen == 2 * radLen && radLen >= 0,
+                "CudaAgentForceBackend2D::AccumulateForces: positions must hold two values per radius");
+    HAL_REQUIRE(radLen <= h->maxAgents,
+                "CudaAgentForceBackend2D::AccumulateForces called with more agents than the construction-time capacity");
+    HAL_REQUIRE(radLen == 0 || (positions != nullptr && radii != nullptr && velocityDeltas != nullptr),
+                "hal_cuda_accumulate_forces: NULL array");
+    HAL_REQUIRE(RadiusOk(interactionRad), "hal_cuda_accumulate_forces: interactionRad %g outside [0, %g]",
+                interactionRad, kMaxInteractionRad);
+    using namespace halcuda;
+    HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    if (h->pos64.p == nullptr)
+    {
+        size_t m = static_cast<size_t>(h->maxAgents > 0 ? h->maxAgents : 1);
+        HAL_TRY(h->pos64.Alloc(2 * m, "cudaMalloc(agents64)"));
+        HAL_TRY(h->rad64.Alloc(m, "cudaMalloc(agents64)"));
+        HAL_TRY(h->vel64.Alloc(2 * m, "cudaMalloc(agents64)"));
+        HAL_TRY(h->sRad64.Alloc(m, "cudaMalloc(agents64)"));
+    }
+    cudaStream_t s = h->stream.Get();
+    h->n = static_cast<int32_t>(radLen);
+    if (h->n > 0)
+    {
+        HAL_TRY(CudaStatus(cudaMemcpyAsync(h->pos64.p, positions, posLen * sizeof(double), cudaMemcpyHostToDevice, s),
+                           "cudaMemcpy(positions)"));
+        HAL_TRY(CudaStatus(cudaMemcpyAsync(h->rad64.p, radii, radLen * sizeof(double), cudaMemcpyHostToDevice, s),
+                           "cudaMemcpy(radii)"));
+    }
+    HAL_TRY((h->Bin<double, double>(h->pos64.p, h->rad64.p, h->sRad64.p, s)));
+    HAL_TRY((h->Force<double, double>(h->sRad64.p, interactionRad, springConstant, wrapX != 0, wrapY != 0,
+                                      h->vel64.p, s)));
+    if (h->n > 0)
+    {
+        HAL_TRY(CudaStatus(cudaMemcpyAsync(velocityDeltas, h->vel64.p, posLen * sizeof(double), cudaMemcpyDeviceToHost, s),
+                           "cudaMemcpy(velocityDeltas)"));
+    }
+    return CudaStatus(cudaStreamSynchronize(s), "hal_cuda_accumulate_forces");
+}
+
+extern "C" int hal_cuda_agents_upload(hal_cuda_agents *h, const float *positions, const float *radii, int32_t n)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_agents_upload: handle is NULL");
+    HAL_REQUIRE(n >= 0 && n <= h->maxAgents, "AgentForceKernel2D::UploadAgents: agent count %d outside [0, %d]", n,
+                h->maxAgents);
+    HAL_REQUIRE(n == 0 || (positions != nullptr && radii != nullptr), "hal_cuda_agents_upload: NULL array");
+    using namespace halcuda;
+    HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    cudaStream_t s = h->stream.Get();
+    h->n = n;
+    if (n > 0)
+    {
+        HAL_TRY(CudaStatus(cudaMemcpyAsync(h->pos32.p, positions, 2 * static_cast<size_t>(n) * sizeof(float),
+                                           cudaMemcpyHostToDevice, s), "cudaMemcpy(positions)"));
+        HAL_TRY(CudaStatus(cudaMemcpyAsync(h->rad32.p, radii, static_cast<size_t>(n) * sizeof(float),
+                                           cudaMemcpyHostToDevice, s), "cudaMemcpy(radii)"));
+    }
+    return CudaStatus(cudaStreamSynchronize(s), "hal_cuda_agents_upload");
+}
+
+extern "C" int hal_cuda_agents_dispatch(hal_cuda_agents *h, double interactionRad, double springConstant,
+                                        int32_t wrapX, int32_t wrapY)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_agents_dispatch: handle is NULL");
+    HAL_REQUIRE(RadiusOk(interactionRad), "hal_cuda_agents_dispatch: interactionRad %g outside [0, %g]",
+                interactionRad, kMaxInteractionRad);
+    using namespace halcuda;
+    HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    cudaStream_t s = h->stream.Get();
+    HAL_TRY((h->Bin<float, float>(h->pos32.p, h->rad32.p, h->sRad32.p, s)));
+    return h->Force<float, float>(h->sRad32.p, interactionRad, springConstant, wrapX != 0, wrapY != 0, h->vel32.p, s);
+}
+
+extern "C" int hal_cuda_agents_download(hal_cuda_agents *h, float *velocityDeltas, int32_t n)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_agents_download: handle is NULL");
+    HAL_REQUIRE(n == h->n, "hal_cuda_agents_download: %d agents requested, %d uploaded", n, h->n);
+    HAL_REQUIRE(n == 0 || velocityDeltas != nullptr, "hal_cuda_agents_download: NULL array");
+    using namespace halcuda;
+    HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    cudaStream_t s = h->stream.Get();
+    if (n > 0)
+    {
+        HAL_TRY(CudaStatus(cudaMemcpyAsync(velocityDeltas, h->vel32.p, 2 * static_cast<size_t>(n) * sizeof(float),
+                                           cudaMemcpyDeviceToHost, s), "cudaMemcpy(velocityDeltas)"));
+    }
+    return CudaStatus(cudaStreamSynchronize(s), "hal_cuda_agents_download");
+}
+
+extern "C" int hal_cuda_agents_get_bins(hal_cuda_agents *h, int32_t *cellOffsets, int32_t *bucketAgents)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_agents_get_bins: handle is NULL");
+    using namespace halcuda;
+    HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    cudaStream_t s = h->stream.Get();
+    if (cellOffsets != nullptr)
+    {
+        HAL_TRY(CudaStatus(cudaMemcpyAsync(cellOffsets, h->offsets.p, (static_cast<size_t>(h->C) + 1) * sizeof(int32_t),
+                                           cudaMemcpyDeviceToHost, s), "cudaMemcpy(offsets)"));
+    }
+    if (bucketAgents != nullptr && h->n > 0)
+    {
+        HAL_TRY(CudaStatus(cudaMemcpyAsync(bucketAgents, h->bucket.p, static_cast<size_t>(h->n) * sizeof(int32_t),
+                                           cudaMemcpyDeviceToHost, s), "cudaMemcpy(bucket)"));
+    }
+    return CudaStatus(cudaStreamSynchronize(s), "hal_cuda_agents_get_bins");
+}
+
+extern "C" int hal_cuda_agents_sync(hal_cuda_agents *h)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_agents_sync: handle is NULL");
+    HAL_TRY(halcuda::CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    return halcuda::CudaStatus(cudaStreamSynchronize(h->stream.Get()), "hal_cuda_agents_sync");
+}
+
+extern "C" void *hal_cuda_agents_stream(hal_cuda_agents *h)
+{
+    return h ? static_cast<void *>(h->stream.Get()) : nullptr;
+}
+
+extern "C" int hal_cuda_agents_set_stream(hal_cuda_agents *h, void *stream)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_agents_set_stream: handle is NULL");
+    h->stream.Set(stream);
+    return HAL_CUDA_OK;
+}
+
+extern "C" int hal_cuda_agents_profile(hal_cuda_agents *h, int32_t iters, double interactionRad, double springConstant,
+                                       int32_t wrapX, int32_t wrapY, float *ms)
+{
+    HAL_REQUIRE(h != nullptr && ms != nullptr, "hal_cuda_agents_profile: NULL argument");
+    HAL_REQUIRE(iters > 0, "hal_cuda_agents_profile: iters must be positive");
+    HAL_REQUIRE(RadiusOk(interactionRad), "hal_cuda_agents_profile: interactionRad out of range");
+    using namespace halcuda;
+    HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    cudaStream_t s = h->stream.Get();
+    cudaEvent_t ev[6];
+    for (auto &e : ev)
+    {
+        HAL_TRY(CudaStatus(cudaEventCreate(&e), "cudaEventCreate"));
+    }
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    int rc = HAL_CUDA_OK;
+    for (int32_t t = 0; t < iters && rc == HAL_CUDA_OK; t++)
+    {
+        cudaEventRecord(ev[5], s);
+        rc = h->Bin<float, float>(h->pos32.p, h->rad32.p, h->sRad32.p, s, ev);
+        if (rc == HAL_CUDA_OK)
+        {
+            rc = h->Force<float, float>(h->sRad32.p, interactionRad, springConstant, wrapX != 0, wrapY != 0,
+                                        h->vel32.p, s);
+        }
+        cudaEventRecord(ev[4], s);
+        if (rc == HAL_CUDA_OK)
+        {
+            rc = CudaStatus(cudaEventSynchronize(ev[4]), "hal_cuda_agents_profile");
+        }
+        if (rc != HAL_CUDA_OK)
+        {
+            break;
+        }
+        float t0 = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0, tall = 0;
+        cudaEventElapsedTime(&t0, ev[5], ev[0]);
+        cudaEventElapsedTime(&t1, ev[0], ev[1]);
+        cudaEventElapsedTime(&t2, ev[1], ev[2]);
+        cudaEventElapsedTime(&t3, ev[2], ev[3]);
+        cudaEventElapsedTime(&t4, ev[3], ev[4]);
+        cudaEventElapsedTime(&tall, ev[5], ev[4]);
+        acc[0] += t0;
+        acc[1] += t1;
+        acc[2] += t2;
+        acc[3] += t3;
+        acc[4] += t4;
+        acc[5] += tall;
+    }
+    for (auto &e : ev)
+    {
+        cudaEventDestroy(e);
+    }
+    HAL_TRY(rc);
+    for (int q = 0; q < 6; q++)
+    {
+        ms[q] = static_cast<float>(acc[q] / iters);
+    }
+    return HAL_CUDA_OK;
+}

@@ -1,0 +1,220 @@
+// common.cuh -- shared host/device helpers of the hal_cuda library.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "hal_cuda.h"
+
+namespace halcuda
+{
+    // Thread-local message of the last failed call (hal_cuda_last_error).
+    void SetError(const char *fmt, ...);
+    void ClearError();
+
+    // Counts every kernel launch issued by the library (hal_cuda_launch_count).
+    extern std::atomic<int64_t> g_launches;
+    inline void CountLaunch(int64_t n = 1)
+    {
+        g_launches.fetch_add(n, std::memory_order_relaxed);
+    }
+
+    // Device selected for new handles on this thread.
+    int CurrentDevice();
+
+    // Maps a CUDA error to a status, recording the message.
+    inline int CudaStatus(cudaError_t e, const char *what)
+    {
+        if (e == cudaSuccess)
+        {
+            return HAL_CUDA_OK;
+        }
+        SetError("%s: %s", what, cudaGetErrorString(e));
+        return (e == cudaErrorMemoryAllocation) ? HAL_CUDA_ENOMEM : HAL_CUDA_EDEVICE;
+    }
+
+    // Checks a launch and (for synchronous calls) the stream.
+    inline int LaunchStatus(const char *what)
+    {
+        return CudaStatus(cudaGetLastError(), what);
+    }
+
+    // A device buffer owned by a handle.
+    template <typename T>
+    struct DevBuf
+    {
+        T *p = nullptr;
+        size_t n = 0;
+
+        int Alloc(size_t count, const char *what)
+        {
+            Free();
+            if (count == 0)
+            {
+                count = 1;
+            }
+            cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&p), count * sizeof(T));
+            if (e != cudaSuccess)
+            {
+                p = nullptr;
+                return CudaStatus(e, what);
+            }
+            n = count;
+            return HAL_CUDA_OK;
+        }
+
+        void Free()
+        {
+            if (p != nullptr)
+            {
+                cudaFree(p);
+            }
+            p = nullptr;
+            n = 0;
+        }
+
+        ~DevBuf()
+        {
+            Free();
+        }
+    };
+
+    // A pinned host staging buffer, grown on demand.
+    template <typename T>
+    struct HostBuf
+    {
+        T *p = nullptr;
+        size_t n = 0;
+
+        int Reserve(size_t count, const char *what)
+        {
+            if (count <= n)
+            {
+                return HAL_CUDA_OK;
+            }
+            Free();
+            cudaError_t e = cudaMallocHost(reinterpret_cast<void **>(&p), count * sizeof(T));
+            if (e != cudaSuccess)
+            {
+                p = nullptr;
+                return CudaStatus(e, what);
+            }
+            n = count;
+            return HAL_CUDA_OK;
+        }
+
+        void Free()
+        {
+            if (p != nullptr)
+            {
+                cudaFreeHost(p);
+            }
+            p = nullptr;
+            n = 0;
+        }
+
+        ~HostBuf()
+        {
+            Free();
+        }
+    };
+
+    // The stream a handle runs on: its own, or one the caller supplied.
+    struct StreamSlot
+    {
+        cudaStream_t own = nullptr;
+        cudaStream_t user = nullptr;
+        bool hasUser = false;
+
+        int Create(const char *what)
+        {
+            return CudaStatus(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking), what);
+        }
+
+        cudaStream_t Get() const
+        {
+            return hasUser ? user : own;
+        }
+
+        void Set(void *s)
+        {
+            hasUser = (s != nullptr);
+            user = static_cast<cudaStream_t>(s);
+        }
+
+        ~StreamSlot()
+        {
+            if (own != nullptr)
+            {
+                cudaStreamDestroy(own);
+            }
+        }
+    };
+
+    // Cached CUDA graph of a fixed launch sequence, re-captured when its key
+    // changes.
+    struct GraphCache
+    {
+        cudaGraphExec_t exec = nullptr;
+        std::string key;
+
+        void Reset()
+        {
+            if (exec != nullptr)
+            {
+                cudaGraphExecDestroy(exec);
+            }
+            exec = nullptr;
+            key.clear();
+        }
+
+        ~GraphCache()
+        {
+            Reset();
+        }
+    };
+
+    // Ghost-table offsets (see hal_cuda.h).
+    struct GhostView
+    {
+        const float *xlo;  // bc(-1, y), yDim values
+        const float *xhi;  // bc(xDim, y)
+        const float *ylo;  // bc(x, -1), xDim values
+        const float *yhi;  // bc(x, yDim)
+    };
+
+    inline GhostView MakeGhostView(const float *g, int32_t xDim, int32_t yDim)
+    {
+        GhostView v;
+        v.xlo = g;
+        v.xhi = g ? g + yDim : nullptr;
+        v.ylo = g ? g + 2 * yDim : nullptr;
+        v.yhi = g ? g + 2 * yDim + xDim : nullptr;
+        return v;
+    }
+}
+
+#define HAL_TRY(expr)                  \
+    do                                 \
+    {                                  \
+        int _rc = (expr);              \
+        if (_rc != HAL_CUDA_OK)        \
+        {                              \
+            return _rc;                \
+        }                              \
+    } while (0)
+
+#define HAL_REQUIRE(cond, ...)                \
+    do                                        \
+    {                                         \
+        if (!(cond))                          \
+        {                                     \
+            ::halcuda::SetError(__VA_ARGS__); \
+            return HAL_CUDA_EINVAL;           \
+        }                                     \
+    } while (0)

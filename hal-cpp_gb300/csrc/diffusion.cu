@@ -1,0 +1,767 @@
+// diffusion.cu -- explicit 5-point diffusion: the fused per-tick kernel, the
+// FP64 IDiffusionBackend2D::Diffuse kernel, and the hal_cuda_diffusion handle.
+//
+// Math (reference src/Pde/PDEequations.cpp:140-161 and PDEequations.h:50-98,
+// 264-287): for cell i = x*yDim + y with centre value c,
+//   sum = d(x+1) + d(x-1) + d(y+1) + d(y-1),  d(n) = f[n] - c  on the grid,
+//         f[wrap(n)] - c on a wrapped axis, (bc - c)*2 for a Dirichlet ghost,
+//         0 for a zero-flux edge;
+//   deltas[i] += sum * diffRate.
+// The fused tick adds PDEGrid2D's MulAll(-decay), Add(source) and Update()
+// (PDEGrid2D.h:103-186) in the same pass: f'[i] = c + (sum*r - c*decay + src).
+#include "common.cuh"
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+namespace halcuda
+{
+    namespace
+    {
+        constexpr int kTickRowsPerThread = 8;  // rows walked by one thread
+        constexpr int kTickWarps = 8;          // warps per CTA, stacked in x
+
+        // Off-grid neighbour handling of one row (or column) of the stencil.
+        enum NbrMode : int
+        {
+            kNbrGrid = 0,   // value on the grid (or wrapped onto it)
+            kNbrGhost = 1,  // Dirichlet ghost: (bc - c) * 2
+            kNbrNone = 2    // zero-flux: contributes 0
+        };
+
+        __device__ __forceinline__ float NbrTerm(int mode, float v, float c)
+        {
+            return (mode == kNbrGrid) ? (v - c) : ((mode == kNbrGhost) ? (v - c) * 2.0f : 0.0f);
+        }
+
+        struct TickParams
+        {
+            const float *f;
+            float *out;
+            int32_t xDim, yDim;
+            float r, negDecay;
+            int32_t wrapX, wrapY;
+            const float *src;          // dense source or null
+            GhostView ghost;           // all null for zero-flux
+            const int32_t *ptStart;    // point sources grouped by CTA (CSR), or null
+            const int32_t *ptRow;
+            const int32_t *ptCol;
+            const float *ptVal;
+        };
+
+        // Loads VEC consecutive values of row x starting at column y0 (the
+        // part inside the grid) and classifies the row as grid/ghost/none.
+        template <int VEC>
+        __device__ __forceinline__ int LoadRow(const TickParams &p, int32_t x, int32_t y0,
+                                               float (&v)[VEC], bool lowSide)
+        {
+            int mode = kNbrGrid;
+            int32_t row = x;
+            if (x < 0 || x >= p.xDim)
+            {
+                if (p.wrapX)
+                {
+                    row = (x < 0) ? x + p.xDim : x - p.xDim;
+                }
+                else if (p.ghost.xlo != nullptr)
+                {
+                    const float *g = lowSide ? p.ghost.xlo : p.ghost.xhi;
+#pragma unroll
+                    for (int k = 0; k < VEC; k++)
+                    {
+                        v[k] = (y0 + k < p.yDim) ? __ldg(g + y0 + k) : 0.0f;
+                    }
+                    return kNbrGhost;
+                }
+                else
+                {
+#pragma unroll
+                    for (int k = 0; k < VEC; k++)
+                    {
+                        v[k] = 0.0f;
+                    }
+                    return kNbrNone;
+                }
+            }
+            const float *src = p.f + static_cast<int64_t>(row) * p.yDim + y0;
+            if constexpr (VEC == 4)
+            {
+                float4 q = __ldg(reinterpret_cast<const float4 *>(src));
+                v[0] = q.x;
+                v[1] = q.y;
+                v[2] = q.z;
+                v[3] = q.w;
+            }
+            else
+            {
+#pragma unroll
+                for (int k = 0; k < VEC; k++)
+                {
+                    v[k] = (y0 + k < p.yDim) ? __ldg(src + k) : 0.0f;
+                }
+            }
+            return mode;
+        }
+
+        // One fused tick.  Each thread owns VEC consecutive cells of a row
+        // (float4 when yDim % 4 == 0) and walks kTickRowsPerThread rows,
+        // keeping the rows above and below in registers.
+        template <int VEC>
+        __global__ void __launch_bounds__(32 * kTickWarps)
+            TickKernel(TickParams p)
+        {
+            const int lane = threadIdx.x;
+            const int warp = threadIdx.y;
+            const int32_t y0 = (blockIdx.x * 32 + lane) * VEC;
+            const int32_t xs = (blockIdx.y * kTickWarps + warp) * kTickRowsPerThread;
+            if (y0 >= p.yDim || xs >= p.xDim)
+            {
+                return;
+            }
+            const int32_t xe = min(xs + kTickRowsPerThread, p.xDim);
+            const int nValid = min(VEC, p.yDim - y0);
+
+            float up[VEC], cur[VEC], dn[VEC];
+            int upMode = LoadRow<VEC>(p, xs - 1, y0, up, true);
+            LoadRow<VEC>(p, xs, y0, cur, true);
+
+            int32_t ptBeg = 0, ptEnd = 0;
+            if (p.ptStart != nullptr)
+            {
+                int32_t b = blockIdx.y * gridDim.x + blockIdx.x;
+                ptBeg = __ldg(p.ptStart + b);
+                ptEnd = __ldg(p.ptStart + b + 1);
+            }
+
+            for (int32_t x = xs; x < xe; x++)
+            {
+                int dnMode = LoadRow<VEC>(p, x + 1, y0, dn, false);
+                const float *rowp = p.f + static_cast<int64_t>(x) * p.yDim;
+
+                // y neighbours of the first and last owned cells
+                float left, right;
+                int leftMode = kNbrGrid, rightMode = kNbrGrid;
+                if (y0 > 0)
+                {
+                    left = __ldg(rowp + y0 - 1);
+                }
+                else if (p.wrapY)
+                {
+                    left = __ldg(rowp + p.yDim - 1);
+                }
+                else if (p.ghost.ylo != nullptr)
+                {
+                    left = __ldg(p.ghost.ylo + x);
+                    leftMode = kNbrGhost;
+                }
+                else
+                {
+                    left = 0.0f;
+                    leftMode = kNbrNone;
+                }
+                const int32_t yr = y0 + nValid;  // column right of the last owned cell
+                if (yr < p.yDim)
+                {
+                    right = __ldg(rowp + yr);
+                }
+                else if (p.wrapY)
+                {
+                    right = __ldg(rowp);
+                }
+                else if (p.ghost.yhi != nullptr)
+                {
+                    right = __ldg(p.ghost.yhi + x);
+                    rightMode = kNbrGhost;
+                }
+                else
+                {
+                    right = 0.0f;
+                    rightMode = kNbrNone;
+                }
+
+                float o[VEC];
+#pragma unroll
+                for (int k = 0; k < VEC; k++)
+                {
+                    const float c = cur[k];
+                    float yp, ym;
+                    int ypMode = kNbrGrid, ymMode = kNbrGrid;
+                    if (k + 1 < nValid)
+                    {
+                        yp = cur[k + 1];
+                    }
+                    else
+                    {
+                        yp = right;
+                        ypMode = rightMode;
+                    }
+                    if (k > 0)
+                    {
+                        ym = cur[k - 1];
+                    }
+                    else
+                    {
+                        ym = left;
+                        ymMode = leftMode;
+                    }
+                    // reference order: x+1, x-1, y+1, y-1
+                    float sum = NbrTerm(dnMode, dn[k], c);
+                    sum += NbrTerm(upMode, up[k], c);
+                    sum += NbrTerm(ypMode, yp, c);
+                    sum += NbrTerm(ymMode, ym, c);
+                    float d = sum * p.r;
+                    d = fmaf(c, p.negDecay, d);
+                    o[k] = d;
+                }
+                if (p.src != nullptr)
+                {
+                    const float *s = p.src + static_cast<int64_t>(x) * p.yDim + y0;
+                    if constexpr (VEC == 4)
+                    {
+                        float4 q = __ldg(reinterpret_cast<const float4 *>(s));
+                        o[0] += q.x;
+                        o[1] += q.y;
+                        o[2] += q.z;
+                        o[3] += q.w;
+                    }
+                    else
+                    {
+#pragma unroll
+                        for (int k = 0; k < VEC; k++)
+                        {
+                            if (k < nValid)
+                            {
+                                o[k] += __ldg(s + k);
+                            }
+                        }
+                    }
+                }
+                for (int32_t q = ptBeg; q < ptEnd; q++)
+                {
+                    if (__ldg(p.ptRow + q) == x)
+                    {
+                        int32_t col = __ldg(p.ptCol + q) - y0;
+                        float val = __ldg(p.ptVal + q);
+#pragma unroll
+                        for (int k = 0; k < VEC; k++)
+                        {
+                            if (col == k)
+                            {
+                                o[k] += val;
+                            }
+                        }
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < VEC; k++)
+                {
+                    o[k] = cur[k] + o[k];
+                }
+                float *dst = p.out + static_cast<int64_t>(x) * p.yDim + y0;
+                if constexpr (VEC == 4)
+                {
+                    *reinterpret_cast<float4 *>(dst) = make_float4(o[0], o[1], o[2], o[3]);
+                }
+                else
+                {
+#pragma unroll
+                    for (int k = 0; k < VEC; k++)
+                    {
+                        if (k < nValid)
+                        {
+                            dst[k] = o[k];
+                        }
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < VEC; k++)
+                {
+                    up[k] = cur[k];
+                    cur[k] = dn[k];
+                }
+                upMode = kNbrGrid;
+            }
+        }
+
+        // FP64 IDiffusionBackend2D::Diffuse: deltas[i] += sum * r, with the
+        // reference's operation order and no contraction, so the result is
+        // bit-identical to Hal::CpuDiffusionBackend2D.
+        __device__ __forceinline__ double DeltaTerm64(const double *f, double c, int32_t n,
+                                                      int32_t dim, bool wrap, int64_t base,
+                                                      int64_t stride, const double *ghost,
+                                                      int64_t ghostIdx)
+        {
+            if (n >= 0 && n < dim)
+            {
+                return __dsub_rn(f[base + n * stride], c);
+            }
+            if (wrap)
+            {
+                int32_t w = (n < 0) ? n + dim : n - dim;
+                return __dsub_rn(f[base + w * stride], c);
+            }
+            if (ghost != nullptr)
+            {
+                return __dmul_rn(__dsub_rn(ghost[ghostIdx], c), 2.0);
+            }
+            return 0.0;
+        }
+
+        __global__ void Diffuse64Kernel(const double *__restrict__ f, double *__restrict__ deltas,
+                                        int32_t xDim, int32_t yDim, double r, int32_t wrapX,
+                                        int32_t wrapY, const double *__restrict__ ghost)
+        {
+            int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+            int64_t n = static_cast<int64_t>(xDim) * yDim;
+            if (i >= n)
+            {
+                return;
+            }
+            int32_t x = static_cast<int32_t>(i / yDim);
+            int32_t y = static_cast<int32_t>(i - static_cast<int64_t>(x) * yDim);
+            double c = f[i];
+            const double *gx = ghost;
+            const double *gy = ghost ? ghost + 2 * yDim : nullptr;
+            int64_t colBase = y;                                // column y, stride yDim
+            int64_t rowBase = static_cast<int64_t>(x) * yDim;   // row x, stride 1
+            double s = DeltaTerm64(f, c, x + 1, xDim, wrapX, colBase, yDim, gx, yDim + y);
+            s = __dadd_rn(s, DeltaTerm64(f, c, x - 1, xDim, wrapX, colBase, yDim, gx, y));
+            s = __dadd_rn(s, DeltaTerm64(f, c, y + 1, yDim, wrapY, rowBase, 1, gy, xDim + x));
+            s = __dadd_rn(s, DeltaTerm64(f, c, y - 1, yDim, wrapY, rowBase, 1, gy, x));
+            deltas[i] = __dadd_rn(deltas[i], __dmul_rn(s, r));
+        }
+    }
+
+    struct Diffusion
+    {
+        int32_t xDim = 0, yDim = 0;
+        int device = 0;
+        StreamSlot stream;
+        DevBuf<float> field[2];
+        int cur = 0;
+        DevBuf<float> src;
+        bool hasSrc = false;
+        DevBuf<float> ghost;
+        bool hasGhost = false;
+        DevBuf<int32_t> ptStart, ptRow, ptCol;
+        DevBuf<float> ptVal;
+        bool hasPoints = false;
+        DevBuf<double> f64, d64, g64;
+        GraphCache graph[2];  // by the parity of the starting buffer
+        dim3 grid, block;
+
+        void ResetGraphs()
+        {
+            graph[0].Reset();
+            graph[1].Reset();
+        }
+        bool vec4 = false;
+
+        int Init(int32_t x, int32_t y)
+        {
+            xDim = x;
+            yDim = y;
+            device = CurrentDevice();
+            HAL_TRY(CudaStatus(cudaSetDevice(device), "cudaSetDevice"));
+            HAL_TRY(stream.Create("cudaStreamCreate"));
+            size_t n = static_cast<size_t>(x) * static_cast<size_t>(y);
+            HAL_TRY(field[0].Alloc(n, "cudaMalloc(field)"));
+            HAL_TRY(field[1].Alloc(n, "cudaMalloc(field)"));
+            HAL_TRY(CudaStatus(cudaMemset(field[0].p, 0, n * sizeof(float)), "cudaMemset"));
+            vec4 = (yDim % 4) == 0;
+            int vec = vec4 ? 4 : 1;
+            block = dim3(32, kTickWarps);
+            grid = dim3((yDim + 32 * vec - 1) / (32 * vec),
+                        (xDim + kTickWarps * kTickRowsPerThread - 1) / (kTickWarps * kTickRowsPerThread));
+            return HAL_CUDA_OK;
+        }
+
+        size_t Length() const
+        {
+            return static_cast<size_t>(xDim) * static_cast<size_t>(yDim);
+        }
+
+        TickParams Params(const float *in, float *out, double r, double decay, bool wrapX,
+                          bool wrapY, bool useExtras) const
+        {
+            TickParams p;
+            p.f = in;
+            p.out = out;
+            p.xDim = xDim;
+            p.yDim = yDim;
+            p.r = static_cast<float>(r);
+            p.negDecay = static_cast<float>(-decay);
+            p.wrapX = wrapX;
+            p.wrapY = wrapY;
+            p.src = (useExtras && hasSrc) ? src.p : nullptr;
+            p.ghost = MakeGhostView((useExtras && hasGhost) ? ghost.p : nullptr, xDim, yDim);
+            bool pts = useExtras && hasPoints;
+            p.ptStart = pts ? ptStart.p : nullptr;
+            p.ptRow = pts ? ptRow.p : nullptr;
+            p.ptCol = pts ? ptCol.p : nullptr;
+            p.ptVal = pts ? ptVal.p : nullptr;
+            return p;
+        }
+
+        void LaunchTick(const TickParams &p, cudaStream_t s) const
+        {
+            if (vec4)
+            {
+                TickKernel<4><<<grid, block, 0, s>>>(p);
+            }
+            else
+            {
+                TickKernel<1><<<grid, block, 0, s>>>(p);
+            }
+        }
+
+        // Enqueues `ticks` ticks from field[cur], replayed from a graph.
+        int RunTicks(int32_t ticks, double r, double decay, bool wrapX, bool wrapY, bool extras)
+        {
+            if (ticks <= 0)
+            {
+                return HAL_CUDA_OK;
+            }
+            cudaStream_t s = stream.Get();
+            char key[256];
+            snprintf(key, sizeof(key), "%d|%a|%a|%d|%d|%d|%d|%d|%p", ticks, r, decay, wrapX, wrapY,
+                     extras ? 1 : 0, hasSrc, hasGhost, static_cast<void *>(s));
+            GraphCache &graph = this->graph[cur];
+            if (graph.exec == nullptr || graph.key != key)
+            {
+                graph.Reset();
+                cudaGraph_t g = nullptr;
+                HAL_TRY(CudaStatus(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal),
+                                   "cudaStreamBeginCapture"));
+                int c = cur;
+                for (int32_t t = 0; t < ticks; t++)
+                {
+                    TickParams p = Params(field[c].p, field[c ^ 1].p, r, decay, wrapX, wrapY, extras);
+                    LaunchTick(p, s);
+                    c ^= 1;
+                }
+                cudaError_t e = cudaStreamEndCapture(s, &g);
+                HAL_TRY(CudaStatus(e, "cudaStreamEndCapture"));
+                e = cudaGraphInstantiate(&graph.exec, g, 0);
+                cudaGraphDestroy(g);
+                HAL_TRY(CudaStatus(e, "cudaGraphInstantiate"));
+                graph.key = key;
+            }
+            HAL_TRY(CudaStatus(cudaGraphLaunch(graph.exec, s), "cudaGraphLaunch"));
+            CountLaunch(ticks);
+            cur ^= (ticks & 1);
+            return HAL_CUDA_OK;
+        }
+    };
+}
+
+using halcuda::Diffusion;
+
+struct hal_cuda_diffusion : public Diffusion
+{
+};
+
+extern "C" int hal_cuda_diffusion_create(int32_t xDim, int32_t yDim, hal_cuda_diffusion **out)
+{
+    HAL_REQUIRE(out != nullptr, "hal_cuda_diffusion_create: out is NULL");
+    *out = nullptr;
+    HAL_REQUIRE(xDim > 0 && yDim > 0, "hal_cuda_diffusion_create: dimensions must be positive");
+    HAL_REQUIRE(static_cast<int64_t>(xDim) * yDim < (int64_t(1) << 31),
+                "hal_cuda_diffusion_create: xDim*yDim exceeds int32");
+    hal_cuda_diffusion *h = new (std::nothrow) hal_cuda_diffusion();
+    if (h == nullptr)
+    {
+        halcuda::SetError("hal_cuda_diffusion_create: out of host memory");
+        return HAL_CUDA_ENOMEM;
+    }
+    int rc = h->Init(xDim, yDim);
+    if (rc != HAL_CUDA_OK)
+    {
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return HAL_CUDA_OK;
+}
+
+extern "C" int hal_cuda_diffusion_destroy(hal_cuda_diffusion *h)
+{
+    if (h != nullptr)
+    {
+        cudaSetDevice(h->device);
+        cudaStreamSynchronize(h->stream.Get());
+        delete h;
+    }
+    return HAL_CUDA_OK;
+}
+
+namespace
+{
+    int DiffuseCommon(hal_cuda_diffusion *h, const double *field, double *deltas, double r,
+                      int32_t wrapX, int32_t wrapY, const double *ghost, const char *who)
+    {
+        using namespace halcuda;
+        HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+        size_t n = h->Length();
+        size_t ng = ghost ? 2 * (static_cast<size_t>(h->xDim) + h->yDim) : 0;
+        if (h->f64.p == nullptr)
+        {
+            HAL_TRY(h->f64.Alloc(n, "cudaMalloc(f64)"));
+            HAL_TRY(h->d64.Alloc(n, "cudaMalloc(d64)"));
+            HAL_TRY(h->g64.Alloc(2 * (static_cast<size_t>(h->xDim) + h->yDim), "cudaMalloc(g64)"));
+        }
+        cudaStream_t s = h->stream.Get();
+        HAL_TRY(CudaStatus(cudaMemcpyAsync(h->f64.p, field, n * sizeof(double), cudaMemcpyHostToDevice, s),
+                           "cudaMemcpy(field)"));
+        HAL_TRY(CudaStatus(cudaMemcpyAsync(h->d64.p, deltas, n * sizeof(double), cudaMemcpyHostToDevice, s),
+                           "cudaMemcpy(deltas)"));
+        if (ghost)
+        {
+            HAL_TRY(CudaStatus(cudaMemcpyAsync(h->g64.p, ghost, ng * sizeof(double), cudaMemcpyHostToDevice, s),
+                               "cudaMemcpy(ghost)"));
+        }
+        unsigned blocks = static_cast<unsigned>((n + 255) / 256);
+        Diffuse64Kernel<<<blocks, 256, 0, s>>>(h->f64.p, h->d64.p, h->xDim, h->yDim, r, wrapX, wrapY,
+                                               ghost ? h->g64.p : nullptr);
+        CountLaunch();
+        HAL_TRY(LaunchStatus(who));
+        HAL_TRY(CudaStatus(cudaMemcpyAsync(deltas, h->d64.p, n * sizeof(double), cudaMemcpyDeviceToHost, s),
+                           "cudaMemcpy(deltas)"));
+        return CudaStatus(cudaStreamSynchronize(s), who);
+    }
+}
+
+extern "C" int hal_cuda_diffuse(hal_cuda_diffusion *h, const double *field, int64_t fieldLen,
+                                double *deltas, int64_t deltasLen, double diffRate, int32_t xDim,
+                                int32_t yDim, int32_t wrapX, int32_t wrapY)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_diffuse: handle is NULL");
+    int64_t length = static_cast<int64_t>(xDim) * yDim;
+    HAL_REQUIRE(xDim > 0 && yDim > 0 && fieldLen == length && deltasLen == length,
+                "CudaDiffusionBackend2D::Diffuse: field and deltas must each hold xDim*yDim values");
+    HAL_REQUIRE(xDim == h->xDim && yDim == h->yDim,
+                "CudaDiffusionBackend2D::Diffuse called with dimensions differing from construction");
+    HAL_REQUIRE(field != nullptr && deltas != nullptr, "hal_cuda_diffuse: NULL array");
+    return DiffuseCommon(h, field, deltas, diffRate, wrapX, wrapY, nullptr, "hal_cuda_diffuse");
+}
+
+extern "C" int hal_cuda_diffuse_bc(hal_cuda_diffusion *h, const double *field, double *deltas,
+                                   double diffRate, int32_t wrapX, int32_t wrapY, const double *ghost)
+{
+    HAL_REQUIRE(h != nullptr && field != nullptr && deltas != nullptr, "hal_cuda_diffuse_bc: NULL argument");
+    return DiffuseCommon(h, field, deltas, diffRate, wrapX, wrapY, ghost, "hal_cuda_diffuse_bc");
+}
+
+extern "C" int hal_cuda_diffusion_set_field(hal_cuda_diffusion *h, const float *field, int64_t len)
+{
+    HAL_REQUIRE(h != nullptr && field != nullptr, "hal_cuda_diffusion_set_field: NULL argument");
+    HAL_REQUIRE(len == static_cast<int64_t>(h->Length()),
+                "hal_cuda_diffusion_set_field: field must hold xDim*yDim values");
+    HAL_TRY(halcuda::CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    cudaStream_t s = h->stream.Get();
+    HAL_TRY(halcuda::CudaStatus(cudaMemcpyAsync(h->field[h->cur].p, field, h->Length() * sizeof(float),
+                                                cudaMemcpyHostToDevice, s),
+                                "cudaMemcpy(field)"));
+    return halcuda::CudaStatus(cudaStreamSynchronize(s), "hal_cuda_diffusion_set_field");
+}
+
+extern "C" int hal_cuda_diffusion_get_field(hal_cuda_diffusion *h, float *field, int64_t len)
+{
+    HAL_REQUIRE(h != nullptr && field != nullptr, "hal_cuda_diffusion_get_field: NULL argument");
+    HAL_REQUIRE(len == static_cast<int64_t>(h->Length()),
+                "hal_cuda_diffusion_get_field: field must hold xDim*yDim values");
+    HAL_TRY(halcuda::CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    cudaStream_t s = h->stream.Get();
+    HAL_TRY(halcuda::CudaStatus(cudaMemcpyAsync(field, h->field[h->cur].p, h->Length() * sizeof(float),
+                                                cudaMemcpyDeviceToHost, s),
+                                "cudaMemcpy(field)"));
+    return halcuda::CudaStatus(cudaStreamSynchronize(s), "hal_cuda_diffusion_get_field");
+}
+
+extern "C" int hal_cuda_diffusion_set_source(hal_cuda_diffusion *h, const float *dense, int64_t len)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_diffusion_set_source: handle is NULL");
+    HAL_TRY(halcuda::CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    if (dense == nullptr)
+    {
+        h->hasSrc = false;
+        return HAL_CUDA_OK;
+    }
+    HAL_REQUIRE(len == static_cast<int64_t>(h->Length()),
+                "hal_cuda_diffusion_set_source: source must hold xDim*yDim values");
+    if (h->src.p == nullptr)
+    {
+        HAL_TRY(h->src.Alloc(h->Length(), "cudaMalloc(src)"));
+    }
+    HAL_TRY(halcuda::CudaStatus(cudaMemcpy(h->src.p, dense, h->Length() * sizeof(float), cudaMemcpyHostToDevice),
+                                "cudaMemcpy(src)"));
+    h->hasSrc = true;
+    h->ResetGraphs();
+    return HAL_CUDA_OK;
+}
+
+extern "C" int hal_cuda_diffusion_set_point_sources(hal_cuda_diffusion *h, int32_t nPoints,
+                                                    const int32_t *cells, const float *values)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_diffusion_set_point_sources: handle is NULL");
+    HAL_REQUIRE(nPoints >= 0, "hal_cuda_diffusion_set_point_sources: negative count");
+    HAL_TRY(halcuda::CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    h->ResetGraphs();
+    if (nPoints == 0)
+    {
+        h->hasPoints = false;
+        return HAL_CUDA_OK;
+    }
+    HAL_REQUIRE(cells != nullptr && values != nullptr, "hal_cuda_diffusion_set_point_sources: NULL array");
+    int64_t n = static_cast<int64_t>(h->Length());
+    // Group the points by the CTA of the tick kernel that owns their cell.
+    int vec = h->vec4 ? 4 : 1;
+    int32_t gx = static_cast<int32_t>(h->grid.x);
+    int32_t nBlocks = gx * static_cast<int32_t>(h->grid.y);
+    std::vector<int32_t> blockOf(nPoints), start(nBlocks + 1, 0);
+    for (int32_t k = 0; k < nPoints; k++)
+    {
+        HAL_REQUIRE(cells[k] >= 0 && cells[k] < n, "hal_cuda_diffusion_set_point_sources: cell %d out of range",
+                    cells[k]);
+        int32_t x = cells[k] / h->yDim;
+        int32_t y = cells[k] % h->yDim;
+        int32_t bx = y / (32 * vec);
+        int32_t by = x / (halcuda::kTickWarps * halcuda::kTickRowsPerThread);
+        blockOf[k] = by * gx + bx;
+        start[blockOf[k] + 1]++;
+    }
+    for (int32_t b = 0; b < nBlocks; b++)
+    {
+        start[b + 1] += start[b];
+    }
+    std::vector<int32_t> row(nPoints), col(nPoints), cursor(start.begin(), start.end() - 1);
+    std::vector<float> val(nPoints);
+    for (int32_t k = 0; k < nPoints; k++)
+    {
+        int32_t slot = cursor[blockOf[k]]++;
+        row[slot] = cells[k] / h->yDim;
+        col[slot] = cells[k] % h->yDim;
+        val[slot] = values[k];
+    }
+    HAL_TRY(h->ptStart.Alloc(nBlocks + 1, "cudaMalloc(points)"));
+    HAL_TRY(h->ptRow.Alloc(nPoints, "cudaMalloc(points)"));
+    HAL_TRY(h->ptCol.Alloc(nPoints, "cudaMalloc(points)"));
+    HAL_TRY(h->ptVal.Alloc(nPoints, "cudaMalloc(points)"));
+    HAL_TRY(halcuda::CudaStatus(cudaMemcpy(h->ptStart.p, start.data(), (nBlocks + 1) * sizeof(int32_t),
+                                           cudaMemcpyHostToDevice), "cudaMemcpy(points)"));
+    HAL_TRY(halcuda::CudaStatus(cudaMemcpy(h->ptRow.p, row.data(), nPoints * sizeof(int32_t), cudaMemcpyHostToDevice),
+                                "cudaMemcpy(points)"));
+    HAL_TRY(halcuda::CudaStatus(cudaMemcpy(h->ptCol.p, col.data(), nPoints * sizeof(int32_t), cudaMemcpyHostToDevice),
+                                "cudaMemcpy(points)"));
+    HAL_TRY(halcuda::CudaStatus(cudaMemcpy(h->ptVal.p, val.data(), nPoints * sizeof(float), cudaMemcpyHostToDevice),
+                                "cudaMemcpy(points)"));
+    h->hasPoints = true;
+    return HAL_CUDA_OK;
+}
+
+extern "C" int hal_cuda_diffusion_set_dirichlet(hal_cuda_diffusion *h, const float *ghost)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_diffusion_set_dirichlet: handle is NULL");
+    HAL_TRY(halcuda::CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    h->ResetGraphs();
+    if (ghost == nullptr)
+    {
+        h->hasGhost = false;
+        return HAL_CUDA_OK;
+    }
+    size_t ng = 2 * (static_cast<size_t>(h->xDim) + h->yDim);
+    if (h->ghost.p == nullptr)
+    {
+        HAL_TRY(h->ghost.Alloc(ng, "cudaMalloc(ghost)"));
+    }
+    HAL_TRY(halcuda::CudaStatus(cudaMemcpy(h->ghost.p, ghost, ng * sizeof(float), cudaMemcpyHostToDevice),
+                                "cudaMemcpy(ghost)"));
+    h->hasGhost = true;
+    return HAL_CUDA_OK;
+}
+
+extern "C" int hal_cuda_diffusion_run_ticks(hal_cuda_diffusion *h, int32_t ticks, double diffRate,
+                                            double decay, int32_t wrapX, int32_t wrapY)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_diffusion_run_ticks: handle is NULL");
+    HAL_REQUIRE(ticks >= 0, "hal_cuda_diffusion_run_ticks: negative tick count");
+    HAL_REQUIRE(!(diffRate > 0.25), "Diffusion rate above stable maximum value of 0.25");
+    HAL_TRY(halcuda::CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    return h->RunTicks(ticks, diffRate, decay, wrapX != 0, wrapY != 0, true);
+}
+
+extern "C" int hal_cuda_diffusion_run_steps(hal_cuda_diffusion *h, float *field, int64_t len, int32_t steps,
+                                            double diffRate, int32_t wrapX, int32_t wrapY)
+{
+    HAL_REQUIRE(h != nullptr && field != nullptr, "hal_cuda_diffusion_run_steps: NULL argument");
+    HAL_REQUIRE(len == static_cast<int64_t>(h->Length()),
+                "DiffusionKernel2D::RunSteps: field must hold xDim*yDim values");
+    HAL_REQUIRE(steps >= 0, "hal_cuda_diffusion_run_steps: negative step count");
+    HAL_TRY(hal_cuda_diffusion_set_field(h, field, len));
+    HAL_TRY(h->RunTicks(steps, diffRate, 0.0, wrapX != 0, wrapY != 0, false));
+    return hal_cuda_diffusion_get_field(h, field, len);
+}
+
+extern "C" int hal_cuda_diffusion_sync(hal_cuda_diffusion *h)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_diffusion_sync: handle is NULL");
+    HAL_TRY(halcuda::CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    return halcuda::CudaStatus(cudaStreamSynchronize(h->stream.Get()), "hal_cuda_diffusion_sync");
+}
+
+extern "C" void *hal_cuda_diffusion_stream(hal_cuda_diffusion *h)
+{
+    return h ? static_cast<void *>(h->stream.Get()) : nullptr;
+}
+
+extern "C" int hal_cuda_diffusion_set_stream(hal_cuda_diffusion *h, void *stream)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_diffusion_set_stream: handle is NULL");
+    h->stream.Set(stream);
+    h->ResetGraphs();
+    return HAL_CUDA_OK;
+}
+
+extern "C" int hal_cuda_diffusion_profile(hal_cuda_diffusion *h, int32_t iters, double diffRate, double decay,
+                                          int32_t wrapX, int32_t wrapY, float *ms)
+{
+    HAL_REQUIRE(h != nullptr && ms != nullptr, "hal_cuda_diffusion_profile: NULL argument");
+    HAL_REQUIRE(iters > 0, "hal_cuda_diffusion_profile: iters must be positive");
+    HAL_REQUIRE(!(diffRate > 0.25), "Diffusion rate above stable maximum value of 0.25");
+    using namespace halcuda;
+    HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    cudaStream_t s = h->stream.Get();
+    cudaEvent_t e0, e1;
+    HAL_TRY(CudaStatus(cudaEventCreate(&e0), "cudaEventCreate"));
+    HAL_TRY(CudaStatus(cudaEventCreate(&e1), "cudaEventCreate"));
+    double total = 0.0;
+    int rc = HAL_CUDA_OK;
+    for (int32_t t = 0; t < iters; t++)
+    {
+        int c = h->cur;
+        TickParams p = h->Params(h->field[c].p, h->field[c ^ 1].p, diffRate, decay, wrapX != 0, wrapY != 0, true);
+        cudaEventRecord(e0, s);
+        h->LaunchTick(p, s);
+        CountLaunch();
+        cudaEventRecord(e1, s);
+        rc = LaunchStatus("TickKernel launch");
+        if (rc == HAL_CUDA_OK)
+        {
+            rc = CudaStatus(cudaEventSynchronize(e1), "hal_cuda_diffusion_profile");
+        }
+        if (rc != HAL_CUDA_OK)
+        {
+            break;
+        }
+        float a = 0.0f;
+        cudaEventElapsedTime(&a, e0, e1);
+        total += a;
+        h->cur ^= 1;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    HAL_TRY(rc);
+    *ms = static_cast<float>(total / iters);
+    return HAL_CUDA_OK;
+}

@@ -1,0 +1,385 @@
+"""ctypes binding of libhal_cuda.so (the C ABI in include/hal_cuda.h).
+
+This is the Python host side used by the tests and the benchmark; the C++
+host side for HAL-CPP models is hal-cpp_gb300/cpp (Hal::Cuda::*Backend2D).
+Errors follow the reference's convention: HAL_CUDA_EINVAL raises ValueError
+(std::invalid_argument in C++), every other failure RuntimeError.
+
+There is no CPU fallback: importing works without a GPU, but every call that
+needs the CUDA library raises if libhal_cuda.so is missing or no device is
+present.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_DIR, "libhal_cuda.so")
+
+OK, EINVAL, ENOMEM, EDEVICE, ETIMEOUT, ENOTSUP = 0, 1, 2, 3, 4, 5
+ADI_MAX_LINE = 4096
+
+# Every exported symbol of include/hal_cuda.h, with (restype, argtypes).
+_i32, _i64, _f64, _vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p
+_I = ctypes.c_int
+SIGNATURES = {
+    "hal_cuda_version": (ctypes.c_char_p, []),
+    "hal_cuda_last_error": (ctypes.c_char_p, []),
+    "hal_cuda_device_count": (_I, [_vp]),
+    "hal_cuda_set_device": (_I, [_i32]),
+    "hal_cuda_launch_count": (_i64, []),
+    "hal_cuda_diffusion_create": (_I, [_i32, _i32, _vp]),
+    "hal_cuda_diffusion_destroy": (_I, [_vp]),
+    "hal_cuda_diffuse": (_I, [_vp, _vp, _i64, _vp, _i64, _f64, _i32, _i32, _i32, _i32]),
+    "hal_cuda_diffuse_bc": (_I, [_vp, _vp, _vp, _f64, _i32, _i32, _vp]),
+    "hal_cuda_diffusion_set_field": (_I, [_vp, _vp, _i64]),
+    "hal_cuda_diffusion_get_field": (_I, [_vp, _vp, _i64]),
+    "hal_cuda_diffusion_set_source": (_I, [_vp, _vp, _i64]),
+    "hal_cuda_diffusion_set_point_sources": (_I, [_vp, _i32, _vp, _vp]),
+    "hal_cuda_diffusion_set_dirichlet": (_I, [_vp, _vp]),
+    "hal_cuda_diffusion_run_ticks": (_I, [_vp, _i32, _f64, _f64, _i32, _i32]),
+    "hal_cuda_diffusion_run_steps": (_I, [_vp, _vp, _i64, _i32, _f64, _i32, _i32]),
+    "hal_cuda_diffusion_profile": (_I, [_vp, _i32, _f64, _f64, _i32, _i32, _vp]),
+    "hal_cuda_diffusion_sync": (_I, [_vp]),
+    "hal_cuda_diffusion_stream": (_vp, [_vp]),
+    "hal_cuda_diffusion_set_stream": (_I, [_vp, _vp]),
+    "hal_cuda_adi_create": (_I, [_i32, _i32, _vp]),
+    "hal_cuda_adi_destroy": (_I, [_vp]),
+    "hal_cuda_diffuse_adi": (_I, [_vp, _vp, _i64, _vp, _i64, _f64, _i32, _i32, _i32, _i32]),
+    "hal_cuda_diffuse_adi_bc": (_I, [_vp, _vp, _vp, _f64, _i32, _i32, _vp]),
+    "hal_cuda_adi_set_field": (_I, [_vp, _vp, _i64]),
+    "hal_cuda_adi_get_field": (_I, [_vp, _vp, _i64]),
+    "hal_cuda_adi_set_source": (_I, [_vp, _vp, _i64]),
+    "hal_cuda_adi_set_dirichlet": (_I, [_vp, _vp]),
+    "hal_cuda_adi_set_uptake": (_I, [_vp, _vp, _f64]),
+    "hal_cuda_adi_run_ticks": (_I, [_vp, _i32, _f64, _f64, _i32, _i32]),
+    "hal_cuda_adi_run_steps": (_I, [_vp, _vp, _i64, _i32, _f64, _i32, _i32]),
+    "hal_cuda_adi_run_ticks_host": (_I, [_vp, _vp, _vp, _i64, _i32, _f64, _f64, _i32, _i32]),
+    "hal_cuda_adi_profile": (_I, [_vp, _i32, _f64, _f64, _i32, _i32, _vp]),
+    "hal_cuda_adi_sync": (_I, [_vp]),
+    "hal_cuda_adi_stream": (_vp, [_vp]),
+    "hal_cuda_adi_set_stream": (_I, [_vp, _vp]),
+    "hal_cuda_agents_create": (_I, [_i32, _i32, _i32, _vp]),
+    "hal_cuda_agents_destroy": (_I, [_vp]),
+    "hal_cuda_accumulate_forces": (_I, [_vp, _vp, _i64, _vp, _i64, _vp, _f64, _f64, _i32, _i32, _i32,
+                                        _i32]),
+    "hal_cuda_agents_upload": (_I, [_vp, _vp, _vp, _i32]),
+    "hal_cuda_agents_dispatch": (_I, [_vp, _f64, _f64, _i32, _i32]),
+    "hal_cuda_agents_download": (_I, [_vp, _vp, _i32]),
+    "hal_cuda_agents_get_bins": (_I, [_vp, _vp, _vp]),
+    "hal_cuda_agents_profile": (_I, [_vp, _i32, _f64, _f64, _i32, _i32, _vp]),
+    "hal_cuda_agents_sync": (_I, [_vp]),
+    "hal_cuda_agents_stream": (_vp, [_vp]),
+    "hal_cuda_agents_set_stream": (_I, [_vp, _vp]),
+}
+
+_lib = None
+
+
+def lib():
+    """The loaded library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with hal-cpp_gb300/build.py")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    return lib().hal_cuda_last_error().decode()
+
+
+def _check(rc: int, what: str = ""):
+    if rc == OK:
+        return
+    msg = last_error()
+    if rc == EINVAL:
+        raise ValueError(msg or what)
+    raise RuntimeError(f"{what}: status {rc}: {msg}")
+
+
+def version() -> str:
+    return lib().hal_cuda_version().decode()
+
+
+def device_count() -> int:
+    n = ctypes.c_int32(0)
+    rc = lib().hal_cuda_device_count(ctypes.byref(n))
+    return n.value if rc == OK else 0
+
+
+def launch_count() -> int:
+    return int(lib().hal_cuda_launch_count())
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def _f32(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.int32)
+
+
+class _Handle:
+    _prefix = ""
+
+    def __init__(self):
+        self._h = None
+
+    def close(self):
+        if self._h is not None:
+            getattr(lib(), f"hal_cuda_{self._prefix}_destroy")(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def sync(self):
+        _check(getattr(lib(), f"hal_cuda_{self._prefix}_sync")(self._h), "sync")
+
+    def stream(self) -> int:
+        return getattr(lib(), f"hal_cuda_{self._prefix}_stream")(self._h) or 0
+
+    def set_stream(self, stream_ptr: int | None):
+        _check(getattr(lib(), f"hal_cuda_{self._prefix}_set_stream")(self._h, stream_ptr or None),
+               "set_stream")
+
+
+class Diffusion(_Handle):
+    """hal_cuda_diffusion: IDiffusionBackend2D plus the resident fused tick."""
+
+    _prefix = "diffusion"
+
+    def __init__(self, xDim: int, yDim: int):
+        super().__init__()
+        h = ctypes.c_void_p()
+        _check(lib().hal_cuda_diffusion_create(xDim, yDim, ctypes.byref(h)), "diffusion_create")
+        self._h = h
+        self.xDim, self.yDim = xDim, yDim
+
+    def diffuse(self, field, deltas, diffRate, xDim, yDim, wrapX, wrapY):
+        """IDiffusionBackend2D::Diffuse on float64 host arrays; deltas is
+        updated in place and returned."""
+        f = _f64(field)
+        d = np.ascontiguousarray(deltas, dtype=np.float64)
+        _check(lib().hal_cuda_diffuse(self._h, _p(f), f.size, _p(d), d.size, diffRate, xDim, yDim,
+                                      int(wrapX), int(wrapY)), "diffuse")
+        return d
+
+    def diffuse_bc(self, field, deltas, diffRate, wrapX, wrapY, ghost):
+        f = _f64(field)
+        d = np.ascontiguousarray(deltas, dtype=np.float64)
+        g = _f64(ghost)
+        _check(lib().hal_cuda_diffuse_bc(self._h, _p(f), _p(d), diffRate, int(wrapX), int(wrapY),
+                                         _p(g)), "diffuse_bc")
+        return d
+
+    def set_field(self, field):
+        f = _f32(field)
+        _check(lib().hal_cuda_diffusion_set_field(self._h, _p(f), f.size), "set_field")
+
+    def get_field(self):
+        out = np.empty(self.xDim * self.yDim, dtype=np.float32)
+        _check(lib().hal_cuda_diffusion_get_field(self._h, _p(out), out.size), "get_field")
+        return out
+
+    def set_source(self, dense):
+        d = _f32(dense)
+        _check(lib().hal_cuda_diffusion_set_source(self._h, _p(d), 0 if d is None else d.size),
+               "set_source")
+
+    def set_point_sources(self, cells, values):
+        c = _i32(cells)
+        v = _f32(values)
+        n = 0 if c is None else c.size
+        _check(lib().hal_cuda_diffusion_set_point_sources(self._h, n, _p(c), _p(v)),
+               "set_point_sources")
+
+    def set_dirichlet(self, ghost):
+        g = _f32(ghost)
+        _check(lib().hal_cuda_diffusion_set_dirichlet(self._h, _p(g)), "set_dirichlet")
+
+    def run_ticks(self, ticks, diffRate, decay=0.0, wrapX=False, wrapY=False):
+        _check(lib().hal_cuda_diffusion_run_ticks(self._h, ticks, diffRate, decay, int(wrapX),
+                                                  int(wrapY)), "run_ticks")
+
+    def profile(self, iters, diffRate, decay=0.0, wrapX=False, wrapY=False):
+        """Average ms of one fused-tick launch."""
+        ms = np.zeros(1, dtype=np.float32)
+        _check(lib().hal_cuda_diffusion_profile(self._h, iters, diffRate, decay, int(wrapX),
+                                                int(wrapY), _p(ms)), "profile")
+        return float(ms[0])
+
+    def run_steps(self, field, steps, diffRate, wrapX=False, wrapY=False):
+        f = np.array(field, dtype=np.float32, copy=True)
+        _check(lib().hal_cuda_diffusion_run_steps(self._h, _p(f), f.size, steps, diffRate,
+                                                  int(wrapX), int(wrapY)), "run_steps")
+        return f
+
+
+class Adi(_Handle):
+    """hal_cuda_adi: IAdiDiffusionBackend2D plus the resident ADI tick."""
+
+    _prefix = "adi"
+
+    def __init__(self, xDim: int, yDim: int):
+        super().__init__()
+        h = ctypes.c_void_p()
+        _check(lib().hal_cuda_adi_create(xDim, yDim, ctypes.byref(h)), "adi_create")
+        self._h = h
+        self.xDim, self.yDim = xDim, yDim
+
+    def diffuse_adi(self, field, deltas, diffRate, xDim, yDim, wrapX, wrapY):
+        f = _f64(field)
+        d = np.ascontiguousarray(deltas, dtype=np.float64)
+        _check(lib().hal_cuda_diffuse_adi(self._h, _p(f), f.size, _p(d), d.size, diffRate, xDim,
+                                          yDim, int(wrapX), int(wrapY)), "diffuse_adi")
+        return d
+
+    def diffuse_adi_bc(self, field, deltas, diffRate, wrapX, wrapY, ghost):
+        f = _f64(field)
+        d = np.ascontiguousarray(deltas, dtype=np.float64)
+        g = _f64(ghost)
+        _check(lib().hal_cuda_diffuse_adi_bc(self._h, _p(f), _p(d), diffRate, int(wrapX),
+                                             int(wrapY), _p(g)), "diffuse_adi_bc")
+        return d
+
+    def set_field(self, field):
+        f = _f32(field)
+        _check(lib().hal_cuda_adi_set_field(self._h, _p(f), f.size), "set_field")
+
+    def get_field(self):
+        out = np.empty(self.xDim * self.yDim, dtype=np.float32)
+        _check(lib().hal_cuda_adi_get_field(self._h, _p(out), out.size), "get_field")
+        return out
+
+    def set_source(self, dense):
+        d = _f32(dense)
+        _check(lib().hal_cuda_adi_set_source(self._h, _p(d), 0 if d is None else d.size),
+               "set_source")
+
+    def set_dirichlet(self, ghost):
+        g = _f32(ghost)
+        _check(lib().hal_cuda_adi_set_dirichlet(self._h, _p(g)), "set_dirichlet")
+
+    def set_uptake(self, agents, uptake):
+        _check(lib().hal_cuda_adi_set_uptake(self._h, None if agents is None else agents.handle,
+                                             uptake), "set_uptake")
+
+    def run_ticks(self, ticks, diffRate, decay=0.0, wrapX=False, wrapY=False):
+        _check(lib().hal_cuda_adi_run_ticks(self._h, ticks, diffRate, decay, int(wrapX),
+                                            int(wrapY)), "run_ticks")
+
+    def run_steps(self, field, steps, diffRate, wrapX=False, wrapY=False):
+        f = np.array(field, dtype=np.float32, copy=True)
+        _check(lib().hal_cuda_adi_run_steps(self._h, _p(f), f.size, steps, diffRate, int(wrapX),
+                                            int(wrapY)), "run_steps")
+        return f
+
+    def profile(self, iters, diffRate, decay=0.0, wrapX=False, wrapY=False):
+        """Average ms of one launch of (x-sweep, y-sweep)."""
+        ms = np.zeros(2, dtype=np.float32)
+        _check(lib().hal_cuda_adi_profile(self._h, iters, diffRate, decay, int(wrapX), int(wrapY),
+                                          _p(ms)), "profile")
+        return float(ms[0]), float(ms[1])
+
+    def run_ticks_host(self, field, src, ticks, diffRate, decay=0.0, wrapX=False, wrapY=False,
+                       out=None):
+        """Host-to-host ticks: field (and src) uploaded, ticks run, field
+        downloaded.  ``field`` must be a float32 array; it is updated in place
+        when ``out`` is None."""
+        f = field if out is None else out
+        if f is not field:
+            np.copyto(f, field)
+        s = None if src is None else src
+        _check(lib().hal_cuda_adi_run_ticks_host(self._h, f.ctypes.data,
+                                                 None if s is None else s.ctypes.data, f.size,
+                                                 ticks, diffRate, decay, int(wrapX), int(wrapY)),
+               "run_ticks_host")
+        return f
+
+
+class Agents(_Handle):
+    """hal_cuda_agents: IAgentForceBackend2D plus the resident dispatch."""
+
+    _prefix = "agents"
+
+    def __init__(self, xDim: int, yDim: int, maxAgents: int):
+        super().__init__()
+        h = ctypes.c_void_p()
+        _check(lib().hal_cuda_agents_create(xDim, yDim, maxAgents, ctypes.byref(h)),
+               "agents_create")
+        self._h = h
+        self.xDim, self.yDim, self.maxAgents = xDim, yDim, maxAgents
+        self.n = 0
+
+    def accumulate_forces(self, positions, radii, interactionRad, springConstant, xDim, yDim,
+                          wrapX, wrapY):
+        """IAgentForceBackend2D::AccumulateForces; returns velocityDeltas
+        (float64, 2n)."""
+        p = _f64(positions)
+        r = _f64(radii)
+        out = np.zeros(p.size, dtype=np.float64)
+        _check(lib().hal_cuda_accumulate_forces(self._h, _p(p), p.size, _p(r), r.size, _p(out),
+                                                interactionRad, springConstant, xDim, yDim,
+                                                int(wrapX), int(wrapY)), "accumulate_forces")
+        self.n = r.size
+        return out
+
+    def upload(self, positions, radii):
+        p = _f32(positions)
+        r = _f32(radii)
+        _check(lib().hal_cuda_agents_upload(self._h, _p(p), _p(r), r.size), "upload")
+        self.n = r.size
+
+    def dispatch(self, interactionRad, springConstant, wrapX=False, wrapY=False):
+        _check(lib().hal_cuda_agents_dispatch(self._h, interactionRad, springConstant,
+                                              int(wrapX), int(wrapY)), "dispatch")
+
+    def download(self):
+        out = np.empty(2 * self.n, dtype=np.float32)
+        _check(lib().hal_cuda_agents_download(self._h, _p(out), self.n), "download")
+        return out
+
+    def profile(self, iters, interactionRad, springConstant, wrapX=False, wrapY=False):
+        """Average ms per launch: count, scan, scatter, stabilize, forces, whole."""
+        ms = np.zeros(6, dtype=np.float32)
+        _check(lib().hal_cuda_agents_profile(self._h, iters, interactionRad, springConstant,
+                                             int(wrapX), int(wrapY), _p(ms)), "profile")
+        return [float(v) for v in ms]
+
+    def get_bins(self):
+        off = np.empty(self.xDim * self.yDim + 1, dtype=np.int32)
+        bucket = np.empty(max(self.n, 1), dtype=np.int32)
+        _check(lib().hal_cuda_agents_get_bins(self._h, _p(off), _p(bucket)), "get_bins")
+        return off, bucket[: self.n]

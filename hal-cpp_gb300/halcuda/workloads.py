@@ -1,0 +1,62 @@
+"""Seeded synthetic inputs for the benchmark workloads.
+
+numpy's PCG64 stands in for Hal::Rand (xoshiro256**); the shapes, sizes and
+value distributions are the workloads' own:
+
+* explicit   -- field U[0,1); 64 distinct point sources of 0.05; Dirichlet 1.0
+                on the x = -1 edge, 0.0 elsewhere; rate 0.2; decay 0.001
+* adi        -- sum of 200 Gaussian blobs (centre U[0,n)^2, sigma 10 + U[0,70),
+                amplitude U[0,1)); constant source field U[0,0.01); rate 5.0;
+                decay 0.01; zero-flux
+* agents     -- 70% uniform and 30% in a Gaussian cluster (sigma 100 cells)
+                at a seeded centre, clamped into the domain; float32
+                positions; radius 0.5; cutoff 1.0; stiffness 0.1; walls
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def explicit_inputs(n: int = 256, seed: int = 1, n_sources: int = 64):
+    rng = np.random.default_rng(seed)
+    field = rng.random(n * n)
+    sites = rng.choice(n * n, n_sources, replace=False).astype(np.int32)
+    values = np.full(n_sources, 0.05)
+    ghost = np.zeros(4 * n)
+    ghost[:n] = 1.0  # bc(-1, y) = 1.0
+    return dict(field=field, src_idx=sites, src_val=values, ghost=ghost, diffRate=0.2,
+                decay=0.001, xDim=n, yDim=n)
+
+
+def gaussian_blobs(n: int, rng, count: int = 200):
+    field = np.zeros((n, n))
+    coord = np.arange(n, dtype=np.float64)
+    for _ in range(count):
+        cx, cy = rng.random(2) * n
+        sigma = 10.0 + rng.random() * 70.0
+        amp = rng.random()
+        ex = np.exp(-((coord - cx) ** 2) / (2.0 * sigma * sigma))
+        ey = np.exp(-((coord - cy) ** 2) / (2.0 * sigma * sigma))
+        field += amp * np.outer(ex, ey)
+    return field.ravel()
+
+
+def adi_inputs(n: int = 2048, seed: int = 2, blobs: int = 200):
+    rng = np.random.default_rng(seed)
+    field = gaussian_blobs(n, rng, blobs)
+    src = rng.random(n * n) * 0.01
+    return dict(field=field, src=src, diffRate=5.0, decay=0.01, xDim=n, yDim=n)
+
+
+def agent_inputs(n_agents: int = 1_000_000, dim: int = 2048, seed: int = 3):
+    rng = np.random.default_rng(seed)
+    m = int(round(n_agents * 0.3))
+    uni = rng.random((n_agents - m, 2)) * dim
+    centre = rng.random(2) * dim
+    clu = centre + rng.normal(0.0, 100.0, (m, 2))
+    pos = np.concatenate([uni, clu])
+    hi = np.nextafter(np.float32(dim), np.float32(0))
+    pos = np.clip(pos, 0.0, float(hi)).astype(np.float32)
+    radii = np.full(n_agents, 0.5, dtype=np.float32)
+    return dict(positions=pos.ravel(), radii=radii, interactionRad=1.0, springConstant=0.1,
+                xDim=dim, yDim=dim, uptake=0.001)

@@ -1,0 +1,261 @@
+/*
+ * hal_cuda.h -- C ABI of the GB300 (sm_103a) compute backend for HAL-CPP.
+ *
+ * This is the drop-in boundary.  HAL-CPP's three per-tick strategy interfaces
+ *   Hal::IDiffusionBackend2D     (include/Hal/Pde/IDiffusionBackend2D.h:13-33)
+ *   Hal::IAdiDiffusionBackend2D  (include/Hal/Pde/IAdiDiffusionBackend2D.h:12-32)
+ *   Hal::IAgentForceBackend2D    (include/Hal/Agents/IAgentForceBackend2D.h:15-37)
+ * are implemented by the C++ classes Hal::Cuda::CudaDiffusionBackend2D,
+ * CudaAdiDiffusionBackend2D and CudaAgentForceBackend2D, which call only the
+ * functions below.  Signatures carry plain pointers and sizes; nothing here
+ * needs CUDA or C++ headers.  The Vulkan classes these replace are
+ *   Hal::Gpu::GpuDiffusionBackend2D     (src/Gpu/GpuDiffusionBackend2D.cpp:22-52)
+ *   Hal::Gpu::GpuAdiDiffusionBackend2D  (src/Gpu/GpuAdiDiffusionBackend2D.cpp:24-50)
+ *   Hal::Gpu::GpuAgentForceBackend2D    (src/Gpu/GpuAgentForceBackend2D.cpp:24-68)
+ * and their kernel hosts DiffusionKernel2D / AdiKernel2D / AgentForceKernel2D.
+ *
+ * Conventions
+ *   - Field layout is HAL's row-major i = x*yDim + y (y contiguous).
+ *   - Every call returns an int status: HAL_CUDA_OK or one of the error codes.
+ *     hal_cuda_last_error() gives the message of the calling thread's last
+ *     failure.  HAL_CUDA_EINVAL maps to std::invalid_argument in the C++
+ *     wrappers, every other error to std::runtime_error (the reference's
+ *     convention: IDiffusionBackend2D.cpp:26-31, AdiKernel2D.cpp:66-70).
+ *   - A handle is sized at creation (as the Vulkan backends are,
+ *     GpuDiffusionBackend2D.h:18-20) and owns its device buffers and one CUDA
+ *     stream.  A handle must not be used from two threads at once; separate
+ *     handles may run on separate threads.
+ *   - Calls that take host arrays are synchronous: results are in host
+ *     memory when they return (DiffusionKernel2D.cpp:159-171).  The resident
+ *     calls (set_field / run_ticks / get_field) keep the field in device
+ *     memory between calls; run_ticks only enqueues work on the handle's
+ *     stream, hal_cuda_*_sync waits for it.
+ *   - Arithmetic is FP32 on the device (as in the Vulkan backends); the
+ *     double-precision interface calls convert on the device.
+ *   - Dirichlet boundaries ("ghost tables"): the reference's boundary
+ *     callable bc(x, y) (PDEequations.h:50-98, ADIequations.h:339-378) is only
+ *     evaluated one cell outside the grid, so it is passed as a table of
+ *     2*yDim + 2*xDim values: [0, yDim) = bc(-1, y); [yDim, 2*yDim) =
+ *     bc(xDim, y); then xDim values bc(x, -1); then xDim values bc(x, yDim).
+ *     A NULL table selects the zero-flux form.  Wrapped axes ignore their
+ *     part of the table, as the reference does.
+ */
+#ifndef HAL_CUDA_H
+#define HAL_CUDA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HAL_CUDA_OK 0
+#define HAL_CUDA_EINVAL 1   /* bad argument or size mismatch */
+#define HAL_CUDA_ENOMEM 2   /* device or pinned-host allocation failed */
+#define HAL_CUDA_EDEVICE 3  /* CUDA runtime error, no device, launch failure */
+#define HAL_CUDA_ETIMEOUT 4 /* a bounded device-side wait gave up */
+#define HAL_CUDA_ENOTSUP 5  /* a size or mode this build does not handle */
+
+/* Longest line the ADI sweeps solve (the Vulkan AdiKernel2D caps lines at
+ * kMaxLine = 1024, AdiKernel2D.h:41). */
+#define HAL_CUDA_ADI_MAX_LINE 4096
+
+typedef struct hal_cuda_diffusion hal_cuda_diffusion; /* explicit stencil */
+typedef struct hal_cuda_adi hal_cuda_adi;             /* ADI (implicit) */
+typedef struct hal_cuda_agents hal_cuda_agents;       /* agent forces */
+
+/* ---- library ------------------------------------------------------------ */
+
+/* Version string of this library. */
+const char *hal_cuda_version(void);
+
+/* Message of the calling thread's most recent failed call ("" if none). */
+const char *hal_cuda_last_error(void);
+
+/* Number of visible CUDA devices; selects device `device` for handles created
+ * afterwards on this thread (default 0).  Replaces ComputeContext creation
+ * (include/Hal/Gpu/ComputeContext.h:18-49). */
+int hal_cuda_device_count(int32_t *count);
+int hal_cuda_set_device(int32_t device);
+
+/* Number of kernel launches this library has issued in this process (all
+ * handles).  Used by benchmarks to report their launch counts. */
+int64_t hal_cuda_launch_count(void);
+
+/* ---- explicit diffusion: IDiffusionBackend2D ---------------------------- */
+
+/* GpuDiffusionBackend2D(ComputeContext&, xDim, yDim)
+ * (include/Hal/Gpu/GpuDiffusionBackend2D.h:18-20). */
+int hal_cuda_diffusion_create(int32_t xDim, int32_t yDim, hal_cuda_diffusion **out);
+int hal_cuda_diffusion_destroy(hal_cuda_diffusion *h);
+
+/* IDiffusionBackend2D::Diffuse (IDiffusionBackend2D.h:26-32): deltas[i] +=
+ * diffRate * (sum of the four neighbour differences of field at i), zero-flux
+ * or periodic per axis.  field/deltas are host arrays of fieldLen/deltasLen
+ * doubles; EINVAL unless both equal xDim*yDim (Internal::CheckFieldSizes,
+ * src/Pde/IDiffusionBackend2D.cpp:20-33) and xDim/yDim equal the handle's. */
+int hal_cuda_diffuse(hal_cuda_diffusion *h, const double *field, int64_t fieldLen,
+                     double *deltas, int64_t deltasLen, double diffRate, int32_t xDim,
+                     int32_t yDim, int32_t wrapX, int32_t wrapY);
+
+/* Same with a Dirichlet ghost table (Internal::Diffusion2<BCFn>,
+ * PDEequations.h:264-287); ghost may be NULL (zero-flux). */
+int hal_cuda_diffuse_bc(hal_cuda_diffusion *h, const double *field, double *deltas,
+                        double diffRate, int32_t wrapX, int32_t wrapY, const double *ghost);
+
+/* Resident field (DiffusionKernel2D::UploadField / RunSteps,
+ * src/Gpu/DiffusionKernel2D.cpp:173-304).  len must be xDim*yDim. */
+int hal_cuda_diffusion_set_field(hal_cuda_diffusion *h, const float *field, int64_t len);
+int hal_cuda_diffusion_get_field(hal_cuda_diffusion *h, float *field, int64_t len);
+
+/* Per-tick terms of a HAL model tick on PDEGrid2D (PDEGrid2D.h:103-186):
+ * dense source field (len xDim*yDim, NULL clears it), point sources
+ * (cell index, value; nPoints 0 clears them), Dirichlet ghost table (NULL =
+ * zero-flux).  Stored on the device until changed. */
+int hal_cuda_diffusion_set_source(hal_cuda_diffusion *h, const float *dense, int64_t len);
+int hal_cuda_diffusion_set_point_sources(hal_cuda_diffusion *h, int32_t nPoints,
+                                         const int32_t *cells, const float *values);
+int hal_cuda_diffusion_set_dirichlet(hal_cuda_diffusion *h, const float *ghost);
+
+/* `ticks` fused ticks on the resident field, each
+ *   f' = f + diffRate*L_bc(f) - decay*f + src + points
+ * (PDEGrid2D::Diffusion + MulAll(-decay) + Add + Update).  EINVAL if
+ * diffRate > 0.25 (PDEGrid2D::CheckDiffusionStable, PDEGrid2D.h:436-442).
+ * Asynchronous on the handle's stream; a run of ticks is replayed from a
+ * CUDA graph. */
+int hal_cuda_diffusion_run_ticks(hal_cuda_diffusion *h, int32_t ticks, double diffRate,
+                                 double decay, int32_t wrapX, int32_t wrapY);
+
+/* DiffusionKernel2D::RunSteps(field, steps, diffRate, wrapX, wrapY)
+ * (src/Gpu/DiffusionKernel2D.cpp:244-304): upload, `steps` plain stencil
+ * steps with commit, download.  field is a host array of len floats. */
+int hal_cuda_diffusion_run_steps(hal_cuda_diffusion *h, float *field, int64_t len,
+                                 int32_t steps, double diffRate, int32_t wrapX, int32_t wrapY);
+
+/* Profiling: average device time (ms) of one fused-tick launch over `iters`
+ * individually timed ticks (CUDA events, no graph).  The field advances. */
+int hal_cuda_diffusion_profile(hal_cuda_diffusion *h, int32_t iters, double diffRate,
+                               double decay, int32_t wrapX, int32_t wrapY, float *ms);
+
+int hal_cuda_diffusion_sync(hal_cuda_diffusion *h);
+
+/* The handle's CUDA stream (a cudaStream_t), or replace it with the caller's
+ * (NULL restores the handle's own).  Resident calls run on this stream. */
+void *hal_cuda_diffusion_stream(hal_cuda_diffusion *h);
+int hal_cuda_diffusion_set_stream(hal_cuda_diffusion *h, void *stream);
+
+/* ---- ADI: IAdiDiffusionBackend2D --------------------------------------- */
+
+/* GpuAdiDiffusionBackend2D(ComputeContext&, xDim, yDim)
+ * (include/Hal/Gpu/GpuAdiDiffusionBackend2D.h); ENOTSUP if a side exceeds
+ * HAL_CUDA_ADI_MAX_LINE. */
+int hal_cuda_adi_create(int32_t xDim, int32_t yDim, hal_cuda_adi **out);
+int hal_cuda_adi_destroy(hal_cuda_adi *h);
+
+/* IAdiDiffusionBackend2D::DiffuseADI (IAdiDiffusionBackend2D.h:25-31):
+ * deltas[i] += v[i] - field[i], v = one ADI step of field
+ * (Internal::Diffusion2DADI, ADIequations.h:306-337).  Host double arrays;
+ * size checks as hal_cuda_diffuse. */
+int hal_cuda_diffuse_adi(hal_cuda_adi *h, const double *field, int64_t fieldLen,
+                         double *deltas, int64_t deltasLen, double diffRate, int32_t xDim,
+                         int32_t yDim, int32_t wrapX, int32_t wrapY);
+
+/* Same with a Dirichlet ghost table (Diffusion2DADI<BCFn>,
+ * ADIequations.h:339-378). */
+int hal_cuda_diffuse_adi_bc(hal_cuda_adi *h, const double *field, double *deltas,
+                            double diffRate, int32_t wrapX, int32_t wrapY, const double *ghost);
+
+/* Resident field and per-tick terms, as for the explicit handle. */
+int hal_cuda_adi_set_field(hal_cuda_adi *h, const float *field, int64_t len);
+int hal_cuda_adi_get_field(hal_cuda_adi *h, float *field, int64_t len);
+int hal_cuda_adi_set_source(hal_cuda_adi *h, const float *dense, int64_t len);
+int hal_cuda_adi_set_dirichlet(hal_cuda_adi *h, const float *ghost);
+
+/* Agent uptake coupling: every agent of `agents` (binned by its last
+ * dispatch) multiplies its cell by -uptake each tick, as a model's
+ * PDEGrid2D::Mul(cell, -uptake) per agent (PDEGrid2D.h:126-130).  The agent
+ * handle's grid must match.  agents NULL removes the coupling. */
+int hal_cuda_adi_set_uptake(hal_cuda_adi *h, hal_cuda_agents *agents, double uptake);
+
+/* `ticks` ADI ticks on the resident field, each
+ *   f' = ADI(f) - decay*f + src - uptake*count*f
+ * (PDEGrid2D::DiffusionADI + MulAll + Add + Mul + Update).  Asynchronous;
+ * replayed from a CUDA graph. */
+int hal_cuda_adi_run_ticks(hal_cuda_adi *h, int32_t ticks, double diffRate, double decay,
+                           int32_t wrapX, int32_t wrapY);
+
+/* AdiKernel2D::RunSteps(field, steps, diffRate, wrapX, wrapY)
+ * (src/Gpu/AdiKernel2D.cpp:296-364): upload, `steps` ADI steps, download. */
+int hal_cuda_adi_run_steps(hal_cuda_adi *h, float *field, int64_t len, int32_t steps,
+                           double diffRate, int32_t wrapX, int32_t wrapY);
+
+/* The same ticks as hal_cuda_adi_run_ticks, end to end from host memory:
+ * field and src (src may be NULL) are uploaded, `ticks` ticks run, the field
+ * is downloaded into `field`.  Synchronous. */
+int hal_cuda_adi_run_ticks_host(hal_cuda_adi *h, float *field, const float *src, int64_t len,
+                                int32_t ticks, double diffRate, double decay, int32_t wrapX,
+                                int32_t wrapY);
+
+/* Profiling: runs `iters` ticks with each sweep launched on its own between
+ * CUDA events on the handle's stream (no graph), and returns the average
+ * device time of one launch of each kernel: ms[0] = x-sweep
+ * (AdiColumnSweep), ms[1] = y-sweep with commit (AdiRowSweep).  The resident
+ * field advances by `iters` ticks. */
+int hal_cuda_adi_profile(hal_cuda_adi *h, int32_t iters, double diffRate, double decay,
+                         int32_t wrapX, int32_t wrapY, float *ms);
+
+int hal_cuda_adi_sync(hal_cuda_adi *h);
+void *hal_cuda_adi_stream(hal_cuda_adi *h);
+int hal_cuda_adi_set_stream(hal_cuda_adi *h, void *stream);
+
+/* ---- agent forces: IAgentForceBackend2D --------------------------------- */
+
+/* GpuAgentForceBackend2D(ComputeContext&, xDim, yDim, maxAgents)
+ * (src/Gpu/GpuAgentForceBackend2D.cpp:9-18). */
+int hal_cuda_agents_create(int32_t xDim, int32_t yDim, int32_t maxAgents,
+                           hal_cuda_agents **out);
+int hal_cuda_agents_destroy(hal_cuda_agents *h);
+
+/* IAgentForceBackend2D::AccumulateForces (IAgentForceBackend2D.h:28-36):
+ * positions (posLen = 2n doubles, x0 y0 x1 y1 ...), radii (radLen = n), out
+ * velocityDeltas (2n doubles, overwritten).  EINVAL unless posLen ==
+ * 2*radLen, xDim/yDim match the handle and n <= maxAgents
+ * (GpuAgentForceBackend2D.cpp:34-46).  Positions are rounded to float32 on
+ * the device, as the Vulkan backend does; binning follows the float32 values
+ * exactly (bit-exact with the CPU backend fed the same float32 values). */
+int hal_cuda_accumulate_forces(hal_cuda_agents *h, const double *positions, int64_t posLen,
+                               const double *radii, int64_t radLen, double *velocityDeltas,
+                               double interactionRad, double springConstant, int32_t xDim,
+                               int32_t yDim, int32_t wrapX, int32_t wrapY);
+
+/* Resident agents (AgentForceKernel2D::UploadAgents / Dispatch /
+ * DownloadVelocityDeltas, src/Gpu/AgentForceKernel2D.cpp:173-290). */
+int hal_cuda_agents_upload(hal_cuda_agents *h, const float *positions, const float *radii,
+                           int32_t n);
+int hal_cuda_agents_dispatch(hal_cuda_agents *h, double interactionRad, double springConstant,
+                             int32_t wrapX, int32_t wrapY);
+int hal_cuda_agents_download(hal_cuda_agents *h, float *velocityDeltas, int32_t n);
+
+/* The bins of the last dispatch: cellOffsets (xDim*yDim+1 int32, exclusive
+ * prefix of per-cell counts, cellOffsets[C] == n) and bucketAgents (n int32,
+ * agent indices grouped by cell, ascending within a cell) -- the scratch of
+ * CpuAgentForceBackend2D (src/Agents/CpuAgentForceBackend2D.cpp:85-109).
+ * Either pointer may be NULL. */
+int hal_cuda_agents_get_bins(hal_cuda_agents *h, int32_t *cellOffsets, int32_t *bucketAgents);
+
+/* Profiling: `iters` resident dispatches with each kernel launch between CUDA
+ * events; ms[0..5] = average device time of one launch of: bin count
+ * (including the counts memset), scan (three launches together), unstable
+ * scatter, stabilize, forces, and the whole dispatch. */
+int hal_cuda_agents_profile(hal_cuda_agents *h, int32_t iters, double interactionRad,
+                            double springConstant, int32_t wrapX, int32_t wrapY, float *ms);
+
+int hal_cuda_agents_sync(hal_cuda_agents *h);
+void *hal_cuda_agents_stream(hal_cuda_agents *h);
+int hal_cuda_agents_set_stream(hal_cuda_agents *h, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

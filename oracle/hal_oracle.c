@@ -1,0 +1,875 @@
+/*
+ * hal_oracle.c -- CPU oracle for the HAL-CPP hot path (TEST INFRASTRUCTURE).
+ *
+ * A plain-C restatement of the reference CPU backends.  Each function keeps
+ * the reference's loop order and floating-point expression order so that,
+ * compiled with -ffp-contract=off, the FP64 results are bit-identical to the
+ * reference's own CPU code (pinned against golden vectors made from it).
+ * Nothing in the product path may call this file.
+ */
+#include "hal_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* MathUtil.cpp:41-46 (Wrap) and :381-385 (InDim). */
+static int32_t o_wrap(int32_t val, int32_t max)
+{
+    int32_t mod = val % max;
+    return (mod < 0) ? (max + mod) : mod;
+}
+
+static int o_in_dim(int32_t val, int32_t dim)
+{
+    return (val >= 0) && (val < dim);
+}
+
+/* Ghost lookups for a Dirichlet callable evaluated just outside the grid. */
+static double o_ghost_x(const double *ghost, int32_t x, int32_t y, int32_t yDim)
+{
+    return (x < 0) ? ghost[y] : ghost[yDim + y];
+}
+
+static double o_ghost_y(const double *ghost, int32_t x, int32_t y, int32_t xDim,
+                        int32_t yDim)
+{
+    return (y < 0) ? ghost[2 * yDim + x] : ghost[2 * yDim + xDim + x];
+}
+
+/* DeltaX2D (src/Pde/PDEequations.cpp:24-41) and its Dirichlet form
+ * (include/Hal/Pde/PDEequations.h:50-69). */
+static double o_delta_x(const double *f, double c, int32_t x, int32_t y,
+                        int32_t xDim, int32_t yDim, int wrapX, const double *ghost)
+{
+    if (o_in_dim(x, xDim))
+    {
+        return f[x * yDim + y] - c;
+    }
+    if (wrapX)
+    {
+        return f[o_wrap(x, xDim) * yDim + y] - c;
+    }
+    if (ghost != NULL)
+    {
+        return (o_ghost_x(ghost, x, y, yDim) - c) * 2;
+    }
+    return 0;
+}
+
+/* DeltaY2D (src/Pde/PDEequations.cpp:43-60) and its Dirichlet form
+ * (include/Hal/Pde/PDEequations.h:79-98). */
+static double o_delta_y(const double *f, double c, int32_t x, int32_t y,
+                        int32_t xDim, int32_t yDim, int wrapY, const double *ghost)
+{
+    if (o_in_dim(y, yDim))
+    {
+        return f[x * yDim + y] - c;
+    }
+    if (wrapY)
+    {
+        return f[x * yDim + o_wrap(y, yDim)] - c;
+    }
+    if (ghost != NULL)
+    {
+        return (o_ghost_y(ghost, x, y, xDim, yDim) - c) * 2;
+    }
+    return 0;
+}
+
+void oracle_diffusion2_rows(const double *field, double *deltas, double diffRate,
+                            int32_t xDim, int32_t yDim, int wrapX, int wrapY,
+                            const double *ghost, int32_t x0, int32_t x1)
+{
+    /* src/Pde/PDEequations.cpp:148-160 */
+    for (int32_t x = x0; x < x1; x++)
+    {
+        for (int32_t y = 0; y < yDim; y++)
+        {
+            int32_t i = x * yDim + y;
+            double centerVal = field[i];
+            double deltaSum = o_delta_x(field, centerVal, x + 1, y, xDim, yDim, wrapX, ghost);
+            deltaSum += o_delta_x(field, centerVal, x - 1, y, xDim, yDim, wrapX, ghost);
+            deltaSum += o_delta_y(field, centerVal, x, y + 1, xDim, yDim, wrapY, ghost);
+            deltaSum += o_delta_y(field, centerVal, x, y - 1, xDim, yDim, wrapY, ghost);
+            deltas[i] += deltaSum * diffRate;
+        }
+    }
+}
+
+void oracle_diffusion2(const double *field, double *deltas, double diffRate,
+                       int32_t xDim, int32_t yDim, int wrapX, int wrapY,
+                       const double *ghost)
+{
+    oracle_diffusion2_rows(field, deltas, diffRate, xDim, yDim, wrapX, wrapY, ghost, 0, xDim);
+}
+
+/* ---- Thomas solver: include/Hal/Pde/TdmaSolver.h ------------------------ */
+
+typedef struct o_tdma
+{
+    double *as, *bs, *cs, *ws, *ds, *ys, *zs, *us;
+    int32_t len;
+} o_tdma;
+
+static int o_tdma_init(o_tdma *t, int32_t len)
+{
+    double *block = (double *)calloc((size_t)len * 8 + 8, sizeof(double));
+    if (block == NULL)
+    {
+        return -1;
+    }
+    t->as = block;
+    t->bs = t->as + len + 1;
+    t->cs = t->bs + len + 1;
+    t->ws = t->cs + len + 1;
+    t->ds = t->ws + len + 1;
+    t->ys = t->ds + len + 1;
+    t->zs = t->ys + len + 1;
+    t->us = t->zs + len + 1;
+    t->len = len;
+    return 0;
+}
+
+static void o_tdma_free(o_tdma *t)
+{
+    free(t->as);
+}
+
+/* The coefficient callables of ADISolveRow (ADIequations.h:225-270) and the
+ * adjusted diagonal of TDMAperiodic (TdmaSolver.h:84-95), as data. */
+typedef struct o_coeffs
+{
+    double offDiagonal;
+    double endAdjust;
+    int periodic;     /* diagonal is 1 - 2*offDiagonal everywhere */
+    int adjusted;     /* apply the Sherman-Morrison end adjustment */
+    double gamma, alpha, beta;
+    int32_t len;
+} o_coeffs;
+
+static double o_get_b_raw(const o_coeffs *k, int32_t i)
+{
+    if (k->periodic)
+    {
+        return 1 - 2 * k->offDiagonal;
+    }
+    double weight = 2.0;
+    if (i == 0)
+    {
+        weight += k->endAdjust;
+    }
+    if (i == (k->len - 1))
+    {
+        weight += k->endAdjust;
+    }
+    return 1 - weight * k->offDiagonal;
+}
+
+static double o_get_b(const o_coeffs *k, int32_t i)
+{
+    if (k->adjusted)
+    {
+        if (i == 0)
+        {
+            return o_get_b_raw(k, i) - k->gamma;
+        }
+        if (i == (k->len - 1))
+        {
+            return o_get_b_raw(k, i) - (k->alpha * k->beta) / k->gamma;
+        }
+    }
+    return o_get_b_raw(k, i);
+}
+
+/* TdmaSolver::TDMA (TdmaSolver.h:26-66).  rhs[i] plays getIn(i); the solution
+ * goes to out[i] in the order setOut is called (last to first). */
+static void o_tdma_solve(o_tdma *t, const o_coeffs *k, int32_t n, const double *rhs,
+                         double *out)
+{
+    double *as = t->as, *bs = t->bs, *cs = t->cs, *ws = t->ws, *ds = t->ds;
+    bs[0] = o_get_b(k, 0);
+    cs[0] = k->offDiagonal;
+    ds[0] = rhs[0];
+    for (int32_t i = 1; i < n; i++)
+    {
+        if (i < (n - 1))
+        {
+            cs[i] = k->offDiagonal;
+        }
+        bs[i] = o_get_b(k, i);
+        as[i] = k->offDiagonal;
+        ds[i] = rhs[i];
+        ws[i] = as[i] / bs[i - 1];
+        bs[i] = bs[i] - ws[i] * cs[i - 1];
+        ds[i] = ds[i] - ws[i] * ds[i - 1];
+    }
+    int32_t i = n - 1;
+    double x = ds[i] / bs[i];
+    out[i] = x;
+    for (i -= 1; i >= 0; i--)
+    {
+        x = (ds[i] - cs[i] * x) / bs[i];
+        out[i] = x;
+    }
+}
+
+/* ADISolveRow (ADIequations.h:225-270) with TDMA / TDMAperiodic
+ * (TdmaSolver.h:26-120).  rhs holds getIn(0..len-1); out receives setOut's
+ * values. */
+static void o_adi_solve_row(o_tdma *t, int32_t len, double diffRate, int wrapDim,
+                            int hasBC, const double *rhs, double *out)
+{
+    o_coeffs k;
+    memset(&k, 0, sizeof(k));
+    k.offDiagonal = -diffRate / 2.0;
+    k.len = len;
+    if (wrapDim)
+    {
+        k.periodic = 1;
+        /* TdmaSolver.h:80-82 */
+        const double gamma = -o_get_b(&k, 0);
+        const double alpha = k.offDiagonal;
+        const double beta = k.offDiagonal;
+        k.gamma = gamma;
+        k.alpha = alpha;
+        k.beta = beta;
+        k.adjusted = 1;
+        o_tdma_solve(t, &k, len, rhs, t->ys);
+        /* second right-hand side (TdmaSolver.h:102-110) */
+        for (int32_t i = 0; i < len; i++)
+        {
+            if (i == 0)
+            {
+                t->us[i] = gamma;
+            }
+            else if (i == (len - 1))
+            {
+                t->us[i] = alpha;
+            }
+            else
+            {
+                t->us[i] = 0.0;
+            }
+        }
+        o_tdma_solve(t, &k, len, t->us, t->zs);
+        double vEnd = beta / gamma;
+        double vy = t->ys[0] + t->ys[len - 1] * vEnd;
+        double vz = t->zs[0] + t->zs[len - 1] * vEnd;
+        double factor = vy / (1 + vz);
+        for (int32_t i = 0; i < len; i++)
+        {
+            out[i] = t->ys[i] - factor * t->zs[i];
+        }
+        return;
+    }
+    k.endAdjust = hasBC ? 1.0 : -1.0;
+    o_tdma_solve(t, &k, len, rhs, out);
+}
+
+/* ExplicitDiffusionY2ADI (src/Pde/ADIequations.cpp:34-47, Dirichlet form
+ * ADIequations.h:79-94). */
+static double o_explicit_y2(int32_t x, int32_t y, const double *f, double diffRate,
+                            int32_t xDim, int32_t yDim, int wrapY, const double *ghost)
+{
+    int32_t i = x * yDim + y;
+    double centerVal = f[i];
+    double deltaSum = o_delta_y(f, centerVal, x, y + 1, xDim, yDim, wrapY, ghost);
+    deltaSum += o_delta_y(f, centerVal, x, y - 1, xDim, yDim, wrapY, ghost);
+    return centerVal + (deltaSum * diffRate) / 2;
+}
+
+/* ExplicitDiffusionX2ADI (src/Pde/ADIequations.cpp:19-32, Dirichlet form
+ * ADIequations.h:54-69). */
+static double o_explicit_x2(int32_t x, int32_t y, const double *f, double diffRate,
+                            int32_t xDim, int32_t yDim, int wrapX, const double *ghost)
+{
+    int32_t i = x * yDim + y;
+    double centerVal = f[i];
+    double deltaSum = o_delta_x(f, centerVal, x + 1, y, xDim, yDim, wrapX, ghost);
+    deltaSum += o_delta_x(f, centerVal, x - 1, y, xDim, yDim, wrapX, ghost);
+    return centerVal + (deltaSum * diffRate) / 2;
+}
+
+/* ImplicitBoundarySource (ADIequations.h:198-220) with diffScaleFactor 2. */
+static double o_implicit_source(int32_t i, int32_t len, int wrap, double diffRate,
+                                double lowVal, double highVal)
+{
+    if (wrap)
+    {
+        return 0.0;
+    }
+    double source = 0.0;
+    if (i == 0)
+    {
+        source += lowVal;
+    }
+    if (i == (len - 1))
+    {
+        source += highVal;
+    }
+    return source * 2.0 * diffRate / 2.0;
+}
+
+/* x-sweep lines y in [y0, y1) (ADIequations.h:316-324 / :351-362). */
+static void o_adi_xsweep(o_tdma *t, double *rhs, double *out, const double *field,
+                         double *scratch, double diffRate, int32_t xDim, int32_t yDim,
+                         int wrapX, int wrapY, const double *ghost, int32_t y0, int32_t y1)
+{
+    for (int32_t y = y0; y < y1; y++)
+    {
+        for (int32_t i = 0; i < xDim; i++)
+        {
+            if (ghost == NULL)
+            {
+                rhs[i] = o_explicit_y2(i, y, field, diffRate, xDim, yDim, wrapY, NULL);
+            }
+            else
+            {
+                rhs[i] = o_explicit_y2(i, y, field, diffRate, xDim, yDim, wrapY, ghost) +
+                         o_implicit_source(i, xDim, wrapX, diffRate, ghost[y], ghost[yDim + y]);
+            }
+        }
+        o_adi_solve_row(t, xDim, diffRate, wrapX, ghost != NULL, rhs, out);
+        for (int32_t i = 0; i < xDim; i++)
+        {
+            scratch[i * yDim + y] = out[i];
+        }
+    }
+}
+
+/* y-sweep lines x in [x0, x1) (ADIequations.h:325-336 / :363-377). */
+static void o_adi_ysweep(o_tdma *t, double *rhs, double *out, const double *field,
+                         const double *scratch, double *deltas, double diffRate,
+                         int32_t xDim, int32_t yDim, int wrapX, int wrapY,
+                         const double *ghost, int32_t x0, int32_t x1)
+{
+    for (int32_t x = x0; x < x1; x++)
+    {
+        for (int32_t i = 0; i < yDim; i++)
+        {
+            if (ghost == NULL)
+            {
+                rhs[i] = o_explicit_x2(x, i, scratch, diffRate, xDim, yDim, wrapX, NULL);
+            }
+            else
+            {
+                rhs[i] = o_explicit_x2(x, i, scratch, diffRate, xDim, yDim, wrapX, ghost) +
+                         o_implicit_source(i, yDim, wrapY, diffRate, ghost[2 * yDim + x],
+                                           ghost[2 * yDim + xDim + x]);
+            }
+        }
+        o_adi_solve_row(t, yDim, diffRate, wrapY, ghost != NULL, rhs, out);
+        for (int32_t i = 0; i < yDim; i++)
+        {
+            int32_t index = x * yDim + i;
+            deltas[index] += out[i] - field[index];
+        }
+    }
+}
+
+void oracle_adi2(const double *field, double *scratch, double *deltas,
+                 double diffRate, int32_t xDim, int32_t yDim, int wrapX,
+                 int wrapY, const double *ghost)
+{
+    oracle_adi2_mt(field, scratch, deltas, diffRate, xDim, yDim, wrapX, wrapY, ghost, 1);
+}
+
+typedef struct o_adi_job
+{
+    const double *field;
+    double *scratch, *deltas;
+    double diffRate;
+    int32_t xDim, yDim;
+    int wrapX, wrapY;
+    const double *ghost;
+    int32_t lo, hi;
+    int sweep; /* 0 = x-sweep, 1 = y-sweep */
+} o_adi_job;
+
+static void *o_adi_worker(void *arg)
+{
+    o_adi_job *j = (o_adi_job *)arg;
+    int32_t len = (j->xDim > j->yDim) ? j->xDim : j->yDim;
+    o_tdma t;
+    if (o_tdma_init(&t, len) != 0)
+    {
+        return NULL;
+    }
+    double *rhs = (double *)calloc((size_t)len, sizeof(double));
+    double *out = (double *)calloc((size_t)len, sizeof(double));
+    if (j->sweep == 0)
+    {
+        o_adi_xsweep(&t, rhs, out, j->field, j->scratch, j->diffRate, j->xDim, j->yDim,
+                     j->wrapX, j->wrapY, j->ghost, j->lo, j->hi);
+    }
+    else
+    {
+        o_adi_ysweep(&t, rhs, out, j->field, j->scratch, j->deltas, j->diffRate, j->xDim,
+                     j->yDim, j->wrapX, j->wrapY, j->ghost, j->lo, j->hi);
+    }
+    free(rhs);
+    free(out);
+    o_tdma_free(&t);
+    return NULL;
+}
+
+static void o_run_sweep(o_adi_job *base, int sweep, int32_t lines, int nthreads)
+{
+    if (nthreads < 1)
+    {
+        nthreads = 1;
+    }
+    if (nthreads > lines)
+    {
+        nthreads = lines;
+    }
+    if (nthreads <= 1)
+    {
+        o_adi_job j = *base;
+        j.sweep = sweep;
+        j.lo = 0;
+        j.hi = lines;
+        o_adi_worker(&j);
+        return;
+    }
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)nthreads);
+    o_adi_job *jobs = (o_adi_job *)malloc(sizeof(o_adi_job) * (size_t)nthreads);
+    for (int k = 0; k < nthreads; k++)
+    {
+        jobs[k] = *base;
+        jobs[k].sweep = sweep;
+        jobs[k].lo = (int32_t)(((int64_t)lines * k) / nthreads);
+        jobs[k].hi = (int32_t)(((int64_t)lines * (k + 1)) / nthreads);
+        pthread_create(&th[k], NULL, o_adi_worker, &jobs[k]);
+    }
+    for (int k = 0; k < nthreads; k++)
+    {
+        pthread_join(th[k], NULL);
+    }
+    free(th);
+    free(jobs);
+}
+
+void oracle_adi2_mt(const double *field, double *scratch, double *deltas,
+                    double diffRate, int32_t xDim, int32_t yDim, int wrapX,
+                    int wrapY, const double *ghost, int nthreads)
+{
+    o_adi_job base;
+    base.field = field;
+    base.scratch = scratch;
+    base.deltas = deltas;
+    base.diffRate = diffRate;
+    base.xDim = xDim;
+    base.yDim = yDim;
+    base.wrapX = wrapX;
+    base.wrapY = wrapY;
+    base.ghost = ghost;
+    /* all x-sweep lines complete before any y-sweep line starts, as in the
+     * two consecutive loops of Diffusion2DADI */
+    o_run_sweep(&base, 0, yDim, nthreads);
+    o_run_sweep(&base, 1, xDim, nthreads);
+}
+
+/* ---- explicit stencil, threaded rows (baseline only) --------------------- */
+
+typedef struct o_rows_job
+{
+    const double *field;
+    double *deltas;
+    double diffRate;
+    int32_t xDim, yDim;
+    int wrapX, wrapY;
+    const double *ghost;
+    int32_t lo, hi;
+} o_rows_job;
+
+static void *o_rows_worker(void *arg)
+{
+    o_rows_job *j = (o_rows_job *)arg;
+    oracle_diffusion2_rows(j->field, j->deltas, j->diffRate, j->xDim, j->yDim, j->wrapX,
+                           j->wrapY, j->ghost, j->lo, j->hi);
+    return NULL;
+}
+
+static void o_diffusion2_mt(const double *field, double *deltas, double diffRate,
+                            int32_t xDim, int32_t yDim, int wrapX, int wrapY,
+                            const double *ghost, int nthreads)
+{
+    if (nthreads > xDim)
+    {
+        nthreads = xDim;
+    }
+    if (nthreads <= 1)
+    {
+        oracle_diffusion2(field, deltas, diffRate, xDim, yDim, wrapX, wrapY, ghost);
+        return;
+    }
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)nthreads);
+    o_rows_job *jobs = (o_rows_job *)malloc(sizeof(o_rows_job) * (size_t)nthreads);
+    for (int k = 0; k < nthreads; k++)
+    {
+        o_rows_job j = {field, deltas, diffRate, xDim, yDim, wrapX, wrapY, ghost,
+                        (int32_t)(((int64_t)xDim * k) / nthreads),
+                        (int32_t)(((int64_t)xDim * (k + 1)) / nthreads)};
+        jobs[k] = j;
+        pthread_create(&th[k], NULL, o_rows_worker, &jobs[k]);
+    }
+    for (int k = 0; k < nthreads; k++)
+    {
+        pthread_join(th[k], NULL);
+    }
+    free(th);
+    free(jobs);
+}
+
+/* ---- PDEGrid2D tick -------------------------------------------------- */
+
+int oracle_tick(int mode, double *field, double *deltas, double *scratch,
+                int32_t xDim, int32_t yDim, double diffRate, int wrapX,
+                int wrapY, const double *ghost, double decay,
+                const double *srcDense, int32_t nSrc, const int32_t *srcIdx,
+                const double *srcVal, const int32_t *uptakeCount,
+                double uptake, int nthreads)
+{
+    int32_t length = xDim * yDim;
+    if (mode == 0)
+    {
+        /* PDEGrid2D::CheckDiffusionStable (PDEGrid2D.h:436-442) */
+        if (diffRate > 0.25)
+        {
+            return -1;
+        }
+        o_diffusion2_mt(field, deltas, diffRate, xDim, yDim, wrapX, wrapY, ghost, nthreads);
+    }
+    else
+    {
+        oracle_adi2_mt(field, scratch, deltas, diffRate, xDim, yDim, wrapX, wrapY, ghost,
+                       nthreads);
+    }
+    if (decay != 0.0)
+    {
+        /* MulAll(-decay) -> Mul(i, val): deltas[i] += field[i] * val (:126-130) */
+        double val = -decay;
+        for (int32_t i = 0; i < length; i++)
+        {
+            deltas[i] += field[i] * val;
+        }
+    }
+    if (srcDense != NULL)
+    {
+        for (int32_t i = 0; i < length; i++)
+        {
+            deltas[i] += srcDense[i];
+        }
+    }
+    for (int32_t k = 0; k < nSrc; k++)
+    {
+        deltas[srcIdx[k]] += srcVal[k];
+    }
+    if (uptakeCount != NULL)
+    {
+        double val = -uptake;
+        for (int32_t i = 0; i < length; i++)
+        {
+            for (int32_t a = 0; a < uptakeCount[i]; a++)
+            {
+                deltas[i] += field[i] * val;
+            }
+        }
+    }
+    /* Update() (:178-186) */
+    for (int32_t i = 0; i < length; i++)
+    {
+        field[i] += deltas[i];
+    }
+    memset(deltas, 0, sizeof(double) * (size_t)length);
+    return 0;
+}
+
+/* ---- agents: src/Agents/CpuAgentForceBackend2D.cpp ------------------------ */
+
+/* AgentForceCellCoord (:14-27) */
+static int32_t o_cell_coord(double v, int32_t dim)
+{
+    int32_t c = (int32_t)floor(v);
+    if (c < 0)
+    {
+        c = 0;
+    }
+    else if (c >= dim)
+    {
+        c = dim - 1;
+    }
+    return c;
+}
+
+/* AgentForceDisp (:30-45) */
+static double o_disp(double a, double b, int32_t dim, int wrap)
+{
+    double d = b - a;
+    if (wrap)
+    {
+        double dimF = (double)dim;
+        if (fabs(d) > (dimF * 0.5))
+        {
+            d = (a > b) ? (d + dimF) : (d - dimF);
+        }
+    }
+    return d;
+}
+
+/* AgentForceWrapIndex (:47-52) */
+static int32_t o_wrap_index(int32_t v, int32_t dim)
+{
+    int32_t m = v % dim;
+    return (m < 0) ? (m + dim) : m;
+}
+
+void oracle_agent_bins(const double *positions, int32_t n, int32_t xDim,
+                       int32_t yDim, int32_t *cellOffsets, int32_t *bucketAgents)
+{
+    int32_t numCells = xDim * yDim;
+    memset(cellOffsets, 0, sizeof(int32_t) * ((size_t)numCells + 1));
+    for (int32_t i = 0; i < n; i++)
+    {
+        int32_t cellX = o_cell_coord(positions[(size_t)i * 2], xDim);
+        int32_t cellY = o_cell_coord(positions[(size_t)i * 2 + 1], yDim);
+        cellOffsets[(size_t)(cellX * yDim + cellY) + 1]++;
+    }
+    for (int32_t c = 0; c < numCells; c++)
+    {
+        cellOffsets[(size_t)c + 1] += cellOffsets[(size_t)c];
+    }
+    int32_t *cursors = (int32_t *)malloc(sizeof(int32_t) * ((size_t)numCells + 1));
+    memcpy(cursors, cellOffsets, sizeof(int32_t) * (size_t)numCells);
+    for (int32_t i = 0; i < n; i++)
+    {
+        int32_t cellX = o_cell_coord(positions[(size_t)i * 2], xDim);
+        int32_t cellY = o_cell_coord(positions[(size_t)i * 2 + 1], yDim);
+        int32_t cell = cellX * yDim + cellY;
+        bucketAgents[cursors[cell]] = i;
+        cursors[cell]++;
+    }
+    free(cursors);
+}
+
+void oracle_agent_forces(const double *positions, const double *radii,
+                         int32_t n, double interactionRad, double springConstant,
+                         int32_t xDim, int32_t yDim, int wrapX, int wrapY,
+                         const int32_t *cellOffsets, const int32_t *bucketAgents,
+                         double *velocityDeltas, int32_t i0, int32_t i1)
+{
+    (void)n;
+    for (int32_t i = i0; i < i1; i++)
+    {
+        double posX = positions[(size_t)i * 2];
+        double posY = positions[(size_t)i * 2 + 1];
+        double rad = radii[i];
+
+        int32_t xStart = (int32_t)floor(posX - interactionRad);
+        int32_t xEnd = (int32_t)ceil(posX + interactionRad);
+        int32_t yStart = (int32_t)floor(posY - interactionRad);
+        int32_t yEnd = (int32_t)ceil(posY + interactionRad);
+
+        double velDeltaX = 0.0;
+        double velDeltaY = 0.0;
+        for (int32_t xSq = xStart; xSq < xEnd; xSq++)
+        {
+            int32_t retX = xSq;
+            int inX = (retX >= 0) && (retX < xDim);
+            if (!wrapX && !inX)
+            {
+                continue;
+            }
+            if (wrapX && !inX)
+            {
+                retX = o_wrap_index(retX, xDim);
+            }
+            for (int32_t ySq = yStart; ySq < yEnd; ySq++)
+            {
+                int32_t retY = ySq;
+                int inY = (retY >= 0) && (retY < yDim);
+                if (!wrapY && !inY)
+                {
+                    continue;
+                }
+                if (wrapY && !inY)
+                {
+                    retY = o_wrap_index(retY, yDim);
+                }
+                int32_t cell = retX * yDim + retY;
+                int32_t start = cellOffsets[cell];
+                int32_t end = cellOffsets[cell + 1];
+                for (int32_t k = start; k < end; k++)
+                {
+                    int32_t j = bucketAgents[k];
+                    if (j == i)
+                    {
+                        continue;
+                    }
+                    double xComp = o_disp(posX, positions[(size_t)j * 2], xDim, wrapX);
+                    double yComp = o_disp(posY, positions[(size_t)j * 2 + 1], yDim, wrapY);
+                    double dist = sqrt((xComp * xComp) + (yComp * yComp));
+                    if ((dist < interactionRad) && (dist > 0.0))
+                    {
+                        double touchDist = (rad + radii[j]) - dist;
+                        double force = springConstant * touchDist;
+                        velDeltaX -= (xComp / dist) * force;
+                        velDeltaY -= (yComp / dist) * force;
+                    }
+                }
+            }
+        }
+        velocityDeltas[(size_t)i * 2] = velDeltaX;
+        velocityDeltas[(size_t)i * 2 + 1] = velDeltaY;
+    }
+}
+
+typedef struct o_force_job
+{
+    const double *positions, *radii;
+    int32_t n;
+    double R, k;
+    int32_t xDim, yDim;
+    int wrapX, wrapY;
+    const int32_t *offsets, *bucket;
+    double *out;
+    int32_t lo, hi;
+} o_force_job;
+
+static void *o_force_worker(void *arg)
+{
+    o_force_job *j = (o_force_job *)arg;
+    oracle_agent_forces(j->positions, j->radii, j->n, j->R, j->k, j->xDim, j->yDim,
+                        j->wrapX, j->wrapY, j->offsets, j->bucket, j->out, j->lo, j->hi);
+    return NULL;
+}
+
+int oracle_accumulate_forces(const double *positions, const double *radii,
+                             int32_t n, double *velocityDeltas,
+                             double interactionRad, double springConstant,
+                             int32_t xDim, int32_t yDim, int wrapX, int wrapY,
+                             int32_t *cellOffsets, int32_t *bucketAgents,
+                             int nthreads)
+{
+    oracle_agent_bins(positions, n, xDim, yDim, cellOffsets, bucketAgents);
+    if (nthreads > n)
+    {
+        nthreads = n;
+    }
+    if (nthreads <= 1)
+    {
+        oracle_agent_forces(positions, radii, n, interactionRad, springConstant, xDim, yDim,
+                            wrapX, wrapY, cellOffsets, bucketAgents, velocityDeltas, 0, n);
+        return 0;
+    }
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)nthreads);
+    o_force_job *jobs = (o_force_job *)malloc(sizeof(o_force_job) * (size_t)nthreads);
+    for (int t = 0; t < nthreads; t++)
+    {
+        o_force_job j = {positions, radii, n, interactionRad, springConstant, xDim, yDim,
+                         wrapX, wrapY, cellOffsets, bucketAgents, velocityDeltas,
+                         (int32_t)(((int64_t)n * t) / nthreads),
+                         (int32_t)(((int64_t)n * (t + 1)) / nthreads)};
+        jobs[t] = j;
+        pthread_create(&th[t], NULL, o_force_worker, &jobs[t]);
+    }
+    for (int t = 0; t < nthreads; t++)
+    {
+        pthread_join(th[t], NULL);
+    }
+    free(th);
+    free(jobs);
+    return 0;
+}
+
+/* ---- Hal::Rng (src/Rng.cpp) and the polar Gaussian -------------------- */
+
+/* SplitMix64Next (src/Rng.cpp:61-68) */
+static uint64_t o_splitmix(uint64_t *state)
+{
+    *state += 0x9E3779B97F4A7C15ULL;
+    uint64_t z = *state;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+static uint64_t o_rotl(uint64_t x, int k)
+{
+    return (x << k) | (x >> (64 - k));
+}
+
+void oracle_rand_init(oracle_rand *r, uint64_t seed)
+{
+    /* Rng::Rng(uint64_t) (src/Rng.cpp:85-93) */
+    uint64_t st = seed;
+    r->s[0] = o_splitmix(&st);
+    r->s[1] = o_splitmix(&st);
+    r->s[2] = o_splitmix(&st);
+    r->s[3] = o_splitmix(&st);
+    r->v1 = 0;
+    r->v2 = 0;
+    r->sq = 0;
+    r->phase = 0;
+}
+
+uint64_t oracle_rand_next(oracle_rand *r)
+{
+    /* xoshiro256** step (src/Rng.cpp:104-117) */
+    const uint64_t result = o_rotl(r->s[1] * 5, 7) * 9;
+    const uint64_t t = r->s[1] << 17;
+    r->s[2] ^= r->s[0];
+    r->s[3] ^= r->s[1];
+    r->s[1] ^= r->s[2];
+    r->s[0] ^= r->s[3];
+    r->s[2] ^= t;
+    r->s[3] = o_rotl(r->s[3], 45);
+    return result;
+}
+
+double oracle_rand_double(oracle_rand *r)
+{
+    /* Rng::NextDouble (src/Rng.cpp:139-144) */
+    const uint64_t mantissaBits = oracle_rand_next(r) >> 11;
+    return (double)mantissaBits * (1.0 / 9007199254740992.0);
+}
+
+int32_t oracle_rand_int(oracle_rand *r, int32_t bound)
+{
+    /* Rng::BoundedUint64 / NextInt (src/Rng.cpp:119-137) */
+    uint64_t b = (uint64_t)bound;
+    const uint64_t threshold = (~b + 1) % b;
+    uint64_t v = oracle_rand_next(r);
+    while (v < threshold)
+    {
+        v = oracle_rand_next(r);
+    }
+    return (int32_t)(v % b);
+}
+
+double oracle_rand_gaussian(oracle_rand *r, double mean, double stdDev)
+{
+    /* GaussianSampler::Sample (src/GaussianSampler.cpp:23-47) */
+    double x;
+    if (r->phase == 0)
+    {
+        do
+        {
+            double u1 = oracle_rand_double(r);
+            double u2 = oracle_rand_double(r);
+            r->v1 = 2 * u1 - 1;
+            r->v2 = 2 * u2 - 1;
+            r->sq = r->v1 * r->v1 + r->v2 * r->v2;
+        } while ((r->sq >= 1) || (r->sq == 0));
+        x = r->v1 * sqrt(-2 * log(r->sq) / r->sq);
+    }
+    else
+    {
+        x = r->v2 * sqrt(-2 * log(r->sq) / r->sq);
+    }
+    r->phase = 1 - r->phase;
+    return x * stdDev + mean;
+}

@@ -1,0 +1,133 @@
+/*
+ * hal_oracle.h -- CPU oracle for the HAL-CPP per-tick hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
+ * CPU backends (explicit stencil, ADI/Thomas, cell-bucket agent forces and the
+ * PDEGrid2D tick semantics).  It exists to check the CUDA path: only the test
+ * suite, the smoke check and the CPU-baseline leg of the benchmark may load
+ * it, never the product path.
+ *
+ * Every function follows the reference file:line named beside it, operation
+ * for operation (same loop order, same floating-point expression order), so
+ * that with -ffp-contract=off it reproduces the reference's FP64 results bit
+ * for bit.  Parity is pinned by tests/test_oracle_pin.py against golden
+ * vectors generated from the reference's own CPU code (tests/golden/).
+ *
+ * Layout everywhere: row-major i = x*yDim + y (y contiguous), as in
+ * Hal::PDEGrid2D.
+ *
+ * Dirichlet "ghost" arrays: a boundary callable bc(x, y) of the reference is
+ * only ever evaluated one cell outside the grid, so it is passed as a table
+ * of 2*yDim + 2*xDim values:
+ *   ghost[y]                    = bc(-1,   y)   (x below the grid)
+ *   ghost[yDim + y]             = bc(xDim, y)   (x above the grid)
+ *   ghost[2*yDim + x]           = bc(x, -1)     (y below the grid)
+ *   ghost[2*yDim + xDim + x]    = bc(x, yDim)   (y above the grid)
+ * A NULL ghost table means the zero-flux form of the stencil.
+ */
+#ifndef HAL_ORACLE_H
+#define HAL_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- explicit 5-point stencil -------------------------------------------- */
+
+/* Internal::Diffusion2 (src/Pde/PDEequations.cpp:140-161) and, with a ghost
+ * table, Internal::Diffusion2<BCFn> (include/Hal/Pde/PDEequations.h:264-287):
+ * deltas[i] += diffRate * sum of the four neighbour differences. */
+void oracle_diffusion2(const double *field, double *deltas, double diffRate,
+                       int32_t xDim, int32_t yDim, int wrapX, int wrapY,
+                       const double *ghost);
+
+/* Same stencil, rows [x0, x1) only (used by the multi-threaded baseline). */
+void oracle_diffusion2_rows(const double *field, double *deltas, double diffRate,
+                            int32_t xDim, int32_t yDim, int wrapX, int wrapY,
+                            const double *ghost, int32_t x0, int32_t x1);
+
+/* ---- ADI -------------------------------------------------------------- */
+
+/* Internal::Diffusion2DADI (include/Hal/Pde/ADIequations.h:306-337) and, with
+ * a ghost table, its Dirichlet form (:339-378).  scratch holds xDim*yDim
+ * doubles.  deltas[i] += v - field[i]. */
+void oracle_adi2(const double *field, double *scratch, double *deltas,
+                 double diffRate, int32_t xDim, int32_t yDim, int wrapX,
+                 int wrapY, const double *ghost);
+
+/* Multi-threaded form of oracle_adi2 (lines split over nthreads POSIX
+ * threads; each line is solved exactly as in oracle_adi2, so the result is
+ * identical).  Used only as the CPU baseline. */
+void oracle_adi2_mt(const double *field, double *scratch, double *deltas,
+                    double diffRate, int32_t xDim, int32_t yDim, int wrapX,
+                    int wrapY, const double *ghost, int nthreads);
+
+/* ---- PDEGrid2D tick (include/Hal/Grids/PDEGrid2D.h) --------------------- */
+
+/* One model tick as a HAL model writes it:
+ *   Diffusion(diffRate[, bc]) or DiffusionADI(diffRate[, bc])  (:289-347)
+ *   MulAll(-decay)                                             (:212-218)
+ *   Add(i, srcDense[i]) for every cell (if srcDense)           (:110-114)
+ *   Add(srcIdx[k], srcVal[k]) for k < nSrc                     (:110-114)
+ *   Mul(cell, -uptake) once per agent in the cell (uptakeCount)(:126-130)
+ *   Update()                                                   (:178-186)
+ * field is updated in place; deltas (xDim*yDim, zeroed on entry and on exit)
+ * and scratch (ADI only) are work arrays.  mode 0 = explicit, 1 = ADI.
+ * Returns 0, or -1 for an explicit rate above 0.25 (CheckDiffusionStable,
+ * :436-442). */
+int oracle_tick(int mode, double *field, double *deltas, double *scratch,
+                int32_t xDim, int32_t yDim, double diffRate, int wrapX,
+                int wrapY, const double *ghost, double decay,
+                const double *srcDense, int32_t nSrc, const int32_t *srcIdx,
+                const double *srcVal, const int32_t *uptakeCount,
+                double uptake, int nthreads);
+
+/* ---- cell-bucket agent forces (src/Agents/CpuAgentForceBackend2D.cpp) ---- */
+
+/* Passes 1-3 (:85-109): counts -> exclusive offsets (numCells+1 entries,
+ * offsets[numCells] == n) and the stable scatter of agent indices. */
+void oracle_agent_bins(const double *positions, int32_t n, int32_t xDim,
+                       int32_t yDim, int32_t *cellOffsets, int32_t *bucketAgents);
+
+/* Pass 4 (:111-175) for agents [i0, i1): velocityDeltas[2i], [2i+1]
+ * overwritten with the summed linear-spring response. */
+void oracle_agent_forces(const double *positions, const double *radii,
+                         int32_t n, double interactionRad, double springConstant,
+                         int32_t xDim, int32_t yDim, int wrapX, int wrapY,
+                         const int32_t *cellOffsets, const int32_t *bucketAgents,
+                         double *velocityDeltas, int32_t i0, int32_t i1);
+
+/* CpuAgentForceBackend2D::AccumulateForces (:66-176) end to end.  Scratch
+ * cellOffsets (xDim*yDim+1) and bucketAgents (n) are caller-provided.  Pass 4
+ * is split over nthreads threads (identical result).  Returns 0. */
+int oracle_accumulate_forces(const double *positions, const double *radii,
+                             int32_t n, double *velocityDeltas,
+                             double interactionRad, double springConstant,
+                             int32_t xDim, int32_t yDim, int wrapX, int wrapY,
+                             int32_t *cellOffsets, int32_t *bucketAgents,
+                             int nthreads);
+
+/* ---- Hal::Rng / Hal::Rand (src/Rng.cpp, src/Rand.cpp) ----------------------
+ * xoshiro256** seeded through splitmix64, plus the Marsaglia polar Gaussian
+ * (src/GaussianSampler.cpp:23-47).  Used to rebuild the seeded scenes of the
+ * reference's own tests. */
+typedef struct oracle_rand
+{
+    uint64_t s[4];
+    double v1, v2, sq;
+    int phase;
+} oracle_rand;
+
+void oracle_rand_init(oracle_rand *r, uint64_t seed);
+uint64_t oracle_rand_next(oracle_rand *r);
+double oracle_rand_double(oracle_rand *r);
+int32_t oracle_rand_int(oracle_rand *r, int32_t bound);
+double oracle_rand_gaussian(oracle_rand *r, double mean, double stdDev);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

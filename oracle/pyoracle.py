@@ -1,0 +1,292 @@
+"""ctypes bindings for the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Two libraries are wrapped:
+
+* ``liboracle.so`` -- the plain-C restatement of the reference CPU path
+  (``hal_oracle.c``).  It builds anywhere gcc does and is what the GPU tests,
+  the smoke check and the benchmark's CPU-baseline leg compare against.
+* ``_ref/libhal_ref.so`` -- the reference's own CPU sources plus
+  ``ref_shim.cpp``.  It exists only where the reference tree is present and is
+  used to pin the restatement and to write the golden vectors.
+
+Only ``tests/``, ``__graft_entry__.smoke`` and ``bench.py``'s CPU-baseline
+leg may import this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libhal_ref.so")
+REF_TREE = "/root/reference"
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int32)
+
+
+def build(ref: bool = False) -> None:
+    """Compile liboracle.so (and, when the reference tree exists and ``ref``,
+    the reference library)."""
+    subprocess.run(["make", "-s", "liboracle.so"], cwd=HERE, check=True)
+    if ref and os.path.isdir(REF_TREE):
+        subprocess.run(["make", "-s", "-j8", "ref", f"REF={REF_TREE}"], cwd=HERE, check=True)
+
+
+def _ptr(a, kind=_dp):
+    if a is None:
+        return None
+    return a.ctypes.data_as(kind)
+
+
+def _f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.int32)
+
+
+class _Lib:
+    _lib = None
+    path = ORACLE_SO
+
+    @classmethod
+    def lib(cls):
+        if cls._lib is None:
+            if not os.path.exists(cls.path):
+                raise FileNotFoundError(cls.path)
+            cls._lib = ctypes.CDLL(cls.path)
+            cls._setup(cls._lib)
+        return cls._lib
+
+
+class Oracle(_Lib):
+    """The C restatement."""
+
+    path = ORACLE_SO
+
+    @staticmethod
+    def _setup(L):
+        i32, f64, vp = ctypes.c_int32, ctypes.c_double, ctypes.c_void_p
+        L.oracle_diffusion2.argtypes = [vp, vp, f64, i32, i32, ctypes.c_int, ctypes.c_int, vp]
+        L.oracle_adi2.argtypes = [vp, vp, vp, f64, i32, i32, ctypes.c_int, ctypes.c_int, vp]
+        L.oracle_adi2_mt.argtypes = [vp, vp, vp, f64, i32, i32, ctypes.c_int, ctypes.c_int, vp,
+                                     ctypes.c_int]
+        L.oracle_tick.argtypes = [ctypes.c_int, vp, vp, vp, i32, i32, f64, ctypes.c_int,
+                                  ctypes.c_int, vp, f64, vp, i32, vp, vp, vp, f64, ctypes.c_int]
+        L.oracle_tick.restype = ctypes.c_int
+        L.oracle_agent_bins.argtypes = [vp, i32, i32, i32, vp, vp]
+        L.oracle_accumulate_forces.argtypes = [vp, vp, i32, vp, f64, f64, i32, i32, ctypes.c_int,
+                                               ctypes.c_int, vp, vp, ctypes.c_int]
+        L.oracle_accumulate_forces.restype = ctypes.c_int
+        L.oracle_rand_init.argtypes = [vp, ctypes.c_uint64]
+        L.oracle_rand_double.argtypes = [vp]
+        L.oracle_rand_double.restype = f64
+        L.oracle_rand_int.argtypes = [vp, i32]
+        L.oracle_rand_int.restype = i32
+        L.oracle_rand_gaussian.argtypes = [vp, f64, f64]
+        L.oracle_rand_gaussian.restype = f64
+
+    # -- explicit / ADI ----------------------------------------------------
+    @classmethod
+    def diffuse(cls, field, deltas, r, xDim, yDim, wrapX, wrapY, ghost=None):
+        """deltas += r * L(field) (in place on a float64 copy, returned)."""
+        f = _f64(field)
+        d = _f64(deltas).copy()
+        g = _f64(ghost)
+        cls.lib().oracle_diffusion2(f.ctypes.data, d.ctypes.data, r, xDim, yDim, int(wrapX),
+                                    int(wrapY), None if g is None else g.ctypes.data)
+        return d
+
+    @classmethod
+    def diffuse_adi(cls, field, deltas, r, xDim, yDim, wrapX, wrapY, ghost=None, threads=1):
+        f = _f64(field)
+        d = _f64(deltas).copy()
+        g = _f64(ghost)
+        s = np.zeros_like(f)
+        cls.lib().oracle_adi2_mt(f.ctypes.data, s.ctypes.data, d.ctypes.data, r, xDim, yDim,
+                                 int(wrapX), int(wrapY), None if g is None else g.ctypes.data,
+                                 int(threads))
+        return d
+
+    @classmethod
+    def run_ticks(cls, mode, field, xDim, yDim, r, wrapX=False, wrapY=False, ghost=None,
+                  decay=0.0, src_dense=None, src_idx=None, src_val=None, uptake_count=None,
+                  uptake=0.0, ticks=1, threads=1):
+        """Run ``ticks`` PDEGrid2D ticks (mode 0 explicit, 1 ADI); returns the
+        final field (float64)."""
+        f = _f64(field).copy()
+        n = xDim * yDim
+        d = np.zeros(n, dtype=np.float64)
+        s = np.zeros(n, dtype=np.float64)
+        g = _f64(ghost)
+        sd = _f64(src_dense)
+        si = _i32(src_idx)
+        sv = _f64(src_val)
+        uc = _i32(uptake_count)
+        ns = 0 if si is None else len(si)
+        L = cls.lib()
+        for _ in range(ticks):
+            rc = L.oracle_tick(mode, f.ctypes.data, d.ctypes.data, s.ctypes.data, xDim, yDim, r,
+                               int(wrapX), int(wrapY), None if g is None else g.ctypes.data,
+                               decay, None if sd is None else sd.ctypes.data, ns,
+                               None if si is None else si.ctypes.data,
+                               None if sv is None else sv.ctypes.data,
+                               None if uc is None else uc.ctypes.data, uptake, int(threads))
+            if rc != 0:
+                raise ValueError("Diffusion rate above stable maximum value of 0.25")
+        return f
+
+    # -- agents ------------------------------------------------------------
+    @classmethod
+    def accumulate_forces(cls, positions, radii, R, k, xDim, yDim, wrapX, wrapY, threads=1):
+        """Returns (velocityDeltas[2n], cellOffsets[C+1], bucketAgents[n])."""
+        p = _f64(positions)
+        rad = _f64(radii)
+        n = len(rad)
+        if len(p) != 2 * n:
+            raise ValueError("positions must hold two values per radius")
+        out = np.zeros(2 * n, dtype=np.float64)
+        off = np.zeros(xDim * yDim + 1, dtype=np.int32)
+        bucket = np.zeros(max(n, 1), dtype=np.int32)
+        cls.lib().oracle_accumulate_forces(p.ctypes.data, rad.ctypes.data, n, out.ctypes.data, R,
+                                           k, xDim, yDim, int(wrapX), int(wrapY),
+                                           off.ctypes.data, bucket.ctypes.data, int(threads))
+        return out, off, bucket[:n]
+
+    @classmethod
+    def agent_bins(cls, positions, xDim, yDim):
+        p = _f64(positions)
+        n = len(p) // 2
+        off = np.zeros(xDim * yDim + 1, dtype=np.int32)
+        bucket = np.zeros(max(n, 1), dtype=np.int32)
+        cls.lib().oracle_agent_bins(p.ctypes.data, n, xDim, yDim, off.ctypes.data,
+                                    bucket.ctypes.data)
+        return off, bucket[:n]
+
+    # -- Hal::Rand -----------------------------------------------------------
+    @classmethod
+    def rand_draws(cls, seed, kind, n, bound=1):
+        st = (ctypes.c_byte * 128)()
+        L = cls.lib()
+        L.oracle_rand_init(ctypes.addressof(st), seed)
+        out = np.zeros(n, dtype=np.float64)
+        for i in range(n):
+            if kind == 0:
+                out[i] = L.oracle_rand_double(ctypes.addressof(st))
+            elif kind == 1:
+                out[i] = L.oracle_rand_int(ctypes.addressof(st), bound)
+            else:
+                out[i] = L.oracle_rand_gaussian(ctypes.addressof(st), 0.0, 1.0)
+        return out
+
+
+class Reference(_Lib):
+    """The reference's own CPU code (only where the reference tree was built)."""
+
+    path = REF_SO
+
+    @classmethod
+    def available(cls):
+        return os.path.exists(REF_SO)
+
+    @staticmethod
+    def _setup(L):
+        i32, i64, f64, vp, ci = (ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p,
+                                 ctypes.c_int)
+        L.ref_diffuse.argtypes = [vp, i64, vp, i64, f64, i32, i32, ci, ci]
+        L.ref_diffuse_bc.argtypes = [vp, vp, f64, i32, i32, ci, ci, vp]
+        L.ref_diffuse_adi.argtypes = [vp, i64, vp, i64, f64, i32, i32, ci, ci]
+        L.ref_diffuse_adi_bc.argtypes = [vp, vp, f64, i32, i32, ci, ci, vp]
+        L.ref_pdegrid_run.argtypes = [ci, vp, i32, i32, ci, ci, f64, vp, f64, vp, i32, vp, vp, vp,
+                                      f64, i32]
+        L.ref_accumulate_forces.argtypes = [vp, i64, vp, i64, vp, f64, f64, i32, i32, ci, ci, vp,
+                                            vp]
+        L.ref_rand_draws.argtypes = [ctypes.c_uint64, ci, i32, i32, vp]
+        for name in ("ref_diffuse", "ref_diffuse_bc", "ref_diffuse_adi", "ref_diffuse_adi_bc",
+                     "ref_pdegrid_run", "ref_accumulate_forces"):
+            getattr(L, name).restype = ci
+
+    @classmethod
+    def diffuse(cls, field, deltas, r, xDim, yDim, wrapX, wrapY, ghost=None):
+        f = _f64(field)
+        d = _f64(deltas).copy()
+        L = cls.lib()
+        if ghost is None:
+            rc = L.ref_diffuse(f.ctypes.data, len(f), d.ctypes.data, len(d), r, xDim, yDim,
+                               int(wrapX), int(wrapY))
+        else:
+            g = _f64(ghost)
+            rc = L.ref_diffuse_bc(f.ctypes.data, d.ctypes.data, r, xDim, yDim, int(wrapX),
+                                  int(wrapY), g.ctypes.data)
+        if rc == 1:
+            raise ValueError("invalid_argument")
+        if rc != 0:
+            raise RuntimeError("reference error")
+        return d
+
+    @classmethod
+    def diffuse_adi(cls, field, deltas, r, xDim, yDim, wrapX, wrapY, ghost=None):
+        f = _f64(field)
+        d = _f64(deltas).copy()
+        L = cls.lib()
+        if ghost is None:
+            rc = L.ref_diffuse_adi(f.ctypes.data, len(f), d.ctypes.data, len(d), r, xDim, yDim,
+                                   int(wrapX), int(wrapY))
+        else:
+            g = _f64(ghost)
+            rc = L.ref_diffuse_adi_bc(f.ctypes.data, d.ctypes.data, r, xDim, yDim, int(wrapX),
+                                      int(wrapY), g.ctypes.data)
+        if rc == 1:
+            raise ValueError("invalid_argument")
+        if rc != 0:
+            raise RuntimeError("reference error")
+        return d
+
+    @classmethod
+    def run_ticks(cls, mode, field, xDim, yDim, r, wrapX=False, wrapY=False, ghost=None,
+                  decay=0.0, src_dense=None, src_idx=None, src_val=None, uptake_count=None,
+                  uptake=0.0, ticks=1):
+        f = _f64(field).copy()
+        g, sd, si, sv, uc = _f64(ghost), _f64(src_dense), _i32(src_idx), _f64(src_val), \
+            _i32(uptake_count)
+        ns = 0 if si is None else len(si)
+        rc = cls.lib().ref_pdegrid_run(mode, f.ctypes.data, xDim, yDim, int(wrapX), int(wrapY),
+                                       r, None if g is None else g.ctypes.data, decay,
+                                       None if sd is None else sd.ctypes.data, ns,
+                                       None if si is None else si.ctypes.data,
+                                       None if sv is None else sv.ctypes.data,
+                                       None if uc is None else uc.ctypes.data, uptake, ticks)
+        if rc == 1:
+            raise ValueError("invalid_argument")
+        if rc != 0:
+            raise RuntimeError("reference error")
+        return f
+
+    @classmethod
+    def accumulate_forces(cls, positions, radii, R, k, xDim, yDim, wrapX, wrapY):
+        p = _f64(positions)
+        rad = _f64(radii)
+        n = len(rad)
+        out = np.zeros(len(p), dtype=np.float64)
+        off = np.zeros(xDim * yDim + 1, dtype=np.int32)
+        bucket = np.zeros(max(n, 1), dtype=np.int32)
+        rc = cls.lib().ref_accumulate_forces(p.ctypes.data, len(p), rad.ctypes.data, n,
+                                             out.ctypes.data, R, k, xDim, yDim, int(wrapX),
+                                             int(wrapY), off.ctypes.data, bucket.ctypes.data)
+        if rc == 1:
+            raise ValueError("invalid_argument")
+        if rc != 0:
+            raise RuntimeError("reference error")
+        return out, off, bucket[:n]
+
+    @classmethod
+    def rand_draws(cls, seed, kind, n, bound=1):
+        out = np.zeros(n, dtype=np.float64)
+        cls.lib().ref_rand_draws(seed, kind, bound, n, out.ctypes.data)
+        return out

@@ -1,0 +1,261 @@
+// ref_shim.cpp -- C entry points over the reference's own CPU code.
+//
+// TEST INFRASTRUCTURE ONLY.  Compiled (by oracle/Makefile) together with the
+// reference's CPU sources, read in place from the reference tree, into
+// oracle/_ref/libhal_ref.so.  It lets the golden-vector generator
+// (tests/golden/make_golden.py) and the oracle pin tests run the reference
+// itself: Hal::CpuDiffusionBackend2D, Hal::CpuAdiDiffusionBackend2D,
+// Hal::CpuAgentForceBackend2D, Hal::PDEGrid2D and Hal::Rand.  Nothing here is
+// part of the product.
+#include "Hal/Grids/PDEGrid2D.h"
+#include "Hal/Pde/ADIequations.h"
+#include "Hal/Pde/CpuAdiDiffusionBackend2D.h"
+#include "Hal/Pde/CpuDiffusionBackend2D.h"
+#include "Hal/Pde/PDEequations.h"
+#include "Hal/Pde/TdmaSolver.h"
+#include "Hal/Rand.h"
+#include "Hal/Log/Logger.h"
+
+// The bins of CpuAgentForceBackend2D are private members; the golden vectors
+// for the bit-exact binning check read them straight after AccumulateForces.
+#define private public
+#include "Hal/Agents/CpuAgentForceBackend2D.h"
+#undef private
+
+#include <cstdint>
+#include <cstring>
+#include <stdexcept>
+#include <vector>
+
+namespace
+{
+    // A Dirichlet callable backed by the ghost table layout of hal_oracle.h.
+    struct GhostBc
+    {
+        const double *pGhost;
+        int32_t xDim;
+        int32_t yDim;
+
+        double operator()(int32_t x, int32_t y) const
+        {
+            if (x < 0)
+            {
+                return pGhost[y];
+            }
+            if (x >= xDim)
+            {
+                return pGhost[yDim + y];
+            }
+            if (y < 0)
+            {
+                return pGhost[2 * yDim + x];
+            }
+            return pGhost[2 * yDim + xDim + x];
+        }
+    };
+
+    template <typename Fn>
+    int Guard(Fn fn)
+    {
+        try
+        {
+            fn();
+            return 0;
+        }
+        catch (const std::invalid_argument &)
+        {
+            return 1;
+        }
+        catch (...)
+        {
+            return 2;
+        }
+    }
+
+    void Quiet()
+    {
+        static bool s_done = false;
+        if (!s_done)
+        {
+            // Error-path tests provoke logged errors on purpose.
+            Hal::Logger::Instance().SetMinSeverity(Hal::LogSeverity::Error);
+            s_done = true;
+        }
+    }
+}
+
+extern "C"
+{
+    // IDiffusionBackend2D::Diffuse through Hal::CpuDiffusionBackend2D.
+    int ref_diffuse(const double *field, int64_t fieldLen, double *deltas, int64_t deltasLen,
+                    double diffRate, int32_t xDim, int32_t yDim, int wrapX, int wrapY)
+    {
+        Quiet();
+        return Guard([&]()
+                     {
+            std::vector<double> f(field, field + fieldLen);
+            std::vector<double> d(deltas, deltas + deltasLen);
+            Hal::CpuDiffusionBackend2D backend;
+            backend.Diffuse(f, d, diffRate, xDim, yDim, wrapX != 0, wrapY != 0);
+            std::memcpy(deltas, d.data(), sizeof(double) * d.size()); });
+    }
+
+    // Hal::Internal::Diffusion2<BCFn> with a ghost-table callable.
+    int ref_diffuse_bc(const double *field, double *deltas, double diffRate, int32_t xDim,
+                       int32_t yDim, int wrapX, int wrapY, const double *ghost)
+    {
+        Quiet();
+        return Guard([&]()
+                     { Hal::Internal::Diffusion2(field, deltas, diffRate, xDim, yDim, wrapX != 0, wrapY != 0,
+                                                 GhostBc{ghost, xDim, yDim}); });
+    }
+
+    // IAdiDiffusionBackend2D::DiffuseADI through Hal::CpuAdiDiffusionBackend2D.
+    int ref_diffuse_adi(const double *field, int64_t fieldLen, double *deltas, int64_t deltasLen,
+                        double diffRate, int32_t xDim, int32_t yDim, int wrapX, int wrapY)
+    {
+        Quiet();
+        return Guard([&]()
+                     {
+            std::vector<double> f(field, field + fieldLen);
+            std::vector<double> d(deltas, deltas + deltasLen);
+            Hal::CpuAdiDiffusionBackend2D backend;
+            backend.DiffuseADI(f, d, diffRate, xDim, yDim, wrapX != 0, wrapY != 0);
+            std::memcpy(deltas, d.data(), sizeof(double) * d.size()); });
+    }
+
+    // Hal::Internal::Diffusion2DADI<BCFn> with a ghost-table callable.
+    int ref_diffuse_adi_bc(const double *field, double *deltas, double diffRate, int32_t xDim,
+                           int32_t yDim, int wrapX, int wrapY, const double *ghost)
+    {
+        Quiet();
+        return Guard([&]()
+                     {
+            std::vector<double> scratch(static_cast<size_t>(xDim) * static_cast<size_t>(yDim), 0.0);
+            Hal::TdmaSolver tdma(xDim > yDim ? xDim : yDim);
+            Hal::Internal::Diffusion2DADI(field, scratch.data(), deltas, diffRate, xDim, yDim, wrapX != 0,
+                                          wrapY != 0, GhostBc{ghost, xDim, yDim}, tdma); });
+    }
+
+    // A HAL model's tick loop on Hal::PDEGrid2D: mode 0 = Diffusion, 1 =
+    // DiffusionADI; then MulAll(-decay), Add(dense), Add(points),
+    // Mul(cell,-uptake) per agent, Update().  field is updated in place.
+    int ref_pdegrid_run(int mode, double *field, int32_t xDim, int32_t yDim, int wrapX, int wrapY,
+                        double diffRate, const double *ghost, double decay, const double *srcDense,
+                        int32_t nSrc, const int32_t *srcIdx, const double *srcVal,
+                        const int32_t *uptakeCount, double uptake, int32_t ticks)
+    {
+        Quiet();
+        return Guard([&]()
+                     {
+            Hal::PDEGrid2D grid(xDim, yDim, wrapX != 0, wrapY != 0);
+            int32_t length = xDim * yDim;
+            std::vector<double> f(field, field + length);
+            std::vector<double> zeros(static_cast<size_t>(length), 0.0);
+            grid.SetState(f, zeros, 0);
+            GhostBc bc{ghost, xDim, yDim};
+            for (int32_t t = 0; t < ticks; t++)
+            {
+                if (mode == 0)
+                {
+                    if (ghost != nullptr)
+                    {
+                        grid.Diffusion(diffRate, bc);
+                    }
+                    else
+                    {
+                        grid.Diffusion(diffRate);
+                    }
+                }
+                else
+                {
+                    if (ghost != nullptr)
+                    {
+                        grid.DiffusionADI(diffRate, bc);
+                    }
+                    else
+                    {
+                        grid.DiffusionADI(diffRate);
+                    }
+                }
+                if (decay != 0.0)
+                {
+                    grid.MulAll(-decay);
+                }
+                if (srcDense != nullptr)
+                {
+                    for (int32_t i = 0; i < length; i++)
+                    {
+                        grid.Add(i, srcDense[i]);
+                    }
+                }
+                for (int32_t k = 0; k < nSrc; k++)
+                {
+                    grid.Add(srcIdx[k], srcVal[k]);
+                }
+                if (uptakeCount != nullptr)
+                {
+                    for (int32_t i = 0; i < length; i++)
+                    {
+                        for (int32_t a = 0; a < uptakeCount[i]; a++)
+                        {
+                            grid.Mul(i, -uptake);
+                        }
+                    }
+                }
+                grid.Update();
+            }
+            std::memcpy(field, grid.GetField().data(), sizeof(double) * static_cast<size_t>(length)); });
+    }
+
+    // IAgentForceBackend2D::AccumulateForces through
+    // Hal::CpuAgentForceBackend2D; also returns its bins.  cellOffsets holds
+    // xDim*yDim+1 entries and bucketAgents n entries (either may be null).
+    int ref_accumulate_forces(const double *positions, int64_t posLen, const double *radii,
+                              int64_t radLen, double *velocityDeltas, double interactionRad,
+                              double springConstant, int32_t xDim, int32_t yDim, int wrapX, int wrapY,
+                              int32_t *cellOffsets, int32_t *bucketAgents)
+    {
+        Quiet();
+        return Guard([&]()
+                     {
+            std::vector<double> p(positions, positions + posLen);
+            std::vector<double> r(radii, radii + radLen);
+            std::vector<double> out;
+            Hal::CpuAgentForceBackend2D backend;
+            backend.AccumulateForces(p, r, out, interactionRad, springConstant, xDim, yDim, wrapX != 0,
+                                     wrapY != 0);
+            std::memcpy(velocityDeltas, out.data(), sizeof(double) * out.size());
+            if (cellOffsets != nullptr)
+            {
+                std::memcpy(cellOffsets, backend.m_cellOffsets.data(),
+                            sizeof(int32_t) * backend.m_cellOffsets.size());
+            }
+            if (bucketAgents != nullptr)
+            {
+                std::memcpy(bucketAgents, backend.m_bucketAgents.data(),
+                            sizeof(int32_t) * backend.m_bucketAgents.size());
+            } });
+    }
+
+    // Hal::Rand draws: kind 0 = Double(), 1 = Int(bound), 2 = Gaussian(0, 1).
+    void ref_rand_draws(uint64_t seed, int kind, int32_t bound, int32_t n, double *out)
+    {
+        Hal::Rand rand(seed);
+        for (int32_t i = 0; i < n; i++)
+        {
+            if (kind == 0)
+            {
+                out[i] = rand.Double();
+            }
+            else if (kind == 1)
+            {
+                out[i] = static_cast<double>(rand.Int(bound));
+            }
+            else
+            {
+                out[i] = rand.Gaussian(0.0, 1.0);
+            }
+        }
+    }
+}

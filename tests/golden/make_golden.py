@@ -1,0 +1,196 @@
+"""Writes the golden vectors in this folder from the reference's own CPU code.
+
+Run in a tree where the reference sources exist (it builds
+``oracle/_ref/libhal_ref.so`` from them through ``oracle/Makefile``):
+
+    python tests/golden/make_golden.py
+
+Every output comes from Hal::CpuDiffusionBackend2D, Hal::CpuAdiDiffusionBackend2D,
+Hal::CpuAgentForceBackend2D, Hal::PDEGrid2D or Hal::Rand, called through
+``oracle/ref_shim.cpp``.  The inputs are stored beside the outputs, so the
+fixtures need no random generator to be replayed.  Cases restate the
+reference's own tests (eigenmode decay, the seed-1234 agent scene, Dirichlet
+fixed points) plus random odd-sized and edge-case grids.
+"""
+from __future__ import annotations
+
+import math
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import pyoracle  # noqa: E402
+from pyoracle import Reference as R  # noqa: E402
+
+SIZES = [(17, 29), (1, 7), (7, 1), (1, 1), (2, 2), (3, 5), (9, 40), (40, 9)]
+BIG = [(33, 64, 0, 0, 0), (64, 33, 1, 1, 1), (33, 64, 1, 0, 1)]
+
+
+def _eigen(nx, ny):
+    x = np.arange(nx)[:, None]
+    y = np.arange(ny)[None, :]
+    return (np.sin(2.0 * math.pi * x / nx) * np.sin(2.0 * math.pi * y / ny)).ravel()
+
+
+def stencil_cases(rng):
+    out = {}
+    k = 0
+    for (xd, yd) in SIZES:
+        for wx in (0, 1):
+            for wy in (0, 1):
+                for use_bc in (0, 1):
+                    f = rng.random(xd * yd)
+                    d = rng.random(xd * yd) - 0.5
+                    g = rng.random(2 * (xd + yd)) if use_bc else None
+                    r_exp = 0.2
+                    r_adi = [0.3, 5.0][k % 2]
+                    out[f"c{k}_dims"] = np.array([xd, yd, wx, wy, use_bc], dtype=np.int32)
+                    out[f"c{k}_rates"] = np.array([r_exp, r_adi])
+                    out[f"c{k}_field"] = f
+                    out[f"c{k}_deltas"] = d
+                    if use_bc:
+                        out[f"c{k}_ghost"] = g
+                    out[f"c{k}_explicit"] = R.diffuse(f, d, r_exp, xd, yd, wx, wy, g)
+                    out[f"c{k}_adi"] = R.diffuse_adi(f, d, r_adi, xd, yd, wx, wy, g)
+                    k += 1
+    for (xd, yd, wx, wy, use_bc) in BIG:
+        f = rng.random(xd * yd)
+        d = np.zeros(xd * yd)
+        g = rng.random(2 * (xd + yd)) if use_bc else None
+        out[f"c{k}_dims"] = np.array([xd, yd, wx, wy, use_bc], dtype=np.int32)
+        out[f"c{k}_rates"] = np.array([0.25, 10.0])
+        out[f"c{k}_field"] = f
+        out[f"c{k}_deltas"] = d
+        if use_bc:
+            out[f"c{k}_ghost"] = g
+        out[f"c{k}_explicit"] = R.diffuse(f, d, 0.25, xd, yd, wx, wy, g)
+        out[f"c{k}_adi"] = R.diffuse_adi(f, d, 10.0, xd, yd, wx, wy, g)
+        k += 1
+    out["count"] = np.array([k])
+    # the reference's own interface tests (tests/IDiffusionBackend2DTests.cpp:23-113)
+    f = _eigen(16, 20)
+    out["eig_explicit_field"] = f
+    out["eig_explicit_out"] = R.diffuse(f, np.zeros_like(f), 0.05, 16, 20, 1, 1)
+    f = _eigen(12, 18)
+    out["eig_adi_field"] = f
+    out["eig_adi_out"] = R.diffuse_adi(f, np.zeros_like(f), 0.3, 12, 18, 1, 1)
+    return out
+
+
+def tick_cases(rng):
+    out = {}
+    # Explicit PDEGrid2D tick with a Dirichlet edge, decay and point sources
+    # (the shape of the 256x256 explicit workload, scaled down).
+    xd, yd = 32, 40
+    f = rng.random(xd * yd)
+    ghost = np.zeros(2 * (xd + yd))
+    ghost[:yd] = 1.0  # bc(-1, y) = 1, every other edge 0
+    sites = rng.choice(xd * yd, 12, replace=False).astype(np.int32)
+    vals = np.full(12, 0.05)
+    out["exp_field"] = f
+    out["exp_ghost"] = ghost
+    out["exp_src_idx"] = sites
+    out["exp_src_val"] = vals
+    out["exp_params"] = np.array([xd, yd, 0.2, 0.001, 150])
+    out["exp_out"] = R.run_ticks(0, f, xd, yd, 0.2, False, False, ghost, 0.001, None, sites,
+                                 vals, ticks=150)
+    # ADI tick with decay and a dense source (the 2048^2 ADI workload, scaled down)
+    xd, yd = 40, 48
+    f = rng.random(xd * yd)
+    src = rng.random(xd * yd) * 0.01
+    out["adi_field"] = f
+    out["adi_src"] = src
+    out["adi_params"] = np.array([xd, yd, 5.0, 0.01, 20])
+    out["adi_out"] = R.run_ticks(1, f, xd, yd, 5.0, False, False, None, 0.01, src, ticks=20)
+    # ADI tick with periodic x, Dirichlet y ends, and agent uptake counts
+    xd, yd = 21, 30
+    f = rng.random(xd * yd)
+    ghost = rng.random(2 * (xd + yd))
+    counts = rng.integers(0, 4, xd * yd).astype(np.int32)
+    out["cpl_field"] = f
+    out["cpl_ghost"] = ghost
+    out["cpl_counts"] = counts
+    out["cpl_params"] = np.array([xd, yd, 1.7, 0.005, 0.001, 9])
+    out["cpl_out"] = R.run_ticks(1, f, xd, yd, 1.7, True, False, ghost, 0.005, None, None, None,
+                                 counts, 0.001, ticks=9)
+    # the ADI GPU-vs-CPU case of tests/AdiKernel2DTests.cpp:70-141
+    nx, ny = 20, 14
+    x = np.arange(nx)[:, None]
+    y = np.arange(ny)[None, :]
+    f = (1.0 + 0.3 * x - 0.2 * y + 0.5 * np.sin(0.7 * x * y)).ravel()
+    out["kat_adi_field"] = f
+    out["kat_adi_out"] = R.run_ticks(1, f, nx, ny, 0.6, False, False, ticks=5)
+    return out
+
+
+def agent_cases(rng):
+    out = {}
+    # The seed-1234 scene of tests/IAgentForceBackend2DTests.cpp:25-37:
+    # Rand(1234); x = Double(16), y = Double(16), radius = 0.4 + Double(0.4).
+    u = R.rand_draws(1234, 0, 180)
+    pos = np.empty(120)
+    pos[0::2] = u[0::3] * 16.0
+    pos[1::2] = u[1::3] * 16.0
+    rad = 0.4 + u[2::3] * 0.4
+    v, off, b = R.accumulate_forces(pos, rad, 3.0, 0.4, 16, 16, 1, 1)
+    out.update(s1234_pos=pos, s1234_rad=rad, s1234_vel=v, s1234_off=off, s1234_bucket=b)
+    # float32 positions, walls, a dense cluster plus stragglers outside the domain
+    cases = [
+        ("walls", 64, 48, 3000, 0, 0, 1.0, 0.1),
+        ("torus", 37, 23, 1500, 1, 1, 1.0, 0.1),
+        ("mixed", 30, 50, 2000, 1, 0, 2.3, 0.3),
+        ("tiny", 1, 1, 5, 0, 0, 1.0, 0.1),
+        ("empty", 8, 8, 0, 0, 0, 2.0, 1.0),
+    ]
+    for (name, xd, yd, n, wx, wy, R_, k) in cases:
+        m = int(n * 0.3)
+        uni = rng.random((n - m, 2)) * np.array([xd, yd]) * 1.1 - 0.05 * np.array([xd, yd])
+        clu = rng.normal(0.0, 1.0, (m, 2)) * np.array([xd, yd]) * 0.08 + \
+            np.array([xd, yd]) * 0.4
+        p = np.concatenate([uni, clu]).astype(np.float32).astype(np.float64).ravel()
+        if n >= 4:
+            p[2:4] = p[0:2]  # two coincident agents
+        rad = np.full(n, 0.5)
+        v, off, b = R.accumulate_forces(p, rad, R_, k, xd, yd, wx, wy)
+        out[f"{name}_pos"] = p
+        out[f"{name}_rad"] = rad
+        out[f"{name}_params"] = np.array([xd, yd, n, wx, wy, R_, k])
+        out[f"{name}_vel"] = v
+        out[f"{name}_off"] = off
+        out[f"{name}_bucket"] = b
+    # coincident-agent no-NaN case (tests/IAgentForceBackend2DTests.cpp:153-165)
+    v, off, b = R.accumulate_forces([4.0, 4.0, 4.0, 4.0], [0.5, 0.5], 2.0, 1.0, 8, 8, 0, 0)
+    out["coincident_vel"] = v
+    return out
+
+
+def rand_cases():
+    out = {}
+    for seed in (1, 7, 1234):
+        out[f"double_{seed}"] = R.rand_draws(seed, 0, 64)
+        out[f"int256_{seed}"] = R.rand_draws(seed, 1, 64, 256)
+        out[f"gauss_{seed}"] = R.rand_draws(seed, 2, 64)
+    return out
+
+
+def main():
+    pyoracle.build(ref=True)
+    if not R.available():
+        raise SystemExit("the reference library could not be built (no reference tree?)")
+    rng = np.random.default_rng(20261203)
+    np.savez_compressed(os.path.join(HERE, "stencil.npz"), **stencil_cases(rng))
+    np.savez_compressed(os.path.join(HERE, "ticks.npz"), **tick_cases(rng))
+    np.savez_compressed(os.path.join(HERE, "agents.npz"), **agent_cases(rng))
+    np.savez_compressed(os.path.join(HERE, "rand.npz"), **rand_cases())
+    for name in ("stencil", "ticks", "agents", "rand"):
+        p = os.path.join(HERE, name + ".npz")
+        print(f"{p}: {os.path.getsize(p)} bytes")
+
+
+if __name__ == "__main__":
+    main()

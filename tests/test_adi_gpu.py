@@ -1,0 +1,191 @@
+"""ADI on the GPU (FP32) against the FP64 oracle and the golden vectors.
+
+Tolerance: the GPU solves in FP32 what the reference solves in FP64 by
+Thomas.  One step is held to max|err| <= TOL(r) * max|f| with
+TOL(r) = 2e-6 * (1 + r) (the line systems' condition number grows like
+1 + 2r); multi-step runs to rel-L2 <= 1e-5, the 2048^2 workload target.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import pytest
+
+from conftest import max_rel, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def TOL(r):
+    return 2e-6 * (1.0 + r)
+
+
+def _eigen(nx, ny):
+    x = np.arange(nx)[:, None]
+    y = np.arange(ny)[None, :]
+    return (np.sin(2.0 * math.pi * x / nx) * np.sin(2.0 * math.pi * y / ny)).ravel()
+
+
+def _lambda_cn(r, n, k=1):
+    s = math.sin(math.pi * k / n) ** 2
+    return (1.0 - 2.0 * r * s) / (1.0 + 2.0 * r * s)
+
+
+def _step_err(out, exp, f):
+    scale = max(np.abs(f).max(), np.abs(exp).max(), 1e-30)
+    return float(np.abs(out - exp).max() / scale)
+
+
+def test_diffuse_adi_golden(hal, golden):
+    g = golden("stencil")
+    for k in range(int(g["count"][0])):
+        xd, yd, wx, wy, use_bc = (int(v) for v in g[f"c{k}_dims"])
+        r = float(g[f"c{k}_rates"][1])
+        f = g[f"c{k}_field"]
+        with hal.Adi(xd, yd) as a:
+            if use_bc:
+                out = a.diffuse_adi_bc(f, g[f"c{k}_deltas"].copy(), r, wx, wy, g[f"c{k}_ghost"])
+            else:
+                out = a.diffuse_adi(f, g[f"c{k}_deltas"].copy(), r, xd, yd, wx, wy)
+        err = _step_err(out, g[f"c{k}_adi"], f)
+        assert err <= TOL(r), f"case {k}: {xd}x{yd} wrap {wx}{wy} bc {use_bc} r {r}: {err}"
+
+
+def test_adi_eigenmode_through_interface(hal):
+    """tests/IDiffusionBackend2DTests.cpp:115-144 (GPU epsilon 1e-4 there)."""
+    nx, ny, r = 12, 18, 0.3
+    f = _eigen(nx, ny)
+    lam = _lambda_cn(r, nx) * _lambda_cn(r, ny)
+    with hal.Adi(nx, ny) as a:
+        for _ in range(2):  # second call reuses the handle
+            out = a.diffuse_adi(f, np.zeros_like(f), r, nx, ny, True, True)
+            np.testing.assert_allclose(f + out, lam * f, rtol=0, atol=1e-5)
+
+
+def test_run_steps_cn_nth_power(hal):
+    """tests/AdiKernel2DTests.cpp:18-68: 24x16, r = 0.8, 50 steps (1e-3 there)."""
+    nx, ny, r, steps = 24, 16, 0.8, 50
+    f = _eigen(nx, ny)
+    lam = _lambda_cn(r, nx) * _lambda_cn(r, ny)
+    with hal.Adi(nx, ny) as a:
+        out = a.run_steps(f, steps, r, True, True)
+    np.testing.assert_allclose(out, lam ** steps * f, rtol=0, atol=1e-5)
+
+
+def test_zero_flux_mass_and_cpu_match(hal, golden):
+    """tests/AdiKernel2DTests.cpp:70-141: 20x14, r = 0.6, 5 steps, 1e-4 there."""
+    g = golden("ticks")
+    f = g["kat_adi_field"]
+    with hal.Adi(20, 14) as a:
+        out = a.run_steps(f, 5, 0.6, False, False)
+    assert abs(out.astype(np.float64).sum() - f.sum()) <= 1e-5 * f.sum()
+    assert max_rel(out, g["kat_adi_out"]) <= 1e-5
+
+
+def test_adi_tick_golden(hal, golden):
+    """ADI + decay + dense source, 40x48, r = 5, 20 ticks."""
+    g = golden("ticks")
+    xd, yd, r, decay, ticks = g["adi_params"]
+    with hal.Adi(int(xd), int(yd)) as a:
+        a.set_field(g["adi_field"])
+        a.set_source(g["adi_src"])
+        a.run_ticks(int(ticks), r, decay)
+        out = a.get_field()
+    assert rel_l2(out, g["adi_out"]) <= 1e-5
+
+
+def test_adi_tick_dirichlet_periodic_uptake_golden(hal, golden):
+    """Periodic x, Dirichlet y ends, per-agent uptake (counts from a binned
+    agent set): the coupled tick of the agent workload."""
+    g = golden("ticks")
+    xd, yd, r, decay, uptake, ticks = g["cpl_params"]
+    xd, yd = int(xd), int(yd)
+    counts = g["cpl_counts"]
+    # agents at the cell centres reproduce the per-cell counts
+    cells = np.repeat(np.arange(xd * yd), counts)
+    pos = np.empty(2 * cells.size, np.float32)
+    pos[0::2] = cells // yd + 0.5
+    pos[1::2] = cells % yd + 0.5
+    with hal.Agents(xd, yd, cells.size) as ag, hal.Adi(xd, yd) as a:
+        ag.upload(pos, np.full(cells.size, 0.5, np.float32))
+        ag.dispatch(1.0, 0.1)
+        ag.sync()
+        off, _ = ag.get_bins()
+        assert np.array_equal(np.diff(off), counts)
+        a.set_field(g["cpl_field"])
+        a.set_dirichlet(g["cpl_ghost"])
+        a.set_uptake(ag, uptake)
+        a.run_ticks(int(ticks), r, decay, True, False)
+        out = a.get_field()
+    assert rel_l2(out, g["cpl_out"]) <= 1e-5
+
+
+LINES = [1, 2, 3, 31, 32, 33, 63, 64, 65, 100, 257, 1000, 2048, 4096]
+
+
+@pytest.mark.parametrize("L", LINES)
+def test_line_lengths_against_oracle(hal, oracle, L):
+    """Every chunk layout: one chunk, partial last chunks, full clusters."""
+    rng = np.random.default_rng(L)
+    other = {1: 7, 2: 5, 3: 64, 4096: 3}.get(L, 37)
+    for (xd, yd) in ((L, other), (other, L)):
+        f = rng.random(xd * yd)
+        ghost = rng.random(2 * (xd + yd))
+        for r in (0.3, 5.0, 100.0):
+            for wx, wy, gh in ((False, False, None), (True, True, None), (True, False, ghost),
+                               (False, True, ghost)):
+                exp = oracle.diffuse_adi(f, np.zeros_like(f), r, xd, yd, wx, wy, gh)
+                with hal.Adi(xd, yd) as a:
+                    if gh is None:
+                        out = a.diffuse_adi(f, np.zeros_like(f), r, xd, yd, wx, wy)
+                    else:
+                        out = a.diffuse_adi_bc(f, np.zeros_like(f), r, wx, wy, gh)
+                err = _step_err(out, exp, f)
+                assert err <= TOL(r), (xd, yd, r, wx, wy, gh is None, err)
+
+
+def test_rejects_bad_sizes(hal):
+    with pytest.raises(RuntimeError):
+        hal.Adi(hal.ADI_MAX_LINE + 1, 8)
+    with hal.Adi(4, 4) as a:
+        with pytest.raises(ValueError):
+            a.run_steps(np.zeros(15, np.float32), 1, 0.1)
+        with pytest.raises(ValueError):
+            a.diffuse_adi(np.zeros(12), np.zeros(12), 0.1, 3, 4, False, False)
+        with pytest.raises(ValueError):
+            a.diffuse_adi(np.zeros(16), np.zeros(15), 0.1, 4, 4, False, False)
+
+
+def test_adi_2048_workload_200_ticks(hal, oracle):
+    """The 2048^2 ADI workload end to end: r = 5, decay 0.01, source field,
+    zero-flux, 200 ticks; FP32 on the GPU against FP64 Thomas (target
+    rel-L2 <= 1e-5)."""
+    from halcuda import workloads
+
+    w = workloads.adi_inputs(2048, seed=2)
+    exp = oracle.run_ticks(1, w["field"], 2048, 2048, w["diffRate"], decay=w["decay"],
+                           src_dense=w["src"], ticks=200, threads=16)
+    with hal.Adi(2048, 2048) as a:
+        a.set_field(w["field"])
+        a.set_source(w["src"])
+        a.run_ticks(200, w["diffRate"], w["decay"])
+        out = a.get_field()
+    e2 = rel_l2(out, exp)
+    print(f"2048^2 ADI 200 ticks: rel-L2 {e2:.3e} max-rel {max_rel(out, exp):.3e}")
+    assert e2 <= 1e-5
+
+
+def test_host_ticks_match_resident_ticks(hal):
+    from halcuda import workloads
+
+    w = workloads.adi_inputs(256, seed=4, blobs=20)
+    f32 = w["field"].astype(np.float32)
+    s32 = w["src"].astype(np.float32)
+    with hal.Adi(256, 256) as a:
+        a.set_field(f32)
+        a.set_source(s32)
+        a.run_ticks(7, 5.0, 0.01)
+        res = a.get_field()
+        host = a.run_ticks_host(f32.copy(), s32, 7, 5.0, 0.01)
+    assert np.array_equal(res, host)

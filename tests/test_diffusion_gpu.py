@@ -1,0 +1,160 @@
+"""Explicit diffusion on the GPU against the oracle and the golden vectors.
+
+Tolerances:
+* the FP64 interface call (hal_cuda_diffuse) must be bit-identical to the
+  reference CPU backend (same IEEE operations in the same order);
+* the FP32 fused tick must stay within max|err| <= 1e-5 * max|f| of the FP64
+  oracle, and rel-L2 <= 1e-6 on full-size runs.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import pytest
+
+from conftest import max_rel, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _eigen(nx, ny):
+    x = np.arange(nx)[:, None]
+    y = np.arange(ny)[None, :]
+    return (np.sin(2.0 * math.pi * x / nx) * np.sin(2.0 * math.pi * y / ny)).ravel()
+
+
+def test_diffuse_fp64_bit_exact_golden(hal, golden):
+    g = golden("stencil")
+    for k in range(int(g["count"][0])):
+        xd, yd, wx, wy, use_bc = (int(v) for v in g[f"c{k}_dims"])
+        r = float(g[f"c{k}_rates"][0])
+        with hal.Diffusion(xd, yd) as d:
+            if use_bc:
+                out = d.diffuse_bc(g[f"c{k}_field"], g[f"c{k}_deltas"].copy(), r, wx, wy,
+                                   g[f"c{k}_ghost"])
+            else:
+                out = d.diffuse(g[f"c{k}_field"], g[f"c{k}_deltas"].copy(), r, xd, yd, wx, wy)
+        assert np.array_equal(out, g[f"c{k}_explicit"]), f"case {k}: {xd}x{yd} wrap {wx}{wy}"
+
+
+def test_eigenmode_decay_through_interface(hal):
+    """tests/IDiffusionBackend2DTests.cpp:23-72 (GPU epsilon 1e-4 there)."""
+    nx, ny, r = 16, 20, 0.05
+    f = _eigen(nx, ny)
+    with hal.Diffusion(nx, ny) as d:
+        out = d.diffuse(f, np.zeros_like(f), r, nx, ny, True, True)
+    lam = 1.0 - 4.0 * r * (math.sin(math.pi / nx) ** 2 + math.sin(math.pi / ny) ** 2)
+    np.testing.assert_allclose(f + out, lam * f, rtol=1e-12, atol=1e-12)
+
+
+def test_size_mismatch_rejected(hal):
+    """tests/IDiffusionBackend2DTests.cpp:146-177."""
+    with hal.Diffusion(3, 4) as d:
+        with pytest.raises(ValueError):
+            d.diffuse(np.zeros(12), np.zeros(11), 0.1, 3, 4, False, False)
+        with pytest.raises(ValueError):
+            d.diffuse(np.zeros(12), np.zeros(12), 0.1, 4, 3, False, False)
+        with pytest.raises(ValueError):
+            d.run_steps(np.zeros(15, np.float32), 1, 0.1)
+        with pytest.raises(ValueError):
+            d.run_ticks(1, 0.26)
+
+
+def test_run_steps_eigenmode_nth_power(hal):
+    """DiffusionKernel2DTests.cpp:220-265: lambda^N after N steps, then 2N."""
+    nx, ny, r, steps = 16, 20, 0.05, 50
+    f = _eigen(nx, ny)
+    lam = 1.0 - 4.0 * r * (math.sin(math.pi / nx) ** 2 + math.sin(math.pi / ny) ** 2)
+    with hal.Diffusion(nx, ny) as d:
+        out = d.run_steps(f, steps, r, True, True)
+        np.testing.assert_allclose(out, lam ** steps * f, rtol=0, atol=1e-5)
+        out2 = d.run_steps(out, steps, r, True, True)
+        np.testing.assert_allclose(out2, lam ** (2 * steps) * f, rtol=0, atol=1e-5)
+
+
+def test_fused_tick_golden(hal, golden):
+    """PDEGrid2D tick (Dirichlet edge, decay, point sources), 150 ticks."""
+    g = golden("ticks")
+    xd, yd, r, decay, ticks = g["exp_params"]
+    xd, yd, ticks = int(xd), int(yd), int(ticks)
+    with hal.Diffusion(xd, yd) as d:
+        d.set_field(g["exp_field"])
+        d.set_dirichlet(g["exp_ghost"])
+        d.set_point_sources(g["exp_src_idx"], g["exp_src_val"])
+        d.run_ticks(ticks, r, decay)
+        out = d.get_field()
+    assert max_rel(out, g["exp_out"]) <= 1e-5
+
+
+SIZES = [(1, 1), (1, 9), (9, 1), (2, 2), (5, 7), (8, 12), (33, 64), (64, 33), (70, 130),
+         (129, 257)]
+
+
+@pytest.mark.parametrize("xd,yd", SIZES)
+def test_fused_tick_matches_oracle_all_boundaries(hal, oracle, xd, yd):
+    rng = np.random.default_rng(xd * 1000 + yd)
+    f = rng.random(xd * yd)
+    src = rng.random(xd * yd) * 0.01
+    pts = rng.choice(xd * yd, min(5, xd * yd), replace=False).astype(np.int32)
+    vals = rng.random(pts.size) * 0.1
+    ghost = rng.random(2 * (xd + yd))
+    for wx in (False, True):
+        for wy in (False, True):
+            for gh in (None, ghost):
+                exp = oracle.run_ticks(0, f, xd, yd, 0.21, wx, wy, gh, 0.003, src, pts, vals, ticks=6)
+                with hal.Diffusion(xd, yd) as d:
+                    d.set_field(f)
+                    d.set_source(src)
+                    d.set_point_sources(pts, vals)
+                    d.set_dirichlet(gh)
+                    d.run_ticks(6, 0.21, 0.003, wx, wy)
+                    out = d.get_field()
+                assert max_rel(out, exp) <= 1e-5, (wx, wy, gh is None)
+
+
+def test_graph_replay_and_parity_of_buffers(hal, oracle):
+    """Odd and even tick counts, repeated calls (graph cache per buffer parity)."""
+    rng = np.random.default_rng(3)
+    f = rng.random(40 * 52)
+    exp = oracle.run_ticks(0, f, 40, 52, 0.2, ticks=3 + 4 + 3 + 3)
+    with hal.Diffusion(40, 52) as d:
+        d.set_field(f)
+        for t in (3, 4, 3, 3):
+            d.run_ticks(t, 0.2)
+        out = d.get_field()
+    assert max_rel(out, exp) <= 1e-5
+
+
+def test_explicit_256_config_1000_ticks(hal, oracle):
+    """The 256x256 FP64 workload shape: Dirichlet 1.0 on the left edge, decay
+    0.001, 64 point sources of 0.05, 1000 ticks -- FP32 on the GPU vs FP64."""
+    from halcuda import workloads
+
+    w = workloads.explicit_inputs(256, seed=1)
+    exp = oracle.run_ticks(0, w["field"], 256, 256, w["diffRate"], ghost=w["ghost"],
+                           decay=w["decay"], src_idx=w["src_idx"], src_val=w["src_val"],
+                           ticks=1000, threads=8)
+    with hal.Diffusion(256, 256) as d:
+        d.set_field(w["field"])
+        d.set_dirichlet(w["ghost"])
+        d.set_point_sources(w["src_idx"], w["src_val"])
+        d.run_ticks(1000, w["diffRate"], w["decay"])
+        out = d.get_field()
+    assert rel_l2(out, exp) <= 1e-5
+    assert max_rel(out, exp) <= 2e-5
+
+
+def test_explicit_2048_full_size(hal, oracle):
+    from halcuda import workloads
+
+    w = workloads.explicit_inputs(2048, seed=1)
+    exp = oracle.run_ticks(0, w["field"], 2048, 2048, 0.2, decay=0.001, src_idx=w["src_idx"],
+                           src_val=w["src_val"], ticks=10, threads=16)
+    with hal.Diffusion(2048, 2048) as d:
+        d.set_field(w["field"])
+        d.set_point_sources(w["src_idx"], w["src_val"])
+        d.run_ticks(10, 0.2, 0.001)
+        out = d.get_field()
+    assert rel_l2(out, exp) <= 1e-6
+    assert max_rel(out, exp) <= 1e-5

@@ -1,0 +1,232 @@
+"""Pins the CPU oracle (oracle/hal_oracle.c) to the reference.
+
+CPU only.  Every golden vector in tests/golden/ was written from the
+reference's own CPU code (tests/golden/make_golden.py); the restatement must
+reproduce each FP64 result bit for bit.  The reference's known-answer tests
+(tests/IDiffusionBackend2DTests.cpp, PDEADITests.cpp,
+IAgentForceBackend2DTests.cpp) are restated against the oracle as well.  When
+the reference tree is present, the restatement is also compared with the
+freshly built reference library on new random cases.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import pytest
+
+import pyoracle
+
+
+def _eigen(nx, ny):
+    x = np.arange(nx)[:, None]
+    y = np.arange(ny)[None, :]
+    return (np.sin(2.0 * math.pi * x / nx) * np.sin(2.0 * math.pi * y / ny)).ravel()
+
+
+def test_stencil_and_adi_golden_bit_exact(oracle, golden):
+    g = golden("stencil")
+    count = int(g["count"][0])
+    assert count >= 60
+    for k in range(count):
+        xd, yd, wx, wy, use_bc = (int(v) for v in g[f"c{k}_dims"])
+        r_exp, r_adi = (float(v) for v in g[f"c{k}_rates"])
+        f = g[f"c{k}_field"]
+        d = g[f"c{k}_deltas"]
+        gh = g[f"c{k}_ghost"] if use_bc else None
+        out = oracle.diffuse(f, d, r_exp, xd, yd, wx, wy, gh)
+        assert np.array_equal(out, g[f"c{k}_explicit"]), f"explicit case {k} {xd}x{yd}"
+        out = oracle.diffuse_adi(f, d, r_adi, xd, yd, wx, wy, gh)
+        assert np.array_equal(out, g[f"c{k}_adi"]), f"ADI case {k} {xd}x{yd} wrap {wx}{wy} bc {use_bc}"
+
+
+def test_tick_golden_bit_exact(oracle, golden):
+    g = golden("ticks")
+    xd, yd, r, decay, ticks = g["exp_params"]
+    out = oracle.run_ticks(0, g["exp_field"], int(xd), int(yd), r, ghost=g["exp_ghost"],
+                           decay=decay, src_idx=g["exp_src_idx"], src_val=g["exp_src_val"],
+                           ticks=int(ticks))
+    assert np.array_equal(out, g["exp_out"])
+    xd, yd, r, decay, ticks = g["adi_params"]
+    out = oracle.run_ticks(1, g["adi_field"], int(xd), int(yd), r, decay=decay,
+                           src_dense=g["adi_src"], ticks=int(ticks))
+    assert np.array_equal(out, g["adi_out"])
+    xd, yd, r, decay, uptake, ticks = g["cpl_params"]
+    out = oracle.run_ticks(1, g["cpl_field"], int(xd), int(yd), r, wrapX=True,
+                           ghost=g["cpl_ghost"], decay=decay, uptake_count=g["cpl_counts"],
+                           uptake=uptake, ticks=int(ticks))
+    assert np.array_equal(out, g["cpl_out"])
+    out = oracle.run_ticks(1, g["kat_adi_field"], 20, 14, 0.6, ticks=5)
+    assert np.array_equal(out, g["kat_adi_out"])
+
+
+def test_agents_golden_bit_exact(oracle, golden):
+    g = golden("agents")
+    v, off, b = oracle.accumulate_forces(g["s1234_pos"], g["s1234_rad"], 3.0, 0.4, 16, 16, 1, 1)
+    assert np.array_equal(v, g["s1234_vel"])
+    assert np.array_equal(off, g["s1234_off"])
+    assert np.array_equal(b, g["s1234_bucket"])
+    for name in ("walls", "torus", "mixed", "tiny", "empty"):
+        xd, yd, n, wx, wy, R, k = g[f"{name}_params"]
+        v, off, b = oracle.accumulate_forces(g[f"{name}_pos"], g[f"{name}_rad"], R, k, int(xd),
+                                             int(yd), int(wx), int(wy))
+        assert np.array_equal(v, g[f"{name}_vel"]), name
+        assert np.array_equal(off, g[f"{name}_off"]), name
+        assert np.array_equal(b, g[f"{name}_bucket"]), name
+    v, _, _ = oracle.accumulate_forces([4.0, 4.0, 4.0, 4.0], [0.5, 0.5], 2.0, 1.0, 8, 8, 0, 0)
+    assert np.array_equal(v, g["coincident_vel"])
+    assert np.all(v == 0.0)
+
+
+def test_rand_golden_bit_exact(oracle, golden):
+    g = golden("rand")
+    for seed in (1, 7, 1234):
+        assert np.array_equal(oracle.rand_draws(seed, 0, 64), g[f"double_{seed}"])
+        assert np.array_equal(oracle.rand_draws(seed, 1, 64, 256), g[f"int256_{seed}"])
+        # log() may differ by an ulp between C libraries
+        assert np.allclose(oracle.rand_draws(seed, 2, 64), g[f"gauss_{seed}"], rtol=1e-14,
+                           atol=0)
+
+
+# --- the reference's known-answer tests, restated against the oracle ------
+
+def test_eigenmode_explicit_kat(oracle):
+    """tests/IDiffusionBackend2DTests.cpp:23-54 (epsilon 1e-4 there)."""
+    nx, ny, r = 16, 20, 0.05
+    f = _eigen(nx, ny)
+    d = oracle.diffuse(f, np.zeros_like(f), r, nx, ny, True, True)
+    lam = 1.0 - 4.0 * r * (math.sin(math.pi / nx) ** 2 + math.sin(math.pi / ny) ** 2)
+    np.testing.assert_allclose(f + d, lam * f, rtol=1e-12, atol=1e-12)
+
+
+def _lambda_cn(r, n, k=1):
+    s = math.sin(math.pi * k / n) ** 2
+    return (1.0 - 2.0 * r * s) / (1.0 + 2.0 * r * s)
+
+
+def test_eigenmode_adi_kat(oracle):
+    """tests/IDiffusionBackend2DTests.cpp:76-113 (CPU epsilon 1e-7)."""
+    nx, ny, r = 12, 18, 0.3
+    f = _eigen(nx, ny)
+    d = oracle.diffuse_adi(f, np.zeros_like(f), r, nx, ny, True, True)
+    lam = _lambda_cn(r, nx) * _lambda_cn(r, ny)
+    np.testing.assert_allclose(f + d, lam * f, rtol=1e-7, atol=1e-12)
+
+
+def test_adi_dirichlet_fixed_point_kat(oracle):
+    """PDEADITests.cpp:219-235: a flat field equal to the Dirichlet value stays put."""
+    xd, yd = 7, 5
+    f = np.full(xd * yd, 4.0)
+    ghost = np.full(2 * (xd + yd), 4.0)
+    out = oracle.run_ticks(1, f, xd, yd, 0.9, ghost=ghost)
+    np.testing.assert_allclose(out, 4.0, rtol=1e-12)
+
+
+def test_adi_dirichlet_relaxes_kat(oracle):
+    """PDEADITests.cpp:255-268: periodic x, Dirichlet 2.0, 400 steps -> 2.0."""
+    xd, yd = 8, 6
+    ghost = np.full(2 * (xd + yd), 2.0)
+    out = oracle.run_ticks(1, np.zeros(xd * yd), xd, yd, 1.5, wrapX=True, ghost=ghost, ticks=400)
+    np.testing.assert_allclose(out, 2.0, rtol=1e-6)
+
+
+def test_adi_dirichlet_ramp_kat(oracle):
+    """PDEADITests.cpp:287-352: the linear steady state between 1 and 3 holds."""
+    xd, yd = 6, 4
+
+    def ramp(x):
+        return 1.0 if x < 0 else (3.0 if x >= xd else 1.0 + 2.0 * (x + 0.5) / xd)
+
+    f = np.array([ramp(i // yd) for i in range(xd * yd)])
+    ghost = np.concatenate([np.full(yd, 1.0), np.full(yd, 3.0),
+                            np.array([ramp(x) for x in range(xd)]),
+                            np.array([ramp(x) for x in range(xd)])])
+    out = oracle.run_ticks(1, f, xd, yd, 0.9, ghost=ghost)
+    np.testing.assert_allclose(out, f, rtol=1e-9)
+
+
+def test_explicit_mass_conservation_kat(oracle):
+    """PDEGridTests.cpp:72-104 (2D form): zero-flux and periodic keep the total."""
+    rng = np.random.default_rng(5)
+    for wrap in (False, True):
+        f = rng.random(13 * 11)
+        out = oracle.run_ticks(0, f, 13, 11, 0.24, wrapX=wrap, wrapY=wrap, ticks=20)
+        assert abs(out.sum() - f.sum()) < 1e-10 * f.sum()
+
+
+def test_explicit_rate_cap(oracle):
+    """PDEGrid2D::CheckDiffusionStable (PDEGrid2D.h:436-442)."""
+    with pytest.raises(ValueError):
+        oracle.run_ticks(0, np.zeros(25), 5, 5, 0.26)
+    oracle.run_ticks(0, np.zeros(25), 5, 5, 0.25)
+
+
+def test_bruteforce_forces_kat(oracle, golden):
+    """tests/IAgentForceBackend2DTests.cpp:55-107: cell buckets equal an
+    all-pairs sum (CPU epsilon 1e-12)."""
+    g = golden("agents")
+    pos, rad = g["s1234_pos"], g["s1234_rad"]
+    n = rad.size
+    exp = np.zeros(2 * n)
+    for i in range(n):
+        for j in range(n):
+            if i == j:
+                continue
+            dx = pos[2 * j] - pos[2 * i]
+            dy = pos[2 * j + 1] - pos[2 * i + 1]
+            if abs(dx) > 8:
+                dx = dx + 16 if pos[2 * i] > pos[2 * j] else dx - 16
+            if abs(dy) > 8:
+                dy = dy + 16 if pos[2 * i + 1] > pos[2 * j + 1] else dy - 16
+            dist = math.sqrt(dx * dx + dy * dy)
+            if 0 < dist < 3.0:
+                force = 0.4 * ((rad[i] + rad[j]) - dist)
+                exp[2 * i] -= dx / dist * force
+                exp[2 * i + 1] -= dy / dist * force
+    v, _, _ = oracle.accumulate_forces(pos, rad, 3.0, 0.4, 16, 16, 1, 1)
+    np.testing.assert_allclose(v, exp, rtol=1e-12, atol=1e-12)
+
+
+def test_forces_size_mismatch(oracle):
+    """IAgentForceBackend2DTests.cpp:144-151."""
+    with pytest.raises(ValueError):
+        oracle.accumulate_forces([1.0, 1.0, 2.0], [0.5, 0.5], 2.0, 1.0, 8, 8, 0, 0)
+
+
+def test_threaded_oracle_matches_serial(oracle):
+    rng = np.random.default_rng(11)
+    f = rng.random(70 * 90)
+    a = oracle.diffuse_adi(f, np.zeros_like(f), 5.0, 70, 90, False, True, threads=1)
+    b = oracle.diffuse_adi(f, np.zeros_like(f), 5.0, 70, 90, False, True, threads=4)
+    assert np.array_equal(a, b)
+    pos = (rng.random(4000) * 50).astype(np.float32).astype(np.float64)
+    rad = np.full(2000, 0.5)
+    a = oracle.accumulate_forces(pos, rad, 1.0, 0.1, 50, 50, 0, 0, threads=1)
+    b = oracle.accumulate_forces(pos, rad, 1.0, 0.1, 50, 50, 0, 0, threads=3)
+    assert all(np.array_equal(x, y) for x, y in zip(a, b))
+
+
+@pytest.mark.skipif(not pyoracle.Reference.available() and not __import__("os").path.isdir(
+    pyoracle.REF_TREE), reason="reference tree not present")
+def test_restatement_matches_reference_library_random(oracle):
+    """Fresh random cases through the reference's own compiled CPU code."""
+    pyoracle.build(ref=True)
+    R = pyoracle.Reference
+    rng = np.random.default_rng(99)
+    for _ in range(6):
+        xd, yd = (int(v) for v in rng.integers(1, 40, 2))
+        wx, wy = (bool(v) for v in rng.integers(0, 2, 2))
+        f = rng.random(xd * yd)
+        d = rng.random(xd * yd)
+        gh = rng.random(2 * (xd + yd)) if rng.random() < 0.5 else None
+        r = float(rng.random() * 8)
+        assert np.array_equal(oracle.diffuse(f, d, 0.2, xd, yd, wx, wy, gh),
+                              R.diffuse(f, d, 0.2, xd, yd, wx, wy, gh))
+        assert np.array_equal(oracle.diffuse_adi(f, d, r, xd, yd, wx, wy, gh),
+                              R.diffuse_adi(f, d, r, xd, yd, wx, wy, gh))
+        n = int(rng.integers(0, 300))
+        pos = (rng.random(2 * n) * max(xd, yd)).astype(np.float32).astype(np.float64)
+        rad = 0.3 + rng.random(n) * 0.5
+        a = oracle.accumulate_forces(pos, rad, 1.7, 0.2, xd, yd, wx, wy)
+        b = R.accumulate_forces(pos, rad, 1.7, 0.2, xd, yd, wx, wy)
+        assert all(np.array_equal(x, y) for x, y in zip(a, b))
