@@ -354,9 +354,9 @@ def main():
     col_gbs = ADI_COL_BYTES * CELLS / (ms_col * 1e-3) / 1e9
     row_gbs = ADI_ROW_BYTES * CELLS / (ms_row * 1e-3) / 1e9
     if ms_row >= ms_col:
-        dom, dom_gbs, dom_bytes = "AdiRowSweep", row_gbs, ADI_ROW_BYTES
+        dom, dom_gbs, dom_bytes = "AdiSweep<kSweepTick>", row_gbs, ADI_ROW_BYTES
     else:
-        dom, dom_gbs, dom_bytes = "AdiColumnSweep", col_gbs, ADI_COL_BYTES
+        dom, dom_gbs, dom_bytes = "AdiSweep<kSweepW>", col_gbs, ADI_COL_BYTES
     peak, peak_kind = peaks()
     tick_gbs = (ADI_COL_BYTES + ADI_ROW_BYTES) * CELLS / ((ms_col + ms_row) * 1e-3) / 1e9
 
@@ -408,8 +408,10 @@ def main():
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": dom_gbs / peak,
                          "traffic": profile_traffic(dom),
                          "bytes_per_launch": dom_bytes * CELLS,
-                         "launch_ms": {"AdiColumnSweep": ms_col, "AdiRowSweep": ms_row},
-                         "achieved_by_kernel": {"AdiColumnSweep": col_gbs, "AdiRowSweep": row_gbs},
+                         "launch_ms": {"x-sweep AdiSweep<kSweepW>": ms_col,
+                                       "y-sweep AdiSweep<kSweepTick>": ms_row},
+                         "achieved_by_kernel": {"x-sweep AdiSweep<kSweepW>": col_gbs,
+                                                "y-sweep AdiSweep<kSweepTick>": row_gbs},
                          "tick_achieved": tick_gbs,
                          "note": "working set (3 x 16.8 MB + scratch) stays in the 126 MB L2 "
                                  "across the ticks of a step"},

@@ -2,27 +2,35 @@
 //
 // One ADI step (Internal::Diffusion2DADI, include/Hal/Pde/ADIequations.h:
 // 306-378) is two sweeps:
-//   x-sweep: for every column y, solve (I - r/2 Lx) w = (I + r/2 Ly) f along x
-//            (lines of stride yDim) -> scratch w;
-//   y-sweep: for every row x, solve (I - r/2 Ly) v = (I + r/2 Lx) w along y
-//            (contiguous lines), then commit v.
-// Each line is a tridiagonal system with the same matrix for every line of a
-// sweep; adi_plan.h describes the partitioned Thomas solve used here and the
-// FP64 precomputation it relies on.
+//   x-sweep: for every y, solve (I - r/2 Lx) w = (I + r/2 Ly) f along x;
+//   y-sweep: for every x, solve (I - r/2 Ly) v = (I + r/2 Lx) w along y,
+//            then commit v (PDEGrid2D: f' = f + (v - f) - decay f + src
+//            - uptake n f).
+// Every line of a sweep solves the same tridiagonal matrix; adi_plan.h
+// describes the partitioned Thomas solve and its FP64 precomputation.
 //
-// Kernel mapping (32-row chunks, one per thread, values kept in registers):
-//   AdiColumnSweep -- a lane per column (coalesced 128-byte rows), a warp per
-//     chunk of 32 rows, a thread-block cluster of up to 8 CTAs per 32-column
-//     strip so that all chunks of a line sit in one cluster.  The separator
-//     right-hand sides are exchanged through distributed shared memory.
-//   AdiRowSweep -- a CTA stages R rows (plus the rows above and below, for
-//     the explicit x part) in shared memory with coalesced loads, a thread
-//     per (row, chunk) solves from shared memory, and the commit
-//     (v - decay*f + source - uptake*count*f) streams back coalesced.
+// Layout.  The resident field is kept transposed ("layout B",
+// index y*xDim + x) so that the x-sweep's lines are contiguous.  Each sweep
+// reads contiguous lines and writes its result transposed: the x-sweep reads
+// f (B) and writes w in HAL's layout ("layout A", x*yDim + y), whose y-lines
+// the y-sweep reads, writing f' back in layout B.  Both sweeps therefore run
+// the same kernel, AdiSweep:
+//   1. stage the CTA's R lines plus the line on either side (the explicit
+//      cross-axis term) into shared memory with TMA bulk copies
+//      (cp.async.bulk, one 128-byte chunk each, completion on an mbarrier);
+//      each 32-element chunk occupies 36 floats so that every later access
+//      is a conflict-free 128-bit LDS/STS;
+//   2. each thread solves one 32-row chunk of two lines (two interleaved
+//      Thomas chains in registers), exchanges the separator right-hand sides
+//      through shared memory, applies the banded reduced solve and the
+//      coupling correction (and the periodic Sherman-Morrison correction);
+//   3. the tile is written out transposed, four lines (16 bytes) per store,
+//      with the commit terms applied on the way out.
 #include "common.cuh"
 #include "adi_plan.h"
 
-#include <cooperative_groups.h>
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
 #include <cstring>
 #include <map>
@@ -30,34 +38,19 @@
 #include <string>
 #include <vector>
 
-namespace cg = cooperative_groups;
-
 namespace halcuda
 {
     namespace
     {
         constexpr int M = kAdiM;
         constexpr int kCoefFloats = 3 * kCoefCount * M;
-        constexpr int kRowThreads = 256;
-
-        enum RowMode : int
-        {
-            kRowTick = 0,    // out = f + (v - f) - decay f + src - uptake n f
-            kRowDeltas = 1,  // deltas (FP64) += v - f
-            kRowPlain = 2    // out = v
-        };
-
-        enum NbrMode : int
-        {
-            kNbrGrid = 0,
-            kNbrGhost = 1,
-            kNbrNone = 2
-        };
-
-        __device__ __forceinline__ float NbrTerm(int mode, float v, float c)
-        {
-            return (mode == kNbrGrid) ? (v - c) : ((mode == kNbrGhost) ? (v - c) * 2.0f : 0.0f);
-        }
+        constexpr int kChunkStride = M + 4;  // floats per 32-element chunk in shared memory
+        constexpr int kNL = 2;               // lines solved by one thread
+        constexpr int kMaxThreads = 512;
+        constexpr int kMaxR = 128;           // lines per CTA (a power of two, >= 8)
+        // bound of the mbarrier wait (ns of %globaltimer); the staged copies
+        // take microseconds, so reaching it means the copies never landed
+        constexpr unsigned long long kWaitLimitNs = 2000000000ull;
 
         struct LinePlanDev
         {
@@ -69,39 +62,64 @@ namespace halcuda
             float bog, invDenom;  // periodic: beta/gamma, 1/(1 + v.z_sm)
         };
 
-        __device__ __forceinline__ void ClusterArriveRelaxed()
-        {
-            asm volatile("barrier.cluster.arrive.relaxed.aligned;\n" ::: "memory");
-        }
-
-        __device__ __forceinline__ void ClusterWait()
-        {
-            asm volatile("barrier.cluster.wait.aligned;\n" ::: "memory");
-        }
-
         // Thomas forward elimination and back substitution of one block with
-        // the identity padding described in adi_plan.h.
+        // the identity padding described in adi_plan.h.  The coefficients
+        // are read from shared memory 16 bytes at a time.
         __device__ __forceinline__ void BlockSolve(float (&z)[M], const float *cf)
         {
-            const float *fw = cf + kCoefFw * M;
-            const float *ib = cf + kCoefIb * M;
-            const float *cb = cf + kCoefCb * M;
+            const float4 *fw = reinterpret_cast<const float4 *>(cf + kCoefFw * M);
+            const float4 *ib = reinterpret_cast<const float4 *>(cf + kCoefIb * M);
+            const float4 *cb = reinterpret_cast<const float4 *>(cf + kCoefCb * M);
 #pragma unroll
-            for (int i = 1; i < M; i++)
+            for (int j = 0; j < M / 4; j++)
             {
-                z[i] = fmaf(-fw[i], z[i - 1], z[i]);
+                const float4 w4 = fw[j];
+                if (j > 0)
+                {
+                    z[4 * j] = fmaf(-w4.x, z[4 * j - 1], z[4 * j]);
+                }
+                z[4 * j + 1] = fmaf(-w4.y, z[4 * j], z[4 * j + 1]);
+                z[4 * j + 2] = fmaf(-w4.z, z[4 * j + 1], z[4 * j + 2]);
+                z[4 * j + 3] = fmaf(-w4.w, z[4 * j + 2], z[4 * j + 3]);
             }
-            z[M - 1] *= ib[M - 1];
 #pragma unroll
-            for (int i = M - 2; i >= 0; i--)
+            for (int j = M / 4 - 1; j >= 0; j--)
             {
-                z[i] = fmaf(-cb[i], z[i + 1], z[i] * ib[i]);
+                const float4 i4 = ib[j];
+                const float4 c4 = cb[j];
+                if (j == M / 4 - 1)
+                {
+                    z[4 * j + 3] *= i4.w;
+                }
+                else
+                {
+                    z[4 * j + 3] = fmaf(-c4.w, z[4 * j + 4], z[4 * j + 3] * i4.w);
+                }
+                z[4 * j + 2] = fmaf(-c4.z, z[4 * j + 3], z[4 * j + 2] * i4.z);
+                z[4 * j + 1] = fmaf(-c4.y, z[4 * j + 2], z[4 * j + 1] * i4.y);
+                z[4 * j + 0] = fmaf(-c4.x, z[4 * j + 1], z[4 * j + 0] * i4.x);
+            }
+        }
+
+        // x = z - sL p - sR q over the block.
+        __device__ __forceinline__ void BlockCorrect(float (&z)[M], const float *cf, float sL, float sR)
+        {
+            const float4 *pv = reinterpret_cast<const float4 *>(cf + kCoefP * M);
+            const float4 *qv = reinterpret_cast<const float4 *>(cf + kCoefQ * M);
+#pragma unroll
+            for (int j = 0; j < M / 4; j++)
+            {
+                const float4 p4 = pv[j];
+                const float4 q4 = qv[j];
+                z[4 * j + 0] = fmaf(-sL, p4.x, fmaf(-sR, q4.x, z[4 * j + 0]));
+                z[4 * j + 1] = fmaf(-sL, p4.y, fmaf(-sR, q4.y, z[4 * j + 1]));
+                z[4 * j + 2] = fmaf(-sL, p4.z, fmaf(-sR, q4.z, z[4 * j + 2]));
+                z[4 * j + 3] = fmaf(-sL, p4.w, fmaf(-sR, q4.w, z[4 * j + 3]));
             }
         }
 
         // s_j = sum_m G[j][m] * (xA[m] + xB[m]) over the stored band.
-        __device__ __forceinline__ float BandDot(const LinePlanDev &pl, int j, const float *xA,
-                                                 const float *xB, int stride)
+        __device__ __forceinline__ float BandDot(const LinePlanDev &pl, int j, const float *xA, const float *xB)
         {
             const int S = pl.P - 1;
             const int lo = max(0, j - pl.B);
@@ -110,7 +128,7 @@ namespace halcuda
             float acc = 0.0f;
             for (int m = lo; m <= hi; m++)
             {
-                acc = fmaf(__ldg(g + (m - j + pl.B)), xA[m * stride] + xB[m * stride], acc);
+                acc = fmaf(__ldg(g + (m - j + pl.B)), xA[m] + xB[m], acc);
             }
             return acc;
         }
@@ -127,519 +145,746 @@ namespace halcuda
             return v;
         }
 
-        __device__ __forceinline__ float LoadAsFloat(const float *p)
+        // Float offset, within the staged lines, of element i of chunk k of
+        // staged line `line`.  SWZ: the TMA tensor layout with 128-byte
+        // swizzle (128-byte rows row = line*P + k, 16-byte unit u stored at
+        // u ^ (row & 7); the swizzled path is used only when P % 8 == 0, so
+        // row & 7 == k & 7); otherwise chunks padded to kChunkStride floats
+        // with line stride LS.
+        template <bool SWZ>
+        __device__ __forceinline__ int SOff(int line, int k, int i, int P, int LS)
         {
-            return __ldg(p);
+            if constexpr (SWZ)
+            {
+                // P % 8 == 0, so row & 7 == k & 7
+                return (line * P + k) * M + (i ^ ((k & 7) << 2));
+            }
+            else
+            {
+                return line * LS + k * kChunkStride + i;
+            }
         }
 
-        __device__ __forceinline__ float LoadAsFloat(const double *p)
+        // Float offset of the 16-byte unit q (elements 4q..4q+3) of chunk k.
+        template <bool SWZ>
+        __device__ __forceinline__ int SOff4(int line, int k, int q, int P, int LS)
         {
-            return static_cast<float>(__ldg(p));
+            if constexpr (SWZ)
+            {
+                return (line * P + k) * M + ((q ^ (k & 7)) << 2);
+            }
+            else
+            {
+                return line * LS + k * kChunkStride + 4 * q;
+            }
         }
 
-        // ---------------------------------------------------------------
-        // x-sweep: lines along x (stride yDim), a lane per column.
-        // ---------------------------------------------------------------
-        template <typename TIn>
-        struct ColParams
+        // The same for a precomputed row (line*P + k) and swizzle term k & 7.
+        template <bool SWZ>
+        __device__ __forceinline__ int SOff4Row(int row, int k, int q, int sw, int P, int LS)
         {
-            const TIn *f;
-            float *w;
-            int32_t L;      // xDim (line length)
-            int32_t ncols;  // yDim
-            float halfR, r;
-            int32_t wrapY;
-            GhostView ghost;
-            LinePlanDev plan;
+            if constexpr (SWZ)
+            {
+                return row * M + ((q ^ sw) << 2);
+            }
+            else
+            {
+                return (row / P) * LS + k * kChunkStride + 4 * q;
+            }
+        }
+
+        // An opaque copy of v: keeps the compiler from holding values derived
+        // from v in registers across a long stretch of code.
+        __device__ __forceinline__ int Opaque(int v)
+        {
+            int r;
+            asm volatile("mov.b32 %0, %1;" : "=r"(r) : "r"(v));
+            return r;
+        }
+
+        // Element pos of a staged line.
+        template <bool SWZ>
+        __device__ __forceinline__ int SPos(int line, int32_t pos, int P, int LS)
+        {
+            return SOff<SWZ>(line, pos >> 5, pos & 31, P, LS);
+        }
+
+        __device__ __forceinline__ float4 Ld4(const float *p)
+        {
+            return *reinterpret_cast<const float4 *>(p);
+        }
+
+        __device__ __forceinline__ void St4(float *p, float4 v)
+        {
+            *reinterpret_cast<float4 *>(p) = v;
+        }
+
+        __device__ __forceinline__ uint32_t SmemAddr(const void *p)
+        {
+            return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+        }
+
+        __device__ __forceinline__ unsigned long long GlobalTimerNs()
+        {
+            unsigned long long t;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+            return t;
+        }
+
+        enum SweepMode : int
+        {
+            kSweepW = 0,      // x-sweep: out (transposed) = w
+            kSweepTick = 1,   // y-sweep: out (transposed) = committed f'
+            kSweepPlain = 2,  // y-sweep: out (transposed) = v
+            kSweepDeltas = 3  // y-sweep: deltas (line-major, FP64) += v - f64
         };
 
-        // Right-hand side (I + r/2 Ly) f at (row, col) plus the Dirichlet
-        // source of the implicit axis (ExplicitDiffusionY2ADI,
-        // src/Pde/ADIequations.cpp:34-47; ImplicitBoundarySource,
-        // ADIequations.h:198-220).  Called by all 32 lanes together.
-        template <typename TIn>
-        __device__ __forceinline__ float ColumnRhs(const ColParams<TIn> &p, int32_t row, int32_t col,
-                                                   bool colOk, int lane)
+        struct SweepParams
         {
-            const TIn *rowp = p.f + static_cast<int64_t>(row) * p.ncols;
-            float c = colOk ? LoadAsFloat(rowp + col) : 0.0f;
-            float left = __shfl_up_sync(0xffffffffu, c, 1);
-            float right = __shfl_down_sync(0xffffffffu, c, 1);
-            if (!colOk)
-            {
-                return 0.0f;
-            }
-            if (lane == 0 && col > 0)
-            {
-                left = LoadAsFloat(rowp + col - 1);
-            }
-            if (lane == 31 && col + 1 < p.ncols)
-            {
-                right = LoadAsFloat(rowp + col + 1);
-            }
-            float tp, tm;
-            if (col + 1 < p.ncols)
-            {
-                tp = right - c;
-            }
-            else if (p.wrapY)
-            {
-                tp = LoadAsFloat(rowp) - c;
-            }
-            else if (p.ghost.yhi != nullptr)
-            {
-                tp = (__ldg(p.ghost.yhi + row) - c) * 2.0f;
-            }
-            else
-            {
-                tp = 0.0f;
-            }
-            if (col > 0)
-            {
-                tm = left - c;
-            }
-            else if (p.wrapY)
-            {
-                tm = LoadAsFloat(rowp + p.ncols - 1) - c;
-            }
-            else if (p.ghost.ylo != nullptr)
-            {
-                tm = (__ldg(p.ghost.ylo + row) - c) * 2.0f;
-            }
-            else
-            {
-                tm = 0.0f;
-            }
-            float d = fmaf(tp + tm, p.halfR, c);
-            if (p.ghost.xlo != nullptr && !p.plan.periodic)
-            {
-                if (row == 0)
-                {
-                    d = fmaf(p.r, __ldg(p.ghost.xlo + col), d);
-                }
-                if (row == p.L - 1)
-                {
-                    d = fmaf(p.r, __ldg(p.ghost.xhi + col), d);
-                }
-            }
-            return d;
-        }
+            const float *in;          // Nlines lines of L floats, line-major
+            int32_t L, Nlines;
+            int32_t wrapLines;        // the explicit (cross-line) axis wraps
+            const float *ghostLo;     // Dirichlet ghost line before line 0 (L values) or null
+            const float *ghostHi;     // ghost line after line Nlines-1
+            const float *implLo;      // Dirichlet value before position 0, per line, or null
+            const float *implHi;      // Dirichlet value after position L-1, per line
+            float halfR, r;
+            LinePlanDev plan;         // lines of length L along the implicit axis
+            int32_t R, LS;            // lines per CTA, shared-memory line stride (floats)
+            float *out;               // transposed output: out[pos * Nlines + line]
+            const float *f;           // kSweepTick: field before the step (output layout)
+            const float *src;         // kSweepTick: dense source (output layout) or null
+            const int32_t *cellOffsets;  // kSweepTick: agent bins (line-major), or null
+            float negDecay, negUptake;
+            const double *f64;        // kSweepDeltas: field (line-major)
+            double *deltas;           // kSweepDeltas: deltas (line-major)
+            int32_t *err;             // set to 1 if a bounded wait gave up
+        };
 
-        template <typename TIn>
-        __global__ void __launch_bounds__(512) AdiColumnSweep(ColParams<TIn> p)
+        template <int MODE, bool SWZ>
+        __global__ void __launch_bounds__(kMaxThreads)
+            AdiSweep(SweepParams p, const __grid_constant__ CUtensorMap tmap)
         {
-            __shared__ float sCoef[kCoefFloats];
-            __shared__ float xA[kAdiMaxChunks * 32];
-            __shared__ float xB[kAdiMaxChunks * 32];
-            __shared__ float xZ0[32];
-            __shared__ float xZL[32];
-
-            cg::cluster_group cl = cg::this_cluster();
-            const int lane = threadIdx.x;
-            const int warp = threadIdx.y;
-            const int W = blockDim.y;
-            const unsigned K = cl.num_blocks();
-            const int rank = static_cast<int>(cl.block_rank());
-            const int tid = warp * 32 + lane;
-            for (int q = tid; q < kCoefFloats; q += 32 * W)
-            {
-                sCoef[q] = __ldg(p.plan.coef + q);
-            }
-            __syncthreads();
-            ClusterArriveRelaxed();
-
+            extern __shared__ __align__(16) float smem[];
+            __shared__ __align__(8) unsigned long long mbar;
+            __shared__ int s_fail;
+            __shared__ uint32_t s_tmaBytes;
             const int P = p.plan.P;
-            const int k = rank * W + warp;
-            const int32_t col = blockIdx.y * 32 + lane;
-            const bool colOk = col < p.ncols;
-            const bool chunkOk = k < P;
-            const int32_t base = k * M;
-
-            float z[M];
-#pragma unroll
-            for (int i = 0; i < M; i++)
-            {
-                const int32_t row = base + i;
-                z[i] = 0.0f;
-                if (chunkOk && row < p.L)  // warp-uniform
-                {
-                    z[i] = ColumnRhs(p, row, col, colOk, lane);
-                }
-            }
-
-            const int type = AdiBlockType(k, P);
-            const float *cf = sCoef + type * kCoefCount * M;
-            if (chunkOk)
-            {
-                BlockSolve(z, cf);
-            }
-
-            const float a = p.plan.a;
-            ClusterWait();  // every CTA of the cluster is running
-            if (chunkOk && k < P - 1)
-            {
-                const float vA = fmaf(-a, z[M - 2], z[M - 1]);
-                for (unsigned q = 0; q < K; q++)
-                {
-                    cl.map_shared_rank(xA, q)[k * 32 + lane] = vA;
-                }
-            }
-            if (chunkOk && k >= 1)
-            {
-                const float vB = -a * z[0];
-                for (unsigned q = 0; q < K; q++)
-                {
-                    cl.map_shared_rank(xB, q)[(k - 1) * 32 + lane] = vB;
-                }
-            }
-            if (p.plan.periodic && P > 1)
-            {
-                if (k == 0)
-                {
-                    for (unsigned q = 0; q < K; q++)
-                    {
-                        cl.map_shared_rank(xZ0, q)[lane] = z[0];
-                    }
-                }
-                if (k == P - 1)
-                {
-                    const float zl = SelectReg(z, p.plan.nlast - 1);
-                    for (unsigned q = 0; q < K; q++)
-                    {
-                        cl.map_shared_rank(xZL, q)[lane] = zl;
-                    }
-                }
-            }
-            cl.sync();
-
-            if (chunkOk)
-            {
-                float sL = 0.0f, sR = 0.0f;
-                if (P > 1)
-                {
-                    if (k < P - 1)
-                    {
-                        sR = BandDot(p.plan, k, xA + lane, xB + lane, 32);
-                    }
-                    if (k >= 1)
-                    {
-                        sL = BandDot(p.plan, k - 1, xA + lane, xB + lane, 32);
-                    }
-                }
-                const float *pv = cf + kCoefP * M;
-                const float *qv = cf + kCoefQ * M;
-#pragma unroll
-                for (int i = 0; i < M; i++)
-                {
-                    z[i] = fmaf(-sL, pv[i], fmaf(-sR, qv[i], z[i]));
-                }
-                if (k < P - 1)
-                {
-                    z[M - 1] = sR;
-                }
-                if (p.plan.periodic)
-                {
-                    float y0, yl;
-                    if (P == 1)
-                    {
-                        y0 = z[0];
-                        yl = SelectReg(z, p.L - 1);
-                    }
-                    else
-                    {
-                        const float s0 = BandDot(p.plan, 0, xA + lane, xB + lane, 32);
-                        const float sl = BandDot(p.plan, P - 2, xA + lane, xB + lane, 32);
-                        y0 = xZ0[lane] - s0 * sCoef[0 * kCoefCount * M + kCoefQ * M + 0];
-                        yl = xZL[lane] - sl * sCoef[2 * kCoefCount * M + kCoefP * M + p.plan.nlast - 1];
-                    }
-                    const float factor = fmaf(yl, p.plan.bog, y0) * p.plan.invDenom;
-#pragma unroll
-                    for (int i = 0; i < M; i++)
-                    {
-                        const int32_t row = base + i;
-                        if (row < p.L)
-                        {
-                            z[i] = fmaf(-factor, __ldg(p.plan.zsm + row), z[i]);
-                        }
-                    }
-                }
-                if (colOk)
-                {
-#pragma unroll
-                    for (int i = 0; i < M; i++)
-                    {
-                        const int32_t row = base + i;
-                        if (row < p.L)
-                        {
-                            p.w[static_cast<int64_t>(row) * p.ncols + col] = z[i];
-                        }
-                    }
-                }
-            }
-        }
-
-        // ---------------------------------------------------------------
-        // y-sweep: contiguous lines, R rows per CTA staged in shared memory.
-        // ---------------------------------------------------------------
-        template <typename TF>
-        struct RowParams
-        {
-            const float *w;        // x-sweep result
-            const TF *f;           // field before the step (commit input)
-            float *out;            // kRowTick / kRowPlain
-            double *deltas;        // kRowDeltas
-            const float *src;      // dense source or null
-            const int32_t *cellOffsets;  // uptake counts (offsets[c+1]-offsets[c]) or null
-            float negUptake, negDecay;
-            int32_t xDim;
-            int32_t L;             // yDim
-            float halfR, r;
-            int32_t wrapX;
-            GhostView ghost;
-            LinePlanDev plan;
-            int32_t R;             // rows per CTA
-            int32_t LP;            // padded row length in shared memory
-        };
-
-        __device__ __forceinline__ int PadIdx(int32_t y)
-        {
-            return (y / M) * (M + 1) + (y % M);
-        }
-
-        template <typename TF, int MODE>
-        __global__ void __launch_bounds__(kRowThreads) AdiRowSweep(RowParams<TF> p)
-        {
-            extern __shared__ float smem[];
-            float *sCoef = smem;
-            float *sRows = sCoef + kCoefFloats;                 // (R+2) * LP
-            float *xA = sRows + (p.R + 2) * p.LP;                // R * P
-            float *xB = xA + p.R * p.plan.P;                     // R * P
-            float *xZ0 = xB + p.R * p.plan.P;                    // R
-            float *xZL = xZ0 + p.R;                              // R
+            const int R = p.R;
+            // staged lines first, on a 1024-byte boundary (128-byte swizzle)
+            float *sLines = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(smem) + 1023) & ~uintptr_t(1023));
+            float *sCoef = sLines + (R + 2) * p.LS;  // kCoefFloats
+            float *xA = sCoef + kCoefFloats;         // R * P
+            float *xB = xA + R * P;                  // R * P
 
             const int tid = threadIdx.x;
             const int nthreads = blockDim.x;
-            const int P = p.plan.P;
-            const int32_t x0 = blockIdx.x * p.R;
+            const int32_t x0 = blockIdx.x * R;
+            const int32_t L = p.L;
+            const bool vecL = (L & 3) == 0;
 
-            for (int q = tid; q < kCoefFloats; q += nthreads)
+            // ---- 1. stage lines x0-1 .. x0+R --------------------------------
+            __shared__ const float *sSrc[kMaxR + 2];
+            __shared__ int sTma[kMaxR + 2];
+            const uint32_t bar = SmemAddr(&mbar);
+            const int nStaged = R + 2;
+            uint32_t tmaBytes = 0;
+            if constexpr (SWZ)
             {
-                sCoef[q] = __ldg(p.plan.coef + q);
+                // one 3-D tensor copy: 32 floats x P chunks x (R+2) lines; lines
+                // outside the grid arrive as zeros
+                tmaBytes = static_cast<uint32_t>(nStaged) * static_cast<uint32_t>(P) * M * 4u;
+                if (tid == 0)
+                {
+                    s_fail = 0;
+                    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
+                    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(tmaBytes)
+                                 : "memory");
+                    asm volatile(
+                        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(SmemAddr(sLines)),
+                        "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(0), "r"(0), "r"(x0 - 1), "r"(bar)
+                        : "memory");
+                }
+                for (int q = tid; q < kCoefFloats / 4; q += nthreads)
+                {
+                    St4(sCoef + 4 * q, __ldg(reinterpret_cast<const float4 *>(p.plan.coef) + q));
+                }
+                __syncthreads();  // mbarrier initialised before anyone waits on it
             }
-            // Stage rows x0-1 .. x0+R of w.
-            for (int rr = 0; rr < p.R + 2; rr++)
+            else
             {
-                int32_t xg = x0 - 1 + rr;
-                const float *src = nullptr;
-                const float *ghostRow = nullptr;
-                if (xg >= 0 && xg < p.xDim)
+                if (tid == 0)
                 {
-                    src = p.w + static_cast<int64_t>(xg) * p.L;
+                    s_fail = 0;
+                    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
+                    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
                 }
-                else if (p.wrapX)
+                for (int rs = tid; rs < nStaged; rs += nthreads)
                 {
-                    int32_t xw = (xg < 0) ? xg + p.xDim : xg - p.xDim;
-                    src = p.w + static_cast<int64_t>(xw) * p.L;
-                }
-                else if (p.ghost.xlo != nullptr)
-                {
-                    ghostRow = (xg < 0) ? p.ghost.xlo : p.ghost.xhi;
-                }
-                float *dst = sRows + rr * p.LP;
-                if (src != nullptr && (p.L % 4) == 0)
-                {
-                    const float4 *s4 = reinterpret_cast<const float4 *>(src);
-                    for (int32_t q = tid; q < p.L / 4; q += nthreads)
+                    // source of staged line rs: a grid line, the neighbour line
+                    // beyond an edge (wrapped, a Dirichlet ghost line, or zeros);
+                    // lines further out (a CTA past the last line) are never read
+                    const int32_t line = x0 - 1 + rs;
+                    const float *src = nullptr;
+                    if (line >= 0 && line < p.Nlines)
                     {
-                        float4 v = __ldg(s4 + q);
-                        int32_t y = q * 4;
-                        int o = PadIdx(y);
-                        dst[o] = v.x;
-                        dst[o + 1] = v.y;
-                        dst[o + 2] = v.z;
-                        dst[o + 3] = v.w;
+                        src = p.in + static_cast<int64_t>(line) * L;
+                    }
+                    else if (line == -1 || line == p.Nlines)
+                    {
+                        if (p.wrapLines)
+                        {
+                            src = p.in + static_cast<int64_t>((line < 0) ? p.Nlines - 1 : 0) * L;
+                        }
+                        else
+                        {
+                            src = (line < 0) ? p.ghostLo : p.ghostHi;
+                        }
+                    }
+                    sSrc[rs] = src;
+                    sTma[rs] = (src != nullptr) && vecL && ((reinterpret_cast<uintptr_t>(src) & 15) == 0);
+                }
+                for (int q = tid; q < kCoefFloats / 4; q += nthreads)
+                {
+                    St4(sCoef + 4 * q, __ldg(reinterpret_cast<const float4 *>(p.plan.coef) + q));
+                }
+                __syncthreads();  // mbarrier initialised, line sources known
+                if (tid == 0)
+                {
+                    for (int rr = 0; rr < nStaged; rr++)
+                    {
+                        tmaBytes += sTma[rr] ? static_cast<uint32_t>(L) * 4u : 0u;
+                    }
+                    if (tmaBytes > 0)
+                    {
+                        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(tmaBytes)
+                                     : "memory");
+                    }
+                    s_tmaBytes = tmaBytes;
+                }
+                __syncthreads();  // the expected byte count is in place before any copy lands
+                tmaBytes = s_tmaBytes;
+                {
+                    // thread -> chunk kc of lines rr0, rr0 + rstride, ...
+                    const int kc = tid % P;
+                    const int rstride = nthreads / P;
+                    const int32_t n = min(M, L - kc * M);  // elements of this chunk inside the line
+                    for (int rr = tid / P; rr < nStaged && tid < rstride * P; rr += rstride)
+                    {
+                        const float *src = sSrc[rr];
+                        float *dst = sLines + rr * p.LS + kc * kChunkStride;
+                        if (sTma[rr])
+                        {
+                            asm volatile(
+                                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                                    SmemAddr(dst)),
+                                "l"(src + kc * M), "r"(static_cast<uint32_t>(n) * 4u), "r"(bar)
+                                : "memory");
+                        }
+                        else
+                        {
+                            for (int i = 0; i < n; i++)
+                            {
+                                dst[i] = (src != nullptr) ? __ldg(src + kc * M + i) : 0.0f;
+                            }
+                        }
+                        for (int i = n; i < M; i++)
+                        {
+                            dst[i] = 0.0f;  // padding past the line end (disjoint from the copy)
+                        }
                     }
                 }
-                else
+            }
+            if (tmaBytes > 0)
+            {
+                // every thread waits for the copies' bytes, suspended in
+                // try_wait between polls; bounded by kWaitLimitNs
+                const unsigned long long t0 = GlobalTimerNs();
+                uint32_t done = 0;
+                while (!done)
                 {
-                    for (int32_t y = tid; y < p.L; y += nthreads)
+                    asm volatile(
+                        "{ .reg .pred ok; mbarrier.try_wait.parity.shared::cta.b64 ok, [%1], 0, %2; selp.u32 %0, 1, 0, ok; }"
+                        : "=r"(done)
+                        : "r"(bar), "r"(1000000u)
+                        : "memory");
+                    if (!done && GlobalTimerNs() - t0 > kWaitLimitNs)
                     {
-                        float v = 0.0f;
-                        if (src != nullptr)
+                        s_fail = 1;
+                        break;
+                    }
+                }
+            }
+            if constexpr (SWZ)
+            {
+                // the lines just outside the grid: a wrapped line or a
+                // Dirichlet ghost line replaces the zeros of the tensor copy
+                for (int side = 0; side < 2; side++)
+                {
+                    const int32_t line = (side == 0) ? -1 : p.Nlines;
+                    const int rr = line - (x0 - 1);
+                    if (rr < 0 || rr >= nStaged)
+                    {
+                        continue;
+                    }
+                    const float *src = p.wrapLines ? p.in + static_cast<int64_t>((side == 0) ? p.Nlines - 1 : 0) * L
+                                                   : ((side == 0) ? p.ghostLo : p.ghostHi);
+                    if (src == nullptr)
+                    {
+                        continue;
+                    }
+                    for (int32_t pos = tid; pos < L; pos += nthreads)
+                    {
+                        sLines[SPos<SWZ>(rr, pos, P, p.LS)] = __ldg(src + pos);
+                    }
+                }
+            }
+            __syncthreads();
+            if (s_fail)
+            {
+                if (tid == 0)
+                {
+                    atomicExch(p.err, 1);
+                }
+                return;  // uniform: every thread saw the same flag after the barrier
+            }
+
+            // ---- 2a. right-hand sides, in place -----------------------------
+            // (I + r/2 L_cross) on every staged CTA line: each thread walks
+            // 16-byte units of all R+2 staged lines with a three-line window
+            // in registers and overwrites line ll+1 with its right-hand side
+            // (ExplicitDiffusion*2ADI, src/Pde/ADIequations.cpp:19-47, and the
+            // implicit-axis Dirichlet term ImplicitBoundarySource,
+            // ADIequations.h:198-220).
+            {
+                const bool hasGhost = (p.ghostLo != nullptr);
+                const int nUnits = P * (M / 4);
+                for (int u = tid; u < nUnits; u += nthreads)
+                {
+                    const int kk = u >> 3;
+                    const int q = u & 7;
+                    float4 up = Ld4(sLines + SOff4<SWZ>(0, kk, q, P, p.LS));
+                    float4 c = Ld4(sLines + SOff4<SWZ>(1, kk, q, P, p.LS));
+                    for (int ll = 0; ll < R; ll++)
+                    {
+                        const int32_t line = x0 + ll;
+                        const float4 dn = Ld4(sLines + SOff4<SWZ>(ll + 2, kk, q, P, p.LS));
+                        if (line < p.Nlines)
                         {
-                            v = __ldg(src + y);
+                            const float wUp = (line >= 1 || p.wrapLines) ? 1.0f : (hasGhost ? 2.0f : 0.0f);
+                            const float wDn = (line + 1 < p.Nlines || p.wrapLines) ? 1.0f : (hasGhost ? 2.0f : 0.0f);
+                            float4 z4;
+                            // centre + (d(+1) + d(-1)) * r / 2, the differences first
+                            z4.x = fmaf((dn.x - c.x) * wDn + (up.x - c.x) * wUp, p.halfR, c.x);
+                            z4.y = fmaf((dn.y - c.y) * wDn + (up.y - c.y) * wUp, p.halfR, c.y);
+                            z4.z = fmaf((dn.z - c.z) * wDn + (up.z - c.z) * wUp, p.halfR, c.z);
+                            z4.w = fmaf((dn.w - c.w) * wDn + (up.w - c.w) * wUp, p.halfR, c.w);
+                            if (p.implLo != nullptr)
+                            {
+                                const int32_t pos0 = 4 * u;
+                                if (pos0 == 0)
+                                {
+                                    z4.x = fmaf(p.r, __ldg(p.implLo + line), z4.x);
+                                }
+                                const int32_t last = L - 1 - pos0;  // component of position L-1
+                                if (last >= 0 && last < 4)
+                                {
+                                    const float add = p.r * __ldg(p.implHi + line);
+                                    z4.x += (last == 0) ? add : 0.0f;
+                                    z4.y += (last == 1) ? add : 0.0f;
+                                    z4.z += (last == 2) ? add : 0.0f;
+                                    z4.w += (last == 3) ? add : 0.0f;
+                                }
+                            }
+                            St4(sLines + SOff4<SWZ>(ll + 1, kk, q, P, p.LS), z4);
                         }
-                        else if (ghostRow != nullptr)
-                        {
-                            v = __ldg(ghostRow + y);
-                        }
-                        dst[PadIdx(y)] = v;
+                        up = c;
+                        c = dn;
                     }
                 }
             }
             __syncthreads();
 
-            const int rho = tid / P;
-            const int k = tid - rho * P;
-            const int32_t x = x0 + rho;
-            const bool active = (rho < p.R) && (x < p.xDim);
+            // ---- 2b. solve: thread -> (line pair g, chunk k) ---------------
+            const int g = tid / P;
+            const int k = tid - g * P;
             const int type = AdiBlockType(k, P);
             const float *cf = sCoef + type * kCoefCount * M;
-
-            float z[M];
-            if (active)
-            {
-                const int upMode = (x - 1 >= 0 || p.wrapX) ? kNbrGrid : ((p.ghost.xlo != nullptr) ? kNbrGhost : kNbrNone);
-                const int dnMode = (x + 1 < p.xDim || p.wrapX) ? kNbrGrid : ((p.ghost.xlo != nullptr) ? kNbrGhost : kNbrNone);
-                const float *rowC = sRows + (rho + 1) * p.LP + k * (M + 1);
-                const float *rowU = rowC - p.LP;
-                const float *rowD = rowC + p.LP;
+            const float a = p.plan.a;
+            float z[kNL][M];
+            bool act[kNL];
 #pragma unroll
-                for (int i = 0; i < M; i++)
+            for (int j = 0; j < kNL; j++)
+            {
+                const int ll = g * kNL + j;  // line within the CTA
+                act[j] = (ll < R) && (x0 + ll < p.Nlines);
+#pragma unroll
+                for (int q = 0; q < M / 4; q++)
                 {
-                    const int32_t y = k * M + i;
-                    const float c = rowC[i];
-                    // ExplicitDiffusionX2ADI order: x+1 then x-1
-                    float d = fmaf(NbrTerm(dnMode, rowD[i], c) + NbrTerm(upMode, rowU[i], c), p.halfR, c);
-                    if (p.ghost.ylo != nullptr && !p.plan.periodic)
-                    {
-                        if (y == 0)
-                        {
-                            d = fmaf(p.r, __ldg(p.ghost.ylo + x), d);
-                        }
-                        if (y == p.L - 1)
-                        {
-                            d = fmaf(p.r, __ldg(p.ghost.yhi + x), d);
-                        }
-                    }
-                    z[i] = (y < p.L) ? d : 0.0f;
+                    const float4 v = act[j] ? Ld4(sLines + SOff4<SWZ>(ll + 1, k, q, P, p.LS))
+                                            : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    z[j][4 * q + 0] = v.x;
+                    z[j][4 * q + 1] = v.y;
+                    z[j][4 * q + 2] = v.z;
+                    z[j][4 * q + 3] = v.w;
                 }
-                BlockSolve(z, cf);
-                const float a = p.plan.a;
+            }
+#pragma unroll
+            for (int j = 0; j < kNL; j++)
+            {
+                BlockSolve(z[j], cf);
+            }
+#pragma unroll
+            for (int j = 0; j < kNL; j++)
+            {
+                if (!act[j])
+                {
+                    continue;
+                }
+                const int ll = g * kNL + j;
                 if (k < P - 1)
                 {
-                    xA[rho * P + k] = fmaf(-a, z[M - 2], z[M - 1]);
+                    xA[ll * P + k] = fmaf(-a, z[j][M - 2], z[j][M - 1]);
                 }
                 if (k >= 1)
                 {
-                    xB[rho * P + k - 1] = -a * z[0];
-                }
-                if (p.plan.periodic && P > 1)
-                {
-                    if (k == 0)
-                    {
-                        xZ0[rho] = z[0];
-                    }
-                    if (k == P - 1)
-                    {
-                        xZL[rho] = SelectReg(z, p.plan.nlast - 1);
-                    }
+                    xB[ll * P + k - 1] = -a * z[j][0];
                 }
             }
             __syncthreads();
-            if (active)
+#pragma unroll
+            for (int j = 0; j < kNL; j++)
             {
-                const float *rA = xA + rho * P;
-                const float *rB = xB + rho * P;
+                if (!act[j])
+                {
+                    continue;
+                }
+                const int ll = g * kNL + j;
+                const float *rA = xA + ll * P;
+                const float *rB = xB + ll * P;
                 float sL = 0.0f, sR = 0.0f;
                 if (P > 1)
                 {
                     if (k < P - 1)
                     {
-                        sR = BandDot(p.plan, k, rA, rB, 1);
+                        sR = BandDot(p.plan, k, rA, rB);
                     }
                     if (k >= 1)
                     {
-                        sL = BandDot(p.plan, k - 1, rA, rB, 1);
+                        sL = BandDot(p.plan, k - 1, rA, rB);
                     }
                 }
-                const float *pv = cf + kCoefP * M;
-                const float *qv = cf + kCoefQ * M;
-#pragma unroll
-                for (int i = 0; i < M; i++)
-                {
-                    z[i] = fmaf(-sL, pv[i], fmaf(-sR, qv[i], z[i]));
-                }
+                BlockCorrect(z[j], cf, sL, sR);
                 if (k < P - 1)
                 {
-                    z[M - 1] = sR;
+                    z[j][M - 1] = sR;
                 }
-                if (p.plan.periodic)
-                {
-                    float y0, yl;
-                    if (P == 1)
-                    {
-                        y0 = z[0];
-                        yl = SelectReg(z, p.L - 1);
-                    }
-                    else
-                    {
-                        const float s0 = BandDot(p.plan, 0, rA, rB, 1);
-                        const float sl = BandDot(p.plan, P - 2, rA, rB, 1);
-                        y0 = xZ0[rho] - s0 * sCoef[0 * kCoefCount * M + kCoefQ * M + 0];
-                        yl = xZL[rho] - sl * sCoef[2 * kCoefCount * M + kCoefP * M + p.plan.nlast - 1];
-                    }
-                    const float factor = fmaf(yl, p.plan.bog, y0) * p.plan.invDenom;
+                // every staged-line read finished before the barrier above,
+                // so the line's buffer can take the solution
+                const int swo = Opaque(k & 7);
+                const int rowo = Opaque((ll + 1) * P + k);
 #pragma unroll
-                    for (int i = 0; i < M; i++)
-                    {
-                        const int32_t y = k * M + i;
-                        if (y < p.L)
-                        {
-                            z[i] = fmaf(-factor, __ldg(p.plan.zsm + y), z[i]);
-                        }
-                    }
-                }
-                // the halo reads of every thread finished before the barrier
-                // above, so the row buffer can take the solution
-                float *rowC = sRows + (rho + 1) * p.LP + k * (M + 1);
-#pragma unroll
-                for (int i = 0; i < M; i++)
+                for (int q = 0; q < M / 4; q++)
                 {
-                    rowC[i] = z[i];
+                    const int o = SWZ ? SOff4Row<SWZ>(rowo, k, q, swo, P, p.LS) : SOff4<SWZ>(ll + 1, k, q, P, p.LS);
+                    St4(sLines + o, make_float4(z[j][4 * q], z[j][4 * q + 1], z[j][4 * q + 2], z[j][4 * q + 3]));
                 }
             }
             __syncthreads();
 
-            // Commit, streamed row by row with coalesced accesses.
-            for (int rr = 0; rr < p.R; rr++)
+            // ---- 2c. periodic lines: Sherman-Morrison correction -----------
+            // x = y - factor * z_sm, factor = (y_0 + y_{L-1} beta/gamma) /
+            // (1 + z_sm,0 + z_sm,L-1 beta/gamma) (TdmaSolver::TDMAperiodic,
+            // include/Hal/Pde/TdmaSolver.h:112-119)
+            if (p.plan.periodic)
             {
-                const int32_t xr = x0 + rr;
-                if (xr >= p.xDim)
+                float *sFactor = xA;  // the exchange rows are free now
+                for (int ll = tid; ll < R; ll += nthreads)
                 {
-                    break;
+                    const float y0 = sLines[SPos<SWZ>(ll + 1, 0, P, p.LS)];
+                    const float yl = sLines[SPos<SWZ>(ll + 1, L - 1, P, p.LS)];
+                    sFactor[ll] = fmaf(yl, p.plan.bog, y0) * p.plan.invDenom;
                 }
-                const float *rowV = sRows + (rr + 1) * p.LP;
-                const int64_t rowBase = static_cast<int64_t>(xr) * p.L;
-                for (int32_t y = tid; y < p.L; y += nthreads)
+                __syncthreads();
+                const int nUnits = P * (M / 4);
+                for (int u = tid; u < nUnits; u += nthreads)
                 {
-                    const float v = rowV[PadIdx(y)];
-                    const int64_t i = rowBase + y;
-                    if constexpr (MODE == kRowPlain)
+                    const int kk = u >> 3;
+                    const int q = u & 7;
+                    float zs[4];
+#pragma unroll
+                    for (int e = 0; e < 4; e++)
                     {
-                        p.out[i] = v;
+                        const int32_t pos = 4 * u + e;
+                        zs[e] = (pos < L) ? __ldg(p.plan.zsm + pos) : 0.0f;
                     }
-                    else if constexpr (MODE == kRowDeltas)
+                    for (int ll = 0; ll < R; ll++)
                     {
-                        const double fv = p.f[i];
-                        p.deltas[i] = p.deltas[i] + (static_cast<double>(v) - fv);
-                    }
-                    else
-                    {
-                        const float fv = static_cast<float>(p.f[i]);
-                        float d = v - fv;
-                        d = fmaf(fv, p.negDecay, d);
-                        if (p.src != nullptr)
+                        if (x0 + ll >= p.Nlines)
                         {
-                            d += __ldg(p.src + i);
+                            break;
                         }
-                        if (p.cellOffsets != nullptr)
-                        {
-                            const int32_t n = __ldg(p.cellOffsets + i + 1) - __ldg(p.cellOffsets + i);
-                            d = fmaf(fv, p.negUptake * static_cast<float>(n), d);
-                        }
-                        p.out[i] = fv + d;
+                        const float fct = sFactor[ll];
+                        float *at = sLines + SOff4<SWZ>(ll + 1, kk, q, P, p.LS);
+                        float4 v = Ld4(at);
+                        v.x = fmaf(-fct, zs[0], v.x);
+                        v.y = fmaf(-fct, zs[1], v.y);
+                        v.z = fmaf(-fct, zs[2], v.z);
+                        v.w = fmaf(-fct, zs[3], v.w);
+                        St4(at, v);
                     }
+                }
+                __syncthreads();
+            }
+
+            // ---- 3. write out ---------------------------------------------
+            if constexpr (MODE == kSweepDeltas)
+            {
+                for (int ll = 0; ll < R; ll++)
+                {
+                    const int32_t line = x0 + ll;
+                    if (line >= p.Nlines)
+                    {
+                        break;
+                    }
+                    const int64_t base = static_cast<int64_t>(line) * L;
+                    for (int32_t pos = tid; pos < L; pos += nthreads)
+                    {
+                        const double v = static_cast<double>(sLines[SPos<SWZ>(ll + 1, pos, P, p.LS)]);
+                        p.deltas[base + pos] = p.deltas[base + pos] + (v - p.f64[base + pos]);
+                    }
+                }
+            }
+            else
+            {
+                // thread -> group qd of 4 lines; out[pos * Nlines + line]
+                const int Q = R >> 2;                   // a power of two <= 32
+                const int qd = tid & (Q - 1);
+                const int32_t line0 = x0 + 4 * qd;
+                const int step = nthreads / Q;
+                const bool vecOut = (p.Nlines & 3) == 0;
+                const bool quadOk = line0 < p.Nlines;
+                if (vecOut && vecL)
+                {
+                    // 16-byte units: 4 positions x 4 lines move as a 4x4 block
+                    // (4 LDS.128, a register transpose, 4 STG.128)
+                    const int32_t nU = L >> 2;
+                    constexpr int kUB = 2;
+                    for (int32_t u0 = tid / Q; u0 < nU && quadOk; u0 += kUB * step)
+                    {
+                        float4 o[kUB][4];
+                        float4 fv[kUB][4], sv[kUB][4];
+#pragma unroll
+                        for (int b = 0; b < kUB; b++)
+                        {
+                            const int32_t u = u0 + b * step;
+                            const bool ok = u < nU;
+                            const int kk = u >> 3;
+                            const int q = u & 7;
+                            float4 a[4];
+#pragma unroll
+                            for (int e = 0; e < 4; e++)
+                            {
+                                a[e] = ok ? Ld4(sLines + SOff4<SWZ>(4 * qd + 1 + e, kk, q, P, p.LS))
+                                          : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                            }
+                            o[b][0] = make_float4(a[0].x, a[1].x, a[2].x, a[3].x);
+                            o[b][1] = make_float4(a[0].y, a[1].y, a[2].y, a[3].y);
+                            o[b][2] = make_float4(a[0].z, a[1].z, a[2].z, a[3].z);
+                            o[b][3] = make_float4(a[0].w, a[1].w, a[2].w, a[3].w);
+#pragma unroll
+                            for (int i = 0; i < 4; i++)
+                            {
+                                fv[b][i] = sv[b][i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                            }
+                            if constexpr (MODE == kSweepTick)
+                            {
+                                if (ok)
+                                {
+#pragma unroll
+                                    for (int i = 0; i < 4; i++)
+                                    {
+                                        const int64_t gi = static_cast<int64_t>(4 * u + i) * p.Nlines + line0;
+                                        fv[b][i] = __ldg(reinterpret_cast<const float4 *>(p.f + gi));
+                                        if (p.src != nullptr)
+                                        {
+                                            sv[b][i] = __ldg(reinterpret_cast<const float4 *>(p.src + gi));
+                                        }
+                                    }
+                                }
+                            }
+                        }
+#pragma unroll
+                        for (int b = 0; b < kUB; b++)
+                        {
+                            const int32_t u = u0 + b * step;
+                            if (u >= nU)
+                            {
+                                continue;
+                            }
+#pragma unroll
+                            for (int i = 0; i < 4; i++)
+                            {
+                                float4 w4 = o[b][i];
+                                if constexpr (MODE == kSweepTick)
+                                {
+                                    // per-agent uptake counts of the 4 lines at position 4u+i
+                                    int32_t n0 = 0, n1 = 0, n2 = 0, n3 = 0;
+                                    if (p.cellOffsets != nullptr)
+                                    {
+                                        const int64_t ci = static_cast<int64_t>(line0) * L + 4 * u + i;
+                                        n0 = __ldg(p.cellOffsets + ci + 1) - __ldg(p.cellOffsets + ci);
+                                        n1 = __ldg(p.cellOffsets + ci + L + 1) - __ldg(p.cellOffsets + ci + L);
+                                        n2 = __ldg(p.cellOffsets + ci + 2 * L + 1) - __ldg(p.cellOffsets + ci + 2 * L);
+                                        n3 = __ldg(p.cellOffsets + ci + 3 * L + 1) - __ldg(p.cellOffsets + ci + 3 * L);
+                                    }
+                                    auto commit = [&](float vv, float f0, float s0, int32_t nv) {
+                                        float d = vv - f0;
+                                        d = fmaf(f0, p.negDecay, d);
+                                        d += s0;
+                                        d = fmaf(f0, p.negUptake * static_cast<float>(nv), d);
+                                        return f0 + d;
+                                    };
+                                    w4.x = commit(w4.x, fv[b][i].x, sv[b][i].x, n0);
+                                    w4.y = commit(w4.y, fv[b][i].y, sv[b][i].y, n1);
+                                    w4.z = commit(w4.z, fv[b][i].z, sv[b][i].z, n2);
+                                    w4.w = commit(w4.w, fv[b][i].w, sv[b][i].w, n3);
+                                }
+                                St4(p.out + static_cast<int64_t>(4 * u + i) * p.Nlines + line0, w4);
+                            }
+                        }
+                    }
+                    return;
+                }
+                constexpr int kBatch = 2;
+                for (int32_t pos0 = tid / Q; pos0 < L && quadOk; pos0 += kBatch * step)
+                {
+                    float4 v[kBatch], fv[kBatch], sv[kBatch];
+                    int32_t nn[kBatch][4];
+#pragma unroll
+                    for (int b = 0; b < kBatch; b++)
+                    {
+                        const int32_t pos = pos0 + b * step;
+                        v[b] = fv[b] = sv[b] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                        nn[b][0] = nn[b][1] = nn[b][2] = nn[b][3] = 0;
+                        if (pos < L)
+                        {
+                            v[b] = make_float4(sLines[SPos<SWZ>(4 * qd + 1, pos, P, p.LS)],
+                                               sLines[SPos<SWZ>(4 * qd + 2, pos, P, p.LS)],
+                                               sLines[SPos<SWZ>(4 * qd + 3, pos, P, p.LS)],
+                                               sLines[SPos<SWZ>(4 * qd + 4, pos, P, p.LS)]);
+                            if constexpr (MODE == kSweepTick)
+                            {
+                                const int64_t gi = static_cast<int64_t>(pos) * p.Nlines + line0;
+                                if (vecOut)
+                                {
+                                    fv[b] = __ldg(reinterpret_cast<const float4 *>(p.f + gi));
+                                    if (p.src != nullptr)
+                                    {
+                                        sv[b] = __ldg(reinterpret_cast<const float4 *>(p.src + gi));
+                                    }
+                                }
+                                else
+                                {
+                                    float tf[4] = {0, 0, 0, 0}, ts[4] = {0, 0, 0, 0};
+#pragma unroll
+                                    for (int e = 0; e < 4; e++)
+                                    {
+                                        if (line0 + e < p.Nlines)
+                                        {
+                                            tf[e] = __ldg(p.f + gi + e);
+                                            ts[e] = (p.src != nullptr) ? __ldg(p.src + gi + e) : 0.0f;
+                                        }
+                                    }
+                                    fv[b] = make_float4(tf[0], tf[1], tf[2], tf[3]);
+                                    sv[b] = make_float4(ts[0], ts[1], ts[2], ts[3]);
+                                }
+                                if (p.cellOffsets != nullptr)
+                                {
+#pragma unroll
+                                    for (int e = 0; e < 4; e++)
+                                    {
+                                        if (line0 + e < p.Nlines)
+                                        {
+                                            const int64_t ci = static_cast<int64_t>(line0 + e) * L + pos;
+                                            nn[b][e] = __ldg(p.cellOffsets + ci + 1) - __ldg(p.cellOffsets + ci);
+                                        }
+                                    }
+                                }
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int b = 0; b < kBatch; b++)
+                    {
+                        const int32_t pos = pos0 + b * step;
+                        if (pos >= L)
+                        {
+                            continue;
+                        }
+                        float4 o = v[b];
+                        if constexpr (MODE == kSweepTick)
+                        {
+                            auto commit = [&](float vv, float f0, float s0, int32_t n0) {
+                                float d = vv - f0;
+                                d = fmaf(f0, p.negDecay, d);
+                                d += s0;
+                                d = fmaf(f0, p.negUptake * static_cast<float>(n0), d);
+                                return f0 + d;
+                            };
+                            o.x = commit(v[b].x, fv[b].x, sv[b].x, nn[b][0]);
+                            o.y = commit(v[b].y, fv[b].y, sv[b].y, nn[b][1]);
+                            o.z = commit(v[b].z, fv[b].z, sv[b].z, nn[b][2]);
+                            o.w = commit(v[b].w, fv[b].w, sv[b].w, nn[b][3]);
+                        }
+                        const int64_t gi = static_cast<int64_t>(pos) * p.Nlines + line0;
+                        if (vecOut)
+                        {
+                            St4(p.out + gi, o);
+                        }
+                        else
+                        {
+                            const float t[4] = {o.x, o.y, o.z, o.w};
+#pragma unroll
+                            for (int e = 0; e < 4; e++)
+                            {
+                                if (line0 + e < p.Nlines)
+                                {
+                                    p.out[gi + e] = t[e];
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+        }
+
+        // out[c][r] = in[r][c] for an rows x cols matrix (32x32 tiles).
+        template <typename TIn>
+        __global__ void Transpose(const TIn *__restrict__ in, float *__restrict__ out, int32_t rows, int32_t cols)
+        {
+            __shared__ float tile[32][33];
+            const int32_t c0 = blockIdx.x * 32;
+            const int32_t r0 = blockIdx.y * 32;
+            for (int j = threadIdx.y; j < 32; j += blockDim.y)
+            {
+                const int32_t r = r0 + j;
+                const int32_t c = c0 + threadIdx.x;
+                if (r < rows && c < cols)
+                {
+                    tile[j][threadIdx.x] = static_cast<float>(in[static_cast<int64_t>(r) * cols + c]);
+                }
+            }
+            __syncthreads();
+            for (int j = threadIdx.y; j < 32; j += blockDim.y)
+            {
+                const int32_t c = c0 + j;
+                const int32_t r = r0 + threadIdx.x;
+                if (r < rows && c < cols)
+                {
+                    out[static_cast<int64_t>(c) * rows + r] = tile[threadIdx.x][j];
                 }
             }
         }
@@ -695,28 +940,98 @@ namespace halcuda
             return HAL_CUDA_OK;
         }
 
-        size_t RowSmemBytes(int32_t R, int32_t LP, int32_t P)
+        // Launch shape of a sweep over lines of length L: lines per CTA R (a
+        // power of two >= 8, so the transposed stores cover whole 32-byte
+        // sectors), threads = (R / kNL) * P.  swz: the staged lines use the
+        // 128-byte-swizzled tensor layout (L % 256 == 0).
+        struct SweepShape
         {
-            return sizeof(float) * (static_cast<size_t>(kCoefFloats) + static_cast<size_t>(R + 2) * LP +
-                                    2 * static_cast<size_t>(R) * P + 2 * static_cast<size_t>(R));
+            int32_t R, threads, LS;
+            size_t smem;
+        };
+
+        SweepShape ShapeFor(int32_t P, int32_t Nlines, bool swz)
+        {
+            SweepShape s;
+            // The largest power of two (<= kMaxR, <= 1024/P threads-wise)
+            // that still gives enough CTAs to cover the SMs: longer line
+            // groups make the transposed stores longer contiguous segments.
+            int32_t R = 8;
+            while (R * 2 <= 1024 / P && R * 2 <= kMaxR && (Nlines + 2 * R - 1) / (2 * R) >= 120)
+            {
+                R *= 2;
+            }
+            s.R = R;
+            s.threads = ((R / kNL) * P + 31) & ~31;
+            s.LS = swz ? P * M : P * kChunkStride + 4;  // padded: lines 4 mod 32 banks apart
+            s.smem = 1024 + sizeof(float) * (static_cast<size_t>(kCoefFloats) + static_cast<size_t>(R + 2) * s.LS +
+                                             2 * static_cast<size_t>(R) * P + 2 * static_cast<size_t>(R));
+            return s;
         }
 
-        template <typename TF, int MODE>
-        int EnableRowSmem(size_t bytes)
+        template <int MODE, bool SWZ>
+        int EnableSweepSmem(size_t bytes)
         {
             static size_t s_enabled = 0;
             if (bytes > s_enabled)
             {
-                HAL_TRY(CudaStatus(cudaFuncSetAttribute(AdiRowSweep<TF, MODE>,
+                HAL_TRY(CudaStatus(cudaFuncSetAttribute(AdiSweep<MODE, SWZ>,
                                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                         static_cast<int>(bytes)),
-                                   "cudaFuncSetAttribute(AdiRowSweep)"));
+                                   "cudaFuncSetAttribute(AdiSweep)"));
                 s_enabled = bytes;
             }
             return HAL_CUDA_OK;
         }
-    }
 
+        template <int MODE>
+        int EnableSweepSmemBoth(int32_t P, int32_t Nlines)
+        {
+            HAL_TRY((EnableSweepSmem<MODE, true>(ShapeFor(P, Nlines, true).smem)));
+            return EnableSweepSmem<MODE, false>(ShapeFor(P, Nlines, false).smem);
+        }
+
+        // cuTensorMapEncodeTiled through the runtime's driver entry point.
+        PFN_cuTensorMapEncodeTiled_v12000 TensorMapEncoder()
+        {
+            static PFN_cuTensorMapEncodeTiled_v12000 s_fn = nullptr;
+            static bool s_tried = false;
+            if (!s_tried)
+            {
+                s_tried = true;
+                void *fn = nullptr;
+                cudaDriverEntryPointQueryResult q;
+                if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                        cudaSuccess &&
+                    q == cudaDriverEntryPointSuccess)
+                {
+                    s_fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+                }
+            }
+            return s_fn;
+        }
+
+        // Tensor map over Nlines lines of L floats (L % 256 == 0) seen as
+        // [line][chunk][32], box = (R+2) lines x P chunks x 32, 128-byte
+        // swizzle, zero fill outside the tensor.
+        bool MakeLineTensorMap(CUtensorMap &map, const float *base, int32_t L, int32_t Nlines, int32_t R)
+        {
+            PFN_cuTensorMapEncodeTiled_v12000 enc = TensorMapEncoder();
+            if (enc == nullptr || (L % (8 * M)) != 0 || (reinterpret_cast<uintptr_t>(base) & 15) != 0)
+            {
+                return false;
+            }
+            const cuuint64_t P = static_cast<cuuint64_t>(L / M);
+            cuuint64_t gdim[3] = {static_cast<cuuint64_t>(M), P, static_cast<cuuint64_t>(Nlines)};
+            cuuint64_t gstride[2] = {static_cast<cuuint64_t>(M) * 4u, static_cast<cuuint64_t>(L) * 4u};
+            cuuint32_t box[3] = {static_cast<cuuint32_t>(M), static_cast<cuuint32_t>(P), static_cast<cuuint32_t>(R + 2)};
+            cuuint32_t estr[3] = {1, 1, 1};
+            CUresult r = enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(base), gdim, gstride, box,
+                             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            return r == CUDA_SUCCESS;
+        }
+    }
 }
 
 struct hal_cuda_agents;  // agents.cu
@@ -731,19 +1046,25 @@ namespace halcuda
         int32_t xDim = 0, yDim = 0;
         int device = 0;
         StreamSlot stream;
-        DevBuf<float> field[2];
+        DevBuf<float> field[2];  // layout B (y*xDim + x)
         int cur = 0;
-        DevBuf<float> w;
-        DevBuf<float> src;
+        DevBuf<float> w;         // x-sweep output, layout A; also staging for uploads
+        DevBuf<float> src;       // layout B
         bool hasSrc = false;
-        DevBuf<float> ghost;
+        DevBuf<float> ghost;     // ghost table (hal_cuda.h layout)
         bool hasGhost = false;
         DevBuf<double> f64, d64;
-        DevBuf<float> g32;  // ghost table of the FP64 interface call, in float
+        DevBuf<float> g32;       // ghost table of the FP64 interface call, in float
+        DevBuf<int32_t> err;
         const hal_cuda_agents *agents = nullptr;
         double uptake = 0.0;
         std::map<std::string, std::unique_ptr<LinePlanBuf>> plans;
         GraphCache graph[2];  // by the parity of the starting buffer
+        // TMA tensor maps of the staged lines: x-sweep input field[0] /
+        // field[1] (lines along x), y-sweep input w (lines along y)
+        CUtensorMap tmapX[2];
+        CUtensorMap tmapY;
+        bool swzX = false, swzY = false;
 
         void ResetGraphs()
         {
@@ -762,7 +1083,16 @@ namespace halcuda
             HAL_TRY(field[0].Alloc(n, "cudaMalloc(field)"));
             HAL_TRY(field[1].Alloc(n, "cudaMalloc(field)"));
             HAL_TRY(w.Alloc(n, "cudaMalloc(scratch)"));
+            HAL_TRY(err.Alloc(1, "cudaMalloc(err)"));
             HAL_TRY(CudaStatus(cudaMemset(field[0].p, 0, n * sizeof(float)), "cudaMemset"));
+            HAL_TRY(CudaStatus(cudaMemset(err.p, 0, sizeof(int32_t)), "cudaMemset"));
+            std::memset(tmapX, 0, sizeof(tmapX));
+            std::memset(&tmapY, 0, sizeof(tmapY));
+            const int32_t Px = (xDim + M - 1) / M, Py = (yDim + M - 1) / M;
+            const int32_t Rx = ShapeFor(Px, yDim, true).R, Ry = ShapeFor(Py, xDim, true).R;
+            swzX = MakeLineTensorMap(tmapX[0], field[0].p, xDim, yDim, Rx) &&
+                   MakeLineTensorMap(tmapX[1], field[1].p, xDim, yDim, Rx);
+            swzY = MakeLineTensorMap(tmapY, w.p, yDim, xDim, Ry);
             return HAL_CUDA_OK;
         }
 
@@ -780,7 +1110,7 @@ namespace halcuda
             {
                 if (plans.size() > 16)
                 {
-                    // plans captured in the cached graph may be freed
+                    // plans captured in the cached graphs may be freed
                     HAL_TRY(CudaStatus(cudaStreamSynchronize(stream.Get()), "cudaStreamSynchronize"));
                     ResetGraphs();
                     plans.clear();
@@ -793,59 +1123,108 @@ namespace halcuda
             return HAL_CUDA_OK;
         }
 
-        template <typename TIn>
-        int LaunchColumn(const TIn *f, double r, bool wrapX, bool wrapY, const float *ghostTab,
-                         cudaStream_t s)
+        // Checks (and clears) the device error flag of the bounded waits.
+        int CheckDeviceError(const char *who)
         {
-            const LinePlanDev *pl = nullptr;
-            int ends = wrapX ? kEndsPeriodic : (ghostTab ? kEndsDirichlet : kEndsZeroFlux);
-            HAL_TRY(Plan(xDim, r, ends, &pl));
-            ColParams<TIn> p;
-            p.f = f;
-            p.w = w.p;
-            p.L = xDim;
-            p.ncols = yDim;
-            p.halfR = static_cast<float>(r / 2.0);
-            p.r = static_cast<float>(r);
-            p.wrapY = wrapY;
-            p.ghost = MakeGhostView(ghostTab, xDim, yDim);
-            p.plan = *pl;
-            const int P = pl->P;
-            int K = (P + 7) / 8;
-            if (K > 8)
+            int32_t h = 0;
+            HAL_TRY(CudaStatus(cudaMemcpyAsync(&h, err.p, sizeof(int32_t), cudaMemcpyDeviceToHost, stream.Get()),
+                               "cudaMemcpy(err)"));
+            HAL_TRY(CudaStatus(cudaStreamSynchronize(stream.Get()), who));
+            if (h != 0)
             {
-                K = 8;
+                cudaMemsetAsync(err.p, 0, sizeof(int32_t), stream.Get());
+                SetError("%s: a staged copy did not complete within its wait limit", who);
+                return HAL_CUDA_ETIMEOUT;
             }
-            int W = (P + K - 1) / K;
-            cudaLaunchConfig_t cfg = {};
-            cfg.gridDim = dim3(K, (yDim + 31) / 32, 1);
-            cfg.blockDim = dim3(32, W, 1);
-            cfg.dynamicSmemBytes = 0;
-            cfg.stream = s;
-            cudaLaunchAttribute attr[1];
-            attr[0].id = cudaLaunchAttributeClusterDimension;
-            attr[0].val.clusterDim.x = K;
-            attr[0].val.clusterDim.y = 1;
-            attr[0].val.clusterDim.z = 1;
-            cfg.attrs = attr;
-            cfg.numAttrs = 1;
-            cudaError_t e = cudaLaunchKernelEx(&cfg, AdiColumnSweep<TIn>, p);
-            CountLaunch();
-            return CudaStatus(e, "AdiColumnSweep launch");
+            return HAL_CUDA_OK;
         }
 
-        template <typename TF, int MODE>
-        int LaunchRow(const TF *f, float *out, double *deltas, double r, double decay, bool wrapX,
-                      bool wrapY, const float *ghostTab, bool extras, cudaStream_t s)
+        template <typename TIn>
+        int TransposeTo(const TIn *in, float *out, int32_t rows, int32_t cols, cudaStream_t s)
+        {
+            dim3 block(32, 8);
+            dim3 grid((cols + 31) / 32, (rows + 31) / 32);
+            Transpose<TIn><<<grid, block, 0, s>>>(in, out, rows, cols);
+            CountLaunch();
+            return LaunchStatus("Transpose launch");
+        }
+
+        template <int MODE>
+        int LaunchSweep(SweepParams &p, cudaStream_t s, const CUtensorMap *tmap)
+        {
+            const bool swz = (tmap != nullptr);
+            SweepShape sh = ShapeFor(p.plan.P, p.Nlines, swz);
+            p.R = sh.R;
+            p.LS = sh.LS;
+            unsigned blocks = static_cast<unsigned>((p.Nlines + sh.R - 1) / sh.R);
+            if (swz)
+            {
+                HAL_TRY((EnableSweepSmem<MODE, true>(sh.smem)));
+                AdiSweep<MODE, true><<<blocks, sh.threads, sh.smem, s>>>(p, *tmap);
+            }
+            else
+            {
+                CUtensorMap none;
+                std::memset(&none, 0, sizeof(none));
+                HAL_TRY((EnableSweepSmem<MODE, false>(sh.smem)));
+                AdiSweep<MODE, false><<<blocks, sh.threads, sh.smem, s>>>(p, none);
+            }
+            CountLaunch();
+            return LaunchStatus("AdiSweep launch");
+        }
+
+        // x-sweep: lines along x (layout B input), w out in layout A.
+        int LaunchX(const float *fB, double r, bool wrapX, bool wrapY, const float *ghostTab, cudaStream_t s)
         {
             const LinePlanDev *pl = nullptr;
-            int ends = wrapY ? kEndsPeriodic : (ghostTab ? kEndsDirichlet : kEndsZeroFlux);
+            const int ends = wrapX ? kEndsPeriodic : (ghostTab ? kEndsDirichlet : kEndsZeroFlux);
+            HAL_TRY(Plan(xDim, r, ends, &pl));
+            GhostView gv = MakeGhostView(ghostTab, xDim, yDim);
+            SweepParams p = {};
+            p.in = fB;
+            p.L = xDim;
+            p.Nlines = yDim;
+            p.wrapLines = wrapY;
+            p.ghostLo = (!wrapY) ? gv.ylo : nullptr;  // bc(x, -1) for every x
+            p.ghostHi = (!wrapY) ? gv.yhi : nullptr;
+            p.implLo = (!wrapX) ? gv.xlo : nullptr;   // bc(-1, y) for every line y
+            p.implHi = (!wrapX) ? gv.xhi : nullptr;
+            p.halfR = static_cast<float>(r / 2.0);
+            p.r = static_cast<float>(r);
+            p.plan = *pl;
+            p.out = w.p;
+            p.err = err.p;
+            const CUtensorMap *tm = nullptr;
+            if (swzX)
+            {
+                tm = (fB == field[0].p) ? &tmapX[0] : ((fB == field[1].p) ? &tmapX[1] : nullptr);
+            }
+            return LaunchSweep<kSweepW>(p, s, tm);
+        }
+
+        // y-sweep: lines along y (w in layout A).
+        template <int MODE>
+        int LaunchY(float *outB, const float *fB, const double *f64, double *deltas, double r, double decay,
+                    bool wrapX, bool wrapY, const float *ghostTab, bool extras, cudaStream_t s)
+        {
+            const LinePlanDev *pl = nullptr;
+            const int ends = wrapY ? kEndsPeriodic : (ghostTab ? kEndsDirichlet : kEndsZeroFlux);
             HAL_TRY(Plan(yDim, r, ends, &pl));
-            RowParams<TF> p;
-            p.w = w.p;
-            p.f = f;
-            p.out = out;
-            p.deltas = deltas;
+            GhostView gv = MakeGhostView(ghostTab, xDim, yDim);
+            SweepParams p = {};
+            p.in = w.p;
+            p.L = yDim;
+            p.Nlines = xDim;
+            p.wrapLines = wrapX;
+            p.ghostLo = (!wrapX) ? gv.xlo : nullptr;  // bc(-1, y) for every y
+            p.ghostHi = (!wrapX) ? gv.xhi : nullptr;
+            p.implLo = (!wrapY) ? gv.ylo : nullptr;   // bc(x, -1) for every line x
+            p.implHi = (!wrapY) ? gv.yhi : nullptr;
+            p.halfR = static_cast<float>(r / 2.0);
+            p.r = static_cast<float>(r);
+            p.plan = *pl;
+            p.out = outB;
+            p.f = fB;
             p.src = (extras && hasSrc) ? src.p : nullptr;
             p.cellOffsets = nullptr;
             p.negUptake = 0.0f;
@@ -856,42 +1235,36 @@ namespace halcuda
                 p.negUptake = static_cast<float>(-uptake);
             }
             p.negDecay = static_cast<float>(-decay);
-            p.xDim = xDim;
-            p.L = yDim;
-            p.halfR = static_cast<float>(r / 2.0);
-            p.r = static_cast<float>(r);
-            p.wrapX = wrapX;
-            p.ghost = MakeGhostView(ghostTab, xDim, yDim);
-            p.plan = *pl;
-            const int P = pl->P;
-            int R = kRowThreads / P;
-            if (R < 1)
-            {
-                R = 1;
-            }
-            p.R = R;
-            p.LP = P * (M + 1);
-            int threads = ((R * P + 31) / 32) * 32;
-            size_t smem = RowSmemBytes(R, p.LP, P);
-            HAL_TRY((EnableRowSmem<TF, MODE>(smem)));
-            unsigned blocks = static_cast<unsigned>((xDim + R - 1) / R);
-            AdiRowSweep<TF, MODE><<<blocks, threads, smem, s>>>(p);
-            CountLaunch();
-            return LaunchStatus("AdiRowSweep launch");
+            p.f64 = f64;
+            p.deltas = deltas;
+            p.err = err.p;
+            return LaunchSweep<MODE>(p, s, swzY ? &tmapY : nullptr);
         }
 
-        int EnqueueTick(int c, double r, double decay, bool wrapX, bool wrapY, bool extras, int mode,
-                        cudaStream_t s)
+        // Sets the shared-memory limits of both sweeps before a graph
+        // capture (the attribute call is not a stream operation).
+        int PrepareShapes(double r, bool wrapX, bool wrapY, const float *g)
         {
-            const float *g = (mode != kRowPlain && hasGhost) ? ghost.p : nullptr;
-            HAL_TRY(LaunchColumn<float>(field[c].p, r, wrapX, wrapY, g, s));
-            if (mode == kRowPlain)
+            const LinePlanDev *px = nullptr, *py = nullptr;
+            HAL_TRY(Plan(xDim, r, wrapX ? kEndsPeriodic : (g ? kEndsDirichlet : kEndsZeroFlux), &px));
+            HAL_TRY(Plan(yDim, r, wrapY ? kEndsPeriodic : (g ? kEndsDirichlet : kEndsZeroFlux), &py));
+            HAL_TRY(EnableSweepSmemBoth<kSweepW>(px->P, yDim));
+            HAL_TRY(EnableSweepSmemBoth<kSweepTick>(py->P, xDim));
+            HAL_TRY(EnableSweepSmemBoth<kSweepPlain>(py->P, xDim));
+            return HAL_CUDA_OK;
+        }
+
+        int EnqueueTick(int c, double r, double decay, bool wrapX, bool wrapY, bool plain, cudaStream_t s)
+        {
+            const float *g = (!plain && hasGhost) ? ghost.p : nullptr;
+            HAL_TRY(LaunchX(field[c].p, r, wrapX, wrapY, g, s));
+            if (plain)
             {
-                return LaunchRow<float, kRowPlain>(field[c].p, field[c ^ 1].p, nullptr, r, decay, wrapX, wrapY,
-                                                   nullptr, false, s);
+                return LaunchY<kSweepPlain>(field[c ^ 1].p, field[c].p, nullptr, nullptr, r, decay, wrapX, wrapY,
+                                            nullptr, false, s);
             }
-            return LaunchRow<float, kRowTick>(field[c].p, field[c ^ 1].p, nullptr, r, decay, wrapX, wrapY, g,
-                                              extras, s);
+            return LaunchY<kSweepTick>(field[c ^ 1].p, field[c].p, nullptr, nullptr, r, decay, wrapX, wrapY, g,
+                                       true, s);
         }
 
         int RunTicks(int32_t ticks, double r, double decay, bool wrapX, bool wrapY, bool plain)
@@ -901,29 +1274,16 @@ namespace halcuda
                 return HAL_CUDA_OK;
             }
             cudaStream_t s = stream.Get();
-            // make sure both plans exist before capture (no allocation inside)
-            const LinePlanDev *pl = nullptr;
             const float *g = (!plain && hasGhost) ? ghost.p : nullptr;
-            HAL_TRY(Plan(xDim, r, wrapX ? kEndsPeriodic : (g ? kEndsDirichlet : kEndsZeroFlux), &pl));
-            HAL_TRY(Plan(yDim, r, wrapY ? kEndsPeriodic : (g ? kEndsDirichlet : kEndsZeroFlux), &pl));
+            HAL_TRY(PrepareShapes(r, wrapX, wrapY, g));
             char key[256];
             snprintf(key, sizeof(key), "%d|%a|%a|%d|%d|%d|%d|%d|%p|%p|%a", ticks, r, decay, wrapX, wrapY,
-                     plain ? 1 : 0, hasSrc, hasGhost, static_cast<void *>(s),
-                     static_cast<const void *>(agents), uptake);
+                     plain ? 1 : 0, hasSrc, hasGhost, static_cast<void *>(s), static_cast<const void *>(agents),
+                     uptake);
             GraphCache &graph = this->graph[cur];
             if (graph.exec == nullptr || graph.key != key)
             {
                 graph.Reset();
-                // Warm the per-kernel shared-memory attribute outside capture.
-                {
-                    const LinePlanDev *py = nullptr;
-                    HAL_TRY(Plan(yDim, r, wrapY ? kEndsPeriodic : (g ? kEndsDirichlet : kEndsZeroFlux), &py));
-                    int R = kRowThreads / py->P;
-                    R = R < 1 ? 1 : R;
-                    size_t smem = RowSmemBytes(R, py->P * (M + 1), py->P);
-                    HAL_TRY((EnableRowSmem<float, kRowTick>(smem)));
-                    HAL_TRY((EnableRowSmem<float, kRowPlain>(smem)));
-                }
                 cudaGraph_t gr = nullptr;
                 HAL_TRY(CudaStatus(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal),
                                    "cudaStreamBeginCapture"));
@@ -931,7 +1291,7 @@ namespace halcuda
                 int rc = HAL_CUDA_OK;
                 for (int32_t t = 0; t < ticks && rc == HAL_CUDA_OK; t++)
                 {
-                    rc = EnqueueTick(c, r, decay, wrapX, wrapY, true, plain ? kRowPlain : kRowTick, s);
+                    rc = EnqueueTick(c, r, decay, wrapX, wrapY, plain, s);
                     c ^= 1;
                 }
                 cudaError_t e = cudaStreamEndCapture(s, &gr);
@@ -957,6 +1317,35 @@ namespace halcuda
             cur ^= (ticks & 1);
             return HAL_CUDA_OK;
         }
+
+        // Host field (layout A) -> field[cur] (layout B).
+        int Upload(const float *host, cudaStream_t s)
+        {
+            HAL_TRY(CudaStatus(cudaMemcpyAsync(w.p, host, Length() * sizeof(float), cudaMemcpyHostToDevice, s),
+                               "cudaMemcpy(field)"));
+            return TransposeTo<float>(w.p, field[cur].p, xDim, yDim, s);
+        }
+
+        // field[cur] (layout B) -> host (layout A).
+        int Download(float *host, cudaStream_t s)
+        {
+            HAL_TRY(TransposeTo<float>(field[cur].p, w.p, yDim, xDim, s));
+            return CudaStatus(cudaMemcpyAsync(host, w.p, Length() * sizeof(float), cudaMemcpyDeviceToHost, s),
+                              "cudaMemcpy(field)");
+        }
+
+        int UploadSource(const float *host, cudaStream_t s)
+        {
+            if (src.p == nullptr)
+            {
+                HAL_TRY(src.Alloc(Length(), "cudaMalloc(src)"));
+            }
+            HAL_TRY(CudaStatus(cudaMemcpyAsync(w.p, host, Length() * sizeof(float), cudaMemcpyHostToDevice, s),
+                               "cudaMemcpy(src)"));
+            HAL_TRY(TransposeTo<float>(w.p, src.p, xDim, yDim, s));
+            hasSrc = true;
+            return HAL_CUDA_OK;
+        }
     };
 }
 
@@ -971,6 +1360,8 @@ extern "C" int hal_cuda_adi_create(int32_t xDim, int32_t yDim, hal_cuda_adi **ou
     HAL_REQUIRE(out != nullptr, "hal_cuda_adi_create: out is NULL");
     *out = nullptr;
     HAL_REQUIRE(xDim > 0 && yDim > 0, "hal_cuda_adi_create: dimensions must be positive");
+    HAL_REQUIRE(static_cast<int64_t>(xDim) * yDim < (int64_t(1) << 31),
+                "hal_cuda_adi_create: xDim*yDim exceeds int32");
     if (xDim > HAL_CUDA_ADI_MAX_LINE || yDim > HAL_CUDA_ADI_MAX_LINE)
     {
         halcuda::SetError("hal_cuda_adi_create: ADI lines are limited to %d cells (got %d x %d)",
@@ -1028,6 +1419,7 @@ namespace
             {
                 gf[i] = static_cast<float>(ghost[i]);
             }
+            HAL_TRY(CudaStatus(cudaStreamSynchronize(s), "cudaStreamSynchronize"));
             HAL_TRY(CudaStatus(cudaMemcpy(h->g32.p, gf.data(), ng * sizeof(float), cudaMemcpyHostToDevice),
                                "cudaMemcpy(ghost)"));
             g = h->g32.p;
@@ -1036,12 +1428,15 @@ namespace
                            "cudaMemcpy(field)"));
         HAL_TRY(CudaStatus(cudaMemcpyAsync(h->d64.p, deltas, n * sizeof(double), cudaMemcpyHostToDevice, s),
                            "cudaMemcpy(deltas)"));
-        HAL_TRY(h->LaunchColumn<double>(h->f64.p, r, wrapX != 0, wrapY != 0, g, s));
-        HAL_TRY((h->LaunchRow<double, halcuda::kRowDeltas>(h->f64.p, nullptr, h->d64.p, r, 0.0, wrapX != 0,
-                                                           wrapY != 0, g, false, s)));
+        // the field in layout B, in float, in the spare buffer of the pair
+        float *fB = h->field[h->cur ^ 1].p;
+        HAL_TRY(h->TransposeTo<double>(h->f64.p, fB, h->xDim, h->yDim, s));
+        HAL_TRY(h->LaunchX(fB, r, wrapX != 0, wrapY != 0, g, s));
+        HAL_TRY(h->LaunchY<kSweepDeltas>(nullptr, nullptr, h->f64.p, h->d64.p, r, 0.0, wrapX != 0, wrapY != 0, g,
+                                          false, s));
         HAL_TRY(CudaStatus(cudaMemcpyAsync(deltas, h->d64.p, n * sizeof(double), cudaMemcpyDeviceToHost, s),
                            "cudaMemcpy(deltas)"));
-        return CudaStatus(cudaStreamSynchronize(s), who);
+        return h->CheckDeviceError(who);
     }
 }
 
@@ -1072,9 +1467,7 @@ extern "C" int hal_cuda_adi_set_field(hal_cuda_adi *h, const float *field, int64
     HAL_REQUIRE(len == static_cast<int64_t>(h->Length()), "hal_cuda_adi_set_field: field must hold xDim*yDim values");
     HAL_TRY(halcuda::CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
     cudaStream_t s = h->stream.Get();
-    HAL_TRY(halcuda::CudaStatus(cudaMemcpyAsync(h->field[h->cur].p, field, h->Length() * sizeof(float),
-                                                cudaMemcpyHostToDevice, s),
-                                "cudaMemcpy(field)"));
+    HAL_TRY(h->Upload(field, s));
     return halcuda::CudaStatus(cudaStreamSynchronize(s), "hal_cuda_adi_set_field");
 }
 
@@ -1084,10 +1477,8 @@ extern "C" int hal_cuda_adi_get_field(hal_cuda_adi *h, float *field, int64_t len
     HAL_REQUIRE(len == static_cast<int64_t>(h->Length()), "hal_cuda_adi_get_field: field must hold xDim*yDim values");
     HAL_TRY(halcuda::CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
     cudaStream_t s = h->stream.Get();
-    HAL_TRY(halcuda::CudaStatus(cudaMemcpyAsync(field, h->field[h->cur].p, h->Length() * sizeof(float),
-                                                cudaMemcpyDeviceToHost, s),
-                                "cudaMemcpy(field)"));
-    return halcuda::CudaStatus(cudaStreamSynchronize(s), "hal_cuda_adi_get_field");
+    HAL_TRY(h->Download(field, s));
+    return h->CheckDeviceError("hal_cuda_adi_get_field");
 }
 
 extern "C" int hal_cuda_adi_set_source(hal_cuda_adi *h, const float *dense, int64_t len)
@@ -1100,15 +1491,9 @@ extern "C" int hal_cuda_adi_set_source(hal_cuda_adi *h, const float *dense, int6
         return HAL_CUDA_OK;
     }
     HAL_REQUIRE(len == static_cast<int64_t>(h->Length()), "hal_cuda_adi_set_source: source must hold xDim*yDim values");
-    if (h->src.p == nullptr)
-    {
-        HAL_TRY(h->src.Alloc(h->Length(), "cudaMalloc(src)"));
-    }
-    HAL_TRY(halcuda::CudaStatus(cudaStreamSynchronize(h->stream.Get()), "cudaStreamSynchronize"));
-    HAL_TRY(halcuda::CudaStatus(cudaMemcpy(h->src.p, dense, h->Length() * sizeof(float), cudaMemcpyHostToDevice),
-                                "cudaMemcpy(src)"));
-    h->hasSrc = true;
-    return HAL_CUDA_OK;
+    cudaStream_t s = h->stream.Get();
+    HAL_TRY(h->UploadSource(dense, s));
+    return halcuda::CudaStatus(cudaStreamSynchronize(s), "hal_cuda_adi_set_source");
 }
 
 extern "C" int hal_cuda_adi_set_dirichlet(hal_cuda_adi *h, const float *ghost)
@@ -1180,34 +1565,25 @@ extern "C" int hal_cuda_adi_run_ticks_host(hal_cuda_adi *h, float *field, const 
     HAL_REQUIRE(ticks >= 0, "hal_cuda_adi_run_ticks_host: negative tick count");
     HAL_TRY(halcuda::CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
     cudaStream_t s = h->stream.Get();
-    size_t bytes = h->Length() * sizeof(float);
     if (src != nullptr)
     {
-        if (h->src.p == nullptr)
-        {
-            HAL_TRY(h->src.Alloc(h->Length(), "cudaMalloc(src)"));
-        }
-        HAL_TRY(halcuda::CudaStatus(cudaMemcpyAsync(h->src.p, src, bytes, cudaMemcpyHostToDevice, s),
-                                    "cudaMemcpy(src)"));
-        h->hasSrc = true;
+        HAL_TRY(h->UploadSource(src, s));
     }
     else
     {
         h->hasSrc = false;
     }
-    HAL_TRY(halcuda::CudaStatus(cudaMemcpyAsync(h->field[h->cur].p, field, bytes, cudaMemcpyHostToDevice, s),
-                                "cudaMemcpy(field)"));
+    HAL_TRY(h->Upload(field, s));
     HAL_TRY(h->RunTicks(ticks, diffRate, decay, wrapX != 0, wrapY != 0, false));
-    HAL_TRY(halcuda::CudaStatus(cudaMemcpyAsync(field, h->field[h->cur].p, bytes, cudaMemcpyDeviceToHost, s),
-                                "cudaMemcpy(field)"));
-    return halcuda::CudaStatus(cudaStreamSynchronize(s), "hal_cuda_adi_run_ticks_host");
+    HAL_TRY(h->Download(field, s));
+    return h->CheckDeviceError("hal_cuda_adi_run_ticks_host");
 }
 
 extern "C" int hal_cuda_adi_sync(hal_cuda_adi *h)
 {
     HAL_REQUIRE(h != nullptr, "hal_cuda_adi_sync: handle is NULL");
     HAL_TRY(halcuda::CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
-    return halcuda::CudaStatus(cudaStreamSynchronize(h->stream.Get()), "hal_cuda_adi_sync");
+    return h->CheckDeviceError("hal_cuda_adi_sync");
 }
 
 extern "C" void *hal_cuda_adi_stream(hal_cuda_adi *h)
@@ -1231,26 +1607,27 @@ extern "C" int hal_cuda_adi_profile(hal_cuda_adi *h, int32_t iters, double diffR
     using namespace halcuda;
     HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
     cudaStream_t s = h->stream.Get();
+    const float *g = h->hasGhost ? h->ghost.p : nullptr;
+    HAL_TRY(h->PrepareShapes(diffRate, wrapX != 0, wrapY != 0, g));
     cudaEvent_t ev[3];
     for (auto &e : ev)
     {
         HAL_TRY(CudaStatus(cudaEventCreate(&e), "cudaEventCreate"));
     }
-    const float *g = h->hasGhost ? h->ghost.p : nullptr;
-    double tCol = 0.0, tRow = 0.0;
+    double tX = 0.0, tY = 0.0;
     int rc = HAL_CUDA_OK;
     for (int32_t t = 0; t < iters && rc == HAL_CUDA_OK; t++)
     {
         int c = h->cur;
         cudaEventRecord(ev[0], s);
-        rc = h->LaunchColumn<float>(h->field[c].p, diffRate, wrapX != 0, wrapY != 0, g, s);
+        rc = h->LaunchX(h->field[c].p, diffRate, wrapX != 0, wrapY != 0, g, s);
         if (rc != HAL_CUDA_OK)
         {
             break;
         }
         cudaEventRecord(ev[1], s);
-        rc = h->LaunchRow<float, halcuda::kRowTick>(h->field[c].p, h->field[c ^ 1].p, nullptr, diffRate, decay,
-                                                    wrapX != 0, wrapY != 0, g, true, s);
+        rc = h->LaunchY<kSweepTick>(h->field[c ^ 1].p, h->field[c].p, nullptr, nullptr, diffRate, decay, wrapX != 0,
+                                    wrapY != 0, g, true, s);
         if (rc != HAL_CUDA_OK)
         {
             break;
@@ -1260,8 +1637,8 @@ extern "C" int hal_cuda_adi_profile(hal_cuda_adi *h, int32_t iters, double diffR
         float a = 0.0f, b = 0.0f;
         cudaEventElapsedTime(&a, ev[0], ev[1]);
         cudaEventElapsedTime(&b, ev[1], ev[2]);
-        tCol += a;
-        tRow += b;
+        tX += a;
+        tY += b;
         h->cur ^= 1;
     }
     for (auto &e : ev)
@@ -1269,7 +1646,8 @@ extern "C" int hal_cuda_adi_profile(hal_cuda_adi *h, int32_t iters, double diffR
         cudaEventDestroy(e);
     }
     HAL_TRY(rc);
-    ms[0] = static_cast<float>(tCol / iters);
-    ms[1] = static_cast<float>(tRow / iters);
+    HAL_TRY(h->CheckDeviceError("hal_cuda_adi_profile"));
+    ms[0] = static_cast<float>(tX / iters);
+    ms[1] = static_cast<float>(tY / iters);
     return HAL_CUDA_OK;
 }

@@ -19,7 +19,7 @@ namespace halcuda
 {
     namespace
     {
-        constexpr int kTickRowsPerThread = 8;  // rows walked by one thread
+        constexpr int kTickRowsPerThread = 4;  // rows owned by one thread
         constexpr int kTickWarps = 8;          // warps per CTA, stacked in x
 
         // Off-grid neighbour handling of one row (or column) of the stencil.
@@ -30,9 +30,9 @@ namespace halcuda
             kNbrNone = 2    // zero-flux: contributes 0
         };
 
-        __device__ __forceinline__ float NbrTerm(int mode, float v, float c)
+        __device__ __forceinline__ float ModeWeight(int mode)
         {
-            return (mode == kNbrGrid) ? (v - c) : ((mode == kNbrGhost) ? (v - c) * 2.0f : 0.0f);
+            return (mode == kNbrGrid) ? 1.0f : ((mode == kNbrGhost) ? 2.0f : 0.0f);
         }
 
         struct TickParams
@@ -104,28 +104,120 @@ namespace halcuda
             return mode;
         }
 
-        // One fused tick.  Each thread owns VEC consecutive cells of a row
-        // (float4 when yDim % 4 == 0) and walks kTickRowsPerThread rows,
-        // keeping the rows above and below in registers.
+        // One fused tick.  Each thread owns VEC consecutive cells (float4 when
+        // yDim % 4 == 0) of kTickRowsPerThread consecutive rows.  Every load
+        // of the thread -- the rows above, inside and below its strip, the
+        // y neighbours of each row and the source -- is issued before the
+        // first result is computed.
         template <int VEC>
         __global__ void __launch_bounds__(32 * kTickWarps)
             TickKernel(TickParams p)
         {
+            constexpr int T = kTickRowsPerThread;
             const int lane = threadIdx.x;
             const int warp = threadIdx.y;
             const int32_t y0 = (blockIdx.x * 32 + lane) * VEC;
-            const int32_t xs = (blockIdx.y * kTickWarps + warp) * kTickRowsPerThread;
+            const int32_t xs = (blockIdx.y * kTickWarps + warp) * T;
             if (y0 >= p.yDim || xs >= p.xDim)
             {
                 return;
             }
-            const int32_t xe = min(xs + kTickRowsPerThread, p.xDim);
             const int nValid = min(VEC, p.yDim - y0);
 
-            float up[VEC], cur[VEC], dn[VEC];
-            int upMode = LoadRow<VEC>(p, xs - 1, y0, up, true);
-            LoadRow<VEC>(p, xs, y0, cur, true);
+            float rows[T + 2][VEC];
+            int mode[T + 2];
+#pragma unroll
+            for (int j = 0; j < T + 2; j++)
+            {
+                const int32_t x = xs - 1 + j;
+                if (x <= p.xDim)  // rows past the strip's last "below" row are unused
+                {
+                    mode[j] = LoadRow<VEC>(p, x, y0, rows[j], j == 0);
+                }
+                else
+                {
+                    mode[j] = kNbrNone;
+#pragma unroll
+                    for (int k = 0; k < VEC; k++)
+                    {
+                        rows[j][k] = 0.0f;
+                    }
+                }
+            }
+            float left[T], right[T], srcv[T][VEC];
+            int leftMode = kNbrGrid, rightMode = kNbrGrid;
+            const int32_t yr = y0 + nValid;  // column right of the last owned cell
+            if (y0 == 0)
+            {
+                leftMode = p.wrapY ? kNbrGrid : ((p.ghost.ylo != nullptr) ? kNbrGhost : kNbrNone);
+            }
+            if (yr >= p.yDim)
+            {
+                rightMode = p.wrapY ? kNbrGrid : ((p.ghost.yhi != nullptr) ? kNbrGhost : kNbrNone);
+            }
+#pragma unroll
+            for (int t = 0; t < T; t++)
+            {
+                const int32_t x = xs + t;
+                left[t] = 0.0f;
+                right[t] = 0.0f;
+#pragma unroll
+                for (int k = 0; k < VEC; k++)
+                {
+                    srcv[t][k] = 0.0f;
+                }
+                if (x < p.xDim)
+                {
+                    const float *rowp = p.f + static_cast<int64_t>(x) * p.yDim;
+                    if (y0 > 0)
+                    {
+                        left[t] = __ldg(rowp + y0 - 1);
+                    }
+                    else if (p.wrapY)
+                    {
+                        left[t] = __ldg(rowp + p.yDim - 1);
+                    }
+                    else if (p.ghost.ylo != nullptr)
+                    {
+                        left[t] = __ldg(p.ghost.ylo + x);
+                    }
+                    if (yr < p.yDim)
+                    {
+                        right[t] = __ldg(rowp + yr);
+                    }
+                    else if (p.wrapY)
+                    {
+                        right[t] = __ldg(rowp);
+                    }
+                    else if (p.ghost.yhi != nullptr)
+                    {
+                        right[t] = __ldg(p.ghost.yhi + x);
+                    }
+                    if (p.src != nullptr)
+                    {
+                        const float *s = p.src + static_cast<int64_t>(x) * p.yDim + y0;
+                        if constexpr (VEC == 4)
+                        {
+                            float4 q = __ldg(reinterpret_cast<const float4 *>(s));
+                            srcv[t][0] = q.x;
+                            srcv[t][1] = q.y;
+                            srcv[t][2] = q.z;
+                            srcv[t][3] = q.w;
+                        }
+                        else
+                        {
+#pragma unroll
+                            for (int k = 0; k < VEC; k++)
+                            {
+                                srcv[t][k] = (k < nValid) ? __ldg(s + k) : 0.0f;
+                            }
+                        }
+                    }
+                }
+            }
 
+            const float wLeft = ModeWeight(leftMode);
+            const float wRight = ModeWeight(rightMode);
             int32_t ptBeg = 0, ptEnd = 0;
             if (p.ptStart != nullptr)
             {
@@ -134,108 +226,38 @@ namespace halcuda
                 ptEnd = __ldg(p.ptStart + b + 1);
             }
 
-            for (int32_t x = xs; x < xe; x++)
+#pragma unroll
+            for (int t = 0; t < T; t++)
             {
-                int dnMode = LoadRow<VEC>(p, x + 1, y0, dn, false);
-                const float *rowp = p.f + static_cast<int64_t>(x) * p.yDim;
-
-                // y neighbours of the first and last owned cells
-                float left, right;
-                int leftMode = kNbrGrid, rightMode = kNbrGrid;
-                if (y0 > 0)
+                const int32_t x = xs + t;
+                if (x >= p.xDim)
                 {
-                    left = __ldg(rowp + y0 - 1);
+                    break;
                 }
-                else if (p.wrapY)
-                {
-                    left = __ldg(rowp + p.yDim - 1);
-                }
-                else if (p.ghost.ylo != nullptr)
-                {
-                    left = __ldg(p.ghost.ylo + x);
-                    leftMode = kNbrGhost;
-                }
-                else
-                {
-                    left = 0.0f;
-                    leftMode = kNbrNone;
-                }
-                const int32_t yr = y0 + nValid;  // column right of the last owned cell
-                if (yr < p.yDim)
-                {
-                    right = __ldg(rowp + yr);
-                }
-                else if (p.wrapY)
-                {
-                    right = __ldg(rowp);
-                }
-                else if (p.ghost.yhi != nullptr)
-                {
-                    right = __ldg(p.ghost.yhi + x);
-                    rightMode = kNbrGhost;
-                }
-                else
-                {
-                    right = 0.0f;
-                    rightMode = kNbrNone;
-                }
-
+                const float *up = rows[t];
+                const float *cur = rows[t + 1];
+                const float *dn = rows[t + 2];
+                // difference weights: 1 on the grid, 2 for a Dirichlet ghost
+                // ((bc - c) * 2), 0 past a zero-flux edge
+                const float wUp = ModeWeight(mode[t]);
+                const float wDn = ModeWeight(mode[t + 2]);
                 float o[VEC];
 #pragma unroll
                 for (int k = 0; k < VEC; k++)
                 {
                     const float c = cur[k];
-                    float yp, ym;
-                    int ypMode = kNbrGrid, ymMode = kNbrGrid;
-                    if (k + 1 < nValid)
-                    {
-                        yp = cur[k + 1];
-                    }
-                    else
-                    {
-                        yp = right;
-                        ypMode = rightMode;
-                    }
-                    if (k > 0)
-                    {
-                        ym = cur[k - 1];
-                    }
-                    else
-                    {
-                        ym = left;
-                        ymMode = leftMode;
-                    }
+                    const float yp = (k + 1 < nValid) ? cur[k + 1] : right[t];
+                    const float wYp = (k + 1 < nValid) ? 1.0f : wRight;
+                    const float ym = (k > 0) ? cur[k - 1] : left[t];
+                    const float wYm = (k > 0) ? 1.0f : wLeft;
                     // reference order: x+1, x-1, y+1, y-1
-                    float sum = NbrTerm(dnMode, dn[k], c);
-                    sum += NbrTerm(upMode, up[k], c);
-                    sum += NbrTerm(ypMode, yp, c);
-                    sum += NbrTerm(ymMode, ym, c);
+                    float sum = (dn[k] - c) * wDn;
+                    sum = fmaf(up[k] - c, wUp, sum);
+                    sum = fmaf(yp - c, wYp, sum);
+                    sum = fmaf(ym - c, wYm, sum);
                     float d = sum * p.r;
                     d = fmaf(c, p.negDecay, d);
-                    o[k] = d;
-                }
-                if (p.src != nullptr)
-                {
-                    const float *s = p.src + static_cast<int64_t>(x) * p.yDim + y0;
-                    if constexpr (VEC == 4)
-                    {
-                        float4 q = __ldg(reinterpret_cast<const float4 *>(s));
-                        o[0] += q.x;
-                        o[1] += q.y;
-                        o[2] += q.z;
-                        o[3] += q.w;
-                    }
-                    else
-                    {
-#pragma unroll
-                        for (int k = 0; k < VEC; k++)
-                        {
-                            if (k < nValid)
-                            {
-                                o[k] += __ldg(s + k);
-                            }
-                        }
-                    }
+                    o[k] = d + srcv[t][k];
                 }
                 for (int32_t q = ptBeg; q < ptEnd; q++)
                 {
@@ -274,13 +296,6 @@ namespace halcuda
                         }
                     }
                 }
-#pragma unroll
-                for (int k = 0; k < VEC; k++)
-                {
-                    up[k] = cur[k];
-                    cur[k] = dn[k];
-                }
-                upMode = kNbrGrid;
             }
         }
 

@@ -1,0 +1,56 @@
+"""Small, fixed launches of each hot kernel, for ncu captures.
+
+    python -m halcuda.profcase adi 2048 3        # 3 ADI ticks (x-sweep + y-sweep)
+    python -m halcuda.profcase explicit 2048 3   # 3 fused explicit ticks
+    python -m halcuda.profcase agents 2048 2     # 2 dispatches of 1M agents
+
+Each case builds the benchmark's inputs at the given grid side, runs one
+untimed warm-up launch sequence, then the requested number of individually
+launched iterations (no CUDA graph), so that `ncu -k <kernel> -c <n>` sees
+plain launches with few launches before them.
+"""
+from __future__ import annotations
+
+import sys
+
+import numpy as np
+
+import halcuda as hal
+from halcuda import workloads
+
+
+def main(argv):
+    case = argv[0] if argv else "adi"
+    n = int(argv[1]) if len(argv) > 1 else 2048
+    iters = int(argv[2]) if len(argv) > 2 else 3
+    if case == "adi":
+        w = workloads.adi_inputs(n, seed=2, blobs=20)
+        with hal.Adi(n, n) as a:
+            a.set_field(w["field"])
+            a.set_source(w["src"])
+            a.profile(1, 5.0, 0.01)
+            ms = a.profile(iters, 5.0, 0.01)
+        print(f"adi {n}^2: x-sweep {ms[0]*1e3:.1f} us, y-sweep {ms[1]*1e3:.1f} us")
+    elif case == "explicit":
+        w = workloads.explicit_inputs(n, seed=1)
+        with hal.Diffusion(n, n) as d:
+            d.set_field(w["field"])
+            d.set_point_sources(w["src_idx"], w["src_val"])
+            d.profile(1, 0.2, 0.001)
+            ms = d.profile(iters, 0.2, 0.001)
+        print(f"explicit {n}^2: tick {ms*1e3:.1f} us")
+    elif case == "agents":
+        agents = max(1, int(1_000_000 * (n / 2048) ** 2))
+        w = workloads.agent_inputs(agents, n, seed=3)
+        with hal.Agents(n, n, agents) as ag:
+            ag.upload(w["positions"], w["radii"])
+            ag.profile(1, 1.0, 0.1)
+            ms = ag.profile(iters, 1.0, 0.1)
+        print(f"agents {agents} in {n}^2: " + ", ".join(f"{v*1e3:.1f}" for v in ms) + " us")
+    else:
+        raise SystemExit(f"unknown case {case}")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main(sys.argv[1:]))
