@@ -16,10 +16,14 @@
 // the y-sweep reads, writing f' back in layout B.  Both sweeps therefore run
 // the same kernel, AdiSweep:
 //   1. stage the CTA's R lines plus the line on either side (the explicit
-//      cross-axis term) into shared memory with TMA bulk copies
-//      (cp.async.bulk, one 128-byte chunk each, completion on an mbarrier);
-//      each 32-element chunk occupies 36 floats so that every later access
-//      is a conflict-free 128-bit LDS/STS;
+//      cross-axis term) into shared memory with TMA, completion on an
+//      mbarrier whose wait is bounded.  When L is a multiple of 256 one 3-D
+//      tensor copy (cp.async.bulk.tensor, box 32 x P x (R+2), 128-byte
+//      swizzle, zero fill outside the field) stages the whole tile and the
+//      kernel indexes shared memory through the same swizzle; otherwise each
+//      32-element chunk is a 1-D cp.async.bulk (or plain loads for ragged
+//      lines) into a 36-float slot.  Either way every later access is a
+//      conflict-free 128-bit LDS/STS;
 //   2. each thread solves one 32-row chunk of two lines (two interleaved
 //      Thomas chains in registers), exchanges the separator right-hand sides
 //      through shared memory, applies the banded reduced solve and the
