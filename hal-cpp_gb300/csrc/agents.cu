@@ -705,3 +705,150 @@ extern "C" int hal_cuda_agents_profile(hal_cuda_agents *h, int32_t iters, double
     }
     return HAL_CUDA_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Agent forces without allocation.
+//
+// Some callers cannot call cudaMalloc: a host framework that reserves its
+// device memory in its own pool at start-up and forbids cudaMalloc/cudaFree in
+// its step loop (both synchronise the whole device and stall the framework's
+// other streams), or a plugin whose host budgets device memory and hands it
+// only pointers to inputs and outputs.  For them this entry point runs the same
+// binning and force kernels as hal_cuda_agents_dispatch with every piece of
+// scratch taken from one file-scope device array of fixed size, so it needs no
+// handle and allocates nothing.  The caller passes device pointers to the
+// positions, radii and velocity deltas.
+//
+// The array is a static __device__ variable: every GPU that loads this library
+// holds it (HAL_CUDA_NOALLOC_SCRATCH_BYTES) until the process exits.  In host
+// code its name is only a host-side stand-in, so its device address is looked
+// up once per device with cudaGetSymbolAddress, with that device current,
+// on the first call made on that device.  All calls share it and it keeps the
+// last call's contents; the cell counts, the only part that must start at
+// zero, are cleared on the caller's stream at the start of each call.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace
+{
+    constexpr size_t kNoAllocMaxAgents = HAL_CUDA_NOALLOC_MAX_AGENTS;
+    constexpr size_t kNoAllocMaxCells = HAL_CUDA_NOALLOC_MAX_CELLS;
+    constexpr size_t kNoAllocMaxTiles = (kNoAllocMaxCells + halcuda::kScanTile - 1) / halcuda::kScanTile;
+
+    constexpr size_t Round256(size_t b)
+    {
+        return (b + 255) / 256 * 256;
+    }
+
+    // Byte offsets of the regions of the scratch array (each 256-byte aligned).
+    constexpr size_t kOffPosF = 0;
+    constexpr size_t kOffSPos = kOffPosF + Round256(kNoAllocMaxAgents * sizeof(float2));
+    constexpr size_t kOffSRad = kOffSPos + Round256(kNoAllocMaxAgents * sizeof(float2));
+    constexpr size_t kOffCellOf = kOffSRad + Round256(kNoAllocMaxAgents * sizeof(float));
+    constexpr size_t kOffArrival = kOffCellOf + Round256(kNoAllocMaxAgents * sizeof(int32_t));
+    constexpr size_t kOffBucketTmp = kOffArrival + Round256(kNoAllocMaxAgents * sizeof(int32_t));
+    constexpr size_t kOffBucket = kOffBucketTmp + Round256(kNoAllocMaxAgents * sizeof(int32_t));
+    constexpr size_t kOffCounts = kOffBucket + Round256(kNoAllocMaxAgents * sizeof(int32_t));
+    constexpr size_t kOffOffsets = kOffCounts + Round256(kNoAllocMaxCells * sizeof(int32_t));
+    constexpr size_t kOffTileSums = kOffOffsets + Round256((kNoAllocMaxCells + 1) * sizeof(int32_t));
+    constexpr size_t kNoAllocBytes = kOffTileSums + Round256(kNoAllocMaxTiles * sizeof(int32_t));
+    static_assert(kNoAllocBytes <= HAL_CUDA_NOALLOC_SCRATCH_BYTES, "no-alloc scratch regions exceed the stated size");
+
+    static __device__ __align__(256) unsigned char gNoAllocScratch[HAL_CUDA_NOALLOC_SCRATCH_BYTES];
+
+    constexpr int kNoAllocMaxDevices = 64;
+    std::mutex gNoAllocMutex;
+    unsigned char *gNoAllocAddr[kNoAllocMaxDevices] = {};
+
+    // Device address of gNoAllocScratch on the current device `dev`; resolved
+    // on the first call on that device.
+    int NoAllocScratch(int dev, unsigned char **out)
+    {
+        if (dev < 0 || dev >= kNoAllocMaxDevices)
+        {
+            halcuda::SetError("hal_cuda_agents_forces_noalloc: device ordinal %d not supported", dev);
+            return HAL_CUDA_EDEVICE;
+        }
+        std::lock_guard<std::mutex> lock(gNoAllocMutex);
+        if (gNoAllocAddr[dev] == nullptr)
+        {
+            void *p = nullptr;
+            HAL_TRY(halcuda::CudaStatus(cudaGetSymbolAddress(&p, gNoAllocScratch),
+                                        "cudaGetSymbolAddress(no-alloc scratch)"));
+            gNoAllocAddr[dev] = static_cast<unsigned char *>(p);
+        }
+        *out = gNoAllocAddr[dev];
+        return HAL_CUDA_OK;
+    }
+
+    // The pointer must be device (or managed) memory reachable from `dev`.
+    bool OnDevice(const void *p, int dev)
+    {
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+        {
+            cudaGetLastError();
+            return false;
+        }
+        return a.type == cudaMemoryTypeManaged || (a.type == cudaMemoryTypeDevice && a.device == dev);
+    }
+}
+
+extern "C" int hal_cuda_agents_forces_noalloc(const float *positions, const float *radii, int32_t n,
+                                              float *velocityDeltas, double interactionRad, double springConstant,
+                                              int32_t xDim, int32_t yDim, int32_t wrapX, int32_t wrapY, void *stream)
+{
+    HAL_REQUIRE(xDim > 0 && yDim > 0, "hal_cuda_agents_forces_noalloc: dimensions must be positive");
+    HAL_REQUIRE(static_cast<int64_t>(xDim) * yDim <= static_cast<int64_t>(kNoAllocMaxCells),
+                "hal_cuda_agents_forces_noalloc: grid %d x %d has more than %d cells, the no-alloc limit",
+                xDim, yDim, HAL_CUDA_NOALLOC_MAX_CELLS);
+    HAL_REQUIRE(n >= 0 && static_cast<size_t>(n) <= kNoAllocMaxAgents,
+                "hal_cuda_agents_forces_noalloc: agent count %d outside [0, %d], the no-alloc limit", n,
+                HAL_CUDA_NOALLOC_MAX_AGENTS);
+    HAL_REQUIRE(RadiusOk(interactionRad), "hal_cuda_agents_forces_noalloc: interactionRad %g outside [0, %g]",
+                interactionRad, kMaxInteractionRad);
+    HAL_REQUIRE(n == 0 || (positions != nullptr && radii != nullptr && velocityDeltas != nullptr),
+                "hal_cuda_agents_forces_noalloc: NULL array");
+    using namespace halcuda;
+    int dev = 0;
+    HAL_TRY(CudaStatus(cudaGetDevice(&dev), "cudaGetDevice"));
+    HAL_REQUIRE(n == 0 || (OnDevice(positions, dev) && OnDevice(radii, dev) && OnDevice(velocityDeltas, dev)),
+                "hal_cuda_agents_forces_noalloc: positions, radii and velocityDeltas must be device memory of "
+                "the current device %d", dev);
+    unsigned char *base = nullptr;
+    HAL_TRY(NoAllocScratch(dev, &base));
+    if (n == 0)
+    {
+        return HAL_CUDA_OK;
+    }
+    float2 *posF = reinterpret_cast<float2 *>(base + kOffPosF);
+    float2 *sPos = reinterpret_cast<float2 *>(base + kOffSPos);
+    float *sRad = reinterpret_cast<float *>(base + kOffSRad);
+    int32_t *cellOf = reinterpret_cast<int32_t *>(base + kOffCellOf);
+    int32_t *arrival = reinterpret_cast<int32_t *>(base + kOffArrival);
+    int32_t *bucketTmp = reinterpret_cast<int32_t *>(base + kOffBucketTmp);
+    int32_t *bucket = reinterpret_cast<int32_t *>(base + kOffBucket);
+    int32_t *counts = reinterpret_cast<int32_t *>(base + kOffCounts);
+    int32_t *offsets = reinterpret_cast<int32_t *>(base + kOffOffsets);
+    int32_t *tileSums = reinterpret_cast<int32_t *>(base + kOffTileSums);
+
+    const int64_t C = static_cast<int64_t>(xDim) * yDim;
+    const unsigned nTiles = static_cast<unsigned>((C + kScanTile - 1) / kScanTile);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    HAL_TRY(CudaStatus(cudaMemsetAsync(counts, 0, static_cast<size_t>(C) * sizeof(int32_t), s),
+                       "cudaMemsetAsync(no-alloc counts)"));
+    const int T = 256;
+    const unsigned ablocks = static_cast<unsigned>((n + T - 1) / T);
+    BinCount<float><<<ablocks, T, 0, s>>>(positions, n, xDim, yDim, posF, cellOf, arrival, counts);
+    ScanReduce<<<nTiles, kScanThreads, 0, s>>>(counts, C, tileSums);
+    ScanTiles<<<1, kScanThreads, 0, s>>>(tileSums, static_cast<int32_t>(nTiles));
+    ScanApply<<<nTiles, kScanThreads, 0, s>>>(counts, C, tileSums, offsets, n);
+    Scatter<<<ablocks, T, 0, s>>>(cellOf, arrival, offsets, n, bucketTmp);
+    Stabilize<float><<<ablocks, T, 0, s>>>(cellOf, offsets, bucketTmp, posF, radii, n, bucket, sPos, sRad);
+    const int TF = 128;
+    Forces<float, float><<<static_cast<unsigned>((n + TF - 1) / TF), TF, 0, s>>>(
+        bucket, offsets, sPos, sRad, n, interactionRad, static_cast<float>(interactionRad),
+        static_cast<float>(springConstant), xDim, yDim, wrapX != 0, wrapY != 0, velocityDeltas);
+    CountLaunch(7);
+    return LaunchStatus("hal_cuda_agents_forces_noalloc");
+}

@@ -74,6 +74,8 @@ SIGNATURES = {
     "hal_cuda_agents_sync": (_I, [_vp]),
     "hal_cuda_agents_stream": (_vp, [_vp]),
     "hal_cuda_agents_set_stream": (_I, [_vp, _vp]),
+    "hal_cuda_agents_forces_noalloc": (_I, [_vp, _vp, _i32, _vp, _f64, _f64, _i32, _i32, _i32, _i32,
+                                            _vp]),
 }
 
 _lib = None
@@ -383,3 +385,20 @@ class Agents(_Handle):
         bucket = np.empty(max(self.n, 1), dtype=np.int32)
         _check(lib().hal_cuda_agents_get_bins(self._h, _p(off), _p(bucket)), "get_bins")
         return off, bucket[: self.n]
+
+
+NOALLOC_MAX_AGENTS = 65536
+NOALLOC_MAX_CELLS = 65536
+
+
+def agents_forces_noalloc(positions_ptr: int, radii_ptr: int, n: int, velocity_ptr: int,
+                          interactionRad: float, springConstant: float, xDim: int, yDim: int,
+                          wrapX: bool = False, wrapY: bool = False, stream: int = 0) -> None:
+    """hal_cuda_agents_forces_noalloc: agent forces for callers that cannot
+    allocate device memory.  The pointers are device addresses (FP32; 2n, n
+    and 2n values) owned by the caller; the call only enqueues work on
+    `stream` (0: the legacy default stream)."""
+    _check(lib().hal_cuda_agents_forces_noalloc(
+        ctypes.c_void_p(positions_ptr), ctypes.c_void_p(radii_ptr), n, ctypes.c_void_p(velocity_ptr),
+        interactionRad, springConstant, xDim, yDim, int(wrapX), int(wrapY),
+        ctypes.c_void_p(stream) if stream else None), "agents_forces_noalloc")

@@ -254,6 +254,38 @@ int hal_cuda_agents_sync(hal_cuda_agents *h);
 void *hal_cuda_agents_stream(hal_cuda_agents *h);
 int hal_cuda_agents_set_stream(hal_cuda_agents *h, void *stream);
 
+/* ---- agent forces without allocation --------------------------------------
+ * No counterpart in the reference: the reference's backends allocate their
+ * buffers.  This entry point is for callers that cannot call cudaMalloc -- a
+ * host framework that owns all device memory in its own pool and forbids
+ * cudaMalloc/cudaFree in its step loop (they synchronise the whole device), or
+ * a plugin whose host hands it only pointers to inputs and outputs.  It runs
+ * the same kernels as hal_cuda_agents_dispatch (FP32 positions, radii and
+ * velocity deltas; same bins, same summation order) and allocates nothing: no
+ * handle, no cudaMalloc/cudaFree, no allocating library call.  Its scratch is
+ * one static device array of HAL_CUDA_NOALLOC_SCRATCH_BYTES that every GPU
+ * loading this library holds until the process exits.
+ *
+ * positions (2n floats, x,y interleaved), radii (n) and velocityDeltas (2n) are
+ * device memory of the current device; stream is a cudaStream_t of that device
+ * (NULL: the legacy default stream).  The call only enqueues work: synchronise
+ * the stream before reading velocityDeltas.  n above HAL_CUDA_NOALLOC_MAX_AGENTS
+ * or xDim*yDim above HAL_CUDA_NOALLOC_MAX_CELLS returns HAL_CUDA_EINVAL.
+ *
+ * The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress, with that device current); make that first call
+ * before any stream capture.  Every call on a device shares the one array and
+ * it keeps the last call's contents: calls that overlap on the GPU (different
+ * streams, or host threads racing on one device) race on it and give wrong
+ * results.  Calls ordered on one stream are safe. */
+#define HAL_CUDA_NOALLOC_MAX_AGENTS 65536
+#define HAL_CUDA_NOALLOC_MAX_CELLS 65536
+#define HAL_CUDA_NOALLOC_SCRATCH_BYTES (3u << 20)
+
+int hal_cuda_agents_forces_noalloc(const float *positions, const float *radii, int32_t n,
+                                   float *velocityDeltas, double interactionRad, double springConstant,
+                                   int32_t xDim, int32_t yDim, int32_t wrapX, int32_t wrapY, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
