@@ -1,0 +1,166 @@
+#pragma once
+
+// CUDA (sm_103a) implementations of HAL-CPP's three per-tick strategy
+// interfaces, over the C ABI in hal_cuda.h.  They stand where the Vulkan
+// classes Hal::Gpu::GpuDiffusionBackend2D / GpuAdiDiffusionBackend2D /
+// GpuAgentForceBackend2D stand (src/Gpu/GpuDiffusionBackend2D.cpp:22-52,
+// GpuAdiDiffusionBackend2D.cpp:24-50, GpuAgentForceBackend2D.cpp:24-68):
+// sized at construction, copy-deleted, and throwing std::invalid_argument
+// for size mismatches and std::runtime_error for device failures, after
+// logging through Hal::Logger (IDiffusionBackend2D.cpp:26-31,
+// AdiKernel2D.cpp:66-70).  No ComputeContext: hal_cuda_set_device picks the
+// GPU for handles created afterwards on the calling thread.
+//
+// Beyond the interfaces, each class exposes the device-resident tick that
+// PDEGrid2D performs on the host (PDEGrid2D.h:103-186): set the field,
+// sources and Dirichlet values once, run many ticks, read the field back.
+
+#include "Hal/Agents/IAgentForceBackend2D.h"
+#include "Hal/Pde/IAdiDiffusionBackend2D.h"
+#include "Hal/Pde/IDiffusionBackend2D.h"
+
+#include "hal_cuda.h"
+
+#include <cstdint>
+#include <vector>
+
+namespace Hal::Cuda
+{
+    // Logs and throws for a non-OK status: std::invalid_argument for
+    // HAL_CUDA_EINVAL, std::runtime_error otherwise.
+    void Check(int status, const char *pWhat);
+
+    // Selects the CUDA device for backends constructed afterwards on this
+    // thread.
+    void SetDevice(int32_t device);
+
+    class CudaAgentForceBackend2D;
+
+    class CudaDiffusionBackend2D final : public IDiffusionBackend2D
+    {
+    public:
+        CudaDiffusionBackend2D(int32_t xDim, int32_t yDim);
+        ~CudaDiffusionBackend2D() override;
+
+        // IDiffusionBackend2D::Diffuse: deltas += one explicit step, FP64,
+        // bit-identical to CpuDiffusionBackend2D.
+        void Diffuse(const std::vector<double> &field,
+                     std::vector<double>       &deltas,
+                     double                     diffRate,
+                     int32_t                    xDim,
+                     int32_t                    yDim,
+                     bool                       wrapX,
+                     bool                       wrapY) override;
+
+        // Internal::Diffusion2<BCFn> with the Dirichlet callable given as its
+        // ghost table (2*yDim + 2*xDim values: bc(-1,y), bc(xDim,y),
+        // bc(x,-1), bc(x,yDim)); an empty table means zero-flux.
+        void DiffuseDirichlet(const std::vector<double> &field,
+                              std::vector<double>       &deltas,
+                              double                     diffRate,
+                              bool                       wrapX,
+                              bool                       wrapY,
+                              const std::vector<double> &ghost);
+
+        // Device-resident PDEGrid2D tick: f' = f + r L(f) - decay f + src.
+        void SetField(const std::vector<float> &field);
+        void GetField(std::vector<float> &field);
+        void SetSource(const std::vector<float> &dense);
+        void SetPointSources(const std::vector<int32_t> &cells, const std::vector<float> &values);
+        void SetDirichlet(const std::vector<float> &ghost);
+        void RunTicks(int32_t ticks, double diffRate, double decay, bool wrapX, bool wrapY);
+        void Sync();
+
+        // DiffusionKernel2D::RunSteps: upload, `steps` plain steps, download.
+        void RunSteps(std::vector<float> &field, int32_t steps, double diffRate, bool wrapX, bool wrapY);
+
+        int32_t XDim() const { return m_xDim; }
+        int32_t YDim() const { return m_yDim; }
+
+    private:
+        hal_cuda_diffusion *m_pHandle = nullptr;
+        int32_t             m_xDim;
+        int32_t             m_yDim;
+    };
+
+    class CudaAdiDiffusionBackend2D final : public IAdiDiffusionBackend2D
+    {
+    public:
+        CudaAdiDiffusionBackend2D(int32_t xDim, int32_t yDim);
+        ~CudaAdiDiffusionBackend2D() override;
+
+        // IAdiDiffusionBackend2D::DiffuseADI: deltas += one ADI step.
+        void DiffuseADI(const std::vector<double> &field,
+                        std::vector<double>       &deltas,
+                        double                     diffRate,
+                        int32_t                    xDim,
+                        int32_t                    yDim,
+                        bool                       wrapX,
+                        bool                       wrapY) override;
+
+        // Internal::Diffusion2DADI<BCFn> with a Dirichlet ghost table.
+        void DiffuseADIDirichlet(const std::vector<double> &field,
+                                 std::vector<double>       &deltas,
+                                 double                     diffRate,
+                                 bool                       wrapX,
+                                 bool                       wrapY,
+                                 const std::vector<double> &ghost);
+
+        // Device-resident PDEGrid2D::DiffusionADI tick:
+        // f' = ADI(f) - decay f + src - uptake * (agents in the cell) * f.
+        void SetField(const std::vector<float> &field);
+        void GetField(std::vector<float> &field);
+        void SetSource(const std::vector<float> &dense);
+        void SetDirichlet(const std::vector<float> &ghost);
+        void SetUptake(CudaAgentForceBackend2D *pAgents, double uptake);
+        void RunTicks(int32_t ticks, double diffRate, double decay, bool wrapX, bool wrapY);
+        void Sync();
+
+        // AdiKernel2D::RunSteps: upload, `steps` plain ADI steps, download.
+        void RunSteps(std::vector<float> &field, int32_t steps, double diffRate, bool wrapX, bool wrapY);
+
+        int32_t XDim() const { return m_xDim; }
+        int32_t YDim() const { return m_yDim; }
+
+    private:
+        hal_cuda_adi *m_pHandle = nullptr;
+        int32_t       m_xDim;
+        int32_t       m_yDim;
+    };
+
+    class CudaAgentForceBackend2D final : public IAgentForceBackend2D
+    {
+    public:
+        CudaAgentForceBackend2D(int32_t xDim, int32_t yDim, int32_t maxAgents);
+        ~CudaAgentForceBackend2D() override;
+
+        // IAgentForceBackend2D::AccumulateForces: velocityDeltas resized to
+        // positions.size() and overwritten.  Bins and forces are
+        // bit-identical to the CPU backend's (FP64 throughout).
+        void AccumulateForces(const std::vector<double> &positions,
+                              const std::vector<double> &radii,
+                              std::vector<double>       &velocityDeltas,
+                              double                     interactionRad,
+                              double                     springConstant,
+                              int32_t                    xDim,
+                              int32_t                    yDim,
+                              bool                       wrapX,
+                              bool                       wrapY) override;
+
+        // AgentForceKernel2D's resident form (FP32): upload, dispatch, download.
+        void Upload(const std::vector<float> &positions, const std::vector<float> &radii);
+        void Dispatch(double interactionRad, double springConstant, bool wrapX, bool wrapY);
+        void Download(std::vector<float> &velocityDeltas);
+        // Cell offsets (xDim*yDim + 1) and the agent order of the last binning.
+        void GetBins(std::vector<int32_t> &cellOffsets, std::vector<int32_t> &bucketAgents);
+
+        hal_cuda_agents *Handle() const { return m_pHandle; }
+
+    private:
+        hal_cuda_agents *m_pHandle = nullptr;
+        int32_t          m_xDim;
+        int32_t          m_yDim;
+        int32_t          m_maxAgents;
+        int32_t          m_count = 0;
+    };
+}

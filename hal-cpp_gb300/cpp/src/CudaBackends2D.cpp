@@ -1,0 +1,296 @@
+// Hal::Cuda backends: thin C++ classes over the hal_cuda C ABI.
+#include "Hal/Cuda/CudaBackends2D.h"
+
+#include "Hal/Log/Logger.h"
+
+#include <stdexcept>
+#include <string>
+
+namespace Hal::Cuda
+{
+    void Check(int status, const char *pWhat)
+    {
+        if (status == HAL_CUDA_OK)
+        {
+            return;
+        }
+        std::string msg = std::string(pWhat) + ": " + hal_cuda_last_error();
+        Logger::Instance().Log(LogSeverity::Error, msg);
+        if (status == HAL_CUDA_EINVAL)
+        {
+            throw std::invalid_argument(msg);
+        }
+        throw std::runtime_error(msg);
+    }
+
+    void SetDevice(int32_t device)
+    {
+        Check(hal_cuda_set_device(device), "Hal::Cuda::SetDevice");
+    }
+
+    namespace
+    {
+        const double *GhostOrNull(const std::vector<double> &ghost)
+        {
+            return ghost.empty() ? nullptr : ghost.data();
+        }
+
+        const float *GhostOrNull(const std::vector<float> &ghost)
+        {
+            return ghost.empty() ? nullptr : ghost.data();
+        }
+
+        void CheckGhost(size_t n, int32_t xDim, int32_t yDim, const char *pWhat)
+        {
+            if (n != 0 && n != 2 * static_cast<size_t>(xDim) + 2 * static_cast<size_t>(yDim))
+            {
+                std::string msg = std::string(pWhat) + ": Dirichlet table must hold 2*xDim + 2*yDim values";
+                Logger::Instance().Log(LogSeverity::Error, msg);
+                throw std::invalid_argument(msg);
+            }
+        }
+
+        void CheckCells(const std::vector<double> &a, const std::vector<double> &b, int32_t xDim,
+                        int32_t yDim, const char *pWhat)
+        {
+            const size_t n = static_cast<size_t>(xDim) * static_cast<size_t>(yDim);
+            if (a.size() != n || b.size() != n)
+            {
+                std::string msg = std::string(pWhat) + ": field and deltas must hold xDim*yDim values";
+                Logger::Instance().Log(LogSeverity::Error, msg);
+                throw std::invalid_argument(msg);
+            }
+        }
+    }
+
+    // ---- explicit diffusion -------------------------------------------------
+
+    CudaDiffusionBackend2D::CudaDiffusionBackend2D(int32_t xDim, int32_t yDim) : m_xDim(xDim), m_yDim(yDim)
+    {
+        Check(hal_cuda_diffusion_create(xDim, yDim, &m_pHandle), "CudaDiffusionBackend2D");
+    }
+
+    CudaDiffusionBackend2D::~CudaDiffusionBackend2D()
+    {
+        hal_cuda_diffusion_destroy(m_pHandle);
+    }
+
+    void CudaDiffusionBackend2D::Diffuse(const std::vector<double> &field, std::vector<double> &deltas,
+                                         double diffRate, int32_t xDim, int32_t yDim, bool wrapX, bool wrapY)
+    {
+        Check(hal_cuda_diffuse(m_pHandle, field.data(), static_cast<int64_t>(field.size()), deltas.data(),
+                               static_cast<int64_t>(deltas.size()), diffRate, xDim, yDim, wrapX, wrapY),
+              "CudaDiffusionBackend2D::Diffuse");
+    }
+
+    void CudaDiffusionBackend2D::DiffuseDirichlet(const std::vector<double> &field, std::vector<double> &deltas,
+                                                  double diffRate, bool wrapX, bool wrapY,
+                                                  const std::vector<double> &ghost)
+    {
+        CheckCells(field, deltas, m_xDim, m_yDim, "CudaDiffusionBackend2D::DiffuseDirichlet");
+        CheckGhost(ghost.size(), m_xDim, m_yDim, "CudaDiffusionBackend2D::DiffuseDirichlet");
+        Check(hal_cuda_diffuse_bc(m_pHandle, field.data(), deltas.data(), diffRate, wrapX, wrapY, GhostOrNull(ghost)),
+              "CudaDiffusionBackend2D::DiffuseDirichlet");
+    }
+
+    void CudaDiffusionBackend2D::SetField(const std::vector<float> &field)
+    {
+        Check(hal_cuda_diffusion_set_field(m_pHandle, field.data(), static_cast<int64_t>(field.size())),
+              "CudaDiffusionBackend2D::SetField");
+    }
+
+    void CudaDiffusionBackend2D::GetField(std::vector<float> &field)
+    {
+        field.resize(static_cast<size_t>(m_xDim) * static_cast<size_t>(m_yDim));
+        Check(hal_cuda_diffusion_get_field(m_pHandle, field.data(), static_cast<int64_t>(field.size())),
+              "CudaDiffusionBackend2D::GetField");
+    }
+
+    void CudaDiffusionBackend2D::SetSource(const std::vector<float> &dense)
+    {
+        Check(hal_cuda_diffusion_set_source(m_pHandle, dense.empty() ? nullptr : dense.data(),
+                                            static_cast<int64_t>(dense.size())),
+              "CudaDiffusionBackend2D::SetSource");
+    }
+
+    void CudaDiffusionBackend2D::SetPointSources(const std::vector<int32_t> &cells, const std::vector<float> &values)
+    {
+        if (cells.size() != values.size())
+        {
+            Check(HAL_CUDA_EINVAL, "CudaDiffusionBackend2D::SetPointSources: cells and values differ in length");
+        }
+        Check(hal_cuda_diffusion_set_point_sources(m_pHandle, static_cast<int32_t>(cells.size()), cells.data(),
+                                                   values.data()),
+              "CudaDiffusionBackend2D::SetPointSources");
+    }
+
+    void CudaDiffusionBackend2D::SetDirichlet(const std::vector<float> &ghost)
+    {
+        CheckGhost(ghost.size(), m_xDim, m_yDim, "CudaDiffusionBackend2D::SetDirichlet");
+        Check(hal_cuda_diffusion_set_dirichlet(m_pHandle, GhostOrNull(ghost)), "CudaDiffusionBackend2D::SetDirichlet");
+    }
+
+    void CudaDiffusionBackend2D::RunTicks(int32_t ticks, double diffRate, double decay, bool wrapX, bool wrapY)
+    {
+        Check(hal_cuda_diffusion_run_ticks(m_pHandle, ticks, diffRate, decay, wrapX, wrapY),
+              "CudaDiffusionBackend2D::RunTicks");
+    }
+
+    void CudaDiffusionBackend2D::Sync()
+    {
+        Check(hal_cuda_diffusion_sync(m_pHandle), "CudaDiffusionBackend2D::Sync");
+    }
+
+    void CudaDiffusionBackend2D::RunSteps(std::vector<float> &field, int32_t steps, double diffRate, bool wrapX,
+                                          bool wrapY)
+    {
+        Check(hal_cuda_diffusion_run_steps(m_pHandle, field.data(), static_cast<int64_t>(field.size()), steps,
+                                           diffRate, wrapX, wrapY),
+              "CudaDiffusionBackend2D::RunSteps");
+    }
+
+    // ---- ADI ------------------------------------------------------------------
+
+    CudaAdiDiffusionBackend2D::CudaAdiDiffusionBackend2D(int32_t xDim, int32_t yDim) : m_xDim(xDim), m_yDim(yDim)
+    {
+        Check(hal_cuda_adi_create(xDim, yDim, &m_pHandle), "CudaAdiDiffusionBackend2D");
+    }
+
+    CudaAdiDiffusionBackend2D::~CudaAdiDiffusionBackend2D()
+    {
+        hal_cuda_adi_destroy(m_pHandle);
+    }
+
+    void CudaAdiDiffusionBackend2D::DiffuseADI(const std::vector<double> &field, std::vector<double> &deltas,
+                                               double diffRate, int32_t xDim, int32_t yDim, bool wrapX, bool wrapY)
+    {
+        Check(hal_cuda_diffuse_adi(m_pHandle, field.data(), static_cast<int64_t>(field.size()), deltas.data(),
+                                   static_cast<int64_t>(deltas.size()), diffRate, xDim, yDim, wrapX, wrapY),
+              "CudaAdiDiffusionBackend2D::DiffuseADI");
+    }
+
+    void CudaAdiDiffusionBackend2D::DiffuseADIDirichlet(const std::vector<double> &field,
+                                                        std::vector<double> &deltas, double diffRate, bool wrapX,
+                                                        bool wrapY, const std::vector<double> &ghost)
+    {
+        CheckCells(field, deltas, m_xDim, m_yDim, "CudaAdiDiffusionBackend2D::DiffuseADIDirichlet");
+        CheckGhost(ghost.size(), m_xDim, m_yDim, "CudaAdiDiffusionBackend2D::DiffuseADIDirichlet");
+        Check(hal_cuda_diffuse_adi_bc(m_pHandle, field.data(), deltas.data(), diffRate, wrapX, wrapY,
+                                      GhostOrNull(ghost)),
+              "CudaAdiDiffusionBackend2D::DiffuseADIDirichlet");
+    }
+
+    void CudaAdiDiffusionBackend2D::SetField(const std::vector<float> &field)
+    {
+        Check(hal_cuda_adi_set_field(m_pHandle, field.data(), static_cast<int64_t>(field.size())),
+              "CudaAdiDiffusionBackend2D::SetField");
+    }
+
+    void CudaAdiDiffusionBackend2D::GetField(std::vector<float> &field)
+    {
+        field.resize(static_cast<size_t>(m_xDim) * static_cast<size_t>(m_yDim));
+        Check(hal_cuda_adi_get_field(m_pHandle, field.data(), static_cast<int64_t>(field.size())),
+              "CudaAdiDiffusionBackend2D::GetField");
+    }
+
+    void CudaAdiDiffusionBackend2D::SetSource(const std::vector<float> &dense)
+    {
+        Check(hal_cuda_adi_set_source(m_pHandle, dense.empty() ? nullptr : dense.data(),
+                                      static_cast<int64_t>(dense.size())),
+              "CudaAdiDiffusionBackend2D::SetSource");
+    }
+
+    void CudaAdiDiffusionBackend2D::SetDirichlet(const std::vector<float> &ghost)
+    {
+        CheckGhost(ghost.size(), m_xDim, m_yDim, "CudaAdiDiffusionBackend2D::SetDirichlet");
+        Check(hal_cuda_adi_set_dirichlet(m_pHandle, GhostOrNull(ghost)), "CudaAdiDiffusionBackend2D::SetDirichlet");
+    }
+
+    void CudaAdiDiffusionBackend2D::SetUptake(CudaAgentForceBackend2D *pAgents, double uptake)
+    {
+        Check(hal_cuda_adi_set_uptake(m_pHandle, pAgents ? pAgents->Handle() : nullptr, uptake),
+              "CudaAdiDiffusionBackend2D::SetUptake");
+    }
+
+    void CudaAdiDiffusionBackend2D::RunTicks(int32_t ticks, double diffRate, double decay, bool wrapX, bool wrapY)
+    {
+        Check(hal_cuda_adi_run_ticks(m_pHandle, ticks, diffRate, decay, wrapX, wrapY),
+              "CudaAdiDiffusionBackend2D::RunTicks");
+    }
+
+    void CudaAdiDiffusionBackend2D::Sync()
+    {
+        Check(hal_cuda_adi_sync(m_pHandle), "CudaAdiDiffusionBackend2D::Sync");
+    }
+
+    void CudaAdiDiffusionBackend2D::RunSteps(std::vector<float> &field, int32_t steps, double diffRate, bool wrapX,
+                                             bool wrapY)
+    {
+        Check(hal_cuda_adi_run_steps(m_pHandle, field.data(), static_cast<int64_t>(field.size()), steps, diffRate,
+                                     wrapX, wrapY),
+              "CudaAdiDiffusionBackend2D::RunSteps");
+    }
+
+    // ---- agent forces ---------------------------------------------------------
+
+    CudaAgentForceBackend2D::CudaAgentForceBackend2D(int32_t xDim, int32_t yDim, int32_t maxAgents)
+        : m_xDim(xDim), m_yDim(yDim), m_maxAgents(maxAgents)
+    {
+        Check(hal_cuda_agents_create(xDim, yDim, maxAgents, &m_pHandle), "CudaAgentForceBackend2D");
+    }
+
+    CudaAgentForceBackend2D::~CudaAgentForceBackend2D()
+    {
+        hal_cuda_agents_destroy(m_pHandle);
+    }
+
+    void CudaAgentForceBackend2D::AccumulateForces(const std::vector<double> &positions,
+                                                   const std::vector<double> &radii,
+                                                   std::vector<double> &velocityDeltas, double interactionRad,
+                                                   double springConstant, int32_t xDim, int32_t yDim, bool wrapX,
+                                                   bool wrapY)
+    {
+        if (positions.size() != 2 * radii.size())
+        {
+            Check(HAL_CUDA_EINVAL, "CudaAgentForceBackend2D::AccumulateForces: positions must hold two values per "
+                                   "radius");
+        }
+        velocityDeltas.resize(positions.size());
+        Check(hal_cuda_accumulate_forces(m_pHandle, positions.data(), static_cast<int64_t>(positions.size()),
+                                         radii.data(), static_cast<int64_t>(radii.size()), velocityDeltas.data(),
+                                         interactionRad, springConstant, xDim, yDim, wrapX, wrapY),
+              "CudaAgentForceBackend2D::AccumulateForces");
+        m_count = static_cast<int32_t>(radii.size());
+    }
+
+    void CudaAgentForceBackend2D::Upload(const std::vector<float> &positions, const std::vector<float> &radii)
+    {
+        if (positions.size() != 2 * radii.size())
+        {
+            Check(HAL_CUDA_EINVAL, "CudaAgentForceBackend2D::Upload: positions must hold two values per radius");
+        }
+        Check(hal_cuda_agents_upload(m_pHandle, positions.data(), radii.data(), static_cast<int32_t>(radii.size())),
+              "CudaAgentForceBackend2D::Upload");
+        m_count = static_cast<int32_t>(radii.size());
+    }
+
+    void CudaAgentForceBackend2D::Dispatch(double interactionRad, double springConstant, bool wrapX, bool wrapY)
+    {
+        Check(hal_cuda_agents_dispatch(m_pHandle, interactionRad, springConstant, wrapX, wrapY),
+              "CudaAgentForceBackend2D::Dispatch");
+    }
+
+    void CudaAgentForceBackend2D::Download(std::vector<float> &velocityDeltas)
+    {
+        velocityDeltas.resize(2 * static_cast<size_t>(m_count));
+        Check(hal_cuda_agents_download(m_pHandle, velocityDeltas.data(), m_count), "CudaAgentForceBackend2D::Download");
+    }
+
+    void CudaAgentForceBackend2D::GetBins(std::vector<int32_t> &cellOffsets, std::vector<int32_t> &bucketAgents)
+    {
+        cellOffsets.resize(static_cast<size_t>(m_xDim) * static_cast<size_t>(m_yDim) + 1);
+        bucketAgents.resize(static_cast<size_t>(m_count));
+        Check(hal_cuda_agents_get_bins(m_pHandle, cellOffsets.data(), bucketAgents.empty() ? nullptr : bucketAgents.data()),
+              "CudaAgentForceBackend2D::GetBins");
+    }
+}

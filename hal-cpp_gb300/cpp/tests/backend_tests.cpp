@@ -1,0 +1,382 @@
+// Tests of the Hal::Cuda backends through HAL's strategy interfaces, in the
+// shape of the reference's own interface tests: every check runs against an
+// IDiffusionBackend2D& / IAdiDiffusionBackend2D& / IAgentForceBackend2D&
+// (tests/IDiffusionBackend2DTests.cpp:23-144,
+// tests/IAgentForceBackend2DTests.cpp:25-165, tests/AdiKernel2DTests.cpp:18-141),
+// with the CPU oracle (oracle/hal_oracle.h) as the checker where the
+// reference compares against its CPU backend.
+//
+// Prints one line per check and "backend_tests: N passed, M failed"; the exit
+// status is 0 only if every check passed.
+#include "Hal/Cuda/CudaBackends2D.h"
+
+extern "C"
+{
+#include "hal_oracle.h"
+}
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace
+{
+    int g_passed = 0;
+    int g_failed = 0;
+
+    void Report(const char *pName, bool ok, const std::string &detail)
+    {
+        std::printf("%s %s %s\n", ok ? "PASS" : "FAIL", pName, detail.c_str());
+        (ok ? g_passed : g_failed)++;
+    }
+
+    void Run(const char *pName, const std::function<std::string()> &body)
+    {
+        try
+        {
+            std::string err = body();
+            Report(pName, err.empty(), err);
+        }
+        catch (const std::exception &e)
+        {
+            Report(pName, false, std::string("exception: ") + e.what());
+        }
+    }
+
+    double MaxAbs(const std::vector<double> &a)
+    {
+        double m = 0.0;
+        for (double v : a)
+        {
+            m = std::fmax(m, std::fabs(v));
+        }
+        return m;
+    }
+
+    double MaxAbsDiff(const std::vector<double> &a, const std::vector<double> &b)
+    {
+        double m = 0.0;
+        for (size_t i = 0; i < a.size(); i++)
+        {
+            m = std::fmax(m, std::fabs(a[i] - b[i]));
+        }
+        return m;
+    }
+
+    std::string Fmt(const char *pFmt, double v)
+    {
+        char buf[128];
+        std::snprintf(buf, sizeof(buf), pFmt, v);
+        return buf;
+    }
+
+    // cos(2 pi x / nx) cos(2 pi y / ny): an eigenvector of both axis
+    // Laplacians on a periodic grid.
+    std::vector<double> Eigenmode(int32_t nx, int32_t ny)
+    {
+        std::vector<double> f(static_cast<size_t>(nx) * ny);
+        const double pi = 3.14159265358979323846;
+        for (int32_t x = 0; x < nx; x++)
+        {
+            for (int32_t y = 0; y < ny; y++)
+            {
+                f[static_cast<size_t>(x) * ny + y] = std::cos(2 * pi * x / nx) * std::cos(2 * pi * y / ny);
+            }
+        }
+        return f;
+    }
+
+    // Explicit step: one Diffuse on the eigenmode scales it by
+    // 1 - 4 r (sin^2(pi/nx) + sin^2(pi/ny)); the result also equals the CPU
+    // stencil bit for bit.
+    std::string ExplicitEigenmode(Hal::IDiffusionBackend2D &backend)
+    {
+        const int32_t nx = 16, ny = 20;
+        const double r = 0.05;
+        const double pi = 3.14159265358979323846;
+        std::vector<double> f = Eigenmode(nx, ny);
+        std::vector<double> d(f.size(), 0.0);
+        backend.Diffuse(f, d, r, nx, ny, true, true);
+        const double sx = std::sin(pi / nx), sy = std::sin(pi / ny);
+        const double lambda = 1.0 - 4.0 * r * (sx * sx + sy * sy);
+        double err = 0.0;
+        for (size_t i = 0; i < f.size(); i++)
+        {
+            err = std::fmax(err, std::fabs(f[i] + d[i] - lambda * f[i]));
+        }
+        std::vector<double> exp(f.size(), 0.0);
+        oracle_diffusion2(f.data(), exp.data(), r, nx, ny, 1, 1, nullptr);
+        if (err > 1e-4)
+        {
+            return Fmt("eigenmode error %.3e > 1e-4", err);
+        }
+        if (std::memcmp(exp.data(), d.data(), d.size() * sizeof(double)) != 0)
+        {
+            return "deltas differ from the CPU stencil";
+        }
+        return "";
+    }
+
+    // ADI step on the eigenmode: the Crank-Nicolson factor of each axis,
+    // (1 + r/2 mu) / (1 - r/2 mu) with mu = -4 sin^2(pi/n).
+    std::string AdiEigenmode(Hal::IAdiDiffusionBackend2D &backend)
+    {
+        const int32_t nx = 12, ny = 18;
+        const double r = 0.3;
+        const double pi = 3.14159265358979323846;
+        std::vector<double> f = Eigenmode(nx, ny);
+        std::vector<double> d(f.size(), 0.0);
+        backend.DiffuseADI(f, d, r, nx, ny, true, true);
+        const double mx = -4.0 * std::pow(std::sin(pi / nx), 2), my = -4.0 * std::pow(std::sin(pi / ny), 2);
+        const double g = (1 + 0.5 * r * mx) / (1 - 0.5 * r * mx) * (1 + 0.5 * r * my) / (1 - 0.5 * r * my);
+        double err = 0.0;
+        for (size_t i = 0; i < f.size(); i++)
+        {
+            err = std::fmax(err, std::fabs(f[i] + d[i] - g * f[i]));
+        }
+        return err <= 1e-4 ? "" : Fmt("CN factor error %.3e > 1e-4", err);
+    }
+
+    // ADI against the CPU solver cell for cell (zero-flux and periodic), and
+    // mass conservation with zero-flux edges.
+    std::string AdiMatchesCpu(Hal::IAdiDiffusionBackend2D &backend)
+    {
+        const int32_t nx = 20, ny = 14;
+        std::vector<double> f(static_cast<size_t>(nx) * ny);
+        for (int32_t x = 0; x < nx; x++)
+        {
+            for (int32_t y = 0; y < ny; y++)
+            {
+                f[static_cast<size_t>(x) * ny + y] = 1.0 + 0.3 * x - 0.2 * y + 0.5 * std::sin(0.7 * x * y);
+            }
+        }
+        for (int wrap = 0; wrap < 2; wrap++)
+        {
+            std::vector<double> d(f.size(), 0.0), exp(f.size(), 0.0), scratch(f.size());
+            backend.DiffuseADI(f, d, 0.6, nx, ny, wrap, wrap);
+            oracle_adi2(f.data(), scratch.data(), exp.data(), 0.6, nx, ny, wrap, wrap, nullptr);
+            const double err = MaxAbsDiff(d, exp) / MaxAbs(f);
+            if (err > 1e-5)
+            {
+                return Fmt("ADI differs from the CPU solver: %.3e", err);
+            }
+            double mass = 0.0;
+            for (double v : d)
+            {
+                mass += v;
+            }
+            if (std::fabs(mass) > 1e-3)
+            {
+                return Fmt("mass not conserved: %.3e", mass);
+            }
+        }
+        return "";
+    }
+
+    // Cell-bucket forces against an all-pairs sum with no buckets.
+    std::string BruteForceForces(Hal::IAgentForceBackend2D &backend)
+    {
+        const int32_t dim = 16, n = 60;
+        const double R = 3.0, k = 0.4;
+        oracle_rand rng;
+        oracle_rand_init(&rng, 1234);
+        std::vector<double> pos(2 * n), rad(n);
+        for (int32_t i = 0; i < n; i++)
+        {
+            pos[2 * i] = oracle_rand_double(&rng) * dim;
+            pos[2 * i + 1] = oracle_rand_double(&rng) * dim;
+            rad[i] = 0.4 + 0.4 * oracle_rand_double(&rng);
+        }
+        std::vector<double> v;
+        backend.AccumulateForces(pos, rad, v, R, k, dim, dim, true, true);
+        std::vector<double> exp(2 * n, 0.0);
+        for (int32_t i = 0; i < n; i++)
+        {
+            for (int32_t j = 0; j < n; j++)
+            {
+                if (j == i)
+                {
+                    continue;
+                }
+                double dx = pos[2 * j] - pos[2 * i], dy = pos[2 * j + 1] - pos[2 * i + 1];
+                dx -= dim * std::round(dx / dim);
+                dy -= dim * std::round(dy / dim);
+                const double dist = std::sqrt(dx * dx + dy * dy);
+                if (dist > 0.0 && dist < R)
+                {
+                    const double force = k * ((rad[i] + rad[j]) - dist);
+                    exp[2 * i] -= dx / dist * force;
+                    exp[2 * i + 1] -= dy / dist * force;
+                }
+            }
+        }
+        const double err = MaxAbsDiff(v, exp);
+        return err <= 1e-12 ? "" : Fmt("all-pairs difference %.3e > 1e-12", err);
+    }
+
+    // Bins and FP64 forces equal the CPU backend bit for bit on float32
+    // positions.
+    std::string ForcesMatchCpu(Hal::Cuda::CudaAgentForceBackend2D &backend)
+    {
+        const int32_t dim = 64, n = 4000;
+        oracle_rand rng;
+        oracle_rand_init(&rng, 7);
+        std::vector<double> pos(2 * n), rad(n, 0.5);
+        for (int32_t i = 0; i < 2 * n; i++)
+        {
+            pos[i] = static_cast<double>(static_cast<float>(oracle_rand_double(&rng) * dim));
+        }
+        std::vector<double> v;
+        backend.AccumulateForces(pos, rad, v, 1.0, 0.1, dim, dim, false, false);
+        std::vector<double> exp(2 * n);
+        std::vector<int32_t> off(static_cast<size_t>(dim) * dim + 1), bucket(n);
+        oracle_accumulate_forces(pos.data(), rad.data(), n, exp.data(), 1.0, 0.1, dim, dim, 0, 0, off.data(),
+                                 bucket.data(), 1);
+        std::vector<int32_t> gotOff, gotBucket;
+        backend.GetBins(gotOff, gotBucket);
+        if (gotOff != off || gotBucket != bucket)
+        {
+            return "bins differ from the CPU backend";
+        }
+        if (std::memcmp(v.data(), exp.data(), v.size() * sizeof(double)) != 0)
+        {
+            return "FP64 forces differ from the CPU backend";
+        }
+        return "";
+    }
+
+    std::string CoincidentAgents(Hal::IAgentForceBackend2D &backend)
+    {
+        std::vector<double> pos = {4.0, 4.0, 4.0, 4.0}, rad = {0.5, 0.5}, v;
+        backend.AccumulateForces(pos, rad, v, 2.0, 1.0, 8, 8, false, false);
+        if (v.size() != 4)
+        {
+            return "velocityDeltas not resized";
+        }
+        for (double x : v)
+        {
+            if (x != 0.0)
+            {
+                return "coincident agents pushed apart or NaN";
+            }
+        }
+        return "";
+    }
+
+    template <typename Fn>
+    std::string Throws(Fn fn, const char *pWhat)
+    {
+        try
+        {
+            fn();
+        }
+        catch (const std::invalid_argument &)
+        {
+            return "";
+        }
+        return std::string(pWhat) + " did not throw std::invalid_argument";
+    }
+
+    std::string SizeMismatches(Hal::IDiffusionBackend2D &diff, Hal::IAdiDiffusionBackend2D &adi,
+                               Hal::IAgentForceBackend2D &agents)
+    {
+        std::vector<double> f(16 * 20), d(16 * 20 - 1), v;
+        std::string e = Throws([&] { diff.Diffuse(f, d, 0.1, 16, 20, false, false); }, "Diffuse");
+        if (e.empty())
+        {
+            std::vector<double> f2(12 * 18), d2(12 * 17);
+            e = Throws([&] { adi.DiffuseADI(f2, d2, 0.1, 12, 18, false, false); }, "DiffuseADI");
+        }
+        if (e.empty())
+        {
+            std::vector<double> pos(5), rad(2);
+            e = Throws([&] { agents.AccumulateForces(pos, rad, v, 1.0, 1.0, 16, 16, false, false); },
+                       "AccumulateForces");
+        }
+        return e;
+    }
+
+    // Resident ticks (PDEGrid2D semantics: decay, dense source, Dirichlet)
+    // against the CPU tick, explicit and ADI.
+    std::string ResidentTicks(Hal::Cuda::CudaDiffusionBackend2D &diff, Hal::Cuda::CudaAdiDiffusionBackend2D &adi)
+    {
+        const int32_t nx = diff.XDim(), ny = diff.YDim();
+        const size_t cells = static_cast<size_t>(nx) * ny;
+        oracle_rand rng;
+        oracle_rand_init(&rng, 99);
+        std::vector<double> f(cells), src(cells), ghost(2 * (nx + ny), 0.0);
+        for (size_t i = 0; i < cells; i++)
+        {
+            f[i] = static_cast<float>(oracle_rand_double(&rng));
+            src[i] = static_cast<float>(0.01 * oracle_rand_double(&rng));
+        }
+        for (int32_t y = 0; y < ny; y++)
+        {
+            ghost[y] = 1.0;  // bc(-1, y) = 1, 0 elsewhere
+        }
+        std::vector<float> f32(f.begin(), f.end()), s32(src.begin(), src.end()), g32(ghost.begin(), ghost.end());
+        for (int mode = 0; mode < 2; mode++)
+        {
+            const double r = mode == 0 ? 0.2 : 5.0;
+            const int ticks = 30;
+            std::vector<double> exp = f, deltas(cells, 0.0), scratch(cells);
+            for (int t = 0; t < ticks; t++)
+            {
+                oracle_tick(mode, exp.data(), deltas.data(), scratch.data(), nx, ny, r, 0, 0, ghost.data(), 0.01,
+                            src.data(), 0, nullptr, nullptr, nullptr, 0.0, 1);
+            }
+            std::vector<float> got;
+            if (mode == 0)
+            {
+                diff.SetField(f32);
+                diff.SetSource(s32);
+                diff.SetDirichlet(g32);
+                diff.RunTicks(ticks, r, 0.01, false, false);
+                diff.GetField(got);
+            }
+            else
+            {
+                adi.SetField(f32);
+                adi.SetSource(s32);
+                adi.SetDirichlet(g32);
+                adi.RunTicks(ticks, r, 0.01, false, false);
+                adi.GetField(got);
+            }
+            std::vector<double> got64(got.begin(), got.end());
+            const double err = MaxAbsDiff(got64, exp) / MaxAbs(exp);
+            if (err > 1e-5)
+            {
+                return Fmt(mode == 0 ? "explicit ticks differ: %.3e" : "ADI ticks differ: %.3e", err);
+            }
+        }
+        return "";
+    }
+}
+
+int main()
+{
+    Hal::Cuda::CudaDiffusionBackend2D diffEig(16, 20);
+    Hal::Cuda::CudaAdiDiffusionBackend2D adiEig(12, 18);
+    Hal::Cuda::CudaAdiDiffusionBackend2D adiCpu(20, 14);
+    Hal::Cuda::CudaAgentForceBackend2D agents16(16, 16, 64);
+    Hal::Cuda::CudaAgentForceBackend2D agents64(64, 64, 4000);
+    Hal::Cuda::CudaAgentForceBackend2D agents8(8, 8, 4);
+    Hal::Cuda::CudaDiffusionBackend2D diffTick(40, 33);
+    Hal::Cuda::CudaAdiDiffusionBackend2D adiTick(40, 33);
+
+    Run("explicit_eigenmode", [&] { return ExplicitEigenmode(diffEig); });
+    Run("adi_crank_nicolson_factor", [&] { return AdiEigenmode(adiEig); });
+    Run("adi_matches_cpu_and_conserves_mass", [&] { return AdiMatchesCpu(adiCpu); });
+    Run("forces_match_all_pairs", [&] { return BruteForceForces(agents16); });
+    Run("forces_and_bins_match_cpu", [&] { return ForcesMatchCpu(agents64); });
+    Run("coincident_agents", [&] { return CoincidentAgents(agents8); });
+    Run("size_mismatch_throws", [&] { return SizeMismatches(diffEig, adiEig, agents16); });
+    Run("resident_ticks_match_cpu", [&] { return ResidentTicks(diffTick, adiTick); });
+
+    std::printf("backend_tests: %d passed, %d failed\n", g_passed, g_failed);
+    return g_failed == 0 ? 0 : 1;
+}

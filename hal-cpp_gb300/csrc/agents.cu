@@ -14,12 +14,13 @@
 //   Forces       one thread per sorted slot walks the cell window x-major then
 //                y, and each cell's slots in order -- the CPU's summation
 //                order -- and writes the agent's velocity delta.
-// The binning is integer work and matches the CPU bit for bit (positions are
-// float32 on the device; the CPU fed the same float32 values bins
-// identically).  The force sum runs in FP32 on the resident path and in FP64
-// with IEEE round-to-nearest operations (no contraction) on the FP64
-// interface path, where it matches the CPU backend bit for bit for float32
-// positions.
+// The binning is integer work and matches the CPU bit for bit: the cell of a
+// position is floored in the precision the caller gave it (FP64 on the
+// interface path, as the CPU does; FP32 on the resident path, where the CPU
+// fed the same float32 values bins identically).  The force sum runs in FP32
+// on the resident path and in FP64 with IEEE round-to-nearest operations (no
+// contraction) on the FP64 interface path, where positions stay FP64 end to
+// end and the result matches the CPU backend bit for bit.
 #include "common.cuh"
 
 #include <cmath>
@@ -32,10 +33,34 @@ namespace halcuda
         constexpr int kScanItems = 4;
         constexpr int kScanTile = kScanThreads * kScanItems;
 
-        // AgentForceCellCoord (CpuAgentForceBackend2D.cpp:14-27).
-        __device__ __forceinline__ int32_t CellCoord(float v, int32_t dim)
+        // Position pairs in the precision of the path: float2 on the FP32
+        // resident path, double2 on the FP64 interface path.
+        template <typename T>
+        struct Vec2;
+        template <>
+        struct Vec2<float>
         {
-            int32_t c = static_cast<int32_t>(floorf(v));
+            using Type = float2;
+            __device__ static float2 Make(float x, float y) { return make_float2(x, y); }
+        };
+        template <>
+        struct Vec2<double>
+        {
+            using Type = double2;
+            __device__ static double2 Make(double x, double y) { return make_double2(x, y); }
+        };
+        template <typename T>
+        using V2 = typename Vec2<T>::Type;
+
+        // AgentForceCellCoord (CpuAgentForceBackend2D.cpp:14-27): the floor is
+        // taken in the precision of the positions, as the CPU takes it in FP64.
+        __device__ __forceinline__ int32_t Floor32(float v) { return static_cast<int32_t>(floorf(v)); }
+        __device__ __forceinline__ int32_t Floor32(double v) { return static_cast<int32_t>(floor(v)); }
+
+        template <typename TP>
+        __device__ __forceinline__ int32_t CellCoord(TP v, int32_t dim)
+        {
+            int32_t c = Floor32(v);
             c = (c < 0) ? 0 : c;
             c = (c >= dim) ? dim - 1 : c;
             return c;
@@ -43,7 +68,7 @@ namespace halcuda
 
         template <typename TP>
         __global__ void BinCount(const TP *__restrict__ pos, int32_t n, int32_t xDim, int32_t yDim,
-                                 float2 *__restrict__ posF, int32_t *__restrict__ cellOf,
+                                 V2<TP> *__restrict__ posF, int32_t *__restrict__ cellOf,
                                  int32_t *__restrict__ arrival, int32_t *__restrict__ counts)
         {
             int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -51,9 +76,9 @@ namespace halcuda
             {
                 return;
             }
-            float px = static_cast<float>(pos[2 * static_cast<int64_t>(i)]);
-            float py = static_cast<float>(pos[2 * static_cast<int64_t>(i) + 1]);
-            posF[i] = make_float2(px, py);
+            const TP px = pos[2 * static_cast<int64_t>(i)];
+            const TP py = pos[2 * static_cast<int64_t>(i) + 1];
+            posF[i] = Vec2<TP>::Make(px, py);
             int32_t c = CellCoord(px, xDim) * yDim + CellCoord(py, yDim);
             cellOf[i] = c;
             arrival[i] = atomicAdd(counts + c, 1);
@@ -196,11 +221,11 @@ namespace halcuda
         // The CPU scatters in agent-index order (CpuAgentForceBackend2D.cpp:
         // 100-109), so an agent's slot within its cell is the number of
         // lower-indexed agents in the same cell.
-        template <typename TR>
+        template <typename TP, typename TR>
         __global__ void Stabilize(const int32_t *__restrict__ cellOf, const int32_t *__restrict__ offsets,
-                                  const int32_t *__restrict__ bucketTmp, const float2 *__restrict__ posF,
+                                  const int32_t *__restrict__ bucketTmp, const V2<TP> *__restrict__ posF,
                                   const TR *__restrict__ rad, int32_t n, int32_t *__restrict__ bucket,
-                                  float2 *__restrict__ sPos, TR *__restrict__ sRad)
+                                  V2<TP> *__restrict__ sPos, TR *__restrict__ sRad)
         {
             int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
             if (i >= n)
@@ -250,7 +275,7 @@ namespace halcuda
         // Pass 4 (CpuAgentForceBackend2D.cpp:112-175) over cell-sorted slots.
         template <typename T, typename TV>
         __global__ void Forces(const int32_t *__restrict__ bucket, const int32_t *__restrict__ offsets,
-                               const float2 *__restrict__ sPos, const T *__restrict__ sRad, int32_t n,
+                               const V2<T> *__restrict__ sPos, const T *__restrict__ sRad, int32_t n,
                                double interactionRad, T R, T k, int32_t xDim, int32_t yDim, int32_t wrapX,
                                int32_t wrapY, TV *__restrict__ vel)
         {
@@ -260,9 +285,9 @@ namespace halcuda
                 return;
             }
             const int32_t i = bucket[slot];
-            const float2 pf = sPos[slot];
-            const T px = static_cast<T>(pf.x);
-            const T py = static_cast<T>(pf.y);
+            const V2<T> pf = sPos[slot];
+            const T px = pf.x;
+            const T py = pf.y;
             const T rad = sRad[slot];
             // window bounds in FP64, as the CPU computes them
             int32_t xStart = static_cast<int32_t>(floor(static_cast<double>(pf.x) - interactionRad));
@@ -318,9 +343,9 @@ namespace halcuda
                         {
                             continue;
                         }
-                        const float2 pj = sPos[q];
-                        const T xComp = Disp(px, static_cast<T>(pj.x), xDimF, wrapX != 0);
-                        const T yComp = Disp(py, static_cast<T>(pj.y), yDimF, wrapY != 0);
+                        const V2<T> pj = sPos[q];
+                        const T xComp = Disp(px, pj.x, xDimF, wrapX != 0);
+                        const T yComp = Disp(py, pj.y, yDimF, wrapY != 0);
                         const T dist = Sqrt(Add(Mul(xComp, xComp), Mul(yComp, yComp)));
                         if ((dist < R) && (dist > T(0)))
                         {
@@ -347,6 +372,7 @@ namespace halcuda
         DevBuf<float> pos32, rad32, vel32;
         DevBuf<double> pos64, rad64, vel64;
         DevBuf<float2> posF, sPos;
+        DevBuf<double2> posD, sPosD;  // FP64 interface path
         DevBuf<float> sRad32;
         DevBuf<double> sRad64;
         DevBuf<int32_t> cellOf, arrival, counts, offsets, tileSums, bucketTmp, bucket;
@@ -385,6 +411,11 @@ namespace halcuda
         // Bins n agents (positions of type TP, interleaved x,y) and sorts
         // radii of type TR alongside.  With ev != nullptr, records an event
         // after each stage (count, scan, scatter, stabilize) for profiling.
+        V2<float> *PosBuf(float) { return posF.p; }
+        V2<double> *PosBuf(double) { return posD.p; }
+        V2<float> *SortedPosBuf(float) { return sPos.p; }
+        V2<double> *SortedPosBuf(double) { return sPosD.p; }
+
         template <typename TP, typename TR>
         int Bin(const TP *pos, const TR *rad, TR *sRad, cudaStream_t s, cudaEvent_t *ev = nullptr)
         {
@@ -394,7 +425,8 @@ namespace halcuda
             unsigned ablocks = static_cast<unsigned>((n + T - 1) / T);
             if (n > 0)
             {
-                BinCount<TP><<<ablocks, T, 0, s>>>(pos, n, xDim, yDim, posF.p, cellOf.p, arrival.p, counts.p);
+                BinCount<TP><<<ablocks, T, 0, s>>>(pos, n, xDim, yDim, PosBuf(TP()), cellOf.p, arrival.p,
+                                                   counts.p);
                 CountLaunch();
             }
             if (ev)
@@ -420,8 +452,8 @@ namespace halcuda
             }
             if (n > 0)
             {
-                Stabilize<TR><<<ablocks, T, 0, s>>>(cellOf.p, offsets.p, bucketTmp.p, posF.p, rad, n, bucket.p,
-                                                    sPos.p, sRad);
+                Stabilize<TP, TR><<<ablocks, T, 0, s>>>(cellOf.p, offsets.p, bucketTmp.p, PosBuf(TP()), rad, n,
+                                                        bucket.p, SortedPosBuf(TP()), sRad);
                 CountLaunch();
             }
             if (ev)
@@ -440,7 +472,7 @@ namespace halcuda
             }
             const int T_ = 128;
             unsigned blocks = static_cast<unsigned>((n + T_ - 1) / T_);
-            Forces<T, TV><<<blocks, T_, 0, s>>>(bucket.p, offsets.p, sPos.p, sRad, n, R, static_cast<T>(R),
+            Forces<T, TV><<<blocks, T_, 0, s>>>(bucket.p, offsets.p, SortedPosBuf(T()), sRad, n, R, static_cast<T>(R),
                                                 static_cast<T>(k), xDim, yDim, wrapX, wrapY, vel);
             CountLaunch();
             return LaunchStatus("agent forces");
@@ -531,13 +563,15 @@ extern "C" int hal_cuda_accumulate_forces(hal_cuda_agents *h, const double *posi
                 interactionRad, kMaxInteractionRad);
     using namespace halcuda;
     HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
-    if (h->pos64.p == nullptr)
+    if (h->sPosD.p == nullptr)  // the last of the FP64 buffers: all or none are allocated
     {
         size_t m = static_cast<size_t>(h->maxAgents > 0 ? h->maxAgents : 1);
         HAL_TRY(h->pos64.Alloc(2 * m, "cudaMalloc(agents64)"));
         HAL_TRY(h->rad64.Alloc(m, "cudaMalloc(agents64)"));
         HAL_TRY(h->vel64.Alloc(2 * m, "cudaMalloc(agents64)"));
         HAL_TRY(h->sRad64.Alloc(m, "cudaMalloc(agents64)"));
+        HAL_TRY(h->posD.Alloc(m, "cudaMalloc(agents64)"));
+        HAL_TRY(h->sPosD.Alloc(m, "cudaMalloc(agents64)"));
     }
     cudaStream_t s = h->stream.Get();
     h->n = static_cast<int32_t>(radLen);
@@ -844,7 +878,7 @@ extern "C" int hal_cuda_agents_forces_noalloc(const float *positions, const floa
     ScanTiles<<<1, kScanThreads, 0, s>>>(tileSums, static_cast<int32_t>(nTiles));
     ScanApply<<<nTiles, kScanThreads, 0, s>>>(counts, C, tileSums, offsets, n);
     Scatter<<<ablocks, T, 0, s>>>(cellOf, arrival, offsets, n, bucketTmp);
-    Stabilize<float><<<ablocks, T, 0, s>>>(cellOf, offsets, bucketTmp, posF, radii, n, bucket, sPos, sRad);
+    Stabilize<float, float><<<ablocks, T, 0, s>>>(cellOf, offsets, bucketTmp, posF, radii, n, bucket, sPos, sRad);
     const int TF = 128;
     Forces<float, float><<<static_cast<unsigned>((n + TF - 1) / TF), TF, 0, s>>>(
         bucket, offsets, sPos, sRad, n, interactionRad, static_cast<float>(interactionRad),

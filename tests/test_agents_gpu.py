@@ -1,8 +1,9 @@
 """Agent forces on the GPU against the oracle and the golden vectors.
 
 * bins (cell offsets and bucket order) are integer results: bit-exact;
-* the FP64 interface call (hal_cuda_accumulate_forces) sums in FP64 with
-  IEEE operations in the CPU's order: bit-exact for float32 positions;
+* the FP64 interface call (hal_cuda_accumulate_forces) keeps positions in
+  FP64 and sums with IEEE operations in the CPU's order: bit-exact for any
+  double positions;
 * the FP32 resident dispatch: max|err| <= 1e-4 * max|v| (float32 sums of
   up to a few dozen pair terms).
 """
@@ -135,3 +136,25 @@ def test_million_agent_workload(hal, oracle):
         off2, bucket2 = ag.get_bins()
     assert np.array_equal(off2, eoff) and np.array_equal(bucket2, eb)
     assert max_rel(v32, exp) <= 1e-4
+
+
+@pytest.mark.parametrize("wrap", [False, True])
+def test_fp64_positions_off_the_float_grid(hal, oracle, wrap):
+    """The FP64 interface path keeps positions in FP64: cells are floored in
+    FP64 (a position just below an integer stays in the lower cell, as on the
+    CPU) and the forces equal the CPU backend's bit for bit."""
+    rng = np.random.default_rng(21)
+    dim, n = 48, 6000
+    pos = rng.random(2 * n) * dim
+    # a sixth of the agents sit within 1e-12 of a cell boundary, on either side
+    k = n // 6
+    edges = rng.integers(1, dim, 2 * k).astype(np.float64)
+    pos[: 2 * k] = edges + rng.choice([-1e-12, -3e-15, 0.0, 3e-15, 1e-12], 2 * k)
+    rad = 0.3 + 0.4 * rng.random(n)
+    v_exp, off_exp, b_exp = oracle.accumulate_forces(pos, rad, 1.7, 0.3, dim, dim, int(wrap), int(wrap))
+    with hal.Agents(dim, dim, n) as ag:
+        v = ag.accumulate_forces(pos, rad, 1.7, 0.3, dim, dim, wrap, wrap)
+        off, b = ag.get_bins()
+    assert np.array_equal(off, off_exp)
+    assert np.array_equal(b, b_exp)
+    assert np.array_equal(v, v_exp)
