@@ -32,6 +32,7 @@
 //      with the commit terms applied on the way out.
 #include "common.cuh"
 #include "adi_plan.h"
+#include "adi_sweep.h"
 
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -55,16 +56,6 @@ namespace halcuda
         // bound of the mbarrier wait (ns of %globaltimer); the staged copies
         // take microseconds, so reaching it means the copies never landed
         constexpr unsigned long long kWaitLimitNs = 2000000000ull;
-
-        struct LinePlanDev
-        {
-            int32_t L, P, B, periodic, nlast;
-            float a;              // off-diagonal, a == c == -r/2
-            const float *coef;    // [3][kCoefCount][M]
-            const float *gband;   // [(P-1)][2B+1]
-            const float *zsm;     // [L], periodic only
-            float bog, invDenom;  // periodic: beta/gamma, 1/(1 + v.z_sm)
-        };
 
         // Thomas forward elimination and back substitution of one block with
         // the identity padding described in adi_plan.h.  The coefficients
@@ -235,39 +226,10 @@ namespace halcuda
             return t;
         }
 
-        enum SweepMode : int
-        {
-            kSweepW = 0,      // x-sweep: out (transposed) = w
-            kSweepTick = 1,   // y-sweep: out (transposed) = committed f'
-            kSweepPlain = 2,  // y-sweep: out (transposed) = v
-            kSweepDeltas = 3  // y-sweep: deltas (line-major, FP64) += v - f64
-        };
-
-        struct SweepParams
-        {
-            const float *in;          // Nlines lines of L floats, line-major
-            int32_t L, Nlines;
-            int32_t wrapLines;        // the explicit (cross-line) axis wraps
-            const float *ghostLo;     // Dirichlet ghost line before line 0 (L values) or null
-            const float *ghostHi;     // ghost line after line Nlines-1
-            const float *implLo;      // Dirichlet value before position 0, per line, or null
-            const float *implHi;      // Dirichlet value after position L-1, per line
-            float halfR, r;
-            LinePlanDev plan;         // lines of length L along the implicit axis
-            int32_t R, LS;            // lines per CTA, shared-memory line stride (floats)
-            float *out;               // transposed output: out[pos * Nlines + line]
-            const float *f;           // kSweepTick: field before the step (output layout)
-            const float *src;         // kSweepTick: dense source (output layout) or null
-            const int32_t *cellOffsets;  // kSweepTick: agent bins (line-major), or null
-            float negDecay, negUptake;
-            const double *f64;        // kSweepDeltas: field (line-major)
-            double *deltas;           // kSweepDeltas: deltas (line-major)
-            int32_t *err;             // set to 1 if a bounded wait gave up
-        };
-
+        // One CTA's tile of a sweep: lines x0 .. x0+R-1 of the grid p.  tmap
+        // is the grid's line tensor map (SWZ) or null.
         template <int MODE, bool SWZ>
-        __global__ void __launch_bounds__(kMaxThreads)
-            AdiSweep(SweepParams p, const __grid_constant__ CUtensorMap tmap)
+        __device__ __forceinline__ void SweepTile(const SweepParams &p, const CUtensorMap *tmap, const int32_t x0)
         {
             extern __shared__ __align__(16) float smem[];
             __shared__ __align__(8) unsigned long long mbar;
@@ -283,7 +245,6 @@ namespace halcuda
 
             const int tid = threadIdx.x;
             const int nthreads = blockDim.x;
-            const int32_t x0 = blockIdx.x * R;
             const int32_t L = p.L;
             const bool vecL = (L & 3) == 0;
 
@@ -308,7 +269,7 @@ namespace halcuda
                     asm volatile(
                         "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
                         " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(SmemAddr(sLines)),
-                        "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(0), "r"(0), "r"(x0 - 1), "r"(bar)
+                        "l"(reinterpret_cast<uint64_t>(tmap)), "r"(0), "r"(0), "r"(x0 - 1), "r"(bar)
                         : "memory");
                 }
                 for (int q = tid; q < kCoefFloats / 4; q += nthreads)
@@ -865,6 +826,23 @@ namespace halcuda
             }
         }
 
+        template <int MODE, bool SWZ>
+        __global__ void __launch_bounds__(kMaxThreads)
+            AdiSweep(SweepParams p, const __grid_constant__ CUtensorMap tmap)
+        {
+            SweepTile<MODE, SWZ>(p, &tmap, static_cast<int32_t>(blockIdx.x) * p.R);
+        }
+
+        // Batched form: CTA b runs tile tiles[b] = (grid, first line) of the
+        // table's grids, with the 36-float chunk staging (no tensor map).
+        template <int MODE>
+        __global__ void __launch_bounds__(kMaxThreads)
+            AdiSweepTiles(const SweepParams *__restrict__ table, const int2 *__restrict__ tiles)
+        {
+            const int2 t = tiles[blockIdx.x];
+            SweepTile<MODE, false>(table[t.x], nullptr, t.y);
+        }
+
         // out[c][r] = in[r][c] for an rows x cols matrix (32x32 tiles).
         template <typename TIn>
         __global__ void Transpose(const TIn *__restrict__ in, float *__restrict__ out, int32_t rows, int32_t cols)
@@ -1034,6 +1012,142 @@ namespace halcuda
                              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
             return r == CUDA_SUCCESS;
+        }
+    }
+}
+
+namespace halcuda
+{
+    static_assert(kSweepTileThreads == kMaxThreads, "batched sweep CTAs use the kernel's thread bound");
+
+    SweepTileShape SweepTileShapeFor(int32_t P)
+    {
+        // every tile CTA has kSweepTileThreads threads: as many lines as
+        // (R / kNL) * P threads allow, a power of two in [8, kMaxR]
+        SweepTileShape sh;
+        int32_t R = 8;
+        while (R * 2 <= kMaxR && (R * 2 / kNL) * P <= kSweepTileThreads)
+        {
+            R *= 2;
+        }
+        sh.R = R;
+        sh.LS = P * kChunkStride + 4;
+        sh.smem = 1024 + sizeof(float) * (static_cast<size_t>(kCoefFloats) + static_cast<size_t>(R + 2) * sh.LS +
+                                          2 * static_cast<size_t>(R) * P + 2 * static_cast<size_t>(R));
+        return sh;
+    }
+
+    namespace
+    {
+        template <int MODE>
+        int PrepareTiles(size_t smem)
+        {
+            static size_t s_enabled = 0;
+            if (smem > s_enabled)
+            {
+                HAL_TRY(CudaStatus(cudaFuncSetAttribute(AdiSweepTiles<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                        static_cast<int>(smem)),
+                                   "cudaFuncSetAttribute(AdiSweepTiles)"));
+                s_enabled = smem;
+            }
+            return HAL_CUDA_OK;
+        }
+
+        template <int MODE>
+        int LaunchTiles(const SweepParams *table, const int2 *tiles, int32_t nTiles, size_t smem, cudaStream_t s)
+        {
+            AdiSweepTiles<MODE><<<static_cast<unsigned>(nTiles), kSweepTileThreads, smem, s>>>(table, tiles);
+            CountLaunch();
+            return LaunchStatus("AdiSweepTiles");
+        }
+    }
+
+    int PrepareSweepTiles(int mode, size_t smem)
+    {
+        switch (mode)
+        {
+        case kSweepW:
+            return PrepareTiles<kSweepW>(smem);
+        case kSweepTick:
+            return PrepareTiles<kSweepTick>(smem);
+        default:
+            SetError("PrepareSweepTiles: unsupported mode %d", mode);
+            return HAL_CUDA_EINVAL;
+        }
+    }
+
+    AdiDevicePlan::~AdiDevicePlan()
+    {
+        cudaFree(m_pCoef);
+        cudaFree(m_pGband);
+        cudaFree(m_pZsm);
+    }
+
+    int AdiDevicePlan::Build(int32_t L, double r, int ends)
+    {
+        AdiLinePlanHost h;
+        if (!BuildAdiLinePlan(L, r, ends, h))
+        {
+            SetError("ADI line length %d outside [1, %d]", L, HAL_CUDA_ADI_MAX_LINE);
+            return HAL_CUDA_ENOTSUP;
+        }
+        if (!(h.selfCheck < 1e-5))
+        {
+            SetError("ADI plan self-check failed (L=%d, r=%g, rel err %g)", L, r, h.selfCheck);
+            return HAL_CUDA_ENOTSUP;
+        }
+        auto upload = [](const std::vector<float> &v, float **dst) {
+            if (v.empty())
+            {
+                return HAL_CUDA_OK;
+            }
+            HAL_TRY(CudaStatus(cudaMalloc(reinterpret_cast<void **>(dst), v.size() * sizeof(float)), "cudaMalloc(plan)"));
+            return CudaStatus(cudaMemcpy(*dst, v.data(), v.size() * sizeof(float), cudaMemcpyHostToDevice),
+                              "cudaMemcpy(plan)");
+        };
+        HAL_TRY(upload(h.coef, &m_pCoef));
+        HAL_TRY(upload(h.gband, &m_pGband));
+        HAL_TRY(upload(h.zsm, &m_pZsm));
+        m_dev = {};
+        m_dev.L = h.L;
+        m_dev.P = h.P;
+        m_dev.B = h.B;
+        m_dev.periodic = (ends == kEndsPeriodic) ? 1 : 0;
+        m_dev.nlast = h.L - (h.P - 1) * kAdiM;
+        m_dev.a = static_cast<float>(h.offDiag);
+        m_dev.coef = m_pCoef;
+        m_dev.gband = m_pGband;
+        m_dev.zsm = m_pZsm;
+        m_dev.bog = static_cast<float>(h.betaOverGamma);
+        m_dev.invDenom = static_cast<float>(h.invDenom);
+        return HAL_CUDA_OK;
+    }
+
+    int LaunchTranspose(const float *in, float *out, int32_t rows, int32_t cols, cudaStream_t s)
+    {
+        dim3 block(32, 8);
+        dim3 grid((cols + 31) / 32, (rows + 31) / 32);
+        Transpose<float><<<grid, block, 0, s>>>(in, out, rows, cols);
+        CountLaunch();
+        return LaunchStatus("Transpose launch");
+    }
+
+    int LaunchSweepTiles(int mode, const SweepParams *table, const int2 *tiles, int32_t nTiles, size_t smem,
+                         cudaStream_t s)
+    {
+        if (nTiles <= 0)
+        {
+            return HAL_CUDA_OK;
+        }
+        switch (mode)
+        {
+        case kSweepW:
+            return LaunchTiles<kSweepW>(table, tiles, nTiles, smem, s);
+        case kSweepTick:
+            return LaunchTiles<kSweepTick>(table, tiles, nTiles, smem, s);
+        default:
+            SetError("LaunchSweepTiles: unsupported mode %d", mode);
+            return HAL_CUDA_EINVAL;
         }
     }
 }

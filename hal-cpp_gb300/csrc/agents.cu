@@ -22,6 +22,7 @@
 // contraction) on the FP64 interface path, where positions stay FP64 end to
 // end and the result matches the CPU backend bit for bit.
 #include "common.cuh"
+#include "agents_wells.h"
 
 #include <cmath>
 
@@ -272,19 +273,15 @@ namespace halcuda
             return d;
         }
 
-        // Pass 4 (CpuAgentForceBackend2D.cpp:112-175) over cell-sorted slots.
+        // Pass 4 (CpuAgentForceBackend2D.cpp:112-175) for the agent in sorted
+        // slot `slot` (agent i); offsets are the cell offsets of its grid.
         template <typename T, typename TV>
-        __global__ void Forces(const int32_t *__restrict__ bucket, const int32_t *__restrict__ offsets,
-                               const V2<T> *__restrict__ sPos, const T *__restrict__ sRad, int32_t n,
-                               double interactionRad, T R, T k, int32_t xDim, int32_t yDim, int32_t wrapX,
-                               int32_t wrapY, TV *__restrict__ vel)
+        __device__ __forceinline__ void ForceSlot(const int32_t slot, const int32_t i,
+                                                  const int32_t *__restrict__ offsets,
+                                                  const V2<T> *__restrict__ sPos, const T *__restrict__ sRad,
+                                                  double interactionRad, T R, T k, int32_t xDim, int32_t yDim,
+                                                  int32_t wrapX, int32_t wrapY, TV *__restrict__ vel)
         {
-            int32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-            if (slot >= n)
-            {
-                return;
-            }
-            const int32_t i = bucket[slot];
             const V2<T> pf = sPos[slot];
             const T px = pf.x;
             const T py = pf.y;
@@ -359,6 +356,63 @@ namespace halcuda
             }
             vel[2 * static_cast<int64_t>(i)] = static_cast<TV>(vx);
             vel[2 * static_cast<int64_t>(i) + 1] = static_cast<TV>(vy);
+        }
+
+        // Pass 4 over cell-sorted slots: one thread per slot.
+        template <typename T, typename TV>
+        __global__ void Forces(const int32_t *__restrict__ bucket, const int32_t *__restrict__ offsets,
+                               const V2<T> *__restrict__ sPos, const T *__restrict__ sRad, int32_t n,
+                               double interactionRad, T R, T k, int32_t xDim, int32_t yDim, int32_t wrapX,
+                               int32_t wrapY, TV *__restrict__ vel)
+        {
+            const int32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+            if (slot >= n)
+            {
+                return;
+            }
+            ForceSlot<T, TV>(slot, bucket[slot], offsets, sPos, sRad, interactionRad, R, k, xDim, yDim, wrapX, wrapY,
+                             vel);
+        }
+
+        // ---- many independent wells in one pass ------------------------------
+        // Agents of all wells are concatenated, and so are the cells of the
+        // wells that have agents (well w's cells start at cellBase); the
+        // count, scan, scatter and stable-rank passes then run unchanged over
+        // the concatenation, and each agent's window walks its own well.
+
+        __global__ void BinCountWells(const float *__restrict__ pos, const int32_t *__restrict__ wellOf,
+                                      const AgentWellDev *__restrict__ wells, int32_t n, float2 *__restrict__ posF,
+                                      int32_t *__restrict__ cellOf, int32_t *__restrict__ arrival,
+                                      int32_t *__restrict__ counts)
+        {
+            const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+            if (i >= n)
+            {
+                return;
+            }
+            const AgentWellDev wd = wells[wellOf[i]];
+            const float px = pos[2 * static_cast<int64_t>(i)];
+            const float py = pos[2 * static_cast<int64_t>(i) + 1];
+            posF[i] = make_float2(px, py);
+            const int32_t c = static_cast<int32_t>(wd.cellBase) + CellCoord(px, wd.xDim) * wd.yDim + CellCoord(py, wd.yDim);
+            cellOf[i] = c;
+            arrival[i] = atomicAdd(counts + c, 1);
+        }
+
+        __global__ void ForcesWells(const int32_t *__restrict__ bucket, const int32_t *__restrict__ offsets,
+                                    const float2 *__restrict__ sPos, const float *__restrict__ sRad,
+                                    const int32_t *__restrict__ wellOf, const AgentWellDev *__restrict__ wells,
+                                    int32_t n, double interactionRad, float R, float k, float *__restrict__ vel)
+        {
+            const int32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+            if (slot >= n)
+            {
+                return;
+            }
+            const int32_t i = bucket[slot];
+            const AgentWellDev wd = wells[wellOf[i]];
+            ForceSlot<float, float>(slot, i, offsets + wd.cellBase, sPos, sRad, interactionRad, R, k, wd.xDim,
+                                    wd.yDim, wd.wrapX, wd.wrapY, vel);
         }
     }
 
@@ -885,4 +939,37 @@ extern "C" int hal_cuda_agents_forces_noalloc(const float *positions, const floa
         static_cast<float>(springConstant), xDim, yDim, wrapX != 0, wrapY != 0, velocityDeltas);
     CountLaunch(7);
     return LaunchStatus("hal_cuda_agents_forces_noalloc");
+}
+
+namespace halcuda
+{
+    int32_t AgentScanTiles(int64_t cells)
+    {
+        return static_cast<int32_t>((cells + kScanTile - 1) / kScanTile);
+    }
+
+    int LaunchAgentWells(const AgentWellsArgs &a, cudaStream_t s)
+    {
+        if (a.n <= 0)
+        {
+            return HAL_CUDA_OK;
+        }
+        HAL_TRY(CudaStatus(cudaMemsetAsync(a.counts, 0, static_cast<size_t>(a.cells) * sizeof(int32_t), s),
+                           "cudaMemsetAsync(well counts)"));
+        const int T = 256;
+        const unsigned ablocks = static_cast<unsigned>((a.n + T - 1) / T);
+        const int32_t nTiles = AgentScanTiles(a.cells);
+        BinCountWells<<<ablocks, T, 0, s>>>(a.pos, a.wellOf, a.wells, a.n, a.posF, a.cellOf, a.arrival, a.counts);
+        ScanReduce<<<nTiles, kScanThreads, 0, s>>>(a.counts, a.cells, a.tileSums);
+        ScanTiles<<<1, kScanThreads, 0, s>>>(a.tileSums, nTiles);
+        ScanApply<<<nTiles, kScanThreads, 0, s>>>(a.counts, a.cells, a.tileSums, a.offsets, a.n);
+        Scatter<<<ablocks, T, 0, s>>>(a.cellOf, a.arrival, a.offsets, a.n, a.bucketTmp);
+        Stabilize<float, float><<<ablocks, T, 0, s>>>(a.cellOf, a.offsets, a.bucketTmp, a.posF, a.rad, a.n, a.bucket,
+                                                      a.sPos, a.sRad);
+        const int TF = 128;
+        ForcesWells<<<static_cast<unsigned>((a.n + TF - 1) / TF), TF, 0, s>>>(
+            a.bucket, a.offsets, a.sPos, a.sRad, a.wellOf, a.wells, a.n, a.interactionRad, a.R, a.k, a.vel);
+        CountLaunch(7);
+        return LaunchStatus("agent wells");
+    }
 }

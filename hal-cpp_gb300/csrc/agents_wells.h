@@ -1,0 +1,43 @@
+// agents_wells.h -- the agent force pass over many independent wells at once
+// (agents.cu), used by the batched wells handle (wells.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace halcuda
+{
+    // One well's grid inside the concatenated cell array.
+    struct AgentWellDev
+    {
+        int64_t cellBase;       // first cell of the well in the concatenation
+        int32_t xDim, yDim;
+        int32_t wrapX, wrapY;
+    };
+
+    // Device arrays of one pass (n agents, `cells` concatenated cells).
+    struct AgentWellsArgs
+    {
+        const float *pos;          // 2n, (x, y) interleaved, well-local coordinates
+        const float *rad;          // n
+        const int32_t *wellOf;     // n
+        const AgentWellDev *wells;
+        int32_t n;
+        int64_t cells;
+        float2 *posF, *sPos;       // n each
+        float *sRad;               // n
+        int32_t *cellOf, *arrival, *bucketTmp, *bucket;  // n each
+        int32_t *counts;           // cells
+        int32_t *offsets;          // cells + 1
+        int32_t *tileSums;         // AgentScanTiles(cells)
+        double interactionRad;
+        float R, k;
+        float *vel;                // 2n, overwritten
+    };
+
+    int32_t AgentScanTiles(int64_t cells);
+
+    // Count, scan, scatter, stable rank and forces of every well's agents.
+    int LaunchAgentWells(const AgentWellsArgs &a, cudaStream_t s);
+}

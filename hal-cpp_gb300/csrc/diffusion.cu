@@ -10,6 +10,7 @@
 // The fused tick adds PDEGrid2D's MulAll(-decay), Add(source) and Update()
 // (PDEGrid2D.h:103-186) in the same pass: f'[i] = c + (sum*r - c*decay + src).
 #include "common.cuh"
+#include "tick_params.h"
 
 #include <algorithm>
 #include <cstring>
@@ -19,8 +20,6 @@ namespace halcuda
 {
     namespace
     {
-        constexpr int kTickRowsPerThread = 4;  // rows owned by one thread
-        constexpr int kTickWarps = 8;          // warps per CTA, stacked in x
 
         // Off-grid neighbour handling of one row (or column) of the stencil.
         enum NbrMode : int
@@ -35,20 +34,6 @@ namespace halcuda
             return (mode == kNbrGrid) ? 1.0f : ((mode == kNbrGhost) ? 2.0f : 0.0f);
         }
 
-        struct TickParams
-        {
-            const float *f;
-            float *out;
-            int32_t xDim, yDim;
-            float r, negDecay;
-            int32_t wrapX, wrapY;
-            const float *src;          // dense source or null
-            GhostView ghost;           // all null for zero-flux
-            const int32_t *ptStart;    // point sources grouped by CTA (CSR), or null
-            const int32_t *ptRow;
-            const int32_t *ptCol;
-            const float *ptVal;
-        };
 
         // Loads VEC consecutive values of row x starting at column y0 (the
         // part inside the grid) and classifies the row as grid/ghost/none.
@@ -109,15 +94,16 @@ namespace halcuda
         // of the thread -- the rows above, inside and below its strip, the
         // y neighbours of each row and the source -- is issued before the
         // first result is computed.
+        // CTA (bx, by) of the tick of grid p: columns from bx * 32 * VEC, rows
+        // from by * kTickWarps * kTickRowsPerThread.
         template <int VEC>
-        __global__ void __launch_bounds__(32 * kTickWarps)
-            TickKernel(TickParams p)
+        __device__ __forceinline__ void TickTile(const TickParams &p, const int32_t bx, const int32_t by)
         {
             constexpr int T = kTickRowsPerThread;
             const int lane = threadIdx.x;
             const int warp = threadIdx.y;
-            const int32_t y0 = (blockIdx.x * 32 + lane) * VEC;
-            const int32_t xs = (blockIdx.y * kTickWarps + warp) * T;
+            const int32_t y0 = (bx * 32 + lane) * VEC;
+            const int32_t xs = (by * kTickWarps + warp) * T;
             if (y0 >= p.yDim || xs >= p.xDim)
             {
                 return;
@@ -221,7 +207,8 @@ namespace halcuda
             int32_t ptBeg = 0, ptEnd = 0;
             if (p.ptStart != nullptr)
             {
-                int32_t b = blockIdx.y * gridDim.x + blockIdx.x;
+                const int32_t gridX = (p.yDim + 32 * VEC - 1) / (32 * VEC);
+                int32_t b = by * gridX + bx;
                 ptBeg = __ldg(p.ptStart + b);
                 ptEnd = __ldg(p.ptStart + b + 1);
             }
@@ -299,6 +286,22 @@ namespace halcuda
             }
         }
 
+        template <int VEC>
+        __global__ void __launch_bounds__(32 * kTickWarps)
+            TickKernel(TickParams p)
+        {
+            TickTile<VEC>(p, static_cast<int32_t>(blockIdx.x), static_cast<int32_t>(blockIdx.y));
+        }
+
+        // Batched form: CTA b runs tile tiles[b] = (grid, CTA column, CTA row).
+        template <int VEC>
+        __global__ void __launch_bounds__(32 * kTickWarps)
+            TickTiles(const TickParams *__restrict__ table, const int4 *__restrict__ tiles)
+        {
+            const int4 t = tiles[blockIdx.x];
+            TickTile<VEC>(table[t.x], t.y, t.z);
+        }
+
         // FP64 IDiffusionBackend2D::Diffuse: deltas[i] += sum * r, with the
         // reference's operation order and no contraction, so the result is
         // bit-identical to Hal::CpuDiffusionBackend2D.
@@ -346,6 +349,25 @@ namespace halcuda
             s = __dadd_rn(s, DeltaTerm64(f, c, y - 1, yDim, wrapY, rowBase, 1, gy, x));
             deltas[i] = __dadd_rn(deltas[i], __dmul_rn(s, r));
         }
+    }
+
+    int LaunchTickTiles(const TickParams *table, const int4 *tiles, int32_t nTiles, int vec, cudaStream_t s)
+    {
+        if (nTiles <= 0)
+        {
+            return HAL_CUDA_OK;
+        }
+        const dim3 block(32, kTickWarps);
+        if (vec == 4)
+        {
+            TickTiles<4><<<static_cast<unsigned>(nTiles), block, 0, s>>>(table, tiles);
+        }
+        else
+        {
+            TickTiles<1><<<static_cast<unsigned>(nTiles), block, 0, s>>>(table, tiles);
+        }
+        CountLaunch();
+        return LaunchStatus("TickTiles");
     }
 
     struct Diffusion

@@ -1,0 +1,35 @@
+// tick_params.h -- parameters of one fused explicit tick (the TickKernel's
+// input), shared by the single-grid handle (diffusion.cu) and the batched
+// wells handle (wells.cu).
+#pragma once
+
+#include "common.cuh"
+
+#include <cstdint>
+
+namespace halcuda
+{
+    struct TickParams
+    {
+        const float *f;
+        float *out;
+        int32_t xDim, yDim;
+        float r, negDecay;
+        int32_t wrapX, wrapY;
+        const float *src;          // dense source or null
+        GhostView ghost;           // all null for zero-flux
+        const int32_t *ptStart;    // point sources grouped by CTA (CSR), or null
+        const int32_t *ptRow;
+        const int32_t *ptCol;
+        const float *ptVal;
+    };
+
+    // Geometry of the tick's CTAs: 32 lanes x kTickWarps warps; a lane owns
+    // VEC consecutive cells of kTickRowsPerThread consecutive rows.
+    constexpr int kTickRowsPerThread = 4;
+    constexpr int kTickWarps = 8;
+
+    // Batched ticks: tile b = (grid index, CTA column, CTA row) of the
+    // table's grids.  vec is 4 (every grid's yDim % 4 == 0) or 1.
+    int LaunchTickTiles(const TickParams *table, const int4 *tiles, int32_t nTiles, int vec, cudaStream_t s);
+}

@@ -74,6 +74,18 @@ SIGNATURES = {
     "hal_cuda_agents_sync": (_I, [_vp]),
     "hal_cuda_agents_stream": (_vp, [_vp]),
     "hal_cuda_agents_set_stream": (_I, [_vp, _vp]),
+    "hal_cuda_wells_create": (_I, [_vp, _i32, _vp]),
+    "hal_cuda_wells_destroy": (_I, [_vp]),
+    "hal_cuda_wells_set_field": (_I, [_vp, _i32, _vp, _i64]),
+    "hal_cuda_wells_get_field": (_I, [_vp, _i32, _vp, _i64]),
+    "hal_cuda_wells_set_source": (_I, [_vp, _i32, _vp, _i64]),
+    "hal_cuda_wells_set_agents": (_I, [_vp, _vp, _vp, _vp]),
+    "hal_cuda_wells_run_ticks": (_I, [_vp, _i32, _f64, _f64]),
+    "hal_cuda_wells_get_forces": (_I, [_vp, _vp, _i64]),
+    "hal_cuda_wells_profile": (_I, [_vp, _i32, _f64, _f64, _vp]),
+    "hal_cuda_wells_sync": (_I, [_vp]),
+    "hal_cuda_wells_stream": (_vp, [_vp]),
+    "hal_cuda_wells_set_stream": (_I, [_vp, _vp]),
     "hal_cuda_agents_forces_noalloc": (_I, [_vp, _vp, _i32, _vp, _f64, _f64, _i32, _i32, _i32, _i32,
                                             _vp]),
 }
@@ -385,6 +397,88 @@ class Agents(_Handle):
         bucket = np.empty(max(self.n, 1), dtype=np.int32)
         _check(lib().hal_cuda_agents_get_bins(self._h, _p(off), _p(bucket)), "get_bins")
         return off, bucket[: self.n]
+
+
+WELL_EXPLICIT, WELL_ADI = 0, 1
+WELLS_MAX_SIDE = 4096
+
+
+class WellDesc(ctypes.Structure):
+    """hal_cuda_well_desc."""
+
+    _fields_ = [("xDim", ctypes.c_int32), ("yDim", ctypes.c_int32), ("kind", ctypes.c_int32),
+                ("wrapX", ctypes.c_int32), ("wrapY", ctypes.c_int32), ("maxAgents", ctypes.c_int32),
+                ("diffRate", ctypes.c_double), ("decay", ctypes.c_double)]
+
+
+class Wells(_Handle):
+    """hal_cuda_wells: many independent wells (MultiWellExperiment::Step) per
+    launch.  `wells` is a sequence of dicts with keys xDim, yDim, kind
+    ("explicit" or "adi"), diffRate, decay and optionally wrapX, wrapY,
+    maxAgents."""
+
+    _prefix = "wells"
+
+    def __init__(self, wells):
+        super().__init__()
+        arr = (WellDesc * len(wells))()
+        for i, w in enumerate(wells):
+            kind = w["kind"]
+            arr[i] = WellDesc(int(w["xDim"]), int(w["yDim"]),
+                              WELL_ADI if kind in ("adi", WELL_ADI) else WELL_EXPLICIT,
+                              int(bool(w.get("wrapX", False))), int(bool(w.get("wrapY", False))),
+                              int(w.get("maxAgents", 0)), float(w["diffRate"]), float(w.get("decay", 0.0)))
+        h = ctypes.c_void_p()
+        _check(lib().hal_cuda_wells_create(ctypes.cast(arr, ctypes.c_void_p), len(wells), ctypes.byref(h)),
+               "wells_create")
+        self._h = h
+        self.wells = [dict(w) for w in wells]
+        self.counts = np.zeros(len(wells), dtype=np.int32)
+
+    def _cells(self, well):
+        w = self.wells[well]
+        return int(w["xDim"]) * int(w["yDim"])
+
+    def set_field(self, well, field):
+        f = _f32(field)
+        _check(lib().hal_cuda_wells_set_field(self._h, well, _p(f), f.size), "wells_set_field")
+
+    def get_field(self, well):
+        out = np.empty(self._cells(well), dtype=np.float32)
+        _check(lib().hal_cuda_wells_get_field(self._h, well, _p(out), out.size), "wells_get_field")
+        return out
+
+    def set_source(self, well, dense):
+        if dense is None:
+            _check(lib().hal_cuda_wells_set_source(self._h, well, None, 0), "wells_set_source")
+            return
+        d = _f32(dense)
+        _check(lib().hal_cuda_wells_set_source(self._h, well, _p(d), d.size), "wells_set_source")
+
+    def set_agents(self, counts, positions, radii):
+        c = np.ascontiguousarray(counts, dtype=np.int32)
+        p = _f32(positions)
+        r = _f32(radii)
+        _check(lib().hal_cuda_wells_set_agents(self._h, _p(c), _p(p) if p.size else None,
+                                               _p(r) if r.size else None), "wells_set_agents")
+        self.counts = c.copy()
+
+    def run_ticks(self, ticks, interactionRad=1.0, springConstant=0.1):
+        _check(lib().hal_cuda_wells_run_ticks(self._h, ticks, interactionRad, springConstant),
+               "wells_run_ticks")
+
+    def get_forces(self):
+        out = np.empty(2 * int(self.counts.sum()), dtype=np.float32)
+        _check(lib().hal_cuda_wells_get_forces(self._h, _p(out) if out.size else None, out.size),
+               "wells_get_forces")
+        return out
+
+    def profile(self, iters, interactionRad=1.0, springConstant=0.1):
+        """Average ms per tick: explicit tiles, ADI x, ADI y, agents, whole."""
+        ms = np.zeros(5, dtype=np.float32)
+        _check(lib().hal_cuda_wells_profile(self._h, iters, interactionRad, springConstant, _p(ms)),
+               "wells_profile")
+        return [float(v) for v in ms]
 
 
 NOALLOC_MAX_AGENTS = 65536

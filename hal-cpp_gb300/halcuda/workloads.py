@@ -11,6 +11,11 @@ value distributions are the workloads' own:
 * agents     -- 70% uniform and 30% in a Gaussian cluster (sigma 100 cells)
                 at a seeded centre, clamped into the domain; float32
                 positions; radius 0.5; cutoff 1.0; stiffness 0.1; walls
+* wells      -- 512 independent square wells, side round(64 * 16^U) (log-
+                uniform in [64, 1024]); half explicit with rate U[0.05, 0.24],
+                half ADI with rate U[1, 10]; decay U[0, 0.02]; field U[0,1);
+                0..20000 uniform agents each (radius 0.5, cutoff 1.0,
+                stiffness 0.1, walls)
 """
 from __future__ import annotations
 
@@ -60,3 +65,30 @@ def agent_inputs(n_agents: int = 1_000_000, dim: int = 2048, seed: int = 3):
     radii = np.full(n_agents, 0.5, dtype=np.float32)
     return dict(positions=pos.ravel(), radii=radii, interactionRad=1.0, springConstant=0.1,
                 xDim=dim, yDim=dim, uptake=0.001)
+
+
+def wells_inputs(n_wells: int = 512, seed: int = 4, max_agents: int = 20000, min_side: int = 64,
+                 max_side: int = 1024):
+    """Well descriptors (hal.Wells dicts) plus per-well fields and agents."""
+    rng = np.random.default_rng(seed)
+    ratio = max_side / min_side
+    sides = np.rint(min_side * ratio ** rng.random(n_wells)).astype(np.int32)
+    kinds = rng.random(n_wells) < 0.5
+    wells, fields, counts, pos, rad = [], [], [], [], []
+    for i in range(n_wells):
+        n = int(sides[i])
+        adi = bool(kinds[i])
+        rate = float(rng.uniform(1.0, 10.0) if adi else rng.uniform(0.05, 0.24))
+        decay = float(rng.uniform(0.0, 0.02))
+        na = int(rng.integers(0, max_agents + 1))
+        wells.append(dict(xDim=n, yDim=n, kind="adi" if adi else "explicit", diffRate=rate, decay=decay,
+                          maxAgents=na))
+        fields.append(rng.random(n * n).astype(np.float32))
+        counts.append(na)
+        hi = np.nextafter(np.float32(n), np.float32(0))
+        pos.append(np.minimum(rng.random(2 * na) * n, hi).astype(np.float32))
+        rad.append(np.full(na, 0.5, dtype=np.float32))
+    return dict(wells=wells, fields=fields, counts=np.array(counts, dtype=np.int32),
+                positions=np.concatenate(pos) if pos else np.zeros(0, np.float32),
+                radii=np.concatenate(rad) if rad else np.zeros(0, np.float32),
+                interactionRad=1.0, springConstant=0.1)

@@ -254,6 +254,70 @@ int hal_cuda_agents_sync(hal_cuda_agents *h);
 void *hal_cuda_agents_stream(hal_cuda_agents *h);
 int hal_cuda_agents_set_stream(hal_cuda_agents *h, void *stream);
 
+/* ---- batched wells: many independent simulations per launch -------------
+ * MultiWellExperiment::Step / StepMultiThread
+ * (include/Hal/Tools/MultiWellExperiment.h:83-103) advance independent wells
+ * one after another, or on host threads through Hal::MultiThread
+ * (include/Hal/Concurrency/MultiThread.h:19-91).  Here every well's tick runs
+ * in the same few launches:
+ *   - one launch over the tiles of every explicit well (the fused tick of
+ *     hal_cuda_diffusion_run_ticks);
+ *   - two launches (x- and y-sweep) over the line groups of every ADI well
+ *     (the tick of hal_cuda_adi_run_ticks);
+ *   - one agent force pass over the concatenated agents and cells of every
+ *     well that has agents (hal_cuda_agents_dispatch's kernels).
+ * A tick is replayed from a CUDA graph.  Each well's field, and its agents'
+ * velocity deltas, are bit-identical to running that well alone on the
+ * single-grid handles. */
+#define HAL_CUDA_WELL_EXPLICIT 0
+#define HAL_CUDA_WELL_ADI 1
+#define HAL_CUDA_WELLS_MAX_SIDE 4096
+
+typedef struct hal_cuda_well_desc
+{
+    int32_t xDim, yDim;  /* grid of the well, each in [1, HAL_CUDA_WELLS_MAX_SIDE] */
+    int32_t kind;        /* HAL_CUDA_WELL_EXPLICIT or HAL_CUDA_WELL_ADI */
+    int32_t wrapX, wrapY;
+    int32_t maxAgents;   /* capacity of the well's agent set, 0 for none */
+    double diffRate;     /* D*dt/dx^2; at most 0.25 for an explicit well */
+    double decay;        /* per-tick decay: f' = ... - decay*f */
+} hal_cuda_well_desc;
+
+typedef struct hal_cuda_wells hal_cuda_wells;
+
+int hal_cuda_wells_create(const hal_cuda_well_desc *wells, int32_t nWells, hal_cuda_wells **out);
+int hal_cuda_wells_destroy(hal_cuda_wells *h);
+
+/* Field (HAL layout x*yDim + y, len = xDim*yDim floats) and constant dense
+ * source (NULL clears it) of one well. */
+int hal_cuda_wells_set_field(hal_cuda_wells *h, int32_t well, const float *field, int64_t len);
+int hal_cuda_wells_get_field(hal_cuda_wells *h, int32_t well, float *field, int64_t len);
+int hal_cuda_wells_set_source(hal_cuda_wells *h, int32_t well, const float *dense, int64_t len);
+
+/* Agents of every well at once: counts[w] <= maxAgents of well w; positions
+ * (x, y interleaved, the well's own coordinates) and radii concatenated in
+ * well order (2*sum and sum floats). */
+int hal_cuda_wells_set_agents(hal_cuda_wells *h, const int32_t *counts, const float *positions,
+                              const float *radii);
+
+/* `ticks` ticks of every well: its field tick, then its agents' force pass
+ * (interactionRad, springConstant).  Asynchronous on the handle's stream. */
+int hal_cuda_wells_run_ticks(hal_cuda_wells *h, int32_t ticks, double interactionRad,
+                             double springConstant);
+
+/* Velocity deltas of the last force pass, every well's agents concatenated
+ * in well order (len = 2*sum(counts) floats). */
+int hal_cuda_wells_get_forces(hal_cuda_wells *h, float *velocityDeltas, int64_t len);
+
+/* Profiling: average device ms over `iters` ticks launched one kernel at a
+ * time: ms[0] explicit tiles, ms[1] ADI x-sweep tiles, ms[2] ADI y-sweep
+ * tiles, ms[3] agent pass, ms[4] whole tick.  Fields advance. */
+int hal_cuda_wells_profile(hal_cuda_wells *h, int32_t iters, double interactionRad,
+                           double springConstant, float *ms);
+int hal_cuda_wells_sync(hal_cuda_wells *h);
+void *hal_cuda_wells_stream(hal_cuda_wells *h);
+int hal_cuda_wells_set_stream(hal_cuda_wells *h, void *stream);
+
 /* ---- agent forces without allocation --------------------------------------
  * No counterpart in the reference: the reference's backends allocate their
  * buffers.  This entry point is for callers that cannot call cudaMalloc -- a

@@ -1,0 +1,161 @@
+"""Batched wells (MultiWellExperiment::Step over many wells per launch).
+
+Every well of a batch must equal the same well run alone on the single-grid
+handles bit for bit (same kernels, same arithmetic), and through them the
+CPU oracle within the usual tolerances:
+* explicit and ADI fields: bit-identical to hal.Diffusion / hal.Adi
+  run_ticks; against the FP64 oracle ticks max-rel <= 1e-5 (explicit) and
+  <= 2e-6 (1 + r) per tick (ADI);
+* agent forces: bit-identical to hal.Agents dispatch; bins per well follow
+  the CPU's order, so the FP32 forces equal the single-grid ones exactly.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import max_rel
+
+pytestmark = pytest.mark.gpu
+
+R, K = 1.0, 0.1
+
+
+def _mixed_wells(rng):
+    """Sizes that exercise every tile path: float4 and scalar rows, ragged
+    line groups, 1-wide grids, periodic and zero-flux, with and without
+    agents and sources."""
+    specs = [
+        (64, 64, "explicit", 0.2, 0.001, False, False, 500),
+        (37, 50, "explicit", 0.24, 0.0, True, False, 0),
+        (130, 33, "explicit", 0.05, 0.02, False, True, 300),
+        (1, 40, "explicit", 0.1, 0.0, False, False, 0),
+        (96, 80, "adi", 5.0, 0.01, False, False, 800),
+        (257, 31, "adi", 1.5, 0.0, True, True, 0),
+        (33, 200, "adi", 10.0, 0.005, False, True, 200),
+        (48, 1, "adi", 2.0, 0.0, False, False, 0),
+        (256, 256, "adi", 3.0, 0.02, False, False, 2000),
+        (200, 128, "explicit", 0.15, 0.01, False, False, 1500),
+    ]
+    wells, fields, srcs, pos, rad, counts = [], [], [], [], [], []
+    for i, (xd, yd, kind, rate, decay, wx, wy, na) in enumerate(specs):
+        wells.append(dict(xDim=xd, yDim=yd, kind=kind, diffRate=rate, decay=decay, wrapX=wx, wrapY=wy,
+                          maxAgents=na + 7))
+        fields.append(rng.random(xd * yd).astype(np.float32))
+        srcs.append((rng.random(xd * yd) * 0.01).astype(np.float32) if i % 2 == 0 else None)
+        counts.append(na)
+        p = rng.random((na, 2)) * (xd, yd)
+        hi = np.array([np.nextafter(np.float32(xd), np.float32(0)), np.nextafter(np.float32(yd), np.float32(0))])
+        pos.append(np.minimum(p, hi).astype(np.float32).ravel())
+        rad.append((0.3 + 0.4 * rng.random(na)).astype(np.float32))
+    return wells, fields, srcs, np.array(counts, np.int32), pos, rad
+
+
+def _alone(hal, w, field, src, ticks):
+    with (hal.Adi(w["xDim"], w["yDim"]) if w["kind"] == "adi" else hal.Diffusion(w["xDim"], w["yDim"])) as h:
+        h.set_field(field)
+        if src is not None:
+            h.set_source(src)
+        h.run_ticks(ticks, w["diffRate"], w["decay"], w["wrapX"], w["wrapY"])
+        return h.get_field()
+
+
+def _alone_forces(hal, w, pos, rad):
+    with hal.Agents(w["xDim"], w["yDim"], max(len(rad), 1)) as ag:
+        ag.upload(pos, rad)
+        ag.dispatch(R, K, w["wrapX"], w["wrapY"])
+        return ag.download()
+
+
+def test_wells_equal_single_grid_handles(hal, oracle):
+    rng = np.random.default_rng(40)
+    wells, fields, srcs, counts, pos, rad = _mixed_wells(rng)
+    ticks = 7
+    with hal.Wells(wells) as b:
+        for i, f in enumerate(fields):
+            b.set_field(i, f)
+            if srcs[i] is not None:
+                b.set_source(i, srcs[i])
+        b.set_agents(counts, np.concatenate(pos), np.concatenate(rad))
+        b.run_ticks(3, R, K)
+        b.run_ticks(ticks - 3, R, K)  # graphs of both parities
+        got = [b.get_field(i) for i in range(len(wells))]
+        forces = b.get_forces()
+    at = 0
+    for i, w in enumerate(wells):
+        exp = _alone(hal, w, fields[i], srcs[i], ticks)
+        assert np.array_equal(got[i], exp), (i, w)
+        # the oracle, FP64 from the same float32 start
+        mode = 1 if w["kind"] == "adi" else 0
+        ref = oracle.run_ticks(mode, fields[i].astype(np.float64), w["xDim"], w["yDim"], w["diffRate"],
+                               decay=w["decay"], src_dense=None if srcs[i] is None else srcs[i].astype(np.float64),
+                               ticks=ticks, wrapX=w["wrapX"], wrapY=w["wrapY"])
+        # FP32 against FP64: 1e-5 per explicit run; an ADI step's FP32 solve
+        # error is up to 2e-6 (1 + r) of the field and accumulates per tick
+        tol = 2e-6 * (1 + w["diffRate"]) * ticks if mode == 1 else 1e-5
+        assert max_rel(got[i], ref) <= tol, (i, w)
+        n = int(counts[i])
+        v = forces[2 * at: 2 * (at + n)]
+        at += n
+        if n:
+            assert np.array_equal(v, _alone_forces(hal, w, pos[i], rad[i])), (i, w)
+
+
+def test_wells_profile_and_source_clear(hal):
+    rng = np.random.default_rng(41)
+    wells, fields, srcs, counts, pos, rad = _mixed_wells(rng)
+    with hal.Wells(wells) as b:
+        for i, f in enumerate(fields):
+            b.set_field(i, f)
+            b.set_source(i, (rng.random(f.size) * 0.01).astype(np.float32))
+            b.set_source(i, None)  # cleared again: plain decay and diffusion
+        b.set_agents(counts, np.concatenate(pos), np.concatenate(rad))
+        ms = b.profile(3, R, K)
+        assert len(ms) == 5 and ms[4] > 0.0
+        got = [b.get_field(i) for i in range(len(wells))]
+    for i, w in enumerate(wells):
+        assert np.array_equal(got[i], _alone(hal, w, fields[i], None, 3)), (i, w)
+
+
+def test_wells_reject_bad_input(hal):
+    with pytest.raises(ValueError):
+        hal.Wells([dict(xDim=8, yDim=8, kind="explicit", diffRate=0.3, decay=0.0)])
+    with pytest.raises(ValueError):
+        hal.Wells([dict(xDim=hal.WELLS_MAX_SIDE + 1, yDim=8, kind="adi", diffRate=1.0, decay=0.0)])
+    with pytest.raises(ValueError):
+        hal.Wells([])
+    with hal.Wells([dict(xDim=8, yDim=8, kind="adi", diffRate=1.0, decay=0.0, maxAgents=2)]) as b:
+        with pytest.raises(ValueError):
+            b.set_field(0, np.zeros(63, np.float32))
+        with pytest.raises(ValueError):
+            b.set_field(1, np.zeros(64, np.float32))
+        with pytest.raises(ValueError):
+            b.set_agents([3], np.zeros(6, np.float32), np.zeros(3, np.float32))
+        with pytest.raises(ValueError):
+            b.run_ticks(1, -1.0, 0.1)
+
+
+def test_wells_batched_workload_sample(hal):
+    """512 wells of the batched workload (109M cells, 5.2M agents): two
+    ticks, and a sample of wells against the single-grid handles."""
+    from halcuda import workloads
+
+    w = workloads.wells_inputs()
+    rng = np.random.default_rng(5)
+    sample = sorted(rng.choice(len(w["wells"]), 8, replace=False).tolist())
+    with hal.Wells(w["wells"]) as b:
+        for i, f in enumerate(w["fields"]):
+            b.set_field(i, f)
+        b.set_agents(w["counts"], w["positions"], w["radii"])
+        b.run_ticks(2, R, K)
+        got = {i: b.get_field(i) for i in sample}
+        forces = b.get_forces()
+    starts = np.concatenate([[0], np.cumsum(w["counts"])])
+    for i in sample:
+        wd = w["wells"][i]
+        wd = dict(wd, wrapX=False, wrapY=False)
+        assert np.array_equal(got[i], _alone(hal, wd, w["fields"][i], None, 2)), i
+        a, e = int(starts[i]), int(starts[i + 1])
+        if e > a:
+            exp = _alone_forces(hal, wd, w["positions"][2 * a: 2 * e], w["radii"][a:e])
+            assert np.array_equal(forces[2 * a: 2 * e], exp), i
