@@ -271,6 +271,89 @@ def secondary_agents(hal, stream, iters=20):
                          "traffic": None}}
 
 
+def secondary_wells(hal, torch, stream, ticks=20, plain_ticks=3):
+    """512 independent wells (109M cells, 5.2M agents): one batched tick of
+    every well against per-well launches of the single-grid handles."""
+    from halcuda import workloads
+
+    w = workloads.wells_inputs()
+    R, k = w["interactionRad"], w["springConstant"]
+    wells = w["wells"]
+    cells_exp = sum(d["xDim"] * d["yDim"] for d in wells if d["kind"] == "explicit")
+    cells_adi = sum(d["xDim"] * d["yDim"] for d in wells if d["kind"] == "adi")
+    cells_ag = sum(d["xDim"] * d["yDim"] for d in wells if d["maxAgents"] > 0)
+    n_ag = int(w["counts"].sum())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    with hal.Wells(wells) as b:
+        b.set_stream(stream.cuda_stream)
+        for i, f in enumerate(w["fields"]):
+            b.set_field(i, f)
+        b.set_agents(w["counts"], w["positions"], w["radii"])
+        b.run_ticks(4, R, k)  # warm-up; captures both parities' graphs
+        b.sync()
+        ev0.record(stream)
+        b.run_ticks(ticks, R, k)
+        ev1.record(stream)
+        ev1.synchronize()
+        ms_batched = ev0.elapsed_time(ev1) / ticks
+        stages = b.profile(3, R, k)
+
+    # the same wells, one single-grid handle per well, launched one by one
+    starts = np.concatenate([[0], np.cumsum(w["counts"])]).astype(np.int64)
+    handles = []
+    try:
+        for i, d in enumerate(wells):
+            h = (hal.Adi if d["kind"] == "adi" else hal.Diffusion)(d["xDim"], d["yDim"])
+            h.set_stream(stream.cuda_stream)
+            h.set_field(w["fields"][i])
+            ag = None
+            a, e = int(starts[i]), int(starts[i + 1])
+            if e > a:
+                ag = hal.Agents(d["xDim"], d["yDim"], e - a)
+                ag.set_stream(stream.cuda_stream)
+                ag.upload(w["positions"][2 * a: 2 * e], w["radii"][a:e])
+            handles.append((h, ag, d))
+
+        def plain_tick():
+            for h, ag, d in handles:
+                h.run_ticks(1, d["diffRate"], d["decay"])
+                if ag is not None:
+                    ag.dispatch(R, k)
+
+        plain_tick()
+        plain_tick()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(plain_ticks):
+            plain_tick()
+        ev1.record(stream)
+        ev1.synchronize()
+        ms_plain = ev0.elapsed_time(ev1) / plain_ticks
+    finally:
+        for h, ag, _ in handles:
+            h.close()
+            if ag is not None:
+                ag.close()
+
+    # algorithmic bytes of one tick: explicit 8 B/cell, ADI 20 B/cell (x-sweep
+    # 8, y-sweep 12 without a source), agents 28 B/agent + 16 B/bin
+    bytes_tick = 8 * cells_exp + 20 * cells_adi + 28 * n_ag + 16 * cells_ag
+    peak, _ = peaks()
+    ach = bytes_tick / (ms_batched * 1e-3) / 1e9
+    cells = cells_exp + cells_adi
+    return {"workload": "wells-512-side64..1024-explicit+adi-agents0..20000",
+            "value": cells / (ms_batched * 1e-3), "unit": "cell-updates/s",
+            "agents_per_s": n_ag / (ms_batched * 1e-3),
+            "ms_per_tick_batched": ms_batched, "ms_per_tick_per_well_launches": ms_plain,
+            "speedup_vs_per_well_launches": ms_plain / ms_batched,
+            "ms_by_stage": {"explicit": stages[0], "adi_x": stages[1], "adi_y": stages[2],
+                            "agents": stages[3], "tick": stages[4]},
+            "cells": cells, "agents": n_ag,
+            "roofline": {"kernel": "whole batched tick", "bound": "hbm", "achieved": ach, "peak": peak,
+                         "unit": "GB/s", "frac": ach / peak, "traffic": None}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -387,7 +470,8 @@ def main():
     secondary = None
     if not args.no_secondary and rank == 0:
         secondary = {"explicit": secondary_explicit(hal, torch, stream),
-                     "agents": secondary_agents(hal, stream)}
+                     "agents": secondary_agents(hal, stream),
+                     "wells": secondary_wells(hal, torch, stream)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
