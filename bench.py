@@ -354,6 +354,49 @@ def secondary_wells(hal, torch, stream, ticks=20, plain_ticks=3):
                          "unit": "GB/s", "frac": ach / peak, "traffic": None}}
 
 
+def secondary_adjoint(hal, directions=None):
+    """Parameter recovery on 512^2: the gradient of the field misfit after 500
+    variable-rate ADI steps (checkpoints every 22) with respect to D(x), decay
+    and source; its device time against one forward pass, and central finite
+    differences (h = 1e-3) of the device loss on random directions."""
+    from halcuda import workloads
+
+    w = workloads.adjoint_inputs()
+    n, steps = w["xDim"], w["steps"]
+    dirs = w["fd_directions"] if directions is None else directions
+    h = w["fd_h"]
+    rng = np.random.default_rng(6)
+    with hal.Adjoint(n, n) as a:
+        a.set_problem(w["f0"], np.zeros_like(w["f0"]), steps, w["checkpoint_every"])
+        _, target = a.forward(w["D_true"], w["decay"], w["src"], want_field=True)
+        a.set_problem(w["f0"], target, steps, w["checkpoint_every"])
+        fwd, grad = [], []
+        for _ in range(3):
+            a.forward(w["D"], w["decay"], w["src"])
+            loss, gD, gK, gS = a.gradient(w["D"], w["decay"], w["src"])
+            t = a.times()
+            fwd.append(t[0])
+            grad.append(t[1])
+        ms_fwd, ms_grad = min(fwd), min(grad)
+        g64 = gD.astype(np.float64)
+        errs, ok = [], 0
+        for _ in range(dirs):
+            v = rng.standard_normal(n * n).astype(np.float32)
+            f = lambda t: a.forward(w["D"] + np.float32(t) * v, w["decay"], w["src"])
+            f1 = (f(h) - f(-h)) / (2 * h)
+            f2 = (f(2 * h) - f(-2 * h)) / (4 * h)
+            dd = float(g64 @ v.astype(np.float64))
+            errs.append(abs(f1 - dd) / max(abs(dd), 1e-30))
+            ok += abs(f1 - dd) <= 2e-2 * abs(dd) + 3 * abs(f1 - f2)
+    return {"workload": "adjoint-512x512-500steps-ckpt22-D0.5..5-decay0.005",
+            "value": ms_grad / ms_fwd, "unit": "t(gradient)/t(forward)", "higher_is_better": False,
+            "ms_forward": ms_fwd, "ms_gradient": ms_grad, "loss": loss,
+            "fd": {"directions": dirs, "h": h, "median_rel_err": float(np.median(errs)),
+                   "max_rel_err": float(np.max(errs)),
+                   "within_2pct_plus_noise": int(ok)},
+            "note": "FP32 device loss; FD noise estimated from differences at h and 2h"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -471,7 +514,8 @@ def main():
     if not args.no_secondary and rank == 0:
         secondary = {"explicit": secondary_explicit(hal, torch, stream),
                      "agents": secondary_agents(hal, stream),
-                     "wells": secondary_wells(hal, torch, stream)}
+                     "wells": secondary_wells(hal, torch, stream),
+                     "adjoint": secondary_adjoint(hal)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -1,0 +1,838 @@
+// adjoint.cu -- variable-rate ADI (a rate D per cell) and the gradient of a
+// field loss by reverse-mode differentiation, with checkpoints.
+//
+// The reference has no variable-rate ADI and no gradient code.  The step is
+// defined from HAL's variable-rate explicit stencil Internal::Diffusion2(...,
+// pDiffRatesX, pDiffRatesY, ...) (src/Pde/PDEequations.cpp:199-230): the
+// face between cells j and j+1 of a line carries cell j's rate, a non-wrapped
+// edge has no face, and L is the face-weighted Laplacian along a line:
+//   w  = (I - Lx/2)^-1 (I + Ly/2) f            x-sweep  (FwdX)
+//   v  = (I - Ly/2)^-1 (I + Lx/2) w            y-sweep  (FwdY)
+//   f' = f + (((v - f) + f*(-decay)) + src)    PDEGrid2D tick order
+// For a constant rate this is Internal::Diffusion2DADI plus the tick.
+//
+// Every line has its own tridiagonal matrix, so the line solves are parallel
+// cyclic reduction in shared memory (one CTA per line, one row per thread);
+// a wrapped line of a power-of-two length needs no Sherman-Morrison step.
+//
+// Gradient of loss = 1/2 |f_T - target|^2.  I - L/2 and I + L/2 are
+// symmetric, so with gbar the adjoint of a step's output:
+//   b2bar = (I - Ly/2)^-1 gbar;        wbar = (I + Lx/2) b2bar
+//   b1bar = (I - Lx/2)^-1 wbar;        fbar = (I + Ly/2) b1bar - decay gbar
+//   dsrc += gbar;   ddecay -= <gbar, f>
+//   dD[owner of face] += -1/2 (p_j+1 - p_j)(q_j+1 - q_j) for the pairs
+//   (b2bar, v) and (b1bar, f) on y-faces, (b2bar, w) and (b1bar, w) on x-faces
+// Two kernels per backward step: BwdY applies the previous step's (I + Ly/2)
+// and then this step's y-solve (both along y), BwdX the x-stencil and x-solve.
+// States are recomputed segment by segment from checkpoints every k steps.
+//
+// Layout: every array is row-major x*yDim + y (HAL's layout).
+#include "common.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <utility>
+#include <vector>
+
+namespace halcuda
+{
+    namespace
+    {
+        constexpr int kMaxAdjLine = HAL_CUDA_ADJOINT_MAX_SIDE;
+
+        enum LineDir : int
+        {
+            kDirX = 0,  // line = fixed y, positions along x (stride yDim)
+            kDirY = 1   // line = fixed x, positions along y (contiguous)
+        };
+
+        struct Grid
+        {
+            int32_t xDim, yDim;
+            int32_t wrapX, wrapY;
+        };
+
+        template <int DIR>
+        __device__ __forceinline__ int64_t Idx(const Grid &g, int32_t line, int32_t pos)
+        {
+            return (DIR == kDirY) ? static_cast<int64_t>(line) * g.yDim + pos
+                                  : static_cast<int64_t>(pos) * g.yDim + line;
+        }
+
+        template <int DIR>
+        __device__ __forceinline__ int32_t LineLen(const Grid &g)
+        {
+            return (DIR == kDirY) ? g.yDim : g.xDim;
+        }
+
+        template <int DIR>
+        __device__ __forceinline__ int32_t Lines(const Grid &g)
+        {
+            return (DIR == kDirY) ? g.xDim : g.yDim;
+        }
+
+        template <int DIR>
+        __device__ __forceinline__ bool Wrap(const Grid &g)
+        {
+            return (DIR == kDirY) ? g.wrapY != 0 : g.wrapX != 0;
+        }
+
+        template <int DIR>
+        __device__ __forceinline__ bool WrapCross(const Grid &g)
+        {
+            return (DIR == kDirY) ? g.wrapX != 0 : g.wrapY != 0;
+        }
+
+        // Face weights below (eL) and above (eR) position j of a line whose
+        // rates sit in sD (one per position).
+        __device__ __forceinline__ void Faces(const float *sD, int32_t j, int32_t n, bool wrap, float &eL, float &eR)
+        {
+            eL = (j > 0) ? sD[j - 1] : (wrap ? sD[n - 1] : 0.0f);
+            eR = (j < n - 1) ? sD[j] : (wrap ? sD[n - 1] : 0.0f);
+        }
+
+        // (L u)_j along the line, with the line's u and rates in shared memory.
+        __device__ __forceinline__ float LapAlong(const float *su, const float *sD, int32_t j, int32_t n, bool wrap)
+        {
+            float eL, eR;
+            Faces(sD, j, n, wrap, eL, eR);
+            const float c = su[j];
+            const float lo = (j > 0) ? su[j - 1] : (wrap ? su[n - 1] : c);
+            const float hi = (j < n - 1) ? su[j + 1] : (wrap ? su[0] : c);
+            return eR * (hi - c) + eL * (lo - c);
+        }
+
+        // (L_cross u) at (line, j): the neighbours are lines line-1 and
+        // line+1; the face (line, line+1) carries D(line, j), the face
+        // (line-1, line) carries D(line-1, j).
+        template <int DIR>
+        __device__ __forceinline__ float LapCross(const Grid &g, const float *__restrict__ u,
+                                                  const float *__restrict__ D, int32_t line, int32_t j, float c)
+        {
+            const int32_t nl = Lines<DIR>(g);
+            const bool wrap = WrapCross<DIR>(g);
+            float acc = 0.0f;
+            if (line + 1 < nl || (wrap && nl > 1))
+            {
+                const int32_t up = (line + 1 < nl) ? line + 1 : 0;
+                acc += D[Idx<DIR>(g, line, j)] * (u[Idx<DIR>(g, up, j)] - c);
+            }
+            if (line > 0 || (wrap && nl > 1))
+            {
+                const int32_t dn = (line > 0) ? line - 1 : nl - 1;
+                acc += D[Idx<DIR>(g, dn, j)] * (u[Idx<DIR>(g, dn, j)] - c);
+            }
+            return acc;
+        }
+
+        // -1/2 (p_j+1 - p_j)(q_j+1 - q_j) for the face above position j (the
+        // face owned by j), 0 if it does not exist.
+        __device__ __forceinline__ float FaceGrad(const float *sp, const float *sq, int32_t j, int32_t n, bool wrap)
+        {
+            if (j < n - 1)
+            {
+                return -0.5f * (sp[j + 1] - sp[j]) * (sq[j + 1] - sq[j]);
+            }
+            if (wrap && n > 1)
+            {
+                return -0.5f * (sp[0] - sp[j]) * (sq[0] - sq[j]);
+            }
+            return 0.0f;
+        }
+
+        // Solves (I - L/2) x = d along the line by parallel cyclic reduction;
+        // thread j holds row j (j < n); sm holds 4 * blockDim.x floats.  A
+        // wrapped line must have a power-of-two length.
+        __device__ float PcrSolve(const float *sD, float d, int32_t j, int32_t n, bool wrap, float *sm)
+        {
+            float *sa = sm, *sb = sm + blockDim.x, *sc = sb + blockDim.x, *sd = sc + blockDim.x;
+            float a = 0.0f, b = 1.0f, c = 0.0f;
+            if (j < n)
+            {
+                float eL, eR;
+                Faces(sD, j, n, wrap, eL, eR);
+                a = -0.5f * eL;
+                c = -0.5f * eR;
+                b = 1.0f + 0.5f * (eL + eR);
+            }
+            for (int32_t delta = 1; delta < n; delta <<= 1)
+            {
+                if (j < n)
+                {
+                    sa[j] = a;
+                    sb[j] = b;
+                    sc[j] = c;
+                    sd[j] = d;
+                }
+                __syncthreads();
+                if (j < n)
+                {
+                    float al = 0.0f, bl = 1.0f, cl = 0.0f, dl = 0.0f;
+                    float ar = 0.0f, br = 1.0f, cr = 0.0f, dr = 0.0f;
+                    int32_t il = j - delta, ir = j + delta;
+                    if (wrap)
+                    {
+                        il = (il < 0) ? il + n : il;
+                        ir = (ir >= n) ? ir - n : ir;
+                    }
+                    if (il >= 0)
+                    {
+                        al = sa[il];
+                        bl = sb[il];
+                        cl = sc[il];
+                        dl = sd[il];
+                    }
+                    if (ir < n)
+                    {
+                        ar = sa[ir];
+                        br = sb[ir];
+                        cr = sc[ir];
+                        dr = sd[ir];
+                    }
+                    // fast reciprocal division (about 2 ulp): the rows are
+                    // diagonally dominant, so the reduction stays well
+                    // conditioned
+                    const float alpha = -__fdividef(a, bl);
+                    const float gamma = -__fdividef(c, br);
+                    b = b + alpha * cl + gamma * ar;
+                    d = d + alpha * dl + gamma * dr;
+                    a = alpha * al;
+                    c = gamma * cr;
+                }
+                __syncthreads();
+            }
+            // non-wrapped: every coupling left the line; wrapped: the last
+            // step coupled each row to itself
+            return wrap ? d / (a + b + c) : d / b;
+        }
+
+        __device__ __forceinline__ double BlockSum(double v, double *sred)
+        {
+            for (int o = 16; o > 0; o >>= 1)
+            {
+                v += __shfl_down_sync(0xffffffffu, v, o);
+            }
+            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+            __syncthreads();
+            if (lane == 0)
+            {
+                sred[warp] = v;
+            }
+            __syncthreads();
+            double t = 0.0;
+            if (threadIdx.x == 0)
+            {
+                for (int k = 0; k < static_cast<int>((blockDim.x + 31) / 32); k++)
+                {
+                    t += sred[k];
+                }
+            }
+            return t;
+        }
+
+        // Shared memory of the line kernels: 4 PCR arrays + 4 line arrays.
+        __host__ __device__ constexpr size_t LineSmemFloats(int threads)
+        {
+            return 8 * static_cast<size_t>(threads);
+        }
+
+        // x-sweep: w = (I - Lx/2)^-1 (I + Ly/2) f, one CTA per line y, in
+        // residual form: w = f + (I - Lx/2)^-1 (Lx + Ly) f / 2, so that the
+        // solve's rounding scales with the step's change, not the field.
+        __global__ void FwdX(Grid g, const float *__restrict__ f, const float *__restrict__ D, float *__restrict__ w)
+        {
+            extern __shared__ float sm[];
+            float *sD = sm + 4 * blockDim.x;
+            float *su = sD + blockDim.x;
+            const int32_t line = blockIdx.x;
+            const int32_t n = g.xDim;
+            const int32_t j = threadIdx.x;
+            float c = 0.0f, lap = 0.0f;
+            if (j < n)
+            {
+                const int64_t i = Idx<kDirX>(g, line, j);
+                sD[j] = D[i];
+                c = f[i];
+                su[j] = c;
+                lap = LapCross<kDirX>(g, f, D, line, j, c);
+            }
+            __syncthreads();
+            if (j < n)
+            {
+                lap += LapAlong(su, sD, j, n, g.wrapX != 0);
+            }
+            const float e = PcrSolve(sD, 0.5f * lap, j, n, g.wrapX != 0, sm);
+            if (j < n)
+            {
+                w[Idx<kDirX>(g, line, j)] = c + e;
+            }
+        }
+
+        // y-sweep and commit: v = (I - Ly/2)^-1 (I + Lx/2) w,
+        // f' = f + (((v - f) + f*(-decay)) + src); v is kept when vOut != null.
+        __global__ void FwdY(Grid g, const float *__restrict__ w, const float *__restrict__ f,
+                             const float *__restrict__ D, const float *__restrict__ src, float negDecay,
+                             float *__restrict__ fOut, float *__restrict__ vOut)
+        {
+            extern __shared__ float sm[];
+            float *sD = sm + 4 * blockDim.x;
+            float *su = sD + blockDim.x;
+            const int32_t line = blockIdx.x;
+            const int32_t n = g.yDim;
+            const int32_t j = threadIdx.x;
+            float c = 0.0f, lap = 0.0f;
+            if (j < n)
+            {
+                const int64_t i = Idx<kDirY>(g, line, j);
+                sD[j] = D[i];
+                c = w[i];
+                su[j] = c;
+                lap = LapCross<kDirY>(g, w, D, line, j, c);
+            }
+            __syncthreads();
+            if (j < n)
+            {
+                lap += LapAlong(su, sD, j, n, g.wrapY != 0);
+            }
+            // residual form: v = w + (I - Ly/2)^-1 (Lx + Ly) w / 2
+            const float e = PcrSolve(sD, 0.5f * lap, j, n, g.wrapY != 0, sm);
+            if (j < n)
+            {
+                const int64_t i = Idx<kDirY>(g, line, j);
+                const float f0 = f[i];
+                // v - f = (w - f) + e: both small, so the commit keeps the
+                // field's precision
+                float delta = (c - f0) + e;
+                delta = delta + f0 * negDecay;
+                if (src != nullptr)
+                {
+                    delta = delta + src[i];
+                }
+                fOut[i] = f0 + delta;
+                if (vOut != nullptr)
+                {
+                    vOut[i] = c + e;
+                }
+            }
+        }
+
+        // loss += 1/2 (f - target)^2; gbar = f - target.
+        __global__ void LossGrad(int64_t n, const float *__restrict__ f, const float *__restrict__ target,
+                                 float *__restrict__ gbar, double *__restrict__ loss)
+        {
+            __shared__ double sred[32];
+            double acc = 0.0;
+            for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+                 i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+            {
+                const float r = f[i] - target[i];
+                if (gbar != nullptr)
+                {
+                    gbar[i] = r;
+                }
+                acc += 0.5 * static_cast<double>(r) * static_cast<double>(r);
+            }
+            const double t = BlockSum(acc, sred);
+            if (threadIdx.x == 0)
+            {
+                atomicAdd(loss, t);
+            }
+        }
+
+        enum BwdYMode : int
+        {
+            kBwdFirst = 0,  // gbar given (the last step's output adjoint)
+            kBwdNext = 1,   // gbar = (I + Ly/2) b1bar - decay gbarPrev
+            kBwdTail = 2    // the y-stencil part of kBwdNext only (after step 0)
+        };
+
+        // Backward along y for step t: [gbar from step t+1] then the y-solve.
+        __global__ void BwdY(Grid g, int mode, const float *__restrict__ D, float decay,
+                             const float *__restrict__ b1bar,     // step t+1's x-solve adjoint (kBwdNext/Tail)
+                             const float *__restrict__ gPrev,     // adjoint of f_t+2 (kBwdNext/Tail), or gbar (kBwdFirst)
+                             const float *__restrict__ fNext,     // f_t+1 (kBwdNext/Tail)
+                             const float *__restrict__ fT,        // f_t (input of step t)
+                             const float *__restrict__ vT,        // v_t
+                             float *__restrict__ gOut,            // adjoint of f_t+1 (gbar of step t)
+                             float *__restrict__ b2bar, float *__restrict__ dD, float *__restrict__ dS,
+                             double *__restrict__ dDecay)
+        {
+            extern __shared__ float sm[];
+            float *sD = sm + 4 * blockDim.x;
+            float *sp = sD + blockDim.x;
+            float *sq = sp + blockDim.x;
+            float *sr = sq + blockDim.x;
+            __shared__ double sred[32];
+            const int32_t line = blockIdx.x;
+            const int32_t n = g.yDim;
+            const bool wrap = g.wrapY != 0;
+            const int32_t j = threadIdx.x;
+            const int64_t i = (j < n) ? Idx<kDirY>(g, line, j) : 0;
+            float gbar = 0.0f, dDacc = 0.0f;
+            if (j < n)
+            {
+                sD[j] = D[i];
+                if (mode == kBwdFirst)
+                {
+                    gbar = gPrev[i];
+                }
+                else
+                {
+                    sp[j] = b1bar[i];
+                    sq[j] = fNext[i];
+                }
+            }
+            __syncthreads();
+            if (mode != kBwdFirst)
+            {
+                if (j < n)
+                {
+                    gbar = (sp[j] + 0.5f * LapAlong(sp, sD, j, n, wrap)) - decay * gPrev[i];
+                    dDacc += FaceGrad(sp, sq, j, n, wrap);
+                }
+                if (mode == kBwdTail)
+                {
+                    if (j < n)
+                    {
+                        dD[i] += dDacc;
+                    }
+                    return;
+                }
+            }
+            double kacc = 0.0;
+            if (j < n)
+            {
+                dS[i] += gbar;
+                kacc = -static_cast<double>(gbar) * static_cast<double>(fT[i]);
+                gOut[i] = gbar;
+            }
+            const double ksum = BlockSum(kacc, sred);
+            if (threadIdx.x == 0)
+            {
+                atomicAdd(dDecay, ksum);
+            }
+            // residual form: b2bar = gbar + (I - Ly/2)^-1 (Ly gbar) / 2
+            if (j < n)
+            {
+                sq[j] = gbar;
+            }
+            __syncthreads();
+            const float lapg = (j < n) ? LapAlong(sq, sD, j, n, wrap) : 0.0f;
+            const float x = gbar + PcrSolve(sD, 0.5f * lapg, j, n, wrap, sm);
+            if (j < n)
+            {
+                sp[j] = x;
+                sr[j] = vT[i];
+            }
+            __syncthreads();
+            if (j < n)
+            {
+                dDacc += FaceGrad(sp, sr, j, n, wrap);
+                b2bar[i] = x;
+                dD[i] += dDacc;
+            }
+        }
+
+        // Backward along x for step t: wbar = (I + Lx/2) b2bar, b1bar = (I - Lx/2)^-1 wbar.
+        __global__ void BwdX(Grid g, const float *__restrict__ D, const float *__restrict__ b2bar,
+                             const float *__restrict__ wT, float *__restrict__ b1bar, float *__restrict__ dD)
+        {
+            extern __shared__ float sm[];
+            float *sD = sm + 4 * blockDim.x;
+            float *sp = sD + blockDim.x;
+            float *sw = sp + blockDim.x;
+            const int32_t line = blockIdx.x;
+            const int32_t n = g.xDim;
+            const bool wrap = g.wrapX != 0;
+            const int32_t j = threadIdx.x;
+            const int64_t i = (j < n) ? Idx<kDirX>(g, line, j) : 0;
+            if (j < n)
+            {
+                sD[j] = D[i];
+                sp[j] = b2bar[i];
+                sw[j] = wT[i];
+            }
+            __syncthreads();
+            float wbar = 0.0f, dDacc = 0.0f, lapb = 0.0f;
+            if (j < n)
+            {
+                lapb = LapAlong(sp, sD, j, n, wrap);
+                wbar = sp[j] + 0.5f * lapb;
+                dDacc = FaceGrad(sp, sw, j, n, wrap);
+            }
+            // residual form: b1bar = wbar + (I - Lx/2)^-1 (Lx wbar) / 2, with
+            // Lx wbar = Lx b2bar + Lx (Lx b2bar) / 2
+            float *sl = sw + blockDim.x;
+            if (j < n)
+            {
+                sl[j] = lapb;
+            }
+            __syncthreads();
+            const float lapw = (j < n) ? lapb + 0.5f * LapAlong(sl, sD, j, n, wrap) : 0.0f;
+            __syncthreads();
+            const float x = wbar + PcrSolve(sD, 0.5f * lapw, j, n, wrap, sm);
+            if (j < n)
+            {
+                sp[j] = x;
+            }
+            __syncthreads();
+            if (j < n)
+            {
+                dDacc += FaceGrad(sp, sw, j, n, wrap);
+                b1bar[i] = x;
+                dD[i] += dDacc;
+            }
+        }
+    }
+
+    struct Adjoint
+    {
+        int device = 0;
+        StreamSlot stream;
+        Grid g{};
+        int64_t n = 0;
+        int32_t steps = 0, every = 1;
+        bool hasProblem = false;
+        DevBuf<float> f0, target, D, src;
+        DevBuf<float> ckpt;                 // checkpoints: one field every `every` steps
+        DevBuf<float> segF, segW, segV;     // states of one segment
+        DevBuf<float> work[2];              // forward ping-pong
+        DevBuf<float> gA, gB, b1, b2, dD, dS;
+        DevBuf<double> acc;                 // [0] loss, [1] d loss / d decay
+        float msForward = 0.0f, msGradient = 0.0f;
+
+        int32_t Segments() const
+        {
+            return (steps + every - 1) / every;
+        }
+
+        int Init(int32_t xDim, int32_t yDim, int32_t wrapX, int32_t wrapY)
+        {
+            device = CurrentDevice();
+            HAL_TRY(CudaStatus(cudaSetDevice(device), "cudaSetDevice"));
+            HAL_TRY(stream.Create("cudaStreamCreate"));
+            g.xDim = xDim;
+            g.yDim = yDim;
+            g.wrapX = wrapX != 0;
+            g.wrapY = wrapY != 0;
+            n = static_cast<int64_t>(xDim) * yDim;
+            const size_t m = static_cast<size_t>(n);
+            HAL_TRY(f0.Alloc(m, "cudaMalloc(adjoint)"));
+            HAL_TRY(target.Alloc(m, "cudaMalloc(adjoint)"));
+            HAL_TRY(D.Alloc(m, "cudaMalloc(adjoint)"));
+            HAL_TRY(src.Alloc(m, "cudaMalloc(adjoint)"));
+            HAL_TRY(work[0].Alloc(m, "cudaMalloc(adjoint)"));
+            HAL_TRY(work[1].Alloc(m, "cudaMalloc(adjoint)"));
+            HAL_TRY(gA.Alloc(m, "cudaMalloc(adjoint)"));
+            HAL_TRY(gB.Alloc(m, "cudaMalloc(adjoint)"));
+            HAL_TRY(b1.Alloc(m, "cudaMalloc(adjoint)"));
+            HAL_TRY(b2.Alloc(m, "cudaMalloc(adjoint)"));
+            HAL_TRY(dD.Alloc(m, "cudaMalloc(adjoint)"));
+            HAL_TRY(dS.Alloc(m, "cudaMalloc(adjoint)"));
+            HAL_TRY(acc.Alloc(2, "cudaMalloc(adjoint)"));
+            return HAL_CUDA_OK;
+        }
+
+        static int Threads(int32_t len)
+        {
+            return (len + 31) & ~31;
+        }
+
+        int LaunchFwd(const float *fIn, float *fOut, float *wOut, float *vOut, const float *srcp, float negDecay,
+                      cudaStream_t s)
+        {
+            const int tx = Threads(g.xDim), ty = Threads(g.yDim);
+            FwdX<<<g.yDim, tx, LineSmemFloats(tx) * sizeof(float), s>>>(g, fIn, D.p, wOut);
+            FwdY<<<g.xDim, ty, LineSmemFloats(ty) * sizeof(float), s>>>(g, wOut, fIn, D.p, srcp, negDecay, fOut,
+                                                                         vOut);
+            CountLaunch(2);
+            return LaunchStatus("adjoint forward step");
+        }
+
+        int Upload(const float *hD, const float *hSrc, bool &useSrc, cudaStream_t s)
+        {
+            const size_t bytes = static_cast<size_t>(n) * sizeof(float);
+            HAL_TRY(CudaStatus(cudaMemcpyAsync(D.p, hD, bytes, cudaMemcpyHostToDevice, s), "cudaMemcpy(D)"));
+            useSrc = (hSrc != nullptr);
+            if (useSrc)
+            {
+                HAL_TRY(CudaStatus(cudaMemcpyAsync(src.p, hSrc, bytes, cudaMemcpyHostToDevice, s), "cudaMemcpy(src)"));
+            }
+            return HAL_CUDA_OK;
+        }
+
+        // `steps` forward steps from f0; checkpoints stored when ck != null.
+        // Returns the buffer holding f_T.
+        const float *Forward(const float *srcp, float negDecay, float *ck, cudaStream_t s, int &rc)
+        {
+            const size_t bytes = static_cast<size_t>(n) * sizeof(float);
+            rc = CudaStatus(cudaMemcpyAsync(work[0].p, f0.p, bytes, cudaMemcpyDeviceToDevice, s), "cudaMemcpy(f0)");
+            int c = 0;
+            for (int32_t t = 0; t < steps && rc == HAL_CUDA_OK; t++)
+            {
+                if (ck != nullptr && t % every == 0)
+                {
+                    rc = CudaStatus(cudaMemcpyAsync(ck + static_cast<size_t>(t / every) * n, work[c].p, bytes,
+                                                    cudaMemcpyDeviceToDevice, s), "cudaMemcpy(checkpoint)");
+                }
+                if (rc == HAL_CUDA_OK)
+                {
+                    rc = LaunchFwd(work[c].p, work[c ^ 1].p, b1.p, nullptr, srcp, negDecay, s);
+                }
+                c ^= 1;
+            }
+            return work[c].p;
+        }
+
+        int LaunchLoss(const float *fT, float *gbar, cudaStream_t s)
+        {
+            const int T = 256;
+            const int blocks = static_cast<int>(std::min<int64_t>((n + T - 1) / T, 1024));
+            LossGrad<<<blocks, T, 0, s>>>(n, fT, target.p, gbar, acc.p);
+            CountLaunch();
+            return LaunchStatus("adjoint loss");
+        }
+
+        int RunForward(const float *hD, double decay, const float *hSrc, double *loss, float *hFT)
+        {
+            cudaStream_t s = stream.Get();
+            bool useSrc = false;
+            HAL_TRY(Upload(hD, hSrc, useSrc, s));
+            HAL_TRY(CudaStatus(cudaMemsetAsync(acc.p, 0, 2 * sizeof(double), s), "cudaMemset(acc)"));
+            cudaEvent_t e0, e1;
+            HAL_TRY(CudaStatus(cudaEventCreate(&e0), "cudaEventCreate"));
+            HAL_TRY(CudaStatus(cudaEventCreate(&e1), "cudaEventCreate"));
+            cudaEventRecord(e0, s);
+            int rc = HAL_CUDA_OK;
+            const float *fT = Forward(useSrc ? src.p : nullptr, static_cast<float>(-decay), nullptr, s, rc);
+            if (rc == HAL_CUDA_OK)
+            {
+                rc = LaunchLoss(fT, nullptr, s);
+            }
+            cudaEventRecord(e1, s);
+            double h[2] = {0, 0};
+            if (rc == HAL_CUDA_OK)
+            {
+                rc = CudaStatus(cudaMemcpyAsync(h, acc.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, s),
+                                "cudaMemcpy(loss)");
+            }
+            if (rc == HAL_CUDA_OK && hFT != nullptr)
+            {
+                rc = CudaStatus(cudaMemcpyAsync(hFT, fT, static_cast<size_t>(n) * sizeof(float), cudaMemcpyDeviceToHost,
+                                                s), "cudaMemcpy(f_T)");
+            }
+            if (rc == HAL_CUDA_OK)
+            {
+                rc = CudaStatus(cudaStreamSynchronize(s), "adjoint forward");
+            }
+            if (rc == HAL_CUDA_OK)
+            {
+                cudaEventElapsedTime(&msForward, e0, e1);
+                *loss = h[0];
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return rc;
+        }
+
+        int RunGradient(const float *hD, double decay, const float *hSrc, double *loss, float *hgD, double *hgK,
+                        float *hgS)
+        {
+            cudaStream_t s = stream.Get();
+            bool useSrc = false;
+            HAL_TRY(Upload(hD, hSrc, useSrc, s));
+            const size_t bytes = static_cast<size_t>(n) * sizeof(float);
+            const float *srcp = useSrc ? src.p : nullptr;
+            const float negDecay = static_cast<float>(-decay);
+            HAL_TRY(CudaStatus(cudaMemsetAsync(acc.p, 0, 2 * sizeof(double), s), "cudaMemset(acc)"));
+            HAL_TRY(CudaStatus(cudaMemsetAsync(dD.p, 0, bytes, s), "cudaMemset(dD)"));
+            HAL_TRY(CudaStatus(cudaMemsetAsync(dS.p, 0, bytes, s), "cudaMemset(dS)"));
+            cudaEvent_t e0, e1;
+            HAL_TRY(CudaStatus(cudaEventCreate(&e0), "cudaEventCreate"));
+            HAL_TRY(CudaStatus(cudaEventCreate(&e1), "cudaEventCreate"));
+            cudaEventRecord(e0, s);
+            int rc = HAL_CUDA_OK;
+            const float *fT = Forward(srcp, negDecay, ckpt.p, s, rc);
+            float *gCur = gA.p, *gNext = gB.p;  // gCur: adjoint of the latest output handled
+            if (rc == HAL_CUDA_OK)
+            {
+                rc = LaunchLoss(fT, gCur, s);
+            }
+            const int tx = Threads(g.xDim), ty = Threads(g.yDim);
+            const size_t smx = LineSmemFloats(tx) * sizeof(float), smy = LineSmemFloats(ty) * sizeof(float);
+            bool first = true;
+            for (int32_t seg = Segments() - 1; seg >= 0 && rc == HAL_CUDA_OK; seg--)
+            {
+                const int32_t t0 = seg * every;
+                const int32_t t1 = std::min(steps, t0 + every);
+                // recompute the segment's states f_t0..f_t1, w and v
+                rc = CudaStatus(cudaMemcpyAsync(segF.p, ckpt.p + static_cast<size_t>(seg) * n, bytes,
+                                                cudaMemcpyDeviceToDevice, s), "cudaMemcpy(segment)");
+                for (int32_t t = t0; t < t1 && rc == HAL_CUDA_OK; t++)
+                {
+                    const size_t k = static_cast<size_t>(t - t0);
+                    rc = LaunchFwd(segF.p + k * n, segF.p + (k + 1) * n, segW.p + k * n, segV.p + k * n, srcp,
+                                   negDecay, s);
+                }
+                for (int32_t t = t1 - 1; t >= t0 && rc == HAL_CUDA_OK; t--)
+                {
+                    const size_t k = static_cast<size_t>(t - t0);
+                    const float *fNext = segF.p + (k + 1) * n;
+                    BwdY<<<g.xDim, ty, smy, s>>>(g, first ? kBwdFirst : kBwdNext, D.p, static_cast<float>(decay),
+                                                 b1.p, gCur, fNext, segF.p + k * n, segV.p + k * n, gNext, b2.p,
+                                                 dD.p, dS.p, acc.p + 1);
+                    BwdX<<<g.yDim, tx, smx, s>>>(g, D.p, b2.p, segW.p + k * n, b1.p, dD.p);
+                    CountLaunch(2);
+                    rc = LaunchStatus("adjoint backward step");
+                    std::swap(gCur, gNext);
+                    first = false;
+                }
+            }
+            if (rc == HAL_CUDA_OK && steps > 0)
+            {
+                // the y-stencil part of step 0's (I + Ly/2) b1bar: its D terms
+                BwdY<<<g.xDim, ty, smy, s>>>(g, kBwdTail, D.p, static_cast<float>(decay), b1.p, gCur, segF.p,
+                                             segF.p, segV.p, gNext, b2.p, dD.p, dS.p, acc.p + 1);
+                CountLaunch();
+                rc = LaunchStatus("adjoint backward tail");
+            }
+            cudaEventRecord(e1, s);
+            double h[2] = {0, 0};
+            if (rc == HAL_CUDA_OK)
+            {
+                rc = CudaStatus(cudaMemcpyAsync(h, acc.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, s),
+                                "cudaMemcpy(loss)");
+            }
+            if (rc == HAL_CUDA_OK && hgD != nullptr)
+            {
+                rc = CudaStatus(cudaMemcpyAsync(hgD, dD.p, bytes, cudaMemcpyDeviceToHost, s), "cudaMemcpy(dD)");
+            }
+            if (rc == HAL_CUDA_OK && hgS != nullptr)
+            {
+                rc = CudaStatus(cudaMemcpyAsync(hgS, dS.p, bytes, cudaMemcpyDeviceToHost, s), "cudaMemcpy(dS)");
+            }
+            if (rc == HAL_CUDA_OK)
+            {
+                rc = CudaStatus(cudaStreamSynchronize(s), "adjoint gradient");
+            }
+            if (rc == HAL_CUDA_OK)
+            {
+                cudaEventElapsedTime(&msGradient, e0, e1);
+                *loss = h[0];
+                if (hgK != nullptr)
+                {
+                    *hgK = h[1];
+                }
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return rc;
+        }
+    };
+
+    namespace
+    {
+        bool PowerOfTwo(int32_t v)
+        {
+            return v > 0 && (v & (v - 1)) == 0;
+        }
+    }
+}
+
+using halcuda::Adjoint;
+
+struct hal_cuda_adjoint : public Adjoint
+{
+};
+
+extern "C" int hal_cuda_adjoint_create(int32_t xDim, int32_t yDim, int32_t wrapX, int32_t wrapY,
+                                       hal_cuda_adjoint **out)
+{
+    HAL_REQUIRE(out != nullptr, "hal_cuda_adjoint_create: out is NULL");
+    *out = nullptr;
+    HAL_REQUIRE(xDim >= 1 && yDim >= 1 && xDim <= halcuda::kMaxAdjLine && yDim <= halcuda::kMaxAdjLine,
+                "hal_cuda_adjoint_create: grid %d x %d, sides must be in [1, %d]", xDim, yDim, halcuda::kMaxAdjLine);
+    HAL_REQUIRE(!wrapX || halcuda::PowerOfTwo(xDim), "hal_cuda_adjoint_create: a wrapped x axis needs a power-of-two "
+                                                     "xDim (%d)", xDim);
+    HAL_REQUIRE(!wrapY || halcuda::PowerOfTwo(yDim), "hal_cuda_adjoint_create: a wrapped y axis needs a power-of-two "
+                                                     "yDim (%d)", yDim);
+    hal_cuda_adjoint *h = new (std::nothrow) hal_cuda_adjoint();
+    if (h == nullptr)
+    {
+        halcuda::SetError("hal_cuda_adjoint_create: out of host memory");
+        return HAL_CUDA_ENOMEM;
+    }
+    int rc = h->Init(xDim, yDim, wrapX, wrapY);
+    if (rc != HAL_CUDA_OK)
+    {
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return HAL_CUDA_OK;
+}
+
+extern "C" int hal_cuda_adjoint_destroy(hal_cuda_adjoint *h)
+{
+    if (h != nullptr)
+    {
+        cudaSetDevice(h->device);
+        cudaStreamSynchronize(h->stream.Get());
+        delete h;
+    }
+    return HAL_CUDA_OK;
+}
+
+extern "C" int hal_cuda_adjoint_set_problem(hal_cuda_adjoint *h, const float *f0, const float *target, int64_t len,
+                                            int32_t steps, int32_t checkpointEvery)
+{
+    HAL_REQUIRE(h != nullptr && f0 != nullptr && target != nullptr, "hal_cuda_adjoint_set_problem: NULL argument");
+    HAL_REQUIRE(len == h->n, "hal_cuda_adjoint_set_problem: length %lld, grid holds %lld cells",
+                static_cast<long long>(len), static_cast<long long>(h->n));
+    HAL_REQUIRE(steps >= 0, "hal_cuda_adjoint_set_problem: negative step count");
+    HAL_REQUIRE(checkpointEvery >= 1, "hal_cuda_adjoint_set_problem: checkpoint interval must be >= 1");
+    using namespace halcuda;
+    HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    const size_t m = static_cast<size_t>(h->n);
+    h->steps = steps;
+    h->every = std::min(checkpointEvery, std::max(steps, 1));
+    HAL_TRY(h->ckpt.Alloc(m * static_cast<size_t>(std::max(h->Segments(), 1)), "cudaMalloc(checkpoints)"));
+    HAL_TRY(h->segF.Alloc(m * static_cast<size_t>(h->every + 1), "cudaMalloc(segment)"));
+    HAL_TRY(h->segW.Alloc(m * static_cast<size_t>(h->every), "cudaMalloc(segment)"));
+    HAL_TRY(h->segV.Alloc(m * static_cast<size_t>(h->every), "cudaMalloc(segment)"));
+    cudaStream_t s = h->stream.Get();
+    HAL_TRY(CudaStatus(cudaMemcpyAsync(h->f0.p, f0, m * sizeof(float), cudaMemcpyHostToDevice, s), "cudaMemcpy(f0)"));
+    HAL_TRY(CudaStatus(cudaMemcpyAsync(h->target.p, target, m * sizeof(float), cudaMemcpyHostToDevice, s),
+                       "cudaMemcpy(target)"));
+    HAL_TRY(CudaStatus(cudaStreamSynchronize(s), "hal_cuda_adjoint_set_problem"));
+    h->hasProblem = true;
+    return HAL_CUDA_OK;
+}
+
+extern "C" int hal_cuda_adjoint_forward(hal_cuda_adjoint *h, const float *D, double decay, const float *src,
+                                        double *loss, float *fT)
+{
+    HAL_REQUIRE(h != nullptr && D != nullptr && loss != nullptr, "hal_cuda_adjoint_forward: NULL argument");
+    HAL_REQUIRE(h->hasProblem, "hal_cuda_adjoint_forward: call hal_cuda_adjoint_set_problem first");
+    HAL_REQUIRE(std::isfinite(decay), "hal_cuda_adjoint_forward: decay %g", decay);
+    HAL_TRY(halcuda::CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    return h->RunForward(D, decay, src, loss, fT);
+}
+
+extern "C" int hal_cuda_adjoint_gradient(hal_cuda_adjoint *h, const float *D, double decay, const float *src,
+                                         double *loss, float *gradD, double *gradDecay, float *gradSrc)
+{
+    HAL_REQUIRE(h != nullptr && D != nullptr && loss != nullptr, "hal_cuda_adjoint_gradient: NULL argument");
+    HAL_REQUIRE(h->hasProblem, "hal_cuda_adjoint_gradient: call hal_cuda_adjoint_set_problem first");
+    HAL_REQUIRE(std::isfinite(decay), "hal_cuda_adjoint_gradient: decay %g", decay);
+    HAL_TRY(halcuda::CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    return h->RunGradient(D, decay, src, loss, gradD, gradDecay, gradSrc);
+}
+
+extern "C" int hal_cuda_adjoint_times(hal_cuda_adjoint *h, float *msForward, float *msGradient)
+{
+    HAL_REQUIRE(h != nullptr && msForward != nullptr && msGradient != nullptr, "hal_cuda_adjoint_times: NULL argument");
+    *msForward = h->msForward;
+    *msGradient = h->msGradient;
+    return HAL_CUDA_OK;
+}

@@ -86,6 +86,12 @@ SIGNATURES = {
     "hal_cuda_wells_sync": (_I, [_vp]),
     "hal_cuda_wells_stream": (_vp, [_vp]),
     "hal_cuda_wells_set_stream": (_I, [_vp, _vp]),
+    "hal_cuda_adjoint_create": (_I, [_i32, _i32, _i32, _i32, _vp]),
+    "hal_cuda_adjoint_destroy": (_I, [_vp]),
+    "hal_cuda_adjoint_set_problem": (_I, [_vp, _vp, _vp, _i64, _i32, _i32]),
+    "hal_cuda_adjoint_forward": (_I, [_vp, _vp, _f64, _vp, _vp, _vp]),
+    "hal_cuda_adjoint_gradient": (_I, [_vp, _vp, _f64, _vp, _vp, _vp, _vp, _vp]),
+    "hal_cuda_adjoint_times": (_I, [_vp, _vp, _vp]),
     "hal_cuda_agents_forces_noalloc": (_I, [_vp, _vp, _i32, _vp, _f64, _f64, _i32, _i32, _i32, _i32,
                                             _vp]),
 }
@@ -479,6 +485,61 @@ class Wells(_Handle):
         _check(lib().hal_cuda_wells_profile(self._h, iters, interactionRad, springConstant, _p(ms)),
                "wells_profile")
         return [float(v) for v in ms]
+
+
+ADJOINT_MAX_SIDE = 1024
+
+
+class Adjoint(_Handle):
+    """hal_cuda_adjoint: variable-rate ADI steps and the gradient of
+    1/2 |f_T - target|^2 with respect to the rate field D, decay and source."""
+
+    _prefix = "adjoint"
+
+    def __init__(self, xDim, yDim, wrapX=False, wrapY=False):
+        super().__init__()
+        h = ctypes.c_void_p()
+        _check(lib().hal_cuda_adjoint_create(xDim, yDim, int(wrapX), int(wrapY), ctypes.byref(h)),
+               "adjoint_create")
+        self._h = h
+        self.xDim, self.yDim = xDim, yDim
+
+    def sync(self):
+        pass
+
+    def set_problem(self, f0, target, steps, checkpoint_every=22):
+        a = _f32(f0)
+        t = _f32(target)
+        _check(lib().hal_cuda_adjoint_set_problem(self._h, _p(a), _p(t), a.size, steps, checkpoint_every),
+               "adjoint_set_problem")
+
+    def forward(self, D, decay, src=None, want_field=False):
+        d = _f32(D)
+        sv = _f32(src)
+        loss = ctypes.c_double(0.0)
+        fT = np.empty(self.xDim * self.yDim, dtype=np.float32) if want_field else None
+        _check(lib().hal_cuda_adjoint_forward(self._h, _p(d), decay, _p(sv), ctypes.byref(loss), _p(fT)),
+               "adjoint_forward")
+        return (loss.value, fT) if want_field else loss.value
+
+    def gradient(self, D, decay, src=None):
+        """Returns (loss, dD, dDecay, dSrc)."""
+        d = _f32(D)
+        sv = _f32(src)
+        n = self.xDim * self.yDim
+        gD = np.empty(n, dtype=np.float32)
+        gS = np.empty(n, dtype=np.float32)
+        loss = ctypes.c_double(0.0)
+        gK = ctypes.c_double(0.0)
+        _check(lib().hal_cuda_adjoint_gradient(self._h, _p(d), decay, _p(sv), ctypes.byref(loss), _p(gD),
+                                               ctypes.byref(gK), _p(gS)), "adjoint_gradient")
+        return loss.value, gD, gK.value, gS
+
+    def times(self):
+        """(ms of the last forward, ms of the last gradient), device time."""
+        a, b = ctypes.c_float(0.0), ctypes.c_float(0.0)
+        _check(lib().hal_cuda_adjoint_times(self._h, ctypes.byref(a), ctypes.byref(b)), "adjoint_times")
+        return a.value, b.value
 
 
 NOALLOC_MAX_AGENTS = 65536

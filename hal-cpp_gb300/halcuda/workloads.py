@@ -16,6 +16,11 @@ value distributions are the workloads' own:
                 half ADI with rate U[1, 10]; decay U[0, 0.02]; field U[0,1);
                 0..20000 uniform agents each (radius 0.5, cutoff 1.0,
                 stiffness 0.1, walls)
+* adjoint    -- 512 x 512, 500 steps, zero-flux; rate field D(x) = 0.5 + 4.5 *
+                normalise(sum of 32 cosine modes, integer wave numbers in
+                [-4, 4], N(0,1) amplitudes, U[0, 2pi) phases); decay 0.005;
+                source U[0, 0.01); initial field 40 Gaussian blobs; target =
+                the final field of the same model with a second seeded D
 """
 from __future__ import annotations
 
@@ -92,3 +97,31 @@ def wells_inputs(n_wells: int = 512, seed: int = 4, max_agents: int = 20000, min
                 positions=np.concatenate(pos) if pos else np.zeros(0, np.float32),
                 radii=np.concatenate(rad) if rad else np.zeros(0, np.float32),
                 interactionRad=1.0, springConstant=0.1)
+
+
+def rate_field(n: int, rng, modes: int = 32, lo: float = 0.5, hi: float = 5.0):
+    """Smooth random rate field in [lo, hi] from `modes` cosine modes."""
+    x = np.arange(n, dtype=np.float64)
+    X, Y = np.meshgrid(x, x, indexing="ij")
+    acc = np.zeros((n, n))
+    for _ in range(modes):
+        kx, ky = rng.integers(-4, 5, 2)
+        amp = rng.standard_normal()
+        phase = rng.random() * 2.0 * np.pi
+        acc += amp * np.cos(2.0 * np.pi * (kx * X + ky * Y) / n + phase)
+    span = acc.max() - acc.min()
+    acc = (acc - acc.min()) / (span if span > 0 else 1.0)
+    return (lo + (hi - lo) * acc).ravel()
+
+
+def adjoint_inputs(n: int = 512, seed: int = 5, steps: int = 500):
+    """Parameter-recovery problem: initial field, the unknown rate field D, a
+    second seeded ground-truth rate field, decay and source."""
+    rng = np.random.default_rng(seed)
+    f0 = gaussian_blobs(n, rng, 40)
+    D = rate_field(n, rng)
+    D_true = rate_field(n, rng)
+    src = rng.random(n * n) * 0.01
+    return dict(f0=f0.astype(np.float32), D=D.astype(np.float32), D_true=D_true.astype(np.float32),
+                src=src.astype(np.float32), decay=0.005, steps=steps, checkpoint_every=22, xDim=n, yDim=n,
+                fd_directions=64, fd_h=1e-3)

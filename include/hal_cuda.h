@@ -318,6 +318,47 @@ int hal_cuda_wells_sync(hal_cuda_wells *h);
 void *hal_cuda_wells_stream(hal_cuda_wells *h);
 int hal_cuda_wells_set_stream(hal_cuda_wells *h, void *stream);
 
+/* ---- variable-rate ADI and its gradient ------------------------------------
+ * No reference implementation exists (the reference has no variable-rate ADI
+ * and no gradient code).  The step follows HAL's variable-rate explicit
+ * stencil Internal::Diffusion2(..., pDiffRatesX, pDiffRatesY, ...)
+ * (src/Pde/PDEequations.cpp:199-230): the face between cells j and j+1 of a
+ * line carries cell j's rate D (D*dt/dx^2, one per cell, both axes):
+ *   w = (I - Lx/2)^-1 (I + Ly/2) f;  v = (I - Ly/2)^-1 (I + Lx/2) w;
+ *   f' = f + (((v - f) + f*(-decay)) + src)
+ * which for a constant D is hal_cuda_adi_run_ticks' tick.  The gradient of
+ * loss = 1/2 |f_T - target|^2 with respect to D, decay and src comes from
+ * adjoint kernels (transposed stencils and transposed line solves in reverse
+ * sweep order) over states recomputed from checkpoints.  Sides up to
+ * HAL_CUDA_ADJOINT_MAX_SIDE; a wrapped axis needs a power-of-two side. */
+#define HAL_CUDA_ADJOINT_MAX_SIDE 1024
+
+typedef struct hal_cuda_adjoint hal_cuda_adjoint;
+
+int hal_cuda_adjoint_create(int32_t xDim, int32_t yDim, int32_t wrapX, int32_t wrapY,
+                            hal_cuda_adjoint **out);
+int hal_cuda_adjoint_destroy(hal_cuda_adjoint *h);
+
+/* Initial field f0 and target final field (len = xDim*yDim floats each), the
+ * number of steps, and the checkpoint interval (a field is kept every
+ * checkpointEvery steps; the states in between are recomputed). */
+int hal_cuda_adjoint_set_problem(hal_cuda_adjoint *h, const float *f0, const float *target,
+                                 int64_t len, int32_t steps, int32_t checkpointEvery);
+
+/* loss (and f_T when fT is not NULL) for the rate field D (xDim*yDim), decay
+ * and source field (NULL: none). */
+int hal_cuda_adjoint_forward(hal_cuda_adjoint *h, const float *D, double decay, const float *src,
+                             double *loss, float *fT);
+
+/* loss and its gradients: gradD, gradSrc (xDim*yDim each, may be NULL) and
+ * gradDecay (may be NULL). */
+int hal_cuda_adjoint_gradient(hal_cuda_adjoint *h, const float *D, double decay, const float *src,
+                              double *loss, float *gradD, double *gradDecay, float *gradSrc);
+
+/* Device time (ms, CUDA events) of the last forward and gradient calls,
+ * from the first kernel to the last. */
+int hal_cuda_adjoint_times(hal_cuda_adjoint *h, float *msForward, float *msGradient);
+
 /* ---- agent forces without allocation --------------------------------------
  * No counterpart in the reference: the reference's backends allocate their
  * buffers.  This entry point is for callers that cannot call cudaMalloc -- a

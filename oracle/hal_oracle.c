@@ -873,3 +873,337 @@ double oracle_rand_gaussian(oracle_rand *r, double mean, double stdDev)
     r->phase = 1 - r->phase;
     return x * stdDev + mean;
 }
+
+/* ---- variable-rate ADI and its adjoint -------------------------------------
+ * The reference has no variable-rate ADI and no gradient code.  This is the
+ * builder's definition, written from HAL's variable-rate explicit stencil
+ * Internal::Diffusion2(pField, pDeltas, pDiffRatesX, pDiffRatesY, ...)
+ * (src/Pde/PDEequations.cpp:199-230): the face between cells j and j+1 of a
+ * line has the rate of cell j (the +x/+y face uses the cell's own rate, the
+ * -x/-y face the neighbour's), and a non-wrapped edge has no face.  With L
+ * the face-weighted Laplacian of a line, one step is
+ *   b1 = (I + L_y/2) f;  w = (I - L_x/2)^-1 b1;
+ *   b2 = (I + L_x/2) w;  v = (I - L_y/2)^-1 b2;
+ *   f' = f + (((v - f) + f * (-decay)) + src)      (PDEGrid2D tick order)
+ * which for a constant rate D = r is Internal::Diffusion2DADI
+ * (include/Hal/Pde/ADIequations.h:306-337) followed by the tick. */
+
+/* Face weight on the low (eL) and high (eR) side of cell j of a line whose
+ * face weights are e[j] = face (j, j+1) and, wrapped, e[n-1] = face (n-1, 0). */
+static void o_var_faces(const double *e, int32_t n, int wrap, int32_t j, double *eL, double *eR)
+{
+    *eL = (j > 0) ? e[j - 1] : (wrap ? e[n - 1] : 0.0);
+    *eR = (j < n - 1) ? e[j] : (wrap ? e[n - 1] : 0.0);
+}
+
+/* out = (I + s*L) u along one line (s = +1/2 or -1/2). */
+static void o_var_apply(const double *e, int32_t n, int wrap, double s, const double *u, double *out)
+{
+    for (int32_t j = 0; j < n; j++)
+    {
+        double eL, eR;
+        o_var_faces(e, n, wrap, j, &eL, &eR);
+        double lo = (j > 0) ? u[j - 1] : (wrap ? u[n - 1] : u[j]);
+        double hi = (j < n - 1) ? u[j + 1] : (wrap ? u[0] : u[j]);
+        out[j] = u[j] + s * (eR * (hi - u[j]) + eL * (lo - u[j]));
+    }
+}
+
+/* Solves (I - L/2) x = d along one line: Thomas, or for a wrapped line
+ * Sherman-Morrison around Thomas (as TdmaSolver::TDMAperiodic does,
+ * include/Hal/Pde/TdmaSolver.h:68-120).  work holds 6n doubles. */
+static void o_var_solve(const double *e, int32_t n, int wrap, const double *d, double *x, double *work)
+{
+    double *a = work, *b = work + n, *c = work + 2 * n, *y = work + 3 * n, *z = work + 4 * n,
+           *u = work + 5 * n;
+    for (int32_t j = 0; j < n; j++)
+    {
+        double eL, eR;
+        o_var_faces(e, n, wrap, j, &eL, &eR);
+        a[j] = -0.5 * eL;
+        c[j] = -0.5 * eR;
+        b[j] = 1.0 + 0.5 * (eL + eR);
+    }
+    if (n == 1)
+    {
+        /* a wrapped single cell couples only to itself: L = 0 */
+        x[0] = wrap ? d[0] / (a[0] + b[0] + c[0]) : d[0] / b[0];
+        return;
+    }
+    double gamma = 0.0, a0 = a[0], cn = c[n - 1];
+    if (wrap)
+    {
+        gamma = -b[0];
+        b[0] -= gamma;
+        b[n - 1] -= a0 * cn / gamma;
+    }
+    /* Thomas on (a, b, c) for the right-hand sides d -> y and (wrapped) u -> z */
+    for (int32_t pass = 0; pass < (wrap ? 2 : 1); pass++)
+    {
+        const double *rhs = (pass == 0) ? d : u;
+        double *out = (pass == 0) ? y : z;
+        if (pass == 1)
+        {
+            for (int32_t j = 0; j < n; j++)
+            {
+                u[j] = 0.0;
+            }
+            u[0] = gamma;
+            u[n - 1] = cn;
+        }
+        double *cp = x; /* scratch for the modified super-diagonal */
+        double denom = b[0];
+        cp[0] = c[0] / denom;
+        out[0] = rhs[0] / denom;
+        for (int32_t j = 1; j < n; j++)
+        {
+            denom = b[j] - a[j] * cp[j - 1];
+            cp[j] = (j < n - 1) ? c[j] / denom : 0.0;
+            out[j] = (rhs[j] - a[j] * out[j - 1]) / denom;
+        }
+        for (int32_t j = n - 2; j >= 0; j--)
+        {
+            out[j] -= cp[j] * out[j + 1];
+        }
+    }
+    if (!wrap)
+    {
+        for (int32_t j = 0; j < n; j++)
+        {
+            x[j] = y[j];
+        }
+        return;
+    }
+    /* v = (1, 0, ..., a0/gamma) */
+    double vy = y[0] + (a0 / gamma) * y[n - 1];
+    double vz = z[0] + (a0 / gamma) * z[n - 1];
+    double fct = vy / (1.0 + vz);
+    for (int32_t j = 0; j < n; j++)
+    {
+        x[j] = y[j] - fct * z[j];
+    }
+}
+
+/* Gathers line `l` of a row-major xDim x yDim array along x (dir 0: fixed y
+ * = l) or along y (dir 1: fixed x = l). */
+static void o_line_get(const double *g, int32_t xDim, int32_t yDim, int dir, int32_t l, double *out)
+{
+    if (dir == 0)
+    {
+        for (int32_t x = 0; x < xDim; x++)
+        {
+            out[x] = g[(size_t)x * yDim + l];
+        }
+    }
+    else
+    {
+        memcpy(out, g + (size_t)l * yDim, sizeof(double) * (size_t)yDim);
+    }
+}
+
+static void o_line_put(double *g, int32_t xDim, int32_t yDim, int dir, int32_t l, const double *in)
+{
+    if (dir == 0)
+    {
+        for (int32_t x = 0; x < xDim; x++)
+        {
+            g[(size_t)x * yDim + l] = in[x];
+        }
+    }
+    else
+    {
+        memcpy(g + (size_t)l * yDim, in, sizeof(double) * (size_t)yDim);
+    }
+}
+
+/* out = (I + s*L_dir) u, or with solve != 0 out = (I - L_dir/2)^-1 u, over
+ * every line of direction dir; D holds the cell rates. */
+static void o_var_sweep(const double *D, int32_t xDim, int32_t yDim, int wrapX, int wrapY, int dir, int solve,
+                        double s, const double *u, double *out, double *work)
+{
+    const int32_t n = (dir == 0) ? xDim : yDim;
+    const int32_t lines = (dir == 0) ? yDim : xDim;
+    const int wrap = (dir == 0) ? wrapX : wrapY;
+    double *e = work, *ul = work + n, *ol = work + 2 * n, *ws = work + 3 * n;
+    for (int32_t l = 0; l < lines; l++)
+    {
+        o_line_get(D, xDim, yDim, dir, l, e);
+        o_line_get(u, xDim, yDim, dir, l, ul);
+        if (solve)
+        {
+            o_var_solve(e, n, wrap, ul, ol, ws);
+        }
+        else
+        {
+            o_var_apply(e, n, wrap, s, ul, ol);
+        }
+        o_line_put(out, xDim, yDim, dir, l, ol);
+    }
+}
+
+/* Adds, for every face of direction dir, -1/2 (p_j+1 - p_j)(q_j+1 - q_j)
+ * to the rate gradient of the face's owner cell j:  d<p, L q>/d e_face =
+ * -(p_j+1 - p_j)(q_j+1 - q_j). */
+static void o_var_face_grad(const double *p, const double *q, int32_t xDim, int32_t yDim, int wrapX, int wrapY,
+                            int dir, double *gD)
+{
+    for (int32_t x = 0; x < xDim; x++)
+    {
+        for (int32_t y = 0; y < yDim; y++)
+        {
+            int32_t nx = x, ny = y;
+            if (dir == 0)
+            {
+                nx = x + 1;
+                if (nx == xDim)
+                {
+                    if (!wrapX)
+                    {
+                        continue;
+                    }
+                    nx = 0;
+                }
+            }
+            else
+            {
+                ny = y + 1;
+                if (ny == yDim)
+                {
+                    if (!wrapY)
+                    {
+                        continue;
+                    }
+                    ny = 0;
+                }
+            }
+            size_t i = (size_t)x * yDim + y, j = (size_t)nx * yDim + ny;
+            if (i == j)
+            {
+                continue; /* a wrapped line of one cell has no effective face */
+            }
+            gD[i] += -0.5 * (p[j] - p[i]) * (q[j] - q[i]);
+        }
+    }
+}
+
+void oracle_dadi_step(const double *f, const double *D, int32_t xDim, int32_t yDim, int wrapX, int wrapY,
+                      double decay, const double *src, double *w, double *out)
+{
+    size_t len = (size_t)xDim * yDim;
+    int32_t nmax = xDim > yDim ? xDim : yDim;
+    double *b = malloc(sizeof(double) * len);
+    double *work = malloc(sizeof(double) * (size_t)nmax * 9);
+    o_var_sweep(D, xDim, yDim, wrapX, wrapY, 1, 0, 0.5, f, b, work);  /* b1 = (I + Ly/2) f */
+    o_var_sweep(D, xDim, yDim, wrapX, wrapY, 0, 1, 0.0, b, w, work);  /* w = Ax^-1 b1 */
+    o_var_sweep(D, xDim, yDim, wrapX, wrapY, 0, 0, 0.5, w, b, work);  /* b2 = (I + Lx/2) w */
+    o_var_sweep(D, xDim, yDim, wrapX, wrapY, 1, 1, 0.0, b, out, work); /* v = Ay^-1 b2 */
+    for (size_t i = 0; i < len; i++)
+    {
+        double delta = out[i] - f[i];
+        delta += f[i] * (-decay);
+        if (src != NULL)
+        {
+            delta += src[i];
+        }
+        out[i] = f[i] + delta;
+    }
+    free(b);
+    free(work);
+}
+
+double oracle_dadi_loss_grad(const double *f0, const double *target, const double *D, double decay,
+                             const double *src, int32_t xDim, int32_t yDim, int wrapX, int wrapY, int32_t steps,
+                             double *fT, double *gD, double *gDecay, double *gSrc)
+{
+    size_t len = (size_t)xDim * yDim;
+    int grad = (gD != NULL || gDecay != NULL || gSrc != NULL);
+    /* all states f_0..f_T and intermediates w_t (the FP64 oracle keeps every
+     * step; the GPU path checkpoints) */
+    double *fs = malloc(sizeof(double) * len * (size_t)(steps + 1));
+    double *ws = malloc(sizeof(double) * len * (size_t)(steps > 0 ? steps : 1));
+    memcpy(fs, f0, sizeof(double) * len);
+    for (int32_t t = 0; t < steps; t++)
+    {
+        oracle_dadi_step(fs + len * t, D, xDim, yDim, wrapX, wrapY, decay, src, ws + len * t, fs + len * (t + 1));
+    }
+    const double *f = fs + len * (size_t)steps;
+    double loss = 0.0;
+    for (size_t i = 0; i < len; i++)
+    {
+        double r = f[i] - target[i];
+        loss += 0.5 * r * r;
+    }
+    if (fT != NULL)
+    {
+        memcpy(fT, f, sizeof(double) * len);
+    }
+    if (grad)
+    {
+        int32_t nmax = xDim > yDim ? xDim : yDim;
+        double *g = malloc(sizeof(double) * len);
+        double *b2 = malloc(sizeof(double) * len);
+        double *t1 = malloc(sizeof(double) * len);
+        double *b1 = malloc(sizeof(double) * len);
+        double *v = malloc(sizeof(double) * len);
+        double *work = malloc(sizeof(double) * (size_t)nmax * 9);
+        double *dD = calloc(len, sizeof(double));
+        double *dS = calloc(len, sizeof(double));
+        double dK = 0.0;
+        for (size_t i = 0; i < len; i++)
+        {
+            g[i] = f[i] - target[i];
+        }
+        for (int32_t t = steps - 1; t >= 0; t--)
+        {
+            const double *ft = fs + len * t, *wt = ws + len * t;
+            /* v_t from the step's own sweeps */
+            o_var_sweep(D, xDim, yDim, wrapX, wrapY, 0, 0, 0.5, wt, t1, work);
+            o_var_sweep(D, xDim, yDim, wrapX, wrapY, 1, 1, 0.0, t1, v, work);
+            /* f' = v - decay f + src */
+            for (size_t i = 0; i < len; i++)
+            {
+                dS[i] += g[i];
+                dK += -g[i] * ft[i];
+            }
+            /* v = Ay^-1 b2:  b2bar = Ay^-1 g (Ay symmetric), dD += 1/2 <b2bar, dLy v> */
+            o_var_sweep(D, xDim, yDim, wrapX, wrapY, 1, 1, 0.0, g, b2, work);
+            o_var_face_grad(b2, v, xDim, yDim, wrapX, wrapY, 1, dD);
+            /* b2 = (I + Lx/2) w:  wbar = (I + Lx/2) b2bar, dD += 1/2 <b2bar, dLx w> */
+            o_var_face_grad(b2, wt, xDim, yDim, wrapX, wrapY, 0, dD);
+            o_var_sweep(D, xDim, yDim, wrapX, wrapY, 0, 0, 0.5, b2, t1, work);
+            /* w = Ax^-1 b1:  b1bar = Ax^-1 wbar, dD += 1/2 <b1bar, dLx w> */
+            o_var_sweep(D, xDim, yDim, wrapX, wrapY, 0, 1, 0.0, t1, b1, work);
+            o_var_face_grad(b1, wt, xDim, yDim, wrapX, wrapY, 0, dD);
+            /* b1 = (I + Ly/2) f:  fbar = (I + Ly/2) b1bar - decay g, dD += 1/2 <b1bar, dLy f> */
+            o_var_face_grad(b1, ft, xDim, yDim, wrapX, wrapY, 1, dD);
+            o_var_sweep(D, xDim, yDim, wrapX, wrapY, 1, 0, 0.5, b1, t1, work);
+            for (size_t i = 0; i < len; i++)
+            {
+                g[i] = t1[i] - decay * g[i];
+            }
+        }
+        if (gD != NULL)
+        {
+            memcpy(gD, dD, sizeof(double) * len);
+        }
+        if (gSrc != NULL)
+        {
+            memcpy(gSrc, dS, sizeof(double) * len);
+        }
+        if (gDecay != NULL)
+        {
+            *gDecay = dK;
+        }
+        free(g);
+        free(b2);
+        free(t1);
+        free(b1);
+        free(v);
+        free(work);
+        free(dD);
+        free(dS);
+    }
+    free(fs);
+    free(ws);
+    return loss;
+}

@@ -109,6 +109,27 @@ int oracle_accumulate_forces(const double *positions, const double *radii,
                              int32_t *cellOffsets, int32_t *bucketAgents,
                              int nthreads);
 
+/* ---- variable-rate ADI and its adjoint -----------------------------------
+ * No reference implementation exists: the step is defined from HAL's
+ * variable-rate explicit stencil (src/Pde/PDEequations.cpp:199-230; the face
+ * between cells j and j+1 has cell j's rate) as
+ *   w = (I - Lx/2)^-1 (I + Ly/2) f,  v = (I - Ly/2)^-1 (I + Lx/2) w,
+ *   f' = f + (((v - f) + f*(-decay)) + src),
+ * equal to Diffusion2DADI plus the PDEGrid2D tick for a constant rate.  D
+ * holds one rate (D*dt/dx^2) per cell for both axes. */
+
+/* One step; w (xDim*yDim) receives the x-sweep result, out the new field. */
+void oracle_dadi_step(const double *f, const double *D, int32_t xDim, int32_t yDim, int wrapX, int wrapY,
+                      double decay, const double *src, double *w, double *out);
+
+/* `steps` steps from f0; returns loss = 1/2 |f_T - target|^2 and, when the
+ * pointers are not NULL, f_T and the gradients of the loss with respect to D
+ * (per cell), decay and src (per cell), by reverse-mode differentiation of
+ * the steps (every state kept, FP64). */
+double oracle_dadi_loss_grad(const double *f0, const double *target, const double *D, double decay,
+                             const double *src, int32_t xDim, int32_t yDim, int wrapX, int wrapY, int32_t steps,
+                             double *fT, double *gD, double *gDecay, double *gSrc);
+
 /* ---- Hal::Rng / Hal::Rand (src/Rng.cpp, src/Rand.cpp) ----------------------
  * xoshiro256** seeded through splitmix64, plus the Marsaglia polar Gaussian
  * (src/GaussianSampler.cpp:23-47).  Used to rebuild the seeded scenes of the

@@ -84,6 +84,10 @@ class Oracle(_Lib):
         L.oracle_accumulate_forces.argtypes = [vp, vp, i32, vp, f64, f64, i32, i32, ctypes.c_int,
                                                ctypes.c_int, vp, vp, ctypes.c_int]
         L.oracle_accumulate_forces.restype = ctypes.c_int
+        L.oracle_dadi_step.argtypes = [vp, vp, i32, i32, ctypes.c_int, ctypes.c_int, f64, vp, vp, vp]
+        L.oracle_dadi_loss_grad.argtypes = [vp, vp, vp, f64, vp, i32, i32, ctypes.c_int, ctypes.c_int,
+                                            i32, vp, vp, vp, vp]
+        L.oracle_dadi_loss_grad.restype = f64
         L.oracle_rand_init.argtypes = [vp, ctypes.c_uint64]
         L.oracle_rand_double.argtypes = [vp]
         L.oracle_rand_double.restype = f64
@@ -184,6 +188,39 @@ class Oracle(_Lib):
             else:
                 out[i] = L.oracle_rand_gaussian(ctypes.addressof(st), 0.0, 1.0)
         return out
+
+
+    @classmethod
+    def dadi_step(cls, field, D, xDim, yDim, wrapX=False, wrapY=False, decay=0.0, src=None):
+        """One variable-rate ADI step; returns (f', w)."""
+        f = _f64(field)
+        d = _f64(D)
+        sv = _f64(src)
+        w = np.zeros(xDim * yDim)
+        out = np.zeros(xDim * yDim)
+        cls.lib().oracle_dadi_step(f.ctypes.data, d.ctypes.data, xDim, yDim, int(wrapX), int(wrapY), decay,
+                                   None if sv is None else sv.ctypes.data, w.ctypes.data, out.ctypes.data)
+        return out, w
+
+    @classmethod
+    def dadi_loss_grad(cls, f0, target, D, decay, src, xDim, yDim, steps, wrapX=False, wrapY=False,
+                       grad=True):
+        """Loss 1/2|f_T - target|^2 of `steps` variable-rate ADI steps and, with
+        grad, its gradients: returns (loss, f_T, dD, dDecay, dSrc)."""
+        f = _f64(f0)
+        t = _f64(target)
+        d = _f64(D)
+        sv = _f64(src)
+        n = xDim * yDim
+        fT = np.zeros(n)
+        gD = np.zeros(n) if grad else None
+        gS = np.zeros(n) if grad else None
+        gK = ctypes.c_double(0.0)
+        loss = cls.lib().oracle_dadi_loss_grad(
+            f.ctypes.data, t.ctypes.data, d.ctypes.data, decay, None if sv is None else sv.ctypes.data, xDim, yDim,
+            int(wrapX), int(wrapY), steps, fT.ctypes.data, None if gD is None else gD.ctypes.data,
+            ctypes.byref(gK) if grad else None, None if gS is None else gS.ctypes.data)
+        return loss, fT, gD, (gK.value if grad else None), gS
 
 
 class Reference(_Lib):

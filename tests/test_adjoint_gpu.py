@@ -1,0 +1,156 @@
+"""Variable-rate ADI and its adjoint on the GPU (hal_cuda_adjoint_*).
+
+Parity is against the FP64 CPU oracle (oracle_dadi_*), which is itself pinned
+by its constant-rate limit (the reference-pinned ADI tick) and by finite
+differences (tests/test_adjoint_oracle.py):
+* forward: FP32 device steps against FP64, max-rel <= 2e-6 (1 + max D) per
+  step; for a constant rate it is the ADI tick of hal.Adi;
+* gradient: relative L2 error of dL/dD and dL/dsrc and relative error of
+  dL/ddecay <= 2e-3 against the FP64 adjoint;
+* checkpointing: the gradient does not depend on the checkpoint interval
+  (recomputed states are bit-identical);
+* finite differences of the device loss (FP32, h = 1e-3) agree with the
+  directional derivatives within 2% plus three times the rounding noise of
+  the difference (estimated from the differences at h and 2h).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import max_rel, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _problem(n, steps, seed, wrap=False):
+    from halcuda import workloads
+
+    rng = np.random.default_rng(seed)
+    f0 = workloads.gaussian_blobs(n, rng, 8).astype(np.float32)
+    D = workloads.rate_field(n, rng).astype(np.float32)
+    Dt = workloads.rate_field(n, rng).astype(np.float32)
+    src = (rng.random(n * n) * 0.01).astype(np.float32)
+    return f0, D, Dt, src
+
+
+def test_constant_rate_is_the_adi_tick(hal, oracle):
+    n, steps, r = 64, 6, 4.0
+    rng = np.random.default_rng(1)
+    f0 = rng.random(n * n).astype(np.float32)
+    src = (rng.random(n * n) * 0.01).astype(np.float32)
+    D = np.full(n * n, r, np.float32)
+    with hal.Adjoint(n, n) as a:
+        a.set_problem(f0, np.zeros_like(f0), steps, 4)
+        _, fT = a.forward(D, 0.01, src, want_field=True)
+    with hal.Adi(n, n) as adi:
+        adi.set_field(f0)
+        adi.set_source(src)
+        adi.run_ticks(steps, r, 0.01)
+        exp32 = adi.get_field()
+    ref = oracle.run_ticks(1, f0.astype(np.float64), n, n, r, decay=0.01, src_dense=src.astype(np.float64),
+                           ticks=steps)
+    tol = 2e-6 * (1 + r) * steps
+    assert max_rel(fT, ref) <= tol
+    assert max_rel(fT, exp32) <= 2 * tol
+
+
+@pytest.mark.parametrize("wrap", [(False, False), (True, True), (False, True)])
+def test_forward_and_gradient_match_fp64_adjoint(hal, oracle, wrap):
+    n, steps = 64, 40
+    f0, D, Dt, src = _problem(n, steps, 2)
+    decay = 0.005
+    # target: the final field of the same model with the second rate field
+    _, target, *_ = oracle.dadi_loss_grad(f0, np.zeros(n * n), Dt, decay, src, n, n, steps, *wrap, grad=False)
+    loss_ref, fT_ref, gD_ref, gK_ref, gS_ref = oracle.dadi_loss_grad(f0, target, D, decay, src, n, n, steps, *wrap)
+    with hal.Adjoint(n, n, *wrap) as a:
+        a.set_problem(f0, target.astype(np.float32), steps, 7)
+        loss_f, fT = a.forward(D, decay, src, want_field=True)
+        loss, gD, gK, gS = a.gradient(D, decay, src)
+    assert max_rel(fT, fT_ref) <= 2e-6 * (1 + 5.0) * steps
+    assert abs(loss - loss_ref) <= 1e-3 * loss_ref and abs(loss_f - loss) <= 1e-6 * loss
+    assert rel_l2(gD, gD_ref) <= 2e-3
+    assert rel_l2(gS, gS_ref) <= 2e-3
+    assert abs(gK - gK_ref) <= 2e-3 * abs(gK_ref)
+
+
+def test_gradient_independent_of_checkpoint_interval(hal):
+    n, steps = 64, 30
+    f0, D, Dt, src = _problem(n, steps, 3)
+    target = np.roll(f0, 5)
+    out = []
+    for every in (1, 7, 30, 100):
+        with hal.Adjoint(n, n) as a:
+            a.set_problem(f0, target, steps, every)
+            out.append(a.gradient(D, 0.005, src))
+    for loss, gD, gK, gS in out[1:]:
+        assert loss == out[0][0]
+        assert np.array_equal(gD, out[0][1]) and np.array_equal(gS, out[0][3])
+        assert abs(gK - out[0][2]) <= 1e-9 * abs(out[0][2])
+
+
+def test_finite_differences_on_the_device(hal):
+    """Central differences of the device loss, h = 1e-3, on a 128^2 grid."""
+    n, steps = 128, 100
+    f0, D, Dt, src = _problem(n, steps, 4)
+    rng = np.random.default_rng(9)
+    with hal.Adjoint(n, n) as a:
+        a.set_problem(f0, np.zeros_like(f0), steps, 22)
+        _, target = a.forward(Dt, 0.005, src, want_field=True)
+        a.set_problem(f0, target, steps, 22)
+        loss, gD, gK, gS = a.gradient(D, 0.005, src)
+        h = 1e-3
+
+        def fd(f):
+            return (f(h) - f(-h)) / (2 * h), (f(2 * h) - f(-2 * h)) / (4 * h)
+
+        # The device loss is FP32: a central difference at h carries rounding
+        # noise of order (loss rounding) / h.  Its size is estimated from the
+        # spread between the differences at h and 2h (the truncation error,
+        # O(h^2), is far smaller), and the check allows three times that
+        # spread on top of a 2% relative tolerance.
+        for _ in range(4):
+            v = rng.standard_normal(n * n).astype(np.float32)
+            f1, f2 = fd(lambda t: a.forward(D + np.float32(t) * v, 0.005, src))
+            dd = float(gD.astype(np.float64) @ v.astype(np.float64))
+            assert abs(f1 - dd) <= 2e-2 * abs(dd) + 3 * abs(f1 - f2), (f1, f2, dd)
+        f1, f2 = fd(lambda t: a.forward(D, 0.005 + t, src))
+        assert abs(f1 - gK) <= 2e-2 * abs(gK) + 3 * abs(f1 - f2), (f1, f2, gK)
+        f1, f2 = fd(lambda t: a.forward(D, 0.005, src + np.float32(t) * np.sign(gS)))
+        ds = float(np.abs(gS.astype(np.float64)).sum())
+        assert abs(f1 - ds) <= 2e-2 * abs(ds) + 3 * abs(f1 - f2), (f1, f2, ds)
+
+
+def test_rejects_bad_input(hal):
+    with pytest.raises(ValueError):
+        hal.Adjoint(48, 64, True, False)  # wrapped x needs a power of two
+    with pytest.raises(ValueError):
+        hal.Adjoint(hal.ADJOINT_MAX_SIDE + 1, 8)
+    with hal.Adjoint(16, 16) as a:
+        with pytest.raises(ValueError):
+            a.forward(np.ones(256, np.float32), 0.0)
+        with pytest.raises(ValueError):
+            a.set_problem(np.zeros(255, np.float32), np.zeros(255, np.float32), 3)
+
+
+def test_parameter_recovery_workload_on_a_64_copy(hal, oracle):
+    """The parameter-recovery workload's shape on a 64 x 64 copy (500 steps,
+    checkpoints every 22, rates in [0.5, 5], decay 0.005) against the FP64
+    CPU adjoint."""
+    from halcuda import workloads
+
+    w = workloads.adjoint_inputs(n=64, steps=500)
+    n = 64
+    _, target, *_ = oracle.dadi_loss_grad(w["f0"], np.zeros(n * n), w["D_true"], w["decay"], w["src"], n, n,
+                                          w["steps"], grad=False)
+    loss_ref, _, gD_ref, gK_ref, gS_ref = oracle.dadi_loss_grad(w["f0"], target, w["D"], w["decay"], w["src"], n, n,
+                                                                w["steps"])
+    with hal.Adjoint(n, n) as a:
+        a.set_problem(w["f0"], target.astype(np.float32), w["steps"], w["checkpoint_every"])
+        loss, gD, gK, gS = a.gradient(w["D"], w["decay"], w["src"])
+    # over 500 steps the FP32 forward error of f_T enters the residual
+    # f_T - target, which seeds every adjoint field: 1e-2 relative
+    assert abs(loss - loss_ref) <= 1e-3 * loss_ref
+    assert rel_l2(gD, gD_ref) <= 1e-2
+    assert rel_l2(gS, gS_ref) <= 1e-2
+    assert abs(gK - gK_ref) <= 1e-2 * abs(gK_ref)
