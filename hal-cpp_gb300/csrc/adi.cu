@@ -53,6 +53,7 @@ namespace halcuda
         constexpr int kNL = 2;               // lines solved by one thread
         constexpr int kMaxThreads = 512;
         constexpr int kMaxR = 128;           // lines per CTA (a power of two, >= 8)
+        constexpr int kGbandSmem = 2048;     // floats of G's band staged in shared memory
         // bound of the mbarrier wait (ns of %globaltimer); the staged copies
         // take microseconds, so reaching it means the copies never landed
         constexpr unsigned long long kWaitLimitNs = 2000000000ull;
@@ -126,6 +127,103 @@ namespace halcuda
                 acc = fmaf(__ldg(g + (m - j + pl.B)), xA[m] + xB[m], acc);
             }
             return acc;
+        }
+
+        // BlockSolve for all kNL lines of a thread: each coefficient vector is
+        // read from shared memory once and applied to every line, and the
+        // lines' recurrences interleave.
+        __device__ __forceinline__ void BlockSolveN(float (&z)[kNL][M], const float *cf)
+        {
+            const float4 *fw = reinterpret_cast<const float4 *>(cf + kCoefFw * M);
+            const float4 *ib = reinterpret_cast<const float4 *>(cf + kCoefIb * M);
+            const float4 *cb = reinterpret_cast<const float4 *>(cf + kCoefCb * M);
+#pragma unroll
+            for (int j = 0; j < M / 4; j++)
+            {
+                const float4 w4 = fw[j];
+#pragma unroll
+                for (int l = 0; l < kNL; l++)
+                {
+                    if (j > 0)
+                    {
+                        z[l][4 * j] = fmaf(-w4.x, z[l][4 * j - 1], z[l][4 * j]);
+                    }
+                    z[l][4 * j + 1] = fmaf(-w4.y, z[l][4 * j], z[l][4 * j + 1]);
+                    z[l][4 * j + 2] = fmaf(-w4.z, z[l][4 * j + 1], z[l][4 * j + 2]);
+                    z[l][4 * j + 3] = fmaf(-w4.w, z[l][4 * j + 2], z[l][4 * j + 3]);
+                }
+            }
+#pragma unroll
+            for (int j = M / 4 - 1; j >= 0; j--)
+            {
+                const float4 i4 = ib[j];
+                const float4 c4 = cb[j];
+#pragma unroll
+                for (int l = 0; l < kNL; l++)
+                {
+                    if (j == M / 4 - 1)
+                    {
+                        z[l][4 * j + 3] *= i4.w;
+                    }
+                    else
+                    {
+                        z[l][4 * j + 3] = fmaf(-c4.w, z[l][4 * j + 4], z[l][4 * j + 3] * i4.w);
+                    }
+                    z[l][4 * j + 2] = fmaf(-c4.z, z[l][4 * j + 3], z[l][4 * j + 2] * i4.z);
+                    z[l][4 * j + 1] = fmaf(-c4.y, z[l][4 * j + 2], z[l][4 * j + 1] * i4.y);
+                    z[l][4 * j + 0] = fmaf(-c4.x, z[l][4 * j + 1], z[l][4 * j + 0] * i4.x);
+                }
+            }
+        }
+
+        // BlockCorrect for all kNL lines, one read of p and q.
+        __device__ __forceinline__ void BlockCorrectN(float (&z)[kNL][M], const float *cf, const float (&sL)[kNL],
+                                                      const float (&sR)[kNL])
+        {
+            const float4 *pv = reinterpret_cast<const float4 *>(cf + kCoefP * M);
+            const float4 *qv = reinterpret_cast<const float4 *>(cf + kCoefQ * M);
+#pragma unroll
+            for (int j = 0; j < M / 4; j++)
+            {
+                const float4 p4 = pv[j];
+                const float4 q4 = qv[j];
+#pragma unroll
+                for (int l = 0; l < kNL; l++)
+                {
+                    z[l][4 * j + 0] = fmaf(-sL[l], p4.x, fmaf(-sR[l], q4.x, z[l][4 * j + 0]));
+                    z[l][4 * j + 1] = fmaf(-sL[l], p4.y, fmaf(-sR[l], q4.y, z[l][4 * j + 1]));
+                    z[l][4 * j + 2] = fmaf(-sL[l], p4.z, fmaf(-sR[l], q4.z, z[l][4 * j + 2]));
+                    z[l][4 * j + 3] = fmaf(-sL[l], p4.w, fmaf(-sR[l], q4.w, z[l][4 * j + 3]));
+                }
+            }
+        }
+
+        // Separators on both sides of chunk k in one pass over the exchanged
+        // values s_m = xA[m] + xB[m]: sR = row k of G, sL = row k-1 (each 0
+        // where that separator does not exist).  G is the banded inverse,
+        // rows of 2B+1 entries, in shared or global memory.
+        __device__ __forceinline__ void BandDot2(const float *G, int32_t P, int32_t B, int k, const float *xA,
+                                                 const float *xB, float &sL, float &sR)
+        {
+            const int S = P - 1;
+            const int W = 2 * B + 1;
+            sL = 0.0f;
+            sR = 0.0f;
+            const int lo = max(0, k - 1 - B);
+            const int hi = min(S - 1, k + B);
+            const bool hasR = k < S, hasL = k >= 1;
+            for (int m = lo; m <= hi; m++)
+            {
+                const float sm = xA[m] + xB[m];
+                if (hasR && m >= k - B)
+                {
+                    sR = fmaf(G[k * W + (m - k + B)], sm, sR);
+                }
+                if (hasL && m <= k - 1 + B)
+                {
+                    sL = fmaf(G[(k - 1) * W + (m - k + 1 + B)], sm, sL);
+                }
+            }
         }
 
         // z[idx] for a run-time idx without dynamic register indexing.
@@ -231,20 +329,35 @@ namespace halcuda
         template <int MODE, bool SWZ>
         __device__ __forceinline__ void SweepTile(const SweepParams &p, const CUtensorMap *tmap, const int32_t x0)
         {
-            extern __shared__ __align__(16) float smem[];
+            extern __shared__ __align__(1024) float smem[];
             __shared__ __align__(8) unsigned long long mbar;
             __shared__ int s_fail;
             __shared__ uint32_t s_tmaBytes;
             const int P = p.plan.P;
             const int R = p.R;
             // staged lines first, on a 1024-byte boundary (128-byte swizzle)
-            float *sLines = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(smem) + 1023) & ~uintptr_t(1023));
+            // the dynamic buffer is declared 1024-byte aligned (the 128-byte
+            // swizzle pattern repeats every 1024 bytes) and used directly, so
+            // every access through it is a shared-memory access
+            float *sLines = smem;
             float *sCoef = sLines + (R + 2) * p.LS;  // kCoefFloats
             float *xA = sCoef + kCoefFloats;         // R * P
             float *xB = xA + R * P;                  // R * P
+            float *sG = xB + R * P;                  // kGbandSmem: G's band when it fits
+            const int gCount = (P > 1) ? (P - 1) * (2 * p.plan.B + 1) : 0;
+            const bool gInSmem = gCount <= kGbandSmem;
+            const float *G = gInSmem ? sG : p.plan.gband;
 
             const int tid = threadIdx.x;
             const int nthreads = blockDim.x;
+            if ((SmemAddr(smem) & 1023u) != 0u)
+            {
+                if (tid == 0)
+                {
+                    atomicExch(p.err, 2);
+                }
+                return;  // uniform: the address is the same for every thread
+            }
             const int32_t L = p.L;
             const bool vecL = (L & 3) == 0;
 
@@ -275,6 +388,13 @@ namespace halcuda
                 for (int q = tid; q < kCoefFloats / 4; q += nthreads)
                 {
                     St4(sCoef + 4 * q, __ldg(reinterpret_cast<const float4 *>(p.plan.coef) + q));
+                }
+                if (gInSmem)
+                {
+                    for (int q = tid; q < gCount; q += nthreads)
+                    {
+                        sG[q] = __ldg(p.plan.gband + q);
+                    }
                 }
                 __syncthreads();  // mbarrier initialised before anyone waits on it
             }
@@ -314,6 +434,13 @@ namespace halcuda
                 for (int q = tid; q < kCoefFloats / 4; q += nthreads)
                 {
                     St4(sCoef + 4 * q, __ldg(reinterpret_cast<const float4 *>(p.plan.coef) + q));
+                }
+                if (gInSmem)
+                {
+                    for (int q = tid; q < gCount; q += nthreads)
+                    {
+                        sG[q] = __ldg(p.plan.gband + q);
+                    }
                 }
                 __syncthreads();  // mbarrier initialised, line sources known
                 if (tid == 0)
@@ -416,91 +543,86 @@ namespace halcuda
                 return;  // uniform: every thread saw the same flag after the barrier
             }
 
-            // ---- 2a. right-hand sides, in place -----------------------------
-            // (I + r/2 L_cross) on every staged CTA line: each thread walks
-            // 16-byte units of all R+2 staged lines with a three-line window
-            // in registers and overwrites line ll+1 with its right-hand side
-            // (ExplicitDiffusion*2ADI, src/Pde/ADIequations.cpp:19-47, and the
-            // implicit-axis Dirichlet term ImplicitBoundarySource,
-            // ADIequations.h:198-220).
-            {
-                const bool hasGhost = (p.ghostLo != nullptr);
-                const int nUnits = P * (M / 4);
-                for (int u = tid; u < nUnits; u += nthreads)
-                {
-                    const int kk = u >> 3;
-                    const int q = u & 7;
-                    float4 up = Ld4(sLines + SOff4<SWZ>(0, kk, q, P, p.LS));
-                    float4 c = Ld4(sLines + SOff4<SWZ>(1, kk, q, P, p.LS));
-                    for (int ll = 0; ll < R; ll++)
-                    {
-                        const int32_t line = x0 + ll;
-                        const float4 dn = Ld4(sLines + SOff4<SWZ>(ll + 2, kk, q, P, p.LS));
-                        if (line < p.Nlines)
-                        {
-                            const float wUp = (line >= 1 || p.wrapLines) ? 1.0f : (hasGhost ? 2.0f : 0.0f);
-                            const float wDn = (line + 1 < p.Nlines || p.wrapLines) ? 1.0f : (hasGhost ? 2.0f : 0.0f);
-                            float4 z4;
-                            // centre + (d(+1) + d(-1)) * r / 2, the differences first
-                            z4.x = fmaf((dn.x - c.x) * wDn + (up.x - c.x) * wUp, p.halfR, c.x);
-                            z4.y = fmaf((dn.y - c.y) * wDn + (up.y - c.y) * wUp, p.halfR, c.y);
-                            z4.z = fmaf((dn.z - c.z) * wDn + (up.z - c.z) * wUp, p.halfR, c.z);
-                            z4.w = fmaf((dn.w - c.w) * wDn + (up.w - c.w) * wUp, p.halfR, c.w);
-                            if (p.implLo != nullptr)
-                            {
-                                const int32_t pos0 = 4 * u;
-                                if (pos0 == 0)
-                                {
-                                    z4.x = fmaf(p.r, __ldg(p.implLo + line), z4.x);
-                                }
-                                const int32_t last = L - 1 - pos0;  // component of position L-1
-                                if (last >= 0 && last < 4)
-                                {
-                                    const float add = p.r * __ldg(p.implHi + line);
-                                    z4.x += (last == 0) ? add : 0.0f;
-                                    z4.y += (last == 1) ? add : 0.0f;
-                                    z4.z += (last == 2) ? add : 0.0f;
-                                    z4.w += (last == 3) ? add : 0.0f;
-                                }
-                            }
-                            St4(sLines + SOff4<SWZ>(ll + 1, kk, q, P, p.LS), z4);
-                        }
-                        up = c;
-                        c = dn;
-                    }
-                }
-            }
-            __syncthreads();
-
-            // ---- 2b. solve: thread -> (line pair g, chunk k) ---------------
+            // ---- 2. right-hand sides and solve: thread -> (line pair g, chunk k)
+            // Each line's right-hand side (I + r/2 L_cross) is formed while
+            // its chunk is loaded, from the staged lines on either side
+            // (ExplicitDiffusion*2ADI, src/Pde/ADIequations.cpp:19-47), plus
+            // the implicit-axis Dirichlet term ImplicitBoundarySource
+            // (ADIequations.h:198-220) at positions 0 and L-1.  The staged
+            // lines are only read until the exchange barrier below.
             const int g = tid / P;
             const int k = tid - g * P;
             const int type = AdiBlockType(k, P);
             const float *cf = sCoef + type * kCoefCount * M;
             const float a = p.plan.a;
+            const int ll0 = g * kNL;  // first line of the thread within the CTA
             float z[kNL][M];
             bool act[kNL];
-#pragma unroll
-            for (int j = 0; j < kNL; j++)
+            float wUp[kNL], wDn[kNL];
             {
-                const int ll = g * kNL + j;  // line within the CTA
-                act[j] = (ll < R) && (x0 + ll < p.Nlines);
+                const bool hasGhost = (p.ghostLo != nullptr);
 #pragma unroll
-                for (int q = 0; q < M / 4; q++)
+                for (int j = 0; j < kNL; j++)
                 {
-                    const float4 v = act[j] ? Ld4(sLines + SOff4<SWZ>(ll + 1, k, q, P, p.LS))
-                                            : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                    z[j][4 * q + 0] = v.x;
-                    z[j][4 * q + 1] = v.y;
-                    z[j][4 * q + 2] = v.z;
-                    z[j][4 * q + 3] = v.w;
+                    const int32_t line = x0 + ll0 + j;
+                    act[j] = (ll0 + j < R) && (line < p.Nlines);
+                    wUp[j] = (line >= 1 || p.wrapLines) ? 1.0f : (hasGhost ? 2.0f : 0.0f);
+                    wDn[j] = (line + 1 < p.Nlines || p.wrapLines) ? 1.0f : (hasGhost ? 2.0f : 0.0f);
                 }
             }
 #pragma unroll
-            for (int j = 0; j < kNL; j++)
+            for (int q = 0; q < M / 4; q++)
             {
-                BlockSolve(z[j], cf);
+                // staged rows ll0 .. ll0 + kNL + 1: line ll is staged row ll + 1
+                float4 rows[kNL + 2];
+#pragma unroll
+                for (int r = 0; r < kNL + 2; r++)
+                {
+                    rows[r] = (ll0 < R) ? Ld4(sLines + SOff4<SWZ>(ll0 + r, k, q, P, p.LS))
+                                        : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                }
+#pragma unroll
+                for (int j = 0; j < kNL; j++)
+                {
+                    const float4 up = rows[j], c = rows[j + 1], dn = rows[j + 2];
+                    // centre + (d(+1) + d(-1)) * r / 2, the differences first
+                    const float4 v = make_float4(fmaf((dn.x - c.x) * wDn[j] + (up.x - c.x) * wUp[j], p.halfR, c.x),
+                                                 fmaf((dn.y - c.y) * wDn[j] + (up.y - c.y) * wUp[j], p.halfR, c.y),
+                                                 fmaf((dn.z - c.z) * wDn[j] + (up.z - c.z) * wUp[j], p.halfR, c.z),
+                                                 fmaf((dn.w - c.w) * wDn[j] + (up.w - c.w) * wUp[j], p.halfR, c.w));
+                    z[j][4 * q + 0] = act[j] ? v.x : 0.0f;
+                    z[j][4 * q + 1] = act[j] ? v.y : 0.0f;
+                    z[j][4 * q + 2] = act[j] ? v.z : 0.0f;
+                    z[j][4 * q + 3] = act[j] ? v.w : 0.0f;
+                }
             }
+            if (p.implLo != nullptr)
+            {
+                const int lastIdx = (L - 1) - k * M;  // position L-1 within this chunk, if here
+#pragma unroll
+                for (int j = 0; j < kNL; j++)
+                {
+                    if (!act[j])
+                    {
+                        continue;
+                    }
+                    const int32_t line = x0 + ll0 + j;
+                    if (k == 0)
+                    {
+                        z[j][0] = fmaf(p.r, __ldg(p.implLo + line), z[j][0]);
+                    }
+                    if (lastIdx >= 0 && lastIdx < M)
+                    {
+                        const float add = p.r * __ldg(p.implHi + line);
+#pragma unroll
+                        for (int e = 0; e < M; e++)
+                        {
+                            z[j][e] += (e == lastIdx) ? add : 0.0f;
+                        }
+                    }
+                }
+            }
+            BlockSolveN(z, cf);
 #pragma unroll
             for (int j = 0; j < kNL; j++)
             {
@@ -519,6 +641,19 @@ namespace halcuda
                 }
             }
             __syncthreads();
+            float sLs[kNL], sRs[kNL];
+#pragma unroll
+            for (int j = 0; j < kNL; j++)
+            {
+                const int ll = g * kNL + j;
+                sLs[j] = 0.0f;
+                sRs[j] = 0.0f;
+                if (act[j] && P > 1)
+                {
+                    BandDot2(G, P, p.plan.B, k, xA + ll * P, xB + ll * P, sLs[j], sRs[j]);
+                }
+            }
+            BlockCorrectN(z, cf, sLs, sRs);
 #pragma unroll
             for (int j = 0; j < kNL; j++)
             {
@@ -527,24 +662,9 @@ namespace halcuda
                     continue;
                 }
                 const int ll = g * kNL + j;
-                const float *rA = xA + ll * P;
-                const float *rB = xB + ll * P;
-                float sL = 0.0f, sR = 0.0f;
-                if (P > 1)
-                {
-                    if (k < P - 1)
-                    {
-                        sR = BandDot(p.plan, k, rA, rB);
-                    }
-                    if (k >= 1)
-                    {
-                        sL = BandDot(p.plan, k - 1, rA, rB);
-                    }
-                }
-                BlockCorrect(z[j], cf, sL, sR);
                 if (k < P - 1)
                 {
-                    z[j][M - 1] = sR;
+                    z[j][M - 1] = sRs[j];
                 }
                 // every staged-line read finished before the barrier above,
                 // so the line's buffer can take the solution
@@ -946,7 +1066,7 @@ namespace halcuda
             s.R = R;
             s.threads = ((R / kNL) * P + 31) & ~31;
             s.LS = swz ? P * M : P * kChunkStride + 4;  // padded: lines 4 mod 32 banks apart
-            s.smem = 1024 + sizeof(float) * (static_cast<size_t>(kCoefFloats) + static_cast<size_t>(R + 2) * s.LS +
+            s.smem = 1024 + sizeof(float) * (static_cast<size_t>(kCoefFloats) + kGbandSmem + static_cast<size_t>(R + 2) * s.LS +
                                              2 * static_cast<size_t>(R) * P + 2 * static_cast<size_t>(R));
             return s;
         }
@@ -1032,7 +1152,7 @@ namespace halcuda
         }
         sh.R = R;
         sh.LS = P * kChunkStride + 4;
-        sh.smem = 1024 + sizeof(float) * (static_cast<size_t>(kCoefFloats) + static_cast<size_t>(R + 2) * sh.LS +
+        sh.smem = 1024 + sizeof(float) * (static_cast<size_t>(kCoefFloats) + kGbandSmem + static_cast<size_t>(R + 2) * sh.LS +
                                           2 * static_cast<size_t>(R) * P + 2 * static_cast<size_t>(R));
         return sh;
     }
@@ -1251,7 +1371,9 @@ namespace halcuda
             if (h != 0)
             {
                 cudaMemsetAsync(err.p, 0, sizeof(int32_t), stream.Get());
-                SetError("%s: a staged copy did not complete within its wait limit", who);
+                SetError(h == 2 ? "%s: the sweep's shared-memory buffer was not 1024-byte aligned"
+                                : "%s: a staged copy did not complete within its wait limit",
+                         who);
                 return HAL_CUDA_ETIMEOUT;
             }
             return HAL_CUDA_OK;

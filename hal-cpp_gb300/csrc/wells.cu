@@ -485,7 +485,9 @@ namespace halcuda
             if (h != 0)
             {
                 cudaMemsetAsync(err.p, 0, sizeof(int32_t), stream.Get());
-                SetError("%s: a staged copy did not complete within its wait limit", who);
+                SetError(h == 2 ? "%s: the sweep's shared-memory buffer was not 1024-byte aligned"
+                                : "%s: a staged copy did not complete within its wait limit",
+                         who);
                 return HAL_CUDA_ETIMEOUT;
             }
             return HAL_CUDA_OK;
