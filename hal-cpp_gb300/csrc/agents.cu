@@ -25,6 +25,7 @@
 #include "agents_wells.h"
 
 #include <cmath>
+#include <type_traits>
 
 namespace halcuda
 {
@@ -177,7 +178,9 @@ namespace halcuda
         }
 
         // Pass 3: tile-local exclusive scan plus the tile prefix -> offsets.
-        __global__ void __launch_bounds__(kScanThreads) ScanApply(const int32_t *__restrict__ counts, int64_t C,
+        // Also clears the counts it has read, so the next binning starts from
+        // zero without a separate memset.
+        __global__ void __launch_bounds__(kScanThreads) ScanApply(int32_t *__restrict__ counts, int64_t C,
                                                                   const int32_t *__restrict__ tilePrefix,
                                                                   int32_t *__restrict__ offsets, int32_t n)
         {
@@ -188,6 +191,10 @@ namespace halcuda
             for (int q = 0; q < kScanItems; q++)
             {
                 v[q] = (base + q < C) ? counts[base + q] : 0;
+                if (base + q < C)
+                {
+                    counts[base + q] = 0;
+                }
                 s += v[q];
             }
             int32_t excl;
@@ -318,22 +325,24 @@ namespace halcuda
                     retX %= xDim;
                     retX = (retX < 0) ? retX + xDim : retX;
                 }
-                for (int32_t ySq = yStart; ySq < yEnd; ySq++)
+                // The cells (retX, ySq) for consecutive ySq are consecutive
+                // cell indices, and their agents consecutive bucket slots, so
+                // the row is walked as runs of cells that do not wrap: two
+                // offset loads per run, the same visiting order as cell by
+                // cell (the CPU's order).
+                for (int32_t ySq = yStart; ySq < yEnd;)
                 {
                     int32_t retY = ySq;
-                    const bool inY = (retY >= 0) && (retY < yDim);
-                    if (!inY)
+                    if (retY < 0 || retY >= yDim)
                     {
-                        if (!wrapY)
-                        {
-                            continue;
-                        }
-                        retY %= yDim;
+                        retY %= yDim;  // only reached on a wrapped axis (clamped otherwise)
                         retY = (retY < 0) ? retY + yDim : retY;
                     }
+                    const int32_t run = min(yEnd - ySq, yDim - retY);
+                    ySq += run;
                     const int32_t cell = retX * yDim + retY;
                     const int32_t s = __ldg(offsets + cell);
-                    const int32_t e = __ldg(offsets + cell + 1);
+                    const int32_t e = __ldg(offsets + cell + run);
                     for (int32_t q = s; q < e; q++)
                     {
                         if (q == slot)
@@ -343,13 +352,31 @@ namespace halcuda
                         const V2<T> pj = sPos[q];
                         const T xComp = Disp(px, pj.x, xDimF, wrapX != 0);
                         const T yComp = Disp(py, pj.y, yDimF, wrapY != 0);
-                        const T dist = Sqrt(Add(Mul(xComp, xComp), Mul(yComp, yComp)));
-                        if ((dist < R) && (dist > T(0)))
+                        if constexpr (std::is_same<T, double>::value)
                         {
-                            const T touchDist = Sub(Add(rad, sRad[q]), dist);
-                            const T force = Mul(k, touchDist);
-                            vx = Sub(vx, Mul(Div(xComp, dist), force));
-                            vy = Sub(vy, Mul(Div(yComp, dist), force));
+                            // IEEE operations in the CPU's order: bit-exact
+                            const T dist = Sqrt(Add(Mul(xComp, xComp), Mul(yComp, yComp)));
+                            if ((dist < R) && (dist > T(0)))
+                            {
+                                const T touchDist = Sub(Add(rad, sRad[q]), dist);
+                                const T force = Mul(k, touchDist);
+                                vx = Sub(vx, Mul(Div(xComp, dist), force));
+                                vy = Sub(vy, Mul(Div(yComp, dist), force));
+                            }
+                        }
+                        else
+                        {
+                            // FP32 path: 1/d from rsqrt (d^2 = 0 gives NaN,
+                            // which fails both tests like the CPU's d > 0)
+                            const T d2 = fmaf(xComp, xComp, yComp * yComp);
+                            const T inv = rsqrtf(d2);
+                            const T dist = d2 * inv;
+                            if ((dist < R) && (dist > T(0)))
+                            {
+                                const T scale = inv * (k * ((rad + sRad[q]) - dist));
+                                vx -= xComp * scale;
+                                vy -= yComp * scale;
+                            }
                         }
                     }
                 }
@@ -431,6 +458,7 @@ namespace halcuda
         DevBuf<double> sRad64;
         DevBuf<int32_t> cellOf, arrival, counts, offsets, tileSums, bucketTmp, bucket;
         int32_t nTiles = 0;
+        bool countsDirty = true;  // counts not known to be zero (cleared by each scan)
 
         int Init(int32_t x, int32_t y, int32_t maxN)
         {
@@ -473,8 +501,13 @@ namespace halcuda
         template <typename TP, typename TR>
         int Bin(const TP *pos, const TR *rad, TR *sRad, cudaStream_t s, cudaEvent_t *ev = nullptr)
         {
-            HAL_TRY(CudaStatus(cudaMemsetAsync(counts.p, 0, static_cast<size_t>(C) * sizeof(int32_t), s),
-                               "cudaMemsetAsync(counts)"));
+            if (countsDirty)
+            {
+                // a previous binning stopped before its scan cleared the counts
+                HAL_TRY(CudaStatus(cudaMemsetAsync(counts.p, 0, static_cast<size_t>(C) * sizeof(int32_t), s),
+                                   "cudaMemsetAsync(counts)"));
+            }
+            countsDirty = true;
             const int T = 256;
             unsigned ablocks = static_cast<unsigned>((n + T - 1) / T);
             if (n > 0)
@@ -491,6 +524,7 @@ namespace halcuda
             ScanTiles<<<1, kScanThreads, 0, s>>>(tileSums.p, nTiles);
             ScanApply<<<nTiles, kScanThreads, 0, s>>>(counts.p, C, tileSums.p, offsets.p, n);
             CountLaunch(3);
+            countsDirty = (cudaPeekAtLastError() != cudaSuccess);
             if (ev)
             {
                 cudaEventRecord(ev[1], s);
