@@ -378,6 +378,15 @@ def secondary_adjoint(hal, directions=None):
             fwd.append(t[0])
             grad.append(t[1])
         ms_fwd, ms_grad = min(fwd), min(grad)
+        # the same gradient with every state kept (no recomputation)
+        a.set_problem(w["f0"], target, steps, 0)
+        keep = []
+        for _ in range(3):
+            _, gD0, _, _ = a.gradient(w["D"], w["decay"], w["src"])
+            keep.append(a.times()[1])
+        ms_keep = min(keep)
+        keep_equal = bool(np.array_equal(gD0, gD))
+        a.set_problem(w["f0"], target, steps, w["checkpoint_every"])
         g64 = gD.astype(np.float64)
         errs, ok = [], 0
         for _ in range(dirs):
@@ -391,6 +400,9 @@ def secondary_adjoint(hal, directions=None):
     return {"workload": "adjoint-512x512-500steps-ckpt22-D0.5..5-decay0.005",
             "value": ms_grad / ms_fwd, "unit": "t(gradient)/t(forward)", "higher_is_better": False,
             "ms_forward": ms_fwd, "ms_gradient": ms_grad, "loss": loss,
+            "keep_all_states": {"ms_gradient": ms_keep, "ratio": ms_keep / ms_fwd,
+                                "gradient_bit_identical": keep_equal,
+                                "note": "checkpoint interval 0: every state kept (1.5 GB), nothing recomputed"},
             "fd": {"directions": dirs, "h": h, "median_rel_err": float(np.median(errs)),
                    "max_rel_err": float(np.max(errs)),
                    "within_2pct_plus_noise": int(ok)},

@@ -492,6 +492,7 @@ namespace halcuda
         Grid g{};
         int64_t n = 0;
         int32_t steps = 0, every = 1;
+        bool keepAll = false;               // checkpoint interval 0: every state kept, nothing recomputed
         bool hasProblem = false;
         DevBuf<float> f0, target, D, src;
         DevBuf<float> ckpt;                 // checkpoints: one field every `every` steps
@@ -652,29 +653,26 @@ namespace halcuda
             HAL_TRY(CudaStatus(cudaEventCreate(&e1), "cudaEventCreate"));
             cudaEventRecord(e0, s);
             int rc = HAL_CUDA_OK;
-            const float *fT = Forward(srcp, negDecay, ckpt.p, s, rc);
             float *gCur = gA.p, *gNext = gB.p;  // gCur: adjoint of the latest output handled
-            if (rc == HAL_CUDA_OK)
-            {
-                rc = LaunchLoss(fT, gCur, s);
-            }
             const int tx = Threads(g.xDim), ty = Threads(g.yDim);
             const size_t smx = LineSmemFloats(tx) * sizeof(float), smy = LineSmemFloats(ty) * sizeof(float);
             bool first = true;
-            for (int32_t seg = Segments() - 1; seg >= 0 && rc == HAL_CUDA_OK; seg--)
-            {
-                const int32_t t0 = seg * every;
-                const int32_t t1 = std::min(steps, t0 + every);
-                // recompute the segment's states f_t0..f_t1, w and v
-                rc = CudaStatus(cudaMemcpyAsync(segF.p, ckpt.p + static_cast<size_t>(seg) * n, bytes,
-                                                cudaMemcpyDeviceToDevice, s), "cudaMemcpy(segment)");
-                for (int32_t t = t0; t < t1 && rc == HAL_CUDA_OK; t++)
+            // states f_t0..f_t1, w and v of one segment, from the field at t0
+            auto recompute = [&](const float *from, int32_t t0, int32_t t1) {
+                int r = CudaStatus(cudaMemcpyAsync(segF.p, from, bytes, cudaMemcpyDeviceToDevice, s),
+                                   "cudaMemcpy(segment)");
+                for (int32_t t = t0; t < t1 && r == HAL_CUDA_OK; t++)
                 {
                     const size_t k = static_cast<size_t>(t - t0);
-                    rc = LaunchFwd(segF.p + k * n, segF.p + (k + 1) * n, segW.p + k * n, segV.p + k * n, srcp,
-                                   negDecay, s);
+                    r = LaunchFwd(segF.p + k * n, segF.p + (k + 1) * n, segW.p + k * n, segV.p + k * n, srcp,
+                                  negDecay, s);
                 }
-                for (int32_t t = t1 - 1; t >= t0 && rc == HAL_CUDA_OK; t--)
+                return r;
+            };
+            // reverse steps t1-1 .. t0 over the segment's states
+            auto backward = [&](int32_t t0, int32_t t1) {
+                int r = HAL_CUDA_OK;
+                for (int32_t t = t1 - 1; t >= t0 && r == HAL_CUDA_OK; t--)
                 {
                     const size_t k = static_cast<size_t>(t - t0);
                     const float *fNext = segF.p + (k + 1) * n;
@@ -683,9 +681,41 @@ namespace halcuda
                                                  dD.p, dS.p, acc.p + 1);
                     BwdX<<<g.yDim, tx, smx, s>>>(g, D.p, b2.p, segW.p + k * n, b1.p, dD.p);
                     CountLaunch(2);
-                    rc = LaunchStatus("adjoint backward step");
+                    r = LaunchStatus("adjoint backward step");
                     std::swap(gCur, gNext);
                     first = false;
+                }
+                return r;
+            };
+            if (keepAll)
+            {
+                // every state of the run is kept: one forward pass, no recomputation
+                rc = recompute(f0.p, 0, steps);
+                if (rc == HAL_CUDA_OK)
+                {
+                    rc = LaunchLoss(segF.p + static_cast<size_t>(steps) * n, gCur, s);
+                }
+                if (rc == HAL_CUDA_OK)
+                {
+                    rc = backward(0, steps);
+                }
+            }
+            else
+            {
+                const float *fT = Forward(srcp, negDecay, ckpt.p, s, rc);
+                if (rc == HAL_CUDA_OK)
+                {
+                    rc = LaunchLoss(fT, gCur, s);
+                }
+                for (int32_t seg = Segments() - 1; seg >= 0 && rc == HAL_CUDA_OK; seg--)
+                {
+                    const int32_t t0 = seg * every;
+                    const int32_t t1 = std::min(steps, t0 + every);
+                    rc = recompute(ckpt.p + static_cast<size_t>(seg) * n, t0, t1);
+                    if (rc == HAL_CUDA_OK)
+                    {
+                        rc = backward(t0, t1);
+                    }
                 }
             }
             if (rc == HAL_CUDA_OK && steps > 0)
@@ -790,12 +820,13 @@ extern "C" int hal_cuda_adjoint_set_problem(hal_cuda_adjoint *h, const float *f0
     HAL_REQUIRE(len == h->n, "hal_cuda_adjoint_set_problem: length %lld, grid holds %lld cells",
                 static_cast<long long>(len), static_cast<long long>(h->n));
     HAL_REQUIRE(steps >= 0, "hal_cuda_adjoint_set_problem: negative step count");
-    HAL_REQUIRE(checkpointEvery >= 1, "hal_cuda_adjoint_set_problem: checkpoint interval must be >= 1");
+    HAL_REQUIRE(checkpointEvery >= 0, "hal_cuda_adjoint_set_problem: negative checkpoint interval");
     using namespace halcuda;
     HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
     const size_t m = static_cast<size_t>(h->n);
     h->steps = steps;
-    h->every = std::min(checkpointEvery, std::max(steps, 1));
+    h->keepAll = (checkpointEvery == 0);
+    h->every = h->keepAll ? std::max(steps, 1) : std::min(checkpointEvery, std::max(steps, 1));
     HAL_TRY(h->ckpt.Alloc(m * static_cast<size_t>(std::max(h->Segments(), 1)), "cudaMalloc(checkpoints)"));
     HAL_TRY(h->segF.Alloc(m * static_cast<size_t>(h->every + 1), "cudaMalloc(segment)"));
     HAL_TRY(h->segW.Alloc(m * static_cast<size_t>(h->every), "cudaMalloc(segment)"));

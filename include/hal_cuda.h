@@ -340,8 +340,10 @@ int hal_cuda_adjoint_create(int32_t xDim, int32_t yDim, int32_t wrapX, int32_t w
 int hal_cuda_adjoint_destroy(hal_cuda_adjoint *h);
 
 /* Initial field f0 and target final field (len = xDim*yDim floats each), the
- * number of steps, and the checkpoint interval (a field is kept every
- * checkpointEvery steps; the states in between are recomputed). */
+ * number of steps, and the checkpoint interval: a field is kept every
+ * checkpointEvery steps and the states in between are recomputed during the
+ * gradient; 0 keeps every state of the run (3 fields per step of device
+ * memory) and recomputes nothing. */
 int hal_cuda_adjoint_set_problem(hal_cuda_adjoint *h, const float *f0, const float *target,
                                  int64_t len, int32_t steps, int32_t checkpointEvery);
 
