@@ -26,7 +26,7 @@ namespace halcuda
 
     // Geometry of the tick's CTAs: 32 lanes x kTickWarps warps; a lane owns
     // VEC consecutive cells of kTickRowsPerThread consecutive rows.
-    constexpr int kTickRowsPerThread = 4;
+    constexpr int kTickRowsPerThread = 3;
     constexpr int kTickWarps = 8;
 
     // Batched ticks: tile b = (grid index, CTA column, CTA row) of the
