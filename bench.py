@@ -19,7 +19,9 @@ cell-updates per second over all GPUs.
                 measured HBM copy bandwidth.
 * cpu_baseline -- the CPU oracle (a C restatement of the reference's FP64 CPU
                 backend, 1 thread as the reference ships) on a bounded sample.
-* secondary  -- the explicit 2048^2 tick and the 1M-agent force pass.
+* secondary  -- the explicit 2048^2 tick, the 1M-agent force pass, 512
+                batched wells, the adjoint gradient, and the FP64 per-cell
+                rate diffusion / advection stencils.
 
 --impl reference times the CPU oracle alone (all host threads) on the same
 workload, one bounded sample per step.
@@ -354,6 +356,68 @@ def secondary_wells(hal, torch, stream, ticks=20, plain_ticks=3):
                          "unit": "GB/s", "frac": ach / peak, "traffic": None}}
 
 
+def secondary_stencil64(hal, torch, stream, iters=20):
+    """The FP64 per-cell rate diffusion and upwind advection stencils
+    (Internal::Diffusion2 / Advection2) on a 2048^2 grid with per-cell rates
+    and velocities, called through the C ABI with pinned host arrays (copies
+    inside the timed call), beside the kernel launch time and the CPU oracle
+    on the same grid."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    pyoracle.build(ref=False)
+    rng = np.random.default_rng(12)
+
+    def pinned(a):
+        t = torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).pin_memory()
+        return t, t.numpy()
+
+    keep = []
+    arrays = {}
+    for name, a in (("f", rng.random(CELLS)), ("d", np.zeros(CELLS)), ("rx", rng.random(CELLS) * 0.24),
+                    ("ry", rng.random(CELLS) * 0.24), ("vx", rng.random(CELLS) - 0.5),
+                    ("vy", rng.random(CELLS) - 0.5)):
+        t, v = pinned(a)
+        keep.append(t)
+        arrays[name] = v
+    f, d, rx, ry, vx, vy = (arrays[k] for k in ("f", "d", "rx", "ry", "vx", "vy"))
+    # algorithmic bytes per cell: field read, deltas read+write, per-cell arrays read
+    forms = {"diffuse_var": (hal.STENCIL_DIFFUSE_VAR, 40, lambda h: h.diffuse_var(f, d, rx, ry, 0, 0)),
+             "advect": (hal.STENCIL_ADVECT, 24, lambda h: h.advect(f, d, 0.2, -0.1, 0, 0)),
+             "advect_var": (hal.STENCIL_ADVECT_VAR, 40, lambda h: h.advect_var(f, d, vx, vy, 0, 0))}
+    cpu_fn = {"diffuse_var": lambda: pyoracle.Oracle.diffuse_var(f, d, rx, ry, N, N, 0, 0),
+              "advect": lambda: pyoracle.Oracle.advect(f, d, 0.2, -0.1, N, N, 0, 0),
+              "advect_var": lambda: pyoracle.Oracle.advect_var(f, d, vx, vy, N, N, 0, 0)}
+    peak, _ = peaks()
+    out = {}
+    with hal.Diffusion(N, N) as h:
+        h.set_stream(stream.cuda_stream)
+        for name, (kind, bpc, call) in forms.items():
+            d[:] = 0.0
+            call(h)
+            call(h)
+            walls = []
+            for _ in range(iters // 4 or 1):
+                d[:] = 0.0
+                t0 = time.perf_counter()
+                call(h)
+                walls.append(time.perf_counter() - t0)
+            e2e_ms = statistics.median(walls) * 1e3
+            ms = h.stencil64_profile(kind, iters, 0.2, -0.1, 0, 0)
+            t0 = time.perf_counter()
+            cpu_fn[name]()
+            cpu_ms = (time.perf_counter() - t0) * 1e3
+            ach = bpc * CELLS / (ms * 1e-3) / 1e9
+            out[name] = {"kernel_ms": ms, "e2e_ms": e2e_ms, "cpu_oracle_ms": cpu_ms,
+                         "e2e_value": CELLS / (e2e_ms * 1e-3), "unit": "cell-updates/s",
+                         "bytes_per_cell": bpc,
+                         "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                                      "frac": ach / peak}}
+    return {"workload": "fp64-stencils-2048x2048-zeroflux-per-cell-rates-and-velocities", "forms": out,
+            "note": "FP64, bit-identical to the reference; e2e = one C-ABI call on pinned host arrays "
+                    "(wall clock, copies in and out); cpu = the oracle, 1 thread"}
+
+
 def secondary_adjoint(hal, directions=None):
     """Parameter recovery on 512^2: the gradient of the field misfit after 500
     variable-rate ADI steps (checkpoints every 22) with respect to D(x), decay
@@ -527,7 +591,8 @@ def main():
         secondary = {"explicit": secondary_explicit(hal, torch, stream),
                      "agents": secondary_agents(hal, stream),
                      "wells": secondary_wells(hal, torch, stream),
-                     "adjoint": secondary_adjoint(hal)}
+                     "adjoint": secondary_adjoint(hal),
+                     "stencil64": secondary_stencil64(hal, torch, stream)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -13,6 +13,7 @@
 #include "tick_params.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -349,6 +350,141 @@ namespace halcuda
             s = __dadd_rn(s, DeltaTerm64(f, c, y - 1, yDim, wrapY, rowBase, 1, gy, x));
             deltas[i] = __dadd_rn(deltas[i], __dmul_rn(s, r));
         }
+
+        // DisplacedX2D / DisplacedY2D (src/Pde/PDEequations.cpp:163-197): a
+        // per-cell value at neighbour n of a line (wrapped, or 0 off-grid).
+        __device__ __forceinline__ double Displaced64(const double *v, int32_t n, int32_t dim, bool wrap,
+                                                      int64_t base, int64_t stride)
+        {
+            if (n >= 0 && n < dim)
+            {
+                return v[base + n * stride];
+            }
+            if (wrap)
+            {
+                int32_t w = (n < 0) ? n + dim : n - dim;
+                return v[base + w * stride];
+            }
+            return 0.0;
+        }
+
+        // Internal::Diffusion2 with per-cell rates (src/Pde/PDEequations.cpp:
+        // 199-230), IEEE operations in the reference's order.
+        __global__ void DiffuseVar64Kernel(const double *__restrict__ f, double *__restrict__ deltas,
+                                           const double *__restrict__ rx, const double *__restrict__ ry,
+                                           int32_t xDim, int32_t yDim, int32_t wrapX, int32_t wrapY)
+        {
+            int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+            if (i >= static_cast<int64_t>(xDim) * yDim)
+            {
+                return;
+            }
+            int32_t x = static_cast<int32_t>(i / yDim);
+            int32_t y = static_cast<int32_t>(i - static_cast<int64_t>(x) * yDim);
+            const double c = f[i];
+            const int64_t colBase = y, rowBase = static_cast<int64_t>(x) * yDim;
+            const double dp1x = ((x == xDim - 1) && !wrapX) ? Displaced64(rx, x + 1, xDim, wrapX, colBase, yDim) : rx[i];
+            const double dm1x = Displaced64(rx, x - 1, xDim, wrapX, colBase, yDim);
+            const double dp1y = ((y == yDim - 1) && !wrapY) ? Displaced64(ry, y + 1, yDim, wrapY, rowBase, 1) : ry[i];
+            const double dm1y = Displaced64(ry, y - 1, yDim, wrapY, rowBase, 1);
+            double s = __dmul_rn(DeltaTerm64(f, c, x + 1, xDim, wrapX, colBase, yDim, nullptr, 0), dp1x);
+            s = __dadd_rn(s, __dmul_rn(DeltaTerm64(f, c, x - 1, xDim, wrapX, colBase, yDim, nullptr, 0), dm1x));
+            s = __dadd_rn(s, __dmul_rn(DeltaTerm64(f, c, y + 1, yDim, wrapY, rowBase, 1, nullptr, 0), dp1y));
+            s = __dadd_rn(s, __dmul_rn(DeltaTerm64(f, c, y - 1, yDim, wrapY, rowBase, 1, nullptr, 0), dm1y));
+            deltas[i] = __dadd_rn(deltas[i], s);
+        }
+
+        // Internal::Advection2, uniform velocity (src/Pde/PDEequations.cpp:
+        // 380-412): first-order upwind, each term added to deltas in turn.
+        __global__ void Advect64Kernel(const double *__restrict__ f, double *__restrict__ deltas, double xVel,
+                                       double yVel, int32_t xDim, int32_t yDim, int32_t wrapX, int32_t wrapY)
+        {
+            int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+            if (i >= static_cast<int64_t>(xDim) * yDim)
+            {
+                return;
+            }
+            int32_t x = static_cast<int32_t>(i / yDim);
+            int32_t y = static_cast<int32_t>(i - static_cast<int64_t>(x) * yDim);
+            const double c = f[i];
+            const int64_t colBase = y, rowBase = static_cast<int64_t>(x) * yDim;
+            double d = deltas[i];
+            if (xVel > 0)
+            {
+                d = __dadd_rn(d, __dmul_rn(DeltaTerm64(f, c, x - 1, xDim, wrapX, colBase, yDim, nullptr, 0), xVel));
+            }
+            else if (xVel < 0)
+            {
+                d = __dsub_rn(d, __dmul_rn(DeltaTerm64(f, c, x + 1, xDim, wrapX, colBase, yDim, nullptr, 0), xVel));
+            }
+            if (yVel > 0)
+            {
+                d = __dadd_rn(d, __dmul_rn(DeltaTerm64(f, c, y - 1, yDim, wrapY, rowBase, 1, nullptr, 0), yVel));
+            }
+            else if (yVel < 0)
+            {
+                d = __dsub_rn(d, __dmul_rn(DeltaTerm64(f, c, y + 1, yDim, wrapY, rowBase, 1, nullptr, 0), yVel));
+            }
+            deltas[i] = d;
+        }
+
+        // Internal::Advection2, per-cell velocity (src/Pde/PDEequations.cpp:
+        // 535-575): upwind face fluxes, -xFluxP + xFluxM - yFluxP + yFluxM.
+        __global__ void AdvectVar64Kernel(const double *__restrict__ f, double *__restrict__ deltas,
+                                          const double *__restrict__ vx, const double *__restrict__ vy, int32_t xDim,
+                                          int32_t yDim, int32_t wrapX, int32_t wrapY)
+        {
+            int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+            if (i >= static_cast<int64_t>(xDim) * yDim)
+            {
+                return;
+            }
+            int32_t x = static_cast<int32_t>(i / yDim);
+            int32_t y = static_cast<int32_t>(i - static_cast<int64_t>(x) * yDim);
+            const int64_t colBase = y, rowBase = static_cast<int64_t>(x) * yDim;
+            const double xVelP = ((x == xDim - 1) && !wrapX) ? Displaced64(vx, x + 1, xDim, wrapX, colBase, yDim) : vx[i];
+            const double yVelP = ((y == yDim - 1) && !wrapY) ? Displaced64(vy, y + 1, yDim, wrapY, rowBase, 1) : vy[i];
+            const double xVelM = Displaced64(vx, x - 1, xDim, wrapX, colBase, yDim);
+            const double yVelM = Displaced64(vy, y - 1, yDim, wrapY, rowBase, 1);
+            const double c = f[i];
+            double xFluxP = 0.0, xFluxM = 0.0, yFluxP = 0.0, yFluxM = 0.0;
+            if (xVelP > 0)
+            {
+                xFluxP = __dmul_rn(xVelP, c);
+            }
+            else if (xVelP < 0)
+            {
+                xFluxP = __dmul_rn(xVelP, Displaced64(f, x + 1, xDim, wrapX, colBase, yDim));
+            }
+            if (xVelM > 0)
+            {
+                xFluxM = __dmul_rn(xVelM, Displaced64(f, x - 1, xDim, wrapX, colBase, yDim));
+            }
+            else if (xVelM < 0)
+            {
+                xFluxM = __dmul_rn(xVelM, c);
+            }
+            if (yVelP > 0)
+            {
+                yFluxP = __dmul_rn(yVelP, c);
+            }
+            else if (yVelP < 0)
+            {
+                yFluxP = __dmul_rn(yVelP, Displaced64(f, y + 1, yDim, wrapY, rowBase, 1));
+            }
+            if (yVelM > 0)
+            {
+                yFluxM = __dmul_rn(yVelM, Displaced64(f, y - 1, yDim, wrapY, rowBase, 1));
+            }
+            else if (yVelM < 0)
+            {
+                yFluxM = __dmul_rn(yVelM, c);
+            }
+            double t = __dadd_rn(-xFluxP, xFluxM);
+            t = __dsub_rn(t, yFluxP);
+            t = __dadd_rn(t, yFluxM);
+            deltas[i] = __dadd_rn(deltas[i], t);
+        }
     }
 
     int LaunchTickTiles(const TickParams *table, const int4 *tiles, int32_t nTiles, int vec, cudaStream_t s)
@@ -385,6 +521,7 @@ namespace halcuda
         DevBuf<float> ptVal;
         bool hasPoints = false;
         DevBuf<double> f64, d64, g64;
+        DevBuf<double> a64, b64;  // per-cell rates or velocities of the FP64 stencil calls
         GraphCache graph[2];  // by the parity of the starting buffer
         dim3 grid, block;
 
@@ -567,6 +704,142 @@ namespace
                            "cudaMemcpy(deltas)"));
         return CudaStatus(cudaStreamSynchronize(s), who);
     }
+}
+
+namespace
+{
+    enum Stencil64 : int
+    {
+        kVarDiffusion = HAL_CUDA_STENCIL_DIFFUSE_VAR,
+        kAdvection = HAL_CUDA_STENCIL_ADVECT,
+        kVarAdvection = HAL_CUDA_STENCIL_ADVECT_VAR
+    };
+
+    void LaunchStencil64(hal_cuda_diffusion *h, int kind, double xVel, double yVel, int32_t wrapX, int32_t wrapY,
+                         cudaStream_t s)
+    {
+        using namespace halcuda;
+        const size_t n = h->Length();
+        const unsigned blocks = static_cast<unsigned>((n + 255) / 256);
+        if (kind == kVarDiffusion)
+        {
+            DiffuseVar64Kernel<<<blocks, 256, 0, s>>>(h->f64.p, h->d64.p, h->a64.p, h->b64.p, h->xDim, h->yDim, wrapX,
+                                                      wrapY);
+        }
+        else if (kind == kAdvection)
+        {
+            Advect64Kernel<<<blocks, 256, 0, s>>>(h->f64.p, h->d64.p, xVel, yVel, h->xDim, h->yDim, wrapX, wrapY);
+        }
+        else
+        {
+            AdvectVar64Kernel<<<blocks, 256, 0, s>>>(h->f64.p, h->d64.p, h->a64.p, h->b64.p, h->xDim, h->yDim, wrapX,
+                                                     wrapY);
+        }
+    }
+
+    // Upload field, deltas and (for the per-cell forms) two per-cell arrays,
+    // run one FP64 stencil, download deltas.
+    int Stencil64Common(hal_cuda_diffusion *h, int kind, const double *field, double *deltas, const double *a,
+                        const double *b, double xVel, double yVel, int32_t wrapX, int32_t wrapY, const char *who)
+    {
+        using namespace halcuda;
+        HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+        const size_t n = h->Length();
+        if (h->f64.p == nullptr)
+        {
+            HAL_TRY(h->f64.Alloc(n, "cudaMalloc(f64)"));
+            HAL_TRY(h->d64.Alloc(n, "cudaMalloc(d64)"));
+            HAL_TRY(h->g64.Alloc(2 * (static_cast<size_t>(h->xDim) + h->yDim), "cudaMalloc(g64)"));
+        }
+        if (kind != kAdvection && h->b64.p == nullptr)
+        {
+            HAL_TRY(h->a64.Alloc(n, "cudaMalloc(a64)"));
+            HAL_TRY(h->b64.Alloc(n, "cudaMalloc(b64)"));
+        }
+        cudaStream_t s = h->stream.Get();
+        const size_t bytes = n * sizeof(double);
+        HAL_TRY(CudaStatus(cudaMemcpyAsync(h->f64.p, field, bytes, cudaMemcpyHostToDevice, s), "cudaMemcpy(field)"));
+        HAL_TRY(CudaStatus(cudaMemcpyAsync(h->d64.p, deltas, bytes, cudaMemcpyHostToDevice, s), "cudaMemcpy(deltas)"));
+        if (kind != kAdvection)
+        {
+            HAL_TRY(CudaStatus(cudaMemcpyAsync(h->a64.p, a, bytes, cudaMemcpyHostToDevice, s), "cudaMemcpy(x array)"));
+            HAL_TRY(CudaStatus(cudaMemcpyAsync(h->b64.p, b, bytes, cudaMemcpyHostToDevice, s), "cudaMemcpy(y array)"));
+        }
+        LaunchStencil64(h, kind, xVel, yVel, wrapX, wrapY, s);
+        CountLaunch();
+        HAL_TRY(LaunchStatus(who));
+        HAL_TRY(CudaStatus(cudaMemcpyAsync(deltas, h->d64.p, bytes, cudaMemcpyDeviceToHost, s), "cudaMemcpy(deltas)"));
+        return CudaStatus(cudaStreamSynchronize(s), who);
+    }
+}
+
+extern "C" int hal_cuda_diffuse_var(hal_cuda_diffusion *h, const double *field, double *deltas,
+                                    const double *ratesX, const double *ratesY, int32_t wrapX, int32_t wrapY)
+{
+    HAL_REQUIRE(h != nullptr && field != nullptr && deltas != nullptr && ratesX != nullptr && ratesY != nullptr,
+                "hal_cuda_diffuse_var: NULL argument");
+    return Stencil64Common(h, kVarDiffusion, field, deltas, ratesX, ratesY, 0.0, 0.0, wrapX, wrapY,
+                           "hal_cuda_diffuse_var");
+}
+
+extern "C" int hal_cuda_advect(hal_cuda_diffusion *h, const double *field, double *deltas, double xVel, double yVel,
+                               int32_t wrapX, int32_t wrapY)
+{
+    HAL_REQUIRE(h != nullptr && field != nullptr && deltas != nullptr, "hal_cuda_advect: NULL argument");
+    HAL_REQUIRE(std::isfinite(xVel) && std::isfinite(yVel), "hal_cuda_advect: velocity must be finite");
+    return Stencil64Common(h, kAdvection, field, deltas, nullptr, nullptr, xVel, yVel, wrapX, wrapY,
+                           "hal_cuda_advect");
+}
+
+extern "C" int hal_cuda_advect_var(hal_cuda_diffusion *h, const double *field, double *deltas, const double *xVels,
+                                   const double *yVels, int32_t wrapX, int32_t wrapY)
+{
+    HAL_REQUIRE(h != nullptr && field != nullptr && deltas != nullptr && xVels != nullptr && yVels != nullptr,
+                "hal_cuda_advect_var: NULL argument");
+    return Stencil64Common(h, kVarAdvection, field, deltas, xVels, yVels, 0.0, 0.0, wrapX, wrapY,
+                           "hal_cuda_advect_var");
+}
+
+extern "C" int hal_cuda_stencil64_profile(hal_cuda_diffusion *h, int32_t kind, int32_t iters, double xVel,
+                                          double yVel, int32_t wrapX, int32_t wrapY, float *ms)
+{
+    HAL_REQUIRE(h != nullptr && ms != nullptr, "hal_cuda_stencil64_profile: NULL argument");
+    HAL_REQUIRE(iters > 0, "hal_cuda_stencil64_profile: iters must be positive");
+    HAL_REQUIRE(kind == kVarDiffusion || kind == kAdvection || kind == kVarAdvection,
+                "hal_cuda_stencil64_profile: unknown stencil kind");
+    HAL_REQUIRE(h->f64.p != nullptr && (kind == kAdvection || h->b64.p != nullptr),
+                "hal_cuda_stencil64_profile: no arrays uploaded by a call of this kind");
+    using namespace halcuda;
+    HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    cudaStream_t s = h->stream.Get();
+    cudaEvent_t e0, e1;
+    HAL_TRY(CudaStatus(cudaEventCreate(&e0), "cudaEventCreate"));
+    HAL_TRY(CudaStatus(cudaEventCreate(&e1), "cudaEventCreate"));
+    double total = 0.0;
+    int rc = HAL_CUDA_OK;
+    for (int32_t t = 0; t < iters && rc == HAL_CUDA_OK; t++)
+    {
+        cudaEventRecord(e0, s);
+        LaunchStencil64(h, kind, xVel, yVel, wrapX, wrapY, s);
+        CountLaunch();
+        cudaEventRecord(e1, s);
+        rc = LaunchStatus("hal_cuda_stencil64_profile");
+        if (rc == HAL_CUDA_OK)
+        {
+            rc = CudaStatus(cudaEventSynchronize(e1), "hal_cuda_stencil64_profile");
+        }
+        float a = 0.0f;
+        if (rc == HAL_CUDA_OK)
+        {
+            cudaEventElapsedTime(&a, e0, e1);
+        }
+        total += a;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    HAL_TRY(rc);
+    *ms = static_cast<float>(total / iters);
+    return HAL_CUDA_OK;
 }
 
 extern "C" int hal_cuda_diffuse(hal_cuda_diffusion *h, const double *field, int64_t fieldLen,

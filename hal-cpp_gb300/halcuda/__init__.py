@@ -21,6 +21,7 @@ LIB_PATH = os.path.join(PKG_DIR, "libhal_cuda.so")
 
 OK, EINVAL, ENOMEM, EDEVICE, ETIMEOUT, ENOTSUP = 0, 1, 2, 3, 4, 5
 ADI_MAX_LINE = 4096
+STENCIL_DIFFUSE_VAR, STENCIL_ADVECT, STENCIL_ADVECT_VAR = 0, 1, 2
 
 # Every exported symbol of include/hal_cuda.h, with (restype, argtypes).
 _i32, _i64, _f64, _vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p
@@ -35,6 +36,10 @@ SIGNATURES = {
     "hal_cuda_diffusion_destroy": (_I, [_vp]),
     "hal_cuda_diffuse": (_I, [_vp, _vp, _i64, _vp, _i64, _f64, _i32, _i32, _i32, _i32]),
     "hal_cuda_diffuse_bc": (_I, [_vp, _vp, _vp, _f64, _i32, _i32, _vp]),
+    "hal_cuda_diffuse_var": (_I, [_vp, _vp, _vp, _vp, _vp, _i32, _i32]),
+    "hal_cuda_advect": (_I, [_vp, _vp, _vp, _f64, _f64, _i32, _i32]),
+    "hal_cuda_advect_var": (_I, [_vp, _vp, _vp, _vp, _vp, _i32, _i32]),
+    "hal_cuda_stencil64_profile": (_I, [_vp, _i32, _i32, _f64, _f64, _i32, _i32, _vp]),
     "hal_cuda_diffusion_set_field": (_I, [_vp, _vp, _i64]),
     "hal_cuda_diffusion_get_field": (_I, [_vp, _vp, _i64]),
     "hal_cuda_diffusion_set_source": (_I, [_vp, _vp, _i64]),
@@ -223,6 +228,48 @@ class Diffusion(_Handle):
         _check(lib().hal_cuda_diffuse_bc(self._h, _p(f), _p(d), diffRate, int(wrapX), int(wrapY),
                                          _p(g)), "diffuse_bc")
         return d
+
+    def _cells(self, *arrays):
+        n = self.xDim * self.yDim
+        for a in arrays:
+            if a.size != n:
+                raise ValueError(f"array of {a.size} values for a {self.xDim} x {self.yDim} grid")
+
+    def diffuse_var(self, field, deltas, ratesX, ratesY, wrapX, wrapY):
+        """Internal::Diffusion2 with per-cell rates on float64 host arrays;
+        deltas is updated in place and returned."""
+        f, rx, ry = _f64(field), _f64(ratesX), _f64(ratesY)
+        d = np.ascontiguousarray(deltas, dtype=np.float64)
+        self._cells(f, d, rx, ry)
+        _check(lib().hal_cuda_diffuse_var(self._h, _p(f), _p(d), _p(rx), _p(ry), int(wrapX), int(wrapY)),
+               "diffuse_var")
+        return d
+
+    def advect(self, field, deltas, xVel, yVel, wrapX, wrapY):
+        """Internal::Advection2 at a uniform velocity (upwind)."""
+        f = _f64(field)
+        d = np.ascontiguousarray(deltas, dtype=np.float64)
+        self._cells(f, d)
+        _check(lib().hal_cuda_advect(self._h, _p(f), _p(d), float(xVel), float(yVel), int(wrapX), int(wrapY)),
+               "advect")
+        return d
+
+    def advect_var(self, field, deltas, xVels, yVels, wrapX, wrapY):
+        """Internal::Advection2 with per-cell velocities (upwind face fluxes)."""
+        f, vx, vy = _f64(field), _f64(xVels), _f64(yVels)
+        d = np.ascontiguousarray(deltas, dtype=np.float64)
+        self._cells(f, d, vx, vy)
+        _check(lib().hal_cuda_advect_var(self._h, _p(f), _p(d), _p(vx), _p(vy), int(wrapX), int(wrapY)),
+               "advect_var")
+        return d
+
+    def stencil64_profile(self, kind, iters, xVel=0.0, yVel=0.0, wrapX=False, wrapY=False):
+        """Average device ms of one FP64 stencil launch of `kind` (STENCIL_*)
+        on the arrays the last call of that kind uploaded."""
+        ms = ctypes.c_float()
+        _check(lib().hal_cuda_stencil64_profile(self._h, kind, iters, float(xVel), float(yVel), int(wrapX),
+                                                int(wrapY), ctypes.byref(ms)), "stencil64_profile")
+        return ms.value
 
     def set_field(self, field):
         f = _f32(field)

@@ -103,6 +103,34 @@ int hal_cuda_diffuse(hal_cuda_diffusion *h, const double *field, int64_t fieldLe
 int hal_cuda_diffuse_bc(hal_cuda_diffusion *h, const double *field, double *deltas,
                         double diffRate, int32_t wrapX, int32_t wrapY, const double *ghost);
 
+/* Per-cell rate diffusion (Internal::Diffusion2(field, deltas, diffRatesX,
+ * diffRatesY, ...), src/Pde/PDEequations.cpp:199-230): deltas += the
+ * rate-weighted neighbour differences; all arrays xDim*yDim in layout A.
+ * FP64, bit-identical to the reference. */
+int hal_cuda_diffuse_var(hal_cuda_diffusion *h, const double *field, double *deltas,
+                         const double *ratesX, const double *ratesY, int32_t wrapX, int32_t wrapY);
+
+/* First-order upwind advection at a uniform velocity (Internal::Advection2
+ * (field, deltas, xVel, yVel, ...), src/Pde/PDEequations.cpp:380-412).
+ * FP64, bit-identical to the reference. */
+int hal_cuda_advect(hal_cuda_diffusion *h, const double *field, double *deltas, double xVel,
+                    double yVel, int32_t wrapX, int32_t wrapY);
+
+/* Upwind advection with per-cell velocities (Internal::Advection2(field,
+ * deltas, xVels, yVels, ...), src/Pde/PDEequations.cpp:535-575): face
+ * fluxes from the upwind cell.  FP64, bit-identical to the reference. */
+int hal_cuda_advect_var(hal_cuda_diffusion *h, const double *field, double *deltas,
+                        const double *xVels, const double *yVels, int32_t wrapX, int32_t wrapY);
+
+/* Profiling of the three FP64 stencils above: average device time (ms) of one
+ * launch on the arrays the last call of that kind uploaded, over `iters`
+ * individually timed launches.  Deltas accumulate on the device. */
+#define HAL_CUDA_STENCIL_DIFFUSE_VAR 0
+#define HAL_CUDA_STENCIL_ADVECT 1
+#define HAL_CUDA_STENCIL_ADVECT_VAR 2
+int hal_cuda_stencil64_profile(hal_cuda_diffusion *h, int32_t kind, int32_t iters, double xVel,
+                               double yVel, int32_t wrapX, int32_t wrapY, float *ms);
+
 /* Resident field (DiffusionKernel2D::UploadField / RunSteps,
  * src/Gpu/DiffusionKernel2D.cpp:173-304).  len must be xDim*yDim. */
 int hal_cuda_diffusion_set_field(hal_cuda_diffusion *h, const float *field, int64_t len);

@@ -1207,3 +1207,136 @@ double oracle_dadi_loss_grad(const double *f0, const double *target, const doubl
     free(ws);
     return loss;
 }
+
+/* ---- variable-rate diffusion and upwind advection --------------------------- */
+
+/* DisplacedX2D / DisplacedY2D (src/Pde/PDEequations.cpp:163-197): the value of
+ * a per-cell array at a possibly off-grid neighbour, wrapped, or 0. */
+static double o_displaced_x(const double *v, int32_t x, int32_t y, int32_t xDim, int32_t yDim, int wrapX)
+{
+    if (o_in_dim(x, xDim))
+    {
+        return v[x * yDim + y];
+    }
+    if (wrapX)
+    {
+        return v[o_wrap(x, xDim) * yDim + y];
+    }
+    return 0.0;
+}
+
+static double o_displaced_y(const double *v, int32_t x, int32_t y, int32_t xDim, int32_t yDim, int wrapY)
+{
+    (void)xDim;
+    if (o_in_dim(y, yDim))
+    {
+        return v[x * yDim + y];
+    }
+    if (wrapY)
+    {
+        return v[x * yDim + o_wrap(y, yDim)];
+    }
+    return 0.0;
+}
+
+void oracle_diffusion2_var(const double *field, double *deltas, const double *ratesX, const double *ratesY,
+                           int32_t xDim, int32_t yDim, int wrapX, int wrapY)
+{
+    for (int32_t x = 0; x < xDim; x++)
+    {
+        for (int32_t y = 0; y < yDim; y++)
+        {
+            int32_t i = x * yDim + y;
+            double c = field[i];
+            double dp1x = ((x == xDim - 1) && !wrapX) ? o_displaced_x(ratesX, x + 1, y, xDim, yDim, wrapX) : ratesX[i];
+            double dm1x = o_displaced_x(ratesX, x - 1, y, xDim, yDim, wrapX);
+            double dp1y = ((y == yDim - 1) && !wrapY) ? o_displaced_y(ratesY, x, y + 1, xDim, yDim, wrapY) : ratesY[i];
+            double dm1y = o_displaced_y(ratesY, x, y - 1, xDim, yDim, wrapY);
+            double s = o_delta_x(field, c, x + 1, y, xDim, yDim, wrapX, NULL) * dp1x;
+            s += o_delta_x(field, c, x - 1, y, xDim, yDim, wrapX, NULL) * dm1x;
+            s += o_delta_y(field, c, x, y + 1, xDim, yDim, wrapY, NULL) * dp1y;
+            s += o_delta_y(field, c, x, y - 1, xDim, yDim, wrapY, NULL) * dm1y;
+            deltas[i] += s;
+        }
+    }
+}
+
+void oracle_advection2(const double *field, double *deltas, double xVel, double yVel, int32_t xDim, int32_t yDim,
+                       int wrapX, int wrapY)
+{
+    for (int32_t x = 0; x < xDim; x++)
+    {
+        for (int32_t y = 0; y < yDim; y++)
+        {
+            int32_t i = x * yDim + y;
+            double c = field[i];
+            if (xVel > 0)
+            {
+                deltas[i] += o_delta_x(field, c, x - 1, y, xDim, yDim, wrapX, NULL) * xVel;
+            }
+            else if (xVel < 0)
+            {
+                deltas[i] -= o_delta_x(field, c, x + 1, y, xDim, yDim, wrapX, NULL) * xVel;
+            }
+            if (yVel > 0)
+            {
+                deltas[i] += o_delta_y(field, c, x, y - 1, xDim, yDim, wrapY, NULL) * yVel;
+            }
+            else if (yVel < 0)
+            {
+                deltas[i] -= o_delta_y(field, c, x, y + 1, xDim, yDim, wrapY, NULL) * yVel;
+            }
+        }
+    }
+}
+
+void oracle_advection2_var(const double *field, double *deltas, const double *xVels, const double *yVels,
+                           int32_t xDim, int32_t yDim, int wrapX, int wrapY)
+{
+    for (int32_t x = 0; x < xDim; x++)
+    {
+        for (int32_t y = 0; y < yDim; y++)
+        {
+            int32_t i = x * yDim + y;
+            double xVelP = ((x == xDim - 1) && !wrapX) ? o_displaced_x(xVels, x + 1, y, xDim, yDim, wrapX) : xVels[i];
+            double yVelP = ((y == yDim - 1) && !wrapY) ? o_displaced_y(yVels, x, y + 1, xDim, yDim, wrapY) : yVels[i];
+            double xVelM = o_displaced_x(xVels, x - 1, y, xDim, yDim, wrapX);
+            double yVelM = o_displaced_y(yVels, x, y - 1, xDim, yDim, wrapY);
+            double c = field[i];
+            double xFluxP = 0.0, xFluxM = 0.0, yFluxP = 0.0, yFluxM = 0.0;
+            if (xVelP > 0)
+            {
+                xFluxP = xVelP * c;
+            }
+            else if (xVelP < 0)
+            {
+                xFluxP = xVelP * o_displaced_x(field, x + 1, y, xDim, yDim, wrapX);
+            }
+            if (xVelM > 0)
+            {
+                xFluxM = xVelM * o_displaced_x(field, x - 1, y, xDim, yDim, wrapX);
+            }
+            else if (xVelM < 0)
+            {
+                xFluxM = xVelM * c;
+            }
+            if (yVelP > 0)
+            {
+                yFluxP = yVelP * c;
+            }
+            else if (yVelP < 0)
+            {
+                yFluxP = yVelP * o_displaced_y(field, x, y + 1, xDim, yDim, wrapY);
+            }
+            if (yVelM > 0)
+            {
+                yFluxM = yVelM * o_displaced_y(field, x, y - 1, xDim, yDim, wrapY);
+            }
+            else if (yVelM < 0)
+            {
+                yFluxM = yVelM * c;
+            }
+            deltas[i] += -xFluxP + xFluxM - yFluxP + yFluxM;
+        }
+    }
+}

@@ -109,6 +109,24 @@ int oracle_accumulate_forces(const double *positions, const double *radii,
                              int32_t *cellOffsets, int32_t *bucketAgents,
                              int nthreads);
 
+/* ---- variable-rate diffusion and upwind advection ------------------------ */
+
+/* Internal::Diffusion2(pField, pDeltas, pDiffRatesX, pDiffRatesY, ...)
+ * (src/Pde/PDEequations.cpp:199-230): the +x/+y face uses the cell's rate (0
+ * past a non-wrapped edge), the -x/-y face the neighbour's. */
+void oracle_diffusion2_var(const double *field, double *deltas, const double *ratesX, const double *ratesY,
+                           int32_t xDim, int32_t yDim, int wrapX, int wrapY);
+
+/* Internal::Advection2 with a uniform velocity (src/Pde/PDEequations.cpp:
+ * 380-412): first-order upwind. */
+void oracle_advection2(const double *field, double *deltas, double xVel, double yVel, int32_t xDim, int32_t yDim,
+                       int wrapX, int wrapY);
+
+/* Internal::Advection2 with a per-cell velocity field
+ * (src/Pde/PDEequations.cpp:535-575): upwind face fluxes. */
+void oracle_advection2_var(const double *field, double *deltas, const double *xVels, const double *yVels,
+                           int32_t xDim, int32_t yDim, int wrapX, int wrapY);
+
 /* ---- variable-rate ADI and its adjoint -----------------------------------
  * No reference implementation exists: the step is defined from HAL's
  * variable-rate explicit stencil (src/Pde/PDEequations.cpp:199-230; the face

@@ -84,6 +84,10 @@ class Oracle(_Lib):
         L.oracle_accumulate_forces.argtypes = [vp, vp, i32, vp, f64, f64, i32, i32, ctypes.c_int,
                                                ctypes.c_int, vp, vp, ctypes.c_int]
         L.oracle_accumulate_forces.restype = ctypes.c_int
+        ci = ctypes.c_int
+        L.oracle_diffusion2_var.argtypes = [vp, vp, vp, vp, i32, i32, ci, ci]
+        L.oracle_advection2.argtypes = [vp, vp, f64, f64, i32, i32, ci, ci]
+        L.oracle_advection2_var.argtypes = [vp, vp, vp, vp, i32, i32, ci, ci]
         L.oracle_dadi_step.argtypes = [vp, vp, i32, i32, ctypes.c_int, ctypes.c_int, f64, vp, vp, vp]
         L.oracle_dadi_loss_grad.argtypes = [vp, vp, vp, f64, vp, i32, i32, ctypes.c_int, ctypes.c_int,
                                             i32, vp, vp, vp, vp]
@@ -191,6 +195,29 @@ class Oracle(_Lib):
 
 
     @classmethod
+    def diffuse_var(cls, field, deltas, ratesX, ratesY, xDim, yDim, wrapX, wrapY):
+        f, rx, ry = _f64(field), _f64(ratesX), _f64(ratesY)
+        d = _f64(deltas).copy()
+        cls.lib().oracle_diffusion2_var(f.ctypes.data, d.ctypes.data, rx.ctypes.data, ry.ctypes.data, xDim, yDim,
+                                        int(wrapX), int(wrapY))
+        return d
+
+    @classmethod
+    def advect(cls, field, deltas, xVel, yVel, xDim, yDim, wrapX, wrapY):
+        f = _f64(field)
+        d = _f64(deltas).copy()
+        cls.lib().oracle_advection2(f.ctypes.data, d.ctypes.data, xVel, yVel, xDim, yDim, int(wrapX), int(wrapY))
+        return d
+
+    @classmethod
+    def advect_var(cls, field, deltas, xVels, yVels, xDim, yDim, wrapX, wrapY):
+        f, vx, vy = _f64(field), _f64(xVels), _f64(yVels)
+        d = _f64(deltas).copy()
+        cls.lib().oracle_advection2_var(f.ctypes.data, d.ctypes.data, vx.ctypes.data, vy.ctypes.data, xDim, yDim,
+                                        int(wrapX), int(wrapY))
+        return d
+
+    @classmethod
     def dadi_step(cls, field, D, xDim, yDim, wrapX=False, wrapY=False, decay=0.0, src=None):
         """One variable-rate ADI step; returns (f', w)."""
         f = _f64(field)
@@ -223,6 +250,14 @@ class Oracle(_Lib):
         return loss, fT, gD, (gK.value if grad else None), gS
 
 
+def _ok(rc):
+    """Status of a reference shim call: 1 invalid_argument, 2 other error."""
+    if rc == 1:
+        raise ValueError("invalid_argument")
+    if rc != 0:
+        raise RuntimeError("reference error")
+
+
 class Reference(_Lib):
     """The reference's own CPU code (only where the reference tree was built)."""
 
@@ -245,9 +280,35 @@ class Reference(_Lib):
         L.ref_accumulate_forces.argtypes = [vp, i64, vp, i64, vp, f64, f64, i32, i32, ci, ci, vp,
                                             vp]
         L.ref_rand_draws.argtypes = [ctypes.c_uint64, ci, i32, i32, vp]
+        L.ref_diffuse_var.argtypes = [vp, vp, vp, vp, i32, i32, ci, ci]
+        L.ref_advect.argtypes = [vp, vp, f64, f64, i32, i32, ci, ci]
+        L.ref_advect_var.argtypes = [vp, vp, vp, vp, i32, i32, ci, ci]
         for name in ("ref_diffuse", "ref_diffuse_bc", "ref_diffuse_adi", "ref_diffuse_adi_bc",
                      "ref_pdegrid_run", "ref_accumulate_forces"):
             getattr(L, name).restype = ci
+
+    @classmethod
+    def diffuse_var(cls, field, deltas, ratesX, ratesY, xDim, yDim, wrapX, wrapY):
+        f, rx, ry = _f64(field), _f64(ratesX), _f64(ratesY)
+        d = _f64(deltas).copy()
+        _ok(cls.lib().ref_diffuse_var(f.ctypes.data, d.ctypes.data, rx.ctypes.data, ry.ctypes.data, xDim, yDim,
+                                      int(wrapX), int(wrapY)))
+        return d
+
+    @classmethod
+    def advect(cls, field, deltas, xVel, yVel, xDim, yDim, wrapX, wrapY):
+        f = _f64(field)
+        d = _f64(deltas).copy()
+        _ok(cls.lib().ref_advect(f.ctypes.data, d.ctypes.data, xVel, yVel, xDim, yDim, int(wrapX), int(wrapY)))
+        return d
+
+    @classmethod
+    def advect_var(cls, field, deltas, xVels, yVels, xDim, yDim, wrapX, wrapY):
+        f, vx, vy = _f64(field), _f64(xVels), _f64(yVels)
+        d = _f64(deltas).copy()
+        _ok(cls.lib().ref_advect_var(f.ctypes.data, d.ctypes.data, vx.ctypes.data, vy.ctypes.data, xDim, yDim,
+                                     int(wrapX), int(wrapY)))
+        return d
 
     @classmethod
     def diffuse(cls, field, deltas, r, xDim, yDim, wrapX, wrapY, ghost=None):

@@ -87,6 +87,32 @@ namespace
 extern "C"
 {
     // IDiffusionBackend2D::Diffuse through Hal::CpuDiffusionBackend2D.
+    // Internal::Diffusion2 with per-cell rates and the two Advection2 forms
+    // (src/Pde/PDEequations.cpp:199-230, 380-412, 535-575).
+    int ref_diffuse_var(const double *field, double *deltas, const double *ratesX, const double *ratesY,
+                        int32_t xDim, int32_t yDim, int wrapX, int wrapY)
+    {
+        Quiet();
+        return Guard([&]()
+                     { Hal::Internal::Diffusion2(field, deltas, ratesX, ratesY, xDim, yDim, wrapX != 0, wrapY != 0); });
+    }
+
+    int ref_advect(const double *field, double *deltas, double xVel, double yVel, int32_t xDim, int32_t yDim,
+                   int wrapX, int wrapY)
+    {
+        Quiet();
+        return Guard([&]()
+                     { Hal::Internal::Advection2(field, deltas, xVel, yVel, xDim, yDim, wrapX != 0, wrapY != 0); });
+    }
+
+    int ref_advect_var(const double *field, double *deltas, const double *xVels, const double *yVels, int32_t xDim,
+                       int32_t yDim, int wrapX, int wrapY)
+    {
+        Quiet();
+        return Guard([&]()
+                     { Hal::Internal::Advection2(field, deltas, xVels, yVels, xDim, yDim, wrapX != 0, wrapY != 0); });
+    }
+
     int ref_diffuse(const double *field, int64_t fieldLen, double *deltas, int64_t deltasLen,
                     double diffRate, int32_t xDim, int32_t yDim, int wrapX, int wrapY)
     {

@@ -178,6 +178,35 @@ def rand_cases():
     return out
 
 
+def var_stencil_cases(rng):
+    """Internal::Diffusion2 with per-cell rates and both Advection2 forms
+    (src/Pde/PDEequations.cpp:199-230, 380-412, 535-575)."""
+    out = {}
+    k = 0
+    for (xd, yd) in SIZES:
+        n = xd * yd
+        for wx, wy in ((0, 0), (1, 1), (1, 0), (0, 1)):
+            f = rng.random(n)
+            d = rng.random(n) * 0.1
+            rx = rng.random(n) * 0.24
+            ry = rng.random(n) * 0.24
+            vx = rng.random(n) - 0.5
+            vy = rng.random(n) - 0.5
+            vx[::7] = 0.0  # zero velocity faces take neither branch
+            xv, yv = [(0.2, -0.1), (-0.3, 0.15), (0.0, 0.2), (0.1, 0.0)][k % 4]
+            pre = f"c{k}_"
+            out[pre + "dims"] = np.array([xd, yd, wx, wy], dtype=np.int32)
+            out[pre + "vel"] = np.array([xv, yv])
+            for key, v in (("f", f), ("d", d), ("rx", rx), ("ry", ry), ("vx", vx), ("vy", vy)):
+                out[pre + key] = v
+            out[pre + "diffuse_var"] = R.diffuse_var(f, d, rx, ry, xd, yd, wx, wy)
+            out[pre + "advect"] = R.advect(f, d, xv, yv, xd, yd, wx, wy)
+            out[pre + "advect_var"] = R.advect_var(f, d, vx, vy, xd, yd, wx, wy)
+            k += 1
+    out["count"] = np.array([k])
+    return out
+
+
 def main():
     pyoracle.build(ref=True)
     if not R.available():
@@ -187,7 +216,8 @@ def main():
     np.savez_compressed(os.path.join(HERE, "ticks.npz"), **tick_cases(rng))
     np.savez_compressed(os.path.join(HERE, "agents.npz"), **agent_cases(rng))
     np.savez_compressed(os.path.join(HERE, "rand.npz"), **rand_cases())
-    for name in ("stencil", "ticks", "agents", "rand"):
+    np.savez_compressed(os.path.join(HERE, "varstencil.npz"), **var_stencil_cases(np.random.default_rng(8181)))
+    for name in ("stencil", "ticks", "agents", "rand", "varstencil"):
         p = os.path.join(HERE, name + ".npz")
         print(f"{p}: {os.path.getsize(p)} bytes")
 

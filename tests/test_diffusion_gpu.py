@@ -38,6 +38,66 @@ def test_diffuse_fp64_bit_exact_golden(hal, golden):
         assert np.array_equal(out, g[f"c{k}_explicit"]), f"case {k}: {xd}x{yd} wrap {wx}{wy}"
 
 
+def test_var_stencil_fp64_bit_exact_golden(hal, golden):
+    """Per-cell rate diffusion and both upwind advection forms against the
+    reference's vectors, bit for bit."""
+    g = golden("varstencil")
+    for k in range(int(g["count"][0])):
+        xd, yd, wx, wy = (int(v) for v in g[f"c{k}_dims"])
+        xv, yv = (float(v) for v in g[f"c{k}_vel"])
+        f, d = g[f"c{k}_f"], g[f"c{k}_d"]
+        tag = f"case {k}: {xd}x{yd} wrap {wx}{wy}"
+        with hal.Diffusion(xd, yd) as h:
+            assert np.array_equal(h.diffuse_var(f, d.copy(), g[f"c{k}_rx"], g[f"c{k}_ry"], wx, wy),
+                                  g[f"c{k}_diffuse_var"]), tag
+            assert np.array_equal(h.advect(f, d.copy(), xv, yv, wx, wy), g[f"c{k}_advect"]), tag
+            assert np.array_equal(h.advect_var(f, d.copy(), g[f"c{k}_vx"], g[f"c{k}_vy"], wx, wy),
+                                  g[f"c{k}_advect_var"]), tag
+
+
+@pytest.mark.parametrize("xd,yd", [(300, 257), (1024, 1024), (1, 4099)])
+def test_var_stencil_matches_oracle_large(hal, oracle, xd, yd):
+    rng = np.random.default_rng(xd * 7 + yd)
+    n = xd * yd
+    f, d = rng.random(n), rng.random(n) * 0.1
+    rx, ry = rng.random(n) * 0.24, rng.random(n) * 0.24
+    vx, vy = rng.random(n) - 0.5, rng.random(n) - 0.5
+    vy[::5] = 0.0
+    for wx, wy in ((0, 0), (1, 1), (0, 1)):
+        with hal.Diffusion(xd, yd) as h:
+            assert np.array_equal(h.diffuse_var(f, d.copy(), rx, ry, wx, wy),
+                                  oracle.diffuse_var(f, d, rx, ry, xd, yd, wx, wy))
+            for xv, yv in ((0.2, -0.35), (-0.1, 0.0)):
+                assert np.array_equal(h.advect(f, d.copy(), xv, yv, wx, wy),
+                                      oracle.advect(f, d, xv, yv, xd, yd, wx, wy))
+            assert np.array_equal(h.advect_var(f, d.copy(), vx, vy, wx, wy),
+                                  oracle.advect_var(f, d, vx, vy, xd, yd, wx, wy))
+
+
+def test_stencil64_profile_reuses_uploaded_arrays(hal, oracle):
+    """The profiling launches run on the arrays of the last call and keep
+    accumulating into its deltas."""
+    n = 64
+    rng = np.random.default_rng(3)
+    f, vx, vy = rng.random(n * n), rng.random(n * n) - 0.5, rng.random(n * n) - 0.5
+    with hal.Diffusion(n, n) as h:
+        with pytest.raises(ValueError):
+            h.stencil64_profile(hal.STENCIL_ADVECT_VAR, 2)
+        h.advect_var(f, np.zeros(n * n), vx, vy, 0, 0)
+        assert h.stencil64_profile(hal.STENCIL_ADVECT_VAR, 3) > 0.0
+        with pytest.raises(ValueError):
+            h.stencil64_profile(7, 1)
+
+
+def test_var_stencil_rejects_bad_input(hal):
+    with hal.Diffusion(8, 8) as h:
+        z = np.zeros(64)
+        with pytest.raises(ValueError):
+            h.diffuse_var(z, z.copy(), np.zeros(63), z, 0, 0)
+        with pytest.raises(ValueError):
+            h.advect(z, z.copy(), float("nan"), 0.0, 0, 0)
+
+
 def test_eigenmode_decay_through_interface(hal):
     """tests/IDiffusionBackend2DTests.cpp:23-72 (GPU epsilon 1e-4 there)."""
     nx, ny, r = 16, 20, 0.05

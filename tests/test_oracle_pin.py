@@ -40,6 +40,42 @@ def test_stencil_and_adi_golden_bit_exact(oracle, golden):
         assert np.array_equal(out, g[f"c{k}_adi"]), f"ADI case {k} {xd}x{yd} wrap {wx}{wy} bc {use_bc}"
 
 
+def test_var_stencil_golden_bit_exact(oracle, golden):
+    """Per-cell rate diffusion and both upwind advection forms
+    (Internal::Diffusion2 / Advection2, src/Pde/PDEequations.cpp:199-230,
+    380-412, 535-575) against vectors written by the reference."""
+    g = golden("varstencil")
+    count = int(g["count"][0])
+    assert count == 32
+    for k in range(count):
+        xd, yd, wx, wy = (int(v) for v in g[f"c{k}_dims"])
+        xv, yv = (float(v) for v in g[f"c{k}_vel"])
+        f, d = g[f"c{k}_f"], g[f"c{k}_d"]
+        tag = f"case {k} {xd}x{yd} wrap {wx}{wy}"
+        assert np.array_equal(oracle.diffuse_var(f, d, g[f"c{k}_rx"], g[f"c{k}_ry"], xd, yd, wx, wy),
+                              g[f"c{k}_diffuse_var"]), tag
+        assert np.array_equal(oracle.advect(f, d, xv, yv, xd, yd, wx, wy), g[f"c{k}_advect"]), tag
+        assert np.array_equal(oracle.advect_var(f, d, g[f"c{k}_vx"], g[f"c{k}_vy"], xd, yd, wx, wy),
+                              g[f"c{k}_advect_var"]), tag
+
+
+def test_var_stencil_conservation_kat(oracle):
+    """Known answers: with both axes wrapped, every face flux leaves one cell
+    and enters its neighbour, so the sums of the per-cell rate diffusion and
+    of both advection forms vanish; a uniform field does not diffuse."""
+    rng = np.random.default_rng(5)
+    xd, yd = 24, 17
+    n = xd * yd
+    f = rng.random(n)
+    z = np.zeros(n)
+    rx, ry = rng.random(n) * 0.2, rng.random(n) * 0.2
+    vx, vy = rng.random(n) - 0.5, rng.random(n) - 0.5
+    for out in (oracle.diffuse_var(f, z, rx, ry, xd, yd, 1, 1), oracle.advect(f, z, 0.3, -0.2, xd, yd, 1, 1),
+                oracle.advect_var(f, z, vx, vy, xd, yd, 1, 1)):
+        assert abs(out.sum()) <= 1e-12 * n
+    assert not oracle.diffuse_var(np.full(n, 2.5), z, rx, ry, xd, yd, 0, 0).any()
+
+
 def test_tick_golden_bit_exact(oracle, golden):
     g = golden("ticks")
     xd, yd, r, decay, ticks = g["exp_params"]
@@ -224,6 +260,14 @@ def test_restatement_matches_reference_library_random(oracle):
                               R.diffuse(f, d, 0.2, xd, yd, wx, wy, gh))
         assert np.array_equal(oracle.diffuse_adi(f, d, r, xd, yd, wx, wy, gh),
                               R.diffuse_adi(f, d, r, xd, yd, wx, wy, gh))
+        rx, ry = rng.random(xd * yd) * 0.2, rng.random(xd * yd) * 0.2
+        vx, vy = rng.random(xd * yd) - 0.5, rng.random(xd * yd) - 0.5
+        assert np.array_equal(oracle.diffuse_var(f, d, rx, ry, xd, yd, wx, wy),
+                              R.diffuse_var(f, d, rx, ry, xd, yd, wx, wy))
+        assert np.array_equal(oracle.advect(f, d, 0.25, -0.125, xd, yd, wx, wy),
+                              R.advect(f, d, 0.25, -0.125, xd, yd, wx, wy))
+        assert np.array_equal(oracle.advect_var(f, d, vx, vy, xd, yd, wx, wy),
+                              R.advect_var(f, d, vx, vy, xd, yd, wx, wy))
         n = int(rng.integers(0, 300))
         pos = (rng.random(2 * n) * max(xd, yd)).astype(np.float32).astype(np.float64)
         rad = 0.3 + rng.random(n) * 0.5
