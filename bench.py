@@ -381,18 +381,21 @@ def secondary_stencil64(hal, torch, stream, iters=20):
         keep.append(t)
         arrays[name] = v
     f, d, rx, ry, vx, vy = (arrays[k] for k in ("f", "d", "rx", "ry", "vx", "vy"))
-    # algorithmic bytes per cell: field read, deltas read+write, per-cell arrays read
-    forms = {"diffuse_var": (hal.STENCIL_DIFFUSE_VAR, 40, lambda h: h.diffuse_var(f, d, rx, ry, 0, 0)),
-             "advect": (hal.STENCIL_ADVECT, 24, lambda h: h.advect(f, d, 0.2, -0.1, 0, 0)),
-             "advect_var": (hal.STENCIL_ADVECT_VAR, 40, lambda h: h.advect_var(f, d, vx, vy, 0, 0))}
+    # per cell: algorithmic bytes (field read, deltas read+write, per-cell
+    # arrays read) and FP64 operations (the reference's adds, subtracts and
+    # multiplies; the FP64 pipe, not HBM, bounds these kernels on GB300)
+    forms = {"diffuse_var": (hal.STENCIL_DIFFUSE_VAR, 40, 12, lambda h: h.diffuse_var(f, d, rx, ry, 0, 0)),
+             "advect": (hal.STENCIL_ADVECT, 24, 6, lambda h: h.advect(f, d, 0.2, -0.1, 0, 0)),
+             "advect_var": (hal.STENCIL_ADVECT_VAR, 40, 8, lambda h: h.advect_var(f, d, vx, vy, 0, 0))}
     cpu_fn = {"diffuse_var": lambda: pyoracle.Oracle.diffuse_var(f, d, rx, ry, N, N, 0, 0),
               "advect": lambda: pyoracle.Oracle.advect(f, d, 0.2, -0.1, N, N, 0, 0),
               "advect_var": lambda: pyoracle.Oracle.advect_var(f, d, vx, vy, N, N, 0, 0)}
     peak, _ = peaks()
+    fp64_peak = hal.fp64_issue_rate() / 1e9
     out = {}
     with hal.Diffusion(N, N) as h:
         h.set_stream(stream.cuda_stream)
-        for name, (kind, bpc, call) in forms.items():
+        for name, (kind, bpc, opc, call) in forms.items():
             d[:] = 0.0
             call(h)
             call(h)
@@ -407,12 +410,15 @@ def secondary_stencil64(hal, torch, stream, iters=20):
             t0 = time.perf_counter()
             cpu_fn[name]()
             cpu_ms = (time.perf_counter() - t0) * 1e3
-            ach = bpc * CELLS / (ms * 1e-3) / 1e9
+            gbs = bpc * CELLS / (ms * 1e-3) / 1e9
+            gops = opc * CELLS / (ms * 1e-3) / 1e9
             out[name] = {"kernel_ms": ms, "e2e_ms": e2e_ms, "cpu_oracle_ms": cpu_ms,
-                         "e2e_value": CELLS / (e2e_ms * 1e-3), "unit": "cell-updates/s",
-                         "bytes_per_cell": bpc,
-                         "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
-                                      "frac": ach / peak}}
+                         "value": CELLS / (ms * 1e-3), "e2e_value": CELLS / (e2e_ms * 1e-3),
+                         "unit": "cell-updates/s", "bytes_per_cell": bpc, "fp64_ops_per_cell": opc,
+                         "roofline": {"bound": "fp64", "achieved": gops, "peak": fp64_peak,
+                                      "unit": "G FP64 ops/s", "frac": gops / fp64_peak,
+                                      "peak_kind": "measured live (hal_cuda_fp64_issue_rate)",
+                                      "hbm": {"achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak}}}
     return {"workload": "fp64-stencils-2048x2048-zeroflux-per-cell-rates-and-velocities", "forms": out,
             "note": "FP64, bit-identical to the reference; e2e = one C-ABI call on pinned host arrays "
                     "(wall clock, copies in and out); cpu = the oracle, 1 thread"}

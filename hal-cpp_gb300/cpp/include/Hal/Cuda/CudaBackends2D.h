@@ -62,6 +62,39 @@ namespace Hal::Cuda
                               bool                       wrapY,
                               const std::vector<double> &ghost);
 
+        // Internal::Diffusion2 with per-cell rates (src/Pde/PDEequations.cpp:
+        // 199-230); FP64, bit-identical to the CPU code.
+        void DiffuseVariable(const std::vector<double> &field,
+                             std::vector<double>       &deltas,
+                             const std::vector<double> &diffRatesX,
+                             const std::vector<double> &diffRatesY,
+                             bool                       wrapX,
+                             bool                       wrapY);
+
+        // Internal::Advection2 at a uniform velocity (src/Pde/
+        // PDEequations.cpp:380-412) or, with a non-empty ghost table, its
+        // Dirichlet form (include/Hal/Pde/PDEequations.h:413-447).
+        void Advect(const std::vector<double> &field,
+                    std::vector<double>       &deltas,
+                    double                     xVel,
+                    double                     yVel,
+                    bool                       wrapX,
+                    bool                       wrapY,
+                    const std::vector<double> &ghost = {});
+
+        // Internal::Advection2 with per-cell velocities (src/Pde/
+        // PDEequations.cpp:535-575) or, with ghost tables for the field and
+        // the two velocity components, its Dirichlet form (:720-778).
+        void AdvectVariable(const std::vector<double> &field,
+                            std::vector<double>       &deltas,
+                            const std::vector<double> &xVels,
+                            const std::vector<double> &yVels,
+                            bool                       wrapX,
+                            bool                       wrapY,
+                            const std::vector<double> &ghost = {},
+                            const std::vector<double> &ghostXVel = {},
+                            const std::vector<double> &ghostYVel = {});
+
         // Device-resident PDEGrid2D tick: f' = f + r L(f) - decay f + src.
         void SetField(const std::vector<float> &field);
         void GetField(std::vector<float> &field);

@@ -93,6 +93,47 @@ namespace Hal::Cuda
               "CudaDiffusionBackend2D::DiffuseDirichlet");
     }
 
+    void CudaDiffusionBackend2D::DiffuseVariable(const std::vector<double> &field, std::vector<double> &deltas,
+                                                 const std::vector<double> &diffRatesX,
+                                                 const std::vector<double> &diffRatesY, bool wrapX, bool wrapY)
+    {
+        CheckCells(field, deltas, m_xDim, m_yDim, "CudaDiffusionBackend2D::DiffuseVariable");
+        CheckCells(diffRatesX, diffRatesY, m_xDim, m_yDim, "CudaDiffusionBackend2D::DiffuseVariable");
+        Check(hal_cuda_diffuse_var(m_pHandle, field.data(), deltas.data(), diffRatesX.data(), diffRatesY.data(), wrapX,
+                                   wrapY),
+              "CudaDiffusionBackend2D::DiffuseVariable");
+    }
+
+    void CudaDiffusionBackend2D::Advect(const std::vector<double> &field, std::vector<double> &deltas, double xVel,
+                                        double yVel, bool wrapX, bool wrapY, const std::vector<double> &ghost)
+    {
+        CheckCells(field, deltas, m_xDim, m_yDim, "CudaDiffusionBackend2D::Advect");
+        CheckGhost(ghost.size(), m_xDim, m_yDim, "CudaDiffusionBackend2D::Advect");
+        Check(ghost.empty() ? hal_cuda_advect(m_pHandle, field.data(), deltas.data(), xVel, yVel, wrapX, wrapY)
+                            : hal_cuda_advect_bc(m_pHandle, field.data(), deltas.data(), xVel, yVel, wrapX, wrapY,
+                                                 ghost.data()),
+              "CudaDiffusionBackend2D::Advect");
+    }
+
+    void CudaDiffusionBackend2D::AdvectVariable(const std::vector<double> &field, std::vector<double> &deltas,
+                                                const std::vector<double> &xVels, const std::vector<double> &yVels,
+                                                bool wrapX, bool wrapY, const std::vector<double> &ghost,
+                                                const std::vector<double> &ghostXVel,
+                                                const std::vector<double> &ghostYVel)
+    {
+        CheckCells(field, deltas, m_xDim, m_yDim, "CudaDiffusionBackend2D::AdvectVariable");
+        CheckCells(xVels, yVels, m_xDim, m_yDim, "CudaDiffusionBackend2D::AdvectVariable");
+        CheckGhost(ghost.size(), m_xDim, m_yDim, "CudaDiffusionBackend2D::AdvectVariable");
+        CheckGhost(ghostXVel.size(), m_xDim, m_yDim, "CudaDiffusionBackend2D::AdvectVariable");
+        CheckGhost(ghostYVel.size(), m_xDim, m_yDim, "CudaDiffusionBackend2D::AdvectVariable");
+        const bool bc = !ghost.empty() || !ghostXVel.empty() || !ghostYVel.empty();
+        Check(bc ? hal_cuda_advect_var_bc(m_pHandle, field.data(), deltas.data(), xVels.data(), yVels.data(), wrapX,
+                                          wrapY, GhostOrNull(ghost), GhostOrNull(ghostXVel), GhostOrNull(ghostYVel))
+                 : hal_cuda_advect_var(m_pHandle, field.data(), deltas.data(), xVels.data(), yVels.data(), wrapX,
+                                       wrapY),
+              "CudaDiffusionBackend2D::AdvectVariable");
+    }
+
     void CudaDiffusionBackend2D::SetField(const std::vector<float> &field)
     {
         Check(hal_cuda_diffusion_set_field(m_pHandle, field.data(), static_cast<int64_t>(field.size())),

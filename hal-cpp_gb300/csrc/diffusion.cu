@@ -303,9 +303,36 @@ namespace halcuda
             TickTile<VEC>(table[t.x], t.y, t.z);
         }
 
-        // FP64 IDiffusionBackend2D::Diffuse: deltas[i] += sum * r, with the
-        // reference's operation order and no contraction, so the result is
-        // bit-identical to Hal::CpuDiffusionBackend2D.
+        // The FP64 stencils below reproduce the reference's CPU arithmetic bit
+        // for bit: IEEE operations in the reference's order, no contraction.
+        // GB300 issues FP64 at a small fraction of its FP32 rate, so the
+        // cells are indexed without 64-bit division (y from the block's x
+        // index, x from its y index) and sign tests use the bit pattern.
+
+        // v > 0 and v < 0 as IEEE comparisons (false for zeros and NaNs),
+        // decided on the two 32-bit halves of v so that no FP64 compare is
+        // issued: |v| is nonzero and at most infinity, then the sign bit.
+        __device__ __forceinline__ int Sign64(double v)
+        {
+            const int hi = __double2hiint(v);
+            const unsigned lo = static_cast<unsigned>(__double2loint(v));
+            const unsigned mag = static_cast<unsigned>(hi) & 0x7fffffffu;
+            const bool nonzero = (mag | lo) != 0u;
+            const bool notNan = mag < 0x7ff00000u || (mag == 0x7ff00000u && lo == 0u);
+            return (nonzero && notNan) ? (hi < 0 ? -1 : 1) : 0;
+        }
+
+        // vel * (vel > 0 ? ifPos : ifNeg), or +0 when vel is 0 or NaN: the
+        // reference's upwind flux of one face.
+        __device__ __forceinline__ double UpwindFlux64(double vel, double ifPos, double ifNeg)
+        {
+            const int sign = Sign64(vel);
+            const double p = __dmul_rn(vel, sign > 0 ? ifPos : ifNeg);
+            return sign != 0 ? p : 0.0;
+        }
+
+        // field[n] - c along one axis of a line: the neighbour at index n
+        // (wrapped, a Dirichlet ghost doubled, or 0 off-grid) minus the cell.
         __device__ __forceinline__ double DeltaTerm64(const double *f, double c, int32_t n,
                                                       int32_t dim, bool wrap, int64_t base,
                                                       int64_t stride, const double *ghost,
@@ -327,34 +354,13 @@ namespace halcuda
             return 0.0;
         }
 
-        __global__ void Diffuse64Kernel(const double *__restrict__ f, double *__restrict__ deltas,
-                                        int32_t xDim, int32_t yDim, double r, int32_t wrapX,
-                                        int32_t wrapY, const double *__restrict__ ghost)
-        {
-            int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-            int64_t n = static_cast<int64_t>(xDim) * yDim;
-            if (i >= n)
-            {
-                return;
-            }
-            int32_t x = static_cast<int32_t>(i / yDim);
-            int32_t y = static_cast<int32_t>(i - static_cast<int64_t>(x) * yDim);
-            double c = f[i];
-            const double *gx = ghost;
-            const double *gy = ghost ? ghost + 2 * yDim : nullptr;
-            int64_t colBase = y;                                // column y, stride yDim
-            int64_t rowBase = static_cast<int64_t>(x) * yDim;   // row x, stride 1
-            double s = DeltaTerm64(f, c, x + 1, xDim, wrapX, colBase, yDim, gx, yDim + y);
-            s = __dadd_rn(s, DeltaTerm64(f, c, x - 1, xDim, wrapX, colBase, yDim, gx, y));
-            s = __dadd_rn(s, DeltaTerm64(f, c, y + 1, yDim, wrapY, rowBase, 1, gy, xDim + x));
-            s = __dadd_rn(s, DeltaTerm64(f, c, y - 1, yDim, wrapY, rowBase, 1, gy, x));
-            deltas[i] = __dadd_rn(deltas[i], __dmul_rn(s, r));
-        }
-
-        // DisplacedX2D / DisplacedY2D (src/Pde/PDEequations.cpp:163-197): a
-        // per-cell value at neighbour n of a line (wrapped, or 0 off-grid).
+        // DisplacedX2D / DisplacedY2D (src/Pde/PDEequations.cpp:163-197) and
+        // their Dirichlet forms (include/Hal/Pde/PDEequations.h:589-616): a
+        // per-cell value at neighbour n of a line, wrapped, or off-grid the
+        // ghost-table value (not doubled), or 0 without a table.
         __device__ __forceinline__ double Displaced64(const double *v, int32_t n, int32_t dim, bool wrap,
-                                                      int64_t base, int64_t stride)
+                                                      int64_t base, int64_t stride, const double *ghost = nullptr,
+                                                      int64_t ghostIdx = 0)
         {
             if (n >= 0 && n < dim)
             {
@@ -365,125 +371,170 @@ namespace halcuda
                 int32_t w = (n < 0) ? n + dim : n - dim;
                 return v[base + w * stride];
             }
-            return 0.0;
+            return ghost != nullptr ? ghost[ghostIdx] : 0.0;
         }
+
+        // IDiffusionBackend2D::Diffuse: deltas[i] += sum * r, bit-identical
+        // to Hal::CpuDiffusionBackend2D (src/Pde/PDEequations.cpp, the
+        // uniform-rate Diffusion2 and its Dirichlet form).
+        struct Diffuse64Cell
+        {
+            const double *__restrict__ f;
+            double *__restrict__ deltas;
+            const double *__restrict__ ghost;
+            double r;
+            int32_t xDim, yDim, wrapX, wrapY;
+
+            __device__ __forceinline__ void operator()(int32_t x, int32_t y, int64_t i) const
+            {
+                const double c = f[i];
+                const double *gx = ghost;
+                const double *gy = ghost ? ghost + 2 * yDim : nullptr;
+                const int64_t colBase = y;                               // column y, stride yDim
+                const int64_t rowBase = static_cast<int64_t>(x) * yDim;  // row x, stride 1
+                double s = DeltaTerm64(f, c, x + 1, xDim, wrapX, colBase, yDim, gx, yDim + y);
+                s = __dadd_rn(s, DeltaTerm64(f, c, x - 1, xDim, wrapX, colBase, yDim, gx, y));
+                s = __dadd_rn(s, DeltaTerm64(f, c, y + 1, yDim, wrapY, rowBase, 1, gy, xDim + x));
+                s = __dadd_rn(s, DeltaTerm64(f, c, y - 1, yDim, wrapY, rowBase, 1, gy, x));
+                deltas[i] = __dadd_rn(deltas[i], __dmul_rn(s, r));
+            }
+        };
 
         // Internal::Diffusion2 with per-cell rates (src/Pde/PDEequations.cpp:
-        // 199-230), IEEE operations in the reference's order.
-        __global__ void DiffuseVar64Kernel(const double *__restrict__ f, double *__restrict__ deltas,
-                                           const double *__restrict__ rx, const double *__restrict__ ry,
-                                           int32_t xDim, int32_t yDim, int32_t wrapX, int32_t wrapY)
+        // 199-230): the +x face takes the cell's own rate except at a closed
+        // last column, where the displaced (zero) rate applies.
+        struct DiffuseVar64Cell
         {
-            int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-            if (i >= static_cast<int64_t>(xDim) * yDim)
+            const double *__restrict__ f;
+            double *__restrict__ deltas;
+            const double *__restrict__ rx;
+            const double *__restrict__ ry;
+            int32_t xDim, yDim, wrapX, wrapY;
+
+            __device__ __forceinline__ void operator()(int32_t x, int32_t y, int64_t i) const
             {
-                return;
+                const double c = f[i];
+                const int64_t colBase = y, rowBase = static_cast<int64_t>(x) * yDim;
+                const double dp1x =
+                    ((x == xDim - 1) && !wrapX) ? Displaced64(rx, x + 1, xDim, wrapX, colBase, yDim) : rx[i];
+                const double dm1x = Displaced64(rx, x - 1, xDim, wrapX, colBase, yDim);
+                const double dp1y =
+                    ((y == yDim - 1) && !wrapY) ? Displaced64(ry, y + 1, yDim, wrapY, rowBase, 1) : ry[i];
+                const double dm1y = Displaced64(ry, y - 1, yDim, wrapY, rowBase, 1);
+                double s = __dmul_rn(DeltaTerm64(f, c, x + 1, xDim, wrapX, colBase, yDim, nullptr, 0), dp1x);
+                s = __dadd_rn(s, __dmul_rn(DeltaTerm64(f, c, x - 1, xDim, wrapX, colBase, yDim, nullptr, 0), dm1x));
+                s = __dadd_rn(s, __dmul_rn(DeltaTerm64(f, c, y + 1, yDim, wrapY, rowBase, 1, nullptr, 0), dp1y));
+                s = __dadd_rn(s, __dmul_rn(DeltaTerm64(f, c, y - 1, yDim, wrapY, rowBase, 1, nullptr, 0), dm1y));
+                deltas[i] = __dadd_rn(deltas[i], s);
             }
-            int32_t x = static_cast<int32_t>(i / yDim);
-            int32_t y = static_cast<int32_t>(i - static_cast<int64_t>(x) * yDim);
-            const double c = f[i];
-            const int64_t colBase = y, rowBase = static_cast<int64_t>(x) * yDim;
-            const double dp1x = ((x == xDim - 1) && !wrapX) ? Displaced64(rx, x + 1, xDim, wrapX, colBase, yDim) : rx[i];
-            const double dm1x = Displaced64(rx, x - 1, xDim, wrapX, colBase, yDim);
-            const double dp1y = ((y == yDim - 1) && !wrapY) ? Displaced64(ry, y + 1, yDim, wrapY, rowBase, 1) : ry[i];
-            const double dm1y = Displaced64(ry, y - 1, yDim, wrapY, rowBase, 1);
-            double s = __dmul_rn(DeltaTerm64(f, c, x + 1, xDim, wrapX, colBase, yDim, nullptr, 0), dp1x);
-            s = __dadd_rn(s, __dmul_rn(DeltaTerm64(f, c, x - 1, xDim, wrapX, colBase, yDim, nullptr, 0), dm1x));
-            s = __dadd_rn(s, __dmul_rn(DeltaTerm64(f, c, y + 1, yDim, wrapY, rowBase, 1, nullptr, 0), dp1y));
-            s = __dadd_rn(s, __dmul_rn(DeltaTerm64(f, c, y - 1, yDim, wrapY, rowBase, 1, nullptr, 0), dm1y));
-            deltas[i] = __dadd_rn(deltas[i], s);
-        }
+        };
 
         // Internal::Advection2, uniform velocity (src/Pde/PDEequations.cpp:
-        // 380-412): first-order upwind, each term added to deltas in turn.
-        __global__ void Advect64Kernel(const double *__restrict__ f, double *__restrict__ deltas, double xVel,
-                                       double yVel, int32_t xDim, int32_t yDim, int32_t wrapX, int32_t wrapY)
+        // 380-412; Dirichlet form include/Hal/Pde/PDEequations.h:413-447):
+        // first-order upwind, each term added to deltas in turn.
+        struct Advect64Cell
         {
-            int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-            if (i >= static_cast<int64_t>(xDim) * yDim)
+            const double *__restrict__ f;
+            double *__restrict__ deltas;
+            const double *__restrict__ ghost;  // Dirichlet table or nullptr
+            double xVel, yVel;
+            int32_t xDim, yDim, wrapX, wrapY;
+            int32_t xSign, ySign;  // +1 for vel > 0, -1 for vel < 0, else 0 (set on the host)
+
+            __device__ __forceinline__ void operator()(int32_t x, int32_t y, int64_t i) const
             {
-                return;
+                const double c = f[i];
+                const int64_t colBase = y, rowBase = static_cast<int64_t>(x) * yDim;
+                const double *gy = ghost ? ghost + 2 * yDim : nullptr;
+                double d = deltas[i];
+                if (xSign > 0)
+                {
+                    d = __dadd_rn(d, __dmul_rn(DeltaTerm64(f, c, x - 1, xDim, wrapX, colBase, yDim, ghost, y), xVel));
+                }
+                else if (xSign < 0)
+                {
+                    d = __dsub_rn(d,
+                                  __dmul_rn(DeltaTerm64(f, c, x + 1, xDim, wrapX, colBase, yDim, ghost, yDim + y), xVel));
+                }
+                if (ySign > 0)
+                {
+                    d = __dadd_rn(d, __dmul_rn(DeltaTerm64(f, c, y - 1, yDim, wrapY, rowBase, 1, gy, x), yVel));
+                }
+                else if (ySign < 0)
+                {
+                    d = __dsub_rn(d, __dmul_rn(DeltaTerm64(f, c, y + 1, yDim, wrapY, rowBase, 1, gy, xDim + x), yVel));
+                }
+                deltas[i] = d;
             }
-            int32_t x = static_cast<int32_t>(i / yDim);
-            int32_t y = static_cast<int32_t>(i - static_cast<int64_t>(x) * yDim);
-            const double c = f[i];
-            const int64_t colBase = y, rowBase = static_cast<int64_t>(x) * yDim;
-            double d = deltas[i];
-            if (xVel > 0)
-            {
-                d = __dadd_rn(d, __dmul_rn(DeltaTerm64(f, c, x - 1, xDim, wrapX, colBase, yDim, nullptr, 0), xVel));
-            }
-            else if (xVel < 0)
-            {
-                d = __dsub_rn(d, __dmul_rn(DeltaTerm64(f, c, x + 1, xDim, wrapX, colBase, yDim, nullptr, 0), xVel));
-            }
-            if (yVel > 0)
-            {
-                d = __dadd_rn(d, __dmul_rn(DeltaTerm64(f, c, y - 1, yDim, wrapY, rowBase, 1, nullptr, 0), yVel));
-            }
-            else if (yVel < 0)
-            {
-                d = __dsub_rn(d, __dmul_rn(DeltaTerm64(f, c, y + 1, yDim, wrapY, rowBase, 1, nullptr, 0), yVel));
-            }
-            deltas[i] = d;
-        }
+        };
 
         // Internal::Advection2, per-cell velocity (src/Pde/PDEequations.cpp:
-        // 535-575): upwind face fluxes, -xFluxP + xFluxM - yFluxP + yFluxM.
-        __global__ void AdvectVar64Kernel(const double *__restrict__ f, double *__restrict__ deltas,
-                                          const double *__restrict__ vx, const double *__restrict__ vy, int32_t xDim,
-                                          int32_t yDim, int32_t wrapX, int32_t wrapY)
+        // 535-575; Dirichlet form include/Hal/Pde/PDEequations.h:720-778):
+        // upwind face fluxes, -xFluxP + xFluxM - yFluxP + yFluxM.
+        struct AdvectVar64Cell
         {
-            int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-            if (i >= static_cast<int64_t>(xDim) * yDim)
+            const double *__restrict__ f;
+            double *__restrict__ deltas;
+            const double *__restrict__ vx;
+            const double *__restrict__ vy;
+            const double *__restrict__ ghost;    // field boundary table or nullptr
+            const double *__restrict__ ghostVx;  // x-velocity boundary table or nullptr
+            const double *__restrict__ ghostVy;  // y-velocity boundary table or nullptr
+            int32_t xDim, yDim, wrapX, wrapY;
+
+            __device__ __forceinline__ void operator()(int32_t x, int32_t y, int64_t i) const
+            {
+                const int64_t colBase = y, rowBase = static_cast<int64_t>(x) * yDim;
+                const double *gy = ghost ? ghost + 2 * yDim : nullptr;
+                const double *gvy = ghostVy ? ghostVy + 2 * yDim : nullptr;
+                const double xVelP = ((x == xDim - 1) && !wrapX)
+                                         ? Displaced64(vx, x + 1, xDim, wrapX, colBase, yDim, ghostVx, yDim + y)
+                                         : vx[i];
+                const double yVelP = ((y == yDim - 1) && !wrapY)
+                                         ? Displaced64(vy, y + 1, yDim, wrapY, rowBase, 1, gvy, xDim + x)
+                                         : vy[i];
+                const double xVelM = Displaced64(vx, x - 1, xDim, wrapX, colBase, yDim, ghostVx, y);
+                const double yVelM = Displaced64(vy, y - 1, yDim, wrapY, rowBase, 1, gvy, x);
+                const double c = f[i];
+                // Each flux is velocity x upwind value, 0 when the velocity is
+                // neither > 0 nor < 0.  The product is formed on every lane and
+                // selected afterwards, so lanes of a warp with different signs
+                // do not issue the FP64 multiply twice.
+                const double xFluxP =
+                    UpwindFlux64(xVelP, c, Displaced64(f, x + 1, xDim, wrapX, colBase, yDim, ghost, yDim + y));
+                const double xFluxM = UpwindFlux64(xVelM, Displaced64(f, x - 1, xDim, wrapX, colBase, yDim, ghost, y), c);
+                const double yFluxP = UpwindFlux64(yVelP, c, Displaced64(f, y + 1, yDim, wrapY, rowBase, 1, gy, xDim + x));
+                const double yFluxM = UpwindFlux64(yVelM, Displaced64(f, y - 1, yDim, wrapY, rowBase, 1, gy, x), c);
+                // -xFluxP + xFluxM is xFluxM - xFluxP exactly (IEEE a - b = a + (-b))
+                double t = __dsub_rn(xFluxM, xFluxP);
+                t = __dsub_rn(t, yFluxP);
+                t = __dadd_rn(t, yFluxM);
+                deltas[i] = __dadd_rn(deltas[i], t);
+            }
+        };
+
+        // One thread per cell of an xDim x yDim field in layout A: y from the
+        // block's x index (rows read coalesced), x from its y index, striding
+        // by gridDim.y when xDim exceeds the grid's y limit.
+        template <class Cell>
+        __global__ void __launch_bounds__(256) Cells64Kernel(Cell cell, int32_t xDim, int32_t yDim)
+        {
+            const int32_t y = static_cast<int32_t>(blockIdx.x * blockDim.x + threadIdx.x);
+            if (y >= yDim)
             {
                 return;
             }
-            int32_t x = static_cast<int32_t>(i / yDim);
-            int32_t y = static_cast<int32_t>(i - static_cast<int64_t>(x) * yDim);
-            const int64_t colBase = y, rowBase = static_cast<int64_t>(x) * yDim;
-            const double xVelP = ((x == xDim - 1) && !wrapX) ? Displaced64(vx, x + 1, xDim, wrapX, colBase, yDim) : vx[i];
-            const double yVelP = ((y == yDim - 1) && !wrapY) ? Displaced64(vy, y + 1, yDim, wrapY, rowBase, 1) : vy[i];
-            const double xVelM = Displaced64(vx, x - 1, xDim, wrapX, colBase, yDim);
-            const double yVelM = Displaced64(vy, y - 1, yDim, wrapY, rowBase, 1);
-            const double c = f[i];
-            double xFluxP = 0.0, xFluxM = 0.0, yFluxP = 0.0, yFluxM = 0.0;
-            if (xVelP > 0)
+            for (int32_t x = static_cast<int32_t>(blockIdx.y); x < xDim; x += static_cast<int32_t>(gridDim.y))
             {
-                xFluxP = __dmul_rn(xVelP, c);
+                cell(x, y, static_cast<int64_t>(x) * yDim + y);
             }
-            else if (xVelP < 0)
-            {
-                xFluxP = __dmul_rn(xVelP, Displaced64(f, x + 1, xDim, wrapX, colBase, yDim));
-            }
-            if (xVelM > 0)
-            {
-                xFluxM = __dmul_rn(xVelM, Displaced64(f, x - 1, xDim, wrapX, colBase, yDim));
-            }
-            else if (xVelM < 0)
-            {
-                xFluxM = __dmul_rn(xVelM, c);
-            }
-            if (yVelP > 0)
-            {
-                yFluxP = __dmul_rn(yVelP, c);
-            }
-            else if (yVelP < 0)
-            {
-                yFluxP = __dmul_rn(yVelP, Displaced64(f, y + 1, yDim, wrapY, rowBase, 1));
-            }
-            if (yVelM > 0)
-            {
-                yFluxM = __dmul_rn(yVelM, Displaced64(f, y - 1, yDim, wrapY, rowBase, 1));
-            }
-            else if (yVelM < 0)
-            {
-                yFluxM = __dmul_rn(yVelM, c);
-            }
-            double t = __dadd_rn(-xFluxP, xFluxM);
-            t = __dsub_rn(t, yFluxP);
-            t = __dadd_rn(t, yFluxM);
-            deltas[i] = __dadd_rn(deltas[i], t);
+        }
+
+        // One cell per thread.  (A grid of one resident wave with threads
+        // walking x measured 4-9% slower on these FP64-bound kernels.)
+        inline dim3 Cells64Grid(int32_t xDim, int32_t yDim)
+        {
+            return dim3(static_cast<unsigned>((yDim + 255) / 256), static_cast<unsigned>(std::min(xDim, 65535)));
         }
     }
 
@@ -522,6 +573,7 @@ namespace halcuda
         bool hasPoints = false;
         DevBuf<double> f64, d64, g64;
         DevBuf<double> a64, b64;  // per-cell rates or velocities of the FP64 stencil calls
+        DevBuf<double> gv64;      // x- and y-velocity ghost tables of the Dirichlet advection form
         GraphCache graph[2];  // by the parity of the starting buffer
         dim3 grid, block;
 
@@ -695,9 +747,8 @@ namespace
             HAL_TRY(CudaStatus(cudaMemcpyAsync(h->g64.p, ghost, ng * sizeof(double), cudaMemcpyHostToDevice, s),
                                "cudaMemcpy(ghost)"));
         }
-        unsigned blocks = static_cast<unsigned>((n + 255) / 256);
-        Diffuse64Kernel<<<blocks, 256, 0, s>>>(h->f64.p, h->d64.p, h->xDim, h->yDim, r, wrapX, wrapY,
-                                               ghost ? h->g64.p : nullptr);
+        const Diffuse64Cell cell{h->f64.p, h->d64.p, ghost ? h->g64.p : nullptr, r, h->xDim, h->yDim, wrapX, wrapY};
+        Cells64Kernel<<<Cells64Grid(h->xDim, h->yDim), 256, 0, s>>>(cell, h->xDim, h->yDim);
         CountLaunch();
         HAL_TRY(LaunchStatus(who));
         HAL_TRY(CudaStatus(cudaMemcpyAsync(deltas, h->d64.p, n * sizeof(double), cudaMemcpyDeviceToHost, s),
@@ -715,32 +766,38 @@ namespace
         kVarAdvection = HAL_CUDA_STENCIL_ADVECT_VAR
     };
 
+    // ghost / ghostVx / ghostVy: device ghost tables of the Dirichlet forms
+    // (field; x and y velocities), or nullptr for the zero-flux forms.
     void LaunchStencil64(hal_cuda_diffusion *h, int kind, double xVel, double yVel, int32_t wrapX, int32_t wrapY,
-                         cudaStream_t s)
+                         const double *ghost, const double *ghostVx, const double *ghostVy, cudaStream_t s)
     {
         using namespace halcuda;
-        const size_t n = h->Length();
-        const unsigned blocks = static_cast<unsigned>((n + 255) / 256);
+        const dim3 grid = Cells64Grid(h->xDim, h->yDim);
         if (kind == kVarDiffusion)
         {
-            DiffuseVar64Kernel<<<blocks, 256, 0, s>>>(h->f64.p, h->d64.p, h->a64.p, h->b64.p, h->xDim, h->yDim, wrapX,
-                                                      wrapY);
+            const DiffuseVar64Cell cell{h->f64.p, h->d64.p, h->a64.p, h->b64.p, h->xDim, h->yDim, wrapX, wrapY};
+            Cells64Kernel<<<grid, 256, 0, s>>>(cell, h->xDim, h->yDim);
         }
         else if (kind == kAdvection)
         {
-            Advect64Kernel<<<blocks, 256, 0, s>>>(h->f64.p, h->d64.p, xVel, yVel, h->xDim, h->yDim, wrapX, wrapY);
+            const int32_t xSign = xVel > 0 ? 1 : (xVel < 0 ? -1 : 0);
+            const int32_t ySign = yVel > 0 ? 1 : (yVel < 0 ? -1 : 0);
+            const Advect64Cell cell{h->f64.p, h->d64.p, ghost, xVel, yVel, h->xDim, h->yDim, wrapX, wrapY, xSign, ySign};
+            Cells64Kernel<<<grid, 256, 0, s>>>(cell, h->xDim, h->yDim);
         }
         else
         {
-            AdvectVar64Kernel<<<blocks, 256, 0, s>>>(h->f64.p, h->d64.p, h->a64.p, h->b64.p, h->xDim, h->yDim, wrapX,
-                                                     wrapY);
+            const AdvectVar64Cell cell{h->f64.p, h->d64.p, h->a64.p, h->b64.p, ghost, ghostVx, ghostVy,
+                                       h->xDim,  h->yDim,  wrapX,    wrapY};
+            Cells64Kernel<<<grid, 256, 0, s>>>(cell, h->xDim, h->yDim);
         }
     }
 
     // Upload field, deltas and (for the per-cell forms) two per-cell arrays,
     // run one FP64 stencil, download deltas.
     int Stencil64Common(hal_cuda_diffusion *h, int kind, const double *field, double *deltas, const double *a,
-                        const double *b, double xVel, double yVel, int32_t wrapX, int32_t wrapY, const char *who)
+                        const double *b, double xVel, double yVel, int32_t wrapX, int32_t wrapY, const double *ghost,
+                        const double *ghostVx, const double *ghostVy, const char *who)
     {
         using namespace halcuda;
         HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
@@ -756,6 +813,11 @@ namespace
             HAL_TRY(h->a64.Alloc(n, "cudaMalloc(a64)"));
             HAL_TRY(h->b64.Alloc(n, "cudaMalloc(b64)"));
         }
+        const size_t ng = 2 * (static_cast<size_t>(h->xDim) + h->yDim);
+        if ((ghostVx != nullptr || ghostVy != nullptr) && h->gv64.p == nullptr)
+        {
+            HAL_TRY(h->gv64.Alloc(2 * ng, "cudaMalloc(gv64)"));
+        }
         cudaStream_t s = h->stream.Get();
         const size_t bytes = n * sizeof(double);
         HAL_TRY(CudaStatus(cudaMemcpyAsync(h->f64.p, field, bytes, cudaMemcpyHostToDevice, s), "cudaMemcpy(field)"));
@@ -765,7 +827,27 @@ namespace
             HAL_TRY(CudaStatus(cudaMemcpyAsync(h->a64.p, a, bytes, cudaMemcpyHostToDevice, s), "cudaMemcpy(x array)"));
             HAL_TRY(CudaStatus(cudaMemcpyAsync(h->b64.p, b, bytes, cudaMemcpyHostToDevice, s), "cudaMemcpy(y array)"));
         }
-        LaunchStencil64(h, kind, xVel, yVel, wrapX, wrapY, s);
+        const double *dGhost = nullptr, *dGhostVx = nullptr, *dGhostVy = nullptr;
+        if (ghost != nullptr)
+        {
+            HAL_TRY(CudaStatus(cudaMemcpyAsync(h->g64.p, ghost, ng * sizeof(double), cudaMemcpyHostToDevice, s),
+                               "cudaMemcpy(ghost)"));
+            dGhost = h->g64.p;
+        }
+        if (ghostVx != nullptr)
+        {
+            HAL_TRY(CudaStatus(cudaMemcpyAsync(h->gv64.p, ghostVx, ng * sizeof(double), cudaMemcpyHostToDevice, s),
+                               "cudaMemcpy(ghostVx)"));
+            dGhostVx = h->gv64.p;
+        }
+        if (ghostVy != nullptr)
+        {
+            HAL_TRY(CudaStatus(
+                cudaMemcpyAsync(h->gv64.p + ng, ghostVy, ng * sizeof(double), cudaMemcpyHostToDevice, s),
+                "cudaMemcpy(ghostVy)"));
+            dGhostVy = h->gv64.p + ng;
+        }
+        LaunchStencil64(h, kind, xVel, yVel, wrapX, wrapY, dGhost, dGhostVx, dGhostVy, s);
         CountLaunch();
         HAL_TRY(LaunchStatus(who));
         HAL_TRY(CudaStatus(cudaMemcpyAsync(deltas, h->d64.p, bytes, cudaMemcpyDeviceToHost, s), "cudaMemcpy(deltas)"));
@@ -778,17 +860,24 @@ extern "C" int hal_cuda_diffuse_var(hal_cuda_diffusion *h, const double *field, 
 {
     HAL_REQUIRE(h != nullptr && field != nullptr && deltas != nullptr && ratesX != nullptr && ratesY != nullptr,
                 "hal_cuda_diffuse_var: NULL argument");
-    return Stencil64Common(h, kVarDiffusion, field, deltas, ratesX, ratesY, 0.0, 0.0, wrapX, wrapY,
-                           "hal_cuda_diffuse_var");
+    return Stencil64Common(h, kVarDiffusion, field, deltas, ratesX, ratesY, 0.0, 0.0, wrapX, wrapY, nullptr, nullptr,
+                           nullptr, "hal_cuda_diffuse_var");
 }
 
 extern "C" int hal_cuda_advect(hal_cuda_diffusion *h, const double *field, double *deltas, double xVel, double yVel,
                                int32_t wrapX, int32_t wrapY)
 {
     HAL_REQUIRE(h != nullptr && field != nullptr && deltas != nullptr, "hal_cuda_advect: NULL argument");
-    HAL_REQUIRE(std::isfinite(xVel) && std::isfinite(yVel), "hal_cuda_advect: velocity must be finite");
-    return Stencil64Common(h, kAdvection, field, deltas, nullptr, nullptr, xVel, yVel, wrapX, wrapY,
-                           "hal_cuda_advect");
+    return Stencil64Common(h, kAdvection, field, deltas, nullptr, nullptr, xVel, yVel, wrapX, wrapY, nullptr, nullptr,
+                           nullptr, "hal_cuda_advect");
+}
+
+extern "C" int hal_cuda_advect_bc(hal_cuda_diffusion *h, const double *field, double *deltas, double xVel,
+                                  double yVel, int32_t wrapX, int32_t wrapY, const double *ghost)
+{
+    HAL_REQUIRE(h != nullptr && field != nullptr && deltas != nullptr, "hal_cuda_advect_bc: NULL argument");
+    return Stencil64Common(h, kAdvection, field, deltas, nullptr, nullptr, xVel, yVel, wrapX, wrapY, ghost, nullptr,
+                           nullptr, "hal_cuda_advect_bc");
 }
 
 extern "C" int hal_cuda_advect_var(hal_cuda_diffusion *h, const double *field, double *deltas, const double *xVels,
@@ -796,8 +885,18 @@ extern "C" int hal_cuda_advect_var(hal_cuda_diffusion *h, const double *field, d
 {
     HAL_REQUIRE(h != nullptr && field != nullptr && deltas != nullptr && xVels != nullptr && yVels != nullptr,
                 "hal_cuda_advect_var: NULL argument");
-    return Stencil64Common(h, kVarAdvection, field, deltas, xVels, yVels, 0.0, 0.0, wrapX, wrapY,
-                           "hal_cuda_advect_var");
+    return Stencil64Common(h, kVarAdvection, field, deltas, xVels, yVels, 0.0, 0.0, wrapX, wrapY, nullptr, nullptr,
+                           nullptr, "hal_cuda_advect_var");
+}
+
+extern "C" int hal_cuda_advect_var_bc(hal_cuda_diffusion *h, const double *field, double *deltas,
+                                      const double *xVels, const double *yVels, int32_t wrapX, int32_t wrapY,
+                                      const double *ghost, const double *ghostXVel, const double *ghostYVel)
+{
+    HAL_REQUIRE(h != nullptr && field != nullptr && deltas != nullptr && xVels != nullptr && yVels != nullptr,
+                "hal_cuda_advect_var_bc: NULL argument");
+    return Stencil64Common(h, kVarAdvection, field, deltas, xVels, yVels, 0.0, 0.0, wrapX, wrapY, ghost, ghostXVel,
+                           ghostYVel, "hal_cuda_advect_var_bc");
 }
 
 extern "C" int hal_cuda_stencil64_profile(hal_cuda_diffusion *h, int32_t kind, int32_t iters, double xVel,
@@ -820,7 +919,7 @@ extern "C" int hal_cuda_stencil64_profile(hal_cuda_diffusion *h, int32_t kind, i
     for (int32_t t = 0; t < iters && rc == HAL_CUDA_OK; t++)
     {
         cudaEventRecord(e0, s);
-        LaunchStencil64(h, kind, xVel, yVel, wrapX, wrapY, s);
+        LaunchStencil64(h, kind, xVel, yVel, wrapX, wrapY, nullptr, nullptr, nullptr, s);
         CountLaunch();
         cudaEventRecord(e1, s);
         rc = LaunchStatus("hal_cuda_stencil64_profile");

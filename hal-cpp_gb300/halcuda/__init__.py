@@ -39,7 +39,10 @@ SIGNATURES = {
     "hal_cuda_diffuse_var": (_I, [_vp, _vp, _vp, _vp, _vp, _i32, _i32]),
     "hal_cuda_advect": (_I, [_vp, _vp, _vp, _f64, _f64, _i32, _i32]),
     "hal_cuda_advect_var": (_I, [_vp, _vp, _vp, _vp, _vp, _i32, _i32]),
+    "hal_cuda_advect_bc": (_I, [_vp, _vp, _vp, _f64, _f64, _i32, _i32, _vp]),
+    "hal_cuda_advect_var_bc": (_I, [_vp, _vp, _vp, _vp, _vp, _i32, _i32, _vp, _vp, _vp]),
     "hal_cuda_stencil64_profile": (_I, [_vp, _i32, _i32, _f64, _f64, _i32, _i32, _vp]),
+    "hal_cuda_fp64_issue_rate": (_I, [_vp]),
     "hal_cuda_diffusion_set_field": (_I, [_vp, _vp, _i64]),
     "hal_cuda_diffusion_get_field": (_I, [_vp, _vp, _i64]),
     "hal_cuda_diffusion_set_source": (_I, [_vp, _vp, _i64]),
@@ -146,6 +149,13 @@ def launch_count() -> int:
     return int(lib().hal_cuda_launch_count())
 
 
+def fp64_issue_rate() -> float:
+    """Measured FP64 add issue rate of the current device (ops/s)."""
+    v = ctypes.c_double()
+    _check(lib().hal_cuda_fp64_issue_rate(ctypes.byref(v)), "fp64_issue_rate")
+    return v.value
+
+
 def _p(a):
     return None if a is None else a.ctypes.data
 
@@ -245,22 +255,42 @@ class Diffusion(_Handle):
                "diffuse_var")
         return d
 
-    def advect(self, field, deltas, xVel, yVel, wrapX, wrapY):
-        """Internal::Advection2 at a uniform velocity (upwind)."""
+    def _ghost(self, g):
+        if g is None:
+            return None
+        g = _f64(g)
+        if g.size != 2 * (self.xDim + self.yDim):
+            raise ValueError(f"ghost table of {g.size} values, expected {2 * (self.xDim + self.yDim)}")
+        return g
+
+    def advect(self, field, deltas, xVel, yVel, wrapX, wrapY, ghost=None):
+        """Internal::Advection2 at a uniform velocity (upwind); with a ghost
+        table, its Dirichlet form."""
         f = _f64(field)
         d = np.ascontiguousarray(deltas, dtype=np.float64)
         self._cells(f, d)
-        _check(lib().hal_cuda_advect(self._h, _p(f), _p(d), float(xVel), float(yVel), int(wrapX), int(wrapY)),
-               "advect")
+        g = self._ghost(ghost)
+        if g is None:
+            rc = lib().hal_cuda_advect(self._h, _p(f), _p(d), float(xVel), float(yVel), int(wrapX), int(wrapY))
+        else:
+            rc = lib().hal_cuda_advect_bc(self._h, _p(f), _p(d), float(xVel), float(yVel), int(wrapX), int(wrapY),
+                                          _p(g))
+        _check(rc, "advect")
         return d
 
-    def advect_var(self, field, deltas, xVels, yVels, wrapX, wrapY):
-        """Internal::Advection2 with per-cell velocities (upwind face fluxes)."""
+    def advect_var(self, field, deltas, xVels, yVels, wrapX, wrapY, ghost=None, ghost_vx=None, ghost_vy=None):
+        """Internal::Advection2 with per-cell velocities (upwind face fluxes);
+        with ghost tables (field, x velocity, y velocity), its Dirichlet form."""
         f, vx, vy = _f64(field), _f64(xVels), _f64(yVels)
         d = np.ascontiguousarray(deltas, dtype=np.float64)
         self._cells(f, d, vx, vy)
-        _check(lib().hal_cuda_advect_var(self._h, _p(f), _p(d), _p(vx), _p(vy), int(wrapX), int(wrapY)),
-               "advect_var")
+        gs = [self._ghost(g) for g in (ghost, ghost_vx, ghost_vy)]
+        if all(g is None for g in gs):
+            rc = lib().hal_cuda_advect_var(self._h, _p(f), _p(d), _p(vx), _p(vy), int(wrapX), int(wrapY))
+        else:
+            rc = lib().hal_cuda_advect_var_bc(self._h, _p(f), _p(d), _p(vx), _p(vy), int(wrapX), int(wrapY),
+                                              *[None if g is None else _p(g) for g in gs])
+        _check(rc, "advect_var")
         return d
 
     def stencil64_profile(self, kind, iters, xVel=0.0, yVel=0.0, wrapX=False, wrapY=False):

@@ -3,6 +3,8 @@
     python -m halcuda.profcase adi 2048 3        # 3 ADI ticks (x-sweep + y-sweep)
     python -m halcuda.profcase explicit 2048 3   # 3 fused explicit ticks
     python -m halcuda.profcase agents 2048 2     # 2 dispatches of 1M agents
+    python -m halcuda.profcase stencil64 2048 1  # FP64 per-cell rate diffusion,
+                                                 # advection, per-cell advection
 
 Each case builds the benchmark's inputs at the given grid side, runs one
 untimed warm-up launch sequence, then the requested number of individually
@@ -47,6 +49,18 @@ def main(argv):
             ag.profile(1, 1.0, 0.1)
             ms = ag.profile(iters, 1.0, 0.1)
         print(f"agents {agents} in {n}^2: " + ", ".join(f"{v*1e3:.1f}" for v in ms) + " us")
+    elif case == "stencil64":
+        rng = np.random.default_rng(12)
+        cells = n * n
+        f, d = rng.random(cells), np.zeros(cells)
+        rx, ry = rng.random(cells) * 0.24, rng.random(cells) * 0.24
+        vx, vy = rng.random(cells) - 0.5, rng.random(cells) - 0.5
+        with hal.Diffusion(n, n) as h:
+            for _ in range(iters):
+                h.diffuse_var(f, d.copy(), rx, ry, 0, 0)
+                h.advect(f, d.copy(), 0.2, -0.1, 0, 0)
+                h.advect_var(f, d.copy(), vx, vy, 0, 0)
+        print(f"stencil64 {n}^2: {iters} x (diffuse_var, advect, advect_var)")
     else:
         raise SystemExit(f"unknown case {case}")
     return 0

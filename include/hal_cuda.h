@@ -82,6 +82,13 @@ int hal_cuda_set_device(int32_t device);
  * handles).  Used by benchmarks to report their launch counts. */
 int64_t hal_cuda_launch_count(void);
 
+/* Measured FP64 add issue rate of the current device (operations per second,
+ * best of three timed launches of independent add chains on every SM).  The
+ * FP64 stencils (hal_cuda_diffuse*, hal_cuda_advect*) are bound by this rate
+ * on GB300, whose FP64 pipe is a small fraction of its FP32 one; benchmarks
+ * use it as their roofline. */
+int hal_cuda_fp64_issue_rate(double *opsPerSecond);
+
 /* ---- explicit diffusion: IDiffusionBackend2D ---------------------------- */
 
 /* GpuDiffusionBackend2D(ComputeContext&, xDim, yDim)
@@ -122,9 +129,22 @@ int hal_cuda_advect(hal_cuda_diffusion *h, const double *field, double *deltas, 
 int hal_cuda_advect_var(hal_cuda_diffusion *h, const double *field, double *deltas,
                         const double *xVels, const double *yVels, int32_t wrapX, int32_t wrapY);
 
-/* Profiling of the three FP64 stencils above: average device time (ms) of one
- * launch on the arrays the last call of that kind uploaded, over `iters`
- * individually timed launches.  Deltas accumulate on the device. */
+/* Dirichlet forms of the two advection calls, with ghost tables in the layout
+ * of the file header.  hal_cuda_advect_bc: Internal::Advection2<BCFn>
+ * (include/Hal/Pde/PDEequations.h:413-447), an off-grid upwind neighbour
+ * gives (bc - centre) * 2.  hal_cuda_advect_var_bc: Advection2<BCFn,
+ * XVelBCFn, YVelBCFn> (:720-778), the off-grid field value and velocities
+ * are the tables' values (only the x part of ghostXVel and the y part of
+ * ghostYVel are read).  A NULL table reads as 0 (the zero-flux value). */
+int hal_cuda_advect_bc(hal_cuda_diffusion *h, const double *field, double *deltas, double xVel,
+                       double yVel, int32_t wrapX, int32_t wrapY, const double *ghost);
+int hal_cuda_advect_var_bc(hal_cuda_diffusion *h, const double *field, double *deltas,
+                           const double *xVels, const double *yVels, int32_t wrapX, int32_t wrapY,
+                           const double *ghost, const double *ghostXVel, const double *ghostYVel);
+
+/* Profiling of the FP64 stencils above (zero-flux forms): average device time
+ * (ms) of one launch on the arrays the last call of that kind uploaded, over
+ * `iters` individually timed launches.  Deltas accumulate on the device. */
 #define HAL_CUDA_STENCIL_DIFFUSE_VAR 0
 #define HAL_CUDA_STENCIL_ADVECT 1
 #define HAL_CUDA_STENCIL_ADVECT_VAR 2

@@ -1212,7 +1212,12 @@ double oracle_dadi_loss_grad(const double *f0, const double *target, const doubl
 
 /* DisplacedX2D / DisplacedY2D (src/Pde/PDEequations.cpp:163-197): the value of
  * a per-cell array at a possibly off-grid neighbour, wrapped, or 0. */
-static double o_displaced_x(const double *v, int32_t x, int32_t y, int32_t xDim, int32_t yDim, int wrapX)
+/* DisplacedX2D / DisplacedY2D (src/Pde/PDEequations.cpp:163-197) and their
+ * Dirichlet forms (include/Hal/Pde/PDEequations.h:589-616): the value at an
+ * off-grid coordinate of a closed axis is 0, or the boundary value itself
+ * (not doubled) when a ghost table is given. */
+static double o_displaced_x(const double *v, int32_t x, int32_t y, int32_t xDim, int32_t yDim, int wrapX,
+                            const double *ghost)
 {
     if (o_in_dim(x, xDim))
     {
@@ -1222,12 +1227,12 @@ static double o_displaced_x(const double *v, int32_t x, int32_t y, int32_t xDim,
     {
         return v[o_wrap(x, xDim) * yDim + y];
     }
-    return 0.0;
+    return ghost != NULL ? o_ghost_x(ghost, x, y, yDim) : 0.0;
 }
 
-static double o_displaced_y(const double *v, int32_t x, int32_t y, int32_t xDim, int32_t yDim, int wrapY)
+static double o_displaced_y(const double *v, int32_t x, int32_t y, int32_t xDim, int32_t yDim, int wrapY,
+                            const double *ghost)
 {
-    (void)xDim;
     if (o_in_dim(y, yDim))
     {
         return v[x * yDim + y];
@@ -1236,7 +1241,7 @@ static double o_displaced_y(const double *v, int32_t x, int32_t y, int32_t xDim,
     {
         return v[x * yDim + o_wrap(y, yDim)];
     }
-    return 0.0;
+    return ghost != NULL ? o_ghost_y(ghost, x, y, xDim, yDim) : 0.0;
 }
 
 void oracle_diffusion2_var(const double *field, double *deltas, const double *ratesX, const double *ratesY,
@@ -1248,10 +1253,10 @@ void oracle_diffusion2_var(const double *field, double *deltas, const double *ra
         {
             int32_t i = x * yDim + y;
             double c = field[i];
-            double dp1x = ((x == xDim - 1) && !wrapX) ? o_displaced_x(ratesX, x + 1, y, xDim, yDim, wrapX) : ratesX[i];
-            double dm1x = o_displaced_x(ratesX, x - 1, y, xDim, yDim, wrapX);
-            double dp1y = ((y == yDim - 1) && !wrapY) ? o_displaced_y(ratesY, x, y + 1, xDim, yDim, wrapY) : ratesY[i];
-            double dm1y = o_displaced_y(ratesY, x, y - 1, xDim, yDim, wrapY);
+            double dp1x = ((x == xDim - 1) && !wrapX) ? o_displaced_x(ratesX, x + 1, y, xDim, yDim, wrapX, NULL) : ratesX[i];
+            double dm1x = o_displaced_x(ratesX, x - 1, y, xDim, yDim, wrapX, NULL);
+            double dp1y = ((y == yDim - 1) && !wrapY) ? o_displaced_y(ratesY, x, y + 1, xDim, yDim, wrapY, NULL) : ratesY[i];
+            double dm1y = o_displaced_y(ratesY, x, y - 1, xDim, yDim, wrapY, NULL);
             double s = o_delta_x(field, c, x + 1, y, xDim, yDim, wrapX, NULL) * dp1x;
             s += o_delta_x(field, c, x - 1, y, xDim, yDim, wrapX, NULL) * dm1x;
             s += o_delta_y(field, c, x, y + 1, xDim, yDim, wrapY, NULL) * dp1y;
@@ -1261,8 +1266,8 @@ void oracle_diffusion2_var(const double *field, double *deltas, const double *ra
     }
 }
 
-void oracle_advection2(const double *field, double *deltas, double xVel, double yVel, int32_t xDim, int32_t yDim,
-                       int wrapX, int wrapY)
+void oracle_advection2_bc(const double *field, double *deltas, double xVel, double yVel, int32_t xDim,
+                          int32_t yDim, int wrapX, int wrapY, const double *ghost)
 {
     for (int32_t x = 0; x < xDim; x++)
     {
@@ -1272,36 +1277,43 @@ void oracle_advection2(const double *field, double *deltas, double xVel, double 
             double c = field[i];
             if (xVel > 0)
             {
-                deltas[i] += o_delta_x(field, c, x - 1, y, xDim, yDim, wrapX, NULL) * xVel;
+                deltas[i] += o_delta_x(field, c, x - 1, y, xDim, yDim, wrapX, ghost) * xVel;
             }
             else if (xVel < 0)
             {
-                deltas[i] -= o_delta_x(field, c, x + 1, y, xDim, yDim, wrapX, NULL) * xVel;
+                deltas[i] -= o_delta_x(field, c, x + 1, y, xDim, yDim, wrapX, ghost) * xVel;
             }
             if (yVel > 0)
             {
-                deltas[i] += o_delta_y(field, c, x, y - 1, xDim, yDim, wrapY, NULL) * yVel;
+                deltas[i] += o_delta_y(field, c, x, y - 1, xDim, yDim, wrapY, ghost) * yVel;
             }
             else if (yVel < 0)
             {
-                deltas[i] -= o_delta_y(field, c, x, y + 1, xDim, yDim, wrapY, NULL) * yVel;
+                deltas[i] -= o_delta_y(field, c, x, y + 1, xDim, yDim, wrapY, ghost) * yVel;
             }
         }
     }
 }
 
-void oracle_advection2_var(const double *field, double *deltas, const double *xVels, const double *yVels,
-                           int32_t xDim, int32_t yDim, int wrapX, int wrapY)
+void oracle_advection2(const double *field, double *deltas, double xVel, double yVel, int32_t xDim, int32_t yDim,
+                       int wrapX, int wrapY)
+{
+    oracle_advection2_bc(field, deltas, xVel, yVel, xDim, yDim, wrapX, wrapY, NULL);
+}
+
+void oracle_advection2_var_bc(const double *field, double *deltas, const double *xVels, const double *yVels,
+                              int32_t xDim, int32_t yDim, int wrapX, int wrapY, const double *ghost,
+                              const double *ghostXVel, const double *ghostYVel)
 {
     for (int32_t x = 0; x < xDim; x++)
     {
         for (int32_t y = 0; y < yDim; y++)
         {
             int32_t i = x * yDim + y;
-            double xVelP = ((x == xDim - 1) && !wrapX) ? o_displaced_x(xVels, x + 1, y, xDim, yDim, wrapX) : xVels[i];
-            double yVelP = ((y == yDim - 1) && !wrapY) ? o_displaced_y(yVels, x, y + 1, xDim, yDim, wrapY) : yVels[i];
-            double xVelM = o_displaced_x(xVels, x - 1, y, xDim, yDim, wrapX);
-            double yVelM = o_displaced_y(yVels, x, y - 1, xDim, yDim, wrapY);
+            double xVelP = ((x == xDim - 1) && !wrapX) ? o_displaced_x(xVels, x + 1, y, xDim, yDim, wrapX, ghostXVel) : xVels[i];
+            double yVelP = ((y == yDim - 1) && !wrapY) ? o_displaced_y(yVels, x, y + 1, xDim, yDim, wrapY, ghostYVel) : yVels[i];
+            double xVelM = o_displaced_x(xVels, x - 1, y, xDim, yDim, wrapX, ghostXVel);
+            double yVelM = o_displaced_y(yVels, x, y - 1, xDim, yDim, wrapY, ghostYVel);
             double c = field[i];
             double xFluxP = 0.0, xFluxM = 0.0, yFluxP = 0.0, yFluxM = 0.0;
             if (xVelP > 0)
@@ -1310,11 +1322,11 @@ void oracle_advection2_var(const double *field, double *deltas, const double *xV
             }
             else if (xVelP < 0)
             {
-                xFluxP = xVelP * o_displaced_x(field, x + 1, y, xDim, yDim, wrapX);
+                xFluxP = xVelP * o_displaced_x(field, x + 1, y, xDim, yDim, wrapX, ghost);
             }
             if (xVelM > 0)
             {
-                xFluxM = xVelM * o_displaced_x(field, x - 1, y, xDim, yDim, wrapX);
+                xFluxM = xVelM * o_displaced_x(field, x - 1, y, xDim, yDim, wrapX, ghost);
             }
             else if (xVelM < 0)
             {
@@ -1326,11 +1338,11 @@ void oracle_advection2_var(const double *field, double *deltas, const double *xV
             }
             else if (yVelP < 0)
             {
-                yFluxP = yVelP * o_displaced_y(field, x, y + 1, xDim, yDim, wrapY);
+                yFluxP = yVelP * o_displaced_y(field, x, y + 1, xDim, yDim, wrapY, ghost);
             }
             if (yVelM > 0)
             {
-                yFluxM = yVelM * o_displaced_y(field, x, y - 1, xDim, yDim, wrapY);
+                yFluxM = yVelM * o_displaced_y(field, x, y - 1, xDim, yDim, wrapY, ghost);
             }
             else if (yVelM < 0)
             {
@@ -1339,4 +1351,10 @@ void oracle_advection2_var(const double *field, double *deltas, const double *xV
             deltas[i] += -xFluxP + xFluxM - yFluxP + yFluxM;
         }
     }
+}
+
+void oracle_advection2_var(const double *field, double *deltas, const double *xVels, const double *yVels,
+                           int32_t xDim, int32_t yDim, int wrapX, int wrapY)
+{
+    oracle_advection2_var_bc(field, deltas, xVels, yVels, xDim, yDim, wrapX, wrapY, NULL, NULL, NULL);
 }

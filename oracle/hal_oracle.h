@@ -127,6 +127,17 @@ void oracle_advection2(const double *field, double *deltas, double xVel, double 
 void oracle_advection2_var(const double *field, double *deltas, const double *xVels, const double *yVels,
                            int32_t xDim, int32_t yDim, int wrapX, int wrapY);
 
+/* Dirichlet forms: Internal::Advection2<BCFn> (include/Hal/Pde/
+ * PDEequations.h:413-447; an off-grid upwind neighbour gives
+ * (bc - centre) * 2) and Advection2<BCFn, XVelBCFn, YVelBCFn> (:720-778; the
+ * off-grid field and velocities are the boundary values themselves).  Each
+ * callable is a ghost table in the layout above; NULL reads as 0. */
+void oracle_advection2_bc(const double *field, double *deltas, double xVel, double yVel, int32_t xDim,
+                          int32_t yDim, int wrapX, int wrapY, const double *ghost);
+void oracle_advection2_var_bc(const double *field, double *deltas, const double *xVels, const double *yVels,
+                              int32_t xDim, int32_t yDim, int wrapX, int wrapY, const double *ghost,
+                              const double *ghostXVel, const double *ghostYVel);
+
 /* ---- variable-rate ADI and its adjoint -----------------------------------
  * No reference implementation exists: the step is defined from HAL's
  * variable-rate explicit stencil (src/Pde/PDEequations.cpp:199-230; the face

@@ -88,6 +88,8 @@ class Oracle(_Lib):
         L.oracle_diffusion2_var.argtypes = [vp, vp, vp, vp, i32, i32, ci, ci]
         L.oracle_advection2.argtypes = [vp, vp, f64, f64, i32, i32, ci, ci]
         L.oracle_advection2_var.argtypes = [vp, vp, vp, vp, i32, i32, ci, ci]
+        L.oracle_advection2_bc.argtypes = [vp, vp, f64, f64, i32, i32, ci, ci, vp]
+        L.oracle_advection2_var_bc.argtypes = [vp, vp, vp, vp, i32, i32, ci, ci, vp, vp, vp]
         L.oracle_dadi_step.argtypes = [vp, vp, i32, i32, ctypes.c_int, ctypes.c_int, f64, vp, vp, vp]
         L.oracle_dadi_loss_grad.argtypes = [vp, vp, vp, f64, vp, i32, i32, ctypes.c_int, ctypes.c_int,
                                             i32, vp, vp, vp, vp]
@@ -203,18 +205,30 @@ class Oracle(_Lib):
         return d
 
     @classmethod
-    def advect(cls, field, deltas, xVel, yVel, xDim, yDim, wrapX, wrapY):
+    def advect(cls, field, deltas, xVel, yVel, xDim, yDim, wrapX, wrapY, ghost=None):
         f = _f64(field)
         d = _f64(deltas).copy()
-        cls.lib().oracle_advection2(f.ctypes.data, d.ctypes.data, xVel, yVel, xDim, yDim, int(wrapX), int(wrapY))
+        if ghost is None:
+            cls.lib().oracle_advection2(f.ctypes.data, d.ctypes.data, xVel, yVel, xDim, yDim, int(wrapX), int(wrapY))
+        else:
+            g = _f64(ghost)
+            cls.lib().oracle_advection2_bc(f.ctypes.data, d.ctypes.data, xVel, yVel, xDim, yDim, int(wrapX),
+                                           int(wrapY), g.ctypes.data)
         return d
 
     @classmethod
-    def advect_var(cls, field, deltas, xVels, yVels, xDim, yDim, wrapX, wrapY):
+    def advect_var(cls, field, deltas, xVels, yVels, xDim, yDim, wrapX, wrapY, ghost=None, ghost_vx=None,
+                   ghost_vy=None):
         f, vx, vy = _f64(field), _f64(xVels), _f64(yVels)
         d = _f64(deltas).copy()
-        cls.lib().oracle_advection2_var(f.ctypes.data, d.ctypes.data, vx.ctypes.data, vy.ctypes.data, xDim, yDim,
-                                        int(wrapX), int(wrapY))
+        if ghost is None and ghost_vx is None and ghost_vy is None:
+            cls.lib().oracle_advection2_var(f.ctypes.data, d.ctypes.data, vx.ctypes.data, vy.ctypes.data, xDim,
+                                            yDim, int(wrapX), int(wrapY))
+        else:
+            gs = [None if g is None else _f64(g) for g in (ghost, ghost_vx, ghost_vy)]
+            cls.lib().oracle_advection2_var_bc(f.ctypes.data, d.ctypes.data, vx.ctypes.data, vy.ctypes.data, xDim,
+                                               yDim, int(wrapX), int(wrapY),
+                                               *[None if g is None else g.ctypes.data for g in gs])
         return d
 
     @classmethod
@@ -283,6 +297,8 @@ class Reference(_Lib):
         L.ref_diffuse_var.argtypes = [vp, vp, vp, vp, i32, i32, ci, ci]
         L.ref_advect.argtypes = [vp, vp, f64, f64, i32, i32, ci, ci]
         L.ref_advect_var.argtypes = [vp, vp, vp, vp, i32, i32, ci, ci]
+        L.ref_advect_bc.argtypes = [vp, vp, f64, f64, i32, i32, ci, ci, vp]
+        L.ref_advect_var_bc.argtypes = [vp, vp, vp, vp, i32, i32, ci, ci, vp, vp, vp]
         for name in ("ref_diffuse", "ref_diffuse_bc", "ref_diffuse_adi", "ref_diffuse_adi_bc",
                      "ref_pdegrid_run", "ref_accumulate_forces"):
             getattr(L, name).restype = ci
@@ -296,18 +312,30 @@ class Reference(_Lib):
         return d
 
     @classmethod
-    def advect(cls, field, deltas, xVel, yVel, xDim, yDim, wrapX, wrapY):
+    def advect(cls, field, deltas, xVel, yVel, xDim, yDim, wrapX, wrapY, ghost=None):
         f = _f64(field)
         d = _f64(deltas).copy()
-        _ok(cls.lib().ref_advect(f.ctypes.data, d.ctypes.data, xVel, yVel, xDim, yDim, int(wrapX), int(wrapY)))
+        if ghost is None:
+            _ok(cls.lib().ref_advect(f.ctypes.data, d.ctypes.data, xVel, yVel, xDim, yDim, int(wrapX), int(wrapY)))
+        else:
+            g = _f64(ghost)
+            _ok(cls.lib().ref_advect_bc(f.ctypes.data, d.ctypes.data, xVel, yVel, xDim, yDim, int(wrapX), int(wrapY),
+                                        g.ctypes.data))
         return d
 
     @classmethod
-    def advect_var(cls, field, deltas, xVels, yVels, xDim, yDim, wrapX, wrapY):
+    def advect_var(cls, field, deltas, xVels, yVels, xDim, yDim, wrapX, wrapY, ghost=None, ghost_vx=None,
+                   ghost_vy=None):
         f, vx, vy = _f64(field), _f64(xVels), _f64(yVels)
         d = _f64(deltas).copy()
-        _ok(cls.lib().ref_advect_var(f.ctypes.data, d.ctypes.data, vx.ctypes.data, vy.ctypes.data, xDim, yDim,
-                                     int(wrapX), int(wrapY)))
+        if ghost is None:
+            _ok(cls.lib().ref_advect_var(f.ctypes.data, d.ctypes.data, vx.ctypes.data, vy.ctypes.data, xDim, yDim,
+                                         int(wrapX), int(wrapY)))
+        else:
+            g, gx, gy = _f64(ghost), _f64(ghost_vx), _f64(ghost_vy)
+            _ok(cls.lib().ref_advect_var_bc(f.ctypes.data, d.ctypes.data, vx.ctypes.data, vy.ctypes.data, xDim,
+                                            yDim, int(wrapX), int(wrapY), g.ctypes.data, gx.ctypes.data,
+                                            gy.ctypes.data))
         return d
 
     @classmethod

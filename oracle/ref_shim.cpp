@@ -113,6 +113,29 @@ extern "C"
                      { Hal::Internal::Advection2(field, deltas, xVels, yVels, xDim, yDim, wrapX != 0, wrapY != 0); });
     }
 
+    // Hal::Internal::Advection2<BCFn> with a ghost-table callable.
+    int ref_advect_bc(const double *field, double *deltas, double xVel, double yVel, int32_t xDim, int32_t yDim,
+                      int wrapX, int wrapY, const double *ghost)
+    {
+        Quiet();
+        return Guard([&]()
+                     { Hal::Internal::Advection2(field, deltas, xVel, yVel, xDim, yDim, wrapX != 0, wrapY != 0,
+                                                 GhostBc{ghost, xDim, yDim}); });
+    }
+
+    // Hal::Internal::Advection2<BCFn, XVelBCFn, YVelBCFn> with three
+    // ghost-table callables (field, x velocity, y velocity).
+    int ref_advect_var_bc(const double *field, double *deltas, const double *xVels, const double *yVels,
+                          int32_t xDim, int32_t yDim, int wrapX, int wrapY, const double *ghost,
+                          const double *ghostXVel, const double *ghostYVel)
+    {
+        Quiet();
+        return Guard([&]()
+                     { Hal::Internal::Advection2(field, deltas, xVels, yVels, xDim, yDim, wrapX != 0, wrapY != 0,
+                                                 GhostBc{ghost, xDim, yDim}, GhostBc{ghostXVel, xDim, yDim},
+                                                 GhostBc{ghostYVel, xDim, yDim}); });
+    }
+
     int ref_diffuse(const double *field, int64_t fieldLen, double *deltas, int64_t deltasLen,
                     double diffRate, int32_t xDim, int32_t yDim, int wrapX, int wrapY)
     {

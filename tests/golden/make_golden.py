@@ -180,9 +180,12 @@ def rand_cases():
 
 def var_stencil_cases(rng):
     """Internal::Diffusion2 with per-cell rates and both Advection2 forms
-    (src/Pde/PDEequations.cpp:199-230, 380-412, 535-575)."""
+    (src/Pde/PDEequations.cpp:199-230, 380-412, 535-575), each advection form
+    also with Dirichlet ghost tables (include/Hal/Pde/PDEequations.h:413-447,
+    720-778)."""
     out = {}
     k = 0
+    grng = np.random.default_rng(8282)  # ghost tables, drawn apart so the other vectors stay as they were
     for (xd, yd) in SIZES:
         n = xd * yd
         for wx, wy in ((0, 0), (1, 1), (1, 0), (0, 1)):
@@ -202,6 +205,11 @@ def var_stencil_cases(rng):
             out[pre + "diffuse_var"] = R.diffuse_var(f, d, rx, ry, xd, yd, wx, wy)
             out[pre + "advect"] = R.advect(f, d, xv, yv, xd, yd, wx, wy)
             out[pre + "advect_var"] = R.advect_var(f, d, vx, vy, xd, yd, wx, wy)
+            # Dirichlet forms (Advection2<BCFn> and <BCFn, XVelBCFn, YVelBCFn>)
+            g, gvx, gvy = (grng.random(2 * (xd + yd)) - 0.25 for _ in range(3))
+            out[pre + "ghost"], out[pre + "ghost_vx"], out[pre + "ghost_vy"] = g, gvx, gvy
+            out[pre + "advect_bc"] = R.advect(f, d, xv, yv, xd, yd, wx, wy, ghost=g)
+            out[pre + "advect_var_bc"] = R.advect_var(f, d, vx, vy, xd, yd, wx, wy, g, gvx, gvy)
             k += 1
     out["count"] = np.array([k])
     return out

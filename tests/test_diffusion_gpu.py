@@ -53,6 +53,11 @@ def test_var_stencil_fp64_bit_exact_golden(hal, golden):
             assert np.array_equal(h.advect(f, d.copy(), xv, yv, wx, wy), g[f"c{k}_advect"]), tag
             assert np.array_equal(h.advect_var(f, d.copy(), g[f"c{k}_vx"], g[f"c{k}_vy"], wx, wy),
                                   g[f"c{k}_advect_var"]), tag
+            gh = g[f"c{k}_ghost"]
+            assert np.array_equal(h.advect(f, d.copy(), xv, yv, wx, wy, ghost=gh), g[f"c{k}_advect_bc"]), tag
+            assert np.array_equal(h.advect_var(f, d.copy(), g[f"c{k}_vx"], g[f"c{k}_vy"], wx, wy, gh,
+                                               g[f"c{k}_ghost_vx"], g[f"c{k}_ghost_vy"]),
+                                  g[f"c{k}_advect_var_bc"]), tag
 
 
 @pytest.mark.parametrize("xd,yd", [(300, 257), (1024, 1024), (1, 4099)])
@@ -72,6 +77,11 @@ def test_var_stencil_matches_oracle_large(hal, oracle, xd, yd):
                                       oracle.advect(f, d, xv, yv, xd, yd, wx, wy))
             assert np.array_equal(h.advect_var(f, d.copy(), vx, vy, wx, wy),
                                   oracle.advect_var(f, d, vx, vy, xd, yd, wx, wy))
+            gh, gvx, gvy = (rng.random(2 * (xd + yd)) - 0.3 for _ in range(3))
+            assert np.array_equal(h.advect(f, d.copy(), -0.15, 0.25, wx, wy, ghost=gh),
+                                  oracle.advect(f, d, -0.15, 0.25, xd, yd, wx, wy, ghost=gh))
+            assert np.array_equal(h.advect_var(f, d.copy(), vx, vy, wx, wy, gh, gvx, gvy),
+                                  oracle.advect_var(f, d, vx, vy, xd, yd, wx, wy, gh, gvx, gvy))
 
 
 def test_stencil64_profile_reuses_uploaded_arrays(hal, oracle):
@@ -95,7 +105,28 @@ def test_var_stencil_rejects_bad_input(hal):
         with pytest.raises(ValueError):
             h.diffuse_var(z, z.copy(), np.zeros(63), z, 0, 0)
         with pytest.raises(ValueError):
-            h.advect(z, z.copy(), float("nan"), 0.0, 0, 0)
+            h.advect_var(z, z.copy(), z, np.zeros(65), 0, 0)
+        with pytest.raises(ValueError):
+            h.advect(z, z.copy(), 0.1, 0.1, 0, 0, ghost=np.zeros(31))
+
+
+def test_advection_special_velocities(hal, oracle):
+    """Zero of either sign and NaN velocities add no term; infinite ones
+    propagate as in the reference (Advection2 validates nothing)."""
+    xd, yd = 19, 23
+    n = xd * yd
+    rng = np.random.default_rng(17)
+    f, d = rng.random(n), rng.random(n)
+    vx, vy = rng.random(n) - 0.5, rng.random(n) - 0.5
+    vx[::3], vy[::4], vx[1::5], vy[2::7] = 0.0, -0.0, np.nan, np.inf
+    with hal.Diffusion(xd, yd) as h:
+        for xv, yv in ((0.0, -0.0), (np.nan, 0.3), (-np.inf, -0.2), (1e-310, -1e-310)):
+            a = h.advect(f, d.copy(), xv, yv, 1, 0)
+            b = oracle.advect(f, d, xv, yv, xd, yd, 1, 0)
+            assert np.array_equal(a, b, equal_nan=True), (xv, yv)
+        a = h.advect_var(f, d.copy(), vx, vy, 0, 1)
+        b = oracle.advect_var(f, d, vx, vy, xd, yd, 0, 1)
+        assert np.array_equal(a.view(np.int64), b.view(np.int64))
 
 
 def test_eigenmode_decay_through_interface(hal):

@@ -43,7 +43,9 @@ def test_stencil_and_adi_golden_bit_exact(oracle, golden):
 def test_var_stencil_golden_bit_exact(oracle, golden):
     """Per-cell rate diffusion and both upwind advection forms
     (Internal::Diffusion2 / Advection2, src/Pde/PDEequations.cpp:199-230,
-    380-412, 535-575) against vectors written by the reference."""
+    380-412, 535-575), and the advection forms' Dirichlet variants
+    (include/Hal/Pde/PDEequations.h:413-447, 720-778), against vectors
+    written by the reference."""
     g = golden("varstencil")
     count = int(g["count"][0])
     assert count == 32
@@ -57,6 +59,11 @@ def test_var_stencil_golden_bit_exact(oracle, golden):
         assert np.array_equal(oracle.advect(f, d, xv, yv, xd, yd, wx, wy), g[f"c{k}_advect"]), tag
         assert np.array_equal(oracle.advect_var(f, d, g[f"c{k}_vx"], g[f"c{k}_vy"], xd, yd, wx, wy),
                               g[f"c{k}_advect_var"]), tag
+        gh = g[f"c{k}_ghost"]
+        assert np.array_equal(oracle.advect(f, d, xv, yv, xd, yd, wx, wy, ghost=gh), g[f"c{k}_advect_bc"]), tag
+        assert np.array_equal(oracle.advect_var(f, d, g[f"c{k}_vx"], g[f"c{k}_vy"], xd, yd, wx, wy, gh,
+                                                g[f"c{k}_ghost_vx"], g[f"c{k}_ghost_vy"]),
+                              g[f"c{k}_advect_var_bc"]), tag
 
 
 def test_var_stencil_conservation_kat(oracle):
