@@ -252,6 +252,8 @@ def secondary_explicit(hal, torch, stream, warm=5, iters=50):
 def secondary_agents(hal, stream, iters=20):
     from halcuda import workloads
 
+    import torch
+
     w = workloads.agent_inputs(1_000_000, N, seed=3)
     n = w["radii"].size
     with hal.Agents(N, N, n) as ag:
@@ -259,6 +261,15 @@ def secondary_agents(hal, stream, iters=20):
         ag.upload(w["positions"], w["radii"])
         ag.profile(3, 1.0, 0.1)
         ms = ag.profile(iters, 1.0, 0.1)
+        # resident SphericalAgent2D ticks: forces + vel/cap/move/friction,
+        # positions never leave the device
+        ag.step(3, 1.0, 0.1, friction=0.5, maxVel=0.5)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ag.step(iters, 1.0, 0.1, friction=0.5, maxVel=0.5)
+        e1.record(stream)
+        e1.synchronize()
+        ms_step = e0.elapsed_time(e1) / iters
     # algorithmic bytes of the whole dispatch: 28 B/agent + 16 B/bin
     bytes_tick = 28 * n + 16 * CELLS
     peak, _ = peaks()
@@ -268,6 +279,9 @@ def secondary_agents(hal, stream, iters=20):
             "ms_per_dispatch": ms[5],
             "ms_by_stage": {"count": ms[0], "scan": ms[1], "scatter": ms[2], "stabilize": ms[3],
                             "forces": ms[4]},
+            "resident_step": {"ms_per_tick": ms_step, "agents_per_s": n / (ms_step * 1e-3),
+                              "note": "hal_cuda_agents_step: dispatch + fused vel/CapVelocity/ForceMove/"
+                                      "ApplyFriction, friction 0.5, maxVel 0.5, no host copies"},
             "roofline": {"kernel": "whole dispatch", "bound": "hbm", "achieved": ach,
                          "peak": peak, "unit": "GB/s", "frac": ach / peak,
                          "traffic": None}}

@@ -187,6 +187,15 @@ namespace Hal::Cuda
         // Cell offsets (xDim*yDim + 1) and the agent order of the last binning.
         void GetBins(std::vector<int32_t> &cellOffsets, std::vector<int32_t> &bucketAgents);
 
+        // Device-resident SphericalAgent2D ticks (SphericalAgent2D.h:133-162):
+        // each tick computes the forces, then per agent vel += delta,
+        // CapVelocity(maxVel) when maxVel >= 0, ForceMove (MoveSafePT) and
+        // ApplyFriction(friction).  Upload sets the velocities to zero.
+        void SetVelocities(const std::vector<float> &velocities);
+        void Step(int32_t ticks, double interactionRad, double springConstant, bool wrapX, bool wrapY,
+                  double friction, double maxVel = -1.0);
+        void GetState(std::vector<float> &positions, std::vector<float> &velocities);
+
         hal_cuda_agents *Handle() const { return m_pHandle; }
 
     private:

@@ -327,6 +327,33 @@ namespace Hal::Cuda
         Check(hal_cuda_agents_download(m_pHandle, velocityDeltas.data(), m_count), "CudaAgentForceBackend2D::Download");
     }
 
+    void CudaAgentForceBackend2D::SetVelocities(const std::vector<float> &velocities)
+    {
+        if (velocities.size() != 2 * static_cast<size_t>(m_count))
+        {
+            std::string msg = "CudaAgentForceBackend2D::SetVelocities: two values per uploaded agent";
+            Logger::Instance().Log(LogSeverity::Error, msg);
+            throw std::invalid_argument(msg);
+        }
+        Check(hal_cuda_agents_set_velocities(m_pHandle, velocities.empty() ? nullptr : velocities.data(), m_count),
+              "CudaAgentForceBackend2D::SetVelocities");
+    }
+
+    void CudaAgentForceBackend2D::Step(int32_t ticks, double interactionRad, double springConstant, bool wrapX,
+                                       bool wrapY, double friction, double maxVel)
+    {
+        Check(hal_cuda_agents_step(m_pHandle, ticks, interactionRad, springConstant, wrapX, wrapY, friction, maxVel),
+              "CudaAgentForceBackend2D::Step");
+    }
+
+    void CudaAgentForceBackend2D::GetState(std::vector<float> &positions, std::vector<float> &velocities)
+    {
+        positions.resize(2 * static_cast<size_t>(m_count));
+        velocities.resize(2 * static_cast<size_t>(m_count));
+        Check(hal_cuda_agents_get_state(m_pHandle, positions.data(), velocities.data(), m_count),
+              "CudaAgentForceBackend2D::GetState");
+    }
+
     void CudaAgentForceBackend2D::GetBins(std::vector<int32_t> &cellOffsets, std::vector<int32_t> &bucketAgents)
     {
         cellOffsets.resize(static_cast<size_t>(m_xDim) * static_cast<size_t>(m_yDim) + 1);

@@ -360,6 +360,36 @@ namespace
         return "";
     }
 
+    // Resident SphericalAgent2D ticks: one tick's update equals the oracle's
+    // FP32 update of the tick's own deltas, bit for bit.
+    std::string AgentStep(Hal::Cuda::CudaAgentForceBackend2D &agents)
+    {
+        const int32_t n = 3000, dim = 64;
+        oracle_rand rng;
+        oracle_rand_init(&rng, 31);
+        std::vector<float> pos(2 * n), rad(n), vel(2 * n);
+        for (int32_t i = 0; i < n; i++)
+        {
+            pos[2 * i] = static_cast<float>(oracle_rand_double(&rng) * dim * 0.999);
+            pos[2 * i + 1] = static_cast<float>(oracle_rand_double(&rng) * dim * 0.999);
+            rad[i] = static_cast<float>(0.3 + 0.4 * oracle_rand_double(&rng));
+            vel[2 * i] = static_cast<float>(oracle_rand_double(&rng) - 0.5);
+            vel[2 * i + 1] = static_cast<float>(oracle_rand_double(&rng) - 0.5);
+        }
+        agents.Upload(pos, rad);
+        agents.SetVelocities(vel);
+        agents.Step(1, 1.5, 0.2, true, false, 0.7, 0.6);
+        std::vector<float> gotPos, gotVel, deltas;
+        agents.GetState(gotPos, gotVel);
+        agents.Download(deltas);
+        oracle_agents_move_f32(pos.data(), vel.data(), deltas.data(), n, dim, dim, 1, 0, 0.7f, 0.6f);
+        if (gotPos != pos || gotVel != vel)
+        {
+            return "resident agent step differs from the FP32 update of its deltas";
+        }
+        return "";
+    }
+
     // Resident ticks (PDEGrid2D semantics: decay, dense source, Dirichlet)
     // against the CPU tick, explicit and ADI.
     std::string ResidentTicks(Hal::Cuda::CudaDiffusionBackend2D &diff, Hal::Cuda::CudaAdiDiffusionBackend2D &adi)
@@ -437,6 +467,7 @@ int main()
     Run("size_mismatch_throws", [&] { return SizeMismatches(diffEig, adiEig, agents16); });
     Run("resident_ticks_match_cpu", [&] { return ResidentTicks(diffTick, adiTick); });
     Run("variable_rate_and_advection_bit_exact", [&] { return VariableStencils(diffTick); });
+    Run("resident_agent_step_bit_exact", [&] { return AgentStep(agents64); });
 
     std::printf("backend_tests: %d passed, %d failed\n", g_passed, g_failed);
     return g_failed == 0 ? 0 : 1;

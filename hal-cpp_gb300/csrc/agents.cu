@@ -282,12 +282,12 @@ namespace halcuda
 
         // Pass 4 (CpuAgentForceBackend2D.cpp:112-175) for the agent in sorted
         // slot `slot` (agent i); offsets are the cell offsets of its grid.
-        template <typename T, typename TV>
-        __device__ __forceinline__ void ForceSlot(const int32_t slot, const int32_t i,
-                                                  const int32_t *__restrict__ offsets,
-                                                  const V2<T> *__restrict__ sPos, const T *__restrict__ sRad,
-                                                  double interactionRad, T R, T k, int32_t xDim, int32_t yDim,
-                                                  int32_t wrapX, int32_t wrapY, TV *__restrict__ vel)
+        // Returns the agent's velocity delta, the sum over its neighbours.
+        template <typename T>
+        __device__ __forceinline__ V2<T> ForceSlot(const int32_t slot, const int32_t *__restrict__ offsets,
+                                                   const V2<T> *__restrict__ sPos, const T *__restrict__ sRad,
+                                                   double interactionRad, T R, T k, int32_t xDim, int32_t yDim,
+                                                   int32_t wrapX, int32_t wrapY)
         {
             const V2<T> pf = sPos[slot];
             const T px = pf.x;
@@ -381,8 +381,17 @@ namespace halcuda
                     }
                 }
             }
-            vel[2 * static_cast<int64_t>(i)] = static_cast<TV>(vx);
-            vel[2 * static_cast<int64_t>(i) + 1] = static_cast<TV>(vy);
+            V2<T> sum;
+            sum.x = vx;
+            sum.y = vy;
+            return sum;
+        }
+
+        template <typename TV, typename TVec>
+        __device__ __forceinline__ void StoreDelta(TV *__restrict__ vel, int32_t i, TVec d)
+        {
+            vel[2 * static_cast<int64_t>(i)] = static_cast<TV>(d.x);
+            vel[2 * static_cast<int64_t>(i) + 1] = static_cast<TV>(d.y);
         }
 
         // Pass 4 over cell-sorted slots: one thread per slot.
@@ -397,8 +406,100 @@ namespace halcuda
             {
                 return;
             }
-            ForceSlot<T, TV>(slot, bucket[slot], offsets, sPos, sRad, interactionRad, R, k, xDim, yDim, wrapX, wrapY,
-                             vel);
+            StoreDelta(vel, bucket[slot],
+                       ForceSlot<T>(slot, offsets, sPos, sRad, interactionRad, R, k, xDim, yDim, wrapX, wrapY));
+        }
+
+        // SphericalAgent2D's per-tick update after its forces
+        // (include/Hal/Agents/SphericalAgent2D.h:133-162) in FP32, each IEEE
+        // operation rounded to nearest with no contraction:
+        //   vel += delta;  CapVelocity(maxVel) when maxVel >= 0;
+        //   ForceMove: MoveSafePT(pos + vel) (AgentPT2D.h:157-186): a point
+        //     on the grid is taken as is; otherwise each wrapped axis wraps
+        //     (Wrap, src/MathUtil.cpp:48-53) and each closed axis whose new
+        //     coordinate left [0, dim) keeps the old one;
+        //   ApplyFriction(friction): vel *= friction.
+        struct MoveParams
+        {
+            float friction;
+            float maxVel;  // < 0: no cap
+            float xDimF, yDimF;
+            int32_t wrapX, wrapY;
+        };
+
+        __device__ __forceinline__ float WrapCoord(float v, float dim)
+        {
+            const float m = fmodf(v, dim);
+            return (m < 0.0f) ? __fadd_rn(dim, m) : m;
+        }
+
+        __device__ __forceinline__ void MoveAgent(const MoveParams &mp, float2 &p, float2 &v)
+        {
+            if (mp.maxVel >= 0.0f)
+            {
+                const float maxVelSq = __fmul_rn(mp.maxVel, mp.maxVel);
+                const float normSq = __fadd_rn(__fmul_rn(v.x, v.x), __fmul_rn(v.y, v.y));
+                if (normSq > maxVelSq)
+                {
+                    const float conv = __fdiv_rn(mp.maxVel, __fsqrt_rn(normSq));
+                    v.x = __fmul_rn(v.x, conv);
+                    v.y = __fmul_rn(v.y, conv);
+                }
+            }
+            float nx = __fadd_rn(p.x, v.x);
+            float ny = __fadd_rn(p.y, v.y);
+            const bool in = nx >= 0.0f && nx < mp.xDimF && ny >= 0.0f && ny < mp.yDimF;
+            if (!in)
+            {
+                if (mp.wrapX)
+                {
+                    nx = WrapCoord(nx, mp.xDimF);
+                }
+                else if (!(nx >= 0.0f && nx < mp.xDimF))
+                {
+                    nx = p.x;
+                }
+                if (mp.wrapY)
+                {
+                    ny = WrapCoord(ny, mp.yDimF);
+                }
+                else if (!(ny >= 0.0f && ny < mp.yDimF))
+                {
+                    ny = p.y;
+                }
+            }
+            p.x = nx;
+            p.y = ny;
+            v.x = __fmul_rn(v.x, mp.friction);
+            v.y = __fmul_rn(v.y, mp.friction);
+        }
+
+        // Forces of the resident step with the move fused in: the slot's
+        // agent adds its delta to its velocity and moves.  Positions are read
+        // from the cell-sorted copy, so writing the agent-order positions
+        // here races with no other thread.
+        __global__ void ForcesMove(const int32_t *__restrict__ bucket, const int32_t *__restrict__ offsets,
+                                   const float2 *__restrict__ sPos, const float *__restrict__ sRad, int32_t n,
+                                   double interactionRad, float R, float k, int32_t xDim, int32_t yDim,
+                                   MoveParams mp, float *__restrict__ deltas, float2 *__restrict__ pos,
+                                   float2 *__restrict__ velocity)
+        {
+            const int32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+            if (slot >= n)
+            {
+                return;
+            }
+            const int32_t i = bucket[slot];
+            const V2<float> d = ForceSlot<float>(slot, offsets, sPos, sRad, interactionRad, R, k, xDim, yDim,
+                                                 mp.wrapX, mp.wrapY);
+            StoreDelta(deltas, i, d);
+            float2 p = sPos[slot];
+            float2 v = velocity[i];
+            v.x = __fadd_rn(v.x, d.x);
+            v.y = __fadd_rn(v.y, d.y);
+            MoveAgent(mp, p, v);
+            pos[i] = p;
+            velocity[i] = v;
         }
 
         // ---- many independent wells in one pass ------------------------------
@@ -438,8 +539,9 @@ namespace halcuda
             }
             const int32_t i = bucket[slot];
             const AgentWellDev wd = wells[wellOf[i]];
-            ForceSlot<float, float>(slot, i, offsets + wd.cellBase, sPos, sRad, interactionRad, R, k, wd.xDim,
-                                    wd.yDim, wd.wrapX, wd.wrapY, vel);
+            StoreDelta(vel, i,
+                       ForceSlot<float>(slot, offsets + wd.cellBase, sPos, sRad, interactionRad, R, k, wd.xDim,
+                                        wd.yDim, wd.wrapX, wd.wrapY));
         }
     }
 
@@ -451,6 +553,7 @@ namespace halcuda
         int device = 0;
         StreamSlot stream;
         DevBuf<float> pos32, rad32, vel32;
+        DevBuf<float2> velState;  // the agents' own velocities (xVel, yVel) of the resident step
         DevBuf<double> pos64, rad64, vel64;
         DevBuf<float2> posF, sPos;
         DevBuf<double2> posD, sPosD;  // FP64 interface path
@@ -473,6 +576,8 @@ namespace halcuda
             HAL_TRY(pos32.Alloc(2 * m, "cudaMalloc(agents)"));
             HAL_TRY(rad32.Alloc(m, "cudaMalloc(agents)"));
             HAL_TRY(vel32.Alloc(2 * m, "cudaMalloc(agents)"));
+            HAL_TRY(velState.Alloc(m, "cudaMalloc(agents)"));
+            HAL_TRY(CudaStatus(cudaMemset(velState.p, 0, m * sizeof(float2)), "cudaMemset"));
             HAL_TRY(posF.Alloc(m, "cudaMalloc(agents)"));
             HAL_TRY(sPos.Alloc(m, "cudaMalloc(agents)"));
             HAL_TRY(sRad32.Alloc(m, "cudaMalloc(agents)"));
@@ -568,6 +673,27 @@ namespace halcuda
     };
 
     const int32_t *AgentsCellOffsets(const hal_cuda_agents *a, int32_t *xDim, int32_t *yDim);
+}
+
+namespace
+{
+    // One resident tick of the agents: bin, then forces with the move fused.
+    int StepOnce(halcuda::Agents &a, double R, double k, const halcuda::MoveParams &mp, cudaStream_t s)
+    {
+        using namespace halcuda;
+        HAL_TRY((a.Bin<float, float>(a.pos32.p, a.rad32.p, a.sRad32.p, s)));
+        if (a.n == 0)
+        {
+            return HAL_CUDA_OK;
+        }
+        const int T = 128;
+        const unsigned blocks = static_cast<unsigned>((a.n + T - 1) / T);
+        ForcesMove<<<blocks, T, 0, s>>>(a.bucket.p, a.offsets.p, a.sPos.p, a.sRad32.p, a.n, R, static_cast<float>(R),
+                                        static_cast<float>(k), a.xDim, a.yDim, mp, a.vel32.p,
+                                        reinterpret_cast<float2 *>(a.pos32.p), a.velState.p);
+        CountLaunch();
+        return LaunchStatus("agent forces and move");
+    }
 }
 
 using halcuda::Agents;
@@ -697,8 +823,75 @@ extern "C" int hal_cuda_agents_upload(hal_cuda_agents *h, const float *positions
                                            cudaMemcpyHostToDevice, s), "cudaMemcpy(positions)"));
         HAL_TRY(CudaStatus(cudaMemcpyAsync(h->rad32.p, radii, static_cast<size_t>(n) * sizeof(float),
                                            cudaMemcpyHostToDevice, s), "cudaMemcpy(radii)"));
+        HAL_TRY(CudaStatus(cudaMemsetAsync(h->velState.p, 0, static_cast<size_t>(n) * sizeof(float2), s),
+                           "cudaMemsetAsync(velocities)"));
     }
     return CudaStatus(cudaStreamSynchronize(s), "hal_cuda_agents_upload");
+}
+
+extern "C" int hal_cuda_agents_set_velocities(hal_cuda_agents *h, const float *velocities, int32_t n)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_agents_set_velocities: handle is NULL");
+    HAL_REQUIRE(n == h->n, "hal_cuda_agents_set_velocities: %d agents given, %d uploaded", n, h->n);
+    using namespace halcuda;
+    HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    cudaStream_t s = h->stream.Get();
+    if (n > 0)
+    {
+        const size_t bytes = static_cast<size_t>(n) * sizeof(float2);
+        HAL_TRY(CudaStatus(velocities != nullptr
+                               ? cudaMemcpyAsync(h->velState.p, velocities, bytes, cudaMemcpyHostToDevice, s)
+                               : cudaMemsetAsync(h->velState.p, 0, bytes, s),
+                           "hal_cuda_agents_set_velocities"));
+    }
+    return CudaStatus(cudaStreamSynchronize(s), "hal_cuda_agents_set_velocities");
+}
+
+extern "C" int hal_cuda_agents_get_state(hal_cuda_agents *h, float *positions, float *velocities, int32_t n)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_agents_get_state: handle is NULL");
+    HAL_REQUIRE(n == h->n, "hal_cuda_agents_get_state: %d agents requested, %d uploaded", n, h->n);
+    using namespace halcuda;
+    HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    cudaStream_t s = h->stream.Get();
+    const size_t bytes = static_cast<size_t>(n) * sizeof(float2);
+    if (n > 0 && positions != nullptr)
+    {
+        HAL_TRY(CudaStatus(cudaMemcpyAsync(positions, h->pos32.p, bytes, cudaMemcpyDeviceToHost, s),
+                           "cudaMemcpy(positions)"));
+    }
+    if (n > 0 && velocities != nullptr)
+    {
+        HAL_TRY(CudaStatus(cudaMemcpyAsync(velocities, h->velState.p, bytes, cudaMemcpyDeviceToHost, s),
+                           "cudaMemcpy(velocities)"));
+    }
+    return CudaStatus(cudaStreamSynchronize(s), "hal_cuda_agents_get_state");
+}
+
+extern "C" int hal_cuda_agents_step(hal_cuda_agents *h, int32_t ticks, double interactionRad, double springConstant,
+                                    int32_t wrapX, int32_t wrapY, double friction, double maxVel)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_agents_step: handle is NULL");
+    HAL_REQUIRE(ticks >= 0, "hal_cuda_agents_step: ticks must be >= 0");
+    HAL_REQUIRE(RadiusOk(interactionRad), "hal_cuda_agents_step: interactionRad %g outside [0, %g]", interactionRad,
+                kMaxInteractionRad);
+    HAL_REQUIRE(std::isfinite(friction), "hal_cuda_agents_step: friction must be finite");
+    HAL_REQUIRE(!std::isnan(maxVel), "hal_cuda_agents_step: maxVel is NaN");
+    using namespace halcuda;
+    HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    cudaStream_t s = h->stream.Get();
+    MoveParams mp;
+    mp.friction = static_cast<float>(friction);
+    mp.maxVel = (maxVel < 0 || std::isinf(maxVel)) ? -1.0f : static_cast<float>(maxVel);
+    mp.xDimF = static_cast<float>(h->xDim);
+    mp.yDimF = static_cast<float>(h->yDim);
+    mp.wrapX = wrapX != 0;
+    mp.wrapY = wrapY != 0;
+    for (int32_t t = 0; t < ticks; t++)
+    {
+        HAL_TRY(StepOnce(*h, interactionRad, springConstant, mp, s));
+    }
+    return HAL_CUDA_OK;
 }
 
 extern "C" int hal_cuda_agents_dispatch(hal_cuda_agents *h, double interactionRad, double springConstant,

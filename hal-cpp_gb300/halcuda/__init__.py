@@ -77,6 +77,9 @@ SIGNATURES = {
     "hal_cuda_agents_upload": (_I, [_vp, _vp, _vp, _i32]),
     "hal_cuda_agents_dispatch": (_I, [_vp, _f64, _f64, _i32, _i32]),
     "hal_cuda_agents_download": (_I, [_vp, _vp, _i32]),
+    "hal_cuda_agents_set_velocities": (_I, [_vp, _vp, _i32]),
+    "hal_cuda_agents_get_state": (_I, [_vp, _vp, _vp, _i32]),
+    "hal_cuda_agents_step": (_I, [_vp, _i32, _f64, _f64, _i32, _i32, _f64, _f64]),
     "hal_cuda_agents_get_bins": (_I, [_vp, _vp, _vp]),
     "hal_cuda_agents_profile": (_I, [_vp, _i32, _f64, _f64, _i32, _i32, _vp]),
     "hal_cuda_agents_sync": (_I, [_vp]),
@@ -467,6 +470,26 @@ class Agents(_Handle):
         out = np.empty(2 * self.n, dtype=np.float32)
         _check(lib().hal_cuda_agents_download(self._h, _p(out), self.n), "download")
         return out
+
+    def set_velocities(self, velocities=None):
+        """Each agent's (xVel, yVel), interleaved; None sets them to zero."""
+        v = None if velocities is None else _f32(velocities)
+        if v is not None and v.size != 2 * self.n:
+            raise ValueError(f"{v.size} velocity values for {self.n} agents")
+        _check(lib().hal_cuda_agents_set_velocities(self._h, _p(v), self.n), "set_velocities")
+
+    def get_state(self):
+        """(positions, velocities) of the resident agents, float32 interleaved."""
+        p = np.empty(2 * self.n, dtype=np.float32)
+        v = np.empty(2 * self.n, dtype=np.float32)
+        _check(lib().hal_cuda_agents_get_state(self._h, _p(p), _p(v), self.n), "get_state")
+        return p, v
+
+    def step(self, ticks, interactionRad, springConstant, wrapX=False, wrapY=False, friction=1.0, maxVel=-1.0):
+        """`ticks` resident ticks: forces, then vel += delta, CapVelocity
+        (maxVel >= 0), ForceMove, ApplyFriction.  Asynchronous."""
+        _check(lib().hal_cuda_agents_step(self._h, ticks, interactionRad, springConstant, int(wrapX), int(wrapY),
+                                          float(friction), float(maxVel)), "step")
 
     def profile(self, iters, interactionRad, springConstant, wrapX=False, wrapY=False):
         """Average ms per launch: count, scan, scatter, stabilize, forces, whole."""

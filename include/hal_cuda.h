@@ -284,6 +284,27 @@ int hal_cuda_agents_dispatch(hal_cuda_agents *h, double interactionRad, double s
                              int32_t wrapX, int32_t wrapY);
 int hal_cuda_agents_download(hal_cuda_agents *h, float *velocityDeltas, int32_t n);
 
+/* Device-resident agent integration (SphericalAgent2D, include/Hal/Agents/
+ * SphericalAgent2D.h:133-162; MoveSafePT, include/Hal/Agents/AgentPT2D.h:
+ * 157-186).  The handle keeps each agent's velocity (xVel, yVel) beside its
+ * position; hal_cuda_agents_upload sets the velocities to zero
+ * (DefaultInit).  One tick of hal_cuda_agents_step is a dispatch whose force
+ * kernel then updates every agent i, in FP32 with each operation rounded to
+ * nearest:
+ *   vel_i += delta_i (the velocityDeltas of the dispatch);
+ *   CapVelocity(maxVel) when maxVel >= 0 and finite;
+ *   ForceMove: pos_i + vel_i if on the grid, else per axis: wrap a wrapped
+ *     axis, keep the old coordinate of a closed axis that was left;
+ *   ApplyFriction(friction): vel_i *= friction.
+ * Positions stay on the device across ticks; the next tick bins the moved
+ * agents.  hal_cuda_agents_download still returns the last tick's deltas.
+ * Ticks are enqueued on the handle's stream; get_state synchronises. */
+int hal_cuda_agents_set_velocities(hal_cuda_agents *h, const float *velocities, int32_t n);
+int hal_cuda_agents_get_state(hal_cuda_agents *h, float *positions, float *velocities, int32_t n);
+int hal_cuda_agents_step(hal_cuda_agents *h, int32_t ticks, double interactionRad,
+                         double springConstant, int32_t wrapX, int32_t wrapY, double friction,
+                         double maxVel);
+
 /* The bins of the last dispatch: cellOffsets (xDim*yDim+1 int32, exclusive
  * prefix of per-cell counts, cellOffsets[C] == n) and bucketAgents (n int32,
  * agent indices grouped by cell, ascending within a cell) -- the scratch of

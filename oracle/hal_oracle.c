@@ -1358,3 +1358,63 @@ void oracle_advection2_var(const double *field, double *deltas, const double *xV
 {
     oracle_advection2_var_bc(field, deltas, xVels, yVels, xDim, yDim, wrapX, wrapY, NULL, NULL, NULL);
 }
+
+/* ---- agent integration step ------------------------------------------------ */
+
+/* Written once for both precisions: T is double or float, FMOD and SQRT the
+ * matching libm functions. */
+#define O_AGENTS_MOVE(NAME, T, FMOD, SQRT)                                                             \
+    void NAME(T *pos, T *vel, const T *deltas, int32_t n, int32_t xDim, int32_t yDim, int wrapX,        \
+              int wrapY, T friction, T maxVel)                                                          \
+    {                                                                                                   \
+        const T xd = (T)xDim, yd = (T)yDim;                                                             \
+        for (int32_t i = 0; i < n; i++)                                                                 \
+        {                                                                                               \
+            T vx = vel[2 * i] + deltas[2 * i];                                                          \
+            T vy = vel[2 * i + 1] + deltas[2 * i + 1];                                                  \
+            if (maxVel >= 0)                                                                            \
+            { /* CapVelocity, SphericalAgent2D.h:143-153 */                                             \
+                T maxVelSq = maxVel * maxVel;                                                           \
+                T normSq = (vx * vx) + (vy * vy);                                                       \
+                if (normSq > maxVelSq)                                                                  \
+                {                                                                                       \
+                    T conv = maxVel / SQRT(normSq);                                                     \
+                    vx *= conv;                                                                         \
+                    vy *= conv;                                                                         \
+                }                                                                                       \
+            }                                                                                           \
+            /* ForceMove -> MoveSafePT, AgentPT2D.h:157-186 */                                          \
+            T px = pos[2 * i], py = pos[2 * i + 1];                                                     \
+            T nx = px + vx, ny = py + vy;                                                               \
+            int in = (nx >= 0) && (nx < xd) && (ny >= 0) && (ny < yd);                                  \
+            if (!in)                                                                                    \
+            {                                                                                           \
+                if (wrapX)                                                                              \
+                {                                                                                       \
+                    T m = FMOD(nx, xd);                                                                 \
+                    nx = (m < 0) ? (xd + m) : m;                                                        \
+                }                                                                                       \
+                else if (!((nx >= 0) && (nx < xd)))                                                     \
+                {                                                                                       \
+                    nx = px;                                                                            \
+                }                                                                                       \
+                if (wrapY)                                                                              \
+                {                                                                                       \
+                    T m = FMOD(ny, yd);                                                                 \
+                    ny = (m < 0) ? (yd + m) : m;                                                        \
+                }                                                                                       \
+                else if (!((ny >= 0) && (ny < yd)))                                                     \
+                {                                                                                       \
+                    ny = py;                                                                            \
+                }                                                                                       \
+            }                                                                                           \
+            pos[2 * i] = nx;                                                                            \
+            pos[2 * i + 1] = ny;                                                                        \
+            /* ApplyFriction, SphericalAgent2D.h:135-141 */                                             \
+            vel[2 * i] = vx * friction;                                                                 \
+            vel[2 * i + 1] = vy * friction;                                                             \
+        }                                                                                               \
+    }
+
+O_AGENTS_MOVE(oracle_agents_move, double, fmod, sqrt)
+O_AGENTS_MOVE(oracle_agents_move_f32, float, fmodf, sqrtf)

@@ -159,6 +159,24 @@ double oracle_dadi_loss_grad(const double *f0, const double *target, const doubl
                              const double *src, int32_t xDim, int32_t yDim, int wrapX, int wrapY, int32_t steps,
                              double *fT, double *gD, double *gDecay, double *gSrc);
 
+/* ---- agent integration step --------------------------------------------------
+ * SphericalAgent2D's update after its forces (include/Hal/Agents/
+ * SphericalAgent2D.h:133-162), per agent i with velocity delta d_i:
+ *   vel += d;  CapVelocity(maxVel) when maxVel >= 0;
+ *   ForceMove = MoveSafePT(pos + vel) (include/Hal/Agents/AgentPT2D.h:157-186):
+ *     a point on the grid (GridGeometry2D::In, src/Grids/GridGeometry2D.cpp:
+ *     120-124) is taken; otherwise a wrapped axis wraps (Wrap,
+ *     src/MathUtil.cpp:48-53) and a closed axis whose coordinate left
+ *     [0, dim) keeps the old one;
+ *   ApplyFriction(friction): vel *= friction.
+ * pos and vel (2n interleaved values) are updated in place.  The double form
+ * is the reference's arithmetic; the float form is the same steps in FP32,
+ * the precision of the resident device step. */
+void oracle_agents_move(double *pos, double *vel, const double *deltas, int32_t n, int32_t xDim, int32_t yDim,
+                        int wrapX, int wrapY, double friction, double maxVel);
+void oracle_agents_move_f32(float *pos, float *vel, const float *deltas, int32_t n, int32_t xDim, int32_t yDim,
+                            int wrapX, int wrapY, float friction, float maxVel);
+
 /* ---- Hal::Rng / Hal::Rand (src/Rng.cpp, src/Rand.cpp) ----------------------
  * xoshiro256** seeded through splitmix64, plus the Marsaglia polar Gaussian
  * (src/GaussianSampler.cpp:23-47).  Used to rebuild the seeded scenes of the

@@ -88,6 +88,8 @@ class Oracle(_Lib):
         L.oracle_diffusion2_var.argtypes = [vp, vp, vp, vp, i32, i32, ci, ci]
         L.oracle_advection2.argtypes = [vp, vp, f64, f64, i32, i32, ci, ci]
         L.oracle_advection2_var.argtypes = [vp, vp, vp, vp, i32, i32, ci, ci]
+        L.oracle_agents_move.argtypes = [vp, vp, vp, i32, i32, i32, ci, ci, f64, f64]
+        L.oracle_agents_move_f32.argtypes = [vp, vp, vp, i32, i32, i32, ci, ci, ctypes.c_float, ctypes.c_float]
         L.oracle_advection2_bc.argtypes = [vp, vp, f64, f64, i32, i32, ci, ci, vp]
         L.oracle_advection2_var_bc.argtypes = [vp, vp, vp, vp, i32, i32, ci, ci, vp, vp, vp]
         L.oracle_dadi_step.argtypes = [vp, vp, i32, i32, ctypes.c_int, ctypes.c_int, f64, vp, vp, vp]
@@ -232,6 +234,24 @@ class Oracle(_Lib):
         return d
 
     @classmethod
+    def agents_move(cls, pos, vel, deltas, xDim, yDim, wrapX, wrapY, friction, maxVel, f32=False):
+        """SphericalAgent2D's update after its forces; returns (pos, vel).
+        f32 runs the same steps in float, the precision of the device step."""
+        if f32:
+            p = np.array(pos, dtype=np.float32)
+            v = np.array(vel, dtype=np.float32)
+            d = np.ascontiguousarray(deltas, dtype=np.float32)
+            cls.lib().oracle_agents_move_f32(p.ctypes.data, v.ctypes.data, d.ctypes.data, p.size // 2, xDim, yDim,
+                                             int(wrapX), int(wrapY), float(friction), float(maxVel))
+        else:
+            p = np.array(pos, dtype=np.float64)
+            v = np.array(vel, dtype=np.float64)
+            d = _f64(deltas)
+            cls.lib().oracle_agents_move(p.ctypes.data, v.ctypes.data, d.ctypes.data, p.size // 2, xDim, yDim,
+                                         int(wrapX), int(wrapY), float(friction), float(maxVel))
+        return p, v
+
+    @classmethod
     def dadi_step(cls, field, D, xDim, yDim, wrapX=False, wrapY=False, decay=0.0, src=None):
         """One variable-rate ADI step; returns (f', w)."""
         f = _f64(field)
@@ -297,6 +317,7 @@ class Reference(_Lib):
         L.ref_diffuse_var.argtypes = [vp, vp, vp, vp, i32, i32, ci, ci]
         L.ref_advect.argtypes = [vp, vp, f64, f64, i32, i32, ci, ci]
         L.ref_advect_var.argtypes = [vp, vp, vp, vp, i32, i32, ci, ci]
+        L.ref_agents_move.argtypes = [vp, vp, vp, i32, i32, i32, ci, ci, f64, f64]
         L.ref_advect_bc.argtypes = [vp, vp, f64, f64, i32, i32, ci, ci, vp]
         L.ref_advect_var_bc.argtypes = [vp, vp, vp, vp, i32, i32, ci, ci, vp, vp, vp]
         for name in ("ref_diffuse", "ref_diffuse_bc", "ref_diffuse_adi", "ref_diffuse_adi_bc",
@@ -337,6 +358,15 @@ class Reference(_Lib):
                                             yDim, int(wrapX), int(wrapY), g.ctypes.data, gx.ctypes.data,
                                             gy.ctypes.data))
         return d
+
+    @classmethod
+    def agents_move(cls, pos, vel, deltas, xDim, yDim, wrapX, wrapY, friction, maxVel):
+        p = np.array(pos, dtype=np.float64)
+        v = np.array(vel, dtype=np.float64)
+        d = _f64(deltas)
+        _ok(cls.lib().ref_agents_move(p.ctypes.data, v.ctypes.data, d.ctypes.data, p.size // 2, xDim, yDim,
+                                      int(wrapX), int(wrapY), float(friction), float(maxVel)))
+        return p, v
 
     @classmethod
     def diffuse(cls, field, deltas, r, xDim, yDim, wrapX, wrapY, ghost=None):

@@ -7,6 +7,8 @@
 // itself: Hal::CpuDiffusionBackend2D, Hal::CpuAdiDiffusionBackend2D,
 // Hal::CpuAgentForceBackend2D, Hal::PDEGrid2D and Hal::Rand.  Nothing here is
 // part of the product.
+#include "Hal/Agents/SphericalAgent2D.h"
+#include "Hal/Grids/AgentGrid2D.h"
 #include "Hal/Grids/PDEGrid2D.h"
 #include "Hal/Pde/ADIequations.h"
 #include "Hal/Pde/CpuAdiDiffusionBackend2D.h"
@@ -84,6 +86,28 @@ namespace
     }
 }
 
+// A minimal off-lattice model on the reference's own agent grid, as in its
+// tests (tests/SphericalAgentTests.cpp:9-36).
+class ShimCellGrid;
+
+class ShimCell : public Hal::SphericalAgent2D<ShimCellGrid>
+{
+public:
+    explicit ShimCell(ShimCellGrid *pGrid)
+        : Hal::SphericalAgent2D<ShimCellGrid>(pGrid)
+    {
+    }
+};
+
+class ShimCellGrid : public Hal::AgentGrid2D<ShimCell, ShimCellGrid>
+{
+public:
+    ShimCellGrid(int32_t xDim, int32_t yDim, bool wrapX, bool wrapY)
+        : Hal::AgentGrid2D<ShimCell, ShimCellGrid>(xDim, yDim, wrapX, wrapY)
+    {
+    }
+};
+
 extern "C"
 {
     // IDiffusionBackend2D::Diffuse through Hal::CpuDiffusionBackend2D.
@@ -134,6 +158,37 @@ extern "C"
                      { Hal::Internal::Advection2(field, deltas, xVels, yVels, xDim, yDim, wrapX != 0, wrapY != 0,
                                                  GhostBc{ghost, xDim, yDim}, GhostBc{ghostXVel, xDim, yDim},
                                                  GhostBc{ghostYVel, xDim, yDim}); });
+    }
+
+    // One agent update of a SphericalAgent2D model after its forces
+    // (include/Hal/Agents/SphericalAgent2D.h:133-162): SetVelocity(vel +
+    // delta), CapVelocity(maxVel) when maxVel >= 0, ForceMove (MoveSafePT),
+    // ApplyFriction(friction).  Each agent is placed alone on the grid, moved
+    // and disposed of, so the agents do not interact here.
+    int ref_agents_move(double *pos, double *vel, const double *deltas, int32_t n, int32_t xDim, int32_t yDim,
+                        int wrapX, int wrapY, double friction, double maxVel)
+    {
+        Quiet();
+        return Guard([&]()
+                     {
+            ShimCellGrid grid(xDim, yDim, wrapX != 0, wrapY != 0);
+            for (int32_t i = 0; i < n; i++)
+            {
+                ShimCell &a = grid.NewAgentPT(pos[2 * i], pos[2 * i + 1]);
+                a.DefaultInit(0.5);
+                a.SetVelocity(vel[2 * i] + deltas[2 * i], vel[2 * i + 1] + deltas[2 * i + 1]);
+                if (maxVel >= 0)
+                {
+                    a.CapVelocity(maxVel);
+                }
+                a.ForceMove();
+                a.ApplyFriction(friction);
+                pos[2 * i] = a.Xpt();
+                pos[2 * i + 1] = a.Ypt();
+                vel[2 * i] = a.XVel();
+                vel[2 * i + 1] = a.YVel();
+                a.Dispose();
+            } });
     }
 
     int ref_diffuse(const double *field, int64_t fieldLen, double *deltas, int64_t deltasLen,

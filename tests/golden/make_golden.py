@@ -215,6 +215,33 @@ def var_stencil_cases(rng):
     return out
 
 
+def agent_move_cases(rng):
+    """SphericalAgent2D's update after its forces: SetVelocity(vel + delta),
+    CapVelocity, ForceMove (MoveSafePT), ApplyFriction
+    (include/Hal/Agents/SphericalAgent2D.h:133-162, AgentPT2D.h:157-186), run
+    by the reference's own agent grid.  Agents start near the edges as well,
+    so moves leave the grid on wrapped and closed axes."""
+    out = {}
+    cases = [(17, 29, 0, 0, 0.5, -1.0), (40, 9, 1, 1, 1.0, 0.8), (1, 7, 1, 0, 0.0, 2.0), (64, 64, 0, 1, 0.9, 0.0),
+             (33, 5, 1, 1, 0.25, 1e9), (5, 33, 0, 0, 1.0, 1.5)]
+    for k, (xd, yd, wx, wy, fr, mv) in enumerate(cases):
+        n = 400
+        pos = np.stack([rng.random(n) * xd, rng.random(n) * yd], 1)
+        edge = rng.random(n) < 0.3  # a third start within one cell of an edge
+        pos[edge, 0] = np.where(rng.random(edge.sum()) < 0.5, rng.random(edge.sum()),
+                                xd - rng.random(edge.sum()))
+        pos = np.minimum(pos, np.array([xd, yd]) * (1 - 1e-9)).ravel()
+        vel = (rng.random(2 * n) - 0.5) * 2.0
+        dv = (rng.random(2 * n) - 0.5) * 2.0
+        pre = f"c{k}_"
+        out[pre + "dims"] = np.array([xd, yd, wx, wy], dtype=np.int32)
+        out[pre + "params"] = np.array([fr, mv])
+        out[pre + "pos"], out[pre + "vel"], out[pre + "dv"] = pos, vel, dv
+        out[pre + "pos_out"], out[pre + "vel_out"] = R.agents_move(pos, vel, dv, xd, yd, wx, wy, fr, mv)
+    out["count"] = np.array([len(cases)])
+    return out
+
+
 def main():
     pyoracle.build(ref=True)
     if not R.available():
@@ -225,7 +252,8 @@ def main():
     np.savez_compressed(os.path.join(HERE, "agents.npz"), **agent_cases(rng))
     np.savez_compressed(os.path.join(HERE, "rand.npz"), **rand_cases())
     np.savez_compressed(os.path.join(HERE, "varstencil.npz"), **var_stencil_cases(np.random.default_rng(8181)))
-    for name in ("stencil", "ticks", "agents", "rand", "varstencil"):
+    np.savez_compressed(os.path.join(HERE, "agentmove.npz"), **agent_move_cases(np.random.default_rng(9191)))
+    for name in ("stencil", "ticks", "agents", "rand", "varstencil", "agentmove"):
         p = os.path.join(HERE, name + ".npz")
         print(f"{p}: {os.path.getsize(p)} bytes")
 

@@ -83,6 +83,55 @@ def test_var_stencil_conservation_kat(oracle):
     assert not oracle.diffuse_var(np.full(n, 2.5), z, rx, ry, xd, yd, 0, 0).any()
 
 
+def test_agent_move_golden_bit_exact(oracle, golden):
+    """SphericalAgent2D's update after its forces (SetVelocity, CapVelocity,
+    ForceMove -> MoveSafePT, ApplyFriction) against the reference's agent
+    grid, bit for bit."""
+    g = golden("agentmove")
+    for k in range(int(g["count"][0])):
+        xd, yd, wx, wy = (int(v) for v in g[f"c{k}_dims"])
+        fr, mv = (float(v) for v in g[f"c{k}_params"])
+        p, v = oracle.agents_move(g[f"c{k}_pos"], g[f"c{k}_vel"], g[f"c{k}_dv"], xd, yd, wx, wy, fr, mv)
+        assert np.array_equal(p, g[f"c{k}_pos_out"]), k
+        assert np.array_equal(v, g[f"c{k}_vel_out"]), k
+
+
+def test_agent_move_kat(oracle):
+    """The reference's own checks (tests/SphericalAgentTests.cpp:88-103):
+    ApplyFriction(0.5) halves (3, 4); CapVelocity(2) brings |(3, 4)| to 2.
+    And MoveSafePT: leaving a closed edge keeps the coordinate, leaving a
+    wrapped edge wraps it."""
+    z = np.zeros(2)
+    _, v = oracle.agents_move([5.0, 5.0], [3.0, 4.0], z, 100, 100, 0, 0, 0.5, -1.0)
+    assert np.allclose(v, [1.5, 2.0])
+    _, v = oracle.agents_move([5.0, 5.0], [3.0, 4.0], z, 100, 100, 0, 0, 1.0, 2.0)
+    assert abs(math.hypot(*v) - 2.0) < 1e-12
+    p, _ = oracle.agents_move([9.5, 5.0], [1.0, 0.25], z, 10, 10, 0, 0, 1.0, -1.0)
+    assert np.array_equal(p, [9.5, 5.25])
+    p, _ = oracle.agents_move([9.5, 5.0], [1.0, 0.25], z, 10, 10, 1, 0, 1.0, -1.0)
+    assert np.array_equal(p, [0.5, 5.25])
+    p, _ = oracle.agents_move([0.25, 0.5], [-0.5, -1.0], z, 10, 10, 1, 1, 1.0, -1.0)
+    assert np.array_equal(p, [9.75, 9.5])
+    for f32 in (False, True):
+        p, v = oracle.agents_move([2.0, 3.0], [0.5, -0.5], [0.25, 0.25], 10, 10, 0, 0, 0.0, -1.0, f32=f32)
+        assert np.array_equal(p, [2.75, 2.75]) and not v.any()
+
+
+def test_agent_move_f32_tracks_f64(oracle):
+    """The FP32 form takes the same branches as the FP64 one away from the
+    edges and agrees to float rounding."""
+    rng = np.random.default_rng(2)
+    n, xd, yd = 5000, 128, 96
+    pos = np.stack([4 + rng.random(n) * (xd - 8), 4 + rng.random(n) * (yd - 8)], 1).ravel()
+    pos = pos.astype(np.float32).astype(np.float64)
+    vel = ((rng.random(2 * n) - 0.5) * 2).astype(np.float32).astype(np.float64)
+    dv = ((rng.random(2 * n) - 0.5) * 2).astype(np.float32).astype(np.float64)
+    p64, v64 = oracle.agents_move(pos, vel, dv, xd, yd, 1, 0, 0.8, 1.2)
+    p32, v32 = oracle.agents_move(pos, vel, dv, xd, yd, 1, 0, 0.8, 1.2, f32=True)
+    assert np.max(np.abs(p32 - p64)) <= 2e-5
+    assert np.max(np.abs(v32 - v64)) <= 2e-6
+
+
 def test_tick_golden_bit_exact(oracle, golden):
     g = golden("ticks")
     xd, yd, r, decay, ticks = g["exp_params"]
@@ -275,6 +324,12 @@ def test_restatement_matches_reference_library_random(oracle):
                               R.advect(f, d, 0.25, -0.125, xd, yd, wx, wy))
         assert np.array_equal(oracle.advect_var(f, d, vx, vy, xd, yd, wx, wy),
                               R.advect_var(f, d, vx, vy, xd, yd, wx, wy))
+        m = 50
+        mpos = np.stack([rng.random(m) * xd, rng.random(m) * yd], 1).ravel() * (1 - 1e-9)
+        mvel, mdv = rng.random(2 * m) - 0.5, (rng.random(2 * m) - 0.5) * 3
+        a = oracle.agents_move(mpos, mvel, mdv, xd, yd, wx, wy, 0.7, 1.1)
+        b = R.agents_move(mpos, mvel, mdv, xd, yd, wx, wy, 0.7, 1.1)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
         n = int(rng.integers(0, 300))
         pos = (rng.random(2 * n) * max(xd, yd)).astype(np.float32).astype(np.float64)
         rad = 0.3 + rng.random(n) * 0.5
