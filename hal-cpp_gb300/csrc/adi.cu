@@ -1595,6 +1595,12 @@ struct hal_cuda_adi : public Adi
 {
 };
 
+void halcuda::AdiDims(const hal_cuda_adi *h, int32_t *xDim, int32_t *yDim)
+{
+    *xDim = h->xDim;
+    *yDim = h->yDim;
+}
+
 extern "C" int hal_cuda_adi_create(int32_t xDim, int32_t yDim, hal_cuda_adi **out)
 {
     HAL_REQUIRE(out != nullptr, "hal_cuda_adi_create: out is NULL");

@@ -27,6 +27,10 @@ namespace halcuda
     // Device selected for new handles on this thread.
     int CurrentDevice();
 
+    // Grid sizes of the resident handles (for the on-disk format).
+    void DiffusionDims(const hal_cuda_diffusion *h, int32_t *xDim, int32_t *yDim);
+    void AdiDims(const hal_cuda_adi *h, int32_t *xDim, int32_t *yDim);
+
     // Maps a CUDA error to a status, recording the message.
     inline int CudaStatus(cudaError_t e, const char *what)
     {

@@ -688,6 +688,12 @@ struct hal_cuda_diffusion : public Diffusion
 {
 };
 
+void halcuda::DiffusionDims(const hal_cuda_diffusion *h, int32_t *xDim, int32_t *yDim)
+{
+    *xDim = h->xDim;
+    *yDim = h->yDim;
+}
+
 extern "C" int hal_cuda_diffusion_create(int32_t xDim, int32_t yDim, hal_cuda_diffusion **out)
 {
     HAL_REQUIRE(out != nullptr, "hal_cuda_diffusion_create: out is NULL");

@@ -54,6 +54,13 @@ SIGNATURES = {
     "hal_cuda_diffusion_sync": (_I, [_vp]),
     "hal_cuda_diffusion_stream": (_vp, [_vp]),
     "hal_cuda_diffusion_set_stream": (_I, [_vp, _vp]),
+    "hal_cuda_pdegrid2d_write": (_I, [ctypes.c_char_p, _i32, _i32, _i32, _i32, _i32, _vp, _vp]),
+    "hal_cuda_pdegrid2d_read_header": (_I, [ctypes.c_char_p, _vp, _vp, _vp, _vp, _vp]),
+    "hal_cuda_pdegrid2d_read": (_I, [ctypes.c_char_p, _i32, _i32, _vp, _vp]),
+    "hal_cuda_diffusion_save": (_I, [_vp, ctypes.c_char_p, _i32, _i32, _i32]),
+    "hal_cuda_diffusion_load": (_I, [_vp, ctypes.c_char_p, _vp, _vp, _vp]),
+    "hal_cuda_adi_save": (_I, [_vp, ctypes.c_char_p, _i32, _i32, _i32]),
+    "hal_cuda_adi_load": (_I, [_vp, ctypes.c_char_p, _vp, _vp, _vp]),
     "hal_cuda_adi_create": (_I, [_i32, _i32, _vp]),
     "hal_cuda_adi_destroy": (_I, [_vp]),
     "hal_cuda_diffuse_adi": (_I, [_vp, _vp, _i64, _vp, _i64, _f64, _i32, _i32, _i32, _i32]),
@@ -150,6 +157,39 @@ def device_count() -> int:
 
 def launch_count() -> int:
     return int(lib().hal_cuda_launch_count())
+
+
+def _path(path) -> bytes:
+    return os.fsencode(path)
+
+
+def pdegrid2d_write(path, xDim, yDim, wrapX, wrapY, updateCt, field, deltas=None):
+    """Writes a grid state in PDEGrid2D's on-disk format (SavePDEGrid2D)."""
+    f = _f64(field)
+    d = None if deltas is None else _f64(deltas)
+    n = xDim * yDim
+    if f.size != n or (d is not None and d.size != n):
+        raise ValueError(f"field/deltas must hold {n} values")
+    _check(lib().hal_cuda_pdegrid2d_write(_path(path), xDim, yDim, int(wrapX), int(wrapY), updateCt, _p(f),
+                                          _p(d)), "pdegrid2d_write")
+
+
+def pdegrid2d_read(path):
+    """Reads a PDEGrid2D file: dict of xDim, yDim, wrapX, wrapY, updateCt,
+    field, deltas (LoadPDEGrid2D)."""
+    v = [ctypes.c_int32() for _ in range(5)]
+    _check(lib().hal_cuda_pdegrid2d_read_header(_path(path), *[ctypes.byref(x) for x in v]), "pdegrid2d_read")
+    xd, yd, wx, wy, u = (x.value for x in v)
+    f = np.empty(xd * yd, dtype=np.float64)
+    d = np.empty(xd * yd, dtype=np.float64)
+    _check(lib().hal_cuda_pdegrid2d_read(_path(path), xd, yd, _p(f), _p(d)), "pdegrid2d_read")
+    return {"xDim": xd, "yDim": yd, "wrapX": bool(wx), "wrapY": bool(wy), "updateCt": u, "field": f, "deltas": d}
+
+
+def _load_resident(fn, h, path):
+    v = [ctypes.c_int32() for _ in range(3)]
+    _check(fn(h, _path(path), *[ctypes.byref(x) for x in v]), "load")
+    return bool(v[0].value), bool(v[1].value), v[2].value
 
 
 def fp64_issue_rate() -> float:
@@ -296,6 +336,15 @@ class Diffusion(_Handle):
         _check(rc, "advect_var")
         return d
 
+    def save(self, path, wrapX=False, wrapY=False, updateCt=0):
+        """The resident field in PDEGrid2D's on-disk format."""
+        _check(lib().hal_cuda_diffusion_save(self._h, _path(path), int(wrapX), int(wrapY), updateCt), "save")
+
+    def load(self, path):
+        """Loads a PDEGrid2D file into the resident field; returns (wrapX,
+        wrapY, updateCt)."""
+        return _load_resident(lib().hal_cuda_diffusion_load, self._h, path)
+
     def stencil64_profile(self, kind, iters, xVel=0.0, yVel=0.0, wrapX=False, wrapY=False):
         """Average device ms of one FP64 stencil launch of `kind` (STENCIL_*)
         on the arrays the last call of that kind uploaded."""
@@ -382,6 +431,15 @@ class Adi(_Handle):
         out = np.empty(self.xDim * self.yDim, dtype=np.float32)
         _check(lib().hal_cuda_adi_get_field(self._h, _p(out), out.size), "get_field")
         return out
+
+    def save(self, path, wrapX=False, wrapY=False, updateCt=0):
+        """The resident field in PDEGrid2D's on-disk format."""
+        _check(lib().hal_cuda_adi_save(self._h, _path(path), int(wrapX), int(wrapY), updateCt), "save")
+
+    def load(self, path):
+        """Loads a PDEGrid2D file into the resident field; returns (wrapX,
+        wrapY, updateCt)."""
+        return _load_resident(lib().hal_cuda_adi_load, self._h, path)
 
     def set_source(self, dense):
         d = _f32(dense)

@@ -323,6 +323,37 @@ int hal_cuda_agents_sync(hal_cuda_agents *h);
 void *hal_cuda_agents_stream(hal_cuda_agents *h);
 int hal_cuda_agents_set_stream(hal_cuda_agents *h, void *stream);
 
+/* ---- on-disk format: SavePDEGrid2D / LoadPDEGrid2D ------------------------
+ * (src/Grids/PDEGridSerialization.cpp:34-62, through BinaryWriter /
+ * BinaryReader): raw native-endian int32 xDim, int32 yDim, one byte each for
+ * wrapX and wrapY, int32 updateCt, then xDim*yDim doubles of field and as
+ * many of pending deltas, in HAL's layout.  Files are byte-identical to the
+ * reference's.  Reads fail with EINVAL on a short read or invalid
+ * dimensions (Internal::CheckLoadedDims, src/Grids/GridSerialization.cpp:
+ * 14-32).  The write / read calls are host-only and need no GPU. */
+int hal_cuda_pdegrid2d_write(const char *path, int32_t xDim, int32_t yDim, int32_t wrapX,
+                             int32_t wrapY, int32_t updateCt, const double *field,
+                             const double *deltas); /* deltas NULL: zeros */
+int hal_cuda_pdegrid2d_read_header(const char *path, int32_t *xDim, int32_t *yDim, int32_t *wrapX,
+                                   int32_t *wrapY, int32_t *updateCt);
+/* EINVAL unless the file's grid is xDim x yDim; deltas may be NULL. */
+int hal_cuda_pdegrid2d_read(const char *path, int32_t xDim, int32_t yDim, double *field,
+                            double *deltas);
+
+/* Checkpoint / resume of a resident field.  A resident tick commits its own
+ * deltas, so save writes zero deltas; the wrap flags and the update count
+ * (PDEGrid2D::UpdateCt) are the caller's.  load needs the handle's grid size
+ * and returns ENOTSUP for a file with pending deltas; wrapX, wrapY and
+ * updateCt may be NULL. */
+int hal_cuda_diffusion_save(hal_cuda_diffusion *h, const char *path, int32_t wrapX, int32_t wrapY,
+                            int32_t updateCt);
+int hal_cuda_diffusion_load(hal_cuda_diffusion *h, const char *path, int32_t *wrapX, int32_t *wrapY,
+                            int32_t *updateCt);
+int hal_cuda_adi_save(hal_cuda_adi *h, const char *path, int32_t wrapX, int32_t wrapY,
+                      int32_t updateCt);
+int hal_cuda_adi_load(hal_cuda_adi *h, const char *path, int32_t *wrapX, int32_t *wrapY,
+                      int32_t *updateCt);
+
 /* ---- batched wells: many independent simulations per launch -------------
  * MultiWellExperiment::Step / StepMultiThread
  * (include/Hal/Tools/MultiWellExperiment.h:83-103) advance independent wells

@@ -318,6 +318,8 @@ class Reference(_Lib):
         L.ref_advect.argtypes = [vp, vp, f64, f64, i32, i32, ci, ci]
         L.ref_advect_var.argtypes = [vp, vp, vp, vp, i32, i32, ci, ci]
         L.ref_agents_move.argtypes = [vp, vp, vp, i32, i32, i32, ci, ci, f64, f64]
+        L.ref_pdegrid2d_save.argtypes = [ctypes.c_char_p, i32, i32, ci, ci, i32, vp, vp]
+        L.ref_pdegrid2d_load.argtypes = [ctypes.c_char_p, vp, vp, vp, vp, ctypes.c_int64]
         L.ref_advect_bc.argtypes = [vp, vp, f64, f64, i32, i32, ci, ci, vp]
         L.ref_advect_var_bc.argtypes = [vp, vp, vp, vp, i32, i32, ci, ci, vp, vp, vp]
         for name in ("ref_diffuse", "ref_diffuse_bc", "ref_diffuse_adi", "ref_diffuse_adi_bc",
@@ -367,6 +369,27 @@ class Reference(_Lib):
         _ok(cls.lib().ref_agents_move(p.ctypes.data, v.ctypes.data, d.ctypes.data, p.size // 2, xDim, yDim,
                                       int(wrapX), int(wrapY), float(friction), float(maxVel)))
         return p, v
+
+    @classmethod
+    def pdegrid2d_save(cls, path, xDim, yDim, wrapX, wrapY, updateCt, field, deltas):
+        f, d = _f64(field), _f64(deltas)
+        _ok(cls.lib().ref_pdegrid2d_save(os.fsencode(path), xDim, yDim, int(wrapX), int(wrapY), updateCt,
+                                         f.ctypes.data, d.ctypes.data))
+
+    @classmethod
+    def pdegrid2d_load(cls, path, cap=1 << 22):
+        """LoadPDEGrid2D: (xDim, yDim, wrapX, wrapY, updateCt, field, deltas);
+        raises RuntimeError where the reference throws."""
+        dims = np.zeros(4, dtype=np.int32)
+        u = np.zeros(1, dtype=np.int32)
+        f = np.zeros(cap)
+        d = np.zeros(cap)
+        rc = cls.lib().ref_pdegrid2d_load(os.fsencode(path), dims.ctypes.data, u.ctypes.data, f.ctypes.data,
+                                          d.ctypes.data, cap)
+        if rc != 0:
+            raise RuntimeError(f"LoadPDEGrid2D failed ({rc})")
+        n = int(dims[0]) * int(dims[1])
+        return int(dims[0]), int(dims[1]), bool(dims[2]), bool(dims[3]), int(u[0]), f[:n].copy(), d[:n].copy()
 
     @classmethod
     def diffuse(cls, field, deltas, r, xDim, yDim, wrapX, wrapY, ghost=None):

@@ -10,6 +10,7 @@
 #include "Hal/Agents/SphericalAgent2D.h"
 #include "Hal/Grids/AgentGrid2D.h"
 #include "Hal/Grids/PDEGrid2D.h"
+#include "Hal/Grids/PDEGridSerialization.h"
 #include "Hal/Pde/ADIequations.h"
 #include "Hal/Pde/CpuAdiDiffusionBackend2D.h"
 #include "Hal/Pde/CpuDiffusionBackend2D.h"
@@ -189,6 +190,49 @@ extern "C"
                 vel[2 * i + 1] = a.YVel();
                 a.Dispose();
             } });
+    }
+
+    // Hal::SavePDEGrid2D of a grid in the given state, through BinaryWriter.
+    int ref_pdegrid2d_save(const char *path, int32_t xDim, int32_t yDim, int wrapX, int wrapY, int32_t updateCt,
+                           const double *field, const double *deltas)
+    {
+        Quiet();
+        return Guard([&]()
+                     {
+            const size_t n = static_cast<size_t>(xDim) * static_cast<size_t>(yDim);
+            Hal::PDEGrid2D grid(xDim, yDim, wrapX != 0, wrapY != 0);
+            grid.SetState(std::vector<double>(field, field + n), std::vector<double>(deltas, deltas + n), updateCt);
+            Hal::BinaryWriter writer(path);
+            Hal::SavePDEGrid2D(writer, grid);
+            if (!writer.IsGood())
+            {
+                throw std::runtime_error("write failed");
+            } });
+    }
+
+    // Hal::LoadPDEGrid2D: the grid's sizes, flags, update count, field and
+    // deltas (field/deltas hold at most cap values).
+    int ref_pdegrid2d_load(const char *path, int32_t *dims, int32_t *updateCt, double *field, double *deltas,
+                           int64_t cap)
+    {
+        Quiet();
+        return Guard([&]()
+                     {
+            Hal::BinaryReader reader(path);
+            Hal::PDEGrid2D grid = Hal::LoadPDEGrid2D(reader);
+            dims[0] = grid.Xdim();
+            dims[1] = grid.Ydim();
+            dims[2] = grid.IsWrapX();
+            dims[3] = grid.IsWrapY();
+            *updateCt = grid.UpdateCt();
+            const std::vector<double> &f = grid.GetField();
+            const std::vector<double> &d = grid.GetDeltas();
+            if (static_cast<int64_t>(f.size()) > cap)
+            {
+                throw std::runtime_error("grid larger than the buffers");
+            }
+            std::memcpy(field, f.data(), f.size() * sizeof(double));
+            std::memcpy(deltas, d.data(), d.size() * sizeof(double)); });
     }
 
     int ref_diffuse(const double *field, int64_t fieldLen, double *deltas, int64_t deltasLen,

@@ -242,6 +242,18 @@ def agent_move_cases(rng):
     return out
 
 
+def pdegrid_file():
+    """A PDEGrid2D file written by the reference's SavePDEGrid2D
+    (src/Grids/PDEGridSerialization.cpp:34-45): 13 x 7, wrapX only, update
+    count 42, a random field and pending deltas."""
+    rng = np.random.default_rng(7171)
+    f = rng.random(13 * 7)
+    d = (rng.random(13 * 7) - 0.5) * 1e-3
+    path = os.path.join(HERE, "pdegrid2d_13x7.bin")
+    R.pdegrid2d_save(path, 13, 7, 1, 0, 42, f, d)
+    return path
+
+
 def main():
     pyoracle.build(ref=True)
     if not R.available():
@@ -253,6 +265,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "rand.npz"), **rand_cases())
     np.savez_compressed(os.path.join(HERE, "varstencil.npz"), **var_stencil_cases(np.random.default_rng(8181)))
     np.savez_compressed(os.path.join(HERE, "agentmove.npz"), **agent_move_cases(np.random.default_rng(9191)))
+    print(pdegrid_file())
     for name in ("stencil", "ticks", "agents", "rand", "varstencil", "agentmove"):
         p = os.path.join(HERE, name + ".npz")
         print(f"{p}: {os.path.getsize(p)} bytes")
