@@ -28,7 +28,7 @@ namespace halcuda
         float2 *posF, *sPos;       // n each
         float *sRad;               // n
         int32_t *cellOf, *arrival, *bucketTmp, *bucket;  // n each
-        int32_t *counts;           // cells
+        int32_t *counts;           // cells, zero on entry (each binning's scan clears them again)
         int32_t *offsets;          // cells + 1
         int32_t *tileSums;         // AgentScanTiles(cells)
         double interactionRad;

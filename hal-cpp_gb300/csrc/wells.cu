@@ -284,6 +284,8 @@ namespace halcuda
             HAL_TRY(bucket.Alloc(m, "cudaMalloc(well agents)"));
             const size_t C = static_cast<size_t>(agentCells);
             HAL_TRY(binCounts.Alloc(C, "cudaMalloc(well bins)"));
+            // zero once: every binning's scan clears the counts it read
+            HAL_TRY(CudaStatus(cudaMemset(binCounts.p, 0, C * sizeof(int32_t)), "cudaMemset(well bins)"));
             HAL_TRY(offsets.Alloc(C + 1, "cudaMalloc(well bins)"));
             HAL_TRY(tileSums.Alloc(static_cast<size_t>(AgentScanTiles(agentCells)), "cudaMalloc(well bins)"));
             return HAL_CUDA_OK;
