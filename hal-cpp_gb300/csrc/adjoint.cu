@@ -24,7 +24,8 @@
 //   (b2bar, v) and (b1bar, f) on y-faces, (b2bar, w) and (b1bar, w) on x-faces
 // Two kernels per backward step: BwdY applies the previous step's (I + Ly/2)
 // and then this step's y-solve (both along y), BwdX the x-stencil and x-solve.
-// States are recomputed segment by segment from checkpoints every k steps.
+// States are recomputed segment by segment from checkpoints every k steps,
+// each segment on a second stream while the one after it is differentiated.
 //
 // Layout: every array is row-major x*yDim + y (HAL's layout).
 #include "common.cuh"
@@ -496,7 +497,8 @@ namespace halcuda
         bool hasProblem = false;
         DevBuf<float> f0, target, D, src;
         DevBuf<float> ckpt;                 // checkpoints: one field every `every` steps
-        DevBuf<float> segF, segW, segV;     // states of one segment
+        DevBuf<float> segF[2], segW[2], segV[2];  // states of a segment, double-buffered
+        StreamSlot recomputeStream;         // recomputes segment s-1 while segment s is differentiated
         DevBuf<float> work[2];              // forward ping-pong
         DevBuf<float> gA, gB, b1, b2, dD, dS;
         DevBuf<double> acc;                 // [0] loss, [1] d loss / d decay
@@ -512,6 +514,7 @@ namespace halcuda
             device = CurrentDevice();
             HAL_TRY(CudaStatus(cudaSetDevice(device), "cudaSetDevice"));
             HAL_TRY(stream.Create("cudaStreamCreate"));
+            HAL_TRY(recomputeStream.Create("cudaStreamCreate"));
             g.xDim = xDim;
             g.yDim = yDim;
             g.wrapX = wrapX != 0;
@@ -657,29 +660,30 @@ namespace halcuda
             const int tx = Threads(g.xDim), ty = Threads(g.yDim);
             const size_t smx = LineSmemFloats(tx) * sizeof(float), smy = LineSmemFloats(ty) * sizeof(float);
             bool first = true;
-            // states f_t0..f_t1, w and v of one segment, from the field at t0
-            auto recompute = [&](const float *from, int32_t t0, int32_t t1) {
-                int r = CudaStatus(cudaMemcpyAsync(segF.p, from, bytes, cudaMemcpyDeviceToDevice, s),
+            // states f_t0..f_t1, w and v of one segment into buffer b, from
+            // the field at t0, on stream rs
+            auto recompute = [&](int b, const float *from, int32_t t0, int32_t t1, cudaStream_t rs) {
+                int r = CudaStatus(cudaMemcpyAsync(segF[b].p, from, bytes, cudaMemcpyDeviceToDevice, rs),
                                    "cudaMemcpy(segment)");
                 for (int32_t t = t0; t < t1 && r == HAL_CUDA_OK; t++)
                 {
                     const size_t k = static_cast<size_t>(t - t0);
-                    r = LaunchFwd(segF.p + k * n, segF.p + (k + 1) * n, segW.p + k * n, segV.p + k * n, srcp,
-                                  negDecay, s);
+                    r = LaunchFwd(segF[b].p + k * n, segF[b].p + (k + 1) * n, segW[b].p + k * n, segV[b].p + k * n,
+                                  srcp, negDecay, rs);
                 }
                 return r;
             };
-            // reverse steps t1-1 .. t0 over the segment's states
-            auto backward = [&](int32_t t0, int32_t t1) {
+            // reverse steps t1-1 .. t0 over the states in buffer b
+            auto backward = [&](int b, int32_t t0, int32_t t1) {
                 int r = HAL_CUDA_OK;
                 for (int32_t t = t1 - 1; t >= t0 && r == HAL_CUDA_OK; t--)
                 {
                     const size_t k = static_cast<size_t>(t - t0);
-                    const float *fNext = segF.p + (k + 1) * n;
+                    const float *fNext = segF[b].p + (k + 1) * n;
                     BwdY<<<g.xDim, ty, smy, s>>>(g, first ? kBwdFirst : kBwdNext, D.p, static_cast<float>(decay),
-                                                 b1.p, gCur, fNext, segF.p + k * n, segV.p + k * n, gNext, b2.p,
-                                                 dD.p, dS.p, acc.p + 1);
-                    BwdX<<<g.yDim, tx, smx, s>>>(g, D.p, b2.p, segW.p + k * n, b1.p, dD.p);
+                                                 b1.p, gCur, fNext, segF[b].p + k * n, segV[b].p + k * n, gNext,
+                                                 b2.p, dD.p, dS.p, acc.p + 1);
+                    BwdX<<<g.yDim, tx, smx, s>>>(g, D.p, b2.p, segW[b].p + k * n, b1.p, dD.p);
                     CountLaunch(2);
                     r = LaunchStatus("adjoint backward step");
                     std::swap(gCur, gNext);
@@ -687,42 +691,110 @@ namespace halcuda
                 }
                 return r;
             };
+            int lastBuf = 0;  // buffer of segment 0, read by the tail step
             if (keepAll)
             {
                 // every state of the run is kept: one forward pass, no recomputation
-                rc = recompute(f0.p, 0, steps);
+                rc = recompute(0, f0.p, 0, steps, s);
                 if (rc == HAL_CUDA_OK)
                 {
-                    rc = LaunchLoss(segF.p + static_cast<size_t>(steps) * n, gCur, s);
+                    rc = LaunchLoss(segF[0].p + static_cast<size_t>(steps) * n, gCur, s);
                 }
                 if (rc == HAL_CUDA_OK)
                 {
-                    rc = backward(0, steps);
+                    rc = backward(0, 0, steps);
                 }
             }
             else
             {
-                const float *fT = Forward(srcp, negDecay, ckpt.p, s, rc);
+                // Segments are differentiated last to first.  Segment s-1 is
+                // recomputed from its checkpoint on a second stream into the
+                // other buffer while segment s is differentiated; events order
+                // each buffer's writer (recompute) and reader (backward).
+                cudaStream_t rs = recomputeStream.Get();
+                cudaEvent_t ready = nullptr, recDone[2] = {nullptr, nullptr}, bwdDone[2] = {nullptr, nullptr};
+                for (cudaEvent_t *e : {&ready, &recDone[0], &recDone[1], &bwdDone[0], &bwdDone[1]})
+                {
+                    if (rc == HAL_CUDA_OK)
+                    {
+                        rc = CudaStatus(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "cudaEventCreate");
+                    }
+                }
+                const float *fT = (rc == HAL_CUDA_OK) ? Forward(srcp, negDecay, ckpt.p, s, rc) : nullptr;
                 if (rc == HAL_CUDA_OK)
                 {
                     rc = LaunchLoss(fT, gCur, s);
                 }
-                for (int32_t seg = Segments() - 1; seg >= 0 && rc == HAL_CUDA_OK; seg--)
-                {
+                const int32_t S = Segments();
+                auto enqueueRecompute = [&](int32_t seg) {
+                    const int b = seg & 1;
                     const int32_t t0 = seg * every;
-                    const int32_t t1 = std::min(steps, t0 + every);
-                    rc = recompute(ckpt.p + static_cast<size_t>(seg) * n, t0, t1);
+                    // the buffer's previous reader is the backward of segment seg+2
+                    int r = CudaStatus(cudaStreamWaitEvent(rs, bwdDone[b], 0), "cudaStreamWaitEvent");
+                    if (r == HAL_CUDA_OK)
+                    {
+                        r = recompute(b, ckpt.p + static_cast<size_t>(seg) * n, t0, std::min(steps, t0 + every), rs);
+                    }
+                    if (r == HAL_CUDA_OK)
+                    {
+                        r = CudaStatus(cudaEventRecord(recDone[b], rs), "cudaEventRecord");
+                    }
+                    return r;
+                };
+                if (rc == HAL_CUDA_OK)
+                {
+                    // the checkpoints are written by the forward pass on s
+                    rc = CudaStatus(cudaEventRecord(ready, s), "cudaEventRecord");
+                }
+                if (rc == HAL_CUDA_OK)
+                {
+                    rc = CudaStatus(cudaStreamWaitEvent(rs, ready, 0), "cudaStreamWaitEvent");
+                }
+                if (rc == HAL_CUDA_OK && S > 0)
+                {
+                    rc = enqueueRecompute(S - 1);
+                }
+                for (int32_t seg = S - 1; seg >= 0 && rc == HAL_CUDA_OK; seg--)
+                {
+                    if (seg > 0)
+                    {
+                        rc = enqueueRecompute(seg - 1);
+                    }
+                    const int b = seg & 1;
+                    const int32_t t0 = seg * every;
                     if (rc == HAL_CUDA_OK)
                     {
-                        rc = backward(t0, t1);
+                        rc = CudaStatus(cudaStreamWaitEvent(s, recDone[b], 0), "cudaStreamWaitEvent");
+                    }
+                    if (rc == HAL_CUDA_OK)
+                    {
+                        rc = backward(b, t0, std::min(steps, t0 + every));
+                    }
+                    if (rc == HAL_CUDA_OK)
+                    {
+                        rc = CudaStatus(cudaEventRecord(bwdDone[b], s), "cudaEventRecord");
+                    }
+                }
+                // s now follows every recompute (each backward waited on its
+                // own); an early failure still leaves rs to be drained
+                if (rc != HAL_CUDA_OK)
+                {
+                    cudaStreamSynchronize(rs);
+                }
+                for (cudaEvent_t e : {ready, recDone[0], recDone[1], bwdDone[0], bwdDone[1]})
+                {
+                    if (e != nullptr)
+                    {
+                        cudaEventDestroy(e);
                     }
                 }
             }
             if (rc == HAL_CUDA_OK && steps > 0)
             {
                 // the y-stencil part of step 0's (I + Ly/2) b1bar: its D terms
-                BwdY<<<g.xDim, ty, smy, s>>>(g, kBwdTail, D.p, static_cast<float>(decay), b1.p, gCur, segF.p,
-                                             segF.p, segV.p, gNext, b2.p, dD.p, dS.p, acc.p + 1);
+                BwdY<<<g.xDim, ty, smy, s>>>(g, kBwdTail, D.p, static_cast<float>(decay), b1.p, gCur,
+                                             segF[lastBuf].p, segF[lastBuf].p, segV[lastBuf].p, gNext, b2.p, dD.p,
+                                             dS.p, acc.p + 1);
                 CountLaunch();
                 rc = LaunchStatus("adjoint backward tail");
             }
@@ -808,6 +880,7 @@ extern "C" int hal_cuda_adjoint_destroy(hal_cuda_adjoint *h)
     {
         cudaSetDevice(h->device);
         cudaStreamSynchronize(h->stream.Get());
+        cudaStreamSynchronize(h->recomputeStream.Get());
         delete h;
     }
     return HAL_CUDA_OK;
@@ -828,9 +901,24 @@ extern "C" int hal_cuda_adjoint_set_problem(hal_cuda_adjoint *h, const float *f0
     h->keepAll = (checkpointEvery == 0);
     h->every = h->keepAll ? std::max(steps, 1) : std::min(checkpointEvery, std::max(steps, 1));
     HAL_TRY(h->ckpt.Alloc(m * static_cast<size_t>(std::max(h->Segments(), 1)), "cudaMalloc(checkpoints)"));
-    HAL_TRY(h->segF.Alloc(m * static_cast<size_t>(h->every + 1), "cudaMalloc(segment)"));
-    HAL_TRY(h->segW.Alloc(m * static_cast<size_t>(h->every), "cudaMalloc(segment)"));
-    HAL_TRY(h->segV.Alloc(m * static_cast<size_t>(h->every), "cudaMalloc(segment)"));
+    // one segment buffer when every state is kept or there is one segment,
+    // two (recompute of one overlapping the backward of the other) otherwise
+    const int nBuf = (h->keepAll || h->Segments() <= 1) ? 1 : 2;
+    for (int b = 0; b < 2; b++)
+    {
+        if (b < nBuf)
+        {
+            HAL_TRY(h->segF[b].Alloc(m * static_cast<size_t>(h->every + 1), "cudaMalloc(segment)"));
+            HAL_TRY(h->segW[b].Alloc(m * static_cast<size_t>(h->every), "cudaMalloc(segment)"));
+            HAL_TRY(h->segV[b].Alloc(m * static_cast<size_t>(h->every), "cudaMalloc(segment)"));
+        }
+        else
+        {
+            h->segF[b].Free();
+            h->segW[b].Free();
+            h->segV[b].Free();
+        }
+    }
     cudaStream_t s = h->stream.Get();
     HAL_TRY(CudaStatus(cudaMemcpyAsync(h->f0.p, f0, m * sizeof(float), cudaMemcpyHostToDevice, s), "cudaMemcpy(f0)"));
     HAL_TRY(CudaStatus(cudaMemcpyAsync(h->target.p, target, m * sizeof(float), cudaMemcpyHostToDevice, s),
