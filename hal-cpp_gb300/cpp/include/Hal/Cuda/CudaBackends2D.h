@@ -205,4 +205,70 @@ namespace Hal::Cuda
         int32_t          m_maxAgents;
         int32_t          m_count = 0;
     };
+
+    // Many independent wells (MultiWellExperiment::Step, include/Hal/Tools/
+    // MultiWellExperiment.h:83-103) advanced together: each tick runs every
+    // well's field tick and agent force pass in a few batched launches
+    // replayed from a CUDA graph.  Each well equals its own single-grid run.
+    class CudaWells2D
+    {
+    public:
+        explicit CudaWells2D(const std::vector<hal_cuda_well_desc> &wells);
+        ~CudaWells2D();
+        CudaWells2D(const CudaWells2D &) = delete;
+        CudaWells2D &operator=(const CudaWells2D &) = delete;
+
+        void SetField(int32_t well, const std::vector<float> &field);
+        void GetField(int32_t well, std::vector<float> &field);
+        void SetSource(int32_t well, const std::vector<float> &dense);  // empty: no source
+        // counts[w] agents per well; positions (x, y interleaved) and radii
+        // concatenated in well order, in each well's own coordinates.
+        void SetAgents(const std::vector<int32_t> &counts, const std::vector<float> &positions,
+                       const std::vector<float> &radii);
+        void RunTicks(int32_t ticks, double interactionRad, double springConstant);
+        void GetForces(std::vector<float> &velocityDeltas);
+        void Sync();
+
+        hal_cuda_wells *Handle() const { return m_pHandle; }
+
+    private:
+        hal_cuda_wells                *m_pHandle = nullptr;
+        std::vector<hal_cuda_well_desc> m_wells;
+        int64_t                        m_agents = 0;
+    };
+
+    // Forward / backward API of the variable-rate ADI (a rate D per cell, the
+    // face convention of Internal::Diffusion2 with per-cell rates,
+    // src/Pde/PDEequations.cpp:199-230) over `steps` PDEGrid2D ticks:
+    // Forward gives loss = 1/2 |f_T - target|^2, Backward its gradient with
+    // respect to D, decay and the source, by adjoint kernels over states
+    // recomputed from checkpoints every `checkpointEvery` steps (0 keeps
+    // every state).  The reference has no counterpart.
+    class CudaAdjointAdi2D
+    {
+    public:
+        CudaAdjointAdi2D(int32_t xDim, int32_t yDim, bool wrapX, bool wrapY);
+        ~CudaAdjointAdi2D();
+        CudaAdjointAdi2D(const CudaAdjointAdi2D &) = delete;
+        CudaAdjointAdi2D &operator=(const CudaAdjointAdi2D &) = delete;
+
+        void SetProblem(const std::vector<float> &f0, const std::vector<float> &target, int32_t steps,
+                        int32_t checkpointEvery);
+        // Returns the loss; fT (optional) receives the final field.  An empty
+        // src means no source.
+        double Forward(const std::vector<float> &D, double decay, const std::vector<float> &src,
+                       std::vector<float> *pFT = nullptr);
+        // Returns the loss and fills the three gradients.
+        double Backward(const std::vector<float> &D, double decay, const std::vector<float> &src,
+                        std::vector<float> &gradD, double &gradDecay, std::vector<float> &gradSrc);
+        // Device ms of the last Forward and Backward.
+        void Times(float &msForward, float &msBackward) const;
+
+    private:
+        void CheckCells(const std::vector<float> &v, bool allowEmpty, const char *pWhat) const;
+
+        hal_cuda_adjoint *m_pHandle = nullptr;
+        int32_t           m_xDim;
+        int32_t           m_yDim;
+    };
 }

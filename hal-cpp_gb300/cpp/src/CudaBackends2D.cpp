@@ -361,4 +361,145 @@ namespace Hal::Cuda
         Check(hal_cuda_agents_get_bins(m_pHandle, cellOffsets.data(), bucketAgents.empty() ? nullptr : bucketAgents.data()),
               "CudaAgentForceBackend2D::GetBins");
     }
+
+    // ---- CudaWells2D ---------------------------------------------------------
+
+    CudaWells2D::CudaWells2D(const std::vector<hal_cuda_well_desc> &wells)
+        : m_wells(wells)
+    {
+        Check(hal_cuda_wells_create(wells.data(), static_cast<int32_t>(wells.size()), &m_pHandle), "CudaWells2D");
+    }
+
+    CudaWells2D::~CudaWells2D()
+    {
+        hal_cuda_wells_destroy(m_pHandle);
+    }
+
+    void CudaWells2D::SetField(int32_t well, const std::vector<float> &field)
+    {
+        Check(hal_cuda_wells_set_field(m_pHandle, well, field.data(), static_cast<int64_t>(field.size())),
+              "CudaWells2D::SetField");
+    }
+
+    void CudaWells2D::GetField(int32_t well, std::vector<float> &field)
+    {
+        if (well < 0 || well >= static_cast<int32_t>(m_wells.size()))
+        {
+            Check(HAL_CUDA_EINVAL, "CudaWells2D::GetField: no such well");
+        }
+        const hal_cuda_well_desc &d = m_wells[static_cast<size_t>(well)];
+        field.resize(static_cast<size_t>(d.xDim) * static_cast<size_t>(d.yDim));
+        Check(hal_cuda_wells_get_field(m_pHandle, well, field.data(), static_cast<int64_t>(field.size())),
+              "CudaWells2D::GetField");
+    }
+
+    void CudaWells2D::SetSource(int32_t well, const std::vector<float> &dense)
+    {
+        Check(hal_cuda_wells_set_source(m_pHandle, well, dense.empty() ? nullptr : dense.data(),
+                                        static_cast<int64_t>(dense.size())),
+              "CudaWells2D::SetSource");
+    }
+
+    void CudaWells2D::SetAgents(const std::vector<int32_t> &counts, const std::vector<float> &positions,
+                                const std::vector<float> &radii)
+    {
+        int64_t n = 0;
+        for (int32_t c : counts)
+        {
+            n += c;
+        }
+        if (counts.size() != m_wells.size() || static_cast<int64_t>(radii.size()) != n ||
+            static_cast<int64_t>(positions.size()) != 2 * n)
+        {
+            Check(HAL_CUDA_EINVAL, "CudaWells2D::SetAgents: one count per well, two positions and one radius per agent");
+        }
+        Check(hal_cuda_wells_set_agents(m_pHandle, counts.data(), positions.data(), radii.data()),
+              "CudaWells2D::SetAgents");
+        m_agents = n;
+    }
+
+    void CudaWells2D::RunTicks(int32_t ticks, double interactionRad, double springConstant)
+    {
+        Check(hal_cuda_wells_run_ticks(m_pHandle, ticks, interactionRad, springConstant), "CudaWells2D::RunTicks");
+    }
+
+    void CudaWells2D::GetForces(std::vector<float> &velocityDeltas)
+    {
+        velocityDeltas.resize(2 * static_cast<size_t>(m_agents));
+        Check(hal_cuda_wells_get_forces(m_pHandle, velocityDeltas.data(), static_cast<int64_t>(velocityDeltas.size())),
+              "CudaWells2D::GetForces");
+    }
+
+    void CudaWells2D::Sync()
+    {
+        Check(hal_cuda_wells_sync(m_pHandle), "CudaWells2D::Sync");
+    }
+
+    // ---- CudaAdjointAdi2D ------------------------------------------------------
+
+    CudaAdjointAdi2D::CudaAdjointAdi2D(int32_t xDim, int32_t yDim, bool wrapX, bool wrapY)
+        : m_xDim(xDim), m_yDim(yDim)
+    {
+        Check(hal_cuda_adjoint_create(xDim, yDim, wrapX, wrapY, &m_pHandle), "CudaAdjointAdi2D");
+    }
+
+    CudaAdjointAdi2D::~CudaAdjointAdi2D()
+    {
+        hal_cuda_adjoint_destroy(m_pHandle);
+    }
+
+    void CudaAdjointAdi2D::CheckCells(const std::vector<float> &v, bool allowEmpty, const char *pWhat) const
+    {
+        const size_t n = static_cast<size_t>(m_xDim) * static_cast<size_t>(m_yDim);
+        if (v.size() != n && !(allowEmpty && v.empty()))
+        {
+            Check(HAL_CUDA_EINVAL, (std::string(pWhat) + ": arrays must hold xDim*yDim values").c_str());
+        }
+    }
+
+    void CudaAdjointAdi2D::SetProblem(const std::vector<float> &f0, const std::vector<float> &target, int32_t steps,
+                                      int32_t checkpointEvery)
+    {
+        CheckCells(f0, false, "CudaAdjointAdi2D::SetProblem");
+        CheckCells(target, false, "CudaAdjointAdi2D::SetProblem");
+        Check(hal_cuda_adjoint_set_problem(m_pHandle, f0.data(), target.data(), static_cast<int64_t>(f0.size()), steps,
+                                           checkpointEvery),
+              "CudaAdjointAdi2D::SetProblem");
+    }
+
+    double CudaAdjointAdi2D::Forward(const std::vector<float> &D, double decay, const std::vector<float> &src,
+                                     std::vector<float> *pFT)
+    {
+        CheckCells(D, false, "CudaAdjointAdi2D::Forward");
+        CheckCells(src, true, "CudaAdjointAdi2D::Forward");
+        double loss = 0.0;
+        if (pFT != nullptr)
+        {
+            pFT->resize(static_cast<size_t>(m_xDim) * static_cast<size_t>(m_yDim));
+        }
+        Check(hal_cuda_adjoint_forward(m_pHandle, D.data(), decay, src.empty() ? nullptr : src.data(), &loss,
+                                       pFT != nullptr ? pFT->data() : nullptr),
+              "CudaAdjointAdi2D::Forward");
+        return loss;
+    }
+
+    double CudaAdjointAdi2D::Backward(const std::vector<float> &D, double decay, const std::vector<float> &src,
+                                      std::vector<float> &gradD, double &gradDecay, std::vector<float> &gradSrc)
+    {
+        CheckCells(D, false, "CudaAdjointAdi2D::Backward");
+        CheckCells(src, true, "CudaAdjointAdi2D::Backward");
+        const size_t n = static_cast<size_t>(m_xDim) * static_cast<size_t>(m_yDim);
+        gradD.resize(n);
+        gradSrc.resize(n);
+        double loss = 0.0;
+        Check(hal_cuda_adjoint_gradient(m_pHandle, D.data(), decay, src.empty() ? nullptr : src.data(), &loss,
+                                        gradD.data(), &gradDecay, gradSrc.data()),
+              "CudaAdjointAdi2D::Backward");
+        return loss;
+    }
+
+    void CudaAdjointAdi2D::Times(float &msForward, float &msBackward) const
+    {
+        Check(hal_cuda_adjoint_times(m_pHandle, &msForward, &msBackward), "CudaAdjointAdi2D::Times");
+    }
 }

@@ -390,6 +390,135 @@ namespace
         return "";
     }
 
+    double RelL2(const std::vector<float> &a, const std::vector<double> &b)
+    {
+        double num = 0.0, den = 0.0;
+        for (size_t i = 0; i < b.size(); i++)
+        {
+            num += (a[i] - b[i]) * (a[i] - b[i]);
+            den += b[i] * b[i];
+        }
+        return std::sqrt(num / (den > 0.0 ? den : 1.0));
+    }
+
+    // Three wells (explicit, ADI with a source, explicit with agents) in one
+    // batched handle against the single-grid classes: identical fields and
+    // forces.
+    std::string Wells()
+    {
+        std::vector<hal_cuda_well_desc> d(3);
+        d[0] = {40, 33, HAL_CUDA_WELL_EXPLICIT, 0, 1, 0, 0.2, 0.001};
+        d[1] = {48, 48, HAL_CUDA_WELL_ADI, 1, 0, 0, 4.0, 0.01};
+        d[2] = {24, 24, HAL_CUDA_WELL_EXPLICIT, 0, 0, 200, 0.15, 0.0};
+        oracle_rand rng;
+        oracle_rand_init(&rng, 77);
+        auto draw = [&](size_t n, double scale)
+        {
+            std::vector<float> v(n);
+            for (float &x : v)
+            {
+                x = static_cast<float>(scale * oracle_rand_double(&rng));
+            }
+            return v;
+        };
+        std::vector<std::vector<float>> f0;
+        for (const hal_cuda_well_desc &w : d)
+        {
+            f0.push_back(draw(static_cast<size_t>(w.xDim) * w.yDim, 1.0));
+        }
+        const std::vector<float> src1 = draw(48 * 48, 0.01);
+        std::vector<float> pos = draw(400, 23.99), rad(200, 0.5f);
+        const int ticks = 7;
+        Hal::Cuda::CudaWells2D wells(d);
+        for (int w = 0; w < 3; w++)
+        {
+            wells.SetField(w, f0[static_cast<size_t>(w)]);
+        }
+        wells.SetSource(1, src1);
+        wells.SetAgents({0, 0, 200}, pos, rad);
+        wells.RunTicks(ticks, 1.0, 0.1);
+        std::vector<float> got, exp, forces, expForces;
+        wells.GetForces(forces);
+        for (int w = 0; w < 3; w++)
+        {
+            wells.GetField(w, got);
+            const hal_cuda_well_desc &x = d[static_cast<size_t>(w)];
+            if (x.kind == HAL_CUDA_WELL_ADI)
+            {
+                Hal::Cuda::CudaAdiDiffusionBackend2D adi(x.xDim, x.yDim);
+                adi.SetField(f0[static_cast<size_t>(w)]);
+                adi.SetSource(src1);
+                adi.RunTicks(ticks, x.diffRate, x.decay, x.wrapX != 0, x.wrapY != 0);
+                adi.GetField(exp);
+            }
+            else
+            {
+                Hal::Cuda::CudaDiffusionBackend2D diff(x.xDim, x.yDim);
+                diff.SetField(f0[static_cast<size_t>(w)]);
+                diff.RunTicks(ticks, x.diffRate, x.decay, x.wrapX != 0, x.wrapY != 0);
+                diff.GetField(exp);
+            }
+            if (got != exp)
+            {
+                return Fmt("well %g differs from its single-grid run", w);
+            }
+        }
+        Hal::Cuda::CudaAgentForceBackend2D agents(24, 24, 200);
+        agents.Upload(pos, rad);
+        agents.Dispatch(1.0, 0.1, false, false);
+        agents.Download(expForces);
+        return forces == expForces ? "" : "well agent forces differ from the single-grid dispatch";
+    }
+
+    // The adjoint's forward/backward API against the FP64 CPU adjoint, and
+    // the gradient's independence of the checkpoint interval.
+    std::string Adjoint()
+    {
+        const int32_t n = 32, steps = 12;
+        const size_t cells = static_cast<size_t>(n) * n;
+        oracle_rand rng;
+        oracle_rand_init(&rng, 5);
+        std::vector<float> f0(cells), target(cells), D(cells), src(cells);
+        for (size_t i = 0; i < cells; i++)
+        {
+            f0[i] = static_cast<float>(oracle_rand_double(&rng));
+            target[i] = static_cast<float>(oracle_rand_double(&rng));
+            D[i] = static_cast<float>(0.5 + 4.5 * oracle_rand_double(&rng));
+            src[i] = static_cast<float>(0.01 * oracle_rand_double(&rng));
+        }
+        const double decay = 0.005;
+        std::vector<double> f0d(f0.begin(), f0.end()), td(target.begin(), target.end()), Dd(D.begin(), D.end()),
+            sd(src.begin(), src.end()), fT(cells), gD(cells), gS(cells);
+        double gK = 0.0;
+        const double lossRef = oracle_dadi_loss_grad(f0d.data(), td.data(), Dd.data(), decay, sd.data(), n, n, 0, 0,
+                                                     steps, fT.data(), gD.data(), &gK, gS.data());
+        Hal::Cuda::CudaAdjointAdi2D adj(n, n, false, false);
+        std::vector<float> gotD, gotS, firstD;
+        double gotK = 0.0;
+        for (int every : {5, 0})
+        {
+            adj.SetProblem(f0, target, steps, every);
+            const double lf = adj.Forward(D, decay, src);
+            const double lb = adj.Backward(D, decay, src, gotD, gotK, gotS);
+            if (std::fabs(lf - lossRef) > 1e-4 * lossRef || std::fabs(lb - lf) > 1e-6 * lf)
+            {
+                return Fmt("adjoint loss differs from the FP64 adjoint: %.3e", lf - lossRef);
+            }
+            if (RelL2(gotD, gD) > 2e-3 || RelL2(gotS, gS) > 2e-3 || std::fabs(gotK - gK) > 2e-3 * std::fabs(gK))
+            {
+                return Fmt("adjoint gradient differs from the FP64 adjoint: %.3e", RelL2(gotD, gD));
+            }
+            if (every == 0 && gotD != firstD)
+            {
+                return "gradient depends on the checkpoint interval";
+            }
+            firstD = gotD;
+        }
+        float msF = 0.0f, msB = 0.0f;
+        adj.Times(msF, msB);
+        return (msF > 0.0f && msB > 0.0f) ? "" : "adjoint times not recorded";
+    }
+
     // Resident ticks (PDEGrid2D semantics: decay, dense source, Dirichlet)
     // against the CPU tick, explicit and ADI.
     std::string ResidentTicks(Hal::Cuda::CudaDiffusionBackend2D &diff, Hal::Cuda::CudaAdiDiffusionBackend2D &adi)
@@ -468,6 +597,8 @@ int main()
     Run("resident_ticks_match_cpu", [&] { return ResidentTicks(diffTick, adiTick); });
     Run("variable_rate_and_advection_bit_exact", [&] { return VariableStencils(diffTick); });
     Run("resident_agent_step_bit_exact", [&] { return AgentStep(agents64); });
+    Run("batched_wells_equal_single_grids", [&] { return Wells(); });
+    Run("adjoint_forward_backward_api", [&] { return Adjoint(); });
 
     std::printf("backend_tests: %d passed, %d failed\n", g_passed, g_failed);
     return g_failed == 0 ? 0 : 1;
