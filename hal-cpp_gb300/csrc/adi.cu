@@ -1139,14 +1139,15 @@ namespace halcuda
 namespace halcuda
 {
     static_assert(kSweepTileThreads == kMaxThreads, "batched sweep CTAs use the kernel's thread bound");
+    static_assert(kSweepTileMaxR == kMaxR, "batched sweep tiles use the kernel's line bound");
 
-    SweepTileShape SweepTileShapeFor(int32_t P)
+    SweepTileShape SweepTileShapeFor(int32_t P, int32_t rCap)
     {
         // every tile CTA has kSweepTileThreads threads: as many lines as
-        // (R / kNL) * P threads allow, a power of two in [8, kMaxR]
+        // (R / kNL) * P threads allow, a power of two in [8, min(rCap, kMaxR)]
         SweepTileShape sh;
         int32_t R = 8;
-        while (R * 2 <= kMaxR && (R * 2 / kNL) * P <= kSweepTileThreads)
+        while (R * 2 <= kMaxR && R * 2 <= rCap && (R * 2 / kNL) * P <= kSweepTileThreads)
         {
             R *= 2;
         }

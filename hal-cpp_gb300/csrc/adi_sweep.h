@@ -88,8 +88,11 @@ namespace halcuda
         size_t smem;  // dynamic shared memory of one CTA
     };
 
-    // Shape of the tiles of a grid whose lines have P = ceil(L/32) chunks.
-    SweepTileShape SweepTileShapeFor(int32_t P);
+    // Shape of the tiles of a grid whose lines have P = ceil(L/32) chunks:
+    // the most lines per CTA (a power of two, at least 8, at most rCap) that
+    // the CTA's threads cover.
+    constexpr int32_t kSweepTileMaxR = 128;
+    SweepTileShape SweepTileShapeFor(int32_t P, int32_t rCap = kSweepTileMaxR);
 
     // Enables `smem` bytes of dynamic shared memory for the batched kernel of
     // `mode` (kSweepW or kSweepTick); call before capturing a launch.

@@ -1268,7 +1268,7 @@ namespace halcuda
         Scatter<<<ablocks, T, 0, s>>>(a.cellOf, a.arrival, a.offsets, a.n, a.bucketTmp);
         Stabilize<float, float><<<ablocks, T, 0, s>>>(a.cellOf, a.offsets, a.bucketTmp, a.posF, a.rad, a.n, a.bucket,
                                                       a.sPos, a.sRad);
-        const int TF = 128;
+        const int TF = (a.forceThreads == 64 || a.forceThreads == 256) ? a.forceThreads : 128;
         ForcesWells<<<static_cast<unsigned>((a.n + TF - 1) / TF), TF, 0, s>>>(
             a.bucket, a.offsets, a.sPos, a.sRad, a.wellOf, a.wells, a.n, a.interactionRad, a.R, a.k, a.vel);
         CountLaunch(7);

@@ -34,6 +34,7 @@ namespace halcuda
         double interactionRad;
         float R, k;
         float *vel;                // 2n, overwritten
+        int32_t forceThreads = 128;  // block size of the force kernel (64, 128 or 256)
     };
 
     int32_t AgentScanTiles(int64_t cells);

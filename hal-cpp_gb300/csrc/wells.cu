@@ -33,6 +33,7 @@
 #include <memory>
 #include <numeric>
 #include <string>
+#include <utility>
 #include <vector>
 
 namespace halcuda
@@ -76,6 +77,13 @@ namespace halcuda
         int32_t nTilesX = 0, nTilesY = 0;
         size_t smemX = 0, smemY = 0;
         DevBuf<int32_t> err;
+        // Lines per sweep tile are capped at rCap, chosen by the autotuner
+        // (Autotune) the first time the wells tick.
+        int32_t rCap = kSweepTileMaxR;
+        int32_t forceThreads = 128;  // agent force kernel block size, also tuned
+        bool tuned = false;
+        float tunedMs = 0.0f, defaultMs = 0.0f;
+        std::pair<double, double> agentsTunedFor{-1.0, 0.0};  // (R, k) the force block size was tuned for
 
         // agents
         std::vector<int64_t> cellBase;   // well -> first cell in the concatenation, or -1
@@ -217,6 +225,17 @@ namespace halcuda
                 planX.push_back(std::move(px));
                 planY.push_back(std::move(py));
             }
+            for (int c = 0; c < 2; c++)
+            {
+                HAL_TRY(sxTab[c].Alloc(std::max<size_t>(adiWell.size(), 1), "cudaMalloc(sweep table)"));
+                HAL_TRY(syTab[c].Alloc(std::max<size_t>(adiWell.size(), 1), "cudaMalloc(sweep table)"));
+            }
+            return BuildAdiTiles();
+        }
+
+        // Sweep tiles of the ADI wells at the current rCap, largest well first.
+        int BuildAdiTiles()
+        {
             std::vector<int32_t> order = adiWell;
             std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return Cells(a) > Cells(b); });
             std::vector<int2> tx, ty;
@@ -224,8 +243,8 @@ namespace halcuda
             for (int32_t w : order)
             {
                 const int32_t a = adiIdx[w];
-                const SweepTileShape sx = SweepTileShapeFor(planX[a]->Dev().P);
-                const SweepTileShape sy = SweepTileShapeFor(planY[a]->Dev().P);
+                const SweepTileShape sx = SweepTileShapeFor(planX[a]->Dev().P, rCap);
+                const SweepTileShape sy = SweepTileShapeFor(planY[a]->Dev().P, rCap);
                 smemX = std::max(smemX, sx.smem);
                 smemY = std::max(smemY, sy.smem);
                 for (int32_t x0 = 0; x0 < desc[w].yDim; x0 += sx.R)
@@ -241,11 +260,6 @@ namespace halcuda
             nTilesY = static_cast<int32_t>(ty.size());
             HAL_TRY(Upload(tilesX, tx));
             HAL_TRY(Upload(tilesY, ty));
-            for (int c = 0; c < 2; c++)
-            {
-                HAL_TRY(sxTab[c].Alloc(std::max<size_t>(adiWell.size(), 1), "cudaMalloc(sweep table)"));
-                HAL_TRY(syTab[c].Alloc(std::max<size_t>(adiWell.size(), 1), "cudaMalloc(sweep table)"));
-            }
             if (nTilesX > 0)
             {
                 HAL_TRY(PrepareSweepTiles(kSweepW, smemX));
@@ -340,7 +354,7 @@ namespace halcuda
                     p.halfR = static_cast<float>(d.diffRate / 2.0);
                     p.r = static_cast<float>(d.diffRate);
                     p.plan = planX[a]->Dev();
-                    const SweepTileShape shx = SweepTileShapeFor(p.plan.P);
+                    const SweepTileShape shx = SweepTileShapeFor(p.plan.P, rCap);
                     p.R = shx.R;
                     p.LS = shx.LS;
                     p.out = W(w);
@@ -356,7 +370,7 @@ namespace halcuda
                     q.halfR = static_cast<float>(d.diffRate / 2.0);
                     q.r = static_cast<float>(d.diffRate);
                     q.plan = planY[a]->Dev();
-                    const SweepTileShape shy = SweepTileShapeFor(q.plan.P);
+                    const SweepTileShape shy = SweepTileShapeFor(q.plan.P, rCap);
                     q.R = shy.R;
                     q.LS = shy.LS;
                     q.out = F(w, c ^ 1);
@@ -406,28 +420,7 @@ namespace halcuda
             }
             if (nAgents > 0)
             {
-                AgentWellsArgs a;
-                a.pos = apos.p;
-                a.rad = arad.p;
-                a.wellOf = wellOf.p;
-                a.wells = agentWells.p;
-                a.n = nAgents;
-                a.cells = agentCells;
-                a.posF = posF.p;
-                a.sPos = sPos.p;
-                a.sRad = sRad.p;
-                a.cellOf = cellOf.p;
-                a.arrival = arrival.p;
-                a.bucketTmp = bucketTmp.p;
-                a.bucket = bucket.p;
-                a.counts = binCounts.p;
-                a.offsets = offsets.p;
-                a.tileSums = tileSums.p;
-                a.interactionRad = R;
-                a.R = static_cast<float>(R);
-                a.k = static_cast<float>(k);
-                a.vel = avel.p;
-                HAL_TRY(LaunchAgentWells(a, s));
+                HAL_TRY(LaunchAgentWells(AgentArgs(R, k), s));
             }
             if (ev)
             {
@@ -436,13 +429,198 @@ namespace halcuda
             return HAL_CUDA_OK;
         }
 
+        AgentWellsArgs AgentArgs(double R, double k)
+        {
+            AgentWellsArgs a;
+            a.pos = apos.p;
+            a.rad = arad.p;
+            a.wellOf = wellOf.p;
+            a.wells = agentWells.p;
+            a.n = nAgents;
+            a.cells = agentCells;
+            a.posF = posF.p;
+            a.sPos = sPos.p;
+            a.sRad = sRad.p;
+            a.cellOf = cellOf.p;
+            a.arrival = arrival.p;
+            a.bucketTmp = bucketTmp.p;
+            a.bucket = bucket.p;
+            a.counts = binCounts.p;
+            a.offsets = offsets.p;
+            a.tileSums = tileSums.p;
+            a.interactionRad = R;
+            a.R = static_cast<float>(R);
+            a.k = static_cast<float>(k);
+            a.vel = avel.p;
+            a.forceThreads = forceThreads;
+            return a;
+        }
+
         int KernelsPerTick() const
         {
             return (nTiles4 > 0) + (nTiles1 > 0) + (nTilesX > 0) + (nTilesY > 0) + (nAgents > 0 ? 7 : 0);
         }
 
+        // Mean device ms of one x-sweep plus one y-sweep launch over every
+        // ADI well, from the live parity.  The y-sweep writes the other
+        // parity's buffer and the parity is not flipped, so the wells' state
+        // does not change.
+        int TimeSweeps(int warm, int iters, float *ms)
+        {
+            cudaStream_t s = stream.Get();
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            HAL_TRY(CudaStatus(cudaEventCreate(&e0), "cudaEventCreate"));
+            int rc = CudaStatus(cudaEventCreate(&e1), "cudaEventCreate");
+            for (int t = 0; t < warm + iters && rc == HAL_CUDA_OK; t++)
+            {
+                if (t == warm)
+                {
+                    cudaEventRecord(e0, s);
+                }
+                rc = LaunchSweepTiles(kSweepW, sxTab[cur].p, tilesX.p, nTilesX, smemX, s);
+                if (rc == HAL_CUDA_OK)
+                {
+                    rc = LaunchSweepTiles(kSweepTick, syTab[cur].p, tilesY.p, nTilesY, smemY, s);
+                }
+            }
+            if (rc == HAL_CUDA_OK)
+            {
+                cudaEventRecord(e1, s);
+                rc = CudaStatus(cudaEventSynchronize(e1), "wells autotune");
+            }
+            if (rc == HAL_CUDA_OK)
+            {
+                float t = 0.0f;
+                cudaEventElapsedTime(&t, e0, e1);
+                *ms = t / static_cast<float>(iters);
+            }
+            cudaEventDestroy(e0);
+            if (e1 != nullptr)
+            {
+                cudaEventDestroy(e1);
+            }
+            return rc;
+        }
+
+        // Autotuner of the ADI sweep tiles: times the batched x- and y-sweeps
+        // with the lines per tile capped at 128, 64, 32, 16 and 8 (caps that
+        // give the same tiles as a larger one are skipped), on the wells'
+        // own data, and keeps the fastest.  Fewer lines per tile give more,
+        // smaller CTAs (more of them resident per SM); more lines give longer
+        // contiguous stores.  Which wins depends on the mix of well sizes.
+        int Autotune()
+        {
+            tuned = true;
+            if (nTilesX == 0)
+            {
+                rCap = kSweepTileMaxR;
+                return HAL_CUDA_OK;
+            }
+            std::vector<int32_t> prevShape;
+            float best = 0.0f;
+            int32_t bestCap = kSweepTileMaxR;
+            for (int32_t cap = kSweepTileMaxR; cap >= 8; cap /= 2)
+            {
+                std::vector<int32_t> shape;
+                for (size_t a = 0; a < adiWell.size(); a++)
+                {
+                    shape.push_back(SweepTileShapeFor(planX[a]->Dev().P, cap).R);
+                    shape.push_back(SweepTileShapeFor(planY[a]->Dev().P, cap).R);
+                }
+                if (shape == prevShape)
+                {
+                    continue;
+                }
+                prevShape = shape;
+                rCap = cap;
+                HAL_TRY(BuildAdiTiles());
+                HAL_TRY(UploadTables());
+                float ms = 0.0f;
+                HAL_TRY(TimeSweeps(2, 5, &ms));
+                if (cap == kSweepTileMaxR)
+                {
+                    defaultMs = ms;
+                }
+                if (cap == kSweepTileMaxR || ms < best)
+                {
+                    best = ms;
+                    bestCap = cap;
+                }
+            }
+            rCap = bestCap;
+            tunedMs = best;
+            HAL_TRY(BuildAdiTiles());
+            HAL_TRY(UploadTables());
+            ResetGraphs();
+            return HAL_CUDA_OK;
+        }
+
+        // Block size of the agent force kernel (64, 128 or 256 threads),
+        // timed on the wells' agents with the interaction radius and spring
+        // constant of the run.  The pass only rewrites its own bins and
+        // deltas, so repeating it changes nothing.
+        int TuneAgents(double R, double k)
+        {
+            agentsTunedFor = std::make_pair(R, k);
+            if (nAgents == 0)
+            {
+                return HAL_CUDA_OK;
+            }
+            cudaStream_t s = stream.Get();
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            HAL_TRY(CudaStatus(cudaEventCreate(&e0), "cudaEventCreate"));
+            int rc = CudaStatus(cudaEventCreate(&e1), "cudaEventCreate");
+            float best = 0.0f;
+            int32_t bestT = 128;
+            for (int32_t t : {128, 64, 256})
+            {
+                forceThreads = t;
+                const AgentWellsArgs a = AgentArgs(R, k);
+                for (int it = 0; it < 5 && rc == HAL_CUDA_OK; it++)
+                {
+                    if (it == 2)
+                    {
+                        cudaEventRecord(e0, s);
+                    }
+                    rc = LaunchAgentWells(a, s);
+                }
+                if (rc == HAL_CUDA_OK)
+                {
+                    cudaEventRecord(e1, s);
+                    rc = CudaStatus(cudaEventSynchronize(e1), "wells agent autotune");
+                }
+                if (rc != HAL_CUDA_OK)
+                {
+                    break;
+                }
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (t == 128 || ms < best)
+                {
+                    best = ms;
+                    bestT = t;
+                }
+            }
+            cudaEventDestroy(e0);
+            if (e1 != nullptr)
+            {
+                cudaEventDestroy(e1);
+            }
+            forceThreads = bestT;
+            ResetGraphs();
+            return rc;
+        }
+
         int RunTicks(int32_t ticks, double R, double k)
         {
+            if (!tuned)
+            {
+                HAL_TRY(Autotune());
+            }
+            if (agentsTunedFor != std::make_pair(R, k))
+            {
+                HAL_TRY(TuneAgents(R, k));
+            }
             cudaStream_t s = stream.Get();
             char key[160];
             snprintf(key, sizeof(key), "%a|%a|%d|%p", R, k, nAgents, static_cast<void *>(s));
@@ -683,6 +861,7 @@ extern "C" int hal_cuda_wells_set_agents(hal_cuda_wells *h, const int32_t *count
                                            cudaMemcpyHostToDevice, s), "cudaMemcpy(wellOf)"));
     }
     h->counts.assign(counts, counts + h->desc.size());
+    h->agentsTunedFor = std::make_pair(-1.0, 0.0);  // new agents: re-tune the force block size
     h->nAgents = static_cast<int32_t>(n);
     return CudaStatus(cudaStreamSynchronize(s), "hal_cuda_wells_set_agents");
 }
@@ -725,6 +904,14 @@ extern "C" int hal_cuda_wells_profile(hal_cuda_wells *h, int32_t iters, double i
                 "hal_cuda_wells_profile: interactionRad out of range");
     using namespace halcuda;
     HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    if (!h->tuned)
+    {
+        HAL_TRY(h->Autotune());
+    }
+    if (h->agentsTunedFor != std::make_pair(interactionRad, springConstant))
+    {
+        HAL_TRY(h->TuneAgents(interactionRad, springConstant));
+    }
     cudaStream_t s = h->stream.Get();
     cudaEvent_t ev[5];
     for (auto &e : ev)
@@ -768,6 +955,27 @@ extern "C" int hal_cuda_wells_profile(hal_cuda_wells *h, int32_t iters, double i
         ms[q] = static_cast<float>(acc[q] / iters);
     }
     return h->CheckDeviceError("hal_cuda_wells_profile");
+}
+
+extern "C" int hal_cuda_wells_autotune(hal_cuda_wells *h, int32_t *rCap, float *msTuned, float *msDefault)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_wells_autotune: handle is NULL");
+    using namespace halcuda;
+    HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    HAL_TRY(h->Autotune());
+    if (rCap != nullptr)
+    {
+        *rCap = h->rCap;
+    }
+    if (msTuned != nullptr)
+    {
+        *msTuned = h->tunedMs;
+    }
+    if (msDefault != nullptr)
+    {
+        *msDefault = h->defaultMs;
+    }
+    return HAL_CUDA_OK;
 }
 
 extern "C" int hal_cuda_wells_sync(hal_cuda_wells *h)

@@ -101,6 +101,7 @@ SIGNATURES = {
     "hal_cuda_wells_run_ticks": (_I, [_vp, _i32, _f64, _f64]),
     "hal_cuda_wells_get_forces": (_I, [_vp, _vp, _i64]),
     "hal_cuda_wells_profile": (_I, [_vp, _i32, _f64, _f64, _vp]),
+    "hal_cuda_wells_autotune": (_I, [_vp, _vp, _vp, _vp]),
     "hal_cuda_wells_sync": (_I, [_vp]),
     "hal_cuda_wells_stream": (_vp, [_vp]),
     "hal_cuda_wells_set_stream": (_I, [_vp, _vp]),
@@ -630,6 +631,14 @@ class Wells(_Handle):
     def run_ticks(self, ticks, interactionRad=1.0, springConstant=0.1):
         _check(lib().hal_cuda_wells_run_ticks(self._h, ticks, interactionRad, springConstant),
                "wells_run_ticks")
+
+    def autotune(self):
+        """Re-runs the sweep-tile autotuner; returns (rCap, ms tuned, ms default)."""
+        cap = ctypes.c_int32()
+        a, b = ctypes.c_float(), ctypes.c_float()
+        _check(lib().hal_cuda_wells_autotune(self._h, ctypes.byref(cap), ctypes.byref(a), ctypes.byref(b)),
+               "wells_autotune")
+        return cap.value, a.value, b.value
 
     def get_forces(self):
         out = np.empty(2 * int(self.counts.sum()), dtype=np.float32)

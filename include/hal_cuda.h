@@ -414,6 +414,17 @@ int hal_cuda_wells_get_forces(hal_cuda_wells *h, float *velocityDeltas, int64_t 
  * tiles, ms[3] agent pass, ms[4] whole tick.  Fields advance. */
 int hal_cuda_wells_profile(hal_cuda_wells *h, int32_t iters, double interactionRad,
                            double springConstant, float *ms);
+/* Autotuner of the ADI sweep tiles: times the batched x- and y-sweeps of
+ * every ADI well with the lines per tile capped at 128, 64, 32, 16 and 8, on
+ * the wells' own fields (their state does not change), and keeps the
+ * fastest cap.  Runs by itself before the first run_ticks or profile;
+ * calling it again re-tunes.  Returns the chosen cap and the mean ms of one
+ * x- plus y-sweep launch with it and with the uncapped default (any pointer
+ * may be NULL; both times are 0 without ADI wells).  The block size of the
+ * agent force kernel (64, 128 or 256 threads) is tuned the same way, on the
+ * wells' agents, at the first run_ticks or profile after set_agents and for
+ * each new interaction radius and spring constant. */
+int hal_cuda_wells_autotune(hal_cuda_wells *h, int32_t *rCap, float *msTuned, float *msDefault);
 int hal_cuda_wells_sync(hal_cuda_wells *h);
 void *hal_cuda_wells_stream(hal_cuda_wells *h);
 int hal_cuda_wells_set_stream(hal_cuda_wells *h, void *stream);

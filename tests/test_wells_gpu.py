@@ -101,6 +101,30 @@ def test_wells_equal_single_grid_handles(hal, oracle):
             assert np.array_equal(v, _alone_forces(hal, w, pos[i], rad[i])), (i, w)
 
 
+def test_autotune_keeps_state_and_results(hal):
+    """The sweep-tile autotuner times the sweeps on the wells' own data
+    without changing it, and whatever cap it picks, the ticks stay equal to
+    the single-grid handles."""
+    rng = np.random.default_rng(41)
+    wells, fields, srcs, counts, pos, rad = _mixed_wells(rng)
+    with hal.Wells(wells) as b:
+        for i, f in enumerate(fields):
+            b.set_field(i, f)
+            if srcs[i] is not None:
+                b.set_source(i, srcs[i])
+        b.set_agents(counts, np.concatenate(pos), np.concatenate(rad))
+        cap, ms_tuned, ms_default = b.autotune()
+        assert cap in (8, 16, 32, 64, 128)
+        assert 0 < ms_tuned <= ms_default
+        assert all(np.array_equal(b.get_field(i), fields[i]) for i in range(len(wells)))
+        b.run_ticks(4, R, K)
+        b.autotune()  # re-tuning mid-run keeps the state too
+        b.run_ticks(1, R, K)
+        got = [b.get_field(i) for i in range(len(wells))]
+    for i, w in enumerate(wells):
+        assert np.array_equal(got[i], _alone(hal, w, fields[i], srcs[i], 5)), (i, w)
+
+
 def test_wells_profile_and_source_clear(hal):
     rng = np.random.default_rng(41)
     wells, fields, srcs, counts, pos, rad = _mixed_wells(rng)
