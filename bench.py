@@ -142,6 +142,23 @@ def profile_traffic(kernel):
     return None
 
 
+def accuracy(got, ref, what):
+    """max-abs and relative L2 error of an FP32 device result against the
+    FP64 oracle run from the same float32 inputs."""
+    d = np.asarray(got, dtype=np.float64) - np.asarray(ref, dtype=np.float64)
+    den = float(np.linalg.norm(ref))
+    return {"max_abs": float(np.abs(d).max()), "rel_l2": float(np.linalg.norm(d) / (den if den > 0 else 1.0)),
+            "vs": what}
+
+
+def _oracle():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    pyoracle.build(ref=False)
+    return pyoracle.Oracle
+
+
 def cpu_baseline_adi(threads, min_seconds=8.0, max_ticks=40):
     """The oracle's FP64 ADI tick on the full 2048^2 workload, timed on the
     host; returns (cell-updates/s, ticks timed)."""
@@ -238,6 +255,16 @@ def secondary_explicit(hal, torch, stream, warm=5, iters=50):
             times.append(ev0.elapsed_time(ev1))
         ms_tick = min(times) / ticks
         ms_launch = d.profile(iters, 0.2, 0.001)
+        # accuracy: 10 ticks from the float32 start against the FP64 oracle
+        f32 = w["field"].astype(np.float32)
+        d.set_field(f32)
+        d.run_ticks(10, 0.2, 0.001)
+        got = d.get_field()
+    O = _oracle()
+    t0 = time.perf_counter()
+    ref = O.run_ticks(0, f32.astype(np.float64), N, N, 0.2, decay=0.001, src_idx=w["src_idx"], src_val=w["src_val"],
+                      ticks=10)
+    cpu_s = time.perf_counter() - t0
     peak, _ = peaks()
     ach = EXPLICIT_BYTES * CELLS / (ms_launch * 1e-3) / 1e9
     return {"workload": "explicit-2048x2048-r0.2-decay0.001-64sources-zeroflux",
@@ -246,6 +273,9 @@ def secondary_explicit(hal, torch, stream, warm=5, iters=50):
             "roofline": {"kernel": "TickKernel", "bound": "hbm", "achieved": ach, "peak": peak,
                          "unit": "GB/s", "frac": ach / peak,
                          "traffic": profile_traffic("TickKernel")},
+            "accuracy": accuracy(got, ref, "FP64 oracle, 10 ticks from the same float32 field"),
+            "cpu_baseline": {"value": 10 * CELLS / cpu_s, "unit": "cell-updates/s", "cores": 1, "kind": "port",
+                             "sample": "10 FP64 ticks of the same 2048x2048 workload (oracle, 1 thread)"},
             "note": "100-tick graph replays; 33.5 MB ping-pong set is L2-resident"}
 
 
@@ -270,6 +300,16 @@ def secondary_agents(hal, stream, iters=20):
         e1.record(stream)
         e1.synchronize()
         ms_step = e0.elapsed_time(e1) / iters
+        # accuracy: FP32 forces of the starting positions against FP64
+        ag.upload(w["positions"], w["radii"])
+        ag.dispatch(1.0, 0.1)
+        got = ag.download()
+    O = _oracle()
+    pos64 = np.asarray(w["positions"], dtype=np.float32).astype(np.float64)
+    rad64 = np.asarray(w["radii"], dtype=np.float32).astype(np.float64)
+    t0 = time.perf_counter()
+    ref, _, _ = O.accumulate_forces(pos64, rad64, 1.0, 0.1, N, N, False, False)
+    cpu_s = time.perf_counter() - t0
     # algorithmic bytes of the whole dispatch: 28 B/agent + 16 B/bin
     bytes_tick = 28 * n + 16 * CELLS
     peak, _ = peaks()
@@ -284,7 +324,11 @@ def secondary_agents(hal, stream, iters=20):
                                       "ApplyFriction, friction 0.5, maxVel 0.5, no host copies"},
             "roofline": {"kernel": "whole dispatch", "bound": "hbm", "achieved": ach,
                          "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                         "traffic": None}}
+                         "traffic": None},
+            "accuracy": accuracy(got, ref, "FP64 CpuAgentForceBackend2D restatement on the same float32 positions"),
+            "binning": "bit-exact (tests)",
+            "cpu_baseline": {"value": n / cpu_s, "unit": "agents/s", "cores": 1, "kind": "port",
+                             "sample": "one FP64 AccumulateForces of the same 1M agents (oracle, 1 thread)"}}
 
 
 def secondary_wells(hal, torch, stream, ticks=20, plain_ticks=3):
@@ -606,6 +650,17 @@ def main():
         e2e_step = float(t.item())
     e2e_value = world * CELLS * TICKS / (e2e_step * 1e-3)
 
+    acc = None
+    if rank == 0:
+        # 10 ticks from the same float32 field and source against the FP64
+        # oracle (the reference CPU backend's arithmetic)
+        adi.set_field(field_np)
+        adi.run_ticks(10, RATE, DECAY)
+        got = adi.get_field()
+        ref = _oracle().run_ticks(1, field_np.astype(np.float64), N, N, RATE, decay=DECAY,
+                                  src_dense=src_np.astype(np.float64), ticks=10, threads=os.cpu_count() or 1)
+        acc = accuracy(got, ref, "FP64 oracle, 10 ticks from the same float32 field and source")
+
     secondary = None
     if not args.no_secondary and rank == 0:
         secondary = {"explicit": secondary_explicit(hal, torch, stream),
@@ -641,6 +696,7 @@ def main():
                          "note": "working set (3 x 16.8 MB + scratch) stays in the 126 MB L2 "
                                  "across the ticks of a step"},
             "cpu_baseline": cpu,
+            "accuracy": acc,
             "e2e": {"value": e2e_value, "unit": "cell-updates/s",
                     "h2d_bytes_per_step": 2 * CELLS * 4, "d2h_bytes_per_step": CELLS * 4,
                     "ms_per_step": e2e_step,

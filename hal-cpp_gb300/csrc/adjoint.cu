@@ -720,13 +720,61 @@ namespace halcuda
                         rc = CudaStatus(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "cudaEventCreate");
                     }
                 }
-                const float *fT = (rc == HAL_CUDA_OK) ? Forward(srcp, negDecay, ckpt.p, s, rc) : nullptr;
+                // The forward pass keeps checkpoints, and writes the states of
+                // the last two segments (one per buffer) as it goes, so the
+                // backward starts without waiting for a recomputation.
+                const int32_t S = Segments();
+                const int32_t firstKept = std::max(S - 2, 0);
+                const float *fT = nullptr;
+                if (rc == HAL_CUDA_OK)
+                {
+                    rc = CudaStatus(cudaMemcpyAsync(work[0].p, f0.p, bytes, cudaMemcpyDeviceToDevice, s),
+                                    "cudaMemcpy(f0)");
+                }
+                const float *fCur = work[0].p;
+                int c = 0;
+                for (int32_t t = 0; t < steps && rc == HAL_CUDA_OK; t++)
+                {
+                    const int32_t seg = t / every;
+                    if (t % every == 0)
+                    {
+                        rc = CudaStatus(cudaMemcpyAsync(ckpt.p + static_cast<size_t>(seg) * n, fCur, bytes,
+                                                        cudaMemcpyDeviceToDevice, s), "cudaMemcpy(checkpoint)");
+                        if (rc == HAL_CUDA_OK && seg >= firstKept)
+                        {
+                            rc = CudaStatus(cudaMemcpyAsync(segF[seg & 1].p, fCur, bytes, cudaMemcpyDeviceToDevice, s),
+                                            "cudaMemcpy(segment)");
+                        }
+                    }
+                    if (rc != HAL_CUDA_OK)
+                    {
+                        break;
+                    }
+                    if (seg >= firstKept)
+                    {
+                        const int b = seg & 1;
+                        const size_t k = static_cast<size_t>(t - seg * every);
+                        float *fOut = segF[b].p + (k + 1) * n;
+                        rc = LaunchFwd(fCur, fOut, segW[b].p + k * n, segV[b].p + k * n, srcp, negDecay, s);
+                        fCur = fOut;
+                    }
+                    else
+                    {
+                        rc = LaunchFwd(fCur, work[c ^ 1].p, b1.p, nullptr, srcp, negDecay, s);
+                        c ^= 1;
+                        fCur = work[c].p;
+                    }
+                }
+                fT = fCur;
                 if (rc == HAL_CUDA_OK)
                 {
                     rc = LaunchLoss(fT, gCur, s);
                 }
-                const int32_t S = Segments();
                 auto enqueueRecompute = [&](int32_t seg) {
+                    if (seg >= firstKept)
+                    {
+                        return static_cast<int>(HAL_CUDA_OK);  // written by the forward pass
+                    }
                     const int b = seg & 1;
                     const int32_t t0 = seg * every;
                     // the buffer's previous reader is the backward of segment seg+2
