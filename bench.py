@@ -266,13 +266,17 @@ def secondary_explicit(hal, torch, stream, warm=5, iters=50):
                       ticks=10)
     cpu_s = time.perf_counter() - t0
     peak, _ = peaks()
-    ach = EXPLICIT_BYTES * CELLS / (ms_launch * 1e-3) / 1e9
+    # one kernel per tick: the graph's time per tick is the mean launch
+    # duration over back-to-back launches
+    ach = EXPLICIT_BYTES * CELLS / (ms_tick * 1e-3) / 1e9
     return {"workload": "explicit-2048x2048-r0.2-decay0.001-64sources-zeroflux",
             "value": CELLS / (ms_tick * 1e-3), "unit": "cell-updates/s",
             "ms_per_tick_graph": ms_tick,
             "roofline": {"kernel": "TickKernel", "bound": "hbm", "achieved": ach, "peak": peak,
                          "unit": "GB/s", "frac": ach / peak,
-                         "traffic": profile_traffic("TickKernel")},
+                         "traffic": profile_traffic("TickKernel"),
+                         "launch_ms_basis": "graph replay of 100 ticks, one launch per tick",
+                         "isolated_launch_ms": ms_launch},
             "accuracy": accuracy(got, ref, "FP64 oracle, 10 ticks from the same float32 field"),
             "cpu_baseline": {"value": 10 * CELLS / cpu_s, "unit": "cell-updates/s", "cores": 1, "kind": "port",
                              "sample": "10 FP64 ticks of the same 2048x2048 workload (oracle, 1 thread)"},
@@ -614,9 +618,13 @@ def main():
     ms_step = total_ms / args.steps
     value = world * CELLS * TICKS / (ms_step * 1e-3)
 
-    # per-kernel launch times (CUDA events around each launch, same data)
+    # per-kernel launch times: the mean of 200 back-to-back launches of each
+    # sweep replayed from a graph (the steady state of the timed region),
+    # and, for reference, single launches between CUDA events
+    adi.profile_graph(20, RATE, DECAY)
+    ms_col, ms_row = adi.profile_graph(TICKS, RATE, DECAY)
     adi.profile(5, RATE, DECAY)
-    ms_col, ms_row = adi.profile(50, RATE, DECAY)
+    ms_col1, ms_row1 = adi.profile(50, RATE, DECAY)
     col_gbs = ADI_COL_BYTES * CELLS / (ms_col * 1e-3) / 1e9
     row_gbs = ADI_ROW_BYTES * CELLS / (ms_row * 1e-3) / 1e9
     if ms_row >= ms_col:
@@ -624,7 +632,7 @@ def main():
     else:
         dom, dom_gbs, dom_bytes = "AdiSweep<kSweepW>", col_gbs, ADI_COL_BYTES
     peak, peak_kind = peaks()
-    tick_gbs = (ADI_COL_BYTES + ADI_ROW_BYTES) * CELLS / ((ms_col + ms_row) * 1e-3) / 1e9
+    tick_gbs = (ADI_COL_BYTES + ADI_ROW_BYTES) * CELLS * TICKS / (ms_step * 1e-3) / 1e9
 
     # end to end through the host-buffer C-ABI call
     out_host = torch.empty_like(field).pin_memory()
@@ -690,9 +698,13 @@ def main():
                          "bytes_per_launch": dom_bytes * CELLS,
                          "launch_ms": {"x-sweep AdiSweep<kSweepW>": ms_col,
                                        "y-sweep AdiSweep<kSweepTick>": ms_row},
+                         "launch_ms_basis": "mean of 200 back-to-back launches replayed from a CUDA graph",
+                         "isolated_launch_ms": {"x-sweep AdiSweep<kSweepW>": ms_col1,
+                                                "y-sweep AdiSweep<kSweepTick>": ms_row1},
                          "achieved_by_kernel": {"x-sweep AdiSweep<kSweepW>": col_gbs,
                                                 "y-sweep AdiSweep<kSweepTick>": row_gbs},
                          "tick_achieved": tick_gbs,
+                         "tick_frac": tick_gbs / peak,
                          "note": "working set (3 x 16.8 MB + scratch) stays in the 126 MB L2 "
                                  "across the ticks of a step"},
             "cpu_baseline": cpu,

@@ -101,6 +101,8 @@ namespace Hal::Cuda
         void SetSource(const std::vector<float> &dense);
         void SetPointSources(const std::vector<int32_t> &cells, const std::vector<float> &values);
         void SetDirichlet(const std::vector<float> &ghost);
+        // PDEGrid2D::Advection(xVel, yVel) in every following tick (upwind).
+        void SetVelocity(double xVel, double yVel);
         void RunTicks(int32_t ticks, double diffRate, double decay, bool wrapX, bool wrapY);
         void Sync();
 

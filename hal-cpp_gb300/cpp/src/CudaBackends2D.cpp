@@ -134,6 +134,11 @@ namespace Hal::Cuda
               "CudaDiffusionBackend2D::AdvectVariable");
     }
 
+    void CudaDiffusionBackend2D::SetVelocity(double xVel, double yVel)
+    {
+        Check(hal_cuda_diffusion_set_velocity(m_pHandle, xVel, yVel), "CudaDiffusionBackend2D::SetVelocity");
+    }
+
     void CudaDiffusionBackend2D::SetField(const std::vector<float> &field)
     {
         Check(hal_cuda_diffusion_set_field(m_pHandle, field.data(), static_cast<int64_t>(field.size())),

@@ -1846,6 +1846,82 @@ extern "C" int hal_cuda_adi_set_stream(hal_cuda_adi *h, void *stream)
     return HAL_CUDA_OK;
 }
 
+extern "C" int hal_cuda_adi_profile_graph(hal_cuda_adi *h, int32_t iters, double diffRate, double decay,
+                                          int32_t wrapX, int32_t wrapY, float *ms)
+{
+    HAL_REQUIRE(h != nullptr && ms != nullptr, "hal_cuda_adi_profile_graph: NULL argument");
+    HAL_REQUIRE(iters > 0, "hal_cuda_adi_profile_graph: iters must be positive");
+    using namespace halcuda;
+    HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    cudaStream_t s = h->stream.Get();
+    const float *g = h->hasGhost ? h->ghost.p : nullptr;
+    HAL_TRY(h->PrepareShapes(diffRate, wrapX != 0, wrapY != 0, g));
+    const int c = h->cur;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    HAL_TRY(CudaStatus(cudaEventCreate(&e0), "cudaEventCreate"));
+    int rc = CudaStatus(cudaEventCreate(&e1), "cudaEventCreate");
+    for (int which = 0; which < 2 && rc == HAL_CUDA_OK; which++)
+    {
+        // `iters` back-to-back launches of one sweep on the same inputs: the
+        // x-sweep rewrites w, the y-sweep rewrites the other parity's field
+        rc = CudaStatus(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+        int lr = HAL_CUDA_OK;
+        for (int32_t t = 0; t < iters && rc == HAL_CUDA_OK && lr == HAL_CUDA_OK; t++)
+        {
+            lr = (which == 0) ? h->LaunchX(h->field[c].p, diffRate, wrapX != 0, wrapY != 0, g, s)
+                              : h->LaunchY<kSweepTick>(h->field[c ^ 1].p, h->field[c].p, nullptr, nullptr, diffRate,
+                                                       decay, wrapX != 0, wrapY != 0, g, true, s);
+        }
+        cudaGraph_t gr = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(s, &gr);
+        if (rc == HAL_CUDA_OK)
+        {
+            rc = (lr != HAL_CUDA_OK) ? lr : CudaStatus(ec, "cudaStreamEndCapture");
+        }
+        cudaGraphExec_t ex = nullptr;
+        if (rc == HAL_CUDA_OK)
+        {
+            rc = CudaStatus(cudaGraphInstantiate(&ex, gr, 0), "cudaGraphInstantiate");
+        }
+        if (gr != nullptr)
+        {
+            cudaGraphDestroy(gr);
+        }
+        if (rc == HAL_CUDA_OK)
+        {
+            rc = CudaStatus(cudaGraphLaunch(ex, s), "cudaGraphLaunch");  // warm-up replay
+        }
+        if (rc == HAL_CUDA_OK)
+        {
+            cudaEventRecord(e0, s);
+            rc = CudaStatus(cudaGraphLaunch(ex, s), "cudaGraphLaunch");
+            cudaEventRecord(e1, s);
+        }
+        if (rc == HAL_CUDA_OK)
+        {
+            rc = CudaStatus(cudaEventSynchronize(e1), "hal_cuda_adi_profile_graph");
+        }
+        if (rc == HAL_CUDA_OK)
+        {
+            float t = 0.0f;
+            cudaEventElapsedTime(&t, e0, e1);
+            ms[which] = t / static_cast<float>(iters);
+            CountLaunch(2 * static_cast<int64_t>(iters));
+        }
+        if (ex != nullptr)
+        {
+            cudaGraphExecDestroy(ex);
+        }
+    }
+    cudaEventDestroy(e0);
+    if (e1 != nullptr)
+    {
+        cudaEventDestroy(e1);
+    }
+    HAL_TRY(rc);
+    return h->CheckDeviceError("hal_cuda_adi_profile_graph");
+}
+
 extern "C" int hal_cuda_adi_profile(hal_cuda_adi *h, int32_t iters, double diffRate, double decay, int32_t wrapX,
                                     int32_t wrapY, float *ms)
 {

@@ -97,7 +97,7 @@ namespace halcuda
         // first result is computed.
         // CTA (bx, by) of the tick of grid p: columns from bx * 32 * VEC, rows
         // from by * kTickWarps * kTickRowsPerThread.
-        template <int VEC>
+        template <int VEC, bool ADV = false>
         __device__ __forceinline__ void TickTile(const TickParams &p, const int32_t bx, const int32_t by)
         {
             constexpr int T = kTickRowsPerThread;
@@ -238,13 +238,26 @@ namespace halcuda
                     const float wYp = (k + 1 < nValid) ? 1.0f : wRight;
                     const float ym = (k > 0) ? cur[k - 1] : left[t];
                     const float wYm = (k > 0) ? 1.0f : wLeft;
-                    // reference order: x+1, x-1, y+1, y-1
-                    float sum = (dn[k] - c) * wDn;
-                    sum = fmaf(up[k] - c, wUp, sum);
-                    sum = fmaf(yp - c, wYp, sum);
-                    sum = fmaf(ym - c, wYm, sum);
-                    float d = sum * p.r;
-                    d = fmaf(c, p.negDecay, d);
+                    float d;
+                    if constexpr (ADV)
+                    {
+                        // diffusion plus upwind advection: one weight per side
+                        float sum = (dn[k] - c) * (wDn * p.kDn);
+                        sum = fmaf(up[k] - c, wUp * p.kUp, sum);
+                        sum = fmaf(yp - c, wYp * p.kYp, sum);
+                        sum = fmaf(ym - c, wYm * p.kYm, sum);
+                        d = fmaf(c, p.negDecay, sum);
+                    }
+                    else
+                    {
+                        // reference order: x+1, x-1, y+1, y-1
+                        float sum = (dn[k] - c) * wDn;
+                        sum = fmaf(up[k] - c, wUp, sum);
+                        sum = fmaf(yp - c, wYp, sum);
+                        sum = fmaf(ym - c, wYm, sum);
+                        d = sum * p.r;
+                        d = fmaf(c, p.negDecay, d);
+                    }
                     o[k] = d + srcv[t][k];
                 }
                 for (int32_t q = ptBeg; q < ptEnd; q++)
@@ -287,11 +300,11 @@ namespace halcuda
             }
         }
 
-        template <int VEC>
+        template <int VEC, bool ADV>
         __global__ void __launch_bounds__(32 * kTickWarps)
             TickKernel(TickParams p)
         {
-            TickTile<VEC>(p, static_cast<int32_t>(blockIdx.x), static_cast<int32_t>(blockIdx.y));
+            TickTile<VEC, ADV>(p, static_cast<int32_t>(blockIdx.x), static_cast<int32_t>(blockIdx.y));
         }
 
         // Batched form: CTA b runs tile tiles[b] = (grid, CTA column, CTA row).
@@ -571,6 +584,7 @@ namespace halcuda
         DevBuf<int32_t> ptStart, ptRow, ptCol;
         DevBuf<float> ptVal;
         bool hasPoints = false;
+        double xVel = 0.0, yVel = 0.0;  // uniform advection of every tick (PDEGrid2D::Advection)
         DevBuf<double> f64, d64, g64;
         DevBuf<double> a64, b64;  // per-cell rates or velocities of the FP64 stencil calls
         DevBuf<double> gv64;      // x- and y-velocity ghost tables of the Dirichlet advection form
@@ -627,18 +641,35 @@ namespace halcuda
             p.ptRow = pts ? ptRow.p : nullptr;
             p.ptCol = pts ? ptCol.p : nullptr;
             p.ptVal = pts ? ptVal.p : nullptr;
+            const double vx = useExtras ? xVel : 0.0, vy = useExtras ? yVel : 0.0;
+            p.kUp = static_cast<float>(r + std::max(vx, 0.0));
+            p.kDn = static_cast<float>(r + std::max(-vx, 0.0));
+            p.kYm = static_cast<float>(r + std::max(vy, 0.0));
+            p.kYp = static_cast<float>(r + std::max(-vy, 0.0));
             return p;
         }
 
         void LaunchTick(const TickParams &p, cudaStream_t s) const
         {
+            const bool adv = p.kUp != p.r || p.kDn != p.r || p.kYm != p.r || p.kYp != p.r;
             if (vec4)
             {
-                TickKernel<4><<<grid, block, 0, s>>>(p);
+                if (adv)
+                {
+                    TickKernel<4, true><<<grid, block, 0, s>>>(p);
+                }
+                else
+                {
+                    TickKernel<4, false><<<grid, block, 0, s>>>(p);
+                }
+            }
+            else if (adv)
+            {
+                TickKernel<1, true><<<grid, block, 0, s>>>(p);
             }
             else
             {
-                TickKernel<1><<<grid, block, 0, s>>>(p);
+                TickKernel<1, false><<<grid, block, 0, s>>>(p);
             }
         }
 
@@ -651,8 +682,8 @@ namespace halcuda
             }
             cudaStream_t s = stream.Get();
             char key[256];
-            snprintf(key, sizeof(key), "%d|%a|%a|%d|%d|%d|%d|%d|%p", ticks, r, decay, wrapX, wrapY,
-                     extras ? 1 : 0, hasSrc, hasGhost, static_cast<void *>(s));
+            snprintf(key, sizeof(key), "%d|%a|%a|%d|%d|%d|%d|%d|%a|%a|%p", ticks, r, decay, wrapX, wrapY,
+                     extras ? 1 : 0, hasSrc, hasGhost, xVel, yVel, static_cast<void *>(s));
             GraphCache &graph = this->graph[cur];
             if (graph.exec == nullptr || graph.key != key)
             {
@@ -1072,6 +1103,18 @@ extern "C" int hal_cuda_diffusion_set_point_sources(hal_cuda_diffusion *h, int32
     HAL_TRY(halcuda::CudaStatus(cudaMemcpy(h->ptVal.p, val.data(), nPoints * sizeof(float), cudaMemcpyHostToDevice),
                                 "cudaMemcpy(points)"));
     h->hasPoints = true;
+    return HAL_CUDA_OK;
+}
+
+extern "C" int hal_cuda_diffusion_set_velocity(hal_cuda_diffusion *h, double xVel, double yVel)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_diffusion_set_velocity: handle is NULL");
+    HAL_REQUIRE(std::isfinite(xVel) && std::isfinite(yVel), "hal_cuda_diffusion_set_velocity: velocity must be finite");
+    HAL_REQUIRE(!(std::fabs(xVel) + std::fabs(yVel) > 0.5),
+                "Advection rate component sum above stable maximum value of 0.5");
+    h->xVel = xVel;
+    h->yVel = yVel;
+    h->ResetGraphs();
     return HAL_CUDA_OK;
 }
 

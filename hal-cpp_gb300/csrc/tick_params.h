@@ -21,7 +21,12 @@ namespace halcuda
         const int32_t *ptStart;    // point sources grouped by CTA (CSR), or null
         const int32_t *ptRow;
         const int32_t *ptCol;
-        const float *ptVal;
+        const float *ptVal;        // Uniform-velocity upwind advection (PDEGrid2D::Advection): the
+        // weight of each neighbour difference is the diffusion rate plus the
+        // upwind velocity from that side -- x-1: r + max(xVel, 0), x+1:
+        // r + max(-xVel, 0), y-1: r + max(yVel, 0), y+1: r + max(-yVel, 0).
+        // Read only by the advective variant of the tick.
+        float kUp, kDn, kYm, kYp;
     };
 
     // Geometry of the tick's CTAs: 32 lanes x kTickWarps warps; a lane owns

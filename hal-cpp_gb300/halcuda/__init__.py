@@ -47,6 +47,7 @@ SIGNATURES = {
     "hal_cuda_diffusion_get_field": (_I, [_vp, _vp, _i64]),
     "hal_cuda_diffusion_set_source": (_I, [_vp, _vp, _i64]),
     "hal_cuda_diffusion_set_point_sources": (_I, [_vp, _i32, _vp, _vp]),
+    "hal_cuda_diffusion_set_velocity": (_I, [_vp, _f64, _f64]),
     "hal_cuda_diffusion_set_dirichlet": (_I, [_vp, _vp]),
     "hal_cuda_diffusion_run_ticks": (_I, [_vp, _i32, _f64, _f64, _i32, _i32]),
     "hal_cuda_diffusion_run_steps": (_I, [_vp, _vp, _i64, _i32, _f64, _i32, _i32]),
@@ -73,6 +74,7 @@ SIGNATURES = {
     "hal_cuda_adi_run_ticks": (_I, [_vp, _i32, _f64, _f64, _i32, _i32]),
     "hal_cuda_adi_run_steps": (_I, [_vp, _vp, _i64, _i32, _f64, _i32, _i32]),
     "hal_cuda_adi_run_ticks_host": (_I, [_vp, _vp, _vp, _i64, _i32, _f64, _f64, _i32, _i32]),
+    "hal_cuda_adi_profile_graph": (_I, [_vp, _i32, _f64, _f64, _i32, _i32, _vp]),
     "hal_cuda_adi_profile": (_I, [_vp, _i32, _f64, _f64, _i32, _i32, _vp]),
     "hal_cuda_adi_sync": (_I, [_vp]),
     "hal_cuda_adi_stream": (_vp, [_vp]),
@@ -379,6 +381,10 @@ class Diffusion(_Handle):
         g = _f32(ghost)
         _check(lib().hal_cuda_diffusion_set_dirichlet(self._h, _p(g)), "set_dirichlet")
 
+    def set_velocity(self, xVel, yVel):
+        """Uniform upwind advection of every following tick (PDEGrid2D::Advection)."""
+        _check(lib().hal_cuda_diffusion_set_velocity(self._h, float(xVel), float(yVel)), "set_velocity")
+
     def run_ticks(self, ticks, diffRate, decay=0.0, wrapX=False, wrapY=False):
         _check(lib().hal_cuda_diffusion_run_ticks(self._h, ticks, diffRate, decay, int(wrapX),
                                                   int(wrapY)), "run_ticks")
@@ -464,6 +470,14 @@ class Adi(_Handle):
         _check(lib().hal_cuda_adi_run_steps(self._h, _p(f), f.size, steps, diffRate, int(wrapX),
                                             int(wrapY)), "run_steps")
         return f
+
+    def profile_graph(self, iters, diffRate, decay=0.0, wrapX=False, wrapY=False):
+        """Mean ms of one x- and one y-sweep launch among `iters` back-to-back
+        launches replayed from a graph (the field does not change)."""
+        ms = np.zeros(2, dtype=np.float32)
+        _check(lib().hal_cuda_adi_profile_graph(self._h, iters, diffRate, decay, int(wrapX), int(wrapY), _p(ms)),
+               "profile_graph")
+        return float(ms[0]), float(ms[1])
 
     def profile(self, iters, diffRate, decay=0.0, wrapX=False, wrapY=False):
         """Average ms of one launch of (x-sweep, y-sweep)."""

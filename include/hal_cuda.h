@@ -165,8 +165,15 @@ int hal_cuda_diffusion_set_point_sources(hal_cuda_diffusion *h, int32_t nPoints,
                                          const int32_t *cells, const float *values);
 int hal_cuda_diffusion_set_dirichlet(hal_cuda_diffusion *h, const float *ghost);
 
+/* Uniform advection velocity of every following tick (PDEGrid2D::Advection
+ * (xVel, yVel[, bc]), PDEGrid2D.h:351-375, after the diffusion term): first-
+ * order upwind, with the handle's Dirichlet table when one is set.  EINVAL
+ * if |xVel| + |yVel| > 0.5 (CheckAdvectionStable, PDEGrid2D.h:444-450).
+ * (0, 0), the default, is pure diffusion. */
+int hal_cuda_diffusion_set_velocity(hal_cuda_diffusion *h, double xVel, double yVel);
+
 /* `ticks` fused ticks on the resident field, each
- *   f' = f + diffRate*L_bc(f) - decay*f + src + points
+ *   f' = f + diffRate*L_bc(f) [+ advection] - decay*f + src + points
  * (PDEGrid2D::Diffusion + MulAll(-decay) + Add + Update).  EINVAL if
  * diffRate > 0.25 (PDEGrid2D::CheckDiffusionStable, PDEGrid2D.h:436-442).
  * Asynchronous on the handle's stream; a run of ticks is replayed from a
@@ -244,11 +251,19 @@ int hal_cuda_adi_run_ticks_host(hal_cuda_adi *h, float *field, const float *src,
                                 int32_t ticks, double diffRate, double decay, int32_t wrapX,
                                 int32_t wrapY);
 
+/* Steady-state profiling: for each sweep, a CUDA graph of `iters`
+ * back-to-back launches on the same inputs (the x-sweep rewrites w, the
+ * y-sweep the other parity's field), replayed once to warm up and once timed;
+ * ms[0] / ms[1] = the mean device time of one x- / y-sweep launch.  The
+ * resident field does not change. */
+int hal_cuda_adi_profile_graph(hal_cuda_adi *h, int32_t iters, double diffRate, double decay,
+                               int32_t wrapX, int32_t wrapY, float *ms);
+
 /* Profiling: runs `iters` ticks with each sweep launched on its own between
  * CUDA events on the handle's stream (no graph), and returns the average
  * device time of one launch of each kernel: ms[0] = x-sweep
- * (AdiColumnSweep), ms[1] = y-sweep with commit (AdiRowSweep).  The resident
- * field advances by `iters` ticks. */
+ * (AdiSweep<kSweepW>), ms[1] = y-sweep with commit (AdiSweep<kSweepTick>).
+ * The resident field advances by `iters` ticks. */
 int hal_cuda_adi_profile(hal_cuda_adi *h, int32_t iters, double diffRate, double decay,
                          int32_t wrapX, int32_t wrapY, float *ms);
 

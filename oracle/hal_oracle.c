@@ -533,6 +533,17 @@ int oracle_tick(int mode, double *field, double *deltas, double *scratch,
                 const double *srcVal, const int32_t *uptakeCount,
                 double uptake, int nthreads)
 {
+    return oracle_tick_adv(mode, field, deltas, scratch, xDim, yDim, diffRate, 0.0, 0.0, wrapX, wrapY, ghost,
+                           decay, srcDense, nSrc, srcIdx, srcVal, uptakeCount, uptake, nthreads);
+}
+
+int oracle_tick_adv(int mode, double *field, double *deltas, double *scratch,
+                    int32_t xDim, int32_t yDim, double diffRate, double xVel, double yVel,
+                    int wrapX, int wrapY, const double *ghost, double decay,
+                    const double *srcDense, int32_t nSrc, const int32_t *srcIdx,
+                    const double *srcVal, const int32_t *uptakeCount,
+                    double uptake, int nthreads)
+{
     int32_t length = xDim * yDim;
     if (mode == 0)
     {
@@ -547,6 +558,16 @@ int oracle_tick(int mode, double *field, double *deltas, double *scratch,
     {
         oracle_adi2_mt(field, scratch, deltas, diffRate, xDim, yDim, wrapX, wrapY, ghost,
                        nthreads);
+    }
+    if (xVel != 0.0 || yVel != 0.0)
+    {
+        /* PDEGrid2D::Advection(xVel, yVel[, bc]) (PDEGrid2D.h:351-375), after
+         * CheckAdvectionStable (:444-450) */
+        if (fabs(xVel) + fabs(yVel) > 0.5)
+        {
+            return -2;
+        }
+        oracle_advection2_bc(field, deltas, xVel, yVel, xDim, yDim, wrapX, wrapY, ghost);
     }
     if (decay != 0.0)
     {

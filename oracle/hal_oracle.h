@@ -84,6 +84,17 @@ int oracle_tick(int mode, double *field, double *deltas, double *scratch,
                 const double *srcVal, const int32_t *uptakeCount,
                 double uptake, int nthreads);
 
+/* The same tick with PDEGrid2D::Advection(xVel, yVel[, bc]) (PDEGrid2D.h:
+ * 351-375) after the diffusion term: first-order upwind at a uniform
+ * velocity, with the Dirichlet form when a ghost table is given.  Returns -2
+ * when |xVel| + |yVel| > 0.5 (CheckAdvectionStable, :444-450). */
+int oracle_tick_adv(int mode, double *field, double *deltas, double *scratch,
+                    int32_t xDim, int32_t yDim, double diffRate, double xVel, double yVel,
+                    int wrapX, int wrapY, const double *ghost, double decay,
+                    const double *srcDense, int32_t nSrc, const int32_t *srcIdx,
+                    const double *srcVal, const int32_t *uptakeCount,
+                    double uptake, int nthreads);
+
 /* ---- cell-bucket agent forces (src/Agents/CpuAgentForceBackend2D.cpp) ---- */
 
 /* Passes 1-3 (:85-109): counts -> exclusive offsets (numCells+1 entries,

@@ -80,6 +80,9 @@ class Oracle(_Lib):
         L.oracle_tick.argtypes = [ctypes.c_int, vp, vp, vp, i32, i32, f64, ctypes.c_int,
                                   ctypes.c_int, vp, f64, vp, i32, vp, vp, vp, f64, ctypes.c_int]
         L.oracle_tick.restype = ctypes.c_int
+        L.oracle_tick_adv.argtypes = [ctypes.c_int, vp, vp, vp, i32, i32, f64, f64, f64, ctypes.c_int,
+                                      ctypes.c_int, vp, f64, vp, i32, vp, vp, vp, f64, ctypes.c_int]
+        L.oracle_tick_adv.restype = ctypes.c_int
         L.oracle_agent_bins.argtypes = [vp, i32, i32, i32, vp, vp]
         L.oracle_accumulate_forces.argtypes = [vp, vp, i32, vp, f64, f64, i32, i32, ctypes.c_int,
                                                ctypes.c_int, vp, vp, ctypes.c_int]
@@ -129,7 +132,7 @@ class Oracle(_Lib):
     @classmethod
     def run_ticks(cls, mode, field, xDim, yDim, r, wrapX=False, wrapY=False, ghost=None,
                   decay=0.0, src_dense=None, src_idx=None, src_val=None, uptake_count=None,
-                  uptake=0.0, ticks=1, threads=1):
+                  uptake=0.0, ticks=1, threads=1, xVel=0.0, yVel=0.0):
         """Run ``ticks`` PDEGrid2D ticks (mode 0 explicit, 1 ADI); returns the
         final field (float64)."""
         f = _f64(field).copy()
@@ -144,14 +147,17 @@ class Oracle(_Lib):
         ns = 0 if si is None else len(si)
         L = cls.lib()
         for _ in range(ticks):
-            rc = L.oracle_tick(mode, f.ctypes.data, d.ctypes.data, s.ctypes.data, xDim, yDim, r,
-                               int(wrapX), int(wrapY), None if g is None else g.ctypes.data,
-                               decay, None if sd is None else sd.ctypes.data, ns,
-                               None if si is None else si.ctypes.data,
-                               None if sv is None else sv.ctypes.data,
-                               None if uc is None else uc.ctypes.data, uptake, int(threads))
-            if rc != 0:
+            rc = L.oracle_tick_adv(mode, f.ctypes.data, d.ctypes.data, s.ctypes.data, xDim, yDim, r,
+                                   float(xVel), float(yVel), int(wrapX), int(wrapY),
+                                   None if g is None else g.ctypes.data,
+                                   decay, None if sd is None else sd.ctypes.data, ns,
+                                   None if si is None else si.ctypes.data,
+                                   None if sv is None else sv.ctypes.data,
+                                   None if uc is None else uc.ctypes.data, uptake, int(threads))
+            if rc == -1:
                 raise ValueError("Diffusion rate above stable maximum value of 0.25")
+            if rc != 0:
+                raise ValueError("Advection rate component sum above stable maximum value of 0.5")
         return f
 
     # -- agents ------------------------------------------------------------
@@ -311,6 +317,8 @@ class Reference(_Lib):
         L.ref_diffuse_adi_bc.argtypes = [vp, vp, f64, i32, i32, ci, ci, vp]
         L.ref_pdegrid_run.argtypes = [ci, vp, i32, i32, ci, ci, f64, vp, f64, vp, i32, vp, vp, vp,
                                       f64, i32]
+        L.ref_pdegrid_run_adv.argtypes = [ci, vp, i32, i32, ci, ci, f64, f64, f64, vp, f64, vp, i32, vp, vp,
+                                          vp, f64, i32]
         L.ref_accumulate_forces.argtypes = [vp, i64, vp, i64, vp, f64, f64, i32, i32, ci, ci, vp,
                                             vp]
         L.ref_rand_draws.argtypes = [ctypes.c_uint64, ci, i32, i32, vp]
@@ -430,13 +438,13 @@ class Reference(_Lib):
     @classmethod
     def run_ticks(cls, mode, field, xDim, yDim, r, wrapX=False, wrapY=False, ghost=None,
                   decay=0.0, src_dense=None, src_idx=None, src_val=None, uptake_count=None,
-                  uptake=0.0, ticks=1):
+                  uptake=0.0, ticks=1, xVel=0.0, yVel=0.0):
         f = _f64(field).copy()
         g, sd, si, sv, uc = _f64(ghost), _f64(src_dense), _i32(src_idx), _f64(src_val), \
             _i32(uptake_count)
         ns = 0 if si is None else len(si)
-        rc = cls.lib().ref_pdegrid_run(mode, f.ctypes.data, xDim, yDim, int(wrapX), int(wrapY),
-                                       r, None if g is None else g.ctypes.data, decay,
+        rc = cls.lib().ref_pdegrid_run_adv(mode, f.ctypes.data, xDim, yDim, int(wrapX), int(wrapY),
+                                       r, float(xVel), float(yVel), None if g is None else g.ctypes.data, decay,
                                        None if sd is None else sd.ctypes.data, ns,
                                        None if si is None else si.ctypes.data,
                                        None if sv is None else sv.ctypes.data,

@@ -356,6 +356,87 @@ extern "C"
             std::memcpy(field, grid.GetField().data(), sizeof(double) * static_cast<size_t>(length)); });
     }
 
+    // The same tick loop with PDEGrid2D::Advection(xVel, yVel[, bc]) after
+    // the diffusion term.
+    int ref_pdegrid_run_adv(int mode, double *field, int32_t xDim, int32_t yDim, int wrapX, int wrapY,
+                            double diffRate, double xVel, double yVel, const double *ghost, double decay, const double *srcDense,
+                        int32_t nSrc, const int32_t *srcIdx, const double *srcVal,
+                        const int32_t *uptakeCount, double uptake, int32_t ticks)
+    {
+        Quiet();
+        return Guard([&]()
+                     {
+            Hal::PDEGrid2D grid(xDim, yDim, wrapX != 0, wrapY != 0);
+            int32_t length = xDim * yDim;
+            std::vector<double> f(field, field + length);
+            std::vector<double> zeros(static_cast<size_t>(length), 0.0);
+            grid.SetState(f, zeros, 0);
+            GhostBc bc{ghost, xDim, yDim};
+            for (int32_t t = 0; t < ticks; t++)
+            {
+                if (mode == 0)
+                {
+                    if (ghost != nullptr)
+                    {
+                        grid.Diffusion(diffRate, bc);
+                    }
+                    else
+                    {
+                        grid.Diffusion(diffRate);
+                    }
+                }
+                else
+                {
+                    if (ghost != nullptr)
+                    {
+                        grid.DiffusionADI(diffRate, bc);
+                    }
+                    else
+                    {
+                        grid.DiffusionADI(diffRate);
+                    }
+                }
+                if (xVel != 0.0 || yVel != 0.0)
+                {
+                    if (ghost != nullptr)
+                    {
+                        grid.Advection(xVel, yVel, bc);
+                    }
+                    else
+                    {
+                        grid.Advection(xVel, yVel);
+                    }
+                }
+                if (decay != 0.0)
+                {
+                    grid.MulAll(-decay);
+                }
+                if (srcDense != nullptr)
+                {
+                    for (int32_t i = 0; i < length; i++)
+                    {
+                        grid.Add(i, srcDense[i]);
+                    }
+                }
+                for (int32_t k = 0; k < nSrc; k++)
+                {
+                    grid.Add(srcIdx[k], srcVal[k]);
+                }
+                if (uptakeCount != nullptr)
+                {
+                    for (int32_t i = 0; i < length; i++)
+                    {
+                        for (int32_t a = 0; a < uptakeCount[i]; a++)
+                        {
+                            grid.Mul(i, -uptake);
+                        }
+                    }
+                }
+                grid.Update();
+            }
+            std::memcpy(field, grid.GetField().data(), sizeof(double) * static_cast<size_t>(length)); });
+    }
+
     // IAgentForceBackend2D::AccumulateForces through
     // Hal::CpuAgentForceBackend2D; also returns its bins.  cellOffsets holds
     // xDim*yDim+1 entries and bucketAgents n entries (either may be null).

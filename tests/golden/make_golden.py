@@ -242,6 +242,29 @@ def agent_move_cases(rng):
     return out
 
 
+def adv_tick_cases(rng):
+    """PDEGrid2D ticks with Advection(xVel, yVel[, bc]) after the diffusion
+    term (include/Hal/Grids/PDEGrid2D.h:351-375), decay and a dense source,
+    run by the reference's own PDEGrid2D."""
+    out = {}
+    cases = [(40, 33, 0, 0, False, 0.2, 0.15, -0.2), (33, 40, 1, 1, False, 0.24, -0.3, 0.1),
+             (48, 20, 0, 1, True, 0.1, 0.25, 0.25), (17, 64, 1, 0, True, 0.2, 0.0, -0.45)]
+    for k, (xd, yd, wx, wy, bc, r, xv, yv) in enumerate(cases):
+        f = rng.random(xd * yd)
+        src = rng.random(xd * yd) * 0.01
+        gh = rng.random(2 * (xd + yd)) if bc else None
+        pre = f"c{k}_"
+        out[pre + "dims"] = np.array([xd, yd, wx, wy, int(bc)], dtype=np.int32)
+        out[pre + "params"] = np.array([r, xv, yv, 0.005])
+        out[pre + "field"], out[pre + "src"] = f, src
+        if bc:
+            out[pre + "ghost"] = gh
+        out[pre + "out"] = R.run_ticks(0, f, xd, yd, r, wx, wy, gh, decay=0.005, src_dense=src, ticks=6,
+                                       xVel=xv, yVel=yv)
+    out["count"] = np.array([len(cases)])
+    return out
+
+
 def pdegrid_file():
     """A PDEGrid2D file written by the reference's SavePDEGrid2D
     (src/Grids/PDEGridSerialization.cpp:34-45): 13 x 7, wrapX only, update
@@ -265,8 +288,9 @@ def main():
     np.savez_compressed(os.path.join(HERE, "rand.npz"), **rand_cases())
     np.savez_compressed(os.path.join(HERE, "varstencil.npz"), **var_stencil_cases(np.random.default_rng(8181)))
     np.savez_compressed(os.path.join(HERE, "agentmove.npz"), **agent_move_cases(np.random.default_rng(9191)))
+    np.savez_compressed(os.path.join(HERE, "advtick.npz"), **adv_tick_cases(np.random.default_rng(6262)))
     print(pdegrid_file())
-    for name in ("stencil", "ticks", "agents", "rand", "varstencil", "agentmove"):
+    for name in ("stencil", "ticks", "agents", "rand", "varstencil", "agentmove", "advtick"):
         p = os.path.join(HERE, name + ".npz")
         print(f"{p}: {os.path.getsize(p)} bytes")
 

@@ -189,3 +189,27 @@ def test_host_ticks_match_resident_ticks(hal):
         res = a.get_field()
         host = a.run_ticks_host(f32.copy(), s32, 7, 5.0, 0.01)
     assert np.array_equal(res, host)
+
+
+def test_profile_graph_leaves_the_field(hal):
+    """The steady-state sweep profile replays back-to-back launches on the
+    same inputs and leaves the resident field as it was; the ticks after it
+    equal ticks without it."""
+    n = 256
+    rng = np.random.default_rng(12)
+    f0 = rng.random(n * n).astype(np.float32)
+    src = (rng.random(n * n) * 0.01).astype(np.float32)
+    outs = []
+    for probe in (False, True):
+        with hal.Adi(n, n) as a:
+            a.set_field(f0)
+            a.set_source(src)
+            a.run_ticks(3, 5.0, 0.01)
+            if probe:
+                before = a.get_field()
+                msx, msy = a.profile_graph(10, 5.0, 0.01)
+                assert msx > 0 and msy > 0
+                assert np.array_equal(a.get_field(), before)
+            a.run_ticks(3, 5.0, 0.01)
+            outs.append(a.get_field())
+    assert np.array_equal(outs[0], outs[1])

@@ -129,6 +129,61 @@ def test_advection_special_velocities(hal, oracle):
         assert np.array_equal(a.view(np.int64), b.view(np.int64))
 
 
+def test_advection_tick_golden(hal, golden):
+    """Resident FP32 ticks with uniform advection against PDEGrid2D ticks
+    (Diffusion, Advection, MulAll, Add, Update) written by the reference."""
+    g = golden("advtick")
+    for k in range(int(g["count"][0])):
+        xd, yd, wx, wy, bc = (int(v) for v in g[f"c{k}_dims"])
+        r, xv, yv, decay = (float(v) for v in g[f"c{k}_params"])
+        f32 = g[f"c{k}_field"].astype(np.float32)
+        with hal.Diffusion(xd, yd) as d:
+            d.set_field(f32)
+            d.set_source(g[f"c{k}_src"].astype(np.float32))
+            if bc:
+                d.set_dirichlet(g[f"c{k}_ghost"].astype(np.float32))
+            d.set_velocity(xv, yv)
+            d.run_ticks(6, r, decay, wx, wy)
+            out = d.get_field()
+        # the golden run starts from the float64 field: allow its rounding
+        assert max_rel(out, g[f"c{k}_out"]) <= 2e-6, k
+
+
+def test_advection_tick_matches_oracle(hal, oracle):
+    """500 ticks of diffusion plus advection at 256^2 (Dirichlet edges, 64
+    point sources, decay) against the FP64 oracle from the same float32
+    start; zero velocity reproduces the plain tick bit for bit."""
+    from halcuda import workloads
+
+    w = workloads.explicit_inputs(256, seed=5)
+    f32 = w["field"].astype(np.float32)
+    g32 = w["ghost"].astype(np.float32)
+    for xv, yv in ((0.2, -0.15), (-0.3, 0.2), (0.0, 0.45)):
+        # r = 0.1 keeps the centre weight 1 - 4r - |xVel| - |yVel| positive
+        ref = oracle.run_ticks(0, f32.astype(np.float64), 256, 256, 0.1, ghost=g32.astype(np.float64), decay=0.001,
+                               src_idx=w["src_idx"], src_val=w["src_val"], ticks=500, xVel=xv, yVel=yv)
+        with hal.Diffusion(256, 256) as d:
+            d.set_field(f32)
+            d.set_dirichlet(g32)
+            d.set_point_sources(w["src_idx"], w["src_val"])
+            d.set_velocity(xv, yv)
+            d.run_ticks(500, 0.1, 0.001)
+            out = d.get_field()
+        assert rel_l2(out, ref) <= 1e-5, (xv, yv)
+    outs = []
+    for vel in (None, (0.0, 0.0)):
+        with hal.Diffusion(64, 48) as d:
+            d.set_field(f32[:64 * 48])
+            if vel is not None:
+                d.set_velocity(*vel)
+            d.run_ticks(20, 0.2, 0.01, True, False)
+            outs.append(d.get_field())
+    assert np.array_equal(outs[0], outs[1])
+    with hal.Diffusion(8, 8) as d:
+        with pytest.raises(ValueError):
+            d.set_velocity(0.3, -0.3)
+
+
 def test_eigenmode_decay_through_interface(hal):
     """tests/IDiffusionBackend2DTests.cpp:23-72 (GPU epsilon 1e-4 there)."""
     nx, ny, r = 16, 20, 0.05

@@ -83,6 +83,20 @@ def test_var_stencil_conservation_kat(oracle):
     assert not oracle.diffuse_var(np.full(n, 2.5), z, rx, ry, xd, yd, 0, 0).any()
 
 
+def test_advection_tick_golden_bit_exact(oracle, golden):
+    """PDEGrid2D ticks with Advection(xVel, yVel[, bc]) after the diffusion
+    term, against the reference's own PDEGrid2D, bit for bit."""
+    g = golden("advtick")
+    for k in range(int(g["count"][0])):
+        xd, yd, wx, wy, bc = (int(v) for v in g[f"c{k}_dims"])
+        r, xv, yv, decay = (float(v) for v in g[f"c{k}_params"])
+        out = oracle.run_ticks(0, g[f"c{k}_field"], xd, yd, r, wx, wy, g[f"c{k}_ghost"] if bc else None,
+                               decay=decay, src_dense=g[f"c{k}_src"], ticks=6, xVel=xv, yVel=yv)
+        assert np.array_equal(out, g[f"c{k}_out"]), k
+    with pytest.raises(ValueError):  # CheckAdvectionStable
+        oracle.run_ticks(0, np.zeros(4), 2, 2, 0.1, xVel=0.3, yVel=-0.3)
+
+
 def test_agent_move_golden_bit_exact(oracle, golden):
     """SphericalAgent2D's update after its forces (SetVelocity, CapVelocity,
     ForceMove -> MoveSafePT, ApplyFriction) against the reference's agent
