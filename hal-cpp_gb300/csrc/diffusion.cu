@@ -97,6 +97,98 @@ namespace halcuda
         // first result is computed.
         // CTA (bx, by) of the tick of grid p: columns from bx * 32 * VEC, rows
         // from by * kTickWarps * kTickRowsPerThread.
+        // The tick of a thread whose strip and every neighbour of it lie on
+        // the grid (rows xs-1 .. xs+T, columns y0-1 .. y0+4): no wrap, ghost
+        // or zero-flux cases, so every difference weight is 1.  The
+        // arithmetic is the general path's with those weights (x * 1 and
+        // fmaf(x, 1, y) round as x and x + y), so results are bit-identical.
+        template <bool ADV>
+        __device__ __forceinline__ void TickInterior(const TickParams &p, const int32_t bx, const int32_t by,
+                                                     const int32_t y0, const int32_t xs)
+        {
+            constexpr int T = kTickRowsPerThread;
+            const int64_t yD = p.yDim;
+            float4 rows[T + 2];
+#pragma unroll
+            for (int j = 0; j < T + 2; j++)
+            {
+                rows[j] = __ldg(reinterpret_cast<const float4 *>(p.f + (xs - 1 + j) * yD + y0));
+            }
+            float left[T], right[T];
+            float4 srcv[T];
+#pragma unroll
+            for (int t = 0; t < T; t++)
+            {
+                const float *rowp = p.f + (xs + t) * yD;
+                left[t] = __ldg(rowp + y0 - 1);
+                right[t] = __ldg(rowp + y0 + 4);
+                srcv[t] = (p.src != nullptr) ? __ldg(reinterpret_cast<const float4 *>(p.src + (xs + t) * yD + y0))
+                                             : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            }
+            int32_t ptBeg = 0, ptEnd = 0;
+            if (p.ptStart != nullptr)
+            {
+                const int32_t gridX = (p.yDim + 32 * 4 - 1) / (32 * 4);
+                const int32_t b = by * gridX + bx;
+                ptBeg = __ldg(p.ptStart + b);
+                ptEnd = __ldg(p.ptStart + b + 1);
+            }
+#pragma unroll
+            for (int t = 0; t < T; t++)
+            {
+                const float up[4] = {rows[t].x, rows[t].y, rows[t].z, rows[t].w};
+                const float cur[4] = {rows[t + 1].x, rows[t + 1].y, rows[t + 1].z, rows[t + 1].w};
+                const float dn[4] = {rows[t + 2].x, rows[t + 2].y, rows[t + 2].z, rows[t + 2].w};
+                const float sv[4] = {srcv[t].x, srcv[t].y, srcv[t].z, srcv[t].w};
+                float o[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                {
+                    const float c = cur[k];
+                    const float yp = (k < 3) ? cur[k + 1] : right[t];
+                    const float ym = (k > 0) ? cur[k - 1] : left[t];
+                    float d;
+                    if constexpr (ADV)
+                    {
+                        float sum = (dn[k] - c) * p.kDn;
+                        sum = fmaf(up[k] - c, p.kUp, sum);
+                        sum = fmaf(yp - c, p.kYp, sum);
+                        sum = fmaf(ym - c, p.kYm, sum);
+                        d = fmaf(c, p.negDecay, sum);
+                    }
+                    else
+                    {
+                        float sum = dn[k] - c;
+                        sum = (up[k] - c) + sum;
+                        sum = (yp - c) + sum;
+                        sum = (ym - c) + sum;
+                        d = sum * p.r;
+                        d = fmaf(c, p.negDecay, d);
+                    }
+                    o[k] = d + sv[k];
+                }
+                const int32_t x = xs + t;
+                for (int32_t q = ptBeg; q < ptEnd; q++)
+                {
+                    if (__ldg(p.ptRow + q) == x)
+                    {
+                        const int32_t col = __ldg(p.ptCol + q) - y0;
+                        const float val = __ldg(p.ptVal + q);
+#pragma unroll
+                        for (int k = 0; k < 4; k++)
+                        {
+                            if (col == k)
+                            {
+                                o[k] += val;
+                            }
+                        }
+                    }
+                }
+                *reinterpret_cast<float4 *>(p.out + x * yD + y0) =
+                    make_float4(cur[0] + o[0], cur[1] + o[1], cur[2] + o[2], cur[3] + o[3]);
+            }
+        }
+
         template <int VEC, bool ADV = false>
         __device__ __forceinline__ void TickTile(const TickParams &p, const int32_t bx, const int32_t by)
         {
@@ -108,6 +200,14 @@ namespace halcuda
             if (y0 >= p.yDim || xs >= p.xDim)
             {
                 return;
+            }
+            if constexpr (VEC == 4)
+            {
+                if (xs >= 1 && xs + T < p.xDim && y0 >= 1 && y0 + 4 < p.yDim)
+                {
+                    TickInterior<ADV>(p, bx, by, y0, xs);
+                    return;
+                }
             }
             const int nValid = min(VEC, p.yDim - y0);
 
