@@ -27,7 +27,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
                   "--expt-relaxed-constexpr", "-I", INCLUDE, "-I", CSRC]
 
-SOURCES = ["core.cu", "diffusion.cu", "adi.cu", "adi_plan.cpp", "agents.cu", "wells.cu", "adjoint.cu", "pde_io.cpp"]
+SOURCES = ["core.cu", "diffusion.cu", "adi.cu", "adi_plan.cpp", "agents.cu", "wells.cu", "adjoint.cu", "pde_io.cpp", "tick_blocked.cu"]
 
 
 def _nvcc():

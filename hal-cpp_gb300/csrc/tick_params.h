@@ -37,4 +37,34 @@ namespace halcuda
     // Batched ticks: tile b = (grid index, CTA column, CTA row) of the
     // table's grids.  vec is 4 (every grid's yDim % 4 == 0) or 1.
     int LaunchTickTiles(const TickParams *table, const int4 *tiles, int32_t nTiles, int vec, cudaStream_t s);
+
+    // ---- two ticks per launch (temporal blocking, tick_blocked.cu) --------
+    // A CTA computes a kTickBlockRows x kTickBlockCols tile; the field must
+    // have yDim % 4 == 0 and a 16-byte aligned base.
+    constexpr int kTickBlockRows = 32;
+    constexpr int kTickBlockCols = 128;
+
+    struct TickBlockParams
+    {
+        const float *f;
+        float *out;
+        int32_t xDim, yDim;
+        float r, negDecay;
+        int32_t wrapX, wrapY;
+        const float *S;            // dense source plus point sources, or null
+        GhostView ghost;           // all null for zero-flux
+        float kUp, kDn, kYm, kYp;  // per-side weights when advecting (see TickParams)
+        int32_t adv;
+        int32_t *err;              // set to 1 if a staging wait gave up
+    };
+
+    // Opaque 128-byte tensor map (a CUtensorMap) over one field buffer.
+    struct alignas(64) TickBlockTensorMap
+    {
+        unsigned char bytes[128];
+    };
+
+    bool MakeTickBlockTensorMap(TickBlockTensorMap &map, const float *field, int32_t xDim, int32_t yDim);
+    int PrepareTickBlocked();
+    void LaunchTickBlocked2(const TickBlockParams &p, const TickBlockTensorMap &map, cudaStream_t s);
 }

@@ -47,6 +47,7 @@ SIGNATURES = {
     "hal_cuda_diffusion_get_field": (_I, [_vp, _vp, _i64]),
     "hal_cuda_diffusion_set_source": (_I, [_vp, _vp, _i64]),
     "hal_cuda_diffusion_set_point_sources": (_I, [_vp, _i32, _vp, _vp]),
+    "hal_cuda_diffusion_set_blocking": (_I, [_vp, _i32]),
     "hal_cuda_diffusion_set_velocity": (_I, [_vp, _f64, _f64]),
     "hal_cuda_diffusion_set_dirichlet": (_I, [_vp, _vp]),
     "hal_cuda_diffusion_run_ticks": (_I, [_vp, _i32, _f64, _f64, _i32, _i32]),
@@ -380,6 +381,10 @@ class Diffusion(_Handle):
     def set_dirichlet(self, ghost):
         g = _f32(ghost)
         _check(lib().hal_cuda_diffusion_set_dirichlet(self._h, _p(g)), "set_dirichlet")
+
+    def set_blocking(self, ticksPerLaunch):
+        """Ticks per launch: 1, 2 (temporal blocking) or 0 (by grid size)."""
+        _check(lib().hal_cuda_diffusion_set_blocking(self._h, int(ticksPerLaunch)), "set_blocking")
 
     def set_velocity(self, xVel, yVel):
         """Uniform upwind advection of every following tick (PDEGrid2D::Advection)."""

@@ -165,6 +165,17 @@ int hal_cuda_diffusion_set_point_sources(hal_cuda_diffusion *h, int32_t nPoints,
                                          const int32_t *cells, const float *values);
 int hal_cuda_diffusion_set_dirichlet(hal_cuda_diffusion *h, const float *ghost);
 
+/* Ticks per launch of the resident explicit tick: 1, 2 (temporal blocking:
+ * a CTA stages its tile with a 2-cell halo by TMA and computes two ticks in
+ * shared memory, so a pair of ticks reads and writes the field once), or 0
+ * (the default: 1, which measures faster on GB300 at every size -- the
+ * one-tick kernel streams large fields at over 80% of HBM peak, and the
+ * two-tick kernel spends more instructions per cell than it saves in
+ * bytes).  Two ticks need yDim % 4 == 0 (ENOTSUP otherwise).  With 2 the
+ * dense source and the point sources are added as one pre-summed array, so
+ * results match the one-tick launches to FP32 rounding, not bit for bit. */
+int hal_cuda_diffusion_set_blocking(hal_cuda_diffusion *h, int32_t ticksPerLaunch);
+
 /* Uniform advection velocity of every following tick (PDEGrid2D::Advection
  * (xVel, yVel[, bc]), PDEGrid2D.h:351-375, after the diffusion term): first-
  * order upwind, with the handle's Dirichlet table when one is set.  EINVAL
