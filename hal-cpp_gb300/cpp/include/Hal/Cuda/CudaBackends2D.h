@@ -229,6 +229,11 @@ namespace Hal::Cuda
                        const std::vector<float> &radii);
         void RunTicks(int32_t ticks, double interactionRad, double springConstant);
         void GetForces(std::vector<float> &velocityDeltas);
+        // Agents move after their forces each tick (SphericalAgent2D's update,
+        // as CudaAgentForceBackend2D::Step), each within its own well.
+        void SetMotion(bool enabled, double friction, double maxVel = -1.0);
+        void SetVelocities(const std::vector<float> &velocities);
+        void GetAgents(std::vector<float> &positions, std::vector<float> &velocities);
         void Sync();
 
         hal_cuda_wells *Handle() const { return m_pHandle; }

@@ -435,6 +435,27 @@ namespace Hal::Cuda
               "CudaWells2D::GetForces");
     }
 
+    void CudaWells2D::SetMotion(bool enabled, double friction, double maxVel)
+    {
+        Check(hal_cuda_wells_set_motion(m_pHandle, enabled, friction, maxVel), "CudaWells2D::SetMotion");
+    }
+
+    void CudaWells2D::SetVelocities(const std::vector<float> &velocities)
+    {
+        Check(hal_cuda_wells_set_velocities(m_pHandle, velocities.empty() ? nullptr : velocities.data(),
+                                            static_cast<int64_t>(velocities.size())),
+              "CudaWells2D::SetVelocities");
+    }
+
+    void CudaWells2D::GetAgents(std::vector<float> &positions, std::vector<float> &velocities)
+    {
+        positions.resize(2 * static_cast<size_t>(m_agents));
+        velocities.resize(2 * static_cast<size_t>(m_agents));
+        Check(hal_cuda_wells_get_agents(m_pHandle, positions.data(), velocities.data(),
+                                        static_cast<int64_t>(positions.size())),
+              "CudaWells2D::GetAgents");
+    }
+
     void CudaWells2D::Sync()
     {
         Check(hal_cuda_wells_sync(m_pHandle), "CudaWells2D::Sync");

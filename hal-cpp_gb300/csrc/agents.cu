@@ -595,6 +595,41 @@ namespace halcuda
                        ForceSlot<float>(slot, offsets + wd.cellBase, sPos, sRad, interactionRad, R, k, wd.xDim,
                                         wd.yDim, wd.wrapX, wd.wrapY));
         }
+
+        // ForcesWells with each agent's SphericalAgent2D update fused, moved
+        // within its own well (its sizes and wrap flags).
+        __global__ void ForcesWellsMove(const int32_t *__restrict__ bucket, const int32_t *__restrict__ offsets,
+                                        const float2 *__restrict__ sPos, const float *__restrict__ sRad,
+                                        const int32_t *__restrict__ wellOf, const AgentWellDev *__restrict__ wells,
+                                        int32_t n, double interactionRad, float R, float k, float friction,
+                                        float maxVel, float *__restrict__ vel, float2 *__restrict__ pos,
+                                        float2 *__restrict__ velocity)
+        {
+            const int32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+            if (slot >= n)
+            {
+                return;
+            }
+            const int32_t i = bucket[slot];
+            const AgentWellDev wd = wells[wellOf[i]];
+            const V2<float> d = ForceSlot<float>(slot, offsets + wd.cellBase, sPos, sRad, interactionRad, R, k, wd.xDim,
+                                                 wd.yDim, wd.wrapX, wd.wrapY);
+            StoreDelta(vel, i, d);
+            MoveParams mp;
+            mp.friction = friction;
+            mp.maxVel = maxVel;
+            mp.xDimF = static_cast<float>(wd.xDim);
+            mp.yDimF = static_cast<float>(wd.yDim);
+            mp.wrapX = wd.wrapX;
+            mp.wrapY = wd.wrapY;
+            float2 p = sPos[slot];
+            float2 v = velocity[i];
+            v.x = __fadd_rn(v.x, d.x);
+            v.y = __fadd_rn(v.y, d.y);
+            MoveAgent(mp, p, v);
+            pos[i] = p;
+            velocity[i] = v;
+        }
     }
 
     struct Agents
@@ -1269,8 +1304,18 @@ namespace halcuda
         Stabilize<float, float><<<ablocks, T, 0, s>>>(a.cellOf, a.offsets, a.bucketTmp, a.posF, a.rad, a.n, a.bucket,
                                                       a.sPos, a.sRad);
         const int TF = (a.forceThreads == 64 || a.forceThreads == 256) ? a.forceThreads : 128;
-        ForcesWells<<<static_cast<unsigned>((a.n + TF - 1) / TF), TF, 0, s>>>(
-            a.bucket, a.offsets, a.sPos, a.sRad, a.wellOf, a.wells, a.n, a.interactionRad, a.R, a.k, a.vel);
+        const unsigned fblocks = static_cast<unsigned>((a.n + TF - 1) / TF);
+        if (a.velState != nullptr)
+        {
+            ForcesWellsMove<<<fblocks, TF, 0, s>>>(a.bucket, a.offsets, a.sPos, a.sRad, a.wellOf, a.wells, a.n,
+                                                   a.interactionRad, a.R, a.k, a.friction, a.maxVel, a.vel, a.posOut,
+                                                   a.velState);
+        }
+        else
+        {
+            ForcesWells<<<fblocks, TF, 0, s>>>(a.bucket, a.offsets, a.sPos, a.sRad, a.wellOf, a.wells, a.n,
+                                               a.interactionRad, a.R, a.k, a.vel);
+        }
         CountLaunch(7);
         return LaunchStatus("agent wells");
     }

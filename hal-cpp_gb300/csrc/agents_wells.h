@@ -35,6 +35,13 @@ namespace halcuda
         float R, k;
         float *vel;                // 2n, overwritten
         int32_t forceThreads = 128;  // block size of the force kernel (64, 128 or 256)
+        // Motion (SphericalAgent2D's update after the forces, the resident
+        // step of hal_cuda_agents_step): with velState set, each agent's
+        // velocity takes its delta, is capped (maxVel >= 0), moves the agent
+        // (posOut, agent order, the well's own wrap) and takes the friction.
+        float2 *velState = nullptr;  // n, or null: forces only
+        float2 *posOut = nullptr;    // n: the positions, rewritten in place
+        float friction = 1.0f, maxVel = -1.0f;
     };
 
     int32_t AgentScanTiles(int64_t cells);

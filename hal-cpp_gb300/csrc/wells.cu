@@ -93,6 +93,9 @@ namespace halcuda
         std::vector<int32_t> counts;     // agents per well (last set_agents)
         DevBuf<AgentWellDev> agentWells;
         DevBuf<float> apos, arad, avel, sRad;
+        DevBuf<float2> avelState;        // agents' own velocities, for motion
+        bool motion = false;             // agents move after their forces each tick
+        float friction = 1.0f, maxVel = -1.0f;
         DevBuf<float2> posF, sPos;
         DevBuf<int32_t> wellOf, cellOf, arrival, bucketTmp, bucket, binCounts, offsets, tileSums;
 
@@ -288,6 +291,8 @@ namespace halcuda
             HAL_TRY(apos.Alloc(2 * m, "cudaMalloc(well agents)"));
             HAL_TRY(arad.Alloc(m, "cudaMalloc(well agents)"));
             HAL_TRY(avel.Alloc(2 * m, "cudaMalloc(well agents)"));
+            HAL_TRY(avelState.Alloc(m, "cudaMalloc(well agents)"));
+            HAL_TRY(CudaStatus(cudaMemset(avelState.p, 0, m * sizeof(float2)), "cudaMemset"));
             HAL_TRY(sRad.Alloc(m, "cudaMalloc(well agents)"));
             HAL_TRY(posF.Alloc(m, "cudaMalloc(well agents)"));
             HAL_TRY(sPos.Alloc(m, "cudaMalloc(well agents)"));
@@ -453,6 +458,10 @@ namespace halcuda
             a.k = static_cast<float>(k);
             a.vel = avel.p;
             a.forceThreads = forceThreads;
+            a.velState = motion ? avelState.p : nullptr;
+            a.posOut = reinterpret_cast<float2 *>(apos.p);
+            a.friction = friction;
+            a.maxVel = maxVel;
             return a;
         }
 
@@ -575,7 +584,8 @@ namespace halcuda
             for (int32_t t : {128, 64, 256})
             {
                 forceThreads = t;
-                const AgentWellsArgs a = AgentArgs(R, k);
+                AgentWellsArgs a = AgentArgs(R, k);
+                a.velState = nullptr;  // timing runs compute forces only: the agents stay put
                 for (int it = 0; it < 5 && rc == HAL_CUDA_OK; it++)
                 {
                     if (it == 2)
@@ -623,7 +633,8 @@ namespace halcuda
             }
             cudaStream_t s = stream.Get();
             char key[160];
-            snprintf(key, sizeof(key), "%a|%a|%d|%p", R, k, nAgents, static_cast<void *>(s));
+            snprintf(key, sizeof(key), "%a|%a|%d|%d|%a|%a|%d|%p", R, k, nAgents, motion ? 1 : 0,
+                     static_cast<double>(friction), static_cast<double>(maxVel), forceThreads, static_cast<void *>(s));
             for (int32_t t = 0; t < ticks; t++)
             {
                 GraphCache &g = graph[cur];
@@ -859,11 +870,66 @@ extern "C" int hal_cuda_wells_set_agents(hal_cuda_wells *h, const int32_t *count
                                            cudaMemcpyHostToDevice, s), "cudaMemcpy(radii)"));
         HAL_TRY(CudaStatus(cudaMemcpyAsync(h->wellOf.p, wellOf.data(), static_cast<size_t>(n) * sizeof(int32_t),
                                            cudaMemcpyHostToDevice, s), "cudaMemcpy(wellOf)"));
+        HAL_TRY(CudaStatus(cudaMemsetAsync(h->avelState.p, 0, static_cast<size_t>(n) * sizeof(float2), s),
+                           "cudaMemsetAsync(velocities)"));
     }
     h->counts.assign(counts, counts + h->desc.size());
     h->agentsTunedFor = std::make_pair(-1.0, 0.0);  // new agents: re-tune the force block size
     h->nAgents = static_cast<int32_t>(n);
     return CudaStatus(cudaStreamSynchronize(s), "hal_cuda_wells_set_agents");
+}
+
+extern "C" int hal_cuda_wells_set_motion(hal_cuda_wells *h, int32_t enabled, double friction, double maxVel)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_wells_set_motion: handle is NULL");
+    HAL_REQUIRE(std::isfinite(friction), "hal_cuda_wells_set_motion: friction must be finite");
+    HAL_REQUIRE(!std::isnan(maxVel), "hal_cuda_wells_set_motion: maxVel is NaN");
+    h->motion = enabled != 0;
+    h->friction = static_cast<float>(friction);
+    h->maxVel = (maxVel < 0 || std::isinf(maxVel)) ? -1.0f : static_cast<float>(maxVel);
+    h->ResetGraphs();
+    return HAL_CUDA_OK;
+}
+
+extern "C" int hal_cuda_wells_set_velocities(hal_cuda_wells *h, const float *velocities, int64_t len)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_wells_set_velocities: handle is NULL");
+    HAL_REQUIRE(len == 2 * static_cast<int64_t>(h->nAgents), "hal_cuda_wells_set_velocities: %lld values for %d agents",
+                static_cast<long long>(len), h->nAgents);
+    using namespace halcuda;
+    HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    cudaStream_t s = h->stream.Get();
+    if (h->nAgents > 0)
+    {
+        const size_t bytes = static_cast<size_t>(h->nAgents) * sizeof(float2);
+        HAL_TRY(CudaStatus(velocities != nullptr
+                               ? cudaMemcpyAsync(h->avelState.p, velocities, bytes, cudaMemcpyHostToDevice, s)
+                               : cudaMemsetAsync(h->avelState.p, 0, bytes, s),
+                           "hal_cuda_wells_set_velocities"));
+    }
+    return CudaStatus(cudaStreamSynchronize(s), "hal_cuda_wells_set_velocities");
+}
+
+extern "C" int hal_cuda_wells_get_agents(hal_cuda_wells *h, float *positions, float *velocities, int64_t len)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_wells_get_agents: handle is NULL");
+    HAL_REQUIRE(len == 2 * static_cast<int64_t>(h->nAgents), "hal_cuda_wells_get_agents: %lld values for %d agents",
+                static_cast<long long>(len), h->nAgents);
+    using namespace halcuda;
+    HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    cudaStream_t s = h->stream.Get();
+    const size_t bytes = static_cast<size_t>(len) * sizeof(float);
+    if (len > 0 && positions != nullptr)
+    {
+        HAL_TRY(CudaStatus(cudaMemcpyAsync(positions, h->apos.p, bytes, cudaMemcpyDeviceToHost, s),
+                           "cudaMemcpy(positions)"));
+    }
+    if (len > 0 && velocities != nullptr)
+    {
+        HAL_TRY(CudaStatus(cudaMemcpyAsync(velocities, h->avelState.p, bytes, cudaMemcpyDeviceToHost, s),
+                           "cudaMemcpy(velocities)"));
+    }
+    return CudaStatus(cudaStreamSynchronize(s), "hal_cuda_wells_get_agents");
 }
 
 extern "C" int hal_cuda_wells_run_ticks(hal_cuda_wells *h, int32_t ticks, double interactionRad,

@@ -104,6 +104,9 @@ SIGNATURES = {
     "hal_cuda_wells_run_ticks": (_I, [_vp, _i32, _f64, _f64]),
     "hal_cuda_wells_get_forces": (_I, [_vp, _vp, _i64]),
     "hal_cuda_wells_profile": (_I, [_vp, _i32, _f64, _f64, _vp]),
+    "hal_cuda_wells_set_motion": (_I, [_vp, _i32, _f64, _f64]),
+    "hal_cuda_wells_set_velocities": (_I, [_vp, _vp, _i64]),
+    "hal_cuda_wells_get_agents": (_I, [_vp, _vp, _vp, _i64]),
     "hal_cuda_wells_autotune": (_I, [_vp, _vp, _vp, _vp]),
     "hal_cuda_wells_sync": (_I, [_vp]),
     "hal_cuda_wells_stream": (_vp, [_vp]),
@@ -650,6 +653,23 @@ class Wells(_Handle):
     def run_ticks(self, ticks, interactionRad=1.0, springConstant=0.1):
         _check(lib().hal_cuda_wells_run_ticks(self._h, ticks, interactionRad, springConstant),
                "wells_run_ticks")
+
+    def set_motion(self, enabled=True, friction=1.0, maxVel=-1.0):
+        """Agents move after their forces each tick (SphericalAgent2D update)."""
+        _check(lib().hal_cuda_wells_set_motion(self._h, int(enabled), float(friction), float(maxVel)), "set_motion")
+
+    def set_velocities(self, velocities=None):
+        n = 2 * int(self.counts.sum())
+        v = None if velocities is None else _f32(velocities)
+        _check(lib().hal_cuda_wells_set_velocities(self._h, _p(v), n if v is None else v.size), "set_velocities")
+
+    def get_agents(self):
+        """(positions, velocities) of every well's agents, well after well."""
+        n = 2 * int(self.counts.sum())
+        p = np.empty(n, dtype=np.float32)
+        v = np.empty(n, dtype=np.float32)
+        _check(lib().hal_cuda_wells_get_agents(self._h, _p(p), _p(v), n), "get_agents")
+        return p, v
 
     def autotune(self):
         """Re-runs the sweep-tile autotuner; returns (rCap, ms tuned, ms default)."""

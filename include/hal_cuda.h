@@ -431,6 +431,17 @@ int hal_cuda_wells_set_agents(hal_cuda_wells *h, const int32_t *counts, const fl
 int hal_cuda_wells_run_ticks(hal_cuda_wells *h, int32_t ticks, double interactionRad,
                              double springConstant);
 
+/* Motion of the wells' agents: when enabled, each tick's force pass also
+ * applies SphericalAgent2D's update to every agent, in its own well, as
+ * hal_cuda_agents_step does (vel += delta; CapVelocity(maxVel) when maxVel >=
+ * 0; ForceMove with the well's wrap flags; ApplyFriction(friction)), so the
+ * agents move on the device tick after tick.  set_agents sets the velocities
+ * to zero; set_velocities (NULL: zero) and get_agents take 2*sum(counts)
+ * values, well after well. */
+int hal_cuda_wells_set_motion(hal_cuda_wells *h, int32_t enabled, double friction, double maxVel);
+int hal_cuda_wells_set_velocities(hal_cuda_wells *h, const float *velocities, int64_t len);
+int hal_cuda_wells_get_agents(hal_cuda_wells *h, float *positions, float *velocities, int64_t len);
+
 /* Velocity deltas of the last force pass, every well's agents concatenated
  * in well order (len = 2*sum(counts) floats). */
 int hal_cuda_wells_get_forces(hal_cuda_wells *h, float *velocityDeltas, int64_t len);

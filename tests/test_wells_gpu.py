@@ -125,6 +125,41 @@ def test_autotune_keeps_state_and_results(hal):
         assert np.array_equal(got[i], _alone(hal, w, fields[i], srcs[i], 5)), (i, w)
 
 
+def test_wells_motion_equals_single_grid_steps(hal, oracle):
+    """With motion on, every well's agents move tick after tick exactly as
+    that well's agents do under the single-grid resident step."""
+    rng = np.random.default_rng(42)
+    wells, fields, srcs, counts, pos, rad = _mixed_wells(rng)
+    vel = [((rng.random(2 * len(r)) - 0.5) * 0.4).astype(np.float32) for r in rad]
+    ticks, fr, mv = 6, 0.7, 0.3
+    with hal.Wells(wells) as b:
+        for i, f in enumerate(fields):
+            b.set_field(i, f)
+        b.set_agents(counts, np.concatenate(pos), np.concatenate(rad))
+        p0, v0 = b.get_agents()
+        assert np.array_equal(p0, np.concatenate(pos)) and not v0.any()
+        b.set_velocities(np.concatenate(vel))
+        b.set_motion(True, fr, mv)
+        b.run_ticks(ticks, R, K)
+        got_p, got_v = b.get_agents()
+        b.set_motion(False)
+        b.run_ticks(1, R, K)  # forces only: the agents stay where they are
+        assert np.array_equal(b.get_agents()[0], got_p)
+    at = 0
+    for i, w in enumerate(wells):
+        n = int(counts[i])
+        if n == 0:
+            continue
+        with hal.Agents(w["xDim"], w["yDim"], n) as ag:
+            ag.upload(pos[i], rad[i])
+            ag.set_velocities(vel[i])
+            ag.step(ticks, R, K, w["wrapX"], w["wrapY"], friction=fr, maxVel=mv)
+            ep, ev = ag.get_state()
+        assert np.array_equal(got_p[2 * at: 2 * (at + n)], ep), (i, w)
+        assert np.array_equal(got_v[2 * at: 2 * (at + n)], ev), (i, w)
+        at += n
+
+
 def test_wells_profile_and_source_clear(hal):
     rng = np.random.default_rng(41)
     wells, fields, srcs, counts, pos, rad = _mixed_wells(rng)
