@@ -1074,16 +1074,8 @@ namespace halcuda
         template <int MODE, bool SWZ>
         int EnableSweepSmem(size_t bytes)
         {
-            static size_t s_enabled = 0;
-            if (bytes > s_enabled)
-            {
-                HAL_TRY(CudaStatus(cudaFuncSetAttribute(AdiSweep<MODE, SWZ>,
-                                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                        static_cast<int>(bytes)),
-                                   "cudaFuncSetAttribute(AdiSweep)"));
-                s_enabled = bytes;
-            }
-            return HAL_CUDA_OK;
+            static SmemLimit s_limit;
+            return s_limit.Ensure(AdiSweep<MODE, SWZ>, bytes, "cudaFuncSetAttribute(AdiSweep)");
         }
 
         template <int MODE>
@@ -1096,20 +1088,18 @@ namespace halcuda
         // cuTensorMapEncodeTiled through the runtime's driver entry point.
         PFN_cuTensorMapEncodeTiled_v12000 TensorMapEncoder()
         {
-            static PFN_cuTensorMapEncodeTiled_v12000 s_fn = nullptr;
-            static bool s_tried = false;
-            if (!s_tried)
-            {
-                s_tried = true;
+            // looked up once (thread-safe static initialisation)
+            static const PFN_cuTensorMapEncodeTiled_v12000 s_fn = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
                 void *fn = nullptr;
                 cudaDriverEntryPointQueryResult q;
                 if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
                         cudaSuccess &&
                     q == cudaDriverEntryPointSuccess)
                 {
-                    s_fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+                    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
                 }
-            }
+                return nullptr;
+            }();
             return s_fn;
         }
 
@@ -1163,15 +1153,8 @@ namespace halcuda
         template <int MODE>
         int PrepareTiles(size_t smem)
         {
-            static size_t s_enabled = 0;
-            if (smem > s_enabled)
-            {
-                HAL_TRY(CudaStatus(cudaFuncSetAttribute(AdiSweepTiles<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                        static_cast<int>(smem)),
-                                   "cudaFuncSetAttribute(AdiSweepTiles)"));
-                s_enabled = smem;
-            }
-            return HAL_CUDA_OK;
+            static SmemLimit s_limit;
+            return s_limit.Ensure(AdiSweepTiles<MODE>, smem, "cudaFuncSetAttribute(AdiSweepTiles)");
         }
 
         template <int MODE>

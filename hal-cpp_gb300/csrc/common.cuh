@@ -7,7 +7,9 @@
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
+#include <mutex>
 #include <string>
+#include <vector>
 
 #include "hal_cuda.h"
 
@@ -190,6 +192,42 @@ namespace halcuda
         const float *xhi;  // bc(xDim, y)
         const float *ylo;  // bc(x, -1), xDim values
         const float *yhi;  // bc(x, yDim)
+    };
+
+    // Raises a kernel's dynamic shared-memory limit on the calling thread's
+    // current device, once per device and size (the attribute is per device).
+    class SmemLimit
+    {
+    public:
+        template <typename Kernel>
+        int Ensure(Kernel kernel, size_t bytes, const char *what)
+        {
+            int dev = 0;
+            cudaError_t e = cudaGetDevice(&dev);
+            if (e != cudaSuccess)
+            {
+                return CudaStatus(e, what);
+            }
+            std::lock_guard<std::mutex> lock(m_mu);
+            if (static_cast<size_t>(dev) >= m_enabled.size())
+            {
+                m_enabled.resize(static_cast<size_t>(dev) + 1, 0);
+            }
+            if (bytes > m_enabled[static_cast<size_t>(dev)])
+            {
+                e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+                if (e != cudaSuccess)
+                {
+                    return CudaStatus(e, what);
+                }
+                m_enabled[static_cast<size_t>(dev)] = bytes;
+            }
+            return HAL_CUDA_OK;
+        }
+
+    private:
+        std::mutex m_mu;
+        std::vector<size_t> m_enabled;  // by device
     };
 
     inline GhostView MakeGhostView(const float *g, int32_t xDim, int32_t yDim)

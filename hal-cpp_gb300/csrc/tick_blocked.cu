@@ -275,20 +275,18 @@ namespace halcuda
 
         PFN_cuTensorMapEncodeTiled_v12000 Encoder()
         {
-            static PFN_cuTensorMapEncodeTiled_v12000 s_fn = nullptr;
-            static bool s_tried = false;
-            if (!s_tried)
-            {
-                s_tried = true;
+            // looked up once (thread-safe static initialisation)
+            static const PFN_cuTensorMapEncodeTiled_v12000 s_fn = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
                 void *fn = nullptr;
                 cudaDriverEntryPointQueryResult q;
                 if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
                         cudaSuccess &&
                     q == cudaDriverEntryPointSuccess)
                 {
-                    s_fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+                    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
                 }
-            }
+                return nullptr;
+            }();
             return s_fn;
         }
 
@@ -316,15 +314,8 @@ namespace halcuda
 
     int PrepareTickBlocked()
     {
-        static bool s_done = false;
-        if (!s_done)
-        {
-            HAL_TRY(CudaStatus(cudaFuncSetAttribute(TickBlocked2, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                    static_cast<int>(kSmemBytes)),
-                               "cudaFuncSetAttribute(TickBlocked2)"));
-            s_done = true;
-        }
-        return HAL_CUDA_OK;
+        static SmemLimit s_limit;
+        return s_limit.Ensure(TickBlocked2, kSmemBytes, "cudaFuncSetAttribute(TickBlocked2)");
     }
 
     void LaunchTickBlocked2(const TickBlockParams &p, const TickBlockTensorMap &map, cudaStream_t s)
