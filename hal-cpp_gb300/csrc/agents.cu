@@ -364,6 +364,81 @@ namespace halcuda
             const T xDimF = static_cast<T>(xDim);
             const T yDimF = static_cast<T>(yDim);
             T vx = T(0), vy = T(0);
+            // one candidate slot q of the window, in the CPU's visiting order
+            auto visit = [&](int32_t q) {
+                if (q == slot)
+                {
+                    return;
+                }
+                const V2<T> pj = sPos[q];
+                const T xComp = Disp(px, pj.x, xDimF, wrapX != 0);
+                const T yComp = Disp(py, pj.y, yDimF, wrapY != 0);
+                if constexpr (std::is_same<T, double>::value)
+                {
+                    // IEEE operations in the CPU's order: bit-exact
+                    const T dist = Sqrt(Add(Mul(xComp, xComp), Mul(yComp, yComp)));
+                    if ((dist < R) && (dist > T(0)))
+                    {
+                        const T touchDist = Sub(Add(rad, sRad[q]), dist);
+                        const T force = Mul(k, touchDist);
+                        vx = Sub(vx, Mul(Div(xComp, dist), force));
+                        vy = Sub(vy, Mul(Div(yComp, dist), force));
+                    }
+                }
+                else
+                {
+                    // FP32 path: 1/d from rsqrt (d^2 = 0 gives NaN,
+                    // which fails both tests like the CPU's d > 0)
+                    const T d2 = fmaf(xComp, xComp, yComp * yComp);
+                    const T inv = rsqrtf(d2);
+                    const T dist = d2 * inv;
+                    if ((dist < R) && (dist > T(0)))
+                    {
+                        const T scale = inv * (k * ((rad + sRad[q]) - dist));
+                        vx -= xComp * scale;
+                        vy -= yComp * scale;
+                    }
+                }
+            };
+            // Common case: a window of at most four rows whose y-range does
+            // not wrap, so each row is one run of cells.  All rows' offset
+            // pairs are loaded before the first candidate, which shortens the
+            // chain of dependent loads; the visiting order is unchanged.
+            const int32_t nRows = xEnd - xStart;
+            if (nRows > 0 && nRows <= 4 && yStart >= 0 && yEnd <= yDim && yEnd > yStart)
+            {
+                int32_t rs[4], re[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                {
+                    rs[j] = 0;
+                    re[j] = 0;
+                    if (j < nRows)
+                    {
+                        int32_t retX = xStart + j;
+                        if (retX < 0 || retX >= xDim)
+                        {
+                            retX %= xDim;  // only reached on a wrapped axis (clamped otherwise)
+                            retX = (retX < 0) ? retX + xDim : retX;
+                        }
+                        const int32_t cell = retX * yDim + yStart;
+                        rs[j] = __ldg(offsets + cell);
+                        re[j] = __ldg(offsets + cell + (yEnd - yStart));
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                {
+                    for (int32_t q = rs[j]; q < re[j]; q++)
+                    {
+                        visit(q);
+                    }
+                }
+                V2<T> sum;
+                sum.x = vx;
+                sum.y = vy;
+                return sum;
+            }
             for (int32_t xSq = xStart; xSq < xEnd; xSq++)
             {
                 int32_t retX = xSq;
@@ -397,39 +472,7 @@ namespace halcuda
                     const int32_t e = __ldg(offsets + cell + run);
                     for (int32_t q = s; q < e; q++)
                     {
-                        if (q == slot)
-                        {
-                            continue;
-                        }
-                        const V2<T> pj = sPos[q];
-                        const T xComp = Disp(px, pj.x, xDimF, wrapX != 0);
-                        const T yComp = Disp(py, pj.y, yDimF, wrapY != 0);
-                        if constexpr (std::is_same<T, double>::value)
-                        {
-                            // IEEE operations in the CPU's order: bit-exact
-                            const T dist = Sqrt(Add(Mul(xComp, xComp), Mul(yComp, yComp)));
-                            if ((dist < R) && (dist > T(0)))
-                            {
-                                const T touchDist = Sub(Add(rad, sRad[q]), dist);
-                                const T force = Mul(k, touchDist);
-                                vx = Sub(vx, Mul(Div(xComp, dist), force));
-                                vy = Sub(vy, Mul(Div(yComp, dist), force));
-                            }
-                        }
-                        else
-                        {
-                            // FP32 path: 1/d from rsqrt (d^2 = 0 gives NaN,
-                            // which fails both tests like the CPU's d > 0)
-                            const T d2 = fmaf(xComp, xComp, yComp * yComp);
-                            const T inv = rsqrtf(d2);
-                            const T dist = d2 * inv;
-                            if ((dist < R) && (dist > T(0)))
-                            {
-                                const T scale = inv * (k * ((rad + sRad[q]) - dist));
-                                vx -= xComp * scale;
-                                vy -= yComp * scale;
-                            }
-                        }
+                        visit(q);
                     }
                 }
             }
