@@ -5,6 +5,8 @@
     python -m halcuda.profcase agents 2048 2     # 2 dispatches of 1M agents
     python -m halcuda.profcase stencil64 2048 1  # FP64 per-cell rate diffusion,
                                                  # advection, per-cell advection
+    python -m halcuda.profcase wells 0 2         # 2 batched ticks of the 512 wells
+    python -m halcuda.profcase adjoint 256 50    # one gradient: 50 steps, checkpoints every 10
 
 Each case builds the benchmark's inputs at the given grid side, runs one
 untimed warm-up launch sequence, then the requested number of individually
@@ -61,6 +63,27 @@ def main(argv):
                 h.advect(f, d.copy(), 0.2, -0.1, 0, 0)
                 h.advect_var(f, d.copy(), vx, vy, 0, 0)
         print(f"stencil64 {n}^2: {iters} x (diffuse_var, advect, advect_var)")
+    elif case == "wells":
+        w = workloads.wells_inputs()
+        with hal.Wells(w["wells"]) as b:
+            for i, f in enumerate(w["fields"]):
+                b.set_field(i, f)
+            b.set_agents(w["counts"], w["positions"], w["radii"])
+            b.run_ticks(1, w["interactionRad"], w["springConstant"])  # autotune + graph capture
+            b.sync()
+            ms = b.profile(iters, w["interactionRad"], w["springConstant"])
+        print("wells: " + ", ".join(f"{v:.3f}" for v in ms) + " ms (explicit, adi x, adi y, agents, tick)")
+    elif case == "adjoint":
+        rng = np.random.default_rng(4)
+        f0 = workloads.gaussian_blobs(n, rng, 8).astype(np.float32)
+        D = workloads.rate_field(n, rng).astype(np.float32)
+        src = (rng.random(n * n) * 0.01).astype(np.float32)
+        with hal.Adjoint(n, n) as a:
+            a.set_problem(f0, np.roll(f0, 3), iters, 10)
+            a.forward(D, 0.005, src)
+            a.gradient(D, 0.005, src)
+            t = a.times()
+        print(f"adjoint {n}^2, {iters} steps: forward {t[0]:.2f} ms, gradient {t[1]:.2f} ms")
     else:
         raise SystemExit(f"unknown case {case}")
     return 0
