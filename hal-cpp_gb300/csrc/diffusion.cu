@@ -400,8 +400,10 @@ namespace halcuda
             }
         }
 
+        // Four CTAs per SM (64 registers) measured fastest for the plain tick
+        // (6.68 vs 6.78 us at 2048^2); the advective tick is fastest unbounded.
         template <int VEC, bool ADV>
-        __global__ void __launch_bounds__(32 * kTickWarps)
+        __global__ void __launch_bounds__(32 * kTickWarps, ADV ? 1 : 4)
             TickKernel(TickParams p)
         {
             TickTile<VEC, ADV>(p, static_cast<int32_t>(blockIdx.x), static_cast<int32_t>(blockIdx.y));
