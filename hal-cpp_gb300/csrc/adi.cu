@@ -41,6 +41,7 @@
 #include <map>
 #include <memory>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 namespace halcuda
@@ -49,6 +50,11 @@ namespace halcuda
     {
         constexpr int M = kAdiM;
         constexpr int kCoefFloats = 3 * kCoefCount * M;
+        // in shared memory each block type's coefficients start 16 bytes
+        // further along the banks than the last type's, so that a warp whose
+        // chunks span two types reads both in one wavefront
+        constexpr int kCoefTypeStride = kCoefCount * M + 4;
+        constexpr int kCoefSmemFloats = 3 * kCoefTypeStride;
         constexpr int kChunkStride = M + 4;  // floats per 32-element chunk in shared memory
         constexpr int kNL = 2;               // lines solved by one thread
         constexpr int kMaxThreads = 512;
@@ -226,6 +232,37 @@ namespace halcuda
             }
         }
 
+        // BandDot2 for a band half-width B known at compile time: the same
+        // products in the same (ascending m) order, unrolled.
+        template <int B>
+        __device__ __forceinline__ void BandDot2Fixed(const float *G, int32_t P, int k, const float *xA,
+                                                      const float *xB, float &sL, float &sR)
+        {
+            constexpr int W = 2 * B + 1;
+            const int S = P - 1;
+            sL = 0.0f;
+            sR = 0.0f;
+            const bool hasR = k < S, hasL = k >= 1;
+#pragma unroll
+            for (int t = 0; t <= 2 * B + 1; t++)
+            {
+                const int m = k - 1 - B + t;
+                if (m < 0 || m > S - 1)
+                {
+                    continue;
+                }
+                const float sm = xA[m] + xB[m];
+                if (hasR && t >= 1)
+                {
+                    sR = fmaf(G[k * W + (t - 1)], sm, sR);
+                }
+                if (hasL && t <= 2 * B)
+                {
+                    sL = fmaf(G[(k - 1) * W + t], sm, sL);
+                }
+            }
+        }
+
         // z[idx] for a run-time idx without dynamic register indexing.
         __device__ __forceinline__ float SelectReg(const float (&z)[M], int idx)
         {
@@ -286,6 +323,42 @@ namespace halcuda
             }
         }
 
+        // Solution rows (SWZ).  The solve writes each chunk of a line back
+        // over its staged row with the 16-byte units permuted once more by
+        // SolSwz(line quad): the write-out reads the same unit of 4 (or 8)
+        // quads in one quarter-warp, and the extra permutation puts them in
+        // different bank groups.  The permutation is within a row, which the
+        // one thread that solved it writes whole.
+        __device__ __forceinline__ int SolSwz(int ll)
+        {
+            const int qd = ll >> 2;
+            return ((qd << 1) & 6) | ((qd >> 2) & 1);
+        }
+
+        // Float offset of unit q of chunk k of solution line ll (staged row
+        // ll + 1).
+        template <bool SWZ>
+        __device__ __forceinline__ int SolOff4(int ll, int k, int q, int P, int LS)
+        {
+            if constexpr (SWZ)
+            {
+                return ((ll + 1) * P + k) * M + ((q ^ (k & 7) ^ SolSwz(ll)) << 2);
+            }
+            else
+            {
+                return SOff4<SWZ>(ll + 1, k, q, P, LS);
+            }
+        }
+
+        // Element pos of solution line ll.
+        template <bool SWZ>
+        __device__ __forceinline__ int SolPos(int ll, int32_t pos, int P, int LS)
+        {
+            const int k = pos >> 5;
+            const int i = pos & 31;
+            return SolOff4<SWZ>(ll, k, i >> 2, P, LS) + (i & 3);
+        }
+
         // An opaque copy of v: keeps the compiler from holding values derived
         // from v in registers across a long stretch of code.
         __device__ __forceinline__ int Opaque(int v)
@@ -340,8 +413,8 @@ namespace halcuda
             // swizzle pattern repeats every 1024 bytes) and used directly, so
             // every access through it is a shared-memory access
             float *sLines = smem;
-            float *sCoef = sLines + (R + 2) * p.LS;  // kCoefFloats
-            float *xA = sCoef + kCoefFloats;         // R * P
+            float *sCoef = sLines + (R + 2) * p.LS;  // kCoefSmemFloats
+            float *xA = sCoef + kCoefSmemFloats;     // R * P
             float *xB = xA + R * P;                  // R * P
             float *sG = xB + R * P;                  // kGbandSmem: G's band when it fits
             const int gCount = (P > 1) ? (P - 1) * (2 * p.plan.B + 1) : 0;
@@ -387,7 +460,9 @@ namespace halcuda
                 }
                 for (int q = tid; q < kCoefFloats / 4; q += nthreads)
                 {
-                    St4(sCoef + 4 * q, __ldg(reinterpret_cast<const float4 *>(p.plan.coef) + q));
+                    const int t = q / (kCoefCount * M / 4);
+                    St4(sCoef + t * kCoefTypeStride + 4 * (q - t * (kCoefCount * M / 4)),
+                        __ldg(reinterpret_cast<const float4 *>(p.plan.coef) + q));
                 }
                 if (gInSmem)
                 {
@@ -433,7 +508,9 @@ namespace halcuda
                 }
                 for (int q = tid; q < kCoefFloats / 4; q += nthreads)
                 {
-                    St4(sCoef + 4 * q, __ldg(reinterpret_cast<const float4 *>(p.plan.coef) + q));
+                    const int t = q / (kCoefCount * M / 4);
+                    St4(sCoef + t * kCoefTypeStride + 4 * (q - t * (kCoefCount * M / 4)),
+                        __ldg(reinterpret_cast<const float4 *>(p.plan.coef) + q));
                 }
                 if (gInSmem)
                 {
@@ -553,7 +630,7 @@ namespace halcuda
             const int g = tid / P;
             const int k = tid - g * P;
             const int type = AdiBlockType(k, P);
-            const float *cf = sCoef + type * kCoefCount * M;
+            const float *cf = sCoef + type * kCoefTypeStride;
             const float a = p.plan.a;
             const int ll0 = g * kNL;  // first line of the thread within the CTA
             float z[kNL][M];
@@ -570,6 +647,37 @@ namespace halcuda
                     wDn[j] = (line + 1 < p.Nlines || p.wrapLines) ? 1.0f : (hasGhost ? 2.0f : 0.0f);
                 }
             }
+            bool unit = true;  // both lines inside the grid with unit neighbour weights
+#pragma unroll
+            for (int j = 0; j < kNL; j++)
+            {
+                unit = unit && act[j] && wUp[j] == 1.0f && wDn[j] == 1.0f;
+            }
+            if (unit)
+            {
+                // the general form below with every weight 1 and every line
+                // active: the same roundings (x * 1 is exact)
+#pragma unroll
+                for (int q = 0; q < M / 4; q++)
+                {
+                    float4 rows[kNL + 2];
+#pragma unroll
+                    for (int r = 0; r < kNL + 2; r++)
+                    {
+                        rows[r] = Ld4(sLines + SOff4<SWZ>(ll0 + r, k, q, P, p.LS));
+                    }
+#pragma unroll
+                    for (int j = 0; j < kNL; j++)
+                    {
+                        const float4 up = rows[j], c = rows[j + 1], dn = rows[j + 2];
+                        z[j][4 * q + 0] = fmaf((dn.x - c.x) + (up.x - c.x), p.halfR, c.x);
+                        z[j][4 * q + 1] = fmaf((dn.y - c.y) + (up.y - c.y), p.halfR, c.y);
+                        z[j][4 * q + 2] = fmaf((dn.z - c.z) + (up.z - c.z), p.halfR, c.z);
+                        z[j][4 * q + 3] = fmaf((dn.w - c.w) + (up.w - c.w), p.halfR, c.w);
+                    }
+                }
+            }
+            else
 #pragma unroll
             for (int q = 0; q < M / 4; q++)
             {
@@ -650,7 +758,18 @@ namespace halcuda
                 sRs[j] = 0.0f;
                 if (act[j] && P > 1)
                 {
-                    BandDot2(G, P, p.plan.B, k, xA + ll * P, xB + ll * P, sLs[j], sRs[j]);
+                    switch (p.plan.B)
+                    {
+                    case 1:
+                        BandDot2Fixed<1>(G, P, k, xA + ll * P, xB + ll * P, sLs[j], sRs[j]);
+                        break;
+                    case 2:
+                        BandDot2Fixed<2>(G, P, k, xA + ll * P, xB + ll * P, sLs[j], sRs[j]);
+                        break;
+                    default:
+                        BandDot2(G, P, p.plan.B, k, xA + ll * P, xB + ll * P, sLs[j], sRs[j]);
+                        break;
+                    }
                 }
             }
             BlockCorrectN(z, cf, sLs, sRs);
@@ -667,8 +786,9 @@ namespace halcuda
                     z[j][M - 1] = sRs[j];
                 }
                 // every staged-line read finished before the barrier above,
-                // so the line's buffer can take the solution
-                const int swo = Opaque(k & 7);
+                // so the line's buffer can take the solution (SolOff4's unit
+                // order)
+                const int swo = Opaque((k & 7) ^ SolSwz(ll));
                 const int rowo = Opaque((ll + 1) * P + k);
 #pragma unroll
                 for (int q = 0; q < M / 4; q++)
@@ -688,8 +808,8 @@ namespace halcuda
                 float *sFactor = xA;  // the exchange rows are free now
                 for (int ll = tid; ll < R; ll += nthreads)
                 {
-                    const float y0 = sLines[SPos<SWZ>(ll + 1, 0, P, p.LS)];
-                    const float yl = sLines[SPos<SWZ>(ll + 1, L - 1, P, p.LS)];
+                    const float y0 = sLines[SolPos<SWZ>(ll, 0, P, p.LS)];
+                    const float yl = sLines[SolPos<SWZ>(ll, L - 1, P, p.LS)];
                     sFactor[ll] = fmaf(yl, p.plan.bog, y0) * p.plan.invDenom;
                 }
                 __syncthreads();
@@ -712,7 +832,7 @@ namespace halcuda
                             break;
                         }
                         const float fct = sFactor[ll];
-                        float *at = sLines + SOff4<SWZ>(ll + 1, kk, q, P, p.LS);
+                        float *at = sLines + SolOff4<SWZ>(ll, kk, q, P, p.LS);
                         float4 v = Ld4(at);
                         v.x = fmaf(-fct, zs[0], v.x);
                         v.y = fmaf(-fct, zs[1], v.y);
@@ -737,7 +857,7 @@ namespace halcuda
                     const int64_t base = static_cast<int64_t>(line) * L;
                     for (int32_t pos = tid; pos < L; pos += nthreads)
                     {
-                        const double v = static_cast<double>(sLines[SPos<SWZ>(ll + 1, pos, P, p.LS)]);
+                        const double v = static_cast<double>(sLines[SolPos<SWZ>(ll, pos, P, p.LS)]);
                         p.deltas[base + pos] = p.deltas[base + pos] + (v - p.f64[base + pos]);
                     }
                 }
@@ -746,7 +866,10 @@ namespace halcuda
             {
                 // thread -> group qd of 4 lines; out[pos * Nlines + line]
                 const int Q = R >> 2;                   // a power of two <= 32
+                // thread -> (quad qd, first unit uStart): the lanes of a
+                // quarter-warp cover whole 64-byte segments of the output
                 const int qd = tid & (Q - 1);
+                const int uStart = tid / Q;
                 const int32_t line0 = x0 + 4 * qd;
                 const int step = nthreads / Q;
                 const bool vecOut = (p.Nlines & 3) == 0;
@@ -754,97 +877,121 @@ namespace halcuda
                 if (vecOut && vecL)
                 {
                     // 16-byte units: 4 positions x 4 lines move as a 4x4 block
-                    // (4 LDS.128, a register transpose, 4 STG.128)
-                    const int32_t nU = L >> 2;
-                    constexpr int kUB = 2;
-                    for (int32_t u0 = tid / Q; u0 < nU && quadOk; u0 += kUB * step)
-                    {
-                        float4 o[kUB][4];
-                        float4 fv[kUB][4], sv[kUB][4];
-#pragma unroll
-                        for (int b = 0; b < kUB; b++)
+                    // (4 LDS.128, a register transpose, 4 STG.128).  UPT: the
+                    // commit has an uptake term (agents coupled); without it
+                    // the commit skips the count loads and that product.
+                    auto writeVec = [&](auto uptTag) {
+                        constexpr bool UPT = decltype(uptTag)::value;
+                        (void)UPT;
+                        const int32_t nU = L >> 2;
+                        constexpr int kUB = 2;
+                        const bool hasSrc = (p.src != nullptr);
+                        (void)hasSrc;  // read by the commit of MODE kSweepTick only
+                        // unit u of solution line 4qd+e sits at
+                        // SolOff4(4qd, u >> 3, u & 7) + e * lineStride: the
+                        // four lines of a quad share one SolSwz
+                        const int lineStride = SOff4<SWZ>(1, 0, 0, P, p.LS);
+                        const int64_t nl = p.Nlines;
+                        for (int32_t u0 = uStart; u0 < nU && quadOk; u0 += kUB * step)
                         {
-                            const int32_t u = u0 + b * step;
-                            const bool ok = u < nU;
-                            const int kk = u >> 3;
-                            const int q = u & 7;
-                            float4 a[4];
+                            float4 o[kUB][4];
+                            float4 fv[kUB][4], sv[kUB][4];
 #pragma unroll
-                            for (int e = 0; e < 4; e++)
+                            for (int b = 0; b < kUB; b++)
                             {
-                                a[e] = ok ? Ld4(sLines + SOff4<SWZ>(4 * qd + 1 + e, kk, q, P, p.LS))
-                                          : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                            }
-                            o[b][0] = make_float4(a[0].x, a[1].x, a[2].x, a[3].x);
-                            o[b][1] = make_float4(a[0].y, a[1].y, a[2].y, a[3].y);
-                            o[b][2] = make_float4(a[0].z, a[1].z, a[2].z, a[3].z);
-                            o[b][3] = make_float4(a[0].w, a[1].w, a[2].w, a[3].w);
+                                const int32_t u = u0 + b * step;
+                                const bool ok = u < nU;
+                                const float *su = sLines + SolOff4<SWZ>(4 * qd, u >> 3, u & 7, P, p.LS);
+                                float4 a[4];
 #pragma unroll
-                            for (int i = 0; i < 4; i++)
-                            {
-                                fv[b][i] = sv[b][i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                            }
-                            if constexpr (MODE == kSweepTick)
-                            {
-                                if (ok)
+                                for (int e = 0; e < 4; e++)
                                 {
+                                    a[e] = ok ? Ld4(su + e * lineStride) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                                }
+                                o[b][0] = make_float4(a[0].x, a[1].x, a[2].x, a[3].x);
+                                o[b][1] = make_float4(a[0].y, a[1].y, a[2].y, a[3].y);
+                                o[b][2] = make_float4(a[0].z, a[1].z, a[2].z, a[3].z);
+                                o[b][3] = make_float4(a[0].w, a[1].w, a[2].w, a[3].w);
 #pragma unroll
-                                    for (int i = 0; i < 4; i++)
+                                for (int i = 0; i < 4; i++)
+                                {
+                                    fv[b][i] = sv[b][i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                                }
+                                if constexpr (MODE == kSweepTick)
+                                {
+                                    if (ok)
                                     {
-                                        const int64_t gi = static_cast<int64_t>(4 * u + i) * p.Nlines + line0;
-                                        fv[b][i] = __ldg(reinterpret_cast<const float4 *>(p.f + gi));
-                                        if (p.src != nullptr)
+                                        const int64_t g0 = static_cast<int64_t>(4 * u) * nl + line0;
+#pragma unroll
+                                        for (int i = 0; i < 4; i++)
                                         {
-                                            sv[b][i] = __ldg(reinterpret_cast<const float4 *>(p.src + gi));
+                                            fv[b][i] = __ldg(reinterpret_cast<const float4 *>(p.f + g0 + i * nl));
+                                            if (hasSrc)
+                                            {
+                                                sv[b][i] = __ldg(reinterpret_cast<const float4 *>(p.src + g0 + i * nl));
+                                            }
                                         }
                                     }
                                 }
                             }
-                        }
 #pragma unroll
-                        for (int b = 0; b < kUB; b++)
-                        {
-                            const int32_t u = u0 + b * step;
-                            if (u >= nU)
+                            for (int b = 0; b < kUB; b++)
                             {
-                                continue;
-                            }
-#pragma unroll
-                            for (int i = 0; i < 4; i++)
-                            {
-                                float4 w4 = o[b][i];
-                                if constexpr (MODE == kSweepTick)
+                                const int32_t u = u0 + b * step;
+                                if (u >= nU)
                                 {
-                                    // per-agent uptake counts of the 4 lines at position 4u+i
-                                    int32_t n0 = 0, n1 = 0, n2 = 0, n3 = 0;
-                                    if (p.cellOffsets != nullptr)
-                                    {
-                                        const int64_t ci = static_cast<int64_t>(line0) * L + 4 * u + i;
-                                        n0 = __ldg(p.cellOffsets + ci + 1) - __ldg(p.cellOffsets + ci);
-                                        n1 = __ldg(p.cellOffsets + ci + L + 1) - __ldg(p.cellOffsets + ci + L);
-                                        n2 = __ldg(p.cellOffsets + ci + 2 * L + 1) - __ldg(p.cellOffsets + ci + 2 * L);
-                                        n3 = __ldg(p.cellOffsets + ci + 3 * L + 1) - __ldg(p.cellOffsets + ci + 3 * L);
-                                    }
-                                    auto commit = [&](float vv, float f0, float s0, int32_t nv) {
-                                        float d = vv - f0;
-                                        d = fmaf(f0, p.negDecay, d);
-                                        d += s0;
-                                        d = fmaf(f0, p.negUptake * static_cast<float>(nv), d);
-                                        return f0 + d;
-                                    };
-                                    w4.x = commit(w4.x, fv[b][i].x, sv[b][i].x, n0);
-                                    w4.y = commit(w4.y, fv[b][i].y, sv[b][i].y, n1);
-                                    w4.z = commit(w4.z, fv[b][i].z, sv[b][i].z, n2);
-                                    w4.w = commit(w4.w, fv[b][i].w, sv[b][i].w, n3);
+                                    continue;
                                 }
-                                St4(p.out + static_cast<int64_t>(4 * u + i) * p.Nlines + line0, w4);
+                                float *out = p.out + static_cast<int64_t>(4 * u) * nl + line0;
+#pragma unroll
+                                for (int i = 0; i < 4; i++)
+                                {
+                                    float4 w4 = o[b][i];
+                                    if constexpr (MODE == kSweepTick)
+                                    {
+                                        // per-agent uptake counts of the 4 lines at position 4u+i
+                                        int32_t n0 = 0, n1 = 0, n2 = 0, n3 = 0;
+                                        if constexpr (UPT)
+                                        {
+                                            const int64_t ci = static_cast<int64_t>(line0) * L + 4 * u + i;
+                                            n0 = __ldg(p.cellOffsets + ci + 1) - __ldg(p.cellOffsets + ci);
+                                            n1 = __ldg(p.cellOffsets + ci + L + 1) - __ldg(p.cellOffsets + ci + L);
+                                            n2 = __ldg(p.cellOffsets + ci + 2 * L + 1) - __ldg(p.cellOffsets + ci + 2 * L);
+                                            n3 = __ldg(p.cellOffsets + ci + 3 * L + 1) - __ldg(p.cellOffsets + ci + 3 * L);
+                                        }
+                                        // f' = f + ((v - f) - decay f + src - uptake n f)
+                                        auto commit = [&](float vv, float f0, float s0, int32_t nv) {
+                                            float d = vv - f0;
+                                            d = fmaf(f0, p.negDecay, d);
+                                            d += s0;
+                                            if constexpr (UPT)
+                                            {
+                                                d = fmaf(f0, p.negUptake * static_cast<float>(nv), d);
+                                            }
+                                            return f0 + d;
+                                        };
+                                        w4.x = commit(w4.x, fv[b][i].x, sv[b][i].x, n0);
+                                        w4.y = commit(w4.y, fv[b][i].y, sv[b][i].y, n1);
+                                        w4.z = commit(w4.z, fv[b][i].z, sv[b][i].z, n2);
+                                        w4.w = commit(w4.w, fv[b][i].w, sv[b][i].w, n3);
+                                    }
+                                    St4(out + i * nl, w4);
+                                }
                             }
                         }
+                    };
+                    if (MODE == kSweepTick && p.cellOffsets != nullptr)
+                    {
+                        writeVec(std::true_type{});
+                    }
+                    else
+                    {
+                        writeVec(std::false_type{});
                     }
                     return;
                 }
                 constexpr int kBatch = 2;
-                for (int32_t pos0 = tid / Q; pos0 < L && quadOk; pos0 += kBatch * step)
+                for (int32_t pos0 = uStart; pos0 < L && quadOk; pos0 += kBatch * step)
                 {
                     float4 v[kBatch], fv[kBatch], sv[kBatch];
                     int32_t nn[kBatch][4];
@@ -856,10 +1003,10 @@ namespace halcuda
                         nn[b][0] = nn[b][1] = nn[b][2] = nn[b][3] = 0;
                         if (pos < L)
                         {
-                            v[b] = make_float4(sLines[SPos<SWZ>(4 * qd + 1, pos, P, p.LS)],
-                                               sLines[SPos<SWZ>(4 * qd + 2, pos, P, p.LS)],
-                                               sLines[SPos<SWZ>(4 * qd + 3, pos, P, p.LS)],
-                                               sLines[SPos<SWZ>(4 * qd + 4, pos, P, p.LS)]);
+                            v[b] = make_float4(sLines[SolPos<SWZ>(4 * qd, pos, P, p.LS)],
+                                               sLines[SolPos<SWZ>(4 * qd + 1, pos, P, p.LS)],
+                                               sLines[SolPos<SWZ>(4 * qd + 2, pos, P, p.LS)],
+                                               sLines[SolPos<SWZ>(4 * qd + 3, pos, P, p.LS)]);
                             if constexpr (MODE == kSweepTick)
                             {
                                 const int64_t gi = static_cast<int64_t>(pos) * p.Nlines + line0;
@@ -1066,7 +1213,7 @@ namespace halcuda
             s.R = R;
             s.threads = ((R / kNL) * P + 31) & ~31;
             s.LS = swz ? P * M : P * kChunkStride + 4;  // padded: lines 4 mod 32 banks apart
-            s.smem = 1024 + sizeof(float) * (static_cast<size_t>(kCoefFloats) + kGbandSmem + static_cast<size_t>(R + 2) * s.LS +
+            s.smem = 1024 + sizeof(float) * (static_cast<size_t>(kCoefSmemFloats) + kGbandSmem + static_cast<size_t>(R + 2) * s.LS +
                                              2 * static_cast<size_t>(R) * P + 2 * static_cast<size_t>(R));
             return s;
         }
@@ -1143,7 +1290,7 @@ namespace halcuda
         }
         sh.R = R;
         sh.LS = P * kChunkStride + 4;
-        sh.smem = 1024 + sizeof(float) * (static_cast<size_t>(kCoefFloats) + kGbandSmem + static_cast<size_t>(R + 2) * sh.LS +
+        sh.smem = 1024 + sizeof(float) * (static_cast<size_t>(kCoefSmemFloats) + kGbandSmem + static_cast<size_t>(R + 2) * sh.LS +
                                           2 * static_cast<size_t>(R) * P + 2 * static_cast<size_t>(R));
         return sh;
     }
