@@ -797,6 +797,44 @@ namespace halcuda
                     St4(sLines + o, make_float4(z[j][4 * q], z[j][4 * q + 1], z[j][4 * q + 2], z[j][4 * q + 3]));
                 }
             }
+
+            // write-out mapping: thread -> group qd of 4 lines; out[pos *
+            // Nlines + line].  The lanes of a quarter-warp cover whole 64-byte
+            // segments of the output.
+            const int Q = R >> 2;  // a power of two <= 32
+            const int qd = tid & (Q - 1);
+            const int uStart = tid / Q;
+            const int32_t line0 = x0 + 4 * qd;
+            const int step = nthreads / Q;
+            const bool vecOut = (p.Nlines & 3) == 0;
+            const bool quadOk = line0 < p.Nlines;
+            const int32_t nU = L >> 2;
+            constexpr int kUB = 2;
+            const int64_t nl = p.Nlines;
+            // the commit's f and src of this thread's first write-out units,
+            // loaded before the barrier so that their latency overlaps it
+            // (the tensor-staged form; the register budget of the chunked
+            // form has no room for them)
+            constexpr bool kPre = (MODE == kSweepTick) && SWZ;
+            float4 fv0[kUB][4], sv0[kUB][4];
+            if constexpr (kPre)
+            {
+#pragma unroll
+                for (int b = 0; b < kUB; b++)
+                {
+                    const int32_t u = uStart + b * step;
+                    const bool ok = vecOut && vecL && quadOk && u < nU;
+                    const int64_t g0 = static_cast<int64_t>(4 * u) * nl + line0;
+#pragma unroll
+                    for (int i = 0; i < 4; i++)
+                    {
+                        fv0[b][i] = ok ? __ldg(reinterpret_cast<const float4 *>(p.f + g0 + i * nl))
+                                       : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                        sv0[b][i] = (ok && p.src != nullptr) ? __ldg(reinterpret_cast<const float4 *>(p.src + g0 + i * nl))
+                                                             : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    }
+                }
+            }
             __syncthreads();
 
             // ---- 2c. periodic lines: Sherman-Morrison correction -----------
@@ -864,16 +902,6 @@ namespace halcuda
             }
             else
             {
-                // thread -> group qd of 4 lines; out[pos * Nlines + line]
-                const int Q = R >> 2;                   // a power of two <= 32
-                // thread -> (quad qd, first unit uStart): the lanes of a
-                // quarter-warp cover whole 64-byte segments of the output
-                const int qd = tid & (Q - 1);
-                const int uStart = tid / Q;
-                const int32_t line0 = x0 + 4 * qd;
-                const int step = nthreads / Q;
-                const bool vecOut = (p.Nlines & 3) == 0;
-                const bool quadOk = line0 < p.Nlines;
                 if (vecOut && vecL)
                 {
                     // 16-byte units: 4 positions x 4 lines move as a 4x4 block
@@ -883,17 +911,15 @@ namespace halcuda
                     auto writeVec = [&](auto uptTag) {
                         constexpr bool UPT = decltype(uptTag)::value;
                         (void)UPT;
-                        const int32_t nU = L >> 2;
-                        constexpr int kUB = 2;
                         const bool hasSrc = (p.src != nullptr);
                         (void)hasSrc;  // read by the commit of MODE kSweepTick only
                         // unit u of solution line 4qd+e sits at
                         // SolOff4(4qd, u >> 3, u & 7) + e * lineStride: the
                         // four lines of a quad share one SolSwz
                         const int lineStride = SOff4<SWZ>(1, 0, 0, P, p.LS);
-                        const int64_t nl = p.Nlines;
-                        for (int32_t u0 = uStart; u0 < nU && quadOk; u0 += kUB * step)
-                        {
+                        // kUB units from u0 on; PRE: their f and src are fv0/sv0
+                        auto block = [&](int32_t u0, auto preTag) {
+                            constexpr bool PRE = decltype(preTag)::value;
                             float4 o[kUB][4];
                             float4 fv[kUB][4], sv[kUB][4];
 #pragma unroll
@@ -919,7 +945,16 @@ namespace halcuda
                                 }
                                 if constexpr (MODE == kSweepTick)
                                 {
-                                    if (ok)
+                                    if constexpr (PRE && kPre)
+                                    {
+#pragma unroll
+                                        for (int i = 0; i < 4; i++)
+                                        {
+                                            fv[b][i] = fv0[b][i];
+                                            sv[b][i] = sv0[b][i];
+                                        }
+                                    }
+                                    else if (ok)
                                     {
                                         const int64_t g0 = static_cast<int64_t>(4 * u) * nl + line0;
 #pragma unroll
@@ -978,6 +1013,19 @@ namespace halcuda
                                     St4(out + i * nl, w4);
                                 }
                             }
+                        };
+                        int32_t uFirst = uStart;
+                        if constexpr (kPre)
+                        {
+                            if (quadOk && uStart < nU)
+                            {
+                                block(uStart, std::true_type{});
+                            }
+                            uFirst += kUB * step;
+                        }
+                        for (int32_t u0 = uFirst; u0 < nU && quadOk; u0 += kUB * step)
+                        {
+                            block(u0, std::false_type{});
                         }
                     };
                     if (MODE == kSweepTick && p.cellOffsets != nullptr)
