@@ -121,6 +121,47 @@ def test_adi_tick_dirichlet_periodic_uptake_golden(hal, golden):
     assert rel_l2(out, g["cpl_out"]) <= 1e-5
 
 
+@pytest.mark.parametrize("xd,yd", [(512, 256), (256, 512)])
+@pytest.mark.parametrize("wrapX,wrapY,dirichlet,uptake", [
+    (True, False, True, 2e-3), (False, True, True, 0.0), (True, True, False, 2e-3), (False, False, False, 0.0)])
+def test_tensor_staged_tick_against_oracle(hal, oracle, xd, yd, wrapX, wrapY, dirichlet, uptake):
+    """Resident ticks whose line lengths are multiples of 256: both sweeps run
+    the tensor-staged form (swizzled staged rows, the per-quad permutation of
+    the solution rows, 16-byte write-out with the commit, f and src loaded
+    ahead) over several CTAs, with every boundary kind, a dense source, decay
+    and per-agent uptake, against the FP64 oracle."""
+    rng = np.random.default_rng(xd + 3 * yd + 7 * wrapX + 11 * wrapY)
+    n = xd * yd
+    f0 = rng.random(n).astype(np.float32)
+    src = (rng.random(n) * 1e-3).astype(np.float32)
+    ghost = rng.random(2 * (xd + yd)).astype(np.float32) if dirichlet else None
+    r, decay, ticks = 3.0, 5e-3, 6
+    nAgents = 20000
+    pos = np.empty(2 * nAgents, np.float32)
+    pos[0::2] = rng.random(nAgents) * xd
+    pos[1::2] = rng.random(nAgents) * yd
+    with hal.Agents(xd, yd, nAgents) as ag, hal.Adi(xd, yd) as a:
+        counts = None
+        if uptake:
+            ag.upload(pos, np.full(nAgents, 0.5, np.float32))
+            ag.dispatch(1.0, 0.1)
+            ag.sync()
+            off, _ = ag.get_bins()
+            counts = np.diff(off).astype(np.int32)
+            assert counts.sum() == nAgents and counts.max() >= 2
+            a.set_uptake(ag, uptake)
+        a.set_field(f0)
+        a.set_source(src)
+        if ghost is not None:
+            a.set_dirichlet(ghost)
+        a.run_ticks(ticks, r, decay, wrapX, wrapY)
+        out = a.get_field()
+    exp = oracle.run_ticks(1, f0.astype(np.float64), xd, yd, r, wrapX, wrapY,
+                           None if ghost is None else ghost.astype(np.float64), decay,
+                           src_dense=src.astype(np.float64), uptake_count=counts, uptake=uptake, ticks=ticks)
+    assert rel_l2(out, exp) <= 1e-5, rel_l2(out, exp)
+
+
 LINES = [1, 2, 3, 31, 32, 33, 63, 64, 65, 100, 257, 1000, 2048, 4096]
 
 
