@@ -1014,6 +1014,76 @@ namespace halcuda
                                 }
                             }
                         };
+                        if constexpr (kPre)
+                        {
+                            // exactly four units per thread (the thread-capped
+                            // shapes, e.g. 16 lines of 2048): a rotating
+                            // pipeline whose loads run one unit ahead
+                            if (quadOk && uStart + 3 * step < nU && uStart + 4 * step >= nU)
+                            {
+                                auto loadFS = [&](int32_t u, float4(&fo)[4], float4(&so)[4]) {
+                                    const int64_t g0 = static_cast<int64_t>(4 * u) * nl + line0;
+#pragma unroll
+                                    for (int i = 0; i < 4; i++)
+                                    {
+                                        fo[i] = __ldg(reinterpret_cast<const float4 *>(p.f + g0 + i * nl));
+                                        so[i] = hasSrc ? __ldg(reinterpret_cast<const float4 *>(p.src + g0 + i * nl))
+                                                       : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                                    }
+                                };
+                                auto unitOut = [&](int32_t u, const float4(&fi)[4], const float4(&si)[4]) {
+                                    const float *su = sLines + SolOff4<SWZ>(4 * qd, u >> 3, u & 7, P, p.LS);
+                                    float4 a[4];
+#pragma unroll
+                                    for (int e = 0; e < 4; e++)
+                                    {
+                                        a[e] = Ld4(su + e * lineStride);
+                                    }
+                                    const float4 o[4] = {make_float4(a[0].x, a[1].x, a[2].x, a[3].x),
+                                                         make_float4(a[0].y, a[1].y, a[2].y, a[3].y),
+                                                         make_float4(a[0].z, a[1].z, a[2].z, a[3].z),
+                                                         make_float4(a[0].w, a[1].w, a[2].w, a[3].w)};
+                                    float *out = p.out + static_cast<int64_t>(4 * u) * nl + line0;
+#pragma unroll
+                                    for (int i = 0; i < 4; i++)
+                                    {
+                                        int32_t n0 = 0, n1 = 0, n2 = 0, n3 = 0;
+                                        if constexpr (UPT)
+                                        {
+                                            const int64_t ci = static_cast<int64_t>(line0) * L + 4 * u + i;
+                                            n0 = __ldg(p.cellOffsets + ci + 1) - __ldg(p.cellOffsets + ci);
+                                            n1 = __ldg(p.cellOffsets + ci + L + 1) - __ldg(p.cellOffsets + ci + L);
+                                            n2 = __ldg(p.cellOffsets + ci + 2 * L + 1) - __ldg(p.cellOffsets + ci + 2 * L);
+                                            n3 = __ldg(p.cellOffsets + ci + 3 * L + 1) - __ldg(p.cellOffsets + ci + 3 * L);
+                                        }
+                                        auto commit = [&](float vv, float f0, float s0, int32_t nv) {
+                                            float d = vv - f0;
+                                            d = fmaf(f0, p.negDecay, d);
+                                            d += s0;
+                                            if constexpr (UPT)
+                                            {
+                                                d = fmaf(f0, p.negUptake * static_cast<float>(nv), d);
+                                            }
+                                            return f0 + d;
+                                        };
+                                        float4 w4 = o[i];
+                                        w4.x = commit(w4.x, fi[i].x, si[i].x, n0);
+                                        w4.y = commit(w4.y, fi[i].y, si[i].y, n1);
+                                        w4.z = commit(w4.z, fi[i].z, si[i].z, n2);
+                                        w4.w = commit(w4.w, fi[i].w, si[i].w, n3);
+                                        St4(out + i * nl, w4);
+                                    }
+                                };
+                                float4 fC[4], sC[4], fD[4], sD[4];
+                                unitOut(uStart, fv0[0], sv0[0]);
+                                loadFS(uStart + 2 * step, fC, sC);
+                                unitOut(uStart + step, fv0[1], sv0[1]);
+                                loadFS(uStart + 3 * step, fD, sD);
+                                unitOut(uStart + 2 * step, fC, sC);
+                                unitOut(uStart + 3 * step, fD, sD);
+                                return;
+                            }
+                        }
                         int32_t uFirst = uStart;
                         if constexpr (kPre)
                         {
