@@ -359,15 +359,6 @@ namespace halcuda
             return SolOff4<SWZ>(ll, k, i >> 2, P, LS) + (i & 3);
         }
 
-        // An opaque copy of v: keeps the compiler from holding values derived
-        // from v in registers across a long stretch of code.
-        __device__ __forceinline__ int Opaque(int v)
-        {
-            int r;
-            asm volatile("mov.b32 %0, %1;" : "=r"(r) : "r"(v));
-            return r;
-        }
-
         // Element pos of a staged line.
         template <bool SWZ>
         __device__ __forceinline__ int SPos(int line, int32_t pos, int P, int LS)
@@ -788,8 +779,8 @@ namespace halcuda
                 // every staged-line read finished before the barrier above,
                 // so the line's buffer can take the solution (SolOff4's unit
                 // order)
-                const int swo = Opaque((k & 7) ^ SolSwz(ll));
-                const int rowo = Opaque((ll + 1) * P + k);
+                const int swo = (k & 7) ^ SolSwz(ll);
+                const int rowo = (ll + 1) * P + k;
 #pragma unroll
                 for (int q = 0; q < M / 4; q++)
                 {
