@@ -64,79 +64,10 @@ namespace halcuda
         // take microseconds, so reaching it means the copies never landed
         constexpr unsigned long long kWaitLimitNs = 2000000000ull;
 
-        // Thomas forward elimination and back substitution of one block with
-        // the identity padding described in adi_plan.h.  The coefficients
-        // are read from shared memory 16 bytes at a time.
-        __device__ __forceinline__ void BlockSolve(float (&z)[M], const float *cf)
-        {
-            const float4 *fw = reinterpret_cast<const float4 *>(cf + kCoefFw * M);
-            const float4 *ib = reinterpret_cast<const float4 *>(cf + kCoefIb * M);
-            const float4 *cb = reinterpret_cast<const float4 *>(cf + kCoefCb * M);
-#pragma unroll
-            for (int j = 0; j < M / 4; j++)
-            {
-                const float4 w4 = fw[j];
-                if (j > 0)
-                {
-                    z[4 * j] = fmaf(-w4.x, z[4 * j - 1], z[4 * j]);
-                }
-                z[4 * j + 1] = fmaf(-w4.y, z[4 * j], z[4 * j + 1]);
-                z[4 * j + 2] = fmaf(-w4.z, z[4 * j + 1], z[4 * j + 2]);
-                z[4 * j + 3] = fmaf(-w4.w, z[4 * j + 2], z[4 * j + 3]);
-            }
-#pragma unroll
-            for (int j = M / 4 - 1; j >= 0; j--)
-            {
-                const float4 i4 = ib[j];
-                const float4 c4 = cb[j];
-                if (j == M / 4 - 1)
-                {
-                    z[4 * j + 3] *= i4.w;
-                }
-                else
-                {
-                    z[4 * j + 3] = fmaf(-c4.w, z[4 * j + 4], z[4 * j + 3] * i4.w);
-                }
-                z[4 * j + 2] = fmaf(-c4.z, z[4 * j + 3], z[4 * j + 2] * i4.z);
-                z[4 * j + 1] = fmaf(-c4.y, z[4 * j + 2], z[4 * j + 1] * i4.y);
-                z[4 * j + 0] = fmaf(-c4.x, z[4 * j + 1], z[4 * j + 0] * i4.x);
-            }
-        }
-
-        // x = z - sL p - sR q over the block.
-        __device__ __forceinline__ void BlockCorrect(float (&z)[M], const float *cf, float sL, float sR)
-        {
-            const float4 *pv = reinterpret_cast<const float4 *>(cf + kCoefP * M);
-            const float4 *qv = reinterpret_cast<const float4 *>(cf + kCoefQ * M);
-#pragma unroll
-            for (int j = 0; j < M / 4; j++)
-            {
-                const float4 p4 = pv[j];
-                const float4 q4 = qv[j];
-                z[4 * j + 0] = fmaf(-sL, p4.x, fmaf(-sR, q4.x, z[4 * j + 0]));
-                z[4 * j + 1] = fmaf(-sL, p4.y, fmaf(-sR, q4.y, z[4 * j + 1]));
-                z[4 * j + 2] = fmaf(-sL, p4.z, fmaf(-sR, q4.z, z[4 * j + 2]));
-                z[4 * j + 3] = fmaf(-sL, p4.w, fmaf(-sR, q4.w, z[4 * j + 3]));
-            }
-        }
-
-        // s_j = sum_m G[j][m] * (xA[m] + xB[m]) over the stored band.
-        __device__ __forceinline__ float BandDot(const LinePlanDev &pl, int j, const float *xA, const float *xB)
-        {
-            const int S = pl.P - 1;
-            const int lo = max(0, j - pl.B);
-            const int hi = min(S - 1, j + pl.B);
-            const float *g = pl.gband + static_cast<int64_t>(j) * (2 * pl.B + 1);
-            float acc = 0.0f;
-            for (int m = lo; m <= hi; m++)
-            {
-                acc = fmaf(__ldg(g + (m - j + pl.B)), xA[m] + xB[m], acc);
-            }
-            return acc;
-        }
-
-        // BlockSolve for all kNL lines of a thread: each coefficient vector is
-        // read from shared memory once and applied to every line, and the
+        // Thomas forward elimination and back substitution of one 32-row
+        // block (with the identity padding described in adi_plan.h) for all
+        // kNL lines of a thread: each coefficient vector is read from shared
+        // memory 16 bytes at a time, once, and applied to every line, and the
         // lines' recurrences interleave.
         __device__ __forceinline__ void BlockSolveN(float (&z)[kNL][M], const float *cf)
         {
@@ -182,7 +113,8 @@ namespace halcuda
             }
         }
 
-        // BlockCorrect for all kNL lines, one read of p and q.
+        // The coupling correction x = z - sL p - sR q over the block, for all
+        // kNL lines with one read of p and q.
         __device__ __forceinline__ void BlockCorrectN(float (&z)[kNL][M], const float *cf, const float (&sL)[kNL],
                                                       const float (&sR)[kNL])
         {
@@ -261,18 +193,6 @@ namespace halcuda
                     sL = fmaf(G[(k - 1) * W + t], sm, sL);
                 }
             }
-        }
-
-        // z[idx] for a run-time idx without dynamic register indexing.
-        __device__ __forceinline__ float SelectReg(const float (&z)[M], int idx)
-        {
-            float v = 0.0f;
-#pragma unroll
-            for (int i = 0; i < M; i++)
-            {
-                v = (i == idx) ? z[i] : v;
-            }
-            return v;
         }
 
         // Float offset, within the staged lines, of element i of chunk k of
@@ -914,6 +834,7 @@ namespace halcuda
                         // kUB units from u0 on; PRE: their f and src are fv0/sv0
                         auto block = [&](int32_t u0, auto preTag) {
                             constexpr bool PRE = decltype(preTag)::value;
+                            (void)PRE;  // read by the commit of MODE kSweepTick only
                             float4 o[kUB][4];
                             float4 fv[kUB][4], sv[kUB][4];
 #pragma unroll
