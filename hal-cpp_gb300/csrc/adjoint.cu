@@ -513,8 +513,13 @@ namespace halcuda
         {
             device = CurrentDevice();
             HAL_TRY(CudaStatus(cudaSetDevice(device), "cudaSetDevice"));
-            HAL_TRY(stream.Create("cudaStreamCreate"));
-            HAL_TRY(recomputeStream.Create("cudaStreamCreate"));
+            // the backward (and the forward) on the highest-priority stream,
+            // the overlapped recomputation on the lowest: recompute CTAs take
+            // the SMs the critical path leaves free
+            int least = 0, greatest = 0;
+            HAL_TRY(CudaStatus(cudaDeviceGetStreamPriorityRange(&least, &greatest), "cudaDeviceGetStreamPriorityRange"));
+            HAL_TRY(stream.Create("cudaStreamCreate", greatest));
+            HAL_TRY(recomputeStream.Create("cudaStreamCreate", least));
             g.xDim = xDim;
             g.yDim = yDim;
             g.wrapX = wrapX != 0;

@@ -137,9 +137,11 @@ namespace halcuda
         cudaStream_t user = nullptr;
         bool hasUser = false;
 
-        int Create(const char *what)
+        // priority: CUDA's stream priority (0 is the default and the lowest;
+        // cudaDeviceGetStreamPriorityRange gives the highest, a negative value)
+        int Create(const char *what, int priority = 0)
         {
-            return CudaStatus(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking), what);
+            return CudaStatus(cudaStreamCreateWithPriority(&own, cudaStreamNonBlocking, priority), what);
         }
 
         cudaStream_t Get() const
