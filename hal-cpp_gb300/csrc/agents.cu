@@ -8,9 +8,10 @@
 //   scan         reduce-then-scan over the cells (three launches, no spin waits)
 //   Scatter      agent -> offsets[cell] + arrival rank (order within a cell is
 //                the atomic arrival order, not yet the CPU's)
-//   Stabilize    each agent counts the lower-indexed agents of its cell, which
-//                gives exactly the CPU's slot; it writes the final bucket and a
-//                cell-sorted copy of positions and radii
+//   Stabilize    one thread per arrival-order slot: its agent counts the
+//                lower-indexed agents of its cell, which gives exactly the
+//                CPU's slot; it writes the final bucket and a cell-sorted copy
+//                of positions and radii
 //   Forces       one thread per sorted slot walks the cell window x-major then
 //                y, and each cell's slots in order -- the CPU's summation
 //                order -- and writes the agent's velocity delta.
@@ -287,20 +288,24 @@ namespace halcuda
                                   const TR *__restrict__ rad, int32_t n, int32_t *__restrict__ bucket,
                                   V2<TP> *__restrict__ sPos, TR *__restrict__ sRad)
         {
-            int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-            if (i >= n)
+            // thread -> arrival-order slot q: its agent i, then i's stable
+            // slot in the same cell (neighbouring threads share a cell's
+            // offsets and bucket range, and their writes land near q)
+            const int32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+            if (q >= n)
             {
                 return;
             }
-            int32_t c = cellOf[i];
-            int32_t s = offsets[c];
-            int32_t e = offsets[c + 1];
+            const int32_t i = bucketTmp[q];
+            const int32_t c = cellOf[i];
+            const int32_t s = offsets[c];
+            const int32_t e = offsets[c + 1];
             int32_t rank = 0;
-            for (int32_t q = s; q < e; q++)
+            for (int32_t t = s; t < e; t++)
             {
-                rank += (bucketTmp[q] < i) ? 1 : 0;
+                rank += (bucketTmp[t] < i) ? 1 : 0;
             }
-            int32_t slot = s + rank;
+            const int32_t slot = s + rank;
             bucket[slot] = i;
             sPos[slot] = posF[i];
             sRad[slot] = rad[i];
