@@ -224,15 +224,19 @@ namespace halcuda
             }
         }
 
-        // Counts up to this many cells are cleared by ScanApply as it reads
-        // them (cheaper than a memset while they sit in L2); larger ones by a
-        // memset before the binning (clearing in the scan measured 3.5x
-        // slower than a memset plus the plain scan at 109M cells).
-        constexpr int64_t kClearInScanCells = int64_t(16) << 20;
+        // Counts up to this many cells (in practice: all) are cleared by
+        // ScanApply as it reads them, writing only the 4-cell groups that
+        // hold a count; a memset before the binning clears counts not known
+        // to be zero.  With every group written, clearing in the scan had
+        // measured 3.5x slower than a memset at 109M cells; with only the
+        // occupied groups it is faster at both measured sizes (4.19M cells,
+        // 1M agents: 119.2 -> 115.0 us per dispatch; 109M cells, 5.2M
+        // agents: agent pass 0.818 -> 0.772 ms).
+        constexpr int64_t kClearInScanCells = int64_t(1) << 40;
 
         // Pass 3: tile-local exclusive scan plus the tile prefix -> offsets.
-        // With CLEAR it also zeroes the counts it has read, so the next
-        // binning starts from zero without a memset.
+        // With CLEAR it also zeroes the counts it has read (only the groups
+        // holding one), so the next binning starts from zero without a memset.
         template <bool CLEAR>
         __global__ void __launch_bounds__(kScanThreads) ScanApply(int32_t *__restrict__ counts, int64_t C,
                                                                   const int32_t *__restrict__ tilePrefix,
@@ -243,8 +247,19 @@ namespace halcuda
             LoadItems(counts, base, C, v);
             if constexpr (CLEAR)
             {
-                const int32_t zeros[kScanItems] = {0, 0, 0, 0};
-                StoreItems(counts, base, C, zeros);
+                // only groups holding a count are written: most cells are
+                // empty, and an empty group is already cleared
+                int32_t any = 0;
+#pragma unroll
+                for (int q = 0; q < kScanItems; q++)
+                {
+                    any |= v[q];
+                }
+                if (any != 0)
+                {
+                    const int32_t zeros[kScanItems] = {0, 0, 0, 0};
+                    StoreItems(counts, base, C, zeros);
+                }
             }
             int32_t s = 0;
 #pragma unroll
