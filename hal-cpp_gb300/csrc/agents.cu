@@ -69,11 +69,22 @@ namespace halcuda
             return c;
         }
 
+        // Programmatic dependent launch (LaunchChained): the next kernel of a
+        // dispatch may be scheduled once every CTA of this one has started;
+        // each kernel waits for its predecessor to complete before it touches
+        // any buffer (both are no-ops in a plain launch).
+        __device__ __forceinline__ void ChainEntry()
+        {
+            asm volatile("griddepcontrol.launch_dependents;");
+            asm volatile("griddepcontrol.wait;" ::: "memory");
+        }
+
         template <typename TP>
         __global__ void BinCount(const TP *__restrict__ pos, int32_t n, int32_t xDim, int32_t yDim,
                                  V2<TP> *__restrict__ posF, int32_t *__restrict__ cellOf,
                                  int32_t *__restrict__ arrival, int32_t *__restrict__ counts)
         {
+            ChainEntry();
             int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
             if (i >= n)
             {
@@ -85,6 +96,25 @@ namespace halcuda
             int32_t c = CellCoord(px, xDim) * yDim + CellCoord(py, yDim);
             cellOf[i] = c;
             arrival[i] = atomicAdd(counts + c, 1);
+        }
+
+        // A kernel of the agent dispatch, launched with programmatic stream
+        // serialization so that its launch overlaps its predecessor's tail
+        // (the kernels start with ChainEntry).
+        template <typename... KArgs, typename... Args>
+        void LaunchChained(void (*kernel)(KArgs...), unsigned grid, unsigned block, cudaStream_t s, Args... args)
+        {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(grid);
+            cfg.blockDim = dim3(block);
+            cfg.dynamicSmemBytes = 0;
+            cfg.stream = s;
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+            at[0].val.programmaticStreamSerializationAllowed = 1;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
         }
 
         // Inclusive warp scan.
@@ -188,6 +218,7 @@ namespace halcuda
         __global__ void __launch_bounds__(kScanThreads) ScanReduce(const int32_t *__restrict__ counts, int64_t C,
                                                                    int32_t *__restrict__ tileSums)
         {
+            ChainEntry();
             int64_t base = static_cast<int64_t>(blockIdx.x) * kScanTile + threadIdx.x * kScanItems;
             int32_t v[kScanItems];
             LoadItems(counts, base, C, v);
@@ -209,6 +240,7 @@ namespace halcuda
         // chunks of kScanThreads).
         __global__ void __launch_bounds__(kScanThreads) ScanTiles(int32_t *__restrict__ tileSums, int32_t nTiles)
         {
+            ChainEntry();
             int32_t carry = 0;
             for (int32_t base = 0; base < nTiles; base += kScanThreads)
             {
@@ -242,6 +274,7 @@ namespace halcuda
                                                                   const int32_t *__restrict__ tilePrefix,
                                                                   int32_t *__restrict__ offsets, int32_t n)
         {
+            ChainEntry();
             int64_t base = static_cast<int64_t>(blockIdx.x) * kScanTile + threadIdx.x * kScanItems;
             int32_t v[kScanItems];
             LoadItems(counts, base, C, v);
@@ -286,6 +319,7 @@ namespace halcuda
         __global__ void Scatter(const int32_t *__restrict__ cellOf, const int32_t *__restrict__ arrival,
                                 const int32_t *__restrict__ offsets, int32_t n, int32_t *__restrict__ bucketTmp)
         {
+            ChainEntry();
             int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
             if (i >= n)
             {
@@ -303,6 +337,7 @@ namespace halcuda
                                   const TR *__restrict__ rad, int32_t n, int32_t *__restrict__ bucket,
                                   V2<TP> *__restrict__ sPos, TR *__restrict__ sRad)
         {
+            ChainEntry();
             // thread -> arrival-order slot q: its agent i, then i's stable
             // slot in the same cell (neighbouring threads share a cell's
             // offsets and bucket range, and their writes land near q)
@@ -516,6 +551,7 @@ namespace halcuda
                                double interactionRad, T R, T k, int32_t xDim, int32_t yDim, int32_t wrapX,
                                int32_t wrapY, TV *__restrict__ vel)
         {
+            ChainEntry();
             const int32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
             if (slot >= n)
             {
@@ -599,6 +635,7 @@ namespace halcuda
                                    MoveParams mp, float *__restrict__ deltas, float2 *__restrict__ pos,
                                    float2 *__restrict__ velocity)
         {
+            ChainEntry();
             const int32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
             if (slot >= n)
             {
@@ -769,23 +806,23 @@ namespace halcuda
             unsigned ablocks = static_cast<unsigned>((n + T - 1) / T);
             if (n > 0)
             {
-                BinCount<TP><<<ablocks, T, 0, s>>>(pos, n, xDim, yDim, PosBuf(TP()), cellOf.p, arrival.p,
-                                                   counts.p);
+                LaunchChained(BinCount<TP>, ablocks, T, s, pos, n, xDim, yDim, PosBuf(TP()), cellOf.p, arrival.p,
+                              counts.p);
                 CountLaunch();
             }
             if (ev)
             {
                 cudaEventRecord(ev[0], s);
             }
-            ScanReduce<<<nTiles, kScanThreads, 0, s>>>(counts.p, C, tileSums.p);
-            ScanTiles<<<1, kScanThreads, 0, s>>>(tileSums.p, nTiles);
+            LaunchChained(ScanReduce, nTiles, kScanThreads, s, counts.p, C, tileSums.p);
+            LaunchChained(ScanTiles, 1u, kScanThreads, s, tileSums.p, nTiles);
             if (clearInScan)
             {
-                ScanApply<true><<<nTiles, kScanThreads, 0, s>>>(counts.p, C, tileSums.p, offsets.p, n);
+                LaunchChained(ScanApply<true>, nTiles, kScanThreads, s, counts.p, C, tileSums.p, offsets.p, n);
             }
             else
             {
-                ScanApply<false><<<nTiles, kScanThreads, 0, s>>>(counts.p, C, tileSums.p, offsets.p, n);
+                LaunchChained(ScanApply<false>, nTiles, kScanThreads, s, counts.p, C, tileSums.p, offsets.p, n);
             }
             CountLaunch(3);
             countsDirty = !clearInScan || (cudaPeekAtLastError() != cudaSuccess);
@@ -795,7 +832,7 @@ namespace halcuda
             }
             if (n > 0)
             {
-                Scatter<<<ablocks, T, 0, s>>>(cellOf.p, arrival.p, offsets.p, n, bucketTmp.p);
+                LaunchChained(Scatter, ablocks, T, s, cellOf.p, arrival.p, offsets.p, n, bucketTmp.p);
                 CountLaunch();
             }
             if (ev)
@@ -804,8 +841,8 @@ namespace halcuda
             }
             if (n > 0)
             {
-                Stabilize<TP, TR><<<ablocks, T, 0, s>>>(cellOf.p, offsets.p, bucketTmp.p, PosBuf(TP()), rad, n,
-                                                        bucket.p, SortedPosBuf(TP()), sRad);
+                LaunchChained(Stabilize<TP, TR>, ablocks, T, s, cellOf.p, offsets.p, bucketTmp.p, PosBuf(TP()), rad, n,
+                              bucket.p, SortedPosBuf(TP()), sRad);
                 CountLaunch();
             }
             if (ev)
@@ -824,8 +861,9 @@ namespace halcuda
             }
             const int T_ = 128;
             unsigned blocks = static_cast<unsigned>((n + T_ - 1) / T_);
-            Forces<T, TV><<<blocks, T_, 0, s>>>(bucket.p, offsets.p, SortedPosBuf(T()), sRad, n, R, static_cast<T>(R),
-                                                static_cast<T>(k), xDim, yDim, wrapX, wrapY, vel);
+            LaunchChained(Forces<T, TV>, blocks, T_, s, bucket.p, offsets.p, SortedPosBuf(T()), sRad, n, R,
+                          static_cast<T>(R), static_cast<T>(k), xDim, yDim, static_cast<int32_t>(wrapX),
+                          static_cast<int32_t>(wrapY), vel);
             CountLaunch();
             return LaunchStatus("agent forces");
         }
@@ -847,9 +885,9 @@ namespace
         }
         const int T = 128;
         const unsigned blocks = static_cast<unsigned>((a.n + T - 1) / T);
-        ForcesMove<<<blocks, T, 0, s>>>(a.bucket.p, a.offsets.p, a.sPos.p, a.sRad32.p, a.n, R, static_cast<float>(R),
-                                        static_cast<float>(k), a.xDim, a.yDim, mp, a.vel32.p,
-                                        reinterpret_cast<float2 *>(a.pos32.p), a.velState.p);
+        LaunchChained(ForcesMove, blocks, T, s, a.bucket.p, a.offsets.p, a.sPos.p, a.sRad32.p, a.n, R,
+                      static_cast<float>(R), static_cast<float>(k), a.xDim, a.yDim, mp, a.vel32.p,
+                      reinterpret_cast<float2 *>(a.pos32.p), a.velState.p);
         CountLaunch();
         return LaunchStatus("agent forces and move");
     }
