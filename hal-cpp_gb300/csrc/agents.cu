@@ -92,7 +92,10 @@ namespace halcuda
             }
             const TP px = pos[2 * static_cast<int64_t>(i)];
             const TP py = pos[2 * static_cast<int64_t>(i) + 1];
-            posF[i] = Vec2<TP>::Make(px, py);
+            if (posF != nullptr)  // null when the positions are already V2-aligned
+            {
+                posF[i] = Vec2<TP>::Make(px, py);
+            }
             int32_t c = CellCoord(px, xDim) * yDim + CellCoord(py, yDim);
             cellOf[i] = c;
             arrival[i] = atomicAdd(counts + c, 1);
@@ -806,8 +809,10 @@ namespace halcuda
             unsigned ablocks = static_cast<unsigned>((n + T - 1) / T);
             if (n > 0)
             {
-                LaunchChained(BinCount<TP>, ablocks, T, s, pos, n, xDim, yDim, PosBuf(TP()), cellOf.p, arrival.p,
-                              counts.p);
+                // pos is the handle's own device buffer (cudaMalloc'd, so
+                // aligned for V2<TP>): the stabilize pass reads it directly
+                LaunchChained(BinCount<TP>, ablocks, T, s, pos, n, xDim, yDim, static_cast<V2<TP> *>(nullptr),
+                              cellOf.p, arrival.p, counts.p);
                 CountLaunch();
             }
             if (ev)
@@ -841,8 +846,8 @@ namespace halcuda
             }
             if (n > 0)
             {
-                LaunchChained(Stabilize<TP, TR>, ablocks, T, s, cellOf.p, offsets.p, bucketTmp.p, PosBuf(TP()), rad, n,
-                              bucket.p, SortedPosBuf(TP()), sRad);
+                LaunchChained(Stabilize<TP, TR>, ablocks, T, s, cellOf.p, offsets.p, bucketTmp.p,
+                              reinterpret_cast<const V2<TP> *>(pos), rad, n, bucket.p, SortedPosBuf(TP()), sRad);
                 CountLaunch();
             }
             if (ev)
