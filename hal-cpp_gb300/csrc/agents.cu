@@ -745,8 +745,8 @@ namespace halcuda
         DevBuf<float> pos32, rad32, vel32;
         DevBuf<float2> velState;  // the agents' own velocities (xVel, yVel) of the resident step
         DevBuf<double> pos64, rad64, vel64;
-        DevBuf<float2> posF, sPos;
-        DevBuf<double2> posD, sPosD;  // FP64 interface path
+        DevBuf<float2> sPos;
+        DevBuf<double2> sPosD;  // FP64 interface path
         DevBuf<float> sRad32;
         DevBuf<double> sRad64;
         DevBuf<int32_t> cellOf, arrival, counts, offsets, tileSums, bucketTmp, bucket;
@@ -768,7 +768,6 @@ namespace halcuda
             HAL_TRY(vel32.Alloc(2 * m, "cudaMalloc(agents)"));
             HAL_TRY(velState.Alloc(m, "cudaMalloc(agents)"));
             HAL_TRY(CudaStatus(cudaMemset(velState.p, 0, m * sizeof(float2)), "cudaMemset"));
-            HAL_TRY(posF.Alloc(m, "cudaMalloc(agents)"));
             HAL_TRY(sPos.Alloc(m, "cudaMalloc(agents)"));
             HAL_TRY(sRad32.Alloc(m, "cudaMalloc(agents)"));
             HAL_TRY(cellOf.Alloc(m, "cudaMalloc(agents)"));
@@ -783,16 +782,13 @@ namespace halcuda
             return HAL_CUDA_OK;
         }
 
-        // Bins n agents (positions of type TP, interleaved x,y) and sorts
-        // radii of type TR alongside.
-        // Bins n agents (positions of type TP, interleaved x,y) and sorts
-        // radii of type TR alongside.  With ev != nullptr, records an event
-        // after each stage (count, scan, scatter, stabilize) for profiling.
-        V2<float> *PosBuf(float) { return posF.p; }
-        V2<double> *PosBuf(double) { return posD.p; }
         V2<float> *SortedPosBuf(float) { return sPos.p; }
         V2<double> *SortedPosBuf(double) { return sPosD.p; }
 
+        // Bins n agents (positions of type TP, interleaved x,y, in one of the
+        // handle's own device buffers) and sorts radii of type TR alongside.
+        // With ev != nullptr, records an event after each stage (count, scan,
+        // scatter, stabilize) for profiling.
         template <typename TP, typename TR>
         int Bin(const TP *pos, const TR *rad, TR *sRad, cudaStream_t s, cudaEvent_t *ev = nullptr)
         {
@@ -986,7 +982,6 @@ extern "C" int hal_cuda_accumulate_forces(hal_cuda_agents *h, const double *posi
         HAL_TRY(h->rad64.Alloc(m, "cudaMalloc(agents64)"));
         HAL_TRY(h->vel64.Alloc(2 * m, "cudaMalloc(agents64)"));
         HAL_TRY(h->sRad64.Alloc(m, "cudaMalloc(agents64)"));
-        HAL_TRY(h->posD.Alloc(m, "cudaMalloc(agents64)"));
         HAL_TRY(h->sPosD.Alloc(m, "cudaMalloc(agents64)"));
     }
     cudaStream_t s = h->stream.Get();
