@@ -138,6 +138,33 @@ def test_million_agent_workload(hal, oracle):
     assert max_rel(v32, exp) <= 1e-4
 
 
+def test_large_grid_repeated_dispatches(hal, oracle):
+    """25M cells (the counts are cleared inside the scan at every size, only
+    where a 4-cell group held a count): three dispatches of different agent
+    sets on one handle, bins bit-exact against the oracle each time, so a
+    count left behind by an earlier dispatch would show."""
+    xd, yd = 5000, 5000
+    rng = np.random.default_rng(11)
+    with hal.Agents(xd, yd, 300_000) as ag:
+        for n in (300_000, 120_000, 250_000):
+            pos32 = np.empty(2 * n, np.float32)
+            pos32[0::2] = rng.random(n) * xd
+            pos32[1::2] = rng.random(n) * yd
+            # a dense cluster, so that some groups hold several counts
+            m = n // 5
+            pos32[0:2 * m:2] = (xd / 2 + rng.standard_normal(m) * 20).astype(np.float32)
+            pos32[1:2 * m:2] = (yd / 2 + rng.standard_normal(m) * 20).astype(np.float32)
+            rad32 = (0.3 + rng.random(n) * 0.2).astype(np.float32)
+            _, eoff, eb = oracle.accumulate_forces(pos32.astype(np.float64), rad32.astype(np.float64), 1.0, 0.1,
+                                                    xd, yd, 0, 0, threads=16)
+            ag.upload(pos32, rad32)
+            ag.dispatch(1.0, 0.1)
+            ag.sync()
+            off, bucket = ag.get_bins()
+            assert np.array_equal(off, eoff), n
+            assert np.array_equal(bucket, eb), n
+
+
 @pytest.mark.parametrize("wrap", [False, True])
 def test_fp64_positions_off_the_float_grid(hal, oracle, wrap):
     """The FP64 interface path keeps positions in FP64: cells are floored in
