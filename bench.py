@@ -69,6 +69,24 @@ def dist_env():
     return rank, local, world
 
 
+def max_over_ranks(ms, dist=None, device="cuda"):
+    """The job's time: the largest of the ranks' timed milliseconds (every
+    rank receives it).  Single process: ms itself."""
+    if dist is None:
+        return ms
+    import torch
+
+    t = torch.tensor([ms], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(world, units_per_rank_step, ms_step):
+    """Whole-job throughput: every replica processes units_per_rank_step units
+    per step, and the job's step takes the slowest rank's ms_step."""
+    return world * units_per_rank_step / (ms_step * 1e-3)
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -610,13 +628,9 @@ def main():
     launches = hal.launch_count() - launches0
     if dist is not None:
         dist.barrier()
-    total_ms = sum(s.elapsed_time(e) for s, e in zip(ev_s, ev_e))
-    if dist is not None:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(sum(s.elapsed_time(e) for s, e in zip(ev_s, ev_e)), dist)
     ms_step = total_ms / args.steps
-    value = world * CELLS * TICKS / (ms_step * 1e-3)
+    value = job_value(world, CELLS * TICKS, ms_step)
 
     # per-kernel launch times: the mean of 200 back-to-back launches of each
     # sweep replayed from a graph (the steady state of the timed region),
@@ -654,12 +668,8 @@ def main():
         t1.record(stream)
         t1.synchronize()
         e2e_ms.append(t0.elapsed_time(t1))
-    e2e_step = statistics.median(e2e_ms)
-    if dist is not None:
-        t = torch.tensor([e2e_step], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_step = float(t.item())
-    e2e_value = world * CELLS * TICKS / (e2e_step * 1e-3)
+    e2e_step = max_over_ranks(statistics.median(e2e_ms), dist)
+    e2e_value = job_value(world, CELLS * TICKS, e2e_step)
 
     acc = None
     if rank == 0:
