@@ -373,8 +373,6 @@ namespace halcuda
         __device__ __forceinline__ float Add(float a, float b) { return __fadd_rn(a, b); }
         __device__ __forceinline__ float Sub(float a, float b) { return __fsub_rn(a, b); }
         __device__ __forceinline__ float Mul(float a, float b) { return __fmul_rn(a, b); }
-        __device__ __forceinline__ float Div(float a, float b) { return __fdiv_rn(a, b); }
-        __device__ __forceinline__ float Sqrt(float a) { return __fsqrt_rn(a); }
         __device__ __forceinline__ double Abs(double a) { return fabs(a); }
         __device__ __forceinline__ float Abs(float a) { return fabsf(a); }
 
