@@ -353,6 +353,81 @@ def secondary_agents(hal, stream, iters=20):
                              "sample": "one FP64 AccumulateForces of the same 1M agents (oracle, 1 thread)"}}
 
 
+def secondary_coupled(hal, torch, stream, ticks=100, cpu_ticks=2):
+    """1M moving agents coupled to a 2048^2 ADI field: each tick is the
+    resident agent step (bins, forces, SphericalAgent2D move) followed by the
+    ADI tick whose commit removes 0.001 of the field per agent in each cell,
+    both on one stream, for 100 ticks."""
+    from halcuda import workloads
+
+    ag_in = workloads.agent_inputs(1_000_000, N, seed=3)
+    fd_in = workloads.adi_inputs(N, seed=2)
+    n = ag_in["radii"].size
+    f32 = fd_in["field"].astype(np.float32)
+    s32 = fd_in["src"].astype(np.float32)
+    args = (1.0, 0.1, False, False)
+    with hal.Agents(N, N, n) as ag, hal.Adi(N, N) as a:
+        a.set_stream(stream.cuda_stream)
+        ag.set_stream(stream.cuda_stream)
+        a.set_field(f32)
+        a.set_source(s32)
+        a.set_uptake(ag, 0.001)
+
+        def run(k):
+            for _ in range(k):
+                ag.step(1, *args, friction=0.5, maxVel=-1.0)
+                a.run_ticks(1, RATE, DECAY)
+
+        ag.upload(ag_in["positions"], ag_in["radii"])
+        run(5)
+        a.sync()
+        ag.upload(ag_in["positions"], ag_in["radii"])
+        a.set_field(f32)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        run(ticks)
+        e1.record(stream)
+        e1.synchronize()
+        ms_tick = e0.elapsed_time(e1) / ticks
+        ag.set_stream(None)
+        a.set_stream(None)
+    # the same coupled tick on the CPU: FP64 forces, the FP64 agent update and
+    # the FP64 ADI tick with the per-cell counts (oracle, 1 thread)
+    O = _oracle()
+    p = ag_in["positions"].astype(np.float64)
+    rad = ag_in["radii"].astype(np.float64)
+    v = np.zeros_like(p)
+    f = f32.astype(np.float64)
+    s = s32.astype(np.float64)
+    t0 = time.perf_counter()
+    for _ in range(cpu_ticks):
+        dv, off, _ = O.accumulate_forces(p, rad, 1.0, 0.1, N, N, False, False)
+        p, v = O.agents_move(p, v, dv, N, N, False, False, 0.5, -1.0)
+        f = O.run_ticks(1, f, N, N, RATE, decay=DECAY, src_dense=s, uptake_count=np.diff(off).astype(np.int32),
+                        uptake=0.001, ticks=1)
+    cpu_s = (time.perf_counter() - t0) / cpu_ticks
+    # algorithmic bytes of one coupled tick: ADI 24 B/cell plus the y-sweep's
+    # read of the cell offsets (4 B/cell); the agent step's binning and forces
+    # (28 B/agent + 16 B/bin) plus its move (read and write position and
+    # velocity, 16 B/agent)
+    bytes_tick = (24 + 4) * CELLS + (28 + 16) * n + 16 * CELLS
+    peak, _ = peaks()
+    ach = bytes_tick / (ms_tick * 1e-3) / 1e9
+    return {"workload": "coupled-1M-agents-2048x2048-adi-r5-uptake0.001-100ticks",
+            "value": n / (ms_tick * 1e-3), "unit": "agents/s",
+            "cell_updates_per_s": CELLS / (ms_tick * 1e-3), "ms_per_coupled_tick": ms_tick,
+            "roofline": {"kernel": "whole coupled tick (agent step + ADI tick)", "bound": "hbm", "achieved": ach,
+                         "peak": peak, "unit": "GB/s", "frac": ach / peak, "traffic": None,
+                         "bytes_per_tick": bytes_tick},
+            "cpu_baseline": {"value": n / cpu_s, "unit": "agents/s", "cores": 1, "kind": "port",
+                             "ms_per_coupled_tick": cpu_s * 1e3,
+                             "sample": f"{cpu_ticks} FP64 coupled ticks of the same workload (oracle forces, "
+                                       "agent update and ADI tick with uptake, 1 thread)"},
+            "parity": "bins bit-exact every 10th tick and field rel-L2 <= 1e-5 over 100 ticks "
+                      "(tests/test_coupled_gpu.py)"}
+
+
 def secondary_wells(hal, torch, stream, ticks=20, plain_ticks=3):
     """512 independent wells (109M cells, 5.2M agents): one batched tick of
     every well against per-well launches of the single-grid handles."""
@@ -559,6 +634,101 @@ def secondary_adjoint(hal, directions=None):
             "note": "FP32 device loss; FD noise estimated from differences at h and 2h"}
 
 
+def profile_case(case, n, iters):
+    """Small, fixed launches of one hot kernel for an ncu capture: the case's
+    inputs at grid side n, one untimed warm-up launch sequence, then `iters`
+    individually launched iterations (no CUDA graph), so that
+    `ncu -k <kernel> -c <k>` sees plain launches with few launches before them.
+
+        adi N K        K ADI ticks (x-sweep + y-sweep) of the N^2 workload
+        explicit N K   K fused explicit ticks
+        agents N K     K dispatches of the agent workload scaled to N^2 cells
+        stencil64 N K  K x (FP64 per-cell rate diffusion, advection, per-cell advection)
+        wells 0 K      K batched ticks of the 512 wells
+        adjoint N K    one gradient of K steps, checkpoints every 10
+        coupled N K    K coupled ticks (agent step + ADI tick with uptake)
+    """
+    import halcuda as hal
+    from halcuda import workloads
+
+    if case == "adi":
+        w = workloads.adi_inputs(n, seed=2, blobs=20)
+        with hal.Adi(n, n) as a:
+            a.set_field(w["field"])
+            a.set_source(w["src"])
+            a.profile(1, RATE, DECAY)
+            ms = a.profile(iters, RATE, DECAY)
+        print(f"adi {n}^2: x-sweep {ms[0]*1e3:.1f} us, y-sweep {ms[1]*1e3:.1f} us")
+    elif case == "explicit":
+        w = workloads.explicit_inputs(n, seed=1)
+        with hal.Diffusion(n, n) as d:
+            d.set_field(w["field"])
+            d.set_point_sources(w["src_idx"], w["src_val"])
+            d.profile(1, 0.2, 0.001)
+            ms = d.profile(iters, 0.2, 0.001)
+        print(f"explicit {n}^2: tick {ms*1e3:.1f} us")
+    elif case == "agents":
+        agents = max(1, int(1_000_000 * (n / 2048) ** 2))
+        w = workloads.agent_inputs(agents, n, seed=3)
+        with hal.Agents(n, n, agents) as ag:
+            ag.upload(w["positions"], w["radii"])
+            ag.profile(1, 1.0, 0.1)
+            ms = ag.profile(iters, 1.0, 0.1)
+        print(f"agents {agents} in {n}^2: " + ", ".join(f"{v*1e3:.1f}" for v in ms) + " us")
+    elif case == "stencil64":
+        rng = np.random.default_rng(12)
+        cells = n * n
+        f, d = rng.random(cells), np.zeros(cells)
+        rx, ry = rng.random(cells) * 0.24, rng.random(cells) * 0.24
+        vx, vy = rng.random(cells) - 0.5, rng.random(cells) - 0.5
+        with hal.Diffusion(n, n) as h:
+            for _ in range(iters):
+                h.diffuse_var(f, d.copy(), rx, ry, 0, 0)
+                h.advect(f, d.copy(), 0.2, -0.1, 0, 0)
+                h.advect_var(f, d.copy(), vx, vy, 0, 0)
+        print(f"stencil64 {n}^2: {iters} x (diffuse_var, advect, advect_var)")
+    elif case == "wells":
+        w = workloads.wells_inputs()
+        with hal.Wells(w["wells"]) as b:
+            for i, f in enumerate(w["fields"]):
+                b.set_field(i, f)
+            b.set_agents(w["counts"], w["positions"], w["radii"])
+            b.run_ticks(1, w["interactionRad"], w["springConstant"])  # autotune + graph capture
+            b.sync()
+            ms = b.profile(iters, w["interactionRad"], w["springConstant"])
+        print("wells: " + ", ".join(f"{v:.3f}" for v in ms) + " ms (explicit, adi x, adi y, agents, tick)")
+    elif case == "adjoint":
+        rng = np.random.default_rng(4)
+        f0 = workloads.gaussian_blobs(n, rng, 8).astype(np.float32)
+        D = workloads.rate_field(n, rng).astype(np.float32)
+        src = (rng.random(n * n) * 0.01).astype(np.float32)
+        with hal.Adjoint(n, n) as a:
+            a.set_problem(f0, np.roll(f0, 3), iters, 10)
+            a.forward(D, 0.005, src)
+            a.gradient(D, 0.005, src)
+            t = a.times()
+        print(f"adjoint {n}^2, {iters} steps: forward {t[0]:.2f} ms, gradient {t[1]:.2f} ms")
+    elif case == "coupled":
+        agents = max(1, int(1_000_000 * (n / 2048) ** 2))
+        ag_in = workloads.agent_inputs(agents, n, seed=3)
+        fd_in = workloads.adi_inputs(n, seed=2, blobs=20)
+        with hal.Agents(n, n, agents) as ag, hal.Adi(n, n) as a:
+            ag.set_stream(a.stream())
+            ag.upload(ag_in["positions"], ag_in["radii"])
+            a.set_field(fd_in["field"])
+            a.set_source(fd_in["src"])
+            a.set_uptake(ag, 0.001)
+            for _ in range(iters + 1):
+                ag.step(1, 1.0, 0.1, friction=0.5, maxVel=-1.0)
+                a.run_ticks(1, RATE, DECAY)
+            a.sync()
+            ag.set_stream(None)
+        print(f"coupled {agents} agents in {n}^2: {iters + 1} ticks")
+    else:
+        raise SystemExit(f"unknown profile case {case}")
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -567,7 +737,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", default=None,
+                    help="run one small fixed case for an ncu capture instead of the benchmark "
+                         "(adi, explicit, agents, stencil64, wells, adjoint, coupled)")
+    ap.add_argument("--profile-size", type=int, default=2048, help="grid side of the profile case")
+    ap.add_argument("--profile-iters", type=int, default=3, help="launch iterations of the profile case")
     args = ap.parse_args()
+    if args.profile_case is not None:
+        return profile_case(args.profile_case, args.profile_size, args.profile_iters)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
@@ -686,6 +863,7 @@ def main():
     if not args.no_secondary and rank == 0:
         secondary = {"explicit": secondary_explicit(hal, torch, stream),
                      "agents": secondary_agents(hal, stream),
+                     "coupled": secondary_coupled(hal, torch, stream),
                      "wells": secondary_wells(hal, torch, stream),
                      "adjoint": secondary_adjoint(hal),
                      "stencil64": secondary_stencil64(hal, torch, stream)}

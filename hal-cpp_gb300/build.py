@@ -52,7 +52,7 @@ def _compile(src, force, extra):
     path = os.path.join(CSRC, src)
     obj = os.path.join(OBJ, os.path.splitext(src)[0] + ".o")
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
-    deps.append(os.path.join(INCLUDE, "hal_cuda.h"))
+    deps += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
     if not force and not _newer(path, obj, deps):
         return obj, ""
     cmd = [nvcc] + NVFLAGS + extra + ["-c", path, "-o", obj]

@@ -308,6 +308,28 @@ namespace halcuda
             return t;
         }
 
+        // Waits for phase 0 of the mbarrier at shared address bar, suspended
+        // in try_wait between polls, for at most limitNs of %globaltimer;
+        // returns whether the phase completed.
+        __device__ __forceinline__ bool MbarWaitBounded(uint32_t bar, unsigned long long limitNs)
+        {
+            const unsigned long long t0 = GlobalTimerNs();
+            uint32_t done = 0;
+            while (!done)
+            {
+                asm volatile(
+                    "{ .reg .pred ok; mbarrier.try_wait.parity.shared::cta.b64 ok, [%1], 0, %2; selp.u32 %0, 1, 0, ok; }"
+                    : "=r"(done)
+                    : "r"(bar), "r"(1000000u)
+                    : "memory");
+                if (!done && GlobalTimerNs() - t0 > limitNs)
+                {
+                    return false;
+                }
+            }
+            return true;
+        }
+
         // One CTA's tile of a sweep: lines x0 .. x0+R-1 of the grid p.  tmap
         // is the grid's line tensor map (SWZ) or null.
         template <int MODE, bool SWZ>
@@ -480,21 +502,14 @@ namespace halcuda
             if (tmaBytes > 0)
             {
                 // every thread waits for the copies' bytes, suspended in
-                // try_wait between polls; bounded by kWaitLimitNs
-                const unsigned long long t0 = GlobalTimerNs();
-                uint32_t done = 0;
-                while (!done)
+                // try_wait between polls; bounded by kWaitLimitNs.  A wait
+                // that gives up records the failure and waits once more
+                // (bounded again), so that no copy is still writing into
+                // this CTA's shared memory when it exits.
+                if (!MbarWaitBounded(bar, kWaitLimitNs))
                 {
-                    asm volatile(
-                        "{ .reg .pred ok; mbarrier.try_wait.parity.shared::cta.b64 ok, [%1], 0, %2; selp.u32 %0, 1, 0, ok; }"
-                        : "=r"(done)
-                        : "r"(bar), "r"(1000000u)
-                        : "memory");
-                    if (!done && GlobalTimerNs() - t0 > kWaitLimitNs)
-                    {
-                        s_fail = 1;
-                        break;
-                    }
+                    s_fail = 1;
+                    MbarWaitBounded(bar, kWaitLimitNs);
                 }
             }
             if constexpr (SWZ)
@@ -1458,6 +1473,9 @@ namespace halcuda
         DevBuf<double> f64, d64;
         DevBuf<float> g32;       // ghost table of the FP64 interface call, in float
         DevBuf<int32_t> err;
+        // set once a bounded device wait has given up: the sweep that gave
+        // up left its lines undefined, so the handle takes no further ticks
+        bool stopped = false;
         const hal_cuda_agents *agents = nullptr;
         double uptake = 0.0;
         std::map<std::string, std::unique_ptr<LinePlanBuf>> plans;
@@ -1535,8 +1553,22 @@ namespace halcuda
             if (h != 0)
             {
                 cudaMemsetAsync(err.p, 0, sizeof(int32_t), stream.Get());
+                stopped = true;
                 SetError(h == 2 ? "%s: the sweep's shared-memory buffer was not 1024-byte aligned"
                                 : "%s: a staged copy did not complete within its wait limit",
+                         who);
+                return HAL_CUDA_ETIMEOUT;
+            }
+            return HAL_CUDA_OK;
+        }
+
+        // Refuses work on a handle whose device wait has given up before.
+        int Usable(const char *who) const
+        {
+            if (stopped)
+            {
+                SetError("%s: the handle stopped after a sweep gave up waiting for its staged lines; its field is "
+                         "undefined: destroy the handle and create a new one",
                          who);
                 return HAL_CUDA_ETIMEOUT;
             }
@@ -1580,6 +1612,7 @@ namespace halcuda
         // x-sweep: lines along x (layout B input), w out in layout A.
         int LaunchX(const float *fB, double r, bool wrapX, bool wrapY, const float *ghostTab, cudaStream_t s)
         {
+            HAL_TRY(Usable("ADI x-sweep"));
             const LinePlanDev *pl = nullptr;
             const int ends = wrapX ? kEndsPeriodic : (ghostTab ? kEndsDirichlet : kEndsZeroFlux);
             HAL_TRY(Plan(xDim, r, ends, &pl));
@@ -1673,6 +1706,7 @@ namespace halcuda
 
         int RunTicks(int32_t ticks, double r, double decay, bool wrapX, bool wrapY, bool plain)
         {
+            HAL_TRY(Usable("ADI ticks"));
             if (ticks <= 0)
             {
                 return HAL_CUDA_OK;

@@ -1237,6 +1237,7 @@ extern "C" int hal_cuda_agents_profile(hal_cuda_agents *h, int32_t iters, double
 // last call's contents; the cell counts, the only part that must start at
 // zero, are cleared on the caller's stream at the start of each call.
 // ---------------------------------------------------------------------------
+#include <cuda.h>
 #include <mutex>
 
 namespace
@@ -1269,9 +1270,51 @@ namespace
     constexpr int kNoAllocMaxDevices = 64;
     std::mutex gNoAllocMutex;
     unsigned char *gNoAllocAddr[kNoAllocMaxDevices] = {};
+    // The CUDA context each cached address belongs to (its unique id,
+    // cuCtxGetId).  After cudaDeviceReset the runtime creates a new primary
+    // context, loads this module again and the array may sit elsewhere; a
+    // changed id makes the next call look the address up again.
+    unsigned long long gNoAllocCtx[kNoAllocMaxDevices] = {};
 
-    // Device address of gNoAllocScratch on the current device `dev`; resolved
-    // on the first call on that device.
+    using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+    using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
+
+    // Id of the calling thread's current context (0 when it cannot be read).
+    unsigned long long CurrentContextId()
+    {
+        static CtxGetCurrentFn s_getCurrent = nullptr;
+        static CtxGetIdFn s_getId = nullptr;
+        static bool s_resolved = false;
+        if (!s_resolved)
+        {
+            void *fn = nullptr;
+            cudaDriverEntryPointQueryResult q;
+            if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) ==
+                    cudaSuccess && q == cudaDriverEntryPointSuccess)
+            {
+                s_getCurrent = reinterpret_cast<CtxGetCurrentFn>(fn);
+            }
+            fn = nullptr;
+            if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+                q == cudaDriverEntryPointSuccess)
+            {
+                s_getId = reinterpret_cast<CtxGetIdFn>(fn);
+            }
+            s_resolved = true;
+        }
+        CUcontext ctx = nullptr;
+        unsigned long long id = 0;
+        if (s_getCurrent == nullptr || s_getId == nullptr || s_getCurrent(&ctx) != CUDA_SUCCESS || ctx == nullptr ||
+            s_getId(ctx, &id) != CUDA_SUCCESS)
+        {
+            return 0;
+        }
+        return id;
+    }
+
+    // Device address of gNoAllocScratch on the current device `dev`; looked
+    // up on the first call on that device, and again whenever the device's
+    // context has changed since (a cudaDeviceReset in between).
     int NoAllocScratch(int dev, unsigned char **out)
     {
         if (dev < 0 || dev >= kNoAllocMaxDevices)
@@ -1280,12 +1323,16 @@ namespace
             return HAL_CUDA_EDEVICE;
         }
         std::lock_guard<std::mutex> lock(gNoAllocMutex);
-        if (gNoAllocAddr[dev] == nullptr)
+        // an id of 0 (no context yet, or the driver cannot say) never
+        // matches, so the address is looked up then
+        void *p = nullptr;
+        const unsigned long long ctx = CurrentContextId();
+        if (gNoAllocAddr[dev] == nullptr || ctx == 0 || ctx != gNoAllocCtx[dev])
         {
-            void *p = nullptr;
             HAL_TRY(halcuda::CudaStatus(cudaGetSymbolAddress(&p, gNoAllocScratch),
                                         "cudaGetSymbolAddress(no-alloc scratch)"));
             gNoAllocAddr[dev] = static_cast<unsigned char *>(p);
+            gNoAllocCtx[dev] = CurrentContextId();
         }
         *out = gNoAllocAddr[dev];
         return HAL_CUDA_OK;

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "hal_cuda.h"
+#include "hal_cuda_measure.h"
 
 namespace halcuda
 {

@@ -725,6 +725,7 @@ namespace halcuda
         DevBuf<float> combS;
         bool combDirty = true;
         DevBuf<int32_t> blockErr;
+        bool stopped = false;  // a two-tick launch gave up waiting: no further ticks
 
         DevBuf<double> f64, d64, g64;
         DevBuf<double> a64, b64;  // per-cell rates or velocities of the FP64 stencil calls
@@ -896,6 +897,12 @@ namespace halcuda
         // Enqueues `ticks` ticks from field[cur], replayed from a graph.
         int RunTicks(int32_t ticks, double r, double decay, bool wrapX, bool wrapY, bool extras)
         {
+            if (stopped)
+            {
+                SetError("hal_cuda_diffusion_run_ticks: the handle stopped after a two-tick launch gave up waiting "
+                         "for its tile; the field is undefined: destroy the handle and create a new one");
+                return HAL_CUDA_ETIMEOUT;
+            }
             if (ticks <= 0)
             {
                 return HAL_CUDA_OK;
@@ -1270,6 +1277,9 @@ extern "C" int hal_cuda_diffusion_get_field(hal_cuda_diffusion *h, float *field,
                                     "cudaMemcpy(err)"));
         if (err != 0)
         {
+            // the field is undefined from here on, and every later tick of
+            // this handle is refused
+            h->stopped = true;
             halcuda::SetError("hal_cuda_diffusion_get_field: a two-tick launch gave up waiting for its tile");
             return HAL_CUDA_ETIMEOUT;
         }

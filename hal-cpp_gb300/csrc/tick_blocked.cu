@@ -46,6 +46,28 @@ namespace halcuda
             return static_cast<uint32_t>(__cvta_generic_to_shared(p));
         }
 
+        // Waits for phase 0 of the mbarrier at shared address bar for at most
+        // limitNs of %globaltimer; returns whether the phase completed.
+        __device__ __forceinline__ bool MbarWaitBounded(uint32_t bar, unsigned long long limitNs)
+        {
+            const unsigned long long t0 = GlobalTimerNs();
+            uint32_t done = 0;
+            while (!done)
+            {
+                asm volatile(
+                    "{ .reg .pred ok; mbarrier.try_wait.parity.shared::cta.b64 ok, [%1], 0, %2; selp.u32 %0, 1, 0, "
+                    "ok; }"
+                    : "=r"(done)
+                    : "r"(bar), "r"(1000000u)
+                    : "memory");
+                if (!done && GlobalTimerNs() - t0 > limitNs)
+                {
+                    return false;
+                }
+            }
+            return true;
+        }
+
         // Grid coordinate of an extended coordinate on one axis: itself on
         // the grid, wrapped on a periodic axis, else -1 (off the grid).
         __device__ __forceinline__ int32_t OnGrid(int32_t v, int32_t dim, bool wrap)
@@ -125,23 +147,13 @@ namespace halcuda
                     : "memory");
             }
             __syncthreads();  // mbarrier initialised before anyone waits on it
+            // bounded wait for the tile; one that gives up records the
+            // failure and waits once more (bounded again), so that the copy
+            // is not still writing into shared memory when the CTA exits
+            if (!MbarWaitBounded(bar, kWaitLimitNs))
             {
-                const unsigned long long t0 = GlobalTimerNs();
-                uint32_t done = 0;
-                while (!done)
-                {
-                    asm volatile(
-                        "{ .reg .pred ok; mbarrier.try_wait.parity.shared::cta.b64 ok, [%1], 0, %2; selp.u32 %0, 1, 0, "
-                        "ok; }"
-                        : "=r"(done)
-                        : "r"(bar), "r"(1000000u)
-                        : "memory");
-                    if (!done && GlobalTimerNs() - t0 > kWaitLimitNs)
-                    {
-                        s_fail = 1;
-                        break;
-                    }
-                }
+                s_fail = 1;
+                MbarWaitBounded(bar, kWaitLimitNs);
             }
             __syncthreads();
             if (s_fail)

@@ -77,6 +77,9 @@ namespace halcuda
         int32_t nTilesX = 0, nTilesY = 0;
         size_t smemX = 0, smemY = 0;
         DevBuf<int32_t> err;
+        // set once a bounded device wait has given up: the wells' fields are
+        // undefined from then on, so the handle takes no further ticks
+        bool stopped = false;
         // Lines per sweep tile are capped at rCap, chosen by the autotuner
         // (Autotune) the first time the wells tick.
         int32_t rCap = kSweepTileMaxR;
@@ -623,6 +626,12 @@ namespace halcuda
 
         int RunTicks(int32_t ticks, double R, double k)
         {
+            if (stopped)
+            {
+                SetError("hal_cuda_wells_run_ticks: the handle stopped after a sweep gave up waiting for its staged "
+                         "lines; the fields are undefined: destroy the handle and create a new one");
+                return HAL_CUDA_ETIMEOUT;
+            }
             if (!tuned)
             {
                 HAL_TRY(Autotune());
@@ -676,6 +685,7 @@ namespace halcuda
             if (h != 0)
             {
                 cudaMemsetAsync(err.p, 0, sizeof(int32_t), stream.Get());
+                stopped = true;
                 SetError(h == 2 ? "%s: the sweep's shared-memory buffer was not 1024-byte aligned"
                                 : "%s: a staged copy did not complete within its wait limit",
                          who);

@@ -78,17 +78,6 @@ const char *hal_cuda_last_error(void);
 int hal_cuda_device_count(int32_t *count);
 int hal_cuda_set_device(int32_t device);
 
-/* Number of kernel launches this library has issued in this process (all
- * handles).  Used by benchmarks to report their launch counts. */
-int64_t hal_cuda_launch_count(void);
-
-/* Measured FP64 add issue rate of the current device (operations per second,
- * best of three timed launches of independent add chains on every SM).  The
- * FP64 stencils (hal_cuda_diffuse*, hal_cuda_advect*) are bound by this rate
- * on GB300, whose FP64 pipe is a small fraction of its FP32 one; benchmarks
- * use it as their roofline. */
-int hal_cuda_fp64_issue_rate(double *opsPerSecond);
-
 /* ---- explicit diffusion: IDiffusionBackend2D ---------------------------- */
 
 /* GpuDiffusionBackend2D(ComputeContext&, xDim, yDim)
@@ -142,15 +131,6 @@ int hal_cuda_advect_var_bc(hal_cuda_diffusion *h, const double *field, double *d
                            const double *xVels, const double *yVels, int32_t wrapX, int32_t wrapY,
                            const double *ghost, const double *ghostXVel, const double *ghostYVel);
 
-/* Profiling of the FP64 stencils above (zero-flux forms): average device time
- * (ms) of one launch on the arrays the last call of that kind uploaded, over
- * `iters` individually timed launches.  Deltas accumulate on the device. */
-#define HAL_CUDA_STENCIL_DIFFUSE_VAR 0
-#define HAL_CUDA_STENCIL_ADVECT 1
-#define HAL_CUDA_STENCIL_ADVECT_VAR 2
-int hal_cuda_stencil64_profile(hal_cuda_diffusion *h, int32_t kind, int32_t iters, double xVel,
-                               double yVel, int32_t wrapX, int32_t wrapY, float *ms);
-
 /* Resident field (DiffusionKernel2D::UploadField / RunSteps,
  * src/Gpu/DiffusionKernel2D.cpp:173-304).  len must be xDim*yDim. */
 int hal_cuda_diffusion_set_field(hal_cuda_diffusion *h, const float *field, int64_t len);
@@ -197,11 +177,6 @@ int hal_cuda_diffusion_run_ticks(hal_cuda_diffusion *h, int32_t ticks, double di
  * steps with commit, download.  field is a host array of len floats. */
 int hal_cuda_diffusion_run_steps(hal_cuda_diffusion *h, float *field, int64_t len,
                                  int32_t steps, double diffRate, int32_t wrapX, int32_t wrapY);
-
-/* Profiling: average device time (ms) of one fused-tick launch over `iters`
- * individually timed ticks (CUDA events, no graph).  The field advances. */
-int hal_cuda_diffusion_profile(hal_cuda_diffusion *h, int32_t iters, double diffRate,
-                               double decay, int32_t wrapX, int32_t wrapY, float *ms);
 
 int hal_cuda_diffusion_sync(hal_cuda_diffusion *h);
 
@@ -262,22 +237,6 @@ int hal_cuda_adi_run_ticks_host(hal_cuda_adi *h, float *field, const float *src,
                                 int32_t ticks, double diffRate, double decay, int32_t wrapX,
                                 int32_t wrapY);
 
-/* Steady-state profiling: for each sweep, a CUDA graph of `iters`
- * back-to-back launches on the same inputs (the x-sweep rewrites w, the
- * y-sweep the other parity's field), replayed once to warm up and once timed;
- * ms[0] / ms[1] = the mean device time of one x- / y-sweep launch.  The
- * resident field does not change. */
-int hal_cuda_adi_profile_graph(hal_cuda_adi *h, int32_t iters, double diffRate, double decay,
-                               int32_t wrapX, int32_t wrapY, float *ms);
-
-/* Profiling: runs `iters` ticks with each sweep launched on its own between
- * CUDA events on the handle's stream (no graph), and returns the average
- * device time of one launch of each kernel: ms[0] = x-sweep
- * (AdiSweep<kSweepW>), ms[1] = y-sweep with commit (AdiSweep<kSweepTick>).
- * The resident field advances by `iters` ticks. */
-int hal_cuda_adi_profile(hal_cuda_adi *h, int32_t iters, double diffRate, double decay,
-                         int32_t wrapX, int32_t wrapY, float *ms);
-
 int hal_cuda_adi_sync(hal_cuda_adi *h);
 void *hal_cuda_adi_stream(hal_cuda_adi *h);
 int hal_cuda_adi_set_stream(hal_cuda_adi *h, void *stream);
@@ -337,13 +296,6 @@ int hal_cuda_agents_step(hal_cuda_agents *h, int32_t ticks, double interactionRa
  * CpuAgentForceBackend2D (src/Agents/CpuAgentForceBackend2D.cpp:85-109).
  * Either pointer may be NULL. */
 int hal_cuda_agents_get_bins(hal_cuda_agents *h, int32_t *cellOffsets, int32_t *bucketAgents);
-
-/* Profiling: `iters` resident dispatches with each kernel launch between CUDA
- * events; ms[0..5] = average device time of one launch of: bin count
- * (including the counts memset), scan (three launches together), unstable
- * scatter, stabilize, forces, and the whole dispatch. */
-int hal_cuda_agents_profile(hal_cuda_agents *h, int32_t iters, double interactionRad,
-                            double springConstant, int32_t wrapX, int32_t wrapY, float *ms);
 
 int hal_cuda_agents_sync(hal_cuda_agents *h);
 void *hal_cuda_agents_stream(hal_cuda_agents *h);
@@ -446,11 +398,6 @@ int hal_cuda_wells_get_agents(hal_cuda_wells *h, float *positions, float *veloci
  * in well order (len = 2*sum(counts) floats). */
 int hal_cuda_wells_get_forces(hal_cuda_wells *h, float *velocityDeltas, int64_t len);
 
-/* Profiling: average device ms over `iters` ticks launched one kernel at a
- * time: ms[0] explicit tiles, ms[1] ADI x-sweep tiles, ms[2] ADI y-sweep
- * tiles, ms[3] agent pass, ms[4] whole tick.  Fields advance. */
-int hal_cuda_wells_profile(hal_cuda_wells *h, int32_t iters, double interactionRad,
-                           double springConstant, float *ms);
 /* Autotuner of the ADI sweep tiles: times the batched x- and y-sweeps of
  * every ADI well with the lines per tile capped at 128, 64, 32, 16 and 8, on
  * the wells' own fields (their state does not change), and keeps the
@@ -529,7 +476,10 @@ int hal_cuda_adjoint_times(hal_cuda_adjoint *h, float *msForward, float *msGradi
  *
  * The first call on each device looks up the array's device address
  * (cudaGetSymbolAddress, with that device current); make that first call
- * before any stream capture.  Every call on a device shares the one array and
+ * before any stream capture.  The address is kept with the id of the CUDA
+ * context it was looked up in, and looked up again by the first call after the
+ * context changed (a cudaDeviceReset in between), which again must not be made
+ * during a stream capture.  Every call on a device shares the one array and
  * it keeps the last call's contents: calls that overlap on the GPU (different
  * streams, or host threads racing on one device) race on it and give wrong
  * results.  Calls ordered on one stream are safe. */

@@ -23,7 +23,23 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libhal_ref.so")
-REF_TREE = "/root/reference"
+
+
+def _reference_tree() -> str:
+    """Where the reference HAL-CPP tree is: $HAL_REFERENCE_TREE, else the
+    default that oracle/Makefile states (its HAL_REFERENCE_TREE line)."""
+    env = os.environ.get("HAL_REFERENCE_TREE")
+    if env:
+        return env
+    with open(os.path.join(HERE, "Makefile")) as fh:
+        for line in fh:
+            parts = line.split("?=")
+            if len(parts) == 2 and parts[0].strip() == "HAL_REFERENCE_TREE":
+                return parts[1].strip()
+    return ""
+
+
+REF_TREE = _reference_tree()
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int32)
