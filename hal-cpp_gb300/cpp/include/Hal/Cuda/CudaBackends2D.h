@@ -182,6 +182,26 @@ namespace Hal::Cuda
                               bool                       wrapX,
                               bool                       wrapY) override;
 
+        // SphericalAgent2D::SumForces (include/Hal/Agents/SphericalAgent2D.h:
+        // 74-102) of every agent, FP64: velocities (2n, the agents' xVel/yVel;
+        // empty for zeros) are updated in place with each neighbour's
+        // -(disp/d) * law(touchDist), and forceSums (resized to n) receives
+        // the sums of positive forces SumForces returns.  `order` is
+        // HAL_CUDA_ORDER_AGENTGRID (an AgentGrid2D filled in index order:
+        // bit-identical for the linear and clamped laws) or
+        // HAL_CUDA_ORDER_BACKEND.  The law replaces the overlap functor.
+        void SumForces(const std::vector<double> &positions,
+                       const std::vector<double> &radii,
+                       std::vector<double>       &velocities,
+                       std::vector<double>       &forceSums,
+                       double                     interactionRad,
+                       const hal_cuda_force_law  &law,
+                       int32_t                    xDim,
+                       int32_t                    yDim,
+                       bool                       wrapX,
+                       bool                       wrapY,
+                       int32_t                    order = HAL_CUDA_ORDER_AGENTGRID);
+
         // AgentForceKernel2D's resident form (FP32): upload, dispatch, download.
         void Upload(const std::vector<float> &positions, const std::vector<float> &radii);
         void Dispatch(double interactionRad, double springConstant, bool wrapX, bool wrapY);
@@ -196,6 +216,14 @@ namespace Hal::Cuda
         void SetVelocities(const std::vector<float> &velocities);
         void Step(int32_t ticks, double interactionRad, double springConstant, bool wrapX, bool wrapY,
                   double friction, double maxVel = -1.0);
+        // The resident dispatch and step with a force law in place of the
+        // linear spring; with withSums the kernel also keeps each agent's sum
+        // of positive forces (FP32), which GetForceSums downloads, e.g. to gate
+        // division as OffLatticeExample.cpp:156-165 does.
+        void DispatchLaw(double interactionRad, const hal_cuda_force_law &law, bool withSums, bool wrapX, bool wrapY);
+        void StepLaw(int32_t ticks, double interactionRad, const hal_cuda_force_law &law, bool withSums, bool wrapX,
+                     bool wrapY, double friction, double maxVel = -1.0);
+        void GetForceSums(std::vector<float> &forceSums);
         void GetState(std::vector<float> &positions, std::vector<float> &velocities);
 
         hal_cuda_agents *Handle() const { return m_pHandle; }

@@ -309,6 +309,51 @@ namespace Hal::Cuda
         m_count = static_cast<int32_t>(radii.size());
     }
 
+    void CudaAgentForceBackend2D::SumForces(const std::vector<double> &positions, const std::vector<double> &radii,
+                                            std::vector<double> &velocities, std::vector<double> &forceSums,
+                                            double interactionRad, const hal_cuda_force_law &law, int32_t xDim,
+                                            int32_t yDim, bool wrapX, bool wrapY, int32_t order)
+    {
+        if (positions.size() != 2 * radii.size())
+        {
+            Check(HAL_CUDA_EINVAL, "CudaAgentForceBackend2D::SumForces: positions must hold two values per radius");
+        }
+        if (!velocities.empty() && velocities.size() != positions.size())
+        {
+            Check(HAL_CUDA_EINVAL, "CudaAgentForceBackend2D::SumForces: velocities must hold two values per agent");
+        }
+        const bool haveVel = !velocities.empty();
+        velocities.resize(positions.size());
+        forceSums.resize(radii.size());
+        Check(hal_cuda_sum_forces(m_pHandle, positions.data(), radii.data(), static_cast<int64_t>(radii.size()),
+                                  haveVel ? velocities.data() : nullptr, velocities.data(), forceSums.data(),
+                                  interactionRad, &law, order, xDim, yDim, wrapX, wrapY),
+              "CudaAgentForceBackend2D::SumForces");
+        m_count = static_cast<int32_t>(radii.size());
+    }
+
+    void CudaAgentForceBackend2D::DispatchLaw(double interactionRad, const hal_cuda_force_law &law, bool withSums,
+                                              bool wrapX, bool wrapY)
+    {
+        Check(hal_cuda_agents_dispatch_law(m_pHandle, interactionRad, &law, withSums, wrapX, wrapY),
+              "CudaAgentForceBackend2D::DispatchLaw");
+    }
+
+    void CudaAgentForceBackend2D::StepLaw(int32_t ticks, double interactionRad, const hal_cuda_force_law &law,
+                                          bool withSums, bool wrapX, bool wrapY, double friction, double maxVel)
+    {
+        Check(hal_cuda_agents_step_law(m_pHandle, ticks, interactionRad, &law, withSums, wrapX, wrapY, friction,
+                                       maxVel),
+              "CudaAgentForceBackend2D::StepLaw");
+    }
+
+    void CudaAgentForceBackend2D::GetForceSums(std::vector<float> &forceSums)
+    {
+        forceSums.resize(static_cast<size_t>(m_count));
+        Check(hal_cuda_agents_get_force_sums(m_pHandle, forceSums.data(), m_count),
+              "CudaAgentForceBackend2D::GetForceSums");
+    }
+
     void CudaAgentForceBackend2D::Upload(const std::vector<float> &positions, const std::vector<float> &radii)
     {
         if (positions.size() != 2 * radii.size())

@@ -218,6 +218,41 @@ namespace
         return err <= 1e-12 ? "" : Fmt("all-pairs difference %.3e > 1e-12", err);
     }
 
+    // The off-lattice example's force pass (examples/OffLatticeExample.cpp:
+    // 145-165): SumForces with the clamped Hooke law from the cells' current
+    // velocities, returning each cell's force sum; bit-identical to the
+    // restatement of SumForces on the agent grid.
+    std::string ClampedSumForces(Hal::Cuda::CudaAgentForceBackend2D &backend)
+    {
+        const int32_t dim = 64, n = 4000;
+        oracle_rand rng;
+        oracle_rand_init(&rng, 11);
+        std::vector<double> pos(2 * n), rad(n, 0.25), vel(2 * n);
+        for (int32_t i = 0; i < n; i++)
+        {
+            pos[2 * i] = 24.0 + oracle_rand_gaussian(&rng, 0.0, 4.0);
+            pos[2 * i + 1] = 24.0 + oracle_rand_gaussian(&rng, 0.0, 4.0);
+            vel[2 * i] = oracle_rand_double(&rng) - 0.5;
+            vel[2 * i + 1] = oracle_rand_double(&rng) - 0.5;
+        }
+        const hal_cuda_force_law law = {HAL_CUDA_FORCE_LINEAR_CLAMPED, 0.25, 1.0};
+        std::vector<double> v = vel, sums;
+        backend.SumForces(pos, rad, v, sums, 0.5, law, dim, dim, false, false);
+        std::vector<double> expV(2 * n), expS(n);
+        oracle_sum_forces(pos.data(), rad.data(), n, vel.data(), expV.data(), expS.data(), 0.5,
+                          HAL_CUDA_FORCE_LINEAR_CLAMPED, 0.25, 1.0, HAL_CUDA_ORDER_AGENTGRID, dim, dim, 0, 0);
+        if (v != expV || sums != expS)
+        {
+            return Fmt("SumForces differs from the restatement: %.3e", MaxAbsDiff(v, expV) + MaxAbsDiff(sums, expS));
+        }
+        int32_t positive = 0;
+        for (double s : sums)
+        {
+            positive += (s > 0.0) ? 1 : 0;
+        }
+        return positive > n / 4 ? "" : Fmt("only %.0f cells feel a force", static_cast<double>(positive));
+    }
+
     // Bins and FP64 forces equal the CPU backend bit for bit on float32
     // positions.
     std::string ForcesMatchCpu(Hal::Cuda::CudaAgentForceBackend2D &backend)
@@ -593,6 +628,7 @@ int main()
     Run("forces_match_all_pairs", [&] { return BruteForceForces(agents16); });
     Run("forces_and_bins_match_cpu", [&] { return ForcesMatchCpu(agents64); });
     Run("coincident_agents", [&] { return CoincidentAgents(agents8); });
+    Run("clamped_sum_forces_bit_exact", [&] { return ClampedSumForces(agents64); });
     Run("size_mismatch_throws", [&] { return SizeMismatches(diffEig, adiEig, agents16); });
     Run("resident_ticks_match_cpu", [&] { return ResidentTicks(diffTick, adiTick); });
     Run("variable_rate_and_advection_bit_exact", [&] { return VariableStencils(diffTick); });

@@ -388,14 +388,84 @@ namespace halcuda
             return d;
         }
 
-        // Pass 4 (CpuAgentForceBackend2D.cpp:112-175) for the agent in sorted
-        // slot `slot` (agent i); offsets are the cell offsets of its grid.
-        // Returns the agent's velocity delta, the sum over its neighbours.
+        // The agent grid's displacement GridGeometry2D::DispX/DispY
+        // (src/Grids/GridGeometry2D.cpp:132-150) of p2 seen from p1: on a
+        // wrapped axis DispWrap (src/MathUtil.cpp:363-379) shifts one end by
+        // the axis length before subtracting, so it rounds differently from
+        // AgentForceDisp.
         template <typename T>
-        __device__ __forceinline__ V2<T> ForceSlot(const int32_t slot, const int32_t *__restrict__ offsets,
-                                                   const V2<T> *__restrict__ sPos, const T *__restrict__ sRad,
-                                                   double interactionRad, T R, T k, int32_t xDim, int32_t yDim,
-                                                   int32_t wrapX, int32_t wrapY)
+        __device__ __forceinline__ T DispGrid(T p1, T p2, T dimF, bool wrap)
+        {
+            if (wrap && Abs(Sub(p1, p2)) > Mul(dimF, T(0.5)))
+            {
+                return (p1 > p2) ? Sub(Add(p2, dimF), p1) : Sub(p2, Add(p1, dimF));
+            }
+            return Sub(p2, p1);
+        }
+
+        // Overlap force laws: the overlapFun(touchDist, other) of
+        // SphericalAgent2D::SumForces (include/Hal/Agents/SphericalAgent2D.h:
+        // 74-102) as a law kind and its parameters.
+        constexpr int kLawLinear = HAL_CUDA_FORCE_LINEAR;
+        constexpr int kLawClamped = HAL_CUDA_FORCE_LINEAR_CLAMPED;
+        constexpr int kLawPower = HAL_CUDA_FORCE_POWER;
+
+        template <typename T>
+        struct LawParams
+        {
+            T scale;
+            T exponent;
+        };
+
+        __device__ __forceinline__ double Pow(double a, double b) { return pow(a, b); }
+        __device__ __forceinline__ float Pow(float a, float b) { return powf(a, b); }
+
+        template <int LAW, typename T>
+        __device__ __forceinline__ T OverlapForce(T touch, const LawParams<T> &lp)
+        {
+            if constexpr (LAW == kLawLinear)
+            {
+                // springConstant * touchDist (CpuAgentForceBackend2D.cpp:165)
+                return Mul(lp.scale, touch);
+            }
+            else if constexpr (LAW == kLawClamped)
+            {
+                // no force unless overlapping, then Hooke's law
+                // (examples/OffLatticeExample.cpp:147-154)
+                return (touch < T(0)) ? T(0) : Mul(lp.scale, touch);
+            }
+            else
+            {
+                // pow(scale * touchDist, exponent) (examples/Chemotaxis.cpp:128-130)
+                return Pow(Mul(lp.scale, touch), lp.exponent);
+            }
+        }
+
+        // One agent's force sum: its velocity after the neighbours' forces
+        // (or the deltas, from zero) and the sum of its positive forces.
+        template <typename T>
+        struct ForceAcc
+        {
+            V2<T> v;
+            T sum;
+        };
+
+        // Pass 4 (CpuAgentForceBackend2D.cpp:112-175) for the agent in sorted
+        // slot `slot`; offsets are the cell offsets of its grid.  Starting
+        // from v0, each neighbour j within range subtracts (disp/d)*force,
+        // force = LAW(touchDist); with SUM the positive forces are summed as
+        // SumForces returns them.  GRID visits each cell's agents in
+        // descending index order with the agent grid's displacement, which is
+        // SphericalAgent2D::SumForces on an AgentGrid2D whose agents were
+        // created in index order (each square's list is newest first,
+        // AgentPT2D.h:200-241); otherwise the order is the CPU backend's
+        // (ascending index within a cell).
+        template <typename T, int LAW, bool SUM, bool GRID>
+        __device__ __forceinline__ ForceAcc<T> ForceSlotLaw(const int32_t slot, const int32_t *__restrict__ offsets,
+                                                            const V2<T> *__restrict__ sPos,
+                                                            const T *__restrict__ sRad, double interactionRad, T R,
+                                                            const LawParams<T> lp, int32_t xDim, int32_t yDim,
+                                                            int32_t wrapX, int32_t wrapY, V2<T> v0)
         {
             const V2<T> pf = sPos[slot];
             const T px = pf.x;
@@ -419,7 +489,8 @@ namespace halcuda
             }
             const T xDimF = static_cast<T>(xDim);
             const T yDimF = static_cast<T>(yDim);
-            T vx = T(0), vy = T(0);
+            T vx = v0.x, vy = v0.y;
+            T sum = T(0);
             // one candidate slot q of the window, in the CPU's visiting order
             auto visit = [&](int32_t q) {
                 if (q == slot)
@@ -427,8 +498,17 @@ namespace halcuda
                     return;
                 }
                 const V2<T> pj = sPos[q];
-                const T xComp = Disp(px, pj.x, xDimF, wrapX != 0);
-                const T yComp = Disp(py, pj.y, yDimF, wrapY != 0);
+                T xComp, yComp;
+                if constexpr (GRID)
+                {
+                    xComp = DispGrid(px, pj.x, xDimF, wrapX != 0);
+                    yComp = DispGrid(py, pj.y, yDimF, wrapY != 0);
+                }
+                else
+                {
+                    xComp = Disp(px, pj.x, xDimF, wrapX != 0);
+                    yComp = Disp(py, pj.y, yDimF, wrapY != 0);
+                }
                 if constexpr (std::is_same<T, double>::value)
                 {
                     // IEEE operations in the CPU's order: bit-exact
@@ -436,9 +516,16 @@ namespace halcuda
                     if ((dist < R) && (dist > T(0)))
                     {
                         const T touchDist = Sub(Add(rad, sRad[q]), dist);
-                        const T force = Mul(k, touchDist);
+                        const T force = OverlapForce<LAW>(touchDist, lp);
                         vx = Sub(vx, Mul(Div(xComp, dist), force));
                         vy = Sub(vy, Mul(Div(yComp, dist), force));
+                        if constexpr (SUM)
+                        {
+                            if (force > T(0))
+                            {
+                                sum = Add(sum, Abs(force));
+                            }
+                        }
                     }
                 }
                 else
@@ -450,12 +537,57 @@ namespace halcuda
                     const T dist = d2 * inv;
                     if ((dist < R) && (dist > T(0)))
                     {
-                        const T scale = inv * (k * ((rad + sRad[q]) - dist));
+                        const T force = OverlapForce<LAW>((rad + sRad[q]) - dist, lp);
+                        const T scale = inv * force;
                         vx -= xComp * scale;
                         vy -= yComp * scale;
+                        if constexpr (SUM)
+                        {
+                            if (force > T(0))
+                            {
+                                sum += force;
+                            }
+                        }
                     }
                 }
             };
+            auto result = [&]() {
+                ForceAcc<T> acc;
+                acc.v.x = vx;
+                acc.v.y = vy;
+                acc.sum = sum;
+                return acc;
+            };
+            if constexpr (GRID)
+            {
+                // cell by cell, each cell's slots from last to first
+                for (int32_t xSq = xStart; xSq < xEnd; xSq++)
+                {
+                    int32_t retX = xSq;
+                    if (retX < 0 || retX >= xDim)
+                    {
+                        retX %= xDim;  // only reached on a wrapped axis (clamped otherwise)
+                        retX = (retX < 0) ? retX + xDim : retX;
+                    }
+                    for (int32_t ySq = yStart; ySq < yEnd; ySq++)
+                    {
+                        int32_t retY = ySq;
+                        if (retY < 0 || retY >= yDim)
+                        {
+                            retY %= yDim;
+                            retY = (retY < 0) ? retY + yDim : retY;
+                        }
+                        const int32_t cell = retX * yDim + retY;
+                        const int32_t s = __ldg(offsets + cell);
+                        const int32_t e = __ldg(offsets + cell + 1);
+                        for (int32_t q = e - 1; q >= s; q--)
+                        {
+                            visit(q);
+                        }
+                    }
+                }
+                return result();
+            }
             // Common case: a window of at most four rows whose y-range does
             // not wrap, so each row is one run of cells.  All rows' offset
             // pairs are loaded before the first candidate, which shortens the
@@ -490,10 +622,7 @@ namespace halcuda
                         visit(q);
                     }
                 }
-                V2<T> sum;
-                sum.x = vx;
-                sum.y = vy;
-                return sum;
+                return result();
             }
             for (int32_t xSq = xStart; xSq < xEnd; xSq++)
             {
@@ -532,10 +661,22 @@ namespace halcuda
                     }
                 }
             }
-            V2<T> sum;
-            sum.x = vx;
-            sum.y = vy;
-            return sum;
+            return result();
+        }
+
+        // The CPU backend's pass 4: linear law, velocity deltas from zero.
+        template <typename T>
+        __device__ __forceinline__ V2<T> ForceSlot(const int32_t slot, const int32_t *__restrict__ offsets,
+                                                   const V2<T> *__restrict__ sPos, const T *__restrict__ sRad,
+                                                   double interactionRad, T R, T k, int32_t xDim, int32_t yDim,
+                                                   int32_t wrapX, int32_t wrapY)
+        {
+            LawParams<T> lp;
+            lp.scale = k;
+            lp.exponent = T(1);
+            return ForceSlotLaw<T, kLawLinear, false, false>(slot, offsets, sPos, sRad, interactionRad, R, lp, xDim,
+                                                             yDim, wrapX, wrapY, Vec2<T>::Make(T(0), T(0)))
+                .v;
         }
 
         template <typename TV, typename TVec>
@@ -545,12 +686,15 @@ namespace halcuda
             vel[2 * static_cast<int64_t>(i) + 1] = static_cast<TV>(d.y);
         }
 
-        // Pass 4 over cell-sorted slots: one thread per slot.
-        template <typename T, typename TV>
+        // Pass 4 over cell-sorted slots: one thread per slot.  With velIn the
+        // sum starts from the agent's velocity (SumForces adds to xVel/yVel),
+        // otherwise from zero (the interface's velocity deltas); with SUM the
+        // agent's sum of positive forces goes to sums.
+        template <typename T, typename TV, int LAW = kLawLinear, bool SUM = false, bool GRID = false>
         __global__ void Forces(const int32_t *__restrict__ bucket, const int32_t *__restrict__ offsets,
                                const V2<T> *__restrict__ sPos, const T *__restrict__ sRad, int32_t n,
-                               double interactionRad, T R, T k, int32_t xDim, int32_t yDim, int32_t wrapX,
-                               int32_t wrapY, TV *__restrict__ vel)
+                               double interactionRad, T R, LawParams<T> lp, int32_t xDim, int32_t yDim,
+                               int32_t wrapX, int32_t wrapY, TV *vel, T *__restrict__ sums, const TV *velIn)
         {
             ChainEntry();
             const int32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
@@ -558,8 +702,20 @@ namespace halcuda
             {
                 return;
             }
-            StoreDelta(vel, bucket[slot],
-                       ForceSlot<T>(slot, offsets, sPos, sRad, interactionRad, R, k, xDim, yDim, wrapX, wrapY));
+            const int32_t i = bucket[slot];
+            V2<T> v0 = Vec2<T>::Make(T(0), T(0));
+            if (velIn != nullptr)
+            {
+                v0 = Vec2<T>::Make(static_cast<T>(velIn[2 * static_cast<int64_t>(i)]),
+                                   static_cast<T>(velIn[2 * static_cast<int64_t>(i) + 1]));
+            }
+            const ForceAcc<T> acc = ForceSlotLaw<T, LAW, SUM, GRID>(slot, offsets, sPos, sRad, interactionRad, R, lp,
+                                                                    xDim, yDim, wrapX, wrapY, v0);
+            StoreDelta(vel, i, acc.v);
+            if constexpr (SUM)
+            {
+                sums[i] = acc.sum;
+            }
         }
 
         // SphericalAgent2D's per-tick update after its forces
@@ -630,11 +786,12 @@ namespace halcuda
         // agent adds its delta to its velocity and moves.  Positions are read
         // from the cell-sorted copy, so writing the agent-order positions
         // here races with no other thread.
+        template <int LAW = kLawLinear, bool SUM = false>
         __global__ void ForcesMove(const int32_t *__restrict__ bucket, const int32_t *__restrict__ offsets,
                                    const float2 *__restrict__ sPos, const float *__restrict__ sRad, int32_t n,
-                                   double interactionRad, float R, float k, int32_t xDim, int32_t yDim,
+                                   double interactionRad, float R, LawParams<float> lp, int32_t xDim, int32_t yDim,
                                    MoveParams mp, float *__restrict__ deltas, float2 *__restrict__ pos,
-                                   float2 *__restrict__ velocity)
+                                   float2 *__restrict__ velocity, float *__restrict__ sums)
         {
             ChainEntry();
             const int32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
@@ -643,9 +800,14 @@ namespace halcuda
                 return;
             }
             const int32_t i = bucket[slot];
-            const V2<float> d = ForceSlot<float>(slot, offsets, sPos, sRad, interactionRad, R, k, xDim, yDim,
-                                                 mp.wrapX, mp.wrapY);
+            const ForceAcc<float> acc = ForceSlotLaw<float, LAW, SUM, false>(
+                slot, offsets, sPos, sRad, interactionRad, R, lp, xDim, yDim, mp.wrapX, mp.wrapY, make_float2(0.f, 0.f));
+            const V2<float> d = acc.v;
             StoreDelta(deltas, i, d);
+            if constexpr (SUM)
+            {
+                sums[i] = acc.sum;
+            }
             float2 p = sPos[slot];
             float2 v = velocity[i];
             v.x = __fadd_rn(v.x, d.x);
@@ -733,6 +895,24 @@ namespace halcuda
         }
     }
 
+    // A force law of the host API (hal_cuda_force_law) with the output and
+    // order options of one force pass.
+    struct ForceLawSpec
+    {
+        int kind = kLawLinear;
+        double scale = 0.0;
+        double exponent = 1.0;
+        bool sums = false;  // write each agent's sum of positive forces
+        bool grid = false;  // the agent grid's order and displacement (FP64)
+
+        static ForceLawSpec Linear(double k)
+        {
+            ForceLawSpec l;
+            l.scale = k;
+            return l;
+        }
+    };
+
     struct Agents
     {
         int32_t xDim = 0, yDim = 0, maxAgents = 0;
@@ -748,6 +928,9 @@ namespace halcuda
         DevBuf<float> sRad32;
         DevBuf<double> sRad64;
         DevBuf<int32_t> cellOf, arrival, counts, offsets, tileSums, bucketTmp, bucket;
+        DevBuf<float> sums32;    // per-agent sums of positive forces (FP32 path)
+        DevBuf<double> sums64;   // the same, FP64 path
+        bool sumsValid = false;  // sums32 holds the last dispatch's or step's sums
         int32_t nTiles = 0;
         bool countsDirty = true;  // counts not known to be zero (cleared by each scan)
 
@@ -851,20 +1034,65 @@ namespace halcuda
             return LaunchStatus("agent binning");
         }
 
+        // Pass 4 with force law `law`: velocity deltas (from zero, or from
+        // velIn) into vel, and with law.sums each agent's sum of positive
+        // forces into sums.  law.grid (FP64 only) selects the agent grid's
+        // visiting order and displacement.
         template <typename T, typename TV>
-        int Force(const T *sRad, double R, double k, bool wrapX, bool wrapY, TV *vel, cudaStream_t s)
+        int Force(const T *sRad, double R, const ForceLawSpec &law, bool wrapX, bool wrapY, TV *vel, T *sums,
+                  const TV *velIn, cudaStream_t s)
         {
             if (n == 0)
             {
                 return HAL_CUDA_OK;
             }
             const int T_ = 128;
-            unsigned blocks = static_cast<unsigned>((n + T_ - 1) / T_);
-            LaunchChained(Forces<T, TV>, blocks, T_, s, bucket.p, offsets.p, SortedPosBuf(T()), sRad, n, R,
-                          static_cast<T>(R), static_cast<T>(k), xDim, yDim, static_cast<int32_t>(wrapX),
-                          static_cast<int32_t>(wrapY), vel);
+            const unsigned blocks = static_cast<unsigned>((n + T_ - 1) / T_);
+            LawParams<T> lp;
+            lp.scale = static_cast<T>(law.scale);
+            lp.exponent = static_cast<T>(law.exponent);
+            auto go = [&](auto kernel) {
+                LaunchChained(kernel, blocks, T_, s, bucket.p, offsets.p, SortedPosBuf(T()), sRad, n, R,
+                              static_cast<T>(R), lp, xDim, yDim, static_cast<int32_t>(wrapX),
+                              static_cast<int32_t>(wrapY), vel, sums, velIn);
+            };
+            const bool grid = std::is_same<T, double>::value && law.grid;
+            switch (law.kind * 4 + (law.sums ? 2 : 0) + (grid ? 1 : 0))
+            {
+            case 0: go(Forces<T, TV, kLawLinear, false, false>); break;
+            case 1: go(Forces<T, TV, kLawLinear, false, true>); break;
+            case 2: go(Forces<T, TV, kLawLinear, true, false>); break;
+            case 3: go(Forces<T, TV, kLawLinear, true, true>); break;
+            case 4: go(Forces<T, TV, kLawClamped, false, false>); break;
+            case 5: go(Forces<T, TV, kLawClamped, false, true>); break;
+            case 6: go(Forces<T, TV, kLawClamped, true, false>); break;
+            case 7: go(Forces<T, TV, kLawClamped, true, true>); break;
+            case 8: go(Forces<T, TV, kLawPower, false, false>); break;
+            case 9: go(Forces<T, TV, kLawPower, false, true>); break;
+            case 10: go(Forces<T, TV, kLawPower, true, false>); break;
+            default: go(Forces<T, TV, kLawPower, true, true>); break;
+            }
             CountLaunch();
             return LaunchStatus("agent forces");
+        }
+
+        // The interface's pass 4: linear law, deltas from zero.
+        template <typename T, typename TV>
+        int Force(const T *sRad, double R, double k, bool wrapX, bool wrapY, TV *vel, cudaStream_t s)
+        {
+            return Force<T, TV>(sRad, R, ForceLawSpec::Linear(k), wrapX, wrapY, vel, static_cast<T *>(nullptr),
+                                static_cast<const TV *>(nullptr), s);
+        }
+
+        // Buffer of the FP32 force sums, allocated on first use.
+        int SumsBuf32(float **out)
+        {
+            if (sums32.p == nullptr)
+            {
+                HAL_TRY(sums32.Alloc(static_cast<size_t>(maxAgents > 0 ? maxAgents : 1), "cudaMalloc(force sums)"));
+            }
+            *out = sums32.p;
+            return HAL_CUDA_OK;
         }
     };
 
@@ -874,7 +1102,8 @@ namespace halcuda
 namespace
 {
     // One resident tick of the agents: bin, then forces with the move fused.
-    int StepOnce(halcuda::Agents &a, double R, double k, const halcuda::MoveParams &mp, cudaStream_t s)
+    int StepOnce(halcuda::Agents &a, double R, const halcuda::ForceLawSpec &law, const halcuda::MoveParams &mp,
+                 cudaStream_t s)
     {
         using namespace halcuda;
         HAL_TRY((a.Bin<float, float>(a.pos32.p, a.rad32.p, a.sRad32.p, s)));
@@ -882,11 +1111,30 @@ namespace
         {
             return HAL_CUDA_OK;
         }
+        float *sums = nullptr;
+        if (law.sums)
+        {
+            HAL_TRY(a.SumsBuf32(&sums));
+        }
         const int T = 128;
         const unsigned blocks = static_cast<unsigned>((a.n + T - 1) / T);
-        LaunchChained(ForcesMove, blocks, T, s, a.bucket.p, a.offsets.p, a.sPos.p, a.sRad32.p, a.n, R,
-                      static_cast<float>(R), static_cast<float>(k), a.xDim, a.yDim, mp, a.vel32.p,
-                      reinterpret_cast<float2 *>(a.pos32.p), a.velState.p);
+        LawParams<float> lp;
+        lp.scale = static_cast<float>(law.scale);
+        lp.exponent = static_cast<float>(law.exponent);
+        auto go = [&](auto kernel) {
+            LaunchChained(kernel, blocks, T, s, a.bucket.p, a.offsets.p, a.sPos.p, a.sRad32.p, a.n, R,
+                          static_cast<float>(R), lp, a.xDim, a.yDim, mp, a.vel32.p,
+                          reinterpret_cast<float2 *>(a.pos32.p), a.velState.p, sums);
+        };
+        switch (law.kind * 2 + (law.sums ? 1 : 0))
+        {
+        case 0: go(ForcesMove<kLawLinear, false>); break;
+        case 1: go(ForcesMove<kLawLinear, true>); break;
+        case 2: go(ForcesMove<kLawClamped, false>); break;
+        case 3: go(ForcesMove<kLawClamped, true>); break;
+        case 4: go(ForcesMove<kLawPower, false>); break;
+        default: go(ForcesMove<kLawPower, true>); break;
+        }
         CountLaunch();
         return LaunchStatus("agent forces and move");
     }
@@ -955,6 +1203,42 @@ namespace
     }
 }
 
+namespace
+{
+    // A hal_cuda_force_law checked and turned into a spec; sums as given.
+    int LawFrom(const hal_cuda_force_law *law, bool sums, const char *who, halcuda::ForceLawSpec *out)
+    {
+        HAL_REQUIRE(law != nullptr, "%s: law is NULL", who);
+        HAL_REQUIRE(law->kind == HAL_CUDA_FORCE_LINEAR || law->kind == HAL_CUDA_FORCE_LINEAR_CLAMPED ||
+                        law->kind == HAL_CUDA_FORCE_POWER,
+                    "%s: unknown force law kind %d", who, law->kind);
+        HAL_REQUIRE(std::isfinite(law->scale), "%s: the law's scale must be finite", who);
+        HAL_REQUIRE(law->kind != HAL_CUDA_FORCE_POWER || std::isfinite(law->exponent),
+                    "%s: the law's exponent must be finite", who);
+        out->kind = law->kind;
+        out->scale = law->scale;
+        out->exponent = (law->kind == HAL_CUDA_FORCE_POWER) ? law->exponent : 1.0;
+        out->sums = sums;
+        out->grid = false;
+        return HAL_CUDA_OK;
+    }
+
+    // The FP64 interface path's buffers, allocated on its first call.
+    int Ensure64(hal_cuda_agents *h)
+    {
+        if (h->sPosD.p == nullptr)  // the last of the FP64 buffers: all or none are allocated
+        {
+            size_t m = static_cast<size_t>(h->maxAgents > 0 ? h->maxAgents : 1);
+            HAL_TRY(h->pos64.Alloc(2 * m, "cudaMalloc(agents64)"));
+            HAL_TRY(h->rad64.Alloc(m, "cudaMalloc(agents64)"));
+            HAL_TRY(h->vel64.Alloc(2 * m, "cudaMalloc(agents64)"));
+            HAL_TRY(h->sRad64.Alloc(m, "cudaMalloc(agents64)"));
+            HAL_TRY(h->sPosD.Alloc(m, "cudaMalloc(agents64)"));
+        }
+        return HAL_CUDA_OK;
+    }
+}
+
 extern "C" int hal_cuda_accumulate_forces(hal_cuda_agents *h, const double *positions, int64_t posLen,
                                           const double *radii, int64_t radLen, double *velocityDeltas,
                                           double interactionRad, double springConstant, int32_t xDim, int32_t yDim,
@@ -973,15 +1257,7 @@ extern "C" int hal_cuda_accumulate_forces(hal_cuda_agents *h, const double *posi
                 interactionRad, kMaxInteractionRad);
     using namespace halcuda;
     HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
-    if (h->sPosD.p == nullptr)  // the last of the FP64 buffers: all or none are allocated
-    {
-        size_t m = static_cast<size_t>(h->maxAgents > 0 ? h->maxAgents : 1);
-        HAL_TRY(h->pos64.Alloc(2 * m, "cudaMalloc(agents64)"));
-        HAL_TRY(h->rad64.Alloc(m, "cudaMalloc(agents64)"));
-        HAL_TRY(h->vel64.Alloc(2 * m, "cudaMalloc(agents64)"));
-        HAL_TRY(h->sRad64.Alloc(m, "cudaMalloc(agents64)"));
-        HAL_TRY(h->sPosD.Alloc(m, "cudaMalloc(agents64)"));
-    }
+    HAL_TRY(Ensure64(h));
     cudaStream_t s = h->stream.Get();
     h->n = static_cast<int32_t>(radLen);
     if (h->n > 0)
@@ -1000,6 +1276,67 @@ extern "C" int hal_cuda_accumulate_forces(hal_cuda_agents *h, const double *posi
                            "cudaMemcpy(velocityDeltas)"));
     }
     return CudaStatus(cudaStreamSynchronize(s), "hal_cuda_accumulate_forces");
+}
+
+extern "C" int hal_cuda_sum_forces(hal_cuda_agents *h, const double *positions, const double *radii, int64_t n,
+                                   const double *velocities, double *velocitiesOut, double *forceSums,
+                                   double interactionRad, const hal_cuda_force_law *law, int32_t order,
+                                   int32_t xDim, int32_t yDim, int32_t wrapX, int32_t wrapY)
+{
+    const char *who = "hal_cuda_sum_forces";
+    HAL_REQUIRE(h != nullptr, "%s: handle is NULL", who);
+    HAL_REQUIRE(xDim == h->xDim && yDim == h->yDim,
+                "CudaAgentForceBackend2D::SumForces called with dimensions differing from construction");
+    HAL_REQUIRE(n >= 0 && n <= h->maxAgents,
+                "CudaAgentForceBackend2D::SumForces called with more agents than the construction-time capacity");
+    HAL_REQUIRE(n == 0 || (positions != nullptr && radii != nullptr && velocitiesOut != nullptr),
+                "%s: NULL array", who);
+    HAL_REQUIRE(RadiusOk(interactionRad), "%s: interactionRad %g outside [0, %g]", who, interactionRad,
+                kMaxInteractionRad);
+    HAL_REQUIRE(order == HAL_CUDA_ORDER_BACKEND || order == HAL_CUDA_ORDER_AGENTGRID, "%s: unknown order %d", who,
+                order);
+    halcuda::ForceLawSpec spec;
+    HAL_TRY(LawFrom(law, forceSums != nullptr, who, &spec));
+    spec.grid = (order == HAL_CUDA_ORDER_AGENTGRID);
+    using namespace halcuda;
+    HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    HAL_TRY(Ensure64(h));
+    if (forceSums != nullptr && h->sums64.p == nullptr)
+    {
+        HAL_TRY(h->sums64.Alloc(static_cast<size_t>(h->maxAgents > 0 ? h->maxAgents : 1), "cudaMalloc(force sums)"));
+    }
+    cudaStream_t s = h->stream.Get();
+    h->n = static_cast<int32_t>(n);
+    h->sumsValid = false;  // the FP32 sums are not this call's
+    const size_t bytes2 = 2 * static_cast<size_t>(n) * sizeof(double);
+    if (n > 0)
+    {
+        HAL_TRY(CudaStatus(cudaMemcpyAsync(h->pos64.p, positions, bytes2, cudaMemcpyHostToDevice, s),
+                           "cudaMemcpy(positions)"));
+        HAL_TRY(CudaStatus(cudaMemcpyAsync(h->rad64.p, radii, static_cast<size_t>(n) * sizeof(double),
+                                           cudaMemcpyHostToDevice, s), "cudaMemcpy(radii)"));
+        if (velocities != nullptr)
+        {
+            HAL_TRY(CudaStatus(cudaMemcpyAsync(h->vel64.p, velocities, bytes2, cudaMemcpyHostToDevice, s),
+                               "cudaMemcpy(velocities)"));
+        }
+    }
+    HAL_TRY((h->Bin<double, double>(h->pos64.p, h->rad64.p, h->sRad64.p, s)));
+    // velocities in place: each thread reads and writes only its own agent
+    HAL_TRY((h->Force<double, double>(h->sRad64.p, interactionRad, spec, wrapX != 0, wrapY != 0, h->vel64.p,
+                                      forceSums != nullptr ? h->sums64.p : nullptr,
+                                      velocities != nullptr ? h->vel64.p : nullptr, s)));
+    if (n > 0)
+    {
+        HAL_TRY(CudaStatus(cudaMemcpyAsync(velocitiesOut, h->vel64.p, bytes2, cudaMemcpyDeviceToHost, s),
+                           "cudaMemcpy(velocities)"));
+        if (forceSums != nullptr)
+        {
+            HAL_TRY(CudaStatus(cudaMemcpyAsync(forceSums, h->sums64.p, static_cast<size_t>(n) * sizeof(double),
+                                               cudaMemcpyDeviceToHost, s), "cudaMemcpy(force sums)"));
+        }
+    }
+    return CudaStatus(cudaStreamSynchronize(s), who);
 }
 
 extern "C" int hal_cuda_agents_upload(hal_cuda_agents *h, const float *positions, const float *radii, int32_t n)
@@ -1063,43 +1400,106 @@ extern "C" int hal_cuda_agents_get_state(hal_cuda_agents *h, float *positions, f
     return CudaStatus(cudaStreamSynchronize(s), "hal_cuda_agents_get_state");
 }
 
+namespace
+{
+    int StepCommon(hal_cuda_agents *h, int32_t ticks, double interactionRad, const halcuda::ForceLawSpec &law,
+                   int32_t wrapX, int32_t wrapY, double friction, double maxVel, const char *who)
+    {
+        HAL_REQUIRE(h != nullptr, "%s: handle is NULL", who);
+        HAL_REQUIRE(ticks >= 0, "%s: ticks must be >= 0", who);
+        HAL_REQUIRE(RadiusOk(interactionRad), "%s: interactionRad %g outside [0, %g]", who, interactionRad,
+                    kMaxInteractionRad);
+        HAL_REQUIRE(std::isfinite(friction), "%s: friction must be finite", who);
+        HAL_REQUIRE(!std::isnan(maxVel), "%s: maxVel is NaN", who);
+        using namespace halcuda;
+        HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+        cudaStream_t s = h->stream.Get();
+        MoveParams mp;
+        mp.friction = static_cast<float>(friction);
+        mp.maxVel = (maxVel < 0 || std::isinf(maxVel)) ? -1.0f : static_cast<float>(maxVel);
+        mp.xDimF = static_cast<float>(h->xDim);
+        mp.yDimF = static_cast<float>(h->yDim);
+        mp.wrapX = wrapX != 0;
+        mp.wrapY = wrapY != 0;
+        h->sumsValid = false;
+        for (int32_t t = 0; t < ticks; t++)
+        {
+            HAL_TRY(StepOnce(*h, interactionRad, law, mp, s));
+        }
+        h->sumsValid = law.sums && ticks > 0;
+        return HAL_CUDA_OK;
+    }
+
+    int DispatchCommon(hal_cuda_agents *h, double interactionRad, const halcuda::ForceLawSpec &law, int32_t wrapX,
+                       int32_t wrapY, const char *who)
+    {
+        HAL_REQUIRE(h != nullptr, "%s: handle is NULL", who);
+        HAL_REQUIRE(RadiusOk(interactionRad), "%s: interactionRad %g outside [0, %g]", who, interactionRad,
+                    kMaxInteractionRad);
+        using namespace halcuda;
+        HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+        cudaStream_t s = h->stream.Get();
+        h->sumsValid = false;
+        HAL_TRY((h->Bin<float, float>(h->pos32.p, h->rad32.p, h->sRad32.p, s)));
+        float *sums = nullptr;
+        if (law.sums)
+        {
+            HAL_TRY(h->SumsBuf32(&sums));
+        }
+        HAL_TRY((h->Force<float, float>(h->sRad32.p, interactionRad, law, wrapX != 0, wrapY != 0, h->vel32.p, sums,
+                                        static_cast<const float *>(nullptr), s)));
+        h->sumsValid = law.sums;
+        return HAL_CUDA_OK;
+    }
+}
+
 extern "C" int hal_cuda_agents_step(hal_cuda_agents *h, int32_t ticks, double interactionRad, double springConstant,
                                     int32_t wrapX, int32_t wrapY, double friction, double maxVel)
 {
-    HAL_REQUIRE(h != nullptr, "hal_cuda_agents_step: handle is NULL");
-    HAL_REQUIRE(ticks >= 0, "hal_cuda_agents_step: ticks must be >= 0");
-    HAL_REQUIRE(RadiusOk(interactionRad), "hal_cuda_agents_step: interactionRad %g outside [0, %g]", interactionRad,
-                kMaxInteractionRad);
-    HAL_REQUIRE(std::isfinite(friction), "hal_cuda_agents_step: friction must be finite");
-    HAL_REQUIRE(!std::isnan(maxVel), "hal_cuda_agents_step: maxVel is NaN");
-    using namespace halcuda;
-    HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
-    cudaStream_t s = h->stream.Get();
-    MoveParams mp;
-    mp.friction = static_cast<float>(friction);
-    mp.maxVel = (maxVel < 0 || std::isinf(maxVel)) ? -1.0f : static_cast<float>(maxVel);
-    mp.xDimF = static_cast<float>(h->xDim);
-    mp.yDimF = static_cast<float>(h->yDim);
-    mp.wrapX = wrapX != 0;
-    mp.wrapY = wrapY != 0;
-    for (int32_t t = 0; t < ticks; t++)
-    {
-        HAL_TRY(StepOnce(*h, interactionRad, springConstant, mp, s));
-    }
-    return HAL_CUDA_OK;
+    return StepCommon(h, ticks, interactionRad, halcuda::ForceLawSpec::Linear(springConstant), wrapX, wrapY, friction,
+                      maxVel, "hal_cuda_agents_step");
+}
+
+extern "C" int hal_cuda_agents_step_law(hal_cuda_agents *h, int32_t ticks, double interactionRad,
+                                        const hal_cuda_force_law *law, int32_t withSums, int32_t wrapX,
+                                        int32_t wrapY, double friction, double maxVel)
+{
+    halcuda::ForceLawSpec spec;
+    HAL_TRY(LawFrom(law, withSums != 0, "hal_cuda_agents_step_law", &spec));
+    return StepCommon(h, ticks, interactionRad, spec, wrapX, wrapY, friction, maxVel, "hal_cuda_agents_step_law");
 }
 
 extern "C" int hal_cuda_agents_dispatch(hal_cuda_agents *h, double interactionRad, double springConstant,
                                         int32_t wrapX, int32_t wrapY)
 {
-    HAL_REQUIRE(h != nullptr, "hal_cuda_agents_dispatch: handle is NULL");
-    HAL_REQUIRE(RadiusOk(interactionRad), "hal_cuda_agents_dispatch: interactionRad %g outside [0, %g]",
-                interactionRad, kMaxInteractionRad);
+    return DispatchCommon(h, interactionRad, halcuda::ForceLawSpec::Linear(springConstant), wrapX, wrapY,
+                          "hal_cuda_agents_dispatch");
+}
+
+extern "C" int hal_cuda_agents_dispatch_law(hal_cuda_agents *h, double interactionRad, const hal_cuda_force_law *law,
+                                            int32_t withSums, int32_t wrapX, int32_t wrapY)
+{
+    halcuda::ForceLawSpec spec;
+    HAL_TRY(LawFrom(law, withSums != 0, "hal_cuda_agents_dispatch_law", &spec));
+    return DispatchCommon(h, interactionRad, spec, wrapX, wrapY, "hal_cuda_agents_dispatch_law");
+}
+
+extern "C" int hal_cuda_agents_get_force_sums(hal_cuda_agents *h, float *forceSums, int32_t n)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_agents_get_force_sums: handle is NULL");
+    HAL_REQUIRE(n == h->n, "hal_cuda_agents_get_force_sums: %d agents requested, %d uploaded", n, h->n);
+    HAL_REQUIRE(n == 0 || forceSums != nullptr, "hal_cuda_agents_get_force_sums: NULL array");
+    HAL_REQUIRE(h->sumsValid || n == 0,
+                "hal_cuda_agents_get_force_sums: the last dispatch or step did not compute force sums");
     using namespace halcuda;
     HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
     cudaStream_t s = h->stream.Get();
-    HAL_TRY((h->Bin<float, float>(h->pos32.p, h->rad32.p, h->sRad32.p, s)));
-    return h->Force<float, float>(h->sRad32.p, interactionRad, springConstant, wrapX != 0, wrapY != 0, h->vel32.p, s);
+    if (n > 0)
+    {
+        HAL_TRY(CudaStatus(cudaMemcpyAsync(forceSums, h->sums32.p, static_cast<size_t>(n) * sizeof(float),
+                                           cudaMemcpyDeviceToHost, s), "cudaMemcpy(force sums)"));
+    }
+    return CudaStatus(cudaStreamSynchronize(s), "hal_cuda_agents_get_force_sums");
 }
 
 extern "C" int hal_cuda_agents_download(hal_cuda_agents *h, float *velocityDeltas, int32_t n)
@@ -1403,9 +1803,12 @@ extern "C" int hal_cuda_agents_forces_noalloc(const float *positions, const floa
     Scatter<<<ablocks, T, 0, s>>>(cellOf, arrival, offsets, n, bucketTmp);
     Stabilize<float, float><<<ablocks, T, 0, s>>>(cellOf, offsets, bucketTmp, posF, radii, n, bucket, sPos, sRad);
     const int TF = 128;
+    LawParams<float> lp;
+    lp.scale = static_cast<float>(springConstant);
+    lp.exponent = 1.0f;
     Forces<float, float><<<static_cast<unsigned>((n + TF - 1) / TF), TF, 0, s>>>(
-        bucket, offsets, sPos, sRad, n, interactionRad, static_cast<float>(interactionRad),
-        static_cast<float>(springConstant), xDim, yDim, wrapX != 0, wrapY != 0, velocityDeltas);
+        bucket, offsets, sPos, sRad, n, interactionRad, static_cast<float>(interactionRad), lp, xDim, yDim,
+        wrapX != 0, wrapY != 0, velocityDeltas, static_cast<float *>(nullptr), static_cast<const float *>(nullptr));
     CountLaunch(7);
     return LaunchStatus("hal_cuda_agents_forces_noalloc");
 }

@@ -84,6 +84,10 @@ SIGNATURES = {
     "hal_cuda_agents_destroy": (_I, [_vp]),
     "hal_cuda_accumulate_forces": (_I, [_vp, _vp, _i64, _vp, _i64, _vp, _f64, _f64, _i32, _i32, _i32,
                                         _i32]),
+    "hal_cuda_sum_forces": (_I, [_vp, _vp, _vp, _i64, _vp, _vp, _vp, _f64, _vp, _i32, _i32, _i32, _i32, _i32]),
+    "hal_cuda_agents_dispatch_law": (_I, [_vp, _f64, _vp, _i32, _i32, _i32]),
+    "hal_cuda_agents_step_law": (_I, [_vp, _i32, _f64, _vp, _i32, _i32, _i32, _f64, _f64]),
+    "hal_cuda_agents_get_force_sums": (_I, [_vp, _vp, _i32]),
     "hal_cuda_agents_upload": (_I, [_vp, _vp, _vp, _i32]),
     "hal_cuda_agents_dispatch": (_I, [_vp, _f64, _f64, _i32, _i32]),
     "hal_cuda_agents_download": (_I, [_vp, _vp, _i32]),
@@ -510,6 +514,20 @@ class Adi(_Handle):
         return f
 
 
+FORCE_LINEAR, FORCE_LINEAR_CLAMPED, FORCE_POWER = 0, 1, 2
+ORDER_BACKEND, ORDER_AGENTGRID = 0, 1
+
+
+class ForceLaw(ctypes.Structure):
+    """hal_cuda_force_law: the overlap force law of SphericalAgent2D::SumForces."""
+
+    _fields_ = [("kind", ctypes.c_int32), ("scale", ctypes.c_double), ("exponent", ctypes.c_double)]
+
+
+def _law(kind, scale, exponent=1.0):
+    return ForceLaw(int(kind), float(scale), float(exponent))
+
+
 class Agents(_Handle):
     """hal_cuda_agents: IAgentForceBackend2D plus the resident dispatch."""
 
@@ -536,6 +554,38 @@ class Agents(_Handle):
                                                 int(wrapX), int(wrapY)), "accumulate_forces")
         self.n = r.size
         return out
+
+    def sum_forces(self, positions, radii, interactionRad, law, scale, xDim, yDim, wrapX, wrapY,
+                   velocities=None, exponent=1.0, order=ORDER_AGENTGRID, sums=True):
+        """SphericalAgent2D::SumForces of every agent (FP64); returns
+        (velocities after the call [2n], sums of positive forces [n] or None)."""
+        p = _f64(positions)
+        r = _f64(radii)
+        v = None if velocities is None else _f64(velocities)
+        out = np.zeros(p.size, dtype=np.float64)
+        fs = np.zeros(max(r.size, 1), dtype=np.float64) if sums else None
+        lw = _law(law, scale, exponent)
+        _check(lib().hal_cuda_sum_forces(self._h, _p(p), _p(r), r.size, _p(v), _p(out), _p(fs), interactionRad,
+                                         ctypes.byref(lw), int(order), xDim, yDim, int(wrapX), int(wrapY)),
+               "sum_forces")
+        self.n = r.size
+        return out, (fs[: r.size] if sums else None)
+
+    def dispatch_law(self, interactionRad, law, scale, exponent=1.0, sums=True, wrapX=False, wrapY=False):
+        lw = _law(law, scale, exponent)
+        _check(lib().hal_cuda_agents_dispatch_law(self._h, interactionRad, ctypes.byref(lw), int(sums), int(wrapX),
+                                                  int(wrapY)), "dispatch_law")
+
+    def step_law(self, ticks, interactionRad, law, scale, exponent=1.0, sums=True, wrapX=False, wrapY=False,
+                 friction=1.0, maxVel=-1.0):
+        lw = _law(law, scale, exponent)
+        _check(lib().hal_cuda_agents_step_law(self._h, ticks, interactionRad, ctypes.byref(lw), int(sums),
+                                              int(wrapX), int(wrapY), float(friction), float(maxVel)), "step_law")
+
+    def get_force_sums(self):
+        out = np.empty(max(self.n, 1), dtype=np.float32)
+        _check(lib().hal_cuda_agents_get_force_sums(self._h, _p(out), self.n), "get_force_sums")
+        return out[: self.n]
 
     def upload(self, positions, radii):
         p = _f32(positions)

@@ -253,13 +253,68 @@ int hal_cuda_agents_destroy(hal_cuda_agents *h);
  * positions (posLen = 2n doubles, x0 y0 x1 y1 ...), radii (radLen = n), out
  * velocityDeltas (2n doubles, overwritten).  EINVAL unless posLen ==
  * 2*radLen, xDim/yDim match the handle and n <= maxAgents
- * (GpuAgentForceBackend2D.cpp:34-46).  Positions are rounded to float32 on
- * the device, as the Vulkan backend does; binning follows the float32 values
- * exactly (bit-exact with the CPU backend fed the same float32 values). */
+ * (GpuAgentForceBackend2D.cpp:34-46).  Positions, radii and the force sum
+ * stay FP64 on the device, with IEEE operations in the CPU backend's order:
+ * bins, bucket order and velocity deltas are bit-identical to
+ * CpuAgentForceBackend2D's. */
 int hal_cuda_accumulate_forces(hal_cuda_agents *h, const double *positions, int64_t posLen,
                                const double *radii, int64_t radLen, double *velocityDeltas,
                                double interactionRad, double springConstant, int32_t xDim,
                                int32_t yDim, int32_t wrapX, int32_t wrapY);
+
+/* Overlap force laws.  SphericalAgent2D::SumForces (include/Hal/Agents/
+ * SphericalAgent2D.h:74-102) takes a functor overlapFun(touchDist, other) ->
+ * force, where touchDist = (r_i + r_j) - d is positive for overlapping agents;
+ * a device kernel cannot call a host functor, so the law is one of:
+ *   HAL_CUDA_FORCE_LINEAR          scale * touchDist (the interface's law,
+ *                                  CpuAgentForceBackend2D.cpp:165)
+ *   HAL_CUDA_FORCE_LINEAR_CLAMPED  0 when touchDist < 0, else scale * touchDist
+ *                                  (examples/OffLatticeExample.cpp:147-154)
+ *   HAL_CUDA_FORCE_POWER           pow(scale * touchDist, exponent)
+ *                                  (examples/Chemotaxis.cpp:128-130)
+ * A positive force pushes the agents apart. */
+#define HAL_CUDA_FORCE_LINEAR 0
+#define HAL_CUDA_FORCE_LINEAR_CLAMPED 1
+#define HAL_CUDA_FORCE_POWER 2
+
+typedef struct hal_cuda_force_law
+{
+    int32_t kind;    /* HAL_CUDA_FORCE_* */
+    double scale;    /* the spring constant / force scaler */
+    double exponent; /* HAL_CUDA_FORCE_POWER only */
+} hal_cuda_force_law;
+
+/* Order in which each agent visits its neighbours.  The cell window is
+ * walked x-major then y in both; within a cell:
+ *   HAL_CUDA_ORDER_BACKEND    ascending agent index, wrapped displacement
+ *                             AgentForceDisp (CpuAgentForceBackend2D.cpp:
+ *                             30-45, 112-175);
+ *   HAL_CUDA_ORDER_AGENTGRID  descending agent index, wrapped displacement
+ *                             DispX/DispY (src/Grids/GridGeometry2D.cpp:
+ *                             132-150): AgentGrid2D::GetAgentsRadApprox
+ *                             (include/Hal/Grids/AgentGrid2D.h:337-369) on a
+ *                             grid whose agents were created in index order
+ *                             (each square lists its newest agent first,
+ *                             AgentPT2D.h:200-241). */
+#define HAL_CUDA_ORDER_BACKEND 0
+#define HAL_CUDA_ORDER_AGENTGRID 1
+
+/* SphericalAgent2D::SumForces(interactionRad, overlapFun) for every agent at
+ * once, FP64 (IEEE operations in the reference's order).  velocities (2n
+ * doubles, may be NULL for zeros) are the agents' xVel/yVel before the call;
+ * velocitiesOut (2n) receives them after it (velocities plus the forces'
+ * change; with NULL velocities, the velocity deltas).  forceSums (n doubles,
+ * may be NULL) receives each agent's SumForces return value: the sum of its
+ * positive forces, which models gate division on (OffLatticeExample.cpp:
+ * 156-165).  With HAL_CUDA_ORDER_AGENTGRID and the LINEAR or LINEAR_CLAMPED
+ * law the results are bit-identical to SumForces on an AgentGrid2D whose
+ * agents were created in index order; the POWER law calls the device's pow,
+ * which can differ from the host's in the last bit.  Bins as in
+ * hal_cuda_accumulate_forces; sizes as there. */
+int hal_cuda_sum_forces(hal_cuda_agents *h, const double *positions, const double *radii, int64_t n,
+                        const double *velocities, double *velocitiesOut, double *forceSums,
+                        double interactionRad, const hal_cuda_force_law *law, int32_t order,
+                        int32_t xDim, int32_t yDim, int32_t wrapX, int32_t wrapY);
 
 /* Resident agents (AgentForceKernel2D::UploadAgents / Dispatch /
  * DownloadVelocityDeltas, src/Gpu/AgentForceKernel2D.cpp:173-290). */
@@ -296,6 +351,21 @@ int hal_cuda_agents_step(hal_cuda_agents *h, int32_t ticks, double interactionRa
  * CpuAgentForceBackend2D (src/Agents/CpuAgentForceBackend2D.cpp:85-109).
  * Either pointer may be NULL. */
 int hal_cuda_agents_get_bins(hal_cuda_agents *h, int32_t *cellOffsets, int32_t *bucketAgents);
+
+/* The resident dispatch and step with a force law (HAL_CUDA_ORDER_BACKEND
+ * order, FP32): as hal_cuda_agents_dispatch / hal_cuda_agents_step with the
+ * law in place of the linear spring.  With withSums != 0 the force kernel also
+ * writes each agent's sum of positive forces (SumForces' return value, in
+ * FP32), which hal_cuda_agents_get_force_sums downloads (n = the uploaded
+ * count; the sums of the step's last tick, at the positions it started from);
+ * EINVAL when the last dispatch or step computed none. */
+int hal_cuda_agents_dispatch_law(hal_cuda_agents *h, double interactionRad,
+                                 const hal_cuda_force_law *law, int32_t withSums, int32_t wrapX,
+                                 int32_t wrapY);
+int hal_cuda_agents_step_law(hal_cuda_agents *h, int32_t ticks, double interactionRad,
+                             const hal_cuda_force_law *law, int32_t withSums, int32_t wrapX,
+                             int32_t wrapY, double friction, double maxVel);
+int hal_cuda_agents_get_force_sums(hal_cuda_agents *h, float *forceSums, int32_t n);
 
 int hal_cuda_agents_sync(hal_cuda_agents *h);
 void *hal_cuda_agents_stream(hal_cuda_agents *h);

@@ -806,6 +806,144 @@ int oracle_accumulate_forces(const double *positions, const double *radii,
     return 0;
 }
 
+/* ---- SphericalAgent2D::SumForces (include/Hal/Agents/SphericalAgent2D.h:74-102)
+ * over an AgentGrid2D (include/Hal/Grids/AgentGrid2D.h:337-369) ---------- */
+
+/* GridGeometry2D::DispX/DispY (src/Grids/GridGeometry2D.cpp:132-150) with
+ * DispWrap (src/MathUtil.cpp:363-379) on a wrapped axis. */
+static double o_disp_grid(double p1, double p2, int32_t dim, int wrap)
+{
+    if (wrap)
+    {
+        double dimF = (double)dim;
+        if (fabs(p1 - p2) > (dimF / 2))
+        {
+            if (p1 > p2)
+            {
+                p2 = p2 + dimF;
+            }
+            else
+            {
+                p1 = p1 + dimF;
+            }
+        }
+    }
+    return p2 - p1;
+}
+
+/* The overlap force laws of the examples: linear (the backend's spring),
+ * clamped Hooke's law (examples/OffLatticeExample.cpp:147-154) and a power
+ * law (examples/Chemotaxis.cpp:128-130). */
+static double o_overlap_force(int kind, double touchDist, double scale, double exponent)
+{
+    if (kind == 1)
+    {
+        if (touchDist < 0)
+        {
+            return 0;
+        }
+        return scale * touchDist;
+    }
+    if (kind == 2)
+    {
+        return pow(scale * touchDist, exponent);
+    }
+    return scale * touchDist;
+}
+
+void oracle_sum_forces(const double *positions, const double *radii, int32_t n,
+                       const double *velIn, double *velOut, double *sums,
+                       double interactionRad, int kind, double scale, double exponent,
+                       int order, int32_t xDim, int32_t yDim, int wrapX, int wrapY)
+{
+    int32_t numCells = xDim * yDim;
+    int32_t *offsets = (int32_t *)malloc(sizeof(int32_t) * ((size_t)numCells + 1));
+    int32_t *bucket = (int32_t *)malloc(sizeof(int32_t) * ((size_t)n + 1));
+    oracle_agent_bins(positions, n, xDim, yDim, offsets, bucket);
+    for (int32_t i = 0; i < n; i++)
+    {
+        double posX = positions[(size_t)i * 2];
+        double posY = positions[(size_t)i * 2 + 1];
+        double rad = radii[i];
+        double xVel = velIn ? velIn[(size_t)i * 2] : 0.0;
+        double yVel = velIn ? velIn[(size_t)i * 2 + 1] : 0.0;
+        double sum = 0;
+        /* GetAgentsRadApprox: the squares of the window, x-major, skipping
+         * or wrapping off-grid squares */
+        int32_t xStart = (int32_t)floor(posX - interactionRad);
+        int32_t xEnd = (int32_t)ceil(posX + interactionRad);
+        int32_t yStart = (int32_t)floor(posY - interactionRad);
+        int32_t yEnd = (int32_t)ceil(posY + interactionRad);
+        for (int32_t xSq = xStart; xSq < xEnd; xSq++)
+        {
+            for (int32_t ySq = yStart; ySq < yEnd; ySq++)
+            {
+                int32_t retX = xSq;
+                int32_t retY = ySq;
+                int inX = (retX >= 0) && (retX < xDim);
+                int inY = (retY >= 0) && (retY < yDim);
+                if ((!wrapX && !inX) || (!wrapY && !inY))
+                {
+                    continue;
+                }
+                if (wrapX && !inX)
+                {
+                    retX = o_wrap_index(retX, xDim);
+                }
+                if (wrapY && !inY)
+                {
+                    retY = o_wrap_index(retY, yDim);
+                }
+                int32_t cell = retX * yDim + retY;
+                int32_t start = offsets[cell];
+                int32_t end = offsets[cell + 1];
+                int32_t cnt = end - start;
+                for (int32_t t = 0; t < cnt; t++)
+                {
+                    /* a square's agents: newest first on a grid filled in
+                     * index order (AgentPT2D.h:200-241), else ascending */
+                    int32_t j = bucket[order == 1 ? end - 1 - t : start + t];
+                    if (j == i)
+                    {
+                        continue;
+                    }
+                    double xComp, yComp;
+                    if (order == 1)
+                    {
+                        xComp = o_disp_grid(posX, positions[(size_t)j * 2], xDim, wrapX);
+                        yComp = o_disp_grid(posY, positions[(size_t)j * 2 + 1], yDim, wrapY);
+                    }
+                    else
+                    {
+                        xComp = o_disp(posX, positions[(size_t)j * 2], xDim, wrapX);
+                        yComp = o_disp(posY, positions[(size_t)j * 2 + 1], yDim, wrapY);
+                    }
+                    double dist = sqrt((xComp * xComp) + (yComp * yComp));
+                    if ((dist < interactionRad) && (dist > 0.0))
+                    {
+                        double touchDist = (rad + radii[j]) - dist;
+                        double force = o_overlap_force(kind, touchDist, scale, exponent);
+                        xVel -= (xComp / dist) * force;
+                        yVel -= (yComp / dist) * force;
+                        if (force > 0)
+                        {
+                            sum += fabs(force);
+                        }
+                    }
+                }
+            }
+        }
+        velOut[(size_t)i * 2] = xVel;
+        velOut[(size_t)i * 2 + 1] = yVel;
+        if (sums)
+        {
+            sums[i] = sum;
+        }
+    }
+    free(offsets);
+    free(bucket);
+}
+
 /* ---- Hal::Rng (src/Rng.cpp) and the polar Gaussian -------------------- */
 
 /* SplitMix64Next (src/Rng.cpp:61-68) */

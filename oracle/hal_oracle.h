@@ -125,6 +125,19 @@ int oracle_accumulate_forces(const double *positions, const double *radii,
 /* Internal::Diffusion2(pField, pDeltas, pDiffRatesX, pDiffRatesY, ...)
  * (src/Pde/PDEequations.cpp:199-230): the +x/+y face uses the cell's rate (0
  * past a non-wrapped edge), the -x/-y face the neighbour's. */
+/* SphericalAgent2D::SumForces (include/Hal/Agents/SphericalAgent2D.h:74-102)
+ * of every agent, in index order.  kind: 0 linear scale*touchDist, 1 clamped
+ * (0 when touchDist < 0), 2 pow(scale*touchDist, exponent).  order 1 visits
+ * each square's agents newest first with the grid's DispX/DispY, as an
+ * AgentGrid2D filled in index order does; order 0 ascending with
+ * AgentForceDisp, as CpuAgentForceBackend2D does.  velIn (may be NULL for
+ * zeros) -> velOut, sums (may be NULL) = the returned sums of positive
+ * forces. */
+void oracle_sum_forces(const double *positions, const double *radii, int32_t n,
+                       const double *velIn, double *velOut, double *sums,
+                       double interactionRad, int kind, double scale, double exponent,
+                       int order, int32_t xDim, int32_t yDim, int wrapX, int wrapY);
+
 void oracle_diffusion2_var(const double *field, double *deltas, const double *ratesX, const double *ratesY,
                            int32_t xDim, int32_t yDim, int wrapX, int wrapY);
 

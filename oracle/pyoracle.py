@@ -115,6 +115,7 @@ class Oracle(_Lib):
         L.oracle_dadi_loss_grad.argtypes = [vp, vp, vp, f64, vp, i32, i32, ctypes.c_int, ctypes.c_int,
                                             i32, vp, vp, vp, vp]
         L.oracle_dadi_loss_grad.restype = f64
+        L.oracle_sum_forces.argtypes = [vp, vp, i32, vp, vp, vp, f64, ci, f64, f64, ci, i32, i32, ci, ci]
         L.oracle_rand_init.argtypes = [vp, ctypes.c_uint64]
         L.oracle_rand_double.argtypes = [vp]
         L.oracle_rand_double.restype = f64
@@ -192,6 +193,23 @@ class Oracle(_Lib):
                                            k, xDim, yDim, int(wrapX), int(wrapY),
                                            off.ctypes.data, bucket.ctypes.data, int(threads))
         return out, off, bucket[:n]
+
+    @classmethod
+    def sum_forces(cls, positions, radii, R, law, scale, xDim, yDim, wrapX, wrapY, vel=None, exponent=1.0,
+                   order=1):
+        """SphericalAgent2D::SumForces of every agent; returns (velocities
+        after the call [2n], sums of positive forces [n]).  law 0 linear, 1
+        clamped, 2 power; order 1 the agent grid's, 0 the CPU backend's."""
+        p = _f64(positions)
+        rad = _f64(radii)
+        n = len(rad)
+        v = None if vel is None else _f64(vel)
+        out = np.zeros(2 * n, dtype=np.float64)
+        sums = np.zeros(max(n, 1), dtype=np.float64)
+        cls.lib().oracle_sum_forces(p.ctypes.data, rad.ctypes.data, n, None if v is None else v.ctypes.data,
+                                    out.ctypes.data, sums.ctypes.data, R, int(law), float(scale), float(exponent),
+                                    int(order), xDim, yDim, int(wrapX), int(wrapY))
+        return out, sums[:n]
 
     @classmethod
     def agent_bins(cls, positions, xDim, yDim):
@@ -345,6 +363,7 @@ class Reference(_Lib):
         L.ref_pdegrid2d_save.argtypes = [ctypes.c_char_p, i32, i32, ci, ci, i32, vp, vp]
         L.ref_pdegrid2d_load.argtypes = [ctypes.c_char_p, vp, vp, vp, vp, ctypes.c_int64]
         L.ref_advect_bc.argtypes = [vp, vp, f64, f64, i32, i32, ci, ci, vp]
+        L.ref_sum_forces.argtypes = [vp, vp, vp, i32, i32, i32, ci, ci, f64, ci, f64, f64, vp, vp]
         L.ref_advect_var_bc.argtypes = [vp, vp, vp, vp, i32, i32, ci, ci, vp, vp, vp]
         for name in ("ref_diffuse", "ref_diffuse_bc", "ref_diffuse_adi", "ref_diffuse_adi_bc",
                      "ref_pdegrid_run", "ref_accumulate_forces"):
@@ -384,6 +403,20 @@ class Reference(_Lib):
                                             yDim, int(wrapX), int(wrapY), g.ctypes.data, gx.ctypes.data,
                                             gy.ctypes.data))
         return d
+
+    @classmethod
+    def sum_forces(cls, positions, radii, R, law, scale, xDim, yDim, wrapX, wrapY, vel=None, exponent=1.0):
+        """SphericalAgent2D::SumForces on the reference's agent grid; returns
+        (velocities after the call, sums of positive forces)."""
+        p, rad = _f64(positions), _f64(radii)
+        n = len(rad)
+        v = None if vel is None else _f64(vel)
+        out = np.zeros(2 * n, dtype=np.float64)
+        sums = np.zeros(max(n, 1), dtype=np.float64)
+        _ok(cls.lib().ref_sum_forces(p.ctypes.data, rad.ctypes.data, None if v is None else v.ctypes.data, n, xDim,
+                                     yDim, int(wrapX), int(wrapY), R, int(law), float(scale), float(exponent),
+                                     out.ctypes.data, sums.ctypes.data))
+        return out, sums[:n]
 
     @classmethod
     def agents_move(cls, pos, vel, deltas, xDim, yDim, wrapX, wrapY, friction, maxVel):

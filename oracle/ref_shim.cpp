@@ -25,6 +25,7 @@
 #include "Hal/Agents/CpuAgentForceBackend2D.h"
 #undef private
 
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <stdexcept>
@@ -189,6 +190,62 @@ extern "C"
                 vel[2 * i] = a.XVel();
                 vel[2 * i + 1] = a.YVel();
                 a.Dispose();
+            } });
+    }
+
+    // SphericalAgent2D::SumForces (include/Hal/Agents/SphericalAgent2D.h:
+    // 74-102) of every agent on the reference's own agent grid: the agents
+    // are created in index order with their radii and velocities, then each
+    // calls SumForces(interactionRad, law) in index order.  law 0: linear
+    // scale*touchDist; 1: clamped as examples/OffLatticeExample.cpp:147-154;
+    // 2: pow(scale*touchDist, exponent) as examples/Chemotaxis.cpp:128-130.
+    // velOut receives the velocities after the call, sums the returned values.
+    int ref_sum_forces(const double *pos, const double *rad, const double *velIn, int32_t n, int32_t xDim,
+                       int32_t yDim, int wrapX, int wrapY, double interactionRad, int law, double scale,
+                       double exponent, double *velOut, double *sums)
+    {
+        Quiet();
+        return Guard([&]()
+                     {
+            ShimCellGrid grid(xDim, yDim, wrapX != 0, wrapY != 0);
+            std::vector<ShimCell *> agents(static_cast<size_t>(n));
+            for (int32_t i = 0; i < n; i++)
+            {
+                ShimCell &a = grid.NewAgentPT(pos[2 * i], pos[2 * i + 1]);
+                a.DefaultInit(rad[i]);
+                if (velIn != nullptr)
+                {
+                    a.SetVelocity(velIn[2 * i], velIn[2 * i + 1]);
+                }
+                agents[static_cast<size_t>(i)] = &a;
+            }
+            for (int32_t i = 0; i < n; i++)
+            {
+                ShimCell &a = *agents[static_cast<size_t>(i)];
+                double sum = 0;
+                if (law == 1)
+                {
+                    sum = a.SumForces(interactionRad, [scale](double overlap, ShimCell &)
+                                      {
+                        if (overlap < 0)
+                        {
+                            return 0.0;
+                        }
+                        return scale * overlap; });
+                }
+                else if (law == 2)
+                {
+                    sum = a.SumForces(interactionRad, [scale, exponent](double overlap, ShimCell &)
+                                      { return std::pow(scale * overlap, exponent); });
+                }
+                else
+                {
+                    sum = a.SumForces(interactionRad, [scale](double overlap, ShimCell &)
+                                      { return scale * overlap; });
+                }
+                velOut[2 * i] = a.XVel();
+                velOut[2 * i + 1] = a.YVel();
+                sums[i] = sum;
             } });
     }
 

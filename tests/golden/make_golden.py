@@ -3,10 +3,12 @@
 Run in a tree where the reference sources exist (it builds
 ``oracle/_ref/libhal_ref.so`` from them through ``oracle/Makefile``):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py             # every fixture
+    python tests/golden/make_golden.py sumforces   # only the named ones
 
 Every output comes from Hal::CpuDiffusionBackend2D, Hal::CpuAdiDiffusionBackend2D,
-Hal::CpuAgentForceBackend2D, Hal::PDEGrid2D or Hal::Rand, called through
+Hal::CpuAgentForceBackend2D, Hal::PDEGrid2D, Hal::SphericalAgent2D on the
+reference's agent grid or Hal::Rand, called through
 ``oracle/ref_shim.cpp``.  The inputs are stored beside the outputs, so the
 fixtures need no random generator to be replayed.  Cases restate the
 reference's own tests (eigenmode decay, the seed-1234 agent scene, Dirichlet
@@ -265,6 +267,51 @@ def adv_tick_cases(rng):
     return out
 
 
+def sum_forces_cases(rng):
+    """SphericalAgent2D::SumForces (include/Hal/Agents/SphericalAgent2D.h:
+    74-102) on the reference's agent grid, agents created in index order, with
+    the linear law, the clamped law of examples/OffLatticeExample.cpp:147-154
+    and the power law of examples/Chemotaxis.cpp:128-130; starting velocities
+    zero or random; walls, torus and mixed edges; coincident agents."""
+    out = {}
+    # the seed-1234 scene (tests/IAgentForceBackend2DTests.cpp:25-37), periodic
+    u = R.rand_draws(1234, 0, 180)
+    pos = np.empty(120)
+    pos[0::2] = u[0::3] * 16.0
+    pos[1::2] = u[1::3] * 16.0
+    rad = 0.4 + u[2::3] * 0.4
+    scenes = [("s1234", 16, 16, 1, 1, pos, rad)]
+    for (name, xd, yd, n, wx, wy) in [("walls", 40, 30, 800, 0, 0), ("torus", 23, 31, 500, 1, 1),
+                                      ("mixed", 30, 12, 400, 0, 1), ("dense", 6, 5, 250, 1, 0)]:
+        m = int(n * 0.4)
+        uni = rng.random((n - m, 2)) * np.array([xd, yd])
+        clu = np.array([xd, yd]) * 0.5 + rng.normal(0.0, 1.5, (m, 2))
+        p = np.concatenate([uni, clu])
+        hi = np.array([np.nextafter(xd, 0), np.nextafter(yd, 0)])
+        p = np.clip(p, 0.0, hi).ravel()
+        p[2:4] = p[0:2]  # coincident agents: no direction, skipped
+        scenes.append((name, xd, yd, wx, wy, p, 0.25 + 0.35 * rng.random(n)))
+    laws = [(0, 0.4, 1.0), (1, 0.25, 1.0), (2, 0.7, 2.0)]
+    k = 0
+    for (name, xd, yd, wx, wy, p, r) in scenes:
+        out[f"{name}_pos"] = p
+        out[f"{name}_rad"] = r
+        for (law, scale, expo) in laws:
+            for R_ in (1.0, 2.2):
+                with_vel = (k % 2 == 1)
+                vel = (rng.random(p.size) - 0.5) * 0.4 if with_vel else None
+                v, sums = R.sum_forces(p, r, R_, law, scale, xd, yd, wx, wy, vel=vel, exponent=expo)
+                out[f"c{k}_scene"] = np.array([name.encode()])
+                out[f"c{k}_params"] = np.array([xd, yd, wx, wy, R_, law, scale, expo])
+                if vel is not None:
+                    out[f"c{k}_velin"] = vel
+                out[f"c{k}_vel"] = v
+                out[f"c{k}_sums"] = sums
+                k += 1
+    out["count"] = np.array([k])
+    return out
+
+
 def pdegrid_file():
     """A PDEGrid2D file written by the reference's SavePDEGrid2D
     (src/Grids/PDEGridSerialization.cpp:34-45): 13 x 7, wrapX only, update
@@ -281,6 +328,14 @@ def main():
     pyoracle.build(ref=True)
     if not R.available():
         raise SystemExit("the reference library could not be built (no reference tree?)")
+    only = sys.argv[1:]
+    if only:
+        # write only the named fixtures (each has its own seed)
+        makers = {"sumforces": lambda: sum_forces_cases(np.random.default_rng(5353))}
+        for name in only:
+            np.savez_compressed(os.path.join(HERE, name + ".npz"), **makers[name]())
+            print(os.path.join(HERE, name + ".npz"))
+        return
     rng = np.random.default_rng(20261203)
     np.savez_compressed(os.path.join(HERE, "stencil.npz"), **stencil_cases(rng))
     np.savez_compressed(os.path.join(HERE, "ticks.npz"), **tick_cases(rng))
@@ -289,8 +344,9 @@ def main():
     np.savez_compressed(os.path.join(HERE, "varstencil.npz"), **var_stencil_cases(np.random.default_rng(8181)))
     np.savez_compressed(os.path.join(HERE, "agentmove.npz"), **agent_move_cases(np.random.default_rng(9191)))
     np.savez_compressed(os.path.join(HERE, "advtick.npz"), **adv_tick_cases(np.random.default_rng(6262)))
+    np.savez_compressed(os.path.join(HERE, "sumforces.npz"), **sum_forces_cases(np.random.default_rng(5353)))
     print(pdegrid_file())
-    for name in ("stencil", "ticks", "agents", "rand", "varstencil", "agentmove", "advtick"):
+    for name in ("stencil", "ticks", "agents", "rand", "varstencil", "agentmove", "advtick", "sumforces"):
         p = os.path.join(HERE, name + ".npz")
         print(f"{p}: {os.path.getsize(p)} bytes")
 

@@ -350,3 +350,69 @@ def test_restatement_matches_reference_library_random(oracle):
         a = oracle.accumulate_forces(pos, rad, 1.7, 0.2, xd, yd, wx, wy)
         b = R.accumulate_forces(pos, rad, 1.7, 0.2, xd, yd, wx, wy)
         assert all(np.array_equal(x, y) for x, y in zip(a, b))
+
+
+def _sumforces_case(g, k):
+    """Inputs and outputs of golden SumForces case k."""
+    xd, yd, wx, wy, R_, law, scale, expo = (float(v) for v in g[f"c{k}_params"])
+    scene = g[f"c{k}_scene"][0].decode()
+    vin = g[f"c{k}_velin"] if f"c{k}_velin" in g.files else None
+    return dict(pos=g[f"{scene}_pos"], rad=g[f"{scene}_rad"], xd=int(xd), yd=int(yd), wx=int(wx), wy=int(wy),
+                R=R_, law=int(law), scale=scale, expo=expo, vin=vin, vel=g[f"c{k}_vel"], sums=g[f"c{k}_sums"],
+                tag=f"case {k} {scene} law {int(law)} R {R_}")
+
+
+def test_sum_forces_golden_bit_exact(oracle, golden):
+    """SphericalAgent2D::SumForces (include/Hal/Agents/SphericalAgent2D.h:
+    74-102) on the reference's agent grid, for the linear, clamped and power
+    laws, with and without starting velocities: the restatement's agent-grid
+    order reproduces the velocities and the returned sums bit for bit."""
+    g = golden("sumforces")
+    count = int(g["count"][0])
+    assert count == 30
+    laws = set()
+    for k in range(count):
+        c = _sumforces_case(g, k)
+        v, sums = oracle.sum_forces(c["pos"], c["rad"], c["R"], c["law"], c["scale"], c["xd"], c["yd"], c["wx"],
+                                    c["wy"], vel=c["vin"], exponent=c["expo"], order=1)
+        assert np.array_equal(v, c["vel"]), c["tag"]
+        assert np.array_equal(sums, c["sums"]), c["tag"]
+        laws.add(c["law"])
+        # the clamped law never counts a separated pair, so its sums differ
+        # from the linear law's only through overlapping pairs
+        assert (c["sums"] >= 0).all()
+    assert laws == {0, 1, 2}
+
+
+def test_sum_forces_backend_order_is_accumulate_forces(oracle):
+    """With the backend's order and the linear law from zero velocity,
+    SumForces is exactly AccumulateForces (the interface's own definition,
+    IAgentForceBackend2D.h:14)."""
+    rng = np.random.default_rng(31)
+    for (xd, yd, wx, wy) in [(20, 14, 0, 0), (13, 17, 1, 1)]:
+        n = 500
+        pos = np.stack([rng.random(n) * xd, rng.random(n) * yd], 1).ravel()
+        rad = 0.3 + 0.4 * rng.random(n)
+        v, _ = oracle.sum_forces(pos, rad, 2.0, 0, 0.3, xd, yd, wx, wy, order=0)
+        exp, _, _ = oracle.accumulate_forces(pos, rad, 2.0, 0.3, xd, yd, wx, wy)
+        assert np.array_equal(v, exp)
+
+
+@pytest.mark.skipif(not pyoracle.Reference.available() and not __import__("os").path.isdir(
+    pyoracle.REF_TREE), reason="reference tree not present")
+def test_sum_forces_matches_reference_library_random(oracle):
+    pyoracle.build(ref=True)
+    R = pyoracle.Reference
+    rng = np.random.default_rng(77)
+    for _ in range(6):
+        xd, yd = (int(v) for v in rng.integers(1, 30, 2))
+        wx, wy = (int(v) for v in rng.integers(0, 2, 2))
+        n = int(rng.integers(0, 400))
+        pos = np.stack([rng.random(n) * xd, rng.random(n) * yd], 1).ravel() * (1 - 1e-12)
+        rad = 0.2 + rng.random(n) * 0.6
+        vel = rng.random(2 * n) - 0.5
+        for law, scale, expo in [(0, 0.3, 1.0), (1, 0.5, 1.0), (2, 0.6, 2.0)]:
+            R_ = float(0.5 + rng.random() * 2.5)
+            a = oracle.sum_forces(pos, rad, R_, law, scale, xd, yd, wx, wy, vel=vel, exponent=expo, order=1)
+            b = R.sum_forces(pos, rad, R_, law, scale, xd, yd, wx, wy, vel=vel, exponent=expo)
+            assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
