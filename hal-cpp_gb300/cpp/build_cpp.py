@@ -3,7 +3,8 @@
     python hal-cpp_gb300/cpp/build_cpp.py [--hal-include DIR]
 
 * hal-cpp_gb300/libhal_cuda_cpp.so -- the Hal::Cuda backend classes
-  (src/CudaBackends2D.cpp) with the stand-in interface declarations of
+  (src/CudaBackends2D.cpp) and the resident grid Hal::Cuda::CudaPDEGrid2D
+  (src/CudaPDEGrid2D.cpp) with the stand-in interface declarations of
   compat/ (used when the backend is built outside a HAL-CPP tree), linked
   against libhal_cuda.so;
 * hal-cpp_gb300/_build/cpp/backend_tests -- the test driver
@@ -50,7 +51,8 @@ def _run(cmd):
 def build_library():
     os.makedirs(OUT_DIR, exist_ok=True)
     _run([_cxx()] + CXXFLAGS + ["-shared", "-o", LIB,
-          os.path.join(HERE, "src", "CudaBackends2D.cpp"), os.path.join(HERE, "compat", "compat.cpp"),
+          os.path.join(HERE, "src", "CudaBackends2D.cpp"), os.path.join(HERE, "src", "CudaPDEGrid2D.cpp"),
+          os.path.join(HERE, "compat", "compat.cpp"),
           "-I", os.path.join(HERE, "include"), "-I", os.path.join(HERE, "compat"), "-I", INCLUDE,
           "-L", PKG, "-lhal_cuda", "-Wl,-rpath,$ORIGIN"])
     return LIB
@@ -69,8 +71,9 @@ def build_tests():
 
 def check_against_hal(hal_include):
     """Compiles the backend classes against HAL's own headers (no output)."""
-    _run([_cxx()] + CXXFLAGS + ["-fsyntax-only", os.path.join(HERE, "src", "CudaBackends2D.cpp"),
-          "-I", os.path.join(HERE, "include"), "-I", hal_include, "-I", INCLUDE])
+    for src in ("CudaBackends2D.cpp", "CudaPDEGrid2D.cpp"):
+        _run([_cxx()] + CXXFLAGS + ["-fsyntax-only", os.path.join(HERE, "src", src),
+              "-I", os.path.join(HERE, "include"), "-I", hal_include, "-I", INCLUDE])
 
 
 def main(argv=None):

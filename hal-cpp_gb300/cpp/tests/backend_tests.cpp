@@ -9,6 +9,7 @@
 // Prints one line per check and "backend_tests: N passed, M failed"; the exit
 // status is 0 only if every check passed.
 #include "Hal/Cuda/CudaBackends2D.h"
+#include "Hal/Cuda/CudaPDEGrid2D.h"
 
 extern "C"
 {
@@ -251,6 +252,67 @@ namespace
             positive += (s > 0.0) ? 1 : 0;
         }
         return positive > n / 4 ? "" : Fmt("only %.0f cells feel a force", static_cast<double>(positive));
+    }
+
+    // A model's tick on the resident PDEGrid2D, written as against
+    // Hal::PDEGrid2D (examples/CompetitiveRelease.cpp:77-94,147): per-cell
+    // uptake Mul and source Add calls, DiffusionADI with a boundary value,
+    // an explicit step, MulAll decay and Update, three ticks.  Equal bit for
+    // bit to the same calls on the restatement of PDEGrid2D.
+    std::string ResidentGridModelTicks()
+    {
+        const int32_t nx = 40, ny = 33, n = nx * ny, ticks = 3, perTick = 50;
+        oracle_rand rng;
+        oracle_rand_init(&rng, 21);
+        std::vector<double> f0(static_cast<size_t>(n));
+        for (double &v : f0)
+        {
+            v = oracle_rand_double(&rng);
+        }
+        Hal::Cuda::CudaPDEGrid2D grid(nx, ny);
+        grid.SetState(f0, std::vector<double>(static_cast<size_t>(n), 0.0), 0);
+        std::vector<int32_t> ops, iargs;
+        std::vector<double> dargs, arrays;
+        auto op = [&](int32_t code, int32_t i, double d0, double d1 = 0.0, int32_t arr = 0) {
+            ops.push_back(code);
+            iargs.insert(iargs.end(), {arr, i, 0});
+            dargs.insert(dargs.end(), {d0, d1});
+        };
+        const int32_t g = 2 * (nx + ny);
+        arrays.assign(static_cast<size_t>(g), 1.0);  // the boundary value 1.0 as a ghost table
+        for (int32_t t = 0; t < ticks; t++)
+        {
+            for (int32_t k = 0; k < perTick; k++)
+            {
+                const int32_t c = oracle_rand_int(&rng, n);
+                grid.Mul(c, -0.03);
+                op(2, c, -0.03);
+                grid.Add(c, 0.01);
+                op(1, c, 0.01);
+            }
+            grid.DiffusionADI(0.7, 1.0);
+            op(31, 0, 0.7);
+            grid.Diffusion(0.2);
+            op(20, 0, 0.2);
+            grid.MulAll(-0.001);
+            op(12, 0, -0.001);
+            grid.Update();
+            op(50, 0, 0.0);
+        }
+        std::vector<double> f = f0, d(static_cast<size_t>(n), 0.0), rec(4);
+        int32_t uc = 0;
+        oracle_pdegrid_script(nx, ny, 0, 0, f.data(), d.data(), &uc, static_cast<int32_t>(ops.size()), ops.data(),
+                              iargs.data(), dargs.data(), arrays.data(), rec.data());
+        if (grid.GetField() != f || grid.GetDeltas() != d || grid.UpdateCt() != uc)
+        {
+            return Fmt("resident grid differs from the restatement: %.3e", MaxAbsDiff(grid.GetField(), f));
+        }
+        double mx = f[0];
+        for (double v : f)
+        {
+            mx = (v < mx) ? mx : v;
+        }
+        return grid.GetMax() == mx ? "" : "GetMax differs";
     }
 
     // Bins and FP64 forces equal the CPU backend bit for bit on float32
@@ -629,6 +691,7 @@ int main()
     Run("forces_and_bins_match_cpu", [&] { return ForcesMatchCpu(agents64); });
     Run("coincident_agents", [&] { return CoincidentAgents(agents8); });
     Run("clamped_sum_forces_bit_exact", [&] { return ClampedSumForces(agents64); });
+    Run("resident_pdegrid_model_ticks_bit_exact", [&] { return ResidentGridModelTicks(); });
     Run("size_mismatch_throws", [&] { return SizeMismatches(diffEig, adiEig, agents16); });
     Run("resident_ticks_match_cpu", [&] { return ResidentTicks(diffTick, adiTick); });
     Run("variable_rate_and_advection_bit_exact", [&] { return VariableStencils(diffTick); });

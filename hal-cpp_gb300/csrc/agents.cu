@@ -1148,6 +1148,20 @@ struct hal_cuda_agents : public Agents
 
 namespace halcuda
 {
+    AgentBinsView AgentsBins(const hal_cuda_agents *a)
+    {
+        AgentBinsView v;
+        v.offsets = a->offsets.p;
+        v.bucket = a->bucket.p;
+        v.cellOf = a->cellOf.p;
+        v.n = a->n;
+        v.xDim = a->xDim;
+        v.yDim = a->yDim;
+        v.device = a->device;
+        v.stream = a->stream.Get();
+        return v;
+    }
+
     const int32_t *AgentsCellOffsets(const hal_cuda_agents *a, int32_t *xDim, int32_t *yDim)
     {
         *xDim = a->xDim;

@@ -6,6 +6,8 @@
 
 #include <cstdint>
 
+struct hal_cuda_agents;
+
 namespace halcuda
 {
     // One well's grid inside the concatenated cell array.
@@ -46,6 +48,20 @@ namespace halcuda
 
     int32_t AgentScanTiles(int64_t cells);
 
+    // The bins of an agent handle's last binning, for other handles that act
+    // per agent on a grid of the same size (hal_cuda_pdegrid_apply_agents).
+    struct AgentBinsView
+    {
+        const int32_t *offsets;  // xDim*yDim + 1
+        const int32_t *bucket;   // n, ascending agent index within each cell
+        const int32_t *cellOf;   // n, by agent index
+        int32_t n, xDim, yDim;
+        int device;
+        cudaStream_t stream;     // the handle's stream
+    };
+
     // Count, scan, scatter, stable rank and forces of every well's agents.
     int LaunchAgentWells(const AgentWellsArgs &a, cudaStream_t s);
+
+    AgentBinsView AgentsBins(const hal_cuda_agents *a);
 }

@@ -89,6 +89,27 @@ SIGNATURES = {
     "hal_cuda_agents_step_law": (_I, [_vp, _i32, _f64, _vp, _i32, _i32, _i32, _f64, _f64]),
     "hal_cuda_agents_get_force_sums": (_I, [_vp, _vp, _i32]),
     "hal_cuda_agents_upload": (_I, [_vp, _vp, _vp, _i32]),
+    "hal_cuda_pdegrid_create": (_I, [_i32, _i32, _i32, _i32, _vp]),
+    "hal_cuda_pdegrid_destroy": (_I, [_vp]),
+    "hal_cuda_pdegrid_set_state": (_I, [_vp, _vp, _vp, _i32]),
+    "hal_cuda_pdegrid_get_state": (_I, [_vp, _vp, _vp, _vp]),
+    "hal_cuda_pdegrid_dims": (_I, [_vp, _vp]),
+    "hal_cuda_pdegrid_apply": (_I, [_vp, _vp, _i32, _vp, _vp, _f64, _i64]),
+    "hal_cuda_pdegrid_apply_agents": (_I, [_vp, _vp, _i32, _f64, _vp]),
+    "hal_cuda_pdegrid_apply_all": (_I, [_vp, _i32, _f64, _vp]),
+    "hal_cuda_pdegrid_update": (_I, [_vp]),
+    "hal_cuda_pdegrid_set_non_negative": (_I, [_vp]),
+    "hal_cuda_pdegrid_get_cells": (_I, [_vp, _vp, _i64, _vp]),
+    "hal_cuda_pdegrid_gradient": (_I, [_vp, _vp, _vp, _i64, _i32, _f64, _vp, _vp]),
+    "hal_cuda_pdegrid_stats": (_I, [_vp, _f64, _vp]),
+    "hal_cuda_pdegrid_diffusion": (_I, [_vp, _f64, _vp]),
+    "hal_cuda_pdegrid_diffusion_var": (_I, [_vp, _vp, _vp]),
+    "hal_cuda_pdegrid_diffusion_adi": (_I, [_vp, _f64, _vp]),
+    "hal_cuda_pdegrid_advection": (_I, [_vp, _f64, _f64, _vp]),
+    "hal_cuda_pdegrid_advection_var": (_I, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "hal_cuda_pdegrid_sync": (_I, [_vp]),
+    "hal_cuda_pdegrid_stream": (_vp, [_vp]),
+    "hal_cuda_pdegrid_set_stream": (_I, [_vp, _vp]),
     "hal_cuda_agents_dispatch": (_I, [_vp, _f64, _f64, _i32, _i32]),
     "hal_cuda_agents_download": (_I, [_vp, _vp, _i32]),
     "hal_cuda_agents_set_velocities": (_I, [_vp, _vp, _i32]),
@@ -634,6 +655,107 @@ class Agents(_Handle):
         bucket = np.empty(max(self.n, 1), dtype=np.int32)
         _check(lib().hal_cuda_agents_get_bins(self._h, _p(off), _p(bucket)), "get_bins")
         return off, bucket[: self.n]
+
+
+CELL_SET, CELL_ADD, CELL_MUL, CELL_SCALE = 0, 1, 2, 3
+
+
+class PDEGrid(_Handle):
+    """hal_cuda_pdegrid: Hal::PDEGrid2D resident on the device (FP64), the
+    per-cell operations batched into lists."""
+
+    _prefix = "pdegrid"
+
+    def __init__(self, xDim: int, yDim: int, wrapX=False, wrapY=False):
+        super().__init__()
+        h = ctypes.c_void_p()
+        _check(lib().hal_cuda_pdegrid_create(xDim, yDim, int(wrapX), int(wrapY), ctypes.byref(h)),
+               "pdegrid_create")
+        self._h = h
+        self.xDim, self.yDim, self.wrapX, self.wrapY = xDim, yDim, bool(wrapX), bool(wrapY)
+
+    @property
+    def length(self):
+        return self.xDim * self.yDim
+
+    def set_state(self, field, deltas=None, update_ct=0):
+        f = _f64(field)
+        d = _f64(deltas)
+        _check(lib().hal_cuda_pdegrid_set_state(self._h, _p(f), _p(d), int(update_ct)), "pdegrid_set_state")
+
+    def get_state(self):
+        """(field, deltas, updateCt)."""
+        f = np.empty(self.length)
+        d = np.empty(self.length)
+        uc = ctypes.c_int32(0)
+        _check(lib().hal_cuda_pdegrid_get_state(self._h, _p(f), _p(d), ctypes.byref(uc)), "pdegrid_get_state")
+        return f, d, uc.value
+
+    def apply(self, cells, values, op=None, ops=None):
+        """Operations at cells in list order: one `op` for all, or ops[k]."""
+        c = _i32(cells)
+        v = _f64(values)
+        o = _i32(ops)
+        n = 0 if c is None else c.size
+        _check(lib().hal_cuda_pdegrid_apply(self._h, _p(o), -1 if op is None else int(op), _p(c), _p(v), 0.0, n),
+               "pdegrid_apply")
+
+    def apply_agents(self, agents, op, value=0.0, per_agent=None):
+        pa = _f64(per_agent)
+        _check(lib().hal_cuda_pdegrid_apply_agents(self._h, agents.handle, int(op), float(value), _p(pa)),
+               "pdegrid_apply_agents")
+
+    def apply_all(self, op, value=0.0, per_cell=None):
+        pc = _f64(per_cell)
+        _check(lib().hal_cuda_pdegrid_apply_all(self._h, int(op), float(value), _p(pc)), "pdegrid_apply_all")
+
+    def update(self):
+        _check(lib().hal_cuda_pdegrid_update(self._h), "pdegrid_update")
+
+    def set_non_negative(self):
+        _check(lib().hal_cuda_pdegrid_set_non_negative(self._h), "pdegrid_set_non_negative")
+
+    def get_cells(self, cells):
+        c = _i32(cells)
+        out = np.empty(c.size)
+        _check(lib().hal_cuda_pdegrid_get_cells(self._h, _p(c), c.size, _p(out)), "pdegrid_get_cells")
+        return out
+
+    def gradient(self, xs, ys, boundary=None):
+        x, y = _i32(xs), _i32(ys)
+        gx, gy = np.empty(x.size), np.empty(x.size)
+        _check(lib().hal_cuda_pdegrid_gradient(self._h, _p(x), _p(y), x.size, int(boundary is not None),
+                                               0.0 if boundary is None else float(boundary), _p(gx), _p(gy)),
+               "pdegrid_gradient")
+        return gx, gy
+
+    def stats(self, denom_offset=float("nan")):
+        """[GetMax, GetMin, GetAvg, MaxDelta, MaxDeltaScaled(denom_offset)]."""
+        out = np.empty(5)
+        _check(lib().hal_cuda_pdegrid_stats(self._h, float(denom_offset), _p(out)), "pdegrid_stats")
+        return out
+
+    def diffusion(self, diff_coef, ghost=None):
+        g = _f64(ghost)
+        _check(lib().hal_cuda_pdegrid_diffusion(self._h, float(diff_coef), _p(g)), "pdegrid_diffusion")
+
+    def diffusion_var(self, rates_x, rates_y):
+        a, b = _f64(rates_x), _f64(rates_y)
+        _check(lib().hal_cuda_pdegrid_diffusion_var(self._h, _p(a), _p(b)), "pdegrid_diffusion_var")
+
+    def diffusion_adi(self, diff_rate, ghost=None):
+        g = _f64(ghost)
+        _check(lib().hal_cuda_pdegrid_diffusion_adi(self._h, float(diff_rate), _p(g)), "pdegrid_diffusion_adi")
+
+    def advection(self, x_vel, y_vel, ghost=None):
+        g = _f64(ghost)
+        _check(lib().hal_cuda_pdegrid_advection(self._h, float(x_vel), float(y_vel), _p(g)), "pdegrid_advection")
+
+    def advection_var(self, x_vels, y_vels, ghost=None, ghost_x_vel=None, ghost_y_vel=None):
+        a, b = _f64(x_vels), _f64(y_vels)
+        g, gx, gy = _f64(ghost), _f64(ghost_x_vel), _f64(ghost_y_vel)
+        _check(lib().hal_cuda_pdegrid_advection_var(self._h, _p(a), _p(b), _p(g), _p(gx), _p(gy)),
+               "pdegrid_advection_var")
 
 
 WELL_EXPLICIT, WELL_ADI = 0, 1

@@ -371,6 +371,99 @@ int hal_cuda_agents_sync(hal_cuda_agents *h);
 void *hal_cuda_agents_stream(hal_cuda_agents *h);
 int hal_cuda_agents_set_stream(hal_cuda_agents *h, void *stream);
 
+/* ---- device-resident PDEGrid2D -------------------------------------------
+ * Hal::PDEGrid2D (include/Hal/Grids/PDEGrid2D.h:17-458) with its committed
+ * field and its delta buffer kept in device memory, FP64.  Get reads the
+ * committed field; the per-cell operations and the PDE operators accumulate
+ * into the deltas; update commits them (field += deltas, deltas = 0, the
+ * update count + 1).  Every call reproduces the reference's arithmetic bit
+ * for bit, except hal_cuda_pdegrid_stats' average (a parallel sum; within
+ * rounding of GetAvg).  Work is enqueued on the handle's stream; calls that
+ * return values, or read caller arrays, synchronise it first.  EINVAL with
+ * the reference's message where PDEGrid2D throws std::invalid_argument. */
+typedef struct hal_cuda_pdegrid hal_cuda_pdegrid;
+
+/* PDEGrid2D(xDim, yDim, wrapX, wrapY): field and deltas zero, count 0. */
+int hal_cuda_pdegrid_create(int32_t xDim, int32_t yDim, int32_t wrapX, int32_t wrapY,
+                            hal_cuda_pdegrid **out);
+int hal_cuda_pdegrid_destroy(hal_cuda_pdegrid *h);
+
+/* SetState(field, deltas, updateCt) (PDEGrid2D.h:58-75); deltas may be NULL
+ * (zeros).  get_state: GetField / GetDeltas / UpdateCt, any pointer NULL to
+ * skip it.  Arrays hold xDim*yDim doubles in HAL's layout. */
+int hal_cuda_pdegrid_set_state(hal_cuda_pdegrid *h, const double *field, const double *deltas,
+                               int32_t updateCt);
+int hal_cuda_pdegrid_get_state(hal_cuda_pdegrid *h, double *field, double *deltas, int32_t *updateCt);
+/* xDim, yDim, wrapX, wrapY, updateCt into dims[0..4]. */
+int hal_cuda_pdegrid_dims(hal_cuda_pdegrid *h, int32_t *dims);
+
+/* Per-cell operations (PDEGrid2D.h:88-140) on cell i = x*yDim + y:
+ *   SET    deltas[i] = v - field[i]
+ *   ADD    deltas[i] += v
+ *   MUL    deltas[i] += field[i] * v
+ *   SCALE  deltas[i] += field[i] * (v - 1)                              */
+#define HAL_CUDA_CELL_SET 0
+#define HAL_CUDA_CELL_ADD 1
+#define HAL_CUDA_CELL_MUL 2
+#define HAL_CUDA_CELL_SCALE 3
+
+/* n operations, applied as a loop of single calls in list order would:
+ * entry k is operation ops[k] (or `op` for all when ops is NULL) at
+ * cells[k] with value values[k] (or `value` when values is NULL). */
+int hal_cuda_pdegrid_apply(hal_cuda_pdegrid *h, const int32_t *ops, int32_t op, const int32_t *cells,
+                           const double *values, double value, int64_t n);
+
+/* One operation per agent of the agent handle's last binning (dispatch,
+ * step, accumulate_forces or sum_forces), at the agent's cell, the agents of
+ * a cell in index order: e.g. MUL with value -uptake is each agent's
+ * PDEGrid2D::Mul(Isq(), -uptake) (examples/CompetitiveRelease.cpp:147).
+ * perAgent (n doubles by agent index, may be NULL) replaces value.  The grid
+ * must have the agents' size.  Ordered after the agents' last work on their
+ * stream, and their next work after this. */
+int hal_cuda_pdegrid_apply_agents(hal_cuda_pdegrid *h, hal_cuda_agents *agents, int32_t op,
+                                  double value, const double *perAgent);
+
+/* SetAll / AddAll / MulAll (PDEGrid2D.h:188-217): the operation at every
+ * cell; perCell (xDim*yDim, may be NULL) replaces value (SetAll(pVals)). */
+int hal_cuda_pdegrid_apply_all(hal_cuda_pdegrid *h, int32_t op, double value, const double *perCell);
+
+/* Update (PDEGrid2D.h:178-186) and SetNonNegative (:244-255). */
+int hal_cuda_pdegrid_update(hal_cuda_pdegrid *h);
+int hal_cuda_pdegrid_set_non_negative(hal_cuda_pdegrid *h);
+
+/* Get(i) of n cells of the committed field. */
+int hal_cuda_pdegrid_get_cells(hal_cuda_pdegrid *h, const int32_t *cells, int64_t n, double *out);
+
+/* GradientX / GradientY (PDEGrid2D.h:257-285) at n points (xs[k], ys[k]):
+ * off-grid neighbours read the cell's own value (reflecting) or, with
+ * useBoundary, boundaryValue; a wrapped axis wraps. */
+int hal_cuda_pdegrid_gradient(hal_cuda_pdegrid *h, const int32_t *xs, const int32_t *ys, int64_t n,
+                              int32_t useBoundary, double boundaryValue, double *gradX, double *gradY);
+
+/* stats[0..4] = GetMax, GetMin, GetAvg, MaxDelta and MaxDeltaScaled(
+ * denomOffset) (PDEGrid2D.h:142-241); a NaN denomOffset skips the last
+ * (stats[4] = NaN).  GetMax / GetMin keep the reference's choice among equal
+ * values (+0 and -0): the last in cell order. */
+int hal_cuda_pdegrid_stats(hal_cuda_pdegrid *h, double denomOffset, double *stats);
+
+/* The PDE operators, accumulating into the deltas (PDEGrid2D.h:289-400):
+ * Diffusion(diffCoef[, bc]) (EINVAL above 0.25), Diffusion(ratesX, ratesY),
+ * DiffusionADI(diffRate[, bc]), Advection(xVel, yVel[, bc]) (EINVAL when
+ * |xVel| + |yVel| > 0.5), Advection(xVels, yVels[, bc, xVelBC, yVelBC]).
+ * Boundary callables are ghost tables (file header), NULL for none; per-cell
+ * arrays hold xDim*yDim doubles. */
+int hal_cuda_pdegrid_diffusion(hal_cuda_pdegrid *h, double diffCoef, const double *ghost);
+int hal_cuda_pdegrid_diffusion_var(hal_cuda_pdegrid *h, const double *ratesX, const double *ratesY);
+int hal_cuda_pdegrid_diffusion_adi(hal_cuda_pdegrid *h, double diffRate, const double *ghost);
+int hal_cuda_pdegrid_advection(hal_cuda_pdegrid *h, double xVel, double yVel, const double *ghost);
+int hal_cuda_pdegrid_advection_var(hal_cuda_pdegrid *h, const double *xVels, const double *yVels,
+                                   const double *ghost, const double *ghostXVel,
+                                   const double *ghostYVel);
+
+int hal_cuda_pdegrid_sync(hal_cuda_pdegrid *h);
+void *hal_cuda_pdegrid_stream(hal_cuda_pdegrid *h);
+int hal_cuda_pdegrid_set_stream(hal_cuda_pdegrid *h, void *stream);
+
 /* ---- on-disk format: SavePDEGrid2D / LoadPDEGrid2D ------------------------
  * (src/Grids/PDEGridSerialization.cpp:34-62, through BinaryWriter /
  * BinaryReader): raw native-endian int32 xDim, int32 yDim, one byte each for

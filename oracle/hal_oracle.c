@@ -9,6 +9,7 @@
  */
 #include "hal_oracle.h"
 
+#include <float.h>
 #include <math.h>
 #include <pthread.h>
 #include <stdlib.h>
@@ -1577,3 +1578,206 @@ void oracle_advection2_var(const double *field, double *deltas, const double *xV
 
 O_AGENTS_MOVE(oracle_agents_move, double, fmod, sqrt)
 O_AGENTS_MOVE(oracle_agents_move_f32, float, fmodf, sqrtf)
+
+/* ---- Hal::PDEGrid2D call sequences (include/Hal/Grids/PDEGrid2D.h) --------
+ * A script of calls on one grid, run as the reference's PDEGrid2D runs them:
+ * see oracle_pdegrid_script in hal_oracle.h for the encoding. */
+
+static void o_cell_op(int op, double *deltas, const double *field, int32_t i, double v)
+{
+    switch (op)
+    {
+    case 0: /* Set (:88-99) */
+        deltas[i] = v - field[i];
+        break;
+    case 1: /* Add (:101-112) */
+        deltas[i] += v;
+        break;
+    case 2: /* Mul (:114-126) */
+        deltas[i] += field[i] * v;
+        break;
+    default: /* Scale (:128-140) */
+        deltas[i] += field[i] * (v - 1);
+        break;
+    }
+}
+
+/* DisplacedFieldX / DisplacedFieldY (:400-430) */
+static double o_displaced(const double *f, int32_t x, int32_t y, int alongX, int32_t xDim, int32_t yDim,
+                          int wrapX, int wrapY, double oob)
+{
+    if (alongX)
+    {
+        if (o_in_dim(x, xDim))
+        {
+            return f[x * yDim + y];
+        }
+        if (wrapX)
+        {
+            return f[o_wrap(x, xDim) * yDim + y];
+        }
+        return oob;
+    }
+    if (o_in_dim(y, yDim))
+    {
+        return f[x * yDim + y];
+    }
+    if (wrapY)
+    {
+        return f[x * yDim + o_wrap(y, yDim)];
+    }
+    return oob;
+}
+
+int oracle_pdegrid_script(int32_t xDim, int32_t yDim, int wrapX, int wrapY, double *field, double *deltas,
+                          int32_t *updateCt, int32_t nOps, const int32_t *ops, const int32_t *iargs,
+                          const double *dargs, const double *arrays, double *records)
+{
+    int32_t length = xDim * yDim;
+    double *scratch = (double *)malloc(sizeof(double) * ((size_t)length + 1));
+    int32_t nRec = 0;
+    for (int32_t k = 0; k < nOps; k++)
+    {
+        const int32_t *ia = iargs + 3 * (size_t)k;
+        const double *da = dargs + 2 * (size_t)k;
+        const double *arr = arrays + ia[0];
+        int op = ops[k];
+        if (op >= 0 && op <= 3)
+        {
+            o_cell_op(op, deltas, field, ia[1], da[0]);
+        }
+        else if (op >= 10 && op <= 12)
+        {
+            /* SetAll / AddAll / MulAll (:188-217) */
+            for (int32_t i = 0; i < length; i++)
+            {
+                o_cell_op(op - 10, deltas, field, i, da[0]);
+            }
+        }
+        else if (op == 13)
+        {
+            for (int32_t i = 0; i < length; i++)
+            {
+                o_cell_op(0, deltas, field, i, arr[i]);
+            }
+        }
+        else if (op == 20 || op == 21)
+        {
+            if (da[0] > 0.25)
+            {
+                free(scratch);
+                return -1;
+            }
+            oracle_diffusion2(field, deltas, da[0], xDim, yDim, wrapX, wrapY, op == 21 ? arr : NULL);
+        }
+        else if (op == 22)
+        {
+            oracle_diffusion2_var(field, deltas, arr, arr + length, xDim, yDim, wrapX, wrapY);
+        }
+        else if (op == 30 || op == 31)
+        {
+            oracle_adi2(field, scratch, deltas, da[0], xDim, yDim, wrapX, wrapY, op == 31 ? arr : NULL);
+        }
+        else if (op == 40 || op == 41)
+        {
+            if ((fabs(da[0]) + fabs(da[1])) > 0.5)
+            {
+                free(scratch);
+                return -2;
+            }
+            oracle_advection2_bc(field, deltas, da[0], da[1], xDim, yDim, wrapX, wrapY, op == 41 ? arr : NULL);
+        }
+        else if (op == 42)
+        {
+            oracle_advection2_var(field, deltas, arr, arr + length, xDim, yDim, wrapX, wrapY);
+        }
+        else if (op == 43)
+        {
+            int32_t g = 2 * (xDim + yDim);
+            oracle_advection2_var_bc(field, deltas, arr, arr + length, xDim, yDim, wrapX, wrapY, arr + 2 * length,
+                                     arr + 2 * length + g, arr + 2 * length + 2 * g);
+        }
+        else if (op == 50)
+        {
+            /* Update (:178-186) */
+            for (int32_t i = 0; i < length; i++)
+            {
+                field[i] += deltas[i];
+            }
+            memset(deltas, 0, sizeof(double) * (size_t)length);
+            (*updateCt)++;
+        }
+        else if (op == 51)
+        {
+            /* SetNonNegative (:244-255) */
+            for (int32_t i = 0; i < length; i++)
+            {
+                if ((field[i] + deltas[i]) < 0)
+                {
+                    deltas[i] = 0 - field[i];
+                }
+            }
+        }
+        else if (op == 60)
+        {
+            records[nRec++] = field[ia[1]];
+        }
+        else if (op == 61 || op == 62)
+        {
+            /* GetMax / GetMin (:142-164): std::max(field, max) keeps the
+             * later of equal values */
+            double m = (op == 61) ? -DBL_MAX : DBL_MAX;
+            for (int32_t i = 0; i < length; i++)
+            {
+                if (op == 61)
+                {
+                    m = (field[i] < m) ? m : field[i];
+                }
+                else
+                {
+                    m = (m < field[i]) ? m : field[i];
+                }
+            }
+            records[nRec++] = m;
+        }
+        else if (op == 63)
+        {
+            double tot = 0;
+            for (int32_t i = 0; i < length; i++)
+            {
+                tot += field[i];
+            }
+            records[nRec++] = tot / length;
+        }
+        else if (op == 64 || op == 65)
+        {
+            /* MaxDelta / MaxDeltaScaled (:219-241) */
+            double maxDif = 0;
+            for (int32_t i = 0; i < length; i++)
+            {
+                double v = (op == 64) ? fabs(deltas[i]) : fabs(deltas[i] / (fabs(field[i]) + da[0]));
+                maxDif = (maxDif < v) ? v : maxDif;
+            }
+            records[nRec++] = maxDif;
+        }
+        else if (op >= 66 && op <= 69)
+        {
+            /* GradientX / GradientY (:257-285) */
+            int32_t x = ia[1], y = ia[2];
+            double own = field[x * yDim + y];
+            double oob = (op >= 68) ? da[0] : own;
+            if (op == 66 || op == 68)
+            {
+                records[nRec++] = o_displaced(field, x + 1, y, 1, xDim, yDim, wrapX, wrapY, oob) -
+                                  o_displaced(field, x - 1, y, 1, xDim, yDim, wrapX, wrapY, oob);
+            }
+            else
+            {
+                records[nRec++] = o_displaced(field, x, y + 1, 0, xDim, yDim, wrapX, wrapY, oob) -
+                                  o_displaced(field, x, y - 1, 0, xDim, yDim, wrapX, wrapY, oob);
+            }
+        }
+    }
+    free(scratch);
+    return nRec;
+}

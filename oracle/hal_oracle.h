@@ -138,6 +138,23 @@ void oracle_sum_forces(const double *positions, const double *radii, int32_t n,
                        double interactionRad, int kind, double scale, double exponent,
                        int order, int32_t xDim, int32_t yDim, int wrapX, int wrapY);
 
+/* A script of Hal::PDEGrid2D calls (include/Hal/Grids/PDEGrid2D.h) run on
+ * field/deltas/updateCt in place.  Op k has iargs[3k..3k+2] = (offset of
+ * its arrays in `arrays`, i or x, y) and dargs[2k..2k+1]:
+ *   0-3 Set/Add/Mul/Scale(i, d0);  10-12 SetAll/AddAll/MulAll(d0);
+ *   13 SetAll(arrays);  20 Diffusion(d0);  21 Diffusion(d0, ghost table);
+ *   22 Diffusion(ratesX, ratesY);  30 DiffusionADI(d0);  31 DiffusionADI(d0,
+ *   ghost);  40 Advection(d0, d1);  41 Advection(d0, d1, ghost);
+ *   42 Advection(xVels, yVels);  43 the same with field, x- and y-velocity
+ *   ghost tables;  50 Update();  51 SetNonNegative();  records: 60 Get(i),
+ *   61 GetMax, 62 GetMin, 63 GetAvg, 64 MaxDelta, 65 MaxDeltaScaled(d0),
+ *   66/67 GradientX/Y(x, y), 68/69 the same with boundary value d0.
+ * Returns the number of records, -1 / -2 for a rejected diffusion /
+ * advection rate. */
+int oracle_pdegrid_script(int32_t xDim, int32_t yDim, int wrapX, int wrapY, double *field, double *deltas,
+                          int32_t *updateCt, int32_t nOps, const int32_t *ops, const int32_t *iargs,
+                          const double *dargs, const double *arrays, double *records);
+
 void oracle_diffusion2_var(const double *field, double *deltas, const double *ratesX, const double *ratesY,
                            int32_t xDim, int32_t yDim, int wrapX, int wrapY);
 

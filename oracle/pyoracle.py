@@ -116,6 +116,8 @@ class Oracle(_Lib):
                                             i32, vp, vp, vp, vp]
         L.oracle_dadi_loss_grad.restype = f64
         L.oracle_sum_forces.argtypes = [vp, vp, i32, vp, vp, vp, f64, ci, f64, f64, ci, i32, i32, ci, ci]
+        L.oracle_pdegrid_script.argtypes = [i32, i32, ci, ci, vp, vp, vp, i32, vp, vp, vp, vp, vp]
+        L.oracle_pdegrid_script.restype = ci
         L.oracle_rand_init.argtypes = [vp, ctypes.c_uint64]
         L.oracle_rand_double.argtypes = [vp]
         L.oracle_rand_double.restype = f64
@@ -210,6 +212,19 @@ class Oracle(_Lib):
                                     out.ctypes.data, sums.ctypes.data, R, int(law), float(scale), float(exponent),
                                     int(order), xDim, yDim, int(wrapX), int(wrapY))
         return out, sums[:n]
+
+    @classmethod
+    def pdegrid_script(cls, script, field, deltas=None, update_ct=0):
+        """Runs a PDEScript on a PDEGrid2D in the given state; returns
+        (field, deltas, updateCt, records)."""
+        f, d, uc, args = script.prepare(field, deltas, update_ct)
+        n = cls.lib().oracle_pdegrid_script(script.xDim, script.yDim, int(script.wrapX), int(script.wrapY),
+                                            f.ctypes.data, d.ctypes.data, ctypes.addressof(uc), *args)
+        if n == -1:
+            raise ValueError("Diffusion rate above stable maximum value of 0.25")
+        if n == -2:
+            raise ValueError("Advection rate component sum above stable maximum value of 0.5")
+        return f, d, uc.value, script.records[:n].copy()
 
     @classmethod
     def agent_bins(cls, positions, xDim, yDim):
@@ -364,6 +379,7 @@ class Reference(_Lib):
         L.ref_pdegrid2d_load.argtypes = [ctypes.c_char_p, vp, vp, vp, vp, ctypes.c_int64]
         L.ref_advect_bc.argtypes = [vp, vp, f64, f64, i32, i32, ci, ci, vp]
         L.ref_sum_forces.argtypes = [vp, vp, vp, i32, i32, i32, ci, ci, f64, ci, f64, f64, vp, vp]
+        L.ref_pdegrid_script.argtypes = [i32, i32, ci, ci, vp, vp, vp, i32, vp, vp, vp, vp, vp, vp]
         L.ref_advect_var_bc.argtypes = [vp, vp, vp, vp, i32, i32, ci, ci, vp, vp, vp]
         for name in ("ref_diffuse", "ref_diffuse_bc", "ref_diffuse_adi", "ref_diffuse_adi_bc",
                      "ref_pdegrid_run", "ref_accumulate_forces"):
@@ -403,6 +419,16 @@ class Reference(_Lib):
                                             yDim, int(wrapX), int(wrapY), g.ctypes.data, gx.ctypes.data,
                                             gy.ctypes.data))
         return d
+
+    @classmethod
+    def pdegrid_script(cls, script, field, deltas=None, update_ct=0):
+        """The same script on the reference's own Hal::PDEGrid2D."""
+        f, d, uc, args = script.prepare(field, deltas, update_ct)
+        nrec = ctypes.c_int32(0)
+        _ok(cls.lib().ref_pdegrid_script(script.xDim, script.yDim, int(script.wrapX), int(script.wrapY),
+                                         f.ctypes.data, d.ctypes.data, ctypes.addressof(uc), *args,
+                                         ctypes.addressof(nrec)))
+        return f, d, uc.value, script.records[:nrec.value].copy()
 
     @classmethod
     def sum_forces(cls, positions, radii, R, law, scale, xDim, yDim, wrapX, wrapY, vel=None, exponent=1.0):
@@ -526,3 +552,75 @@ class Reference(_Lib):
         out = np.zeros(n, dtype=np.float64)
         cls.lib().ref_rand_draws(seed, kind, bound, n, out.ctypes.data)
         return out
+
+
+class PDEScript:
+    """A sequence of Hal::PDEGrid2D calls on one grid, in the encoding of
+    oracle_pdegrid_script (hal_oracle.h): the oracle, the reference library
+    and the device handle all run the same script.  Each method appends one
+    call; `calls` keeps them as (name, args) for runners that replay them."""
+
+    OPS = {"set": 0, "add": 1, "mul": 2, "scale": 3, "set_all": 10, "add_all": 11, "mul_all": 12,
+           "set_all_values": 13, "diffusion": 20, "diffusion_bc": 21, "diffusion_var": 22, "adi": 30,
+           "adi_bc": 31, "advection": 40, "advection_bc": 41, "advection_var": 42, "advection_var_bc": 43,
+           "update": 50, "set_non_negative": 51, "get": 60, "max": 61, "min": 62, "avg": 63, "max_delta": 64,
+           "max_delta_scaled": 65, "gradient_x": 66, "gradient_y": 67, "gradient_x_bc": 68, "gradient_y_bc": 69}
+
+    def __init__(self, xDim, yDim, wrapX=False, wrapY=False):
+        self.xDim, self.yDim, self.wrapX, self.wrapY = xDim, yDim, bool(wrapX), bool(wrapY)
+        self.calls = []
+
+    def encoded(self):
+        """(ops, iargs, dargs, arrays) of the script, for storing it."""
+        self.prepare(np.zeros(self.xDim * self.yDim), None, 0)
+        return self._keep
+
+    @classmethod
+    def from_encoded(cls, xDim, yDim, wrapX, wrapY, ops, iargs, dargs, arrays):
+        """The script that `encoded` stored."""
+        sc = cls(int(xDim), int(yDim), bool(wrapX), bool(wrapY))
+        names = {v: k for k, v in cls.OPS.items()}
+        n, g = sc.xDim * sc.yDim, 2 * (sc.xDim + sc.yDim)
+        sizes = {13: [n], 21: [g], 31: [g], 41: [g], 22: [n, n], 42: [n, n], 43: [n, n, g, g, g]}
+        for k, op in enumerate(ops):
+            op = int(op)
+            off = int(iargs[3 * k])
+            arrs = None
+            if op in sizes:
+                arrs = []
+                for m in sizes[op]:
+                    arrs.append(np.array(arrays[off: off + m]))
+                    off += m
+            i_or_x, y = int(iargs[3 * k + 1]), int(iargs[3 * k + 2])
+            grad = names[op].startswith("gradient")
+            sc.add(names[op], i=0 if grad else i_or_x, x=i_or_x if grad else 0, y=y, d0=float(dargs[2 * k]),
+                   d1=float(dargs[2 * k + 1]), arrays=arrs)
+        return sc
+
+    def add(self, name, i=0, x=0, y=0, d0=0.0, d1=0.0, arrays=None):
+        self.calls.append((name, dict(i=i, x=x, y=y, d0=d0, d1=d1, arrays=arrays)))
+        return self
+
+    def prepare(self, field, deltas, update_ct):
+        n = self.xDim * self.yDim
+        f = np.array(field, dtype=np.float64).copy()
+        d = np.zeros(n) if deltas is None else np.array(deltas, dtype=np.float64).copy()
+        ops = np.array([self.OPS[c] for c, _ in self.calls], dtype=np.int32)
+        iargs = np.zeros(3 * max(len(self.calls), 1), dtype=np.int32)
+        dargs = np.zeros(2 * max(len(self.calls), 1))
+        chunks, off = [], 0
+        for k, (name, a) in enumerate(self.calls):
+            if a["arrays"] is not None:
+                arr = np.concatenate([np.asarray(v, dtype=np.float64).ravel() for v in a["arrays"]])
+                iargs[3 * k] = off
+                chunks.append(arr)
+                off += arr.size
+            iargs[3 * k + 1] = a["x"] if name.startswith("gradient") else a["i"]
+            iargs[3 * k + 2] = a["y"]
+            dargs[2 * k], dargs[2 * k + 1] = a["d0"], a["d1"]
+        arrays = np.concatenate(chunks) if chunks else np.zeros(1)
+        self.records = np.zeros(max(len(self.calls), 1))
+        self._keep = (ops, iargs, dargs, arrays)
+        uc = ctypes.c_int32(update_ct)
+        return f, d, uc, (len(self.calls), ops.ctypes.data, iargs.ctypes.data, dargs.ctypes.data,
+                          arrays.ctypes.data, self.records.ctypes.data)

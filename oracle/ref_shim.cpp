@@ -249,6 +249,74 @@ extern "C"
             } });
     }
 
+    // A script of calls on the reference's own Hal::PDEGrid2D, in the
+    // encoding of oracle_pdegrid_script (hal_oracle.h): the grid starts in
+    // the given state, every call runs in order, query results go to
+    // records, and the final state is written back.  Returns the number of
+    // records through nRec.
+    int ref_pdegrid_script(int32_t xDim, int32_t yDim, int wrapX, int wrapY, double *field, double *deltas,
+                           int32_t *updateCt, int32_t nOps, const int32_t *ops, const int32_t *iargs,
+                           const double *dargs, const double *arrays, double *records, int32_t *nRec)
+    {
+        Quiet();
+        return Guard([&]()
+                     {
+            const size_t length = static_cast<size_t>(xDim) * static_cast<size_t>(yDim);
+            Hal::PDEGrid2D grid(xDim, yDim, wrapX != 0, wrapY != 0);
+            grid.SetState(std::vector<double>(field, field + length), std::vector<double>(deltas, deltas + length),
+                          *updateCt);
+            const int32_t g = 2 * (xDim + yDim);
+            int32_t r = 0;
+            for (int32_t k = 0; k < nOps; k++)
+            {
+                const int32_t *ia = iargs + 3 * static_cast<size_t>(k);
+                const double *da = dargs + 2 * static_cast<size_t>(k);
+                const double *arr = arrays + ia[0];
+                const std::vector<double> a0(arr, arr + length);
+                switch (ops[k])
+                {
+                case 0: grid.Set(ia[1], da[0]); break;
+                case 1: grid.Add(ia[1], da[0]); break;
+                case 2: grid.Mul(ia[1], da[0]); break;
+                case 3: grid.Scale(ia[1], da[0]); break;
+                case 10: grid.SetAll(da[0]); break;
+                case 11: grid.AddAll(da[0]); break;
+                case 12: grid.MulAll(da[0]); break;
+                case 13: grid.SetAll(arr); break;
+                case 20: grid.Diffusion(da[0]); break;
+                case 21: grid.Diffusion(da[0], GhostBc{arr, xDim, yDim}); break;
+                case 22: grid.Diffusion(a0, std::vector<double>(arr + length, arr + 2 * length)); break;
+                case 30: grid.DiffusionADI(da[0]); break;
+                case 31: grid.DiffusionADI(da[0], GhostBc{arr, xDim, yDim}); break;
+                case 40: grid.Advection(da[0], da[1]); break;
+                case 41: grid.Advection(da[0], da[1], GhostBc{arr, xDim, yDim}); break;
+                case 42: grid.Advection(a0, std::vector<double>(arr + length, arr + 2 * length)); break;
+                case 43:
+                    grid.Advection(a0, std::vector<double>(arr + length, arr + 2 * length),
+                                   GhostBc{arr + 2 * length, xDim, yDim}, GhostBc{arr + 2 * length + g, xDim, yDim},
+                                   GhostBc{arr + 2 * length + 2 * g, xDim, yDim});
+                    break;
+                case 50: grid.Update(); break;
+                case 51: grid.SetNonNegative(); break;
+                case 60: records[r++] = grid.Get(ia[1]); break;
+                case 61: records[r++] = grid.GetMax(); break;
+                case 62: records[r++] = grid.GetMin(); break;
+                case 63: records[r++] = grid.GetAvg(); break;
+                case 64: records[r++] = grid.MaxDelta(); break;
+                case 65: records[r++] = grid.MaxDeltaScaled(da[0]); break;
+                case 66: records[r++] = grid.GradientX(ia[1], ia[2]); break;
+                case 67: records[r++] = grid.GradientY(ia[1], ia[2]); break;
+                case 68: records[r++] = grid.GradientX(ia[1], ia[2], da[0]); break;
+                case 69: records[r++] = grid.GradientY(ia[1], ia[2], da[0]); break;
+                default: throw std::runtime_error("unknown script op");
+                }
+            }
+            std::memcpy(field, grid.GetField().data(), sizeof(double) * length);
+            std::memcpy(deltas, grid.GetDeltas().data(), sizeof(double) * length);
+            *updateCt = grid.UpdateCt();
+            *nRec = r; });
+    }
+
     // Hal::SavePDEGrid2D of a grid in the given state, through BinaryWriter.
     int ref_pdegrid2d_save(const char *path, int32_t xDim, int32_t yDim, int wrapX, int wrapY, int32_t updateCt,
                            const double *field, const double *deltas)

@@ -7,8 +7,9 @@ Run in a tree where the reference sources exist (it builds
     python tests/golden/make_golden.py sumforces   # only the named ones
 
 Every output comes from Hal::CpuDiffusionBackend2D, Hal::CpuAdiDiffusionBackend2D,
-Hal::CpuAgentForceBackend2D, Hal::PDEGrid2D, Hal::SphericalAgent2D on the
-reference's agent grid or Hal::Rand, called through
+Hal::CpuAgentForceBackend2D, Hal::PDEGrid2D (single ticks and whole call
+sequences), Hal::SphericalAgent2D on the reference's agent grid or Hal::Rand,
+called through
 ``oracle/ref_shim.cpp``.  The inputs are stored beside the outputs, so the
 fixtures need no random generator to be replayed.  Cases restate the
 reference's own tests (eigenmode decay, the seed-1234 agent scene, Dirichlet
@@ -312,6 +313,73 @@ def sum_forces_cases(rng):
     return out
 
 
+def pdegrid_script(rng, xd, yd, wx, wy, cells_per_tick=6):
+    """A model-shaped call sequence on one PDEGrid2D: per-cell Set/Add/Mul/
+    Scale (repeated cells included) between explicit, Dirichlet, per-cell
+    rate and ADI diffusion and both advection forms, Update, the whole-grid
+    operations, SetNonNegative and every query."""
+    from pyoracle import PDEScript
+
+    n, g = xd * yd, 2 * (xd + yd)
+    sc = PDEScript(xd, yd, wx, wy)
+    cells = lambda k: rng.integers(0, n, k)
+    for tick in range(4):
+        for c in cells(cells_per_tick):
+            sc.add(["set", "add", "mul", "scale"][int(rng.integers(0, 4))], i=int(c), d0=float(rng.random() - 0.3))
+        hot = int(cells(1)[0])
+        for _ in range(3):  # one cell hit repeatedly: order matters
+            sc.add("mul", i=hot, d0=-0.001).add("add", i=hot, d0=0.02)
+        kind = tick % 4
+        if kind == 0:
+            sc.add("diffusion", d0=0.2).add("advection", d0=0.15, d1=-0.2)
+        elif kind == 1:
+            sc.add("adi", d0=float(0.5 + 4.5 * rng.random())).add("diffusion_bc", d0=0.1, arrays=[rng.random(g)])
+        elif kind == 2:
+            sc.add("adi_bc", d0=3.0, arrays=[rng.random(g)])
+            sc.add("diffusion_var", arrays=[rng.random(n) * 0.2, rng.random(n) * 0.2])
+            sc.add("advection_bc", d0=-0.1, d1=0.25, arrays=[rng.random(g)])
+        else:
+            sc.add("advection_var", arrays=[rng.random(n) - 0.5, rng.random(n) - 0.5])
+            sc.add("advection_var_bc", arrays=[rng.random(n) - 0.5, rng.random(n) - 0.5, rng.random(g),
+                                               rng.random(g) - 0.5, rng.random(g) - 0.5])
+            sc.add("mul_all", d0=-0.01)
+        sc.add("max_delta").add("max_delta_scaled", d0=1e-3)
+        if tick == 2:
+            sc.add("set_non_negative")
+        sc.add("update")
+        for c in cells(3):
+            sc.add("get", i=int(c))
+        sc.add("max").add("min").add("avg")
+        x, y = int(rng.integers(0, xd)), int(rng.integers(0, yd))
+        sc.add("gradient_x", x=x, y=y).add("gradient_y", x=x, y=y).add("gradient_x_bc", x=0, y=y, d0=1.0)
+        sc.add("gradient_y_bc", x=x, y=yd - 1, d0=-0.5)
+    sc.add("add_all", d0=0.01).add("set_all_values", arrays=[rng.random(n)]).add("set", i=0, d0=2.0)
+    sc.add("set_all", d0=0.25).add("update").add("max").add("min")
+    return sc
+
+
+def pdegrid_script_cases(rng):
+    """Hal::PDEGrid2D call sequences (include/Hal/Grids/PDEGrid2D.h) run on the
+    reference's own grid: the final field, deltas and update count and every
+    query result."""
+    out = {}
+    k = 0
+    for (xd, yd, wx, wy) in [(23, 17, 0, 0), (16, 24, 1, 1), (31, 9, 1, 0), (9, 31, 0, 1), (1, 6, 0, 0),
+                             (5, 1, 1, 0)]:
+        sc = pdegrid_script(rng, xd, yd, wx, wy)
+        f0 = rng.random(xd * yd)
+        d0 = (rng.random(xd * yd) - 0.5) * 1e-3
+        f, d, uc, rec = R.pdegrid_script(sc, f0, d0, 7)
+        ops, iargs, dargs, arrays = sc.encoded()
+        out[f"c{k}_dims"] = np.array([xd, yd, wx, wy], dtype=np.int32)
+        out.update({f"c{k}_ops": ops, f"c{k}_iargs": iargs, f"c{k}_dargs": dargs, f"c{k}_arrays": arrays,
+                    f"c{k}_f0": f0, f"c{k}_d0": d0, f"c{k}_field": f, f"c{k}_deltas": d,
+                    f"c{k}_uc": np.array([uc], dtype=np.int32), f"c{k}_records": rec})
+        k += 1
+    out["count"] = np.array([k])
+    return out
+
+
 def pdegrid_file():
     """A PDEGrid2D file written by the reference's SavePDEGrid2D
     (src/Grids/PDEGridSerialization.cpp:34-45): 13 x 7, wrapX only, update
@@ -331,7 +399,8 @@ def main():
     only = sys.argv[1:]
     if only:
         # write only the named fixtures (each has its own seed)
-        makers = {"sumforces": lambda: sum_forces_cases(np.random.default_rng(5353))}
+        makers = {"sumforces": lambda: sum_forces_cases(np.random.default_rng(5353)),
+                  "pdegrid": lambda: pdegrid_script_cases(np.random.default_rng(4242))}
         for name in only:
             np.savez_compressed(os.path.join(HERE, name + ".npz"), **makers[name]())
             print(os.path.join(HERE, name + ".npz"))
@@ -345,8 +414,10 @@ def main():
     np.savez_compressed(os.path.join(HERE, "agentmove.npz"), **agent_move_cases(np.random.default_rng(9191)))
     np.savez_compressed(os.path.join(HERE, "advtick.npz"), **adv_tick_cases(np.random.default_rng(6262)))
     np.savez_compressed(os.path.join(HERE, "sumforces.npz"), **sum_forces_cases(np.random.default_rng(5353)))
+    np.savez_compressed(os.path.join(HERE, "pdegrid.npz"), **pdegrid_script_cases(np.random.default_rng(4242)))
     print(pdegrid_file())
-    for name in ("stencil", "ticks", "agents", "rand", "varstencil", "agentmove", "advtick", "sumforces"):
+    for name in ("stencil", "ticks", "agents", "rand", "varstencil", "agentmove", "advtick", "sumforces",
+                 "pdegrid"):
         p = os.path.join(HERE, name + ".npz")
         print(f"{p}: {os.path.getsize(p)} bytes")
 

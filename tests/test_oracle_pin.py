@@ -416,3 +416,64 @@ def test_sum_forces_matches_reference_library_random(oracle):
             a = oracle.sum_forces(pos, rad, R_, law, scale, xd, yd, wx, wy, vel=vel, exponent=expo, order=1)
             b = R.sum_forces(pos, rad, R_, law, scale, xd, yd, wx, wy, vel=vel, exponent=expo)
             assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def _script_case(g, k):
+    from pyoracle import PDEScript
+
+    xd, yd, wx, wy = (int(v) for v in g[f"c{k}_dims"])
+    sc = PDEScript.from_encoded(xd, yd, wx, wy, g[f"c{k}_ops"], g[f"c{k}_iargs"], g[f"c{k}_dargs"],
+                                g[f"c{k}_arrays"])
+    return sc, g[f"c{k}_f0"], g[f"c{k}_d0"]
+
+
+def test_pdegrid_script_golden_bit_exact(oracle, golden):
+    """Whole Hal::PDEGrid2D call sequences (per-cell Set/Add/Mul/Scale,
+    explicit, Dirichlet, per-cell rate and ADI diffusion, both advection
+    forms, the whole-grid operations, SetNonNegative, Update and every query;
+    include/Hal/Grids/PDEGrid2D.h) written by the reference's own grid: the
+    restatement reproduces the final field and deltas, the update count and
+    every query result bit for bit."""
+    g = golden("pdegrid")
+    count = int(g["count"][0])
+    assert count == 6
+    for k in range(count):
+        sc, f0, d0 = _script_case(g, k)
+        f, d, uc, rec = oracle.pdegrid_script(sc, f0, d0, 7)
+        assert np.array_equal(f, g[f"c{k}_field"]), k
+        assert np.array_equal(d, g[f"c{k}_deltas"]), k
+        assert uc == int(g[f"c{k}_uc"][0]) == 12
+        assert np.array_equal(rec, g[f"c{k}_records"]), k
+
+
+def test_pdegrid_script_rate_checks(oracle):
+    from pyoracle import PDEScript
+
+    f0 = np.zeros(12)
+    with pytest.raises(ValueError, match="Diffusion rate above stable maximum value of 0.25"):
+        oracle.pdegrid_script(PDEScript(3, 4).add("diffusion", d0=0.3), f0)
+    with pytest.raises(ValueError, match="Advection rate component sum above stable maximum value of 0.5"):
+        oracle.pdegrid_script(PDEScript(3, 4).add("advection", d0=0.3, d1=-0.25), f0)
+
+
+@pytest.mark.skipif(not pyoracle.Reference.available() and not __import__("os").path.isdir(
+    pyoracle.REF_TREE), reason="reference tree not present")
+def test_pdegrid_script_matches_reference_library_random(oracle):
+    pyoracle.build(ref=True)
+    import importlib.util
+    import os
+
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(os.path.dirname(__file__), "golden",
+                                                                             "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    rng = np.random.default_rng(515)
+    for _ in range(4):
+        xd, yd = (int(v) for v in rng.integers(1, 30, 2))
+        wx, wy = (bool(v) for v in rng.integers(0, 2, 2))
+        sc = mg.pdegrid_script(rng, xd, yd, wx, wy)
+        f0 = rng.random(xd * yd)
+        a = oracle.pdegrid_script(sc, f0)
+        b = pyoracle.Reference.pdegrid_script(sc, f0)
+        assert all(np.array_equal(x, y) for x, y in zip(a[:2], b[:2])) and a[2] == b[2]
+        assert np.array_equal(a[3], b[3])
