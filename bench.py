@@ -499,8 +499,14 @@ def secondary_wells(hal, torch, stream, ticks=20, plain_ticks=3):
     peak, _ = peaks()
     ach = bytes_tick / (ms_batched * 1e-3) / 1e9
     cells = cells_exp + cells_adi
+    cpu_cells, cpu_agents, cpu_s, cpu_threads = cpu_baseline_wells()
     return {"workload": "wells-512-side64..1024-explicit+adi-agents0..20000",
             "value": cells / (ms_batched * 1e-3), "unit": "cell-updates/s",
+            "cpu_baseline": {"value": cpu_cells, "unit": "cell-updates/s", "agents_per_s": cpu_agents,
+                             "ms_per_tick": cpu_s * 1e3, "cores": cpu_threads, "kind": "port",
+                             "sample": "one FP64 tick of all 512 wells (explicit or ADI tick with decay, and the "
+                                       "agent force pass) with the wells spread over every host thread, as "
+                                       "MultiWellExperiment::StepMultiThread does (oracle)"},
             "agents_per_s": n_ag / (ms_batched * 1e-3),
             "ms_per_tick_batched": ms_batched, "ms_per_tick_per_well_launches": ms_plain,
             "speedup_vs_per_well_launches": ms_plain / ms_batched,
@@ -579,6 +585,84 @@ def secondary_stencil64(hal, torch, stream, iters=20):
                     "(wall clock, copies in and out); cpu = the oracle, 1 thread"}
 
 
+def secondary_interface_calls(timeout=600):
+    """Per-call times of Diffuse, DiffuseADI and AccumulateForces through the
+    C++ backend classes on host std::vector<double> data (upload, kernels and
+    readback in every call), beside the single-threaded CPU oracle on the same
+    call: the counterpart of the reference's examples/BackendBenchmark.cpp
+    sections 1 and 4 (hal-cpp_gb300/cpp/tests/interface_bench.cpp)."""
+    exe = os.path.join(ROOT, "hal-cpp_gb300", "_build", "cpp", "interface_bench")
+    if not os.path.exists(exe):
+        return {"unavailable": "interface_bench not built (hal-cpp_gb300/cpp/build_cpp.py)"}
+    res = subprocess.run([exe], capture_output=True, text=True, timeout=timeout)
+    if res.returncode != 0:
+        return {"unavailable": f"interface_bench exited {res.returncode}: {res.stderr[-300:]}"}
+    rows = [json.loads(line) for line in res.stdout.splitlines() if line.startswith("{")]
+    return {"calls": rows, "cpu": "oracle (the reference CPU backends restated), 1 thread",
+            "note": "one call per interface invocation; GPU times include the host-device copies"}
+
+
+def cpu_baseline_wells(threads=None, ticks=1):
+    """MultiWellExperiment::StepMultiThread (include/Hal/Tools/
+    MultiWellExperiment.h:95-103) on the host: each of the 512 wells' FP64
+    tick (explicit or ADI, with decay) and agent force pass, the wells spread
+    over all host threads (Hal::MultiThread, include/Hal/Concurrency/
+    MultiThread.h:83-91); returns (cell-updates/s, agents/s, s per tick)."""
+    import concurrent.futures as cf
+
+    from halcuda import workloads
+
+    O = _oracle()
+    threads = threads or os.cpu_count() or 1
+    w = workloads.wells_inputs()
+    starts = np.concatenate([[0], np.cumsum(w["counts"])]).astype(np.int64)
+    fields = [f.astype(np.float64) for f in w["fields"]]
+    pos64 = w["positions"].astype(np.float64)
+    rad64 = w["radii"].astype(np.float64)
+
+    def step(i):
+        d = w["wells"][i]
+        fields[i] = O.run_ticks(1 if d["kind"] == "adi" else 0, fields[i], d["xDim"], d["yDim"], d["diffRate"],
+                                decay=d["decay"], ticks=1)
+        a, e = int(starts[i]), int(starts[i + 1])
+        if e > a:
+            O.accumulate_forces(pos64[2 * a: 2 * e], rad64[a:e], w["interactionRad"], w["springConstant"],
+                                d["xDim"], d["yDim"], False, False)
+
+    order = sorted(range(len(w["wells"])), key=lambda i: -w["wells"][i]["xDim"] * w["wells"][i]["yDim"])
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(step, order))  # warm-up tick
+        t0 = time.perf_counter()
+        for _ in range(ticks):
+            list(ex.map(step, order))
+        dt = (time.perf_counter() - t0) / ticks
+    cells = sum(d["xDim"] * d["yDim"] for d in w["wells"])
+    return cells / dt, int(w["counts"].sum()) / dt, dt, threads
+
+
+def cpu_baseline_adjoint(steps=20, n=512):
+    """The FP64 CPU forward and reverse-mode gradient of the variable-rate ADI
+    model (the oracle's restatement) on the workload's 512^2 grid, over a
+    bounded number of steps; returns (ms per forward step, ms per gradient
+    step, their ratio)."""
+    from halcuda import workloads
+
+    O = _oracle()
+    w = workloads.adjoint_inputs(n)
+    f0 = w["f0"].astype(np.float64)
+    D = w["D"].astype(np.float64)
+    src = w["src"].astype(np.float64)
+    t0 = time.perf_counter()
+    f = f0
+    for _ in range(steps):
+        f, _ = O.dadi_step(f, D, n, n, decay=w["decay"], src=src)
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.dadi_loss_grad(f0, np.zeros_like(f0), D, w["decay"], src, n, n, steps)
+    t_grad = time.perf_counter() - t0
+    return 1e3 * t_fwd / steps, 1e3 * t_grad / steps, t_grad / t_fwd
+
+
 def secondary_adjoint(hal, directions=None):
     """Parameter recovery on 512^2: the gradient of the field misfit after 500
     variable-rate ADI steps (checkpoints every 22) with respect to D(x), decay
@@ -622,8 +706,14 @@ def secondary_adjoint(hal, directions=None):
             dd = float(g64 @ v.astype(np.float64))
             errs.append(abs(f1 - dd) / max(abs(dd), 1e-30))
             ok += abs(f1 - dd) <= 2e-2 * abs(dd) + 3 * abs(f1 - f2)
+    cpu_fwd, cpu_grad, cpu_ratio = cpu_baseline_adjoint()
     return {"workload": "adjoint-512x512-500steps-ckpt22-D0.5..5-decay0.005",
             "value": ms_grad / ms_fwd, "unit": "t(gradient)/t(forward)", "higher_is_better": False,
+            "cpu_baseline": {"ms_per_forward_step": cpu_fwd, "ms_per_gradient_step": cpu_grad,
+                             "ratio": cpu_ratio, "cores": 1, "kind": "port",
+                             "gpu_ms_per_forward_step": ms_fwd / steps, "gpu_ms_per_gradient_step": ms_grad / steps,
+                             "sample": "20 FP64 steps of the same 512x512 model: the forward, then the loss and "
+                                       "its reverse-mode gradient with every state kept (oracle, 1 thread)"},
             "ms_forward": ms_fwd, "ms_gradient": ms_grad, "loss": loss,
             "keep_all_states": {"ms_gradient": ms_keep, "ratio": ms_keep / ms_fwd,
                                 "gradient_bit_identical": keep_equal,
@@ -866,7 +956,8 @@ def main():
                      "coupled": secondary_coupled(hal, torch, stream),
                      "wells": secondary_wells(hal, torch, stream),
                      "adjoint": secondary_adjoint(hal),
-                     "stencil64": secondary_stencil64(hal, torch, stream)}
+                     "stencil64": secondary_stencil64(hal, torch, stream),
+                     "interface_calls": secondary_interface_calls()}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -10,6 +10,9 @@
 * hal-cpp_gb300/_build/cpp/backend_tests -- the test driver
   (tests/backend_tests.cpp), which also links the CPU oracle
   (oracle/liboracle.so) as its checker;
+* hal-cpp_gb300/_build/cpp/interface_bench -- per-call times of the three
+  interfaces against the CPU oracle (tests/interface_bench.cpp, run by
+  bench.py);
 * with --hal-include DIR (a HAL-CPP include directory): the backend classes
   are also compiled, syntax and types only, against HAL's own interface
   headers, which shows they drop in unchanged.
@@ -32,6 +35,7 @@ ORACLE = os.path.join(ROOT, "oracle")
 OUT_DIR = os.path.join(PKG, "_build", "cpp")
 LIB = os.path.join(PKG, "libhal_cuda_cpp.so")
 TEST_BIN = os.path.join(OUT_DIR, "backend_tests")
+BENCH_BIN = os.path.join(OUT_DIR, "interface_bench")
 CXXFLAGS = ["-std=c++20", "-O2", "-Wall", "-Wextra", "-fPIC"]
 
 
@@ -62,10 +66,11 @@ def build_tests():
     oracle_so = os.path.join(ORACLE, "liboracle.so")
     if not os.path.exists(oracle_so):
         raise RuntimeError("oracle/liboracle.so is missing: build the oracle first")
-    _run([_cxx()] + CXXFLAGS + ["-o", TEST_BIN, os.path.join(HERE, "tests", "backend_tests.cpp"),
-          "-I", os.path.join(HERE, "include"), "-I", os.path.join(HERE, "compat"), "-I", INCLUDE,
-          "-I", ORACLE, "-L", PKG, "-lhal_cuda_cpp", "-lhal_cuda", "-L", ORACLE, "-loracle",
-          "-Wl,-rpath," + PKG + ":" + ORACLE])
+    for src, out in (("backend_tests.cpp", TEST_BIN), ("interface_bench.cpp", BENCH_BIN)):
+        _run([_cxx()] + CXXFLAGS + ["-o", out, os.path.join(HERE, "tests", src),
+              "-I", os.path.join(HERE, "include"), "-I", os.path.join(HERE, "compat"), "-I", INCLUDE,
+              "-I", ORACLE, "-L", PKG, "-lhal_cuda_cpp", "-lhal_cuda", "-L", ORACLE, "-loracle",
+              "-Wl,-rpath," + PKG + ":" + ORACLE])
     return TEST_BIN
 
 

@@ -364,6 +364,142 @@ namespace halcuda
             sRad[slot] = rad[i];
         }
 
+        // ---- the single-grid dispatch's binning -----------------------------
+        // BinCountTiles: as BinCount, and each agent also counts itself in its
+        // cell's scan tile (tileSums, zero on entry), so the scan needs no
+        // reduce pass over the counts.  Lanes of a warp that hit the same
+        // tile add their count once.
+        template <typename TP>
+        __global__ void BinCountTiles(const TP *__restrict__ pos, int32_t n, int32_t xDim, int32_t yDim,
+                                      int32_t *__restrict__ cellOf, int32_t *__restrict__ arrival,
+                                      int32_t *__restrict__ counts, int32_t *__restrict__ tileSums)
+        {
+            ChainEntry();
+            const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+            const bool live = i < n;
+            int32_t c = 0;
+            if (live)
+            {
+                const TP px = pos[2 * static_cast<int64_t>(i)];
+                const TP py = pos[2 * static_cast<int64_t>(i) + 1];
+                c = CellCoord(px, xDim) * yDim + CellCoord(py, yDim);
+                cellOf[i] = c;
+                arrival[i] = atomicAdd(counts + c, 1);
+            }
+            const int32_t tile = live ? c / kScanTile : -1;
+            const unsigned peers = __match_any_sync(0xffffffffu, tile);
+            const int lane = threadIdx.x & 31;
+            if (live && lane == __ffs(peers) - 1)
+            {
+                atomicAdd(tileSums + tile, __popc(peers));
+            }
+        }
+
+        // ScanApply for tile sums that came from the binning: the tile's
+        // prefix is read, then reset to zero for the next binning (only this
+        // CTA reads it), along with the counts it has read.
+        __global__ void __launch_bounds__(kScanThreads) ScanApplyTiles(int32_t *__restrict__ counts, int64_t C,
+                                                                       int32_t *__restrict__ tilePrefix,
+                                                                       int32_t *__restrict__ offsets, int32_t n)
+        {
+            ChainEntry();
+            const int64_t base = static_cast<int64_t>(blockIdx.x) * kScanTile + threadIdx.x * kScanItems;
+            int32_t v[kScanItems];
+            LoadItems(counts, base, C, v);
+            int32_t any = 0;
+#pragma unroll
+            for (int q = 0; q < kScanItems; q++)
+            {
+                any |= v[q];
+            }
+            if (any != 0)
+            {
+                const int32_t zeros[kScanItems] = {0, 0, 0, 0};
+                StoreItems(counts, base, C, zeros);
+            }
+            int32_t sum = 0;
+#pragma unroll
+            for (int q = 0; q < kScanItems; q++)
+            {
+                sum += v[q];
+            }
+            const int32_t prefix = tilePrefix[blockIdx.x];
+            int32_t excl;
+            BlockExclusiveScan(sum, excl);  // its barriers order the prefix read before the reset
+            if (threadIdx.x == 0)
+            {
+                tilePrefix[blockIdx.x] = 0;
+            }
+            int32_t o[kScanItems];
+            o[0] = prefix + excl;
+#pragma unroll
+            for (int q = 1; q < kScanItems; q++)
+            {
+                o[q] = o[q - 1] + v[q - 1];
+            }
+            StoreItems(offsets, base, C, o);
+            if (blockIdx.x == 0 && threadIdx.x == 0)
+            {
+                offsets[C] = n;
+            }
+        }
+
+        // Scatter in agent order: agent i's position, radius and index go to
+        // slot offsets[cell] + arrival rank of the arrival-ordered copies.
+        // The agent-order reads are coalesced; only the writes scatter.
+        template <typename TP, typename TR>
+        __global__ void ScatterAgents(const int32_t *__restrict__ cellOf, const int32_t *__restrict__ arrival,
+                                      const int32_t *__restrict__ offsets, const V2<TP> *__restrict__ pos,
+                                      const TR *__restrict__ rad, int32_t n, int32_t *__restrict__ bucketTmp,
+                                      V2<TP> *__restrict__ posTmp, TR *__restrict__ radTmp)
+        {
+            ChainEntry();
+            const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+            if (i >= n)
+            {
+                return;
+            }
+            const int32_t q = offsets[cellOf[i]] + arrival[i];
+            bucketTmp[q] = i;
+            posTmp[q] = pos[i];
+            radTmp[q] = rad[i];
+        }
+
+        // Stable order within each cell (the CPU's scatter in agent index
+        // order, CpuAgentForceBackend2D.cpp:100-109): the agent at
+        // arrival-order slot q goes to slot s + (number of lower-indexed
+        // agents of its cell).  Everything is read in slot order: the cell
+        // again from the position, the cell's range of arrival-ordered
+        // indices (shared by neighbouring threads), and the writes land
+        // within the cell's own slots.
+        template <typename TP, typename TR>
+        __global__ void StabilizeSlots(const int32_t *__restrict__ offsets, const int32_t *__restrict__ bucketTmp,
+                                       const V2<TP> *__restrict__ posTmp, const TR *__restrict__ radTmp, int32_t n,
+                                       int32_t xDim, int32_t yDim, int32_t *__restrict__ bucket,
+                                       V2<TP> *__restrict__ sPos, TR *__restrict__ sRad)
+        {
+            ChainEntry();
+            const int32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+            if (q >= n)
+            {
+                return;
+            }
+            const int32_t i = bucketTmp[q];
+            const V2<TP> p = posTmp[q];
+            const int32_t c = CellCoord(p.x, xDim) * yDim + CellCoord(p.y, yDim);
+            const int32_t s = offsets[c];
+            const int32_t e = offsets[c + 1];
+            int32_t rank = 0;
+            for (int32_t t = s; t < e; t++)
+            {
+                rank += (bucketTmp[t] < i) ? 1 : 0;
+            }
+            const int32_t slot = s + rank;
+            bucket[slot] = i;
+            sPos[slot] = p;
+            sRad[slot] = radTmp[q];
+        }
+
         // IEEE-exact FP64 helpers (no contraction) and their FP32 twins.
         __device__ __forceinline__ double Add(double a, double b) { return __dadd_rn(a, b); }
         __device__ __forceinline__ double Sub(double a, double b) { return __dsub_rn(a, b); }
@@ -928,6 +1064,10 @@ namespace halcuda
         DevBuf<float> sRad32;
         DevBuf<double> sRad64;
         DevBuf<int32_t> cellOf, arrival, counts, offsets, tileSums, bucketTmp, bucket;
+        DevBuf<float2> posTmp32;  // arrival-ordered copies of the binning (FP32 path)
+        DevBuf<float> radTmp32;
+        DevBuf<double2> posTmpD;  // the same, FP64 path
+        DevBuf<double> radTmp64;
         DevBuf<float> sums32;    // per-agent sums of positive forces (FP32 path)
         DevBuf<double> sums64;   // the same, FP64 path
         bool sumsValid = false;  // sums32 holds the last dispatch's or step's sums
@@ -959,6 +1099,9 @@ namespace halcuda
             HAL_TRY(offsets.Alloc(static_cast<size_t>(C) + 1, "cudaMalloc(bins)"));
             nTiles = static_cast<int32_t>((C + kScanTile - 1) / kScanTile);
             HAL_TRY(tileSums.Alloc(static_cast<size_t>(nTiles), "cudaMalloc(bins)"));
+            HAL_TRY(CudaStatus(cudaMemset(tileSums.p, 0, static_cast<size_t>(nTiles) * sizeof(int32_t)), "cudaMemset"));
+            HAL_TRY(posTmp32.Alloc(m, "cudaMalloc(agents)"));
+            HAL_TRY(radTmp32.Alloc(m, "cudaMalloc(agents)"));
             HAL_TRY(CudaStatus(cudaMemset(offsets.p, 0, (static_cast<size_t>(C) + 1) * sizeof(int32_t)), "cudaMemset"));
             return HAL_CUDA_OK;
         }
@@ -973,48 +1116,44 @@ namespace halcuda
         template <typename TP, typename TR>
         int Bin(const TP *pos, const TR *rad, TR *sRad, cudaStream_t s, cudaEvent_t *ev = nullptr)
         {
-            const bool clearInScan = C <= kClearInScanCells;
-            if (countsDirty || !clearInScan)
+            if (countsDirty)
             {
-                // large counts, or a previous binning stopped before its scan
-                // cleared them
+                // a previous binning stopped before its scan cleared the
+                // counts and the tile sums
                 HAL_TRY(CudaStatus(cudaMemsetAsync(counts.p, 0, static_cast<size_t>(C) * sizeof(int32_t), s),
                                    "cudaMemsetAsync(counts)"));
+                HAL_TRY(CudaStatus(cudaMemsetAsync(tileSums.p, 0, static_cast<size_t>(nTiles) * sizeof(int32_t), s),
+                                   "cudaMemsetAsync(tile sums)"));
             }
             countsDirty = true;
             const int T = 256;
             unsigned ablocks = static_cast<unsigned>((n + T - 1) / T);
             if (n > 0)
             {
-                // pos is the handle's own device buffer (cudaMalloc'd, so
-                // aligned for V2<TP>): the stabilize pass reads it directly
-                LaunchChained(BinCount<TP>, ablocks, T, s, pos, n, xDim, yDim, static_cast<V2<TP> *>(nullptr),
-                              cellOf.p, arrival.p, counts.p);
+                LaunchChained(BinCountTiles<TP>, ablocks, T, s, pos, n, xDim, yDim, cellOf.p, arrival.p, counts.p,
+                              tileSums.p);
                 CountLaunch();
             }
             if (ev)
             {
                 cudaEventRecord(ev[0], s);
             }
-            LaunchChained(ScanReduce, nTiles, kScanThreads, s, counts.p, C, tileSums.p);
             LaunchChained(ScanTiles, 1u, kScanThreads, s, tileSums.p, nTiles);
-            if (clearInScan)
-            {
-                LaunchChained(ScanApply<true>, nTiles, kScanThreads, s, counts.p, C, tileSums.p, offsets.p, n);
-            }
-            else
-            {
-                LaunchChained(ScanApply<false>, nTiles, kScanThreads, s, counts.p, C, tileSums.p, offsets.p, n);
-            }
-            CountLaunch(3);
-            countsDirty = !clearInScan || (cudaPeekAtLastError() != cudaSuccess);
+            LaunchChained(ScanApplyTiles, nTiles, kScanThreads, s, counts.p, C, tileSums.p, offsets.p, n);
+            CountLaunch(2);
+            countsDirty = (cudaPeekAtLastError() != cudaSuccess);
             if (ev)
             {
                 cudaEventRecord(ev[1], s);
             }
+            V2<TP> *posTmp = TmpPosBuf(TP());
+            TR *radTmp = TmpRadBuf(TR());
             if (n > 0)
             {
-                LaunchChained(Scatter, ablocks, T, s, cellOf.p, arrival.p, offsets.p, n, bucketTmp.p);
+                // pos is the handle's own device buffer (cudaMalloc'd, so
+                // aligned for V2<TP>)
+                LaunchChained(ScatterAgents<TP, TR>, ablocks, T, s, cellOf.p, arrival.p, offsets.p,
+                              reinterpret_cast<const V2<TP> *>(pos), rad, n, bucketTmp.p, posTmp, radTmp);
                 CountLaunch();
             }
             if (ev)
@@ -1023,8 +1162,8 @@ namespace halcuda
             }
             if (n > 0)
             {
-                LaunchChained(Stabilize<TP, TR>, ablocks, T, s, cellOf.p, offsets.p, bucketTmp.p,
-                              reinterpret_cast<const V2<TP> *>(pos), rad, n, bucket.p, SortedPosBuf(TP()), sRad);
+                LaunchChained(StabilizeSlots<TP, TR>, ablocks, T, s, offsets.p, bucketTmp.p, posTmp, radTmp, n, xDim,
+                              yDim, bucket.p, SortedPosBuf(TP()), sRad);
                 CountLaunch();
             }
             if (ev)
@@ -1033,6 +1172,11 @@ namespace halcuda
             }
             return LaunchStatus("agent binning");
         }
+
+        V2<float> *TmpPosBuf(float) { return posTmp32.p; }
+        V2<double> *TmpPosBuf(double) { return posTmpD.p; }
+        float *TmpRadBuf(float) { return radTmp32.p; }
+        double *TmpRadBuf(double) { return radTmp64.p; }
 
         // Pass 4 with force law `law`: velocity deltas (from zero, or from
         // velIn) into vel, and with law.sums each agent's sum of positive
@@ -1247,6 +1391,8 @@ namespace
             HAL_TRY(h->rad64.Alloc(m, "cudaMalloc(agents64)"));
             HAL_TRY(h->vel64.Alloc(2 * m, "cudaMalloc(agents64)"));
             HAL_TRY(h->sRad64.Alloc(m, "cudaMalloc(agents64)"));
+            HAL_TRY(h->posTmpD.Alloc(m, "cudaMalloc(agents64)"));
+            HAL_TRY(h->radTmp64.Alloc(m, "cudaMalloc(agents64)"));
             HAL_TRY(h->sPosD.Alloc(m, "cudaMalloc(agents64)"));
         }
         return HAL_CUDA_OK;

@@ -9,7 +9,8 @@ every call bit for bit:
   (tests/golden/pdegrid.npz) replayed through the C ABI, the per-cell
   operations sent one call each and, separately, batched into one list
   between operators: final field, deltas, update count and every query
-  result equal (GetAvg within 1e-14: a parallel sum);
+  result equal (GetAvg within the reference's own summation error bound,
+  n * eps relative: a parallel sum);
 * random sequences on larger grids against the oracle (which is pinned to the
   reference by tests/test_oracle_pin.py), explicit and ADI diffusion on one
   field, every boundary kind;
@@ -98,12 +99,16 @@ def _avg_positions(script):
 
 
 def _check_records(got, exp, script):
+    """Every query bit-exact, except GetAvg: the reference sums the n cells
+    one after another, whose rounding error is bounded by n * eps relative
+    (the device's blocked sum is more accurate than that)."""
     avg = _avg_positions(script)
     exact = np.ones(exp.size, bool)
     exact[avg] = False
     assert np.array_equal(got[exact], exp[exact])
     if avg:
-        assert np.allclose(got[avg], exp[avg], rtol=1e-14, atol=0)
+        n = script.xDim * script.yDim
+        assert np.allclose(got[avg], exp[avg], rtol=n * np.finfo(np.float64).eps, atol=0)
 
 
 @pytest.mark.parametrize("batch", [False, True])
