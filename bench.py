@@ -760,11 +760,31 @@ def profile_case(case, n, iters):
     elif case == "agents":
         agents = max(1, int(1_000_000 * (n / 2048) ** 2))
         w = workloads.agent_inputs(agents, n, seed=3)
+        import torch
+
         with hal.Agents(n, n, agents) as ag:
             ag.upload(w["positions"], w["radii"])
             ag.profile(1, 1.0, 0.1)
             ms = ag.profile(iters, 1.0, 0.1)
-        print(f"agents {agents} in {n}^2: " + ", ".join(f"{v*1e3:.1f}" for v in ms) + " us")
+            # back-to-back dispatches (chained launches, no events between stages)
+            st = torch.cuda.ExternalStream(ag.stream())
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ag.dispatch(1.0, 0.1)
+            e0.record(st)
+            for _ in range(iters):
+                ag.dispatch(1.0, 0.1)
+            e1.record(st)
+            e1.synchronize()
+            chained = e0.elapsed_time(e1) / iters
+            ag.step(2, 1.0, 0.1, friction=0.5, maxVel=0.5)
+            e0.record(st)
+            ag.step(iters, 1.0, 0.1, friction=0.5, maxVel=0.5)
+            e1.record(st)
+            e1.synchronize()
+            stepped = e0.elapsed_time(e1) / iters
+        print(f"agents {agents} in {n}^2: " + ", ".join(f"{v*1e3:.1f}" for v in ms) + " us "
+              "(count, scan, scatter, stabilize, forces, whole; events between stages); "
+              f"chained dispatch {chained*1e3:.1f} us, resident step {stepped*1e3:.1f} us")
     elif case == "stencil64":
         rng = np.random.default_rng(12)
         cells = n * n

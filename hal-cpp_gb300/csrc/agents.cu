@@ -25,6 +25,7 @@
 #include "common.cuh"
 #include "agents_wells.h"
 
+#include <climits>
 #include <cmath>
 #include <type_traits>
 
@@ -364,117 +365,16 @@ namespace halcuda
             sRad[slot] = rad[i];
         }
 
-        // ---- the single-grid dispatch's binning -----------------------------
-        // BinCountTiles: as BinCount, and each agent also counts itself in its
-        // cell's scan tile (tileSums, zero on entry), so the scan needs no
-        // reduce pass over the counts.  Lanes of a warp that hit the same
-        // tile add their count once.
-        template <typename TP>
-        __global__ void BinCountTiles(const TP *__restrict__ pos, int32_t n, int32_t xDim, int32_t yDim,
-                                      int32_t *__restrict__ cellOf, int32_t *__restrict__ arrival,
-                                      int32_t *__restrict__ counts, int32_t *__restrict__ tileSums)
-        {
-            ChainEntry();
-            const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-            const bool live = i < n;
-            int32_t c = 0;
-            if (live)
-            {
-                const TP px = pos[2 * static_cast<int64_t>(i)];
-                const TP py = pos[2 * static_cast<int64_t>(i) + 1];
-                c = CellCoord(px, xDim) * yDim + CellCoord(py, yDim);
-                cellOf[i] = c;
-                arrival[i] = atomicAdd(counts + c, 1);
-            }
-            const int32_t tile = live ? c / kScanTile : -1;
-            const unsigned peers = __match_any_sync(0xffffffffu, tile);
-            const int lane = threadIdx.x & 31;
-            if (live && lane == __ffs(peers) - 1)
-            {
-                atomicAdd(tileSums + tile, __popc(peers));
-            }
-        }
-
-        // ScanApply for tile sums that came from the binning: the tile's
-        // prefix is read, then reset to zero for the next binning (only this
-        // CTA reads it), along with the counts it has read.
-        __global__ void __launch_bounds__(kScanThreads) ScanApplyTiles(int32_t *__restrict__ counts, int64_t C,
-                                                                       int32_t *__restrict__ tilePrefix,
-                                                                       int32_t *__restrict__ offsets, int32_t n)
-        {
-            ChainEntry();
-            const int64_t base = static_cast<int64_t>(blockIdx.x) * kScanTile + threadIdx.x * kScanItems;
-            int32_t v[kScanItems];
-            LoadItems(counts, base, C, v);
-            int32_t any = 0;
-#pragma unroll
-            for (int q = 0; q < kScanItems; q++)
-            {
-                any |= v[q];
-            }
-            if (any != 0)
-            {
-                const int32_t zeros[kScanItems] = {0, 0, 0, 0};
-                StoreItems(counts, base, C, zeros);
-            }
-            int32_t sum = 0;
-#pragma unroll
-            for (int q = 0; q < kScanItems; q++)
-            {
-                sum += v[q];
-            }
-            const int32_t prefix = tilePrefix[blockIdx.x];
-            int32_t excl;
-            BlockExclusiveScan(sum, excl);  // its barriers order the prefix read before the reset
-            if (threadIdx.x == 0)
-            {
-                tilePrefix[blockIdx.x] = 0;
-            }
-            int32_t o[kScanItems];
-            o[0] = prefix + excl;
-#pragma unroll
-            for (int q = 1; q < kScanItems; q++)
-            {
-                o[q] = o[q - 1] + v[q - 1];
-            }
-            StoreItems(offsets, base, C, o);
-            if (blockIdx.x == 0 && threadIdx.x == 0)
-            {
-                offsets[C] = n;
-            }
-        }
-
-        // Scatter in agent order: agent i's position, radius and index go to
-        // slot offsets[cell] + arrival rank of the arrival-ordered copies.
-        // The agent-order reads are coalesced; only the writes scatter.
-        template <typename TP, typename TR>
-        __global__ void ScatterAgents(const int32_t *__restrict__ cellOf, const int32_t *__restrict__ arrival,
-                                      const int32_t *__restrict__ offsets, const V2<TP> *__restrict__ pos,
-                                      const TR *__restrict__ rad, int32_t n, int32_t *__restrict__ bucketTmp,
-                                      V2<TP> *__restrict__ posTmp, TR *__restrict__ radTmp)
-        {
-            ChainEntry();
-            const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-            if (i >= n)
-            {
-                return;
-            }
-            const int32_t q = offsets[cellOf[i]] + arrival[i];
-            bucketTmp[q] = i;
-            posTmp[q] = pos[i];
-            radTmp[q] = rad[i];
-        }
-
         // Stable order within each cell (the CPU's scatter in agent index
-        // order, CpuAgentForceBackend2D.cpp:100-109): the agent at
-        // arrival-order slot q goes to slot s + (number of lower-indexed
-        // agents of its cell).  Everything is read in slot order: the cell
-        // again from the position, the cell's range of arrival-ordered
-        // indices (shared by neighbouring threads), and the writes land
-        // within the cell's own slots.
+        // order, CpuAgentForceBackend2D.cpp:100-109), one thread per
+        // arrival-order slot q: its agent i, whose position gives its cell
+        // again (no cell-array gather), goes to slot s + (number of
+        // lower-indexed agents of the cell).  Neighbouring threads share a
+        // cell's offsets and range of arrival-ordered indices, and the writes
+        // land within the cell's own slots.
         template <typename TP, typename TR>
         __global__ void StabilizeSlots(const int32_t *__restrict__ offsets, const int32_t *__restrict__ bucketTmp,
-                                       const V2<TP> *__restrict__ posTmp, const TR *__restrict__ radTmp, int32_t n,
+                                       const V2<TP> *__restrict__ pos, const TR *__restrict__ rad, int32_t n,
                                        int32_t xDim, int32_t yDim, int32_t *__restrict__ bucket,
                                        V2<TP> *__restrict__ sPos, TR *__restrict__ sRad)
         {
@@ -485,7 +385,8 @@ namespace halcuda
                 return;
             }
             const int32_t i = bucketTmp[q];
-            const V2<TP> p = posTmp[q];
+            const V2<TP> p = pos[i];
+            const TR r = rad[i];
             const int32_t c = CellCoord(p.x, xDim) * yDim + CellCoord(p.y, yDim);
             const int32_t s = offsets[c];
             const int32_t e = offsets[c + 1];
@@ -497,7 +398,7 @@ namespace halcuda
             const int32_t slot = s + rank;
             bucket[slot] = i;
             sPos[slot] = p;
-            sRad[slot] = radTmp[q];
+            sRad[slot] = r;
         }
 
         // IEEE-exact FP64 helpers (no contraction) and their FP32 twins.
@@ -596,12 +497,20 @@ namespace halcuda
         // created in index order (each square's list is newest first,
         // AgentPT2D.h:200-241); otherwise the order is the CPU backend's
         // (ascending index within a cell).
+        //
+        // With rowDelta, the candidates of the common path (at most four
+        // window rows, none wrapped) are read from the copies cPos/cRad
+        // (a CTA's staged rows in shared memory): window row r's slot q is at
+        // q + rowDelta[r - rowLo].  The values, and so the result, are the
+        // same as from sPos/sRad.
         template <typename T, int LAW, bool SUM, bool GRID>
         __device__ __forceinline__ ForceAcc<T> ForceSlotLaw(const int32_t slot, const int32_t *__restrict__ offsets,
                                                             const V2<T> *__restrict__ sPos,
                                                             const T *__restrict__ sRad, double interactionRad, T R,
                                                             const LawParams<T> lp, int32_t xDim, int32_t yDim,
-                                                            int32_t wrapX, int32_t wrapY, V2<T> v0)
+                                                            int32_t wrapX, int32_t wrapY, V2<T> v0,
+                                                            const V2<T> *cPos = nullptr, const T *cRad = nullptr,
+                                                            const int32_t *rowDelta = nullptr, int32_t rowLo = 0)
         {
             const V2<T> pf = sPos[slot];
             const T px = pf.x;
@@ -627,13 +536,17 @@ namespace halcuda
             const T yDimF = static_cast<T>(yDim);
             T vx = v0.x, vy = v0.y;
             T sum = T(0);
+            // where the candidates are read: slot q's data at cp[q + cd]
+            const V2<T> *cp = sPos;
+            const T *cr = sRad;
+            int32_t cd = 0;
             // one candidate slot q of the window, in the CPU's visiting order
             auto visit = [&](int32_t q) {
                 if (q == slot)
                 {
                     return;
                 }
-                const V2<T> pj = sPos[q];
+                const V2<T> pj = cp[q + cd];
                 T xComp, yComp;
                 if constexpr (GRID)
                 {
@@ -651,7 +564,7 @@ namespace halcuda
                     const T dist = Sqrt(Add(Mul(xComp, xComp), Mul(yComp, yComp)));
                     if ((dist < R) && (dist > T(0)))
                     {
-                        const T touchDist = Sub(Add(rad, sRad[q]), dist);
+                        const T touchDist = Sub(Add(rad, cr[q + cd]), dist);
                         const T force = OverlapForce<LAW>(touchDist, lp);
                         vx = Sub(vx, Mul(Div(xComp, dist), force));
                         vy = Sub(vy, Mul(Div(yComp, dist), force));
@@ -673,7 +586,7 @@ namespace halcuda
                     const T dist = d2 * inv;
                     if ((dist < R) && (dist > T(0)))
                     {
-                        const T force = OverlapForce<LAW>((rad + sRad[q]) - dist, lp);
+                        const T force = OverlapForce<LAW>((rad + cr[q + cd]) - dist, lp);
                         const T scale = inv * force;
                         vx -= xComp * scale;
                         vy -= yComp * scale;
@@ -750,9 +663,19 @@ namespace halcuda
                         re[j] = __ldg(offsets + cell + (yEnd - yStart));
                     }
                 }
+                const bool staged = (rowDelta != nullptr) && xStart >= 0 && xEnd <= xDim;
+                if (staged)
+                {
+                    cp = cPos;
+                    cr = cRad;
+                }
 #pragma unroll
                 for (int j = 0; j < 4; j++)
                 {
+                    if (staged && j < nRows)
+                    {
+                        cd = rowDelta[xStart + j - rowLo];
+                    }
                     for (int32_t q = rs[j]; q < re[j]; q++)
                     {
                         visit(q);
@@ -953,6 +876,139 @@ namespace halcuda
             velocity[i] = v;
         }
 
+        // ---- FP32 forces with the window rows staged in shared memory -------
+        // A CTA's slots are consecutive in cell order, so their windows cover
+        // a few rows of the grid over a common y-range.  The CTA copies those
+        // row segments of the sorted positions and radii into shared memory
+        // (coalesced), and each thread then reads its candidates there
+        // instead of gathering them from L2.  Threads whose window wraps, or
+        // has more than four rows, and CTAs whose rows do not fit, read from
+        // global memory as before; the visiting order and the arithmetic are
+        // those of ForceSlotLaw either way, so the results are the same.
+        constexpr int kStageThreads = 256;
+        constexpr int kStageCap = 3584;  // agents: 28 KB of positions + 14 KB of radii
+        constexpr int kStageRows = 8;
+
+        template <int LAW, bool SUM, bool MOVE>
+        __global__ void __launch_bounds__(kStageThreads)
+            ForcesStaged(const int32_t *__restrict__ bucket, const int32_t *__restrict__ offsets,
+                         const float2 *__restrict__ sPos, const float *__restrict__ sRad, int32_t n,
+                         double interactionRad, float R, LawParams<float> lp, int32_t xDim, int32_t yDim,
+                         int32_t wrapX, int32_t wrapY, MoveParams mp, float *__restrict__ deltas,
+                         float *__restrict__ sums, float2 *__restrict__ posOut, float2 *__restrict__ velocity)
+        {
+            ChainEntry();
+            __shared__ float2 stPos[kStageCap];
+            __shared__ float stRad[kStageCap];
+            __shared__ int32_t sLo, sHi, sYlo, sYhi, sOk, sTotal;
+            __shared__ int32_t sDelta[kStageRows], sStart[kStageRows], sBase[kStageRows];
+            const int tid = threadIdx.x;
+            if (tid == 0)
+            {
+                sLo = INT_MAX;
+                sHi = INT_MIN;
+                sYlo = INT_MAX;
+                sYhi = INT_MIN;
+            }
+            __syncthreads();
+            const int32_t slot = blockIdx.x * blockDim.x + tid;
+            const bool live = slot < n;
+            if (live)
+            {
+                // the window of ForceSlotLaw; its common path with no wrapped row
+                const float2 pf = sPos[slot];
+                int32_t xs = static_cast<int32_t>(floor(static_cast<double>(pf.x) - interactionRad));
+                int32_t xe = static_cast<int32_t>(ceil(static_cast<double>(pf.x) + interactionRad));
+                int32_t ys = static_cast<int32_t>(floor(static_cast<double>(pf.y) - interactionRad));
+                int32_t ye = static_cast<int32_t>(ceil(static_cast<double>(pf.y) + interactionRad));
+                if (!wrapX)
+                {
+                    xs = max(xs, 0);
+                    xe = min(xe, xDim);
+                }
+                if (!wrapY)
+                {
+                    ys = max(ys, 0);
+                    ye = min(ye, yDim);
+                }
+                if (xs >= 0 && xe <= xDim && ys >= 0 && ye <= yDim && xe > xs && ye > ys && xe - xs <= 4)
+                {
+                    atomicMin(&sLo, xs);
+                    atomicMax(&sHi, xe - 1);
+                    atomicMin(&sYlo, ys);
+                    atomicMax(&sYhi, ye - 1);
+                }
+            }
+            __syncthreads();
+            if (tid < 32)
+            {
+                // one lane per staged row: its segment [row*yDim + sYlo, row*yDim + sYhi]
+                const bool any = sHi >= sLo;
+                const int32_t rows = any ? sHi - sLo + 1 : 0;
+                int32_t a = 0, len = 0;
+                if (any && rows <= kStageRows && tid < rows)
+                {
+                    const int64_t rowBase = static_cast<int64_t>(sLo + tid) * yDim;
+                    a = offsets[rowBase + sYlo];
+                    len = offsets[rowBase + sYhi + 1] - a;
+                }
+                const int32_t inc = WarpScan(len, tid);
+                if (tid < kStageRows)
+                {
+                    sStart[tid] = a;
+                    sBase[tid] = inc - len;
+                    sDelta[tid] = (inc - len) - a;
+                }
+                const int32_t total = __shfl_sync(0xffffffffu, inc, 31);
+                if (tid == 0)
+                {
+                    sOk = (any && rows <= kStageRows && total <= kStageCap) ? 1 : 0;
+                    sTotal = total;
+                }
+            }
+            __syncthreads();
+            const bool ok = sOk != 0;
+            if (ok)
+            {
+                const int32_t rows = sHi - sLo + 1;
+                for (int32_t t = tid; t < sTotal; t += blockDim.x)
+                {
+                    int k = 0;
+                    while (k + 1 < rows && sBase[k + 1] <= t)
+                    {
+                        k++;
+                    }
+                    const int32_t src = sStart[k] + (t - sBase[k]);
+                    stPos[t] = sPos[src];
+                    stRad[t] = sRad[src];
+                }
+            }
+            __syncthreads();
+            if (!live)
+            {
+                return;
+            }
+            const int32_t i = bucket[slot];
+            const ForceAcc<float> acc = ForceSlotLaw<float, LAW, SUM, false>(
+                slot, offsets, sPos, sRad, interactionRad, R, lp, xDim, yDim, wrapX, wrapY, make_float2(0.f, 0.f),
+                ok ? stPos : nullptr, ok ? stRad : nullptr, ok ? sDelta : nullptr, sLo);
+            StoreDelta(deltas, i, acc.v);
+            if constexpr (SUM)
+            {
+                sums[i] = acc.sum;
+            }
+            if constexpr (MOVE)
+            {
+                float2 p = sPos[slot];
+                float2 v = velocity[i];
+                v.x = __fadd_rn(v.x, acc.v.x);
+                v.y = __fadd_rn(v.y, acc.v.y);
+                MoveAgent(mp, p, v);
+                posOut[i] = p;
+                velocity[i] = v;
+            }
+        }
+
         // ---- many independent wells in one pass ------------------------------
         // Agents of all wells are concatenated, and so are the cells of the
         // wells that have agents (well w's cells start at cellBase); the
@@ -1064,10 +1120,6 @@ namespace halcuda
         DevBuf<float> sRad32;
         DevBuf<double> sRad64;
         DevBuf<int32_t> cellOf, arrival, counts, offsets, tileSums, bucketTmp, bucket;
-        DevBuf<float2> posTmp32;  // arrival-ordered copies of the binning (FP32 path)
-        DevBuf<float> radTmp32;
-        DevBuf<double2> posTmpD;  // the same, FP64 path
-        DevBuf<double> radTmp64;
         DevBuf<float> sums32;    // per-agent sums of positive forces (FP32 path)
         DevBuf<double> sums64;   // the same, FP64 path
         bool sumsValid = false;  // sums32 holds the last dispatch's or step's sums
@@ -1099,9 +1151,7 @@ namespace halcuda
             HAL_TRY(offsets.Alloc(static_cast<size_t>(C) + 1, "cudaMalloc(bins)"));
             nTiles = static_cast<int32_t>((C + kScanTile - 1) / kScanTile);
             HAL_TRY(tileSums.Alloc(static_cast<size_t>(nTiles), "cudaMalloc(bins)"));
-            HAL_TRY(CudaStatus(cudaMemset(tileSums.p, 0, static_cast<size_t>(nTiles) * sizeof(int32_t)), "cudaMemset"));
-            HAL_TRY(posTmp32.Alloc(m, "cudaMalloc(agents)"));
-            HAL_TRY(radTmp32.Alloc(m, "cudaMalloc(agents)"));
+
             HAL_TRY(CudaStatus(cudaMemset(offsets.p, 0, (static_cast<size_t>(C) + 1) * sizeof(int32_t)), "cudaMemset"));
             return HAL_CUDA_OK;
         }
@@ -1118,42 +1168,35 @@ namespace halcuda
         {
             if (countsDirty)
             {
-                // a previous binning stopped before its scan cleared the
-                // counts and the tile sums
+                // a previous binning stopped before its scan cleared the counts
                 HAL_TRY(CudaStatus(cudaMemsetAsync(counts.p, 0, static_cast<size_t>(C) * sizeof(int32_t), s),
                                    "cudaMemsetAsync(counts)"));
-                HAL_TRY(CudaStatus(cudaMemsetAsync(tileSums.p, 0, static_cast<size_t>(nTiles) * sizeof(int32_t), s),
-                                   "cudaMemsetAsync(tile sums)"));
             }
             countsDirty = true;
             const int T = 256;
             unsigned ablocks = static_cast<unsigned>((n + T - 1) / T);
             if (n > 0)
             {
-                LaunchChained(BinCountTiles<TP>, ablocks, T, s, pos, n, xDim, yDim, cellOf.p, arrival.p, counts.p,
-                              tileSums.p);
+                LaunchChained(BinCount<TP>, ablocks, T, s, pos, n, xDim, yDim, static_cast<V2<TP> *>(nullptr),
+                              cellOf.p, arrival.p, counts.p);
                 CountLaunch();
             }
             if (ev)
             {
                 cudaEventRecord(ev[0], s);
             }
+            LaunchChained(ScanReduce, nTiles, kScanThreads, s, counts.p, C, tileSums.p);
             LaunchChained(ScanTiles, 1u, kScanThreads, s, tileSums.p, nTiles);
-            LaunchChained(ScanApplyTiles, nTiles, kScanThreads, s, counts.p, C, tileSums.p, offsets.p, n);
-            CountLaunch(2);
+            LaunchChained(ScanApply<true>, nTiles, kScanThreads, s, counts.p, C, tileSums.p, offsets.p, n);
+            CountLaunch(3);
             countsDirty = (cudaPeekAtLastError() != cudaSuccess);
             if (ev)
             {
                 cudaEventRecord(ev[1], s);
             }
-            V2<TP> *posTmp = TmpPosBuf(TP());
-            TR *radTmp = TmpRadBuf(TR());
             if (n > 0)
             {
-                // pos is the handle's own device buffer (cudaMalloc'd, so
-                // aligned for V2<TP>)
-                LaunchChained(ScatterAgents<TP, TR>, ablocks, T, s, cellOf.p, arrival.p, offsets.p,
-                              reinterpret_cast<const V2<TP> *>(pos), rad, n, bucketTmp.p, posTmp, radTmp);
+                LaunchChained(Scatter, ablocks, T, s, cellOf.p, arrival.p, offsets.p, n, bucketTmp.p);
                 CountLaunch();
             }
             if (ev)
@@ -1162,8 +1205,11 @@ namespace halcuda
             }
             if (n > 0)
             {
-                LaunchChained(StabilizeSlots<TP, TR>, ablocks, T, s, offsets.p, bucketTmp.p, posTmp, radTmp, n, xDim,
-                              yDim, bucket.p, SortedPosBuf(TP()), sRad);
+                // pos is the handle's own device buffer (cudaMalloc'd, so
+                // aligned for V2<TP>)
+                LaunchChained(StabilizeSlots<TP, TR>, ablocks, T, s, offsets.p, bucketTmp.p,
+                              reinterpret_cast<const V2<TP> *>(pos), rad, n, xDim, yDim, bucket.p, SortedPosBuf(TP()),
+                              sRad);
                 CountLaunch();
             }
             if (ev)
@@ -1172,11 +1218,6 @@ namespace halcuda
             }
             return LaunchStatus("agent binning");
         }
-
-        V2<float> *TmpPosBuf(float) { return posTmp32.p; }
-        V2<double> *TmpPosBuf(double) { return posTmpD.p; }
-        float *TmpRadBuf(float) { return radTmp32.p; }
-        double *TmpRadBuf(double) { return radTmp64.p; }
 
         // Pass 4 with force law `law`: velocity deltas (from zero, or from
         // velIn) into vel, and with law.sums each agent's sum of positive
@@ -1200,6 +1241,13 @@ namespace halcuda
                               static_cast<T>(R), lp, xDim, yDim, static_cast<int32_t>(wrapX),
                               static_cast<int32_t>(wrapY), vel, sums, velIn);
             };
+            if constexpr (std::is_same<T, float>::value && std::is_same<TV, float>::value)
+            {
+                if (velIn == nullptr)
+                {
+                    return ForceStaged32(sRad, R, law, wrapX, wrapY, vel, sums, s);
+                }
+            }
             const bool grid = std::is_same<T, double>::value && law.grid;
             switch (law.kind * 4 + (law.sums ? 2 : 0) + (grid ? 1 : 0))
             {
@@ -1215,6 +1263,35 @@ namespace halcuda
             case 9: go(Forces<T, TV, kLawPower, false, true>); break;
             case 10: go(Forces<T, TV, kLawPower, true, false>); break;
             default: go(Forces<T, TV, kLawPower, true, true>); break;
+            }
+            CountLaunch();
+            return LaunchStatus("agent forces");
+        }
+
+        // The FP32 pass 4 with staged window rows (ForcesStaged), deltas from
+        // zero.
+        int ForceStaged32(const float *sRadP, double R, const ForceLawSpec &law, bool wrapX, bool wrapY, float *vel,
+                          float *sums, cudaStream_t s)
+        {
+            const unsigned blocks = static_cast<unsigned>((n + kStageThreads - 1) / kStageThreads);
+            LawParams<float> lp;
+            lp.scale = static_cast<float>(law.scale);
+            lp.exponent = static_cast<float>(law.exponent);
+            MoveParams mp{};
+            auto go = [&](auto kernel) {
+                LaunchChained(kernel, blocks, kStageThreads, s, bucket.p, offsets.p, sPos.p, sRadP, n, R,
+                              static_cast<float>(R), lp, xDim, yDim, static_cast<int32_t>(wrapX),
+                              static_cast<int32_t>(wrapY), mp, vel, sums, static_cast<float2 *>(nullptr),
+                              static_cast<float2 *>(nullptr));
+            };
+            switch (law.kind * 2 + (law.sums ? 1 : 0))
+            {
+            case 0: go(ForcesStaged<kLawLinear, false, false>); break;
+            case 1: go(ForcesStaged<kLawLinear, true, false>); break;
+            case 2: go(ForcesStaged<kLawClamped, false, false>); break;
+            case 3: go(ForcesStaged<kLawClamped, true, false>); break;
+            case 4: go(ForcesStaged<kLawPower, false, false>); break;
+            default: go(ForcesStaged<kLawPower, true, false>); break;
             }
             CountLaunch();
             return LaunchStatus("agent forces");
@@ -1260,24 +1337,23 @@ namespace
         {
             HAL_TRY(a.SumsBuf32(&sums));
         }
-        const int T = 128;
-        const unsigned blocks = static_cast<unsigned>((a.n + T - 1) / T);
+        const unsigned blocks = static_cast<unsigned>((a.n + kStageThreads - 1) / kStageThreads);
         LawParams<float> lp;
         lp.scale = static_cast<float>(law.scale);
         lp.exponent = static_cast<float>(law.exponent);
         auto go = [&](auto kernel) {
-            LaunchChained(kernel, blocks, T, s, a.bucket.p, a.offsets.p, a.sPos.p, a.sRad32.p, a.n, R,
-                          static_cast<float>(R), lp, a.xDim, a.yDim, mp, a.vel32.p,
-                          reinterpret_cast<float2 *>(a.pos32.p), a.velState.p, sums);
+            LaunchChained(kernel, blocks, kStageThreads, s, a.bucket.p, a.offsets.p, a.sPos.p, a.sRad32.p, a.n, R,
+                          static_cast<float>(R), lp, a.xDim, a.yDim, mp.wrapX, mp.wrapY, mp, a.vel32.p, sums,
+                          reinterpret_cast<float2 *>(a.pos32.p), a.velState.p);
         };
         switch (law.kind * 2 + (law.sums ? 1 : 0))
         {
-        case 0: go(ForcesMove<kLawLinear, false>); break;
-        case 1: go(ForcesMove<kLawLinear, true>); break;
-        case 2: go(ForcesMove<kLawClamped, false>); break;
-        case 3: go(ForcesMove<kLawClamped, true>); break;
-        case 4: go(ForcesMove<kLawPower, false>); break;
-        default: go(ForcesMove<kLawPower, true>); break;
+        case 0: go(ForcesStaged<kLawLinear, false, true>); break;
+        case 1: go(ForcesStaged<kLawLinear, true, true>); break;
+        case 2: go(ForcesStaged<kLawClamped, false, true>); break;
+        case 3: go(ForcesStaged<kLawClamped, true, true>); break;
+        case 4: go(ForcesStaged<kLawPower, false, true>); break;
+        default: go(ForcesStaged<kLawPower, true, true>); break;
         }
         CountLaunch();
         return LaunchStatus("agent forces and move");
@@ -1391,8 +1467,6 @@ namespace
             HAL_TRY(h->rad64.Alloc(m, "cudaMalloc(agents64)"));
             HAL_TRY(h->vel64.Alloc(2 * m, "cudaMalloc(agents64)"));
             HAL_TRY(h->sRad64.Alloc(m, "cudaMalloc(agents64)"));
-            HAL_TRY(h->posTmpD.Alloc(m, "cudaMalloc(agents64)"));
-            HAL_TRY(h->radTmp64.Alloc(m, "cudaMalloc(agents64)"));
             HAL_TRY(h->sPosD.Alloc(m, "cudaMalloc(agents64)"));
         }
         return HAL_CUDA_OK;
