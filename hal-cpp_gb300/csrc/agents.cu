@@ -25,7 +25,6 @@
 #include "common.cuh"
 #include "agents_wells.h"
 
-#include <climits>
 #include <cmath>
 #include <type_traits>
 
@@ -478,6 +477,69 @@ namespace halcuda
             }
         }
 
+        // One neighbour's contribution (CpuAgentForceBackend2D.cpp:153-169,
+        // SphericalAgent2D.h:83-98): the displacement to pj, and for
+        // 0 < d < R the force law's force along it, subtracted from (vx, vy);
+        // with SUM a positive force is added to sum.
+        template <typename T, int LAW, bool SUM, bool GRID>
+        __device__ __forceinline__ void PairStep(T px, T py, T rad, V2<T> pj, T radj, T R, const LawParams<T> &lp,
+                                                 T xDimF, T yDimF, int32_t wrapX, int32_t wrapY, T &vx, T &vy,
+                                                 T &sum)
+        {
+            T xComp, yComp;
+            if constexpr (GRID)
+            {
+                xComp = DispGrid(px, pj.x, xDimF, wrapX != 0);
+                yComp = DispGrid(py, pj.y, yDimF, wrapY != 0);
+            }
+            else
+            {
+                xComp = Disp(px, pj.x, xDimF, wrapX != 0);
+                yComp = Disp(py, pj.y, yDimF, wrapY != 0);
+            }
+            if constexpr (std::is_same<T, double>::value)
+            {
+                // IEEE operations in the CPU's order: bit-exact
+                const T dist = Sqrt(Add(Mul(xComp, xComp), Mul(yComp, yComp)));
+                if ((dist < R) && (dist > T(0)))
+                {
+                    const T touchDist = Sub(Add(rad, radj), dist);
+                    const T force = OverlapForce<LAW>(touchDist, lp);
+                    vx = Sub(vx, Mul(Div(xComp, dist), force));
+                    vy = Sub(vy, Mul(Div(yComp, dist), force));
+                    if constexpr (SUM)
+                    {
+                        if (force > T(0))
+                        {
+                            sum = Add(sum, Abs(force));
+                        }
+                    }
+                }
+            }
+            else
+            {
+                // FP32 path: 1/d from rsqrt (d^2 = 0 gives NaN, which fails
+                // both tests like the CPU's d > 0)
+                const T d2 = fmaf(xComp, xComp, yComp * yComp);
+                const T inv = rsqrtf(d2);
+                const T dist = d2 * inv;
+                if ((dist < R) && (dist > T(0)))
+                {
+                    const T force = OverlapForce<LAW>((rad + radj) - dist, lp);
+                    const T scale = inv * force;
+                    vx -= xComp * scale;
+                    vy -= yComp * scale;
+                    if constexpr (SUM)
+                    {
+                        if (force > T(0))
+                        {
+                            sum += force;
+                        }
+                    }
+                }
+            }
+        }
+
         // One agent's force sum: its velocity after the neighbours' forces
         // (or the deltas, from zero) and the sum of its positive forces.
         template <typename T>
@@ -497,20 +559,12 @@ namespace halcuda
         // created in index order (each square's list is newest first,
         // AgentPT2D.h:200-241); otherwise the order is the CPU backend's
         // (ascending index within a cell).
-        //
-        // With rowDelta, the candidates of the common path (at most four
-        // window rows, none wrapped) are read from the copies cPos/cRad
-        // (a CTA's staged rows in shared memory): window row r's slot q is at
-        // q + rowDelta[r - rowLo].  The values, and so the result, are the
-        // same as from sPos/sRad.
         template <typename T, int LAW, bool SUM, bool GRID>
         __device__ __forceinline__ ForceAcc<T> ForceSlotLaw(const int32_t slot, const int32_t *__restrict__ offsets,
                                                             const V2<T> *__restrict__ sPos,
                                                             const T *__restrict__ sRad, double interactionRad, T R,
                                                             const LawParams<T> lp, int32_t xDim, int32_t yDim,
-                                                            int32_t wrapX, int32_t wrapY, V2<T> v0,
-                                                            const V2<T> *cPos = nullptr, const T *cRad = nullptr,
-                                                            const int32_t *rowDelta = nullptr, int32_t rowLo = 0)
+                                                            int32_t wrapX, int32_t wrapY, V2<T> v0)
         {
             const V2<T> pf = sPos[slot];
             const T px = pf.x;
@@ -536,69 +590,14 @@ namespace halcuda
             const T yDimF = static_cast<T>(yDim);
             T vx = v0.x, vy = v0.y;
             T sum = T(0);
-            // where the candidates are read: slot q's data at cp[q + cd]
-            const V2<T> *cp = sPos;
-            const T *cr = sRad;
-            int32_t cd = 0;
             // one candidate slot q of the window, in the CPU's visiting order
             auto visit = [&](int32_t q) {
                 if (q == slot)
                 {
                     return;
                 }
-                const V2<T> pj = cp[q + cd];
-                T xComp, yComp;
-                if constexpr (GRID)
-                {
-                    xComp = DispGrid(px, pj.x, xDimF, wrapX != 0);
-                    yComp = DispGrid(py, pj.y, yDimF, wrapY != 0);
-                }
-                else
-                {
-                    xComp = Disp(px, pj.x, xDimF, wrapX != 0);
-                    yComp = Disp(py, pj.y, yDimF, wrapY != 0);
-                }
-                if constexpr (std::is_same<T, double>::value)
-                {
-                    // IEEE operations in the CPU's order: bit-exact
-                    const T dist = Sqrt(Add(Mul(xComp, xComp), Mul(yComp, yComp)));
-                    if ((dist < R) && (dist > T(0)))
-                    {
-                        const T touchDist = Sub(Add(rad, cr[q + cd]), dist);
-                        const T force = OverlapForce<LAW>(touchDist, lp);
-                        vx = Sub(vx, Mul(Div(xComp, dist), force));
-                        vy = Sub(vy, Mul(Div(yComp, dist), force));
-                        if constexpr (SUM)
-                        {
-                            if (force > T(0))
-                            {
-                                sum = Add(sum, Abs(force));
-                            }
-                        }
-                    }
-                }
-                else
-                {
-                    // FP32 path: 1/d from rsqrt (d^2 = 0 gives NaN,
-                    // which fails both tests like the CPU's d > 0)
-                    const T d2 = fmaf(xComp, xComp, yComp * yComp);
-                    const T inv = rsqrtf(d2);
-                    const T dist = d2 * inv;
-                    if ((dist < R) && (dist > T(0)))
-                    {
-                        const T force = OverlapForce<LAW>((rad + cr[q + cd]) - dist, lp);
-                        const T scale = inv * force;
-                        vx -= xComp * scale;
-                        vy -= yComp * scale;
-                        if constexpr (SUM)
-                        {
-                            if (force > T(0))
-                            {
-                                sum += force;
-                            }
-                        }
-                    }
-                }
+                PairStep<T, LAW, SUM, GRID>(px, py, rad, sPos[q], sRad[q], R, lp, xDimF, yDimF, wrapX, wrapY, vx,
+                                            vy, sum);
             };
             auto result = [&]() {
                 ForceAcc<T> acc;
@@ -663,19 +662,9 @@ namespace halcuda
                         re[j] = __ldg(offsets + cell + (yEnd - yStart));
                     }
                 }
-                const bool staged = (rowDelta != nullptr) && xStart >= 0 && xEnd <= xDim;
-                if (staged)
-                {
-                    cp = cPos;
-                    cr = cRad;
-                }
 #pragma unroll
                 for (int j = 0; j < 4; j++)
                 {
-                    if (staged && j < nRows)
-                    {
-                        cd = rowDelta[xStart + j - rowLo];
-                    }
                     for (int32_t q = rs[j]; q < re[j]; q++)
                     {
                         visit(q);
@@ -876,139 +865,6 @@ namespace halcuda
             velocity[i] = v;
         }
 
-        // ---- FP32 forces with the window rows staged in shared memory -------
-        // A CTA's slots are consecutive in cell order, so their windows cover
-        // a few rows of the grid over a common y-range.  The CTA copies those
-        // row segments of the sorted positions and radii into shared memory
-        // (coalesced), and each thread then reads its candidates there
-        // instead of gathering them from L2.  Threads whose window wraps, or
-        // has more than four rows, and CTAs whose rows do not fit, read from
-        // global memory as before; the visiting order and the arithmetic are
-        // those of ForceSlotLaw either way, so the results are the same.
-        constexpr int kStageThreads = 256;
-        constexpr int kStageCap = 3584;  // agents: 28 KB of positions + 14 KB of radii
-        constexpr int kStageRows = 8;
-
-        template <int LAW, bool SUM, bool MOVE>
-        __global__ void __launch_bounds__(kStageThreads)
-            ForcesStaged(const int32_t *__restrict__ bucket, const int32_t *__restrict__ offsets,
-                         const float2 *__restrict__ sPos, const float *__restrict__ sRad, int32_t n,
-                         double interactionRad, float R, LawParams<float> lp, int32_t xDim, int32_t yDim,
-                         int32_t wrapX, int32_t wrapY, MoveParams mp, float *__restrict__ deltas,
-                         float *__restrict__ sums, float2 *__restrict__ posOut, float2 *__restrict__ velocity)
-        {
-            ChainEntry();
-            __shared__ float2 stPos[kStageCap];
-            __shared__ float stRad[kStageCap];
-            __shared__ int32_t sLo, sHi, sYlo, sYhi, sOk, sTotal;
-            __shared__ int32_t sDelta[kStageRows], sStart[kStageRows], sBase[kStageRows];
-            const int tid = threadIdx.x;
-            if (tid == 0)
-            {
-                sLo = INT_MAX;
-                sHi = INT_MIN;
-                sYlo = INT_MAX;
-                sYhi = INT_MIN;
-            }
-            __syncthreads();
-            const int32_t slot = blockIdx.x * blockDim.x + tid;
-            const bool live = slot < n;
-            if (live)
-            {
-                // the window of ForceSlotLaw; its common path with no wrapped row
-                const float2 pf = sPos[slot];
-                int32_t xs = static_cast<int32_t>(floor(static_cast<double>(pf.x) - interactionRad));
-                int32_t xe = static_cast<int32_t>(ceil(static_cast<double>(pf.x) + interactionRad));
-                int32_t ys = static_cast<int32_t>(floor(static_cast<double>(pf.y) - interactionRad));
-                int32_t ye = static_cast<int32_t>(ceil(static_cast<double>(pf.y) + interactionRad));
-                if (!wrapX)
-                {
-                    xs = max(xs, 0);
-                    xe = min(xe, xDim);
-                }
-                if (!wrapY)
-                {
-                    ys = max(ys, 0);
-                    ye = min(ye, yDim);
-                }
-                if (xs >= 0 && xe <= xDim && ys >= 0 && ye <= yDim && xe > xs && ye > ys && xe - xs <= 4)
-                {
-                    atomicMin(&sLo, xs);
-                    atomicMax(&sHi, xe - 1);
-                    atomicMin(&sYlo, ys);
-                    atomicMax(&sYhi, ye - 1);
-                }
-            }
-            __syncthreads();
-            if (tid < 32)
-            {
-                // one lane per staged row: its segment [row*yDim + sYlo, row*yDim + sYhi]
-                const bool any = sHi >= sLo;
-                const int32_t rows = any ? sHi - sLo + 1 : 0;
-                int32_t a = 0, len = 0;
-                if (any && rows <= kStageRows && tid < rows)
-                {
-                    const int64_t rowBase = static_cast<int64_t>(sLo + tid) * yDim;
-                    a = offsets[rowBase + sYlo];
-                    len = offsets[rowBase + sYhi + 1] - a;
-                }
-                const int32_t inc = WarpScan(len, tid);
-                if (tid < kStageRows)
-                {
-                    sStart[tid] = a;
-                    sBase[tid] = inc - len;
-                    sDelta[tid] = (inc - len) - a;
-                }
-                const int32_t total = __shfl_sync(0xffffffffu, inc, 31);
-                if (tid == 0)
-                {
-                    sOk = (any && rows <= kStageRows && total <= kStageCap) ? 1 : 0;
-                    sTotal = total;
-                }
-            }
-            __syncthreads();
-            const bool ok = sOk != 0;
-            if (ok)
-            {
-                const int32_t rows = sHi - sLo + 1;
-                for (int32_t t = tid; t < sTotal; t += blockDim.x)
-                {
-                    int k = 0;
-                    while (k + 1 < rows && sBase[k + 1] <= t)
-                    {
-                        k++;
-                    }
-                    const int32_t src = sStart[k] + (t - sBase[k]);
-                    stPos[t] = sPos[src];
-                    stRad[t] = sRad[src];
-                }
-            }
-            __syncthreads();
-            if (!live)
-            {
-                return;
-            }
-            const int32_t i = bucket[slot];
-            const ForceAcc<float> acc = ForceSlotLaw<float, LAW, SUM, false>(
-                slot, offsets, sPos, sRad, interactionRad, R, lp, xDim, yDim, wrapX, wrapY, make_float2(0.f, 0.f),
-                ok ? stPos : nullptr, ok ? stRad : nullptr, ok ? sDelta : nullptr, sLo);
-            StoreDelta(deltas, i, acc.v);
-            if constexpr (SUM)
-            {
-                sums[i] = acc.sum;
-            }
-            if constexpr (MOVE)
-            {
-                float2 p = sPos[slot];
-                float2 v = velocity[i];
-                v.x = __fadd_rn(v.x, acc.v.x);
-                v.y = __fadd_rn(v.y, acc.v.y);
-                MoveAgent(mp, p, v);
-                posOut[i] = p;
-                velocity[i] = v;
-            }
-        }
-
         // ---- many independent wells in one pass ------------------------------
         // Agents of all wells are concatenated, and so are the cells of the
         // wells that have agents (well w's cells start at cellBase); the
@@ -1017,7 +873,7 @@ namespace halcuda
 
         __global__ void BinCountWells(const float *__restrict__ pos, const int32_t *__restrict__ wellOf,
                                       const AgentWellDev *__restrict__ wells, int32_t n, float2 *__restrict__ posF,
-                                      int32_t *__restrict__ cellOf, int32_t *__restrict__ arrival,
+                                      int32_t *__restrict__ binOf, int32_t *__restrict__ arrival,
                                       int32_t *__restrict__ counts)
         {
             const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1029,15 +885,126 @@ namespace halcuda
             const float px = pos[2 * static_cast<int64_t>(i)];
             const float py = pos[2 * static_cast<int64_t>(i) + 1];
             posF[i] = make_float2(px, py);
-            const int32_t c = static_cast<int32_t>(wd.cellBase) + CellCoord(px, wd.xDim) * wd.yDim + CellCoord(py, wd.yDim);
-            cellOf[i] = c;
-            arrival[i] = atomicAdd(counts + c, 1);
+            const int32_t b = static_cast<int32_t>(wd.binBase) + (CellCoord(px, wd.xDim) / kWellBin) * wd.binsY +
+                              CellCoord(py, wd.yDim) / kWellBin;
+            binOf[i] = b;
+            arrival[i] = atomicAdd(counts + b, 1);
+        }
+
+        // The order within a coarse bin: by cell, then by agent index (the
+        // per-cell binning's order for each cell).  The agent at
+        // arrival-order slot q counts the agents of its bin before it.
+        __global__ void StabilizeWells(const int32_t *__restrict__ binOf, const int32_t *__restrict__ offsets,
+                                       const int32_t *__restrict__ bucketTmp, const float2 *__restrict__ posF,
+                                       const float *__restrict__ rad, const int32_t *__restrict__ wellOf,
+                                       const AgentWellDev *__restrict__ wells, int32_t n,
+                                       int32_t *__restrict__ bucket, float2 *__restrict__ sPos,
+                                       float *__restrict__ sRad, int32_t *__restrict__ sCell)
+        {
+            const int32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+            if (q >= n)
+            {
+                return;
+            }
+            const int32_t i = bucketTmp[q];
+            const AgentWellDev wd = wells[wellOf[i]];
+            const float2 p = posF[i];
+            const int32_t c = CellCoord(p.x, wd.xDim) * wd.yDim + CellCoord(p.y, wd.yDim);
+            const int32_t b = binOf[i];
+            const int32_t s = offsets[b];
+            const int32_t e = offsets[b + 1];
+            int32_t rank = 0;
+            for (int32_t t = s; t < e; t++)
+            {
+                const int32_t j = bucketTmp[t];
+                const float2 pj = posF[j];
+                const int32_t cj = CellCoord(pj.x, wd.xDim) * wd.yDim + CellCoord(pj.y, wd.yDim);
+                rank += (cj < c || (cj == c && j < i)) ? 1 : 0;
+            }
+            const int32_t slot = s + rank;
+            bucket[slot] = i;
+            sPos[slot] = p;
+            sRad[slot] = rad[i];
+            sCell[slot] = c;
+        }
+
+        // Pass 4 of one well's agent over the coarse bins: the window's cells
+        // x-major then y, each cell's agents (a run of its bin, in index
+        // order), so the visiting order and the sum are those of ForceSlot
+        // on the well's own per-cell bins.
+        __device__ __forceinline__ V2<float> ForceSlotWell(const int32_t slot, const int32_t *__restrict__ offsets,
+                                                           const float2 *__restrict__ sPos,
+                                                           const float *__restrict__ sRad,
+                                                           const int32_t *__restrict__ sCell, double interactionRad,
+                                                           float R, float k, const AgentWellDev &wd)
+        {
+            const float2 pf = sPos[slot];
+            const float rad = sRad[slot];
+            const int32_t xDim = wd.xDim, yDim = wd.yDim;
+            int32_t xStart = static_cast<int32_t>(floor(static_cast<double>(pf.x) - interactionRad));
+            int32_t xEnd = static_cast<int32_t>(ceil(static_cast<double>(pf.x) + interactionRad));
+            int32_t yStart = static_cast<int32_t>(floor(static_cast<double>(pf.y) - interactionRad));
+            int32_t yEnd = static_cast<int32_t>(ceil(static_cast<double>(pf.y) + interactionRad));
+            if (!wd.wrapX)
+            {
+                xStart = max(xStart, 0);
+                xEnd = min(xEnd, xDim);
+            }
+            if (!wd.wrapY)
+            {
+                yStart = max(yStart, 0);
+                yEnd = min(yEnd, yDim);
+            }
+            LawParams<float> lp;
+            lp.scale = k;
+            lp.exponent = 1.0f;
+            const float xDimF = static_cast<float>(xDim);
+            const float yDimF = static_cast<float>(yDim);
+            float vx = 0.0f, vy = 0.0f, sum = 0.0f;
+            for (int32_t xSq = xStart; xSq < xEnd; xSq++)
+            {
+                int32_t retX = xSq;
+                if (retX < 0 || retX >= xDim)
+                {
+                    retX %= xDim;  // only reached on a wrapped axis (clamped otherwise)
+                    retX = (retX < 0) ? retX + xDim : retX;
+                }
+                const int32_t binRow = static_cast<int32_t>(wd.binBase) + (retX / kWellBin) * wd.binsY;
+                for (int32_t ySq = yStart; ySq < yEnd; ySq++)
+                {
+                    int32_t retY = ySq;
+                    if (retY < 0 || retY >= yDim)
+                    {
+                        retY %= yDim;
+                        retY = (retY < 0) ? retY + yDim : retY;
+                    }
+                    const int32_t cell = retX * yDim + retY;
+                    const int32_t b = binRow + retY / kWellBin;
+                    const int32_t s = __ldg(offsets + b);
+                    const int32_t e = __ldg(offsets + b + 1);
+                    for (int32_t t = s; t < e; t++)
+                    {
+                        const int32_t ct = __ldg(sCell + t);
+                        if (ct > cell)
+                        {
+                            break;  // the bin is ordered by cell
+                        }
+                        if (ct == cell && t != slot)
+                        {
+                            PairStep<float, kLawLinear, false, false>(pf.x, pf.y, rad, sPos[t], sRad[t], R, lp, xDimF,
+                                                                      yDimF, wd.wrapX, wd.wrapY, vx, vy, sum);
+                        }
+                    }
+                }
+            }
+            return make_float2(vx, vy);
         }
 
         __global__ void ForcesWells(const int32_t *__restrict__ bucket, const int32_t *__restrict__ offsets,
                                     const float2 *__restrict__ sPos, const float *__restrict__ sRad,
-                                    const int32_t *__restrict__ wellOf, const AgentWellDev *__restrict__ wells,
-                                    int32_t n, double interactionRad, float R, float k, float *__restrict__ vel)
+                                    const int32_t *__restrict__ sCell, const int32_t *__restrict__ wellOf,
+                                    const AgentWellDev *__restrict__ wells, int32_t n, double interactionRad, float R,
+                                    float k, float *__restrict__ vel)
         {
             const int32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
             if (slot >= n)
@@ -1046,19 +1013,17 @@ namespace halcuda
             }
             const int32_t i = bucket[slot];
             const AgentWellDev wd = wells[wellOf[i]];
-            StoreDelta(vel, i,
-                       ForceSlot<float>(slot, offsets + wd.cellBase, sPos, sRad, interactionRad, R, k, wd.xDim,
-                                        wd.yDim, wd.wrapX, wd.wrapY));
+            StoreDelta(vel, i, ForceSlotWell(slot, offsets, sPos, sRad, sCell, interactionRad, R, k, wd));
         }
 
         // ForcesWells with each agent's SphericalAgent2D update fused, moved
         // within its own well (its sizes and wrap flags).
         __global__ void ForcesWellsMove(const int32_t *__restrict__ bucket, const int32_t *__restrict__ offsets,
                                         const float2 *__restrict__ sPos, const float *__restrict__ sRad,
-                                        const int32_t *__restrict__ wellOf, const AgentWellDev *__restrict__ wells,
-                                        int32_t n, double interactionRad, float R, float k, float friction,
-                                        float maxVel, float *__restrict__ vel, float2 *__restrict__ pos,
-                                        float2 *__restrict__ velocity)
+                                        const int32_t *__restrict__ sCell, const int32_t *__restrict__ wellOf,
+                                        const AgentWellDev *__restrict__ wells, int32_t n, double interactionRad,
+                                        float R, float k, float friction, float maxVel, float *__restrict__ vel,
+                                        float2 *__restrict__ pos, float2 *__restrict__ velocity)
         {
             const int32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
             if (slot >= n)
@@ -1067,8 +1032,7 @@ namespace halcuda
             }
             const int32_t i = bucket[slot];
             const AgentWellDev wd = wells[wellOf[i]];
-            const V2<float> d = ForceSlot<float>(slot, offsets + wd.cellBase, sPos, sRad, interactionRad, R, k, wd.xDim,
-                                                 wd.yDim, wd.wrapX, wd.wrapY);
+            const V2<float> d = ForceSlotWell(slot, offsets, sPos, sRad, sCell, interactionRad, R, k, wd);
             StoreDelta(vel, i, d);
             MoveParams mp;
             mp.friction = friction;
@@ -1087,8 +1051,6 @@ namespace halcuda
         }
     }
 
-    // A force law of the host API (hal_cuda_force_law) with the output and
-    // order options of one force pass.
     struct ForceLawSpec
     {
         int kind = kLawLinear;
@@ -1241,13 +1203,6 @@ namespace halcuda
                               static_cast<T>(R), lp, xDim, yDim, static_cast<int32_t>(wrapX),
                               static_cast<int32_t>(wrapY), vel, sums, velIn);
             };
-            if constexpr (std::is_same<T, float>::value && std::is_same<TV, float>::value)
-            {
-                if (velIn == nullptr)
-                {
-                    return ForceStaged32(sRad, R, law, wrapX, wrapY, vel, sums, s);
-                }
-            }
             const bool grid = std::is_same<T, double>::value && law.grid;
             switch (law.kind * 4 + (law.sums ? 2 : 0) + (grid ? 1 : 0))
             {
@@ -1263,35 +1218,6 @@ namespace halcuda
             case 9: go(Forces<T, TV, kLawPower, false, true>); break;
             case 10: go(Forces<T, TV, kLawPower, true, false>); break;
             default: go(Forces<T, TV, kLawPower, true, true>); break;
-            }
-            CountLaunch();
-            return LaunchStatus("agent forces");
-        }
-
-        // The FP32 pass 4 with staged window rows (ForcesStaged), deltas from
-        // zero.
-        int ForceStaged32(const float *sRadP, double R, const ForceLawSpec &law, bool wrapX, bool wrapY, float *vel,
-                          float *sums, cudaStream_t s)
-        {
-            const unsigned blocks = static_cast<unsigned>((n + kStageThreads - 1) / kStageThreads);
-            LawParams<float> lp;
-            lp.scale = static_cast<float>(law.scale);
-            lp.exponent = static_cast<float>(law.exponent);
-            MoveParams mp{};
-            auto go = [&](auto kernel) {
-                LaunchChained(kernel, blocks, kStageThreads, s, bucket.p, offsets.p, sPos.p, sRadP, n, R,
-                              static_cast<float>(R), lp, xDim, yDim, static_cast<int32_t>(wrapX),
-                              static_cast<int32_t>(wrapY), mp, vel, sums, static_cast<float2 *>(nullptr),
-                              static_cast<float2 *>(nullptr));
-            };
-            switch (law.kind * 2 + (law.sums ? 1 : 0))
-            {
-            case 0: go(ForcesStaged<kLawLinear, false, false>); break;
-            case 1: go(ForcesStaged<kLawLinear, true, false>); break;
-            case 2: go(ForcesStaged<kLawClamped, false, false>); break;
-            case 3: go(ForcesStaged<kLawClamped, true, false>); break;
-            case 4: go(ForcesStaged<kLawPower, false, false>); break;
-            default: go(ForcesStaged<kLawPower, true, false>); break;
             }
             CountLaunch();
             return LaunchStatus("agent forces");
@@ -1337,23 +1263,24 @@ namespace
         {
             HAL_TRY(a.SumsBuf32(&sums));
         }
-        const unsigned blocks = static_cast<unsigned>((a.n + kStageThreads - 1) / kStageThreads);
+        const int T = 128;
+        const unsigned blocks = static_cast<unsigned>((a.n + T - 1) / T);
         LawParams<float> lp;
         lp.scale = static_cast<float>(law.scale);
         lp.exponent = static_cast<float>(law.exponent);
         auto go = [&](auto kernel) {
-            LaunchChained(kernel, blocks, kStageThreads, s, a.bucket.p, a.offsets.p, a.sPos.p, a.sRad32.p, a.n, R,
-                          static_cast<float>(R), lp, a.xDim, a.yDim, mp.wrapX, mp.wrapY, mp, a.vel32.p, sums,
-                          reinterpret_cast<float2 *>(a.pos32.p), a.velState.p);
+            LaunchChained(kernel, blocks, T, s, a.bucket.p, a.offsets.p, a.sPos.p, a.sRad32.p, a.n, R,
+                          static_cast<float>(R), lp, a.xDim, a.yDim, mp, a.vel32.p,
+                          reinterpret_cast<float2 *>(a.pos32.p), a.velState.p, sums);
         };
         switch (law.kind * 2 + (law.sums ? 1 : 0))
         {
-        case 0: go(ForcesStaged<kLawLinear, false, true>); break;
-        case 1: go(ForcesStaged<kLawLinear, true, true>); break;
-        case 2: go(ForcesStaged<kLawClamped, false, true>); break;
-        case 3: go(ForcesStaged<kLawClamped, true, true>); break;
-        case 4: go(ForcesStaged<kLawPower, false, true>); break;
-        default: go(ForcesStaged<kLawPower, true, true>); break;
+        case 0: go(ForcesMove<kLawLinear, false>); break;
+        case 1: go(ForcesMove<kLawLinear, true>); break;
+        case 2: go(ForcesMove<kLawClamped, false>); break;
+        case 3: go(ForcesMove<kLawClamped, true>); break;
+        case 4: go(ForcesMove<kLawPower, false>); break;
+        default: go(ForcesMove<kLawPower, true>); break;
         }
         CountLaunch();
         return LaunchStatus("agent forces and move");
@@ -2084,19 +2011,19 @@ namespace halcuda
             ScanApply<false><<<nTiles, kScanThreads, 0, s>>>(a.counts, a.cells, a.tileSums, a.offsets, a.n);
         }
         Scatter<<<ablocks, T, 0, s>>>(a.cellOf, a.arrival, a.offsets, a.n, a.bucketTmp);
-        Stabilize<float, float><<<ablocks, T, 0, s>>>(a.cellOf, a.offsets, a.bucketTmp, a.posF, a.rad, a.n, a.bucket,
-                                                      a.sPos, a.sRad);
+        StabilizeWells<<<ablocks, T, 0, s>>>(a.cellOf, a.offsets, a.bucketTmp, a.posF, a.rad, a.wellOf, a.wells, a.n,
+                                             a.bucket, a.sPos, a.sRad, a.sCell);
         const int TF = (a.forceThreads == 64 || a.forceThreads == 256) ? a.forceThreads : 128;
         const unsigned fblocks = static_cast<unsigned>((a.n + TF - 1) / TF);
         if (a.velState != nullptr)
         {
-            ForcesWellsMove<<<fblocks, TF, 0, s>>>(a.bucket, a.offsets, a.sPos, a.sRad, a.wellOf, a.wells, a.n,
-                                                   a.interactionRad, a.R, a.k, a.friction, a.maxVel, a.vel, a.posOut,
-                                                   a.velState);
+            ForcesWellsMove<<<fblocks, TF, 0, s>>>(a.bucket, a.offsets, a.sPos, a.sRad, a.sCell, a.wellOf, a.wells,
+                                                   a.n, a.interactionRad, a.R, a.k, a.friction, a.maxVel, a.vel,
+                                                   a.posOut, a.velState);
         }
         else
         {
-            ForcesWells<<<fblocks, TF, 0, s>>>(a.bucket, a.offsets, a.sPos, a.sRad, a.wellOf, a.wells, a.n,
+            ForcesWells<<<fblocks, TF, 0, s>>>(a.bucket, a.offsets, a.sPos, a.sRad, a.sCell, a.wellOf, a.wells, a.n,
                                                a.interactionRad, a.R, a.k, a.vel);
         }
         CountLaunch(7);

@@ -10,12 +10,26 @@ struct hal_cuda_agents;
 
 namespace halcuda
 {
-    // One well's grid inside the concatenated cell array.
+    // The wells' agents are binned in coarse bins of kWellBin x kWellBin
+    // cells: the wells hold far fewer agents than cells (the batched workload:
+    // 5.2M agents in 109M cells), and the scan over the bins costs
+    // kWellBin^2 times less than one over the cells.  Within a bin the agents
+    // are ordered by (cell, agent index), so each cell's agents are a run of
+    // its bin in the order of a per-cell binning.
+    constexpr int32_t kWellBin = 4;
+
+    inline int64_t WellBins(int32_t xDim, int32_t yDim)
+    {
+        return static_cast<int64_t>((xDim + kWellBin - 1) / kWellBin) * ((yDim + kWellBin - 1) / kWellBin);
+    }
+
+    // One well's grid inside the concatenated bin array.
     struct AgentWellDev
     {
-        int64_t cellBase;       // first cell of the well in the concatenation
+        int64_t binBase;        // first coarse bin of the well in the concatenation
         int32_t xDim, yDim;
         int32_t wrapX, wrapY;
+        int32_t binsY;          // coarse bins along y
     };
 
     // Device arrays of one pass (n agents, `cells` concatenated cells).
@@ -26,12 +40,13 @@ namespace halcuda
         const int32_t *wellOf;     // n
         const AgentWellDev *wells;
         int32_t n;
-        int64_t cells;
+        int64_t cells;             // coarse bins of all wells (WellBins summed)
         float2 *posF, *sPos;       // n each
         float *sRad;               // n
-        int32_t *cellOf, *arrival, *bucketTmp, *bucket;  // n each
-        int32_t *counts;           // cells, zero on entry (each binning's scan clears them again)
-        int32_t *offsets;          // cells + 1
+        int32_t *cellOf, *arrival, *bucketTmp, *bucket;  // n each (cellOf: the agent's bin)
+        int32_t *sCell;            // n: each sorted slot's cell within its well
+        int32_t *counts;           // cells (bins), zero on entry (each binning's scan clears them again)
+        int32_t *offsets;          // cells (bins) + 1
         int32_t *tileSums;         // AgentScanTiles(cells)
         double interactionRad;
         float R, k;

@@ -89,8 +89,8 @@ namespace halcuda
         std::pair<double, double> agentsTunedFor{-1.0, 0.0};  // (R, k) the force block size was tuned for
 
         // agents
-        std::vector<int64_t> cellBase;   // well -> first cell in the concatenation, or -1
-        int64_t agentCells = 0;
+        std::vector<int64_t> cellBase;   // well -> first coarse agent bin in the concatenation, or -1
+        int64_t agentCells = 0;          // coarse agent bins of all wells with agents
         int64_t agentCap = 0;
         int32_t nAgents = 0;
         std::vector<int32_t> counts;     // agents per well (last set_agents)
@@ -100,7 +100,7 @@ namespace halcuda
         bool motion = false;             // agents move after their forces each tick
         float friction = 1.0f, maxVel = -1.0f;
         DevBuf<float2> posF, sPos;
-        DevBuf<int32_t> wellOf, cellOf, arrival, bucketTmp, bucket, binCounts, offsets, tileSums;
+        DevBuf<int32_t> wellOf, cellOf, arrival, bucketTmp, bucket, sCell, binCounts, offsets, tileSums;
 
         GraphCache graph[2];             // one tick, by parity
 
@@ -169,7 +169,7 @@ namespace halcuda
                 if (desc[w].maxAgents > 0)
                 {
                     cellBase[w] = agentCells;
-                    agentCells += static_cast<int64_t>(Cells(w));
+                    agentCells += WellBins(desc[w].xDim, desc[w].yDim);
                     agentCap += desc[w].maxAgents;
                 }
             }
@@ -283,11 +283,12 @@ namespace halcuda
             std::vector<AgentWellDev> wd(desc.size());
             for (size_t w = 0; w < desc.size(); w++)
             {
-                wd[w].cellBase = std::max<int64_t>(cellBase[w], 0);
+                wd[w].binBase = std::max<int64_t>(cellBase[w], 0);
                 wd[w].xDim = desc[w].xDim;
                 wd[w].yDim = desc[w].yDim;
                 wd[w].wrapX = desc[w].wrapX;
                 wd[w].wrapY = desc[w].wrapY;
+                wd[w].binsY = (desc[w].yDim + kWellBin - 1) / kWellBin;
             }
             HAL_TRY(Upload(agentWells, wd));
             const size_t m = static_cast<size_t>(agentCap);
@@ -304,6 +305,7 @@ namespace halcuda
             HAL_TRY(arrival.Alloc(m, "cudaMalloc(well agents)"));
             HAL_TRY(bucketTmp.Alloc(m, "cudaMalloc(well agents)"));
             HAL_TRY(bucket.Alloc(m, "cudaMalloc(well agents)"));
+            HAL_TRY(sCell.Alloc(m, "cudaMalloc(well agents)"));
             const size_t C = static_cast<size_t>(agentCells);
             HAL_TRY(binCounts.Alloc(C, "cudaMalloc(well bins)"));
             // zero once: every binning's scan clears the counts it read
@@ -453,6 +455,7 @@ namespace halcuda
             a.arrival = arrival.p;
             a.bucketTmp = bucketTmp.p;
             a.bucket = bucket.p;
+            a.sCell = sCell.p;
             a.counts = binCounts.p;
             a.offsets = offsets.p;
             a.tileSums = tileSums.p;

@@ -5,13 +5,19 @@ by its constant-rate limit (the reference-pinned ADI tick) and by finite
 differences (tests/test_adjoint_oracle.py):
 * forward: FP32 device steps against FP64, max-rel <= 2e-6 (1 + max D) per
   step; for a constant rate it is the ADI tick of hal.Adi;
-* gradient: relative L2 error of dL/dD and dL/dsrc and relative error of
-  dL/ddecay <= 2e-3 against the FP64 adjoint;
+* gradient: relative L2 error of dL/dD and dL/dsrc <= 1e-4 against the FP64
+  adjoint (40 steps and the 500-step workload); dL/ddecay = -sum_t <gbar_t,
+  f_t> is a sum with heavy cancellation over every step and cell, so its FP32
+  inputs' rounding leaves a larger relative error: 1e-3 over 40 steps, 1e-2
+  over 500;
 * checkpointing: the gradient does not depend on the checkpoint interval
   (recomputed states are bit-identical);
-* finite differences of the device loss (FP32, h = 1e-3) agree with the
-  directional derivatives within 2% plus three times the rounding noise of
-  the difference (estimated from the differences at h and 2h).
+* finite differences of the device loss (h = 1e-3) agree with the directional
+  derivatives within 2% plus a fixed bound on the difference's rounding
+  noise: the loss is reduced in FP64 from the FP32 final field, whose error
+  eps_f against the FP64 model is measured here, so each loss is within
+  |r| eps_f + eps_f^2 / 2 of the exact one (r = f_T - target), and a central
+  difference within that over h; the bound allows four times it.
 """
 from __future__ import annotations
 
@@ -69,9 +75,9 @@ def test_forward_and_gradient_match_fp64_adjoint(hal, oracle, wrap):
         loss, gD, gK, gS = a.gradient(D, decay, src)
     assert max_rel(fT, fT_ref) <= 2e-6 * (1 + 5.0) * steps
     assert abs(loss - loss_ref) <= 1e-3 * loss_ref and abs(loss_f - loss) <= 1e-6 * loss
-    assert rel_l2(gD, gD_ref) <= 2e-3
-    assert rel_l2(gS, gS_ref) <= 2e-3
-    assert abs(gK - gK_ref) <= 2e-3 * abs(gK_ref)
+    assert rel_l2(gD, gD_ref) <= 1e-4
+    assert rel_l2(gS, gS_ref) <= 1e-4
+    assert abs(gK - gK_ref) <= 1e-3 * abs(gK_ref)
 
 
 def test_gradient_independent_of_checkpoint_interval(hal):
@@ -89,36 +95,38 @@ def test_gradient_independent_of_checkpoint_interval(hal):
         assert abs(gK - out[0][2]) <= 1e-9 * abs(out[0][2])
 
 
-def test_finite_differences_on_the_device(hal):
-    """Central differences of the device loss, h = 1e-3, on a 128^2 grid."""
+def test_finite_differences_on_the_device(hal, oracle):
+    """Central differences of the device loss, h = 1e-3, on a 128^2 grid,
+    within 2% plus a fixed bound on their rounding noise."""
     n, steps = 128, 100
     f0, D, Dt, src = _problem(n, steps, 4)
     rng = np.random.default_rng(9)
+    h = 1e-3
     with hal.Adjoint(n, n) as a:
         a.set_problem(f0, np.zeros_like(f0), steps, 22)
         _, target = a.forward(Dt, 0.005, src, want_field=True)
         a.set_problem(f0, target, steps, 22)
         loss, gD, gK, gS = a.gradient(D, 0.005, src)
-        h = 1e-3
+        _, fT = a.forward(D, 0.005, src, want_field=True)
+        # the FP32 forward's error against the FP64 model at D
+        _, fT64, *_ = oracle.dadi_loss_grad(f0, target, D, 0.005, src, n, n, steps, grad=False)
+        eps_f = float(np.linalg.norm(fT.astype(np.float64) - fT64))
+        assert eps_f <= 1e-6 * np.linalg.norm(fT64)
+        noise = 4.0 * (np.sqrt(2.0 * loss) * eps_f + 0.5 * eps_f * eps_f) / h
 
         def fd(f):
-            return (f(h) - f(-h)) / (2 * h), (f(2 * h) - f(-2 * h)) / (4 * h)
+            return (f(h) - f(-h)) / (2 * h)
 
-        # The device loss is FP32: a central difference at h carries rounding
-        # noise of order (loss rounding) / h.  Its size is estimated from the
-        # spread between the differences at h and 2h (the truncation error,
-        # O(h^2), is far smaller), and the check allows three times that
-        # spread on top of a 2% relative tolerance.
         for _ in range(4):
             v = rng.standard_normal(n * n).astype(np.float32)
-            f1, f2 = fd(lambda t: a.forward(D + np.float32(t) * v, 0.005, src))
+            f1 = fd(lambda t: a.forward(D + np.float32(t) * v, 0.005, src))
             dd = float(gD.astype(np.float64) @ v.astype(np.float64))
-            assert abs(f1 - dd) <= 2e-2 * abs(dd) + 3 * abs(f1 - f2), (f1, f2, dd)
-        f1, f2 = fd(lambda t: a.forward(D, 0.005 + t, src))
-        assert abs(f1 - gK) <= 2e-2 * abs(gK) + 3 * abs(f1 - f2), (f1, f2, gK)
-        f1, f2 = fd(lambda t: a.forward(D, 0.005, src + np.float32(t) * np.sign(gS)))
+            assert abs(f1 - dd) <= 2e-2 * abs(dd) + noise, (f1, dd, noise)
+        f1 = fd(lambda t: a.forward(D, 0.005 + t, src))
+        assert abs(f1 - gK) <= 2e-2 * abs(gK) + noise, (f1, gK, noise)
+        f1 = fd(lambda t: a.forward(D, 0.005, src + np.float32(t) * np.sign(gS)))
         ds = float(np.abs(gS.astype(np.float64)).sum())
-        assert abs(f1 - ds) <= 2e-2 * abs(ds) + 3 * abs(f1 - f2), (f1, f2, ds)
+        assert abs(f1 - ds) <= 2e-2 * abs(ds) + noise, (f1, ds, noise)
 
 
 def test_rejects_bad_input(hal):
@@ -148,9 +156,10 @@ def test_parameter_recovery_workload_on_a_64_copy(hal, oracle):
     with hal.Adjoint(n, n) as a:
         a.set_problem(w["f0"], target.astype(np.float32), w["steps"], w["checkpoint_every"])
         loss, gD, gK, gS = a.gradient(w["D"], w["decay"], w["src"])
-    # over 500 steps the FP32 forward error of f_T enters the residual
-    # f_T - target, which seeds every adjoint field: 1e-2 relative
-    assert abs(loss - loss_ref) <= 1e-3 * loss_ref
-    assert rel_l2(gD, gD_ref) <= 1e-2
-    assert rel_l2(gS, gS_ref) <= 1e-2
+    # the field gradients to 1e-4 (measured: about 5e-6 for dL/dD and 4e-5
+    # for dL/dsrc); dL/ddecay sums 500 steps of <gbar, f> with heavy
+    # cancellation, so its FP32 inputs leave about 5e-3
+    assert abs(loss - loss_ref) <= 1e-4 * loss_ref
+    assert rel_l2(gD, gD_ref) <= 1e-4
+    assert rel_l2(gS, gS_ref) <= 1e-4
     assert abs(gK - gK_ref) <= 1e-2 * abs(gK_ref)
