@@ -662,12 +662,44 @@ namespace halcuda
                         re[j] = __ldg(offsets + cell + (yEnd - yStart));
                     }
                 }
-#pragma unroll
-                for (int j = 0; j < 4; j++)
+                // The rows' runs, one after another, form one sequence of
+                // candidates in the visiting order; it is walked in groups of
+                // kGroup whose loads are issued before any of them is used, so
+                // a thread waits for one round trip per group, not per
+                // candidate.
+                constexpr int kGroup = 4;
+                const int32_t c1 = re[0] - rs[0];
+                const int32_t c2 = c1 + (re[1] - rs[1]);
+                const int32_t c3 = c2 + (re[2] - rs[2]);
+                const int32_t total = c3 + (re[3] - rs[3]);
+                for (int32_t k0 = 0; k0 < total; k0 += kGroup)
                 {
-                    for (int32_t q = rs[j]; q < re[j]; q++)
+                    int32_t qs[kGroup];
+                    V2<T> pj[kGroup];
+                    T rj[kGroup];
+#pragma unroll
+                    for (int u = 0; u < kGroup; u++)
                     {
-                        visit(q);
+                        const int32_t k = k0 + u;
+                        qs[u] = (k >= total) ? -1
+                                : (k < c1)   ? rs[0] + k
+                                : (k < c2)   ? rs[1] + (k - c1)
+                                : (k < c3)   ? rs[2] + (k - c2)
+                                             : rs[3] + (k - c3);
+                        if (qs[u] >= 0)
+                        {
+                            pj[u] = sPos[qs[u]];
+                            rj[u] = sRad[qs[u]];
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < kGroup; u++)
+                    {
+                        if (qs[u] >= 0 && qs[u] != slot)
+                        {
+                            PairStep<T, LAW, SUM, GRID>(px, py, rad, pj[u], rj[u], R, lp, xDimF, yDimF, wrapX, wrapY,
+                                                        vx, vy, sum);
+                        }
                     }
                 }
                 return result();
