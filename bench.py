@@ -449,10 +449,12 @@ def secondary_wells(hal, torch, stream, ticks=20, plain_ticks=3):
         b.set_agents(w["counts"], w["positions"], w["radii"])
         b.run_ticks(4, R, k)  # warm-up; captures both parities' graphs
         b.sync()
+        l0 = hal.launch_count()
         ev0.record(stream)
         b.run_ticks(ticks, R, k)
         ev1.record(stream)
         ev1.synchronize()
+        launches_per_tick = (hal.launch_count() - l0) / ticks
         ms_batched = ev0.elapsed_time(ev1) / ticks
         stages = b.profile(3, R, k)
 
@@ -510,6 +512,8 @@ def secondary_wells(hal, torch, stream, ticks=20, plain_ticks=3):
             "agents_per_s": n_ag / (ms_batched * 1e-3),
             "ms_per_tick_batched": ms_batched, "ms_per_tick_per_well_launches": ms_plain,
             "speedup_vs_per_well_launches": ms_plain / ms_batched,
+            "kernel_launches_per_tick": launches_per_tick,
+            "agent_bins": "4x4-cell coarse bins per well, ordered by (cell, agent index) within a bin",
             "ms_by_stage": {"explicit": stages[0], "adi_x": stages[1], "adi_y": stages[2],
                             "agents": stages[3], "tick": stages[4]},
             "cells": cells, "agents": n_ag,

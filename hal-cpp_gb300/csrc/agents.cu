@@ -1002,26 +1002,33 @@ namespace halcuda
                     retX = (retX < 0) ? retX + xDim : retX;
                 }
                 const int32_t binRow = static_cast<int32_t>(wd.binBase) + (retX / kWellBin) * wd.binsY;
-                for (int32_t ySq = yStart; ySq < yEnd; ySq++)
+                // the row's window cells as runs that stay in one bin and do
+                // not wrap: a run's cells are consecutive cell indices, so its
+                // agents are one stretch of the bin's (cell, index) order
+                for (int32_t ySq = yStart; ySq < yEnd;)
                 {
                     int32_t retY = ySq;
                     if (retY < 0 || retY >= yDim)
                     {
-                        retY %= yDim;
+                        retY %= yDim;  // only reached on a wrapped axis (clamped otherwise)
                         retY = (retY < 0) ? retY + yDim : retY;
                     }
-                    const int32_t cell = retX * yDim + retY;
-                    const int32_t b = binRow + retY / kWellBin;
-                    const int32_t s = __ldg(offsets + b);
-                    const int32_t e = __ldg(offsets + b + 1);
+                    const int32_t by = retY / kWellBin;
+                    const int32_t binEnd = min((by + 1) * kWellBin, yDim);  // first y past the bin
+                    const int32_t run = min(yEnd - ySq, binEnd - retY);
+                    ySq += run;
+                    const int32_t cLo = retX * yDim + retY;
+                    const int32_t cHi = cLo + run - 1;
+                    const int32_t s = __ldg(offsets + binRow + by);
+                    const int32_t e = __ldg(offsets + binRow + by + 1);
                     for (int32_t t = s; t < e; t++)
                     {
                         const int32_t ct = __ldg(sCell + t);
-                        if (ct > cell)
+                        if (ct > cHi)
                         {
                             break;  // the bin is ordered by cell
                         }
-                        if (ct == cell && t != slot)
+                        if (ct >= cLo && t != slot)
                         {
                             PairStep<float, kLawLinear, false, false>(pf.x, pf.y, rad, sPos[t], sRad[t], R, lp, xDimF,
                                                                       yDimF, wd.wrapX, wd.wrapY, vx, vy, sum);
