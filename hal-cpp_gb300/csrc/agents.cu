@@ -319,6 +319,56 @@ namespace halcuda
             }
         }
 
+        // Passes 2 and 3 in one launch, for grids of at most kScanThreads
+        // tiles: each CTA reduces the tile sums before its own (one per
+        // thread) into its tile's prefix, then runs ScanApply<true>'s tile
+        // scan.  This saves the single-CTA ScanTiles launch between them.
+        __global__ void __launch_bounds__(kScanThreads) ScanApplySum(int32_t *__restrict__ counts, int64_t C,
+                                                                     const int32_t *__restrict__ tileSums,
+                                                                     int32_t *__restrict__ offsets, int32_t n)
+        {
+            ChainEntry();
+            const int32_t before = (static_cast<int32_t>(threadIdx.x) < static_cast<int32_t>(blockIdx.x))
+                                       ? tileSums[threadIdx.x]
+                                       : 0;
+            int32_t unused;
+            const int32_t prefix = BlockExclusiveScan(before, unused);  // the block total
+            const int64_t base = static_cast<int64_t>(blockIdx.x) * kScanTile + threadIdx.x * kScanItems;
+            int32_t v[kScanItems];
+            LoadItems(counts, base, C, v);
+            int32_t any = 0;
+#pragma unroll
+            for (int q = 0; q < kScanItems; q++)
+            {
+                any |= v[q];
+            }
+            if (any != 0)
+            {
+                const int32_t zeros[kScanItems] = {0, 0, 0, 0};
+                StoreItems(counts, base, C, zeros);
+            }
+            int32_t sum = 0;
+#pragma unroll
+            for (int q = 0; q < kScanItems; q++)
+            {
+                sum += v[q];
+            }
+            int32_t excl;
+            BlockExclusiveScan(sum, excl);
+            int32_t o[kScanItems];
+            o[0] = prefix + excl;
+#pragma unroll
+            for (int q = 1; q < kScanItems; q++)
+            {
+                o[q] = o[q - 1] + v[q - 1];
+            }
+            StoreItems(offsets, base, C, o);
+            if (blockIdx.x == 0 && threadIdx.x == 0)
+            {
+                offsets[C] = n;
+            }
+        }
+
         __global__ void Scatter(const int32_t *__restrict__ cellOf, const int32_t *__restrict__ arrival,
                                 const int32_t *__restrict__ offsets, int32_t n, int32_t *__restrict__ bucketTmp)
         {
@@ -1187,9 +1237,17 @@ namespace halcuda
                 cudaEventRecord(ev[0], s);
             }
             LaunchChained(ScanReduce, nTiles, kScanThreads, s, counts.p, C, tileSums.p);
-            LaunchChained(ScanTiles, 1u, kScanThreads, s, tileSums.p, nTiles);
-            LaunchChained(ScanApply<true>, nTiles, kScanThreads, s, counts.p, C, tileSums.p, offsets.p, n);
-            CountLaunch(3);
+            if (nTiles <= kScanThreads)
+            {
+                LaunchChained(ScanApplySum, nTiles, kScanThreads, s, counts.p, C, tileSums.p, offsets.p, n);
+                CountLaunch(2);
+            }
+            else
+            {
+                LaunchChained(ScanTiles, 1u, kScanThreads, s, tileSums.p, nTiles);
+                LaunchChained(ScanApply<true>, nTiles, kScanThreads, s, counts.p, C, tileSums.p, offsets.p, n);
+                CountLaunch(3);
+            }
             countsDirty = (cudaPeekAtLastError() != cudaSuccess);
             if (ev)
             {
