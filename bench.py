@@ -818,7 +818,19 @@ def profile_case(case, n, iters):
             b.run_ticks(1, w["interactionRad"], w["springConstant"])  # autotune + graph capture
             b.sync()
             ms = b.profile(iters, w["interactionRad"], w["springConstant"])
-        print("wells: " + ", ".join(f"{v:.3f}" for v in ms) + " ms (explicit, adi x, adi y, agents, tick)")
+            # the graph-replayed tick, whose three branches run concurrently
+            import torch
+
+            st = torch.cuda.ExternalStream(b.stream())
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            b.run_ticks(2, w["interactionRad"], w["springConstant"])
+            e0.record(st)
+            b.run_ticks(iters, w["interactionRad"], w["springConstant"])
+            e1.record(st)
+            e1.synchronize()
+            replay = e0.elapsed_time(e1) / iters
+        print("wells: " + ", ".join(f"{v:.3f}" for v in ms) + " ms (explicit, adi x, adi y, agents, tick; "
+              f"stages in order); graph-replayed tick {replay:.3f} ms")
     elif case == "adjoint":
         rng = np.random.default_rng(4)
         f0 = workloads.gaussian_blobs(n, rng, 8).astype(np.float32)

@@ -958,6 +958,7 @@ namespace halcuda
                                       int32_t *__restrict__ binOf, int32_t *__restrict__ arrival,
                                       int32_t *__restrict__ counts)
         {
+            ChainEntry();
             const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
             if (i >= n)
             {
@@ -983,6 +984,7 @@ namespace halcuda
                                        int32_t *__restrict__ bucket, float2 *__restrict__ sPos,
                                        float *__restrict__ sRad, int32_t *__restrict__ sCell)
         {
+            ChainEntry();
             const int32_t q = blockIdx.x * blockDim.x + threadIdx.x;
             if (q >= n)
             {
@@ -1095,6 +1097,7 @@ namespace halcuda
                                     const AgentWellDev *__restrict__ wells, int32_t n, double interactionRad, float R,
                                     float k, float *__restrict__ vel)
         {
+            ChainEntry();
             const int32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
             if (slot >= n)
             {
@@ -1114,6 +1117,7 @@ namespace halcuda
                                         float R, float k, float friction, float maxVel, float *__restrict__ vel,
                                         float2 *__restrict__ pos, float2 *__restrict__ velocity)
         {
+            ChainEntry();
             const int32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
             if (slot >= n)
             {
@@ -2096,32 +2100,33 @@ namespace halcuda
         const int T = 256;
         const unsigned ablocks = static_cast<unsigned>((a.n + T - 1) / T);
         const int32_t nTiles = AgentScanTiles(a.cells);
-        BinCountWells<<<ablocks, T, 0, s>>>(a.pos, a.wellOf, a.wells, a.n, a.posF, a.cellOf, a.arrival, a.counts);
-        ScanReduce<<<nTiles, kScanThreads, 0, s>>>(a.counts, a.cells, a.tileSums);
-        ScanTiles<<<1, kScanThreads, 0, s>>>(a.tileSums, nTiles);
+        LaunchChained(BinCountWells, ablocks, T, s, a.pos, a.wellOf, a.wells, a.n, a.posF, a.cellOf, a.arrival,
+                      a.counts);
+        LaunchChained(ScanReduce, nTiles, kScanThreads, s, a.counts, a.cells, a.tileSums);
+        LaunchChained(ScanTiles, 1u, kScanThreads, s, a.tileSums, nTiles);
         if (clearInScan)
         {
-            ScanApply<true><<<nTiles, kScanThreads, 0, s>>>(a.counts, a.cells, a.tileSums, a.offsets, a.n);
+            LaunchChained(ScanApply<true>, nTiles, kScanThreads, s, a.counts, a.cells, a.tileSums, a.offsets, a.n);
         }
         else
         {
-            ScanApply<false><<<nTiles, kScanThreads, 0, s>>>(a.counts, a.cells, a.tileSums, a.offsets, a.n);
+            LaunchChained(ScanApply<false>, nTiles, kScanThreads, s, a.counts, a.cells, a.tileSums, a.offsets, a.n);
         }
-        Scatter<<<ablocks, T, 0, s>>>(a.cellOf, a.arrival, a.offsets, a.n, a.bucketTmp);
-        StabilizeWells<<<ablocks, T, 0, s>>>(a.cellOf, a.offsets, a.bucketTmp, a.posF, a.rad, a.wellOf, a.wells, a.n,
-                                             a.bucket, a.sPos, a.sRad, a.sCell);
+        LaunchChained(Scatter, ablocks, T, s, a.cellOf, a.arrival, a.offsets, a.n, a.bucketTmp);
+        LaunchChained(StabilizeWells, ablocks, T, s, a.cellOf, a.offsets, a.bucketTmp, a.posF, a.rad, a.wellOf,
+                      a.wells, a.n, a.bucket, a.sPos, a.sRad, a.sCell);
         const int TF = (a.forceThreads == 64 || a.forceThreads == 256) ? a.forceThreads : 128;
         const unsigned fblocks = static_cast<unsigned>((a.n + TF - 1) / TF);
         if (a.velState != nullptr)
         {
-            ForcesWellsMove<<<fblocks, TF, 0, s>>>(a.bucket, a.offsets, a.sPos, a.sRad, a.sCell, a.wellOf, a.wells,
-                                                   a.n, a.interactionRad, a.R, a.k, a.friction, a.maxVel, a.vel,
-                                                   a.posOut, a.velState);
+            LaunchChained(ForcesWellsMove, fblocks, TF, s, a.bucket, a.offsets, a.sPos, a.sRad, a.sCell, a.wellOf,
+                          a.wells, a.n, a.interactionRad, a.R, a.k, a.friction, a.maxVel, a.vel, a.posOut,
+                          a.velState);
         }
         else
         {
-            ForcesWells<<<fblocks, TF, 0, s>>>(a.bucket, a.offsets, a.sPos, a.sRad, a.sCell, a.wellOf, a.wells, a.n,
-                                               a.interactionRad, a.R, a.k, a.vel);
+            LaunchChained(ForcesWells, fblocks, TF, s, a.bucket, a.offsets, a.sPos, a.sRad, a.sCell, a.wellOf,
+                          a.wells, a.n, a.interactionRad, a.R, a.k, a.vel);
         }
         CountLaunch(7);
         return LaunchStatus("agent wells");

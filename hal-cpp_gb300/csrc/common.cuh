@@ -165,6 +165,25 @@ namespace halcuda
         }
     };
 
+    // An event without timing, for ordering streams (fork and join).
+    struct EventSlot
+    {
+        cudaEvent_t e = nullptr;
+
+        int Create(const char *what)
+        {
+            return CudaStatus(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), what);
+        }
+
+        ~EventSlot()
+        {
+            if (e != nullptr)
+            {
+                cudaEventDestroy(e);
+            }
+        }
+    };
+
     // Cached CUDA graph of a fixed launch sequence, re-captured when its key
     // changes.
     struct GraphCache

@@ -55,6 +55,10 @@ namespace halcuda
     {
         int device = 0;
         StreamSlot stream;
+        // Graph branch of a tick: the explicit wells' tiles run on their own
+        // stream beside the agent pass and the ADI sweeps (EnqueueTick).
+        StreamSlot sideExplicit;
+        EventSlot fork, joinExplicit;
         std::vector<hal_cuda_well_desc> desc;
         DevBuf<float> arena;
         std::vector<size_t> offF0, offF1, offSrc, offW;
@@ -135,6 +139,9 @@ namespace halcuda
             device = CurrentDevice();
             HAL_TRY(CudaStatus(cudaSetDevice(device), "cudaSetDevice"));
             HAL_TRY(stream.Create("cudaStreamCreate"));
+            HAL_TRY(sideExplicit.Create("cudaStreamCreate"));
+            HAL_TRY(fork.Create("cudaEventCreate"));
+            HAL_TRY(joinExplicit.Create("cudaEventCreate"));
             desc.assign(wells, wells + n);
             const size_t nw = static_cast<size_t>(n);
             offF0.resize(nw);
@@ -408,10 +415,40 @@ namespace halcuda
             return CudaStatus(cudaStreamSynchronize(stream.Get()), "wells tables");
         }
 
-        // One tick of every well from parity c, enqueued on s.  Each stage
-        // may record an event (profiling).
+        // One tick of every well from parity c, enqueued on s.  With ev, the
+        // stages run one after another on s and each records an event
+        // (profiling).  Without, the explicit wells' tiles run on a branch
+        // of their own beside the agent pass and the ADI sweeps, which stay
+        // in order on s: the three read and write disjoint buffers.  The
+        // bandwidth-bound explicit tiles then overlap the agent pass, a
+        // chain of latency-bound gathers.  (The ADI sweep tiles hold a whole
+        // SM's registers each, so a branch beside them finds no free slot.)
         int EnqueueTick(int c, double R, double k, cudaStream_t s, cudaEvent_t *ev)
         {
+            if (ev == nullptr)
+            {
+                const bool exp = nTiles4 > 0 || nTiles1 > 0;
+                if (exp)
+                {
+                    cudaStream_t e = sideExplicit.Get();
+                    HAL_TRY(CudaStatus(cudaEventRecord(fork.e, s), "cudaEventRecord(fork)"));
+                    HAL_TRY(CudaStatus(cudaStreamWaitEvent(e, fork.e, 0), "cudaStreamWaitEvent(fork)"));
+                    HAL_TRY(LaunchTickTiles(tickTab[c].p, tiles4.p, nTiles4, 4, e));
+                    HAL_TRY(LaunchTickTiles(tickTab[c].p, tiles1.p, nTiles1, 1, e));
+                    HAL_TRY(CudaStatus(cudaEventRecord(joinExplicit.e, e), "cudaEventRecord(join)"));
+                }
+                if (nAgents > 0)
+                {
+                    HAL_TRY(LaunchAgentWells(AgentArgs(R, k), s));
+                }
+                HAL_TRY(LaunchSweepTiles(kSweepW, sxTab[c].p, tilesX.p, nTilesX, smemX, s));
+                HAL_TRY(LaunchSweepTiles(kSweepTick, syTab[c].p, tilesY.p, nTilesY, smemY, s));
+                if (exp)
+                {
+                    HAL_TRY(CudaStatus(cudaStreamWaitEvent(s, joinExplicit.e, 0), "cudaStreamWaitEvent(join)"));
+                }
+                return HAL_CUDA_OK;
+            }
             HAL_TRY(LaunchTickTiles(tickTab[c].p, tiles4.p, nTiles4, 4, s));
             HAL_TRY(LaunchTickTiles(tickTab[c].p, tiles1.p, nTiles1, 1, s));
             if (ev)

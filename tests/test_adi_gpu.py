@@ -162,6 +162,47 @@ def test_tensor_staged_tick_against_oracle(hal, oracle, xd, yd, wrapX, wrapY, di
     assert rel_l2(out, exp) <= 1e-5, rel_l2(out, exp)
 
 
+@pytest.mark.parametrize("wrapX,wrapY,dirichlet,uptake", [(True, False, True, 2e-3), (False, True, False, 0.0)])
+def test_ragged_last_tile_tick_against_oracle(hal, oracle, wrapX, wrapY, dirichlet, uptake):
+    """x-lines of 2048 over 1940 lines: tensor-staged 16-line x-sweep tiles,
+    the last one 4 lines wide, with a periodic or Dirichlet x-axis, a dense
+    source, decay and uptake, against the FP64 oracle."""
+    xd, yd = 2048, 1940
+    rng = np.random.default_rng(77 + wrapX)
+    n = xd * yd
+    f0 = rng.random(n).astype(np.float32)
+    src = (rng.random(n) * 1e-3).astype(np.float32)
+    ghost = rng.random(2 * (xd + yd)).astype(np.float32) if dirichlet else None
+    r, decay, ticks = 5.0, 1e-2, 3
+    nAgents = 100000
+    pos = np.empty(2 * nAgents, np.float32)
+    pos[0::2] = rng.random(nAgents) * xd
+    pos[1::2] = rng.random(nAgents) * yd
+    with hal.Agents(xd, yd, nAgents) as ag, hal.Adi(xd, yd) as a:
+        counts = None
+        if uptake:
+            ag.upload(pos, np.full(nAgents, 0.5, np.float32))
+            ag.dispatch(1.0, 0.1)
+            ag.sync()
+            off, _ = ag.get_bins()
+            counts = np.diff(off).astype(np.int32)
+            a.set_uptake(ag, uptake)
+        a.set_field(f0)
+        a.set_source(src)
+        if ghost is not None:
+            a.set_dirichlet(ghost)
+        a.run_ticks(ticks, r, decay, wrapX, wrapY)
+        out = a.get_field()
+    exp = oracle.run_ticks(1, f0.astype(np.float64), xd, yd, r, wrapX, wrapY,
+                           None if ghost is None else ghost.astype(np.float64), decay,
+                           src_dense=src.astype(np.float64), uptake_count=counts, uptake=uptake, ticks=ticks,
+                           threads=16)
+    assert rel_l2(out, exp) <= 1e-5, rel_l2(out, exp)
+    # the last tile's four lines (y = 1936 .. 1939; HAL's layout is x * yDim + y)
+    last = out.reshape(xd, yd)[:, 1936:]
+    assert rel_l2(last, exp.reshape(xd, yd)[:, 1936:]) <= 1e-5
+
+
 LINES = [1, 2, 3, 31, 32, 33, 63, 64, 65, 100, 257, 1000, 2048, 4096]
 
 
