@@ -968,8 +968,8 @@ namespace halcuda
             const float px = pos[2 * static_cast<int64_t>(i)];
             const float py = pos[2 * static_cast<int64_t>(i) + 1];
             posF[i] = make_float2(px, py);
-            const int32_t b = static_cast<int32_t>(wd.binBase) + (CellCoord(px, wd.xDim) / kWellBin) * wd.binsY +
-                              CellCoord(py, wd.yDim) / kWellBin;
+            const int32_t b = static_cast<int32_t>(wd.binBase) + (CellCoord(px, wd.xDim) >> wd.binShift) * wd.binsY +
+                              (CellCoord(py, wd.yDim) >> wd.binShift);
             binOf[i] = b;
             arrival[i] = atomicAdd(counts + b, 1);
         }
@@ -1045,6 +1045,73 @@ namespace halcuda
             const float xDimF = static_cast<float>(xDim);
             const float yDimF = static_cast<float>(yDim);
             float vx = 0.0f, vy = 0.0f, sum = 0.0f;
+            const int32_t sh = wd.binShift;
+            const int32_t nRows = xEnd - xStart;
+            if (sh == 0 && nRows > 0 && nRows <= 4 && yStart >= 0 && yEnd <= yDim && yEnd > yStart)
+            {
+                // One cell per bin and a window whose y-range does not wrap:
+                // each window row is one run of consecutive bins, so one
+                // stretch of slots.  All rows' bounds are loaded before the
+                // first candidate; the rows' stretches, one after another,
+                // are walked in groups of four whose loads are issued before
+                // any of them is used.  The visiting order is unchanged.
+                int32_t rs[4], re[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                {
+                    rs[j] = 0;
+                    re[j] = 0;
+                    if (j < nRows)
+                    {
+                        int32_t retX = xStart + j;
+                        if (retX < 0 || retX >= xDim)
+                        {
+                            retX %= xDim;  // only reached on a wrapped axis (clamped otherwise)
+                            retX = (retX < 0) ? retX + xDim : retX;
+                        }
+                        const int32_t bin = static_cast<int32_t>(wd.binBase) + retX * wd.binsY + yStart;
+                        rs[j] = __ldg(offsets + bin);
+                        re[j] = __ldg(offsets + bin + (yEnd - yStart));
+                    }
+                }
+                constexpr int kGroup = 4;
+                const int32_t c1 = re[0] - rs[0];
+                const int32_t c2 = c1 + (re[1] - rs[1]);
+                const int32_t c3 = c2 + (re[2] - rs[2]);
+                const int32_t total = c3 + (re[3] - rs[3]);
+                for (int32_t k0 = 0; k0 < total; k0 += kGroup)
+                {
+                    int32_t qs[kGroup];
+                    float2 pj[kGroup];
+                    float rj[kGroup];
+#pragma unroll
+                    for (int u = 0; u < kGroup; u++)
+                    {
+                        const int32_t kk = k0 + u;
+                        qs[u] = (kk >= total) ? -1
+                                : (kk < c1)   ? rs[0] + kk
+                                : (kk < c2)   ? rs[1] + (kk - c1)
+                                : (kk < c3)   ? rs[2] + (kk - c2)
+                                              : rs[3] + (kk - c3);
+                        if (qs[u] >= 0)
+                        {
+                            pj[u] = sPos[qs[u]];
+                            rj[u] = sRad[qs[u]];
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < kGroup; u++)
+                    {
+                        if (qs[u] >= 0 && qs[u] != slot)
+                        {
+                            PairStep<float, kLawLinear, false, false>(pf.x, pf.y, rad, pj[u], rj[u], R, lp, xDimF,
+                                                                      yDimF, wd.wrapX, wd.wrapY, vx, vy, sum);
+                        }
+                    }
+                }
+                return make_float2(vx, vy);
+            }
+            const int32_t bs = 1 << sh;
             for (int32_t xSq = xStart; xSq < xEnd; xSq++)
             {
                 int32_t retX = xSq;
@@ -1053,7 +1120,7 @@ namespace halcuda
                     retX %= xDim;  // only reached on a wrapped axis (clamped otherwise)
                     retX = (retX < 0) ? retX + xDim : retX;
                 }
-                const int32_t binRow = static_cast<int32_t>(wd.binBase) + (retX / kWellBin) * wd.binsY;
+                const int32_t binRow = static_cast<int32_t>(wd.binBase) + (retX >> sh) * wd.binsY;
                 // the row's window cells as runs that stay in one bin and do
                 // not wrap: a run's cells are consecutive cell indices, so its
                 // agents are one stretch of the bin's (cell, index) order
@@ -1065,8 +1132,8 @@ namespace halcuda
                         retY %= yDim;  // only reached on a wrapped axis (clamped otherwise)
                         retY = (retY < 0) ? retY + yDim : retY;
                     }
-                    const int32_t by = retY / kWellBin;
-                    const int32_t binEnd = min((by + 1) * kWellBin, yDim);  // first y past the bin
+                    const int32_t by = retY >> sh;
+                    const int32_t binEnd = min((by + 1) * bs, yDim);  // first y past the bin
                     const int32_t run = min(yEnd - ySq, binEnd - retY);
                     ySq += run;
                     const int32_t cLo = retX * yDim + retY;

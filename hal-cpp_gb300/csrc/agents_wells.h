@@ -10,17 +10,32 @@ struct hal_cuda_agents;
 
 namespace halcuda
 {
-    // The wells' agents are binned in coarse bins of kWellBin x kWellBin
-    // cells: the wells hold far fewer agents than cells (the batched workload:
-    // 5.2M agents in 109M cells), and the scan over the bins costs
-    // kWellBin^2 times less than one over the cells.  Within a bin the agents
-    // are ordered by (cell, agent index), so each cell's agents are a run of
-    // its bin in the order of a per-cell binning.
-    constexpr int32_t kWellBin = 4;
+    // The wells' agents are binned in coarse bins of b x b cells, b = 2^shift
+    // chosen per well from its agent capacity: the largest b <= 2^kWellMaxShift
+    // whose bins hold at most one agent on average.  Sparse wells (the
+    // batched workload's large wells: a few thousand agents in up to 1M
+    // cells) thereby scan b^2 times fewer bins than cells, while dense wells
+    // keep one cell per bin, whose force walk reads each window row as one
+    // run of bins.  Within a bin the agents are ordered by (cell, agent
+    // index), so each cell's agents are a run of its bin in the order of a
+    // per-cell binning.
+    constexpr int32_t kWellMaxShift = 3;
 
-    inline int64_t WellBins(int32_t xDim, int32_t yDim)
+    inline int32_t WellBinShift(int32_t xDim, int32_t yDim, int32_t maxAgents)
     {
-        return static_cast<int64_t>((xDim + kWellBin - 1) / kWellBin) * ((yDim + kWellBin - 1) / kWellBin);
+        const double cells = static_cast<double>(xDim) * static_cast<double>(yDim);
+        int32_t shift = 0;
+        while (shift < kWellMaxShift && static_cast<double>(maxAgents) * static_cast<double>(4 << (2 * shift)) <= cells)
+        {
+            shift++;
+        }
+        return shift;
+    }
+
+    inline int64_t WellBins(int32_t xDim, int32_t yDim, int32_t shift)
+    {
+        const int32_t b = 1 << shift;
+        return static_cast<int64_t>((xDim + b - 1) >> shift) * ((yDim + b - 1) >> shift);
     }
 
     // One well's grid inside the concatenated bin array.
@@ -30,6 +45,7 @@ namespace halcuda
         int32_t xDim, yDim;
         int32_t wrapX, wrapY;
         int32_t binsY;          // coarse bins along y
+        int32_t binShift;       // bins of 2^binShift x 2^binShift cells
     };
 
     // Device arrays of one pass (n agents, `cells` concatenated cells).

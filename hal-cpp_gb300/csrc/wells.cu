@@ -176,7 +176,8 @@ namespace halcuda
                 if (desc[w].maxAgents > 0)
                 {
                     cellBase[w] = agentCells;
-                    agentCells += WellBins(desc[w].xDim, desc[w].yDim);
+                    agentCells += WellBins(desc[w].xDim, desc[w].yDim,
+                                           WellBinShift(desc[w].xDim, desc[w].yDim, desc[w].maxAgents));
                     agentCap += desc[w].maxAgents;
                 }
             }
@@ -295,7 +296,8 @@ namespace halcuda
                 wd[w].yDim = desc[w].yDim;
                 wd[w].wrapX = desc[w].wrapX;
                 wd[w].wrapY = desc[w].wrapY;
-                wd[w].binsY = (desc[w].yDim + kWellBin - 1) / kWellBin;
+                wd[w].binShift = WellBinShift(desc[w].xDim, desc[w].yDim, desc[w].maxAgents);
+                wd[w].binsY = (desc[w].yDim + (1 << wd[w].binShift) - 1) >> wd[w].binShift;
             }
             HAL_TRY(Upload(agentWells, wd));
             const size_t m = static_cast<size_t>(agentCap);

@@ -101,6 +101,49 @@ def test_wells_equal_single_grid_handles(hal, oracle):
             assert np.array_equal(v, _alone_forces(hal, w, pos[i], rad[i])), (i, w)
 
 
+def test_wells_bin_sizes_equal_single_grid_forces(hal):
+    """Each well's bin size follows its agent capacity: one cell per bin for
+    dense wells (whose force walk reads each window row as one run of bins),
+    up to 8 x 8 cells for sparse ones.  Dense and sparse wells, with every
+    wrap combination and clustered agents, give the forces of their own
+    single-grid handles bit for bit."""
+    rng = np.random.default_rng(41)
+    specs = [  # xDim, yDim, kind, wrapX, wrapY, agents
+        (40, 50, "explicit", True, False, 3000),    # 1 x 1 bins
+        (64, 64, "adi", False, True, 5000),         # 1 x 1, y wraps: the general walk
+        (70, 30, "explicit", True, True, 2500),     # 1 x 1
+        (33, 47, "adi", False, False, 1200),        # 1 x 1, odd sides
+        (300, 300, "adi", False, False, 1000),      # 8 x 8 bins
+        (100, 300, "explicit", True, True, 400),    # 8 x 8, both wrap
+        (90, 130, "explicit", False, True, 700),    # 4 x 4
+    ]
+    wells, pos, rad, counts = [], [], [], []
+    for xd, yd, kind, wx, wy, na in specs:
+        wells.append(dict(xDim=xd, yDim=yd, kind=kind, diffRate=0.2 if kind == "explicit" else 2.0, decay=0.0,
+                          wrapX=wx, wrapY=wy, maxAgents=na))
+        m = na // 3
+        p = np.concatenate([rng.random((na - m, 2)) * (xd, yd),
+                            np.array([xd, yd]) * 0.4 + rng.normal(0, 3.0, (m, 2))])
+        hi = np.array([np.nextafter(np.float32(xd), np.float32(0)), np.nextafter(np.float32(yd), np.float32(0))])
+        pos.append(np.clip(p, 0, hi).astype(np.float32).ravel())
+        rad.append((0.3 + 0.4 * rng.random(na)).astype(np.float32))
+        counts.append(na)
+    with hal.Wells(wells) as b:
+        for i, w in enumerate(wells):
+            b.set_field(i, np.zeros(w["xDim"] * w["yDim"], np.float32))
+        b.set_agents(np.array(counts, np.int32), np.concatenate(pos), np.concatenate(rad))
+        b.run_ticks(1, R, K)
+        forces = b.get_forces()
+    at = 0
+    for i, w in enumerate(wells):
+        n = counts[i]
+        v = forces[2 * at: 2 * (at + n)]
+        at += n
+        exp = _alone_forces(hal, w, pos[i], rad[i])
+        assert np.abs(exp).max() > 0
+        assert np.array_equal(v, exp), (i, w)
+
+
 def test_autotune_keeps_state_and_results(hal):
     """The sweep-tile autotuner times the sweeps on the wells' own data
     without changing it, and whatever cap it picks, the ticks stay equal to
