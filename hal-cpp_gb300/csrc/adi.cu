@@ -37,6 +37,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -243,12 +244,12 @@ namespace halcuda
             }
         }
 
-        // Solution rows (SWZ).  The solve writes each chunk of a line back
-        // over its staged row with the 16-byte units permuted once more by
-        // SolSwz(line quad): the write-out reads the same unit of 4 (or 8)
-        // quads in one quarter-warp, and the extra permutation puts them in
-        // different bank groups.  The permutation is within a row, which the
-        // one thread that solved it writes whole.
+        // Solution rows (both layouts).  The solve writes each chunk of a
+        // line back over its staged row with the 16-byte units permuted once
+        // more by SolSwz(line quad): the write-out reads the same unit of 4
+        // (or 8) quads in one quarter-warp, and the extra permutation puts
+        // them in different bank groups.  The permutation is within a chunk,
+        // which the one thread that solved it writes whole.
         __device__ __forceinline__ int SolSwz(int ll)
         {
             const int qd = ll >> 2;
@@ -266,7 +267,7 @@ namespace halcuda
             }
             else
             {
-                return SOff4<SWZ>(ll + 1, k, q, P, LS);
+                return SOff4<SWZ>(ll + 1, k, q ^ SolSwz(ll), P, LS);
             }
         }
 
@@ -363,6 +364,26 @@ namespace halcuda
                     atomicExch(p.err, 2);
                 }
                 return;  // uniform: the address is the same for every thread
+            }
+            if constexpr (!SWZ)
+            {
+                // the chunked form also runs the batched tiles, whose shapes
+                // come from a table: the tile's shape must fit its launch
+                // (every line pair of every chunk has a thread, and the
+                // buffers above fit the dynamic shared memory; uniform: the
+                // same values for every thread)
+                uint32_t dynBytes;
+                asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dynBytes));
+                const int64_t need = 4 * (static_cast<int64_t>(R + 2) * p.LS + kCoefSmemFloats +
+                                          2 * static_cast<int64_t>(R) * P + kGbandSmem);
+                if (R < 1 || R > kMaxR || (R / kNL) * P > nthreads || need > static_cast<int64_t>(dynBytes))
+                {
+                    if (tid == 0)
+                    {
+                        atomicExch(p.err, 3);
+                    }
+                    return;
+                }
             }
             const int32_t L = p.L;
             const bool vecL = (L & 3) == 0;
@@ -719,7 +740,8 @@ namespace halcuda
 #pragma unroll
                 for (int q = 0; q < M / 4; q++)
                 {
-                    const int o = SWZ ? SOff4Row<SWZ>(rowo, k, q, swo, P, p.LS) : SOff4<SWZ>(ll + 1, k, q, P, p.LS);
+                    const int o = SWZ ? SOff4Row<SWZ>(rowo, k, q, swo, P, p.LS)
+                                      : SOff4<SWZ>(ll + 1, k, q ^ SolSwz(ll), P, p.LS);
                     St4(sLines + o, make_float4(z[j][4 * q], z[j][4 * q + 1], z[j][4 * q + 2], z[j][4 * q + 3]));
                 }
             }
@@ -1326,17 +1348,19 @@ namespace halcuda
     static_assert(kSweepTileThreads == kMaxThreads, "batched sweep CTAs use the kernel's thread bound");
     static_assert(kSweepTileMaxR == kMaxR, "batched sweep tiles use the kernel's line bound");
 
-    SweepTileShape SweepTileShapeFor(int32_t P, int32_t rCap)
+    SweepTileShape SweepTileShapeFor(int32_t P, int32_t rCap, int32_t budget)
     {
-        // every tile CTA has kSweepTileThreads threads: as many lines as
-        // (R / kNL) * P threads allow, a power of two in [8, min(rCap, kMaxR)]
+        // as many lines as (R / kNL) * P <= budget threads allow, a power of
+        // two in [8, min(rCap, kMaxR)]
+        budget = std::min(budget, kSweepTileThreads);
         SweepTileShape sh;
         int32_t R = 8;
-        while (R * 2 <= kMaxR && R * 2 <= rCap && (R * 2 / kNL) * P <= kSweepTileThreads)
+        while (R * 2 <= kMaxR && R * 2 <= rCap && (R * 2 / kNL) * P <= budget)
         {
             R *= 2;
         }
         sh.R = R;
+        sh.threads = ((R / kNL) * P + 31) & ~31;
         sh.LS = P * kChunkStride + 4;
         sh.smem = 1024 + sizeof(float) * (static_cast<size_t>(kCoefSmemFloats) + kGbandSmem + static_cast<size_t>(R + 2) * sh.LS +
                                           2 * static_cast<size_t>(R) * P + 2 * static_cast<size_t>(R));
@@ -1353,9 +1377,11 @@ namespace halcuda
         }
 
         template <int MODE>
-        int LaunchTiles(const SweepParams *table, const int2 *tiles, int32_t nTiles, size_t smem, cudaStream_t s)
+        int LaunchTiles(const SweepParams *table, const int2 *tiles, int32_t nTiles, size_t smem, int32_t threads,
+                        cudaStream_t s)
         {
-            AdiSweepTiles<MODE><<<static_cast<unsigned>(nTiles), kSweepTileThreads, smem, s>>>(table, tiles);
+            AdiSweepTiles<MODE><<<static_cast<unsigned>(nTiles), static_cast<unsigned>(threads), smem, s>>>(table,
+                                                                                                       tiles);
             CountLaunch();
             return LaunchStatus("AdiSweepTiles");
         }
@@ -1432,18 +1458,24 @@ namespace halcuda
     }
 
     int LaunchSweepTiles(int mode, const SweepParams *table, const int2 *tiles, int32_t nTiles, size_t smem,
-                         cudaStream_t s)
+                         int32_t threads, cudaStream_t s)
     {
         if (nTiles <= 0)
         {
             return HAL_CUDA_OK;
         }
+        if (threads < 32 || threads > kSweepTileThreads || threads % 32 != 0)
+        {
+            SetError("LaunchSweepTiles: %d threads per tile CTA (a multiple of 32 up to %d)", threads,
+                     kSweepTileThreads);
+            return HAL_CUDA_EINVAL;
+        }
         switch (mode)
         {
         case kSweepW:
-            return LaunchTiles<kSweepW>(table, tiles, nTiles, smem, s);
+            return LaunchTiles<kSweepW>(table, tiles, nTiles, smem, threads, s);
         case kSweepTick:
-            return LaunchTiles<kSweepTick>(table, tiles, nTiles, smem, s);
+            return LaunchTiles<kSweepTick>(table, tiles, nTiles, smem, threads, s);
         default:
             SetError("LaunchSweepTiles: unsupported mode %d", mode);
             return HAL_CUDA_EINVAL;
@@ -1554,8 +1586,9 @@ namespace halcuda
             {
                 cudaMemsetAsync(err.p, 0, sizeof(int32_t), stream.Get());
                 stopped = true;
-                SetError(h == 2 ? "%s: the sweep's shared-memory buffer was not 1024-byte aligned"
-                                : "%s: a staged copy did not complete within its wait limit",
+                SetError(h == 2   ? "%s: the sweep's shared-memory buffer was not 1024-byte aligned"
+                         : h == 3 ? "%s: a sweep tile's lines or shared memory exceed its launch (internal error)"
+                                  : "%s: a staged copy did not complete within its wait limit",
                          who);
                 return HAL_CUDA_ETIMEOUT;
             }

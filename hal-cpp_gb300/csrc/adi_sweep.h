@@ -76,29 +76,34 @@ namespace halcuda
 
     // ---- batched sweeps (many independent grids in one launch) ------------
     //
-    // A tile is (index into the SweepParams table, first line).  Every CTA
-    // of the launch has kSweepTileThreads threads; a grid's lines per CTA
-    // (SweepParams::R) and shared-memory stride (LS) come from
-    // SweepTileShape.
+    // A tile is (index into the SweepParams table, first line).  A grid's
+    // lines per CTA (SweepParams::R) and shared-memory stride (LS) come from
+    // SweepTileShape; every CTA of a launch has the largest thread count of
+    // its tiles (at most kSweepTileThreads) and the largest shared memory.
     constexpr int32_t kSweepTileThreads = 512;
 
     struct SweepTileShape
     {
         int32_t R, LS;
-        size_t smem;  // dynamic shared memory of one CTA
+        int32_t threads;  // threads the tile needs: (R / 2) * P, rounded up to a warp
+        size_t smem;      // dynamic shared memory of one CTA
     };
 
     // Shape of the tiles of a grid whose lines have P = ceil(L/32) chunks:
-    // the most lines per CTA (a power of two, at least 8, at most rCap) that
-    // the CTA's threads cover.
+    // the most lines per CTA (a power of two, at least 8, at most rCap)
+    // that `budget` threads cover.  Budgets below kSweepTileThreads give
+    // smaller CTAs, several of which share an SM (each thread keeps up to 128
+    // registers).
     constexpr int32_t kSweepTileMaxR = 128;
-    SweepTileShape SweepTileShapeFor(int32_t P, int32_t rCap = kSweepTileMaxR);
+    SweepTileShape SweepTileShapeFor(int32_t P, int32_t rCap = kSweepTileMaxR, int32_t budget = kSweepTileThreads);
 
     // Enables `smem` bytes of dynamic shared memory for the batched kernel of
     // `mode` (kSweepW or kSweepTick); call before capturing a launch.
     int PrepareSweepTiles(int mode, size_t smem);
 
-    // Launches nTiles CTAs of the batched kernel of `mode` (smem prepared).
+    // Launches nTiles CTAs of `threads` threads (at least every tile's
+    // SweepTileShape::threads) of the batched kernel of `mode` (smem
+    // prepared).
     int LaunchSweepTiles(int mode, const SweepParams *table, const int2 *tiles, int32_t nTiles, size_t smem,
-                         cudaStream_t s);
+                         int32_t threads, cudaStream_t s);
 }

@@ -80,6 +80,7 @@ namespace halcuda
         DevBuf<int2> tilesX, tilesY;
         int32_t nTilesX = 0, nTilesY = 0;
         size_t smemX = 0, smemY = 0;
+        int32_t threadsX = 0, threadsY = 0;  // threads per tile CTA of each sweep
         DevBuf<int32_t> err;
         // set once a bounded device wait has given up: the wells' fields are
         // undefined from then on, so the handle takes no further ticks
@@ -87,6 +88,9 @@ namespace halcuda
         // Lines per sweep tile are capped at rCap, chosen by the autotuner
         // (Autotune) the first time the wells tick.
         int32_t rCap = kSweepTileMaxR;
+        // Threads per tile CTA are at most tileBudget, also chosen by the
+        // autotuner: smaller CTAs (fewer lines each) let several share an SM.
+        int32_t tileBudget = kSweepTileThreads;
         int32_t forceThreads = 128;  // agent force kernel block size, also tuned
         bool tuned = false;
         float tunedMs = 0.0f, defaultMs = 0.0f;
@@ -254,13 +258,16 @@ namespace halcuda
             std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return Cells(a) > Cells(b); });
             std::vector<int2> tx, ty;
             smemX = smemY = 0;
+            threadsX = threadsY = 32;
             for (int32_t w : order)
             {
                 const int32_t a = adiIdx[w];
-                const SweepTileShape sx = SweepTileShapeFor(planX[a]->Dev().P, rCap);
-                const SweepTileShape sy = SweepTileShapeFor(planY[a]->Dev().P, rCap);
+                const SweepTileShape sx = SweepTileShapeFor(planX[a]->Dev().P, rCap, tileBudget);
+                const SweepTileShape sy = SweepTileShapeFor(planY[a]->Dev().P, rCap, tileBudget);
                 smemX = std::max(smemX, sx.smem);
                 smemY = std::max(smemY, sy.smem);
+                threadsX = std::max(threadsX, sx.threads);
+                threadsY = std::max(threadsY, sy.threads);
                 for (int32_t x0 = 0; x0 < desc[w].yDim; x0 += sx.R)
                 {
                     tx.push_back(make_int2(a, x0));
@@ -373,7 +380,7 @@ namespace halcuda
                     p.halfR = static_cast<float>(d.diffRate / 2.0);
                     p.r = static_cast<float>(d.diffRate);
                     p.plan = planX[a]->Dev();
-                    const SweepTileShape shx = SweepTileShapeFor(p.plan.P, rCap);
+                    const SweepTileShape shx = SweepTileShapeFor(p.plan.P, rCap, tileBudget);
                     p.R = shx.R;
                     p.LS = shx.LS;
                     p.out = W(w);
@@ -389,7 +396,7 @@ namespace halcuda
                     q.halfR = static_cast<float>(d.diffRate / 2.0);
                     q.r = static_cast<float>(d.diffRate);
                     q.plan = planY[a]->Dev();
-                    const SweepTileShape shy = SweepTileShapeFor(q.plan.P, rCap);
+                    const SweepTileShape shy = SweepTileShapeFor(q.plan.P, rCap, tileBudget);
                     q.R = shy.R;
                     q.LS = shy.LS;
                     q.out = F(w, c ^ 1);
@@ -443,8 +450,8 @@ namespace halcuda
                 {
                     HAL_TRY(LaunchAgentWells(AgentArgs(R, k), s));
                 }
-                HAL_TRY(LaunchSweepTiles(kSweepW, sxTab[c].p, tilesX.p, nTilesX, smemX, s));
-                HAL_TRY(LaunchSweepTiles(kSweepTick, syTab[c].p, tilesY.p, nTilesY, smemY, s));
+                HAL_TRY(LaunchSweepTiles(kSweepW, sxTab[c].p, tilesX.p, nTilesX, smemX, threadsX, s));
+                HAL_TRY(LaunchSweepTiles(kSweepTick, syTab[c].p, tilesY.p, nTilesY, smemY, threadsY, s));
                 if (exp)
                 {
                     HAL_TRY(CudaStatus(cudaStreamWaitEvent(s, joinExplicit.e, 0), "cudaStreamWaitEvent(join)"));
@@ -457,12 +464,12 @@ namespace halcuda
             {
                 cudaEventRecord(ev[0], s);
             }
-            HAL_TRY(LaunchSweepTiles(kSweepW, sxTab[c].p, tilesX.p, nTilesX, smemX, s));
+            HAL_TRY(LaunchSweepTiles(kSweepW, sxTab[c].p, tilesX.p, nTilesX, smemX, threadsX, s));
             if (ev)
             {
                 cudaEventRecord(ev[1], s);
             }
-            HAL_TRY(LaunchSweepTiles(kSweepTick, syTab[c].p, tilesY.p, nTilesY, smemY, s));
+            HAL_TRY(LaunchSweepTiles(kSweepTick, syTab[c].p, tilesY.p, nTilesY, smemY, threadsY, s));
             if (ev)
             {
                 cudaEventRecord(ev[2], s);
@@ -531,10 +538,10 @@ namespace halcuda
                 {
                     cudaEventRecord(e0, s);
                 }
-                rc = LaunchSweepTiles(kSweepW, sxTab[cur].p, tilesX.p, nTilesX, smemX, s);
+                rc = LaunchSweepTiles(kSweepW, sxTab[cur].p, tilesX.p, nTilesX, smemX, threadsX, s);
                 if (rc == HAL_CUDA_OK)
                 {
-                    rc = LaunchSweepTiles(kSweepTick, syTab[cur].p, tilesY.p, nTilesY, smemY, s);
+                    rc = LaunchSweepTiles(kSweepTick, syTab[cur].p, tilesY.p, nTilesY, smemY, threadsY, s);
                 }
             }
             if (rc == HAL_CUDA_OK)
@@ -557,51 +564,64 @@ namespace halcuda
         }
 
         // Autotuner of the ADI sweep tiles: times the batched x- and y-sweeps
-        // with the lines per tile capped at 128, 64, 32, 16 and 8 (caps that
-        // give the same tiles as a larger one are skipped), on the wells'
-        // own data, and keeps the fastest.  Fewer lines per tile give more,
-        // smaller CTAs (more of them resident per SM); more lines give longer
-        // contiguous stores.  Which wins depends on the mix of well sizes.
+        // with the threads per tile CTA capped at 512, 256 and 128 and the
+        // lines per tile capped at 128, 64, 32, 16 and 8 (settings that give
+        // the same tiles as an earlier one are skipped), on the wells' own
+        // data, and keeps the fastest.  Fewer lines per tile give more,
+        // smaller CTAs: each tile CTA of 512 threads holds a whole SM's
+        // registers, while 256- and 128-thread CTAs share an SM two and four
+        // at a time and overlap one another's staging, solve and write-out.
+        // More lines give longer contiguous stores.  Which wins depends on
+        // the mix of well sizes.
         int Autotune()
         {
             tuned = true;
             if (nTilesX == 0)
             {
                 rCap = kSweepTileMaxR;
+                tileBudget = kSweepTileThreads;
                 return HAL_CUDA_OK;
             }
-            std::vector<int32_t> prevShape;
+            std::vector<std::vector<int32_t>> seen;
             float best = 0.0f;
-            int32_t bestCap = kSweepTileMaxR;
-            for (int32_t cap = kSweepTileMaxR; cap >= 8; cap /= 2)
+            int32_t bestCap = kSweepTileMaxR, bestBudget = kSweepTileThreads;
+            bool first = true;
+            for (int32_t budget = kSweepTileThreads; budget >= 128; budget /= 2)
             {
-                std::vector<int32_t> shape;
-                for (size_t a = 0; a < adiWell.size(); a++)
+                for (int32_t cap = kSweepTileMaxR; cap >= 8; cap /= 2)
                 {
-                    shape.push_back(SweepTileShapeFor(planX[a]->Dev().P, cap).R);
-                    shape.push_back(SweepTileShapeFor(planY[a]->Dev().P, cap).R);
-                }
-                if (shape == prevShape)
-                {
-                    continue;
-                }
-                prevShape = shape;
-                rCap = cap;
-                HAL_TRY(BuildAdiTiles());
-                HAL_TRY(UploadTables());
-                float ms = 0.0f;
-                HAL_TRY(TimeSweeps(2, 5, &ms));
-                if (cap == kSweepTileMaxR)
-                {
-                    defaultMs = ms;
-                }
-                if (cap == kSweepTileMaxR || ms < best)
-                {
-                    best = ms;
-                    bestCap = cap;
+                    std::vector<int32_t> shape;
+                    for (size_t a = 0; a < adiWell.size(); a++)
+                    {
+                        shape.push_back(SweepTileShapeFor(planX[a]->Dev().P, cap, budget).R);
+                        shape.push_back(SweepTileShapeFor(planY[a]->Dev().P, cap, budget).R);
+                    }
+                    if (std::find(seen.begin(), seen.end(), shape) != seen.end())
+                    {
+                        continue;
+                    }
+                    seen.push_back(shape);
+                    rCap = cap;
+                    tileBudget = budget;
+                    HAL_TRY(BuildAdiTiles());
+                    HAL_TRY(UploadTables());
+                    float ms = 0.0f;
+                    HAL_TRY(TimeSweeps(2, 5, &ms));
+                    if (first)
+                    {
+                        defaultMs = ms;
+                    }
+                    if (first || ms < best)
+                    {
+                        best = ms;
+                        bestCap = cap;
+                        bestBudget = budget;
+                    }
+                    first = false;
                 }
             }
             rCap = bestCap;
+            tileBudget = bestBudget;
             tunedMs = best;
             HAL_TRY(BuildAdiTiles());
             HAL_TRY(UploadTables());
@@ -728,8 +748,9 @@ namespace halcuda
             {
                 cudaMemsetAsync(err.p, 0, sizeof(int32_t), stream.Get());
                 stopped = true;
-                SetError(h == 2 ? "%s: the sweep's shared-memory buffer was not 1024-byte aligned"
-                                : "%s: a staged copy did not complete within its wait limit",
+                SetError(h == 2   ? "%s: the sweep's shared-memory buffer was not 1024-byte aligned"
+                         : h == 3 ? "%s: a sweep tile's lines or shared memory exceed its launch (internal error)"
+                                  : "%s: a staged copy did not complete within its wait limit",
                          who);
                 return HAL_CUDA_ETIMEOUT;
             }
