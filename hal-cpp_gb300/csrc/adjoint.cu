@@ -27,8 +27,14 @@
 // States are recomputed segment by segment from checkpoints every k steps,
 // each segment on a second stream while the one after it is differentiated.
 //
-// Layout: every array is row-major x*yDim + y (HAL's layout).
+// Layout: every array is row-major x*yDim + y (HAL's layout), except the
+// x-kernels' own copies, which are line by line (y*xDim + x) so that an x-line
+// CTA reads them contiguously: the rates DT (transposed once per call), the
+// kept states w (FwdX writes them so) and the x-faces' part of dL/dD (added
+// into dD once at the end).  Only the arrays passed between the sweeps (f, w
+// for the y-sweep, b2bar, b1bar) keep HAL's layout and are strided for x-lines.
 #include "common.cuh"
+#include "adi_sweep.h"
 
 #include <algorithm>
 #include <cmath>
@@ -122,6 +128,28 @@ namespace halcuda
             {
                 const int32_t dn = (line > 0) ? line - 1 : nl - 1;
                 acc += D[Idx<DIR>(g, dn, j)] * (u[Idx<DIR>(g, dn, j)] - c);
+            }
+            return acc;
+        }
+
+        // LapCross<kDirX> with the rates read from DT, D transposed (DT[y *
+        // xDim + x] = D(x, y)): the two cross faces' rates of an x-line are then
+        // contiguous along the line, like the line's own.
+        __device__ __forceinline__ float LapCrossXT(const Grid &g, const float *__restrict__ u,
+                                                    const float *__restrict__ DT, int32_t line, int32_t j, float c)
+        {
+            const int32_t nl = g.yDim;
+            const bool wrap = g.wrapY != 0;
+            float acc = 0.0f;
+            if (line + 1 < nl || (wrap && nl > 1))
+            {
+                const int32_t up = (line + 1 < nl) ? line + 1 : 0;
+                acc += DT[static_cast<int64_t>(line) * g.xDim + j] * (u[Idx<kDirX>(g, up, j)] - c);
+            }
+            if (line > 0 || (wrap && nl > 1))
+            {
+                const int32_t dn = (line > 0) ? line - 1 : nl - 1;
+                acc += DT[static_cast<int64_t>(dn) * g.xDim + j] * (u[Idx<kDirX>(g, dn, j)] - c);
             }
             return acc;
         }
@@ -239,8 +267,13 @@ namespace halcuda
 
         // x-sweep: w = (I - Lx/2)^-1 (I + Ly/2) f, one CTA per line y, in
         // residual form: w = f + (I - Lx/2)^-1 (Lx + Ly) f / 2, so that the
-        // solve's rounding scales with the step's change, not the field.
-        __global__ void FwdX(Grid g, const float *__restrict__ f, const float *__restrict__ D, float *__restrict__ w)
+        // solve's rounding scales with the step's change, not the field.  The
+        // rates come from DT (D transposed), contiguous along the line.  w is
+        // written in HAL's layout for the y-sweep, and, when wB is set, also
+        // line by line (wB[y * xDim + x]) as the state the backward x-kernel
+        // reads along the same lines.
+        __global__ void FwdX(Grid g, const float *__restrict__ f, const float *__restrict__ DT, float *__restrict__ w,
+                             float *__restrict__ wB)
         {
             extern __shared__ float sm[];
             float *sD = sm + 4 * blockDim.x;
@@ -252,10 +285,10 @@ namespace halcuda
             if (j < n)
             {
                 const int64_t i = Idx<kDirX>(g, line, j);
-                sD[j] = D[i];
+                sD[j] = DT[static_cast<int64_t>(line) * n + j];
                 c = f[i];
                 su[j] = c;
-                lap = LapCross<kDirX>(g, f, D, line, j, c);
+                lap = LapCrossXT(g, f, DT, line, j, c);
             }
             __syncthreads();
             if (j < n)
@@ -266,6 +299,10 @@ namespace halcuda
             if (j < n)
             {
                 w[Idx<kDirX>(g, line, j)] = c + e;
+                if (wB != nullptr)
+                {
+                    wB[static_cast<int64_t>(line) * n + j] = c + e;
+                }
             }
         }
 
@@ -435,8 +472,11 @@ namespace halcuda
         }
 
         // Backward along x for step t: wbar = (I + Lx/2) b2bar, b1bar = (I - Lx/2)^-1 wbar.
-        __global__ void BwdX(Grid g, const float *__restrict__ D, const float *__restrict__ b2bar,
-                             const float *__restrict__ wT, float *__restrict__ b1bar, float *__restrict__ dD)
+        // The rates DT, the state wB and the x-face gradient dDT are all
+        // line by line (y * xDim + x), contiguous along the CTA's line; only
+        // b2bar and b1bar, which the y-kernels read and write, are strided.
+        __global__ void BwdX(Grid g, const float *__restrict__ DT, const float *__restrict__ b2bar,
+                             const float *__restrict__ wB, float *__restrict__ b1bar, float *__restrict__ dDT)
         {
             extern __shared__ float sm[];
             float *sD = sm + 4 * blockDim.x;
@@ -447,11 +487,12 @@ namespace halcuda
             const bool wrap = g.wrapX != 0;
             const int32_t j = threadIdx.x;
             const int64_t i = (j < n) ? Idx<kDirX>(g, line, j) : 0;
+            const int64_t iB = static_cast<int64_t>(line) * n + j;
             if (j < n)
             {
-                sD[j] = D[i];
+                sD[j] = DT[iB];
                 sp[j] = b2bar[i];
-                sw[j] = wT[i];
+                sw[j] = wB[iB];
             }
             __syncthreads();
             float wbar = 0.0f, dDacc = 0.0f, lapb = 0.0f;
@@ -481,7 +522,33 @@ namespace halcuda
             {
                 dDacc += FaceGrad(sp, sw, j, n, wrap);
                 b1bar[i] = x;
-                dD[i] += dDacc;
+                dDT[iB] += dDacc;
+            }
+        }
+
+        // dD(x, y) += dDT[y * xDim + x]: the x-faces' gradient, accumulated
+        // line by line, added into HAL's layout through a 32 x 32 tile.
+        __global__ void AddTransposed(float *__restrict__ dD, const float *__restrict__ dDT, int32_t xDim,
+                                      int32_t yDim)
+        {
+            __shared__ float tile[32][33];
+            const int32_t x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+            for (int32_t r = threadIdx.y; r < 32; r += blockDim.y)
+            {
+                const int32_t y = y0 + r, x = x0 + threadIdx.x;
+                if (y < yDim && x < xDim)
+                {
+                    tile[r][threadIdx.x] = dDT[static_cast<int64_t>(y) * xDim + x];
+                }
+            }
+            __syncthreads();
+            for (int32_t r = threadIdx.y; r < 32; r += blockDim.y)
+            {
+                const int32_t x = x0 + r, y = y0 + threadIdx.x;
+                if (x < xDim && y < yDim)
+                {
+                    dD[static_cast<int64_t>(x) * yDim + y] += tile[threadIdx.x][r];
+                }
             }
         }
     }
@@ -501,6 +568,11 @@ namespace halcuda
         StreamSlot recomputeStream;         // recomputes segment s-1 while segment s is differentiated
         DevBuf<float> work[2];              // forward ping-pong
         DevBuf<float> gA, gB, b1, b2, dD, dS;
+        // line-by-line (y * xDim + x) copies for the x-kernels: the rates,
+        // the x-faces' part of dL/dD, and the x-sweep's w in HAL's layout for
+        // the y-sweep (scratch: the forward on the main stream and the
+        // recomputations on the second one never run at the same time)
+        DevBuf<float> DT, dDT, wA;
         DevBuf<double> acc;                 // [0] loss, [1] d loss / d decay
         float msForward = 0.0f, msGradient = 0.0f;
 
@@ -537,6 +609,9 @@ namespace halcuda
             HAL_TRY(b1.Alloc(m, "cudaMalloc(adjoint)"));
             HAL_TRY(b2.Alloc(m, "cudaMalloc(adjoint)"));
             HAL_TRY(dD.Alloc(m, "cudaMalloc(adjoint)"));
+            HAL_TRY(DT.Alloc(m, "cudaMalloc(adjoint)"));
+            HAL_TRY(dDT.Alloc(m, "cudaMalloc(adjoint)"));
+            HAL_TRY(wA.Alloc(m, "cudaMalloc(adjoint)"));
             HAL_TRY(dS.Alloc(m, "cudaMalloc(adjoint)"));
             HAL_TRY(acc.Alloc(2, "cudaMalloc(adjoint)"));
             return HAL_CUDA_OK;
@@ -547,12 +622,14 @@ namespace halcuda
             return (len + 31) & ~31;
         }
 
-        int LaunchFwd(const float *fIn, float *fOut, float *wOut, float *vOut, const float *srcp, float negDecay,
+        // One forward step fIn -> fOut; the step's w is kept line by line in
+        // wKeep and its v in vOut when they are set.
+        int LaunchFwd(const float *fIn, float *fOut, float *wKeep, float *vOut, const float *srcp, float negDecay,
                       cudaStream_t s)
         {
             const int tx = Threads(g.xDim), ty = Threads(g.yDim);
-            FwdX<<<g.yDim, tx, LineSmemFloats(tx) * sizeof(float), s>>>(g, fIn, D.p, wOut);
-            FwdY<<<g.xDim, ty, LineSmemFloats(ty) * sizeof(float), s>>>(g, wOut, fIn, D.p, srcp, negDecay, fOut,
+            FwdX<<<g.yDim, tx, LineSmemFloats(tx) * sizeof(float), s>>>(g, fIn, DT.p, wA.p, wKeep);
+            FwdY<<<g.xDim, ty, LineSmemFloats(ty) * sizeof(float), s>>>(g, wA.p, fIn, D.p, srcp, negDecay, fOut,
                                                                          vOut);
             CountLaunch(2);
             return LaunchStatus("adjoint forward step");
@@ -562,6 +639,7 @@ namespace halcuda
         {
             const size_t bytes = static_cast<size_t>(n) * sizeof(float);
             HAL_TRY(CudaStatus(cudaMemcpyAsync(D.p, hD, bytes, cudaMemcpyHostToDevice, s), "cudaMemcpy(D)"));
+            HAL_TRY(LaunchTranspose(D.p, DT.p, g.xDim, g.yDim, s));
             useSrc = (hSrc != nullptr);
             if (useSrc)
             {
@@ -586,7 +664,7 @@ namespace halcuda
                 }
                 if (rc == HAL_CUDA_OK)
                 {
-                    rc = LaunchFwd(work[c].p, work[c ^ 1].p, b1.p, nullptr, srcp, negDecay, s);
+                    rc = LaunchFwd(work[c].p, work[c ^ 1].p, nullptr, nullptr, srcp, negDecay, s);
                 }
                 c ^= 1;
             }
@@ -655,6 +733,7 @@ namespace halcuda
             const float negDecay = static_cast<float>(-decay);
             HAL_TRY(CudaStatus(cudaMemsetAsync(acc.p, 0, 2 * sizeof(double), s), "cudaMemset(acc)"));
             HAL_TRY(CudaStatus(cudaMemsetAsync(dD.p, 0, bytes, s), "cudaMemset(dD)"));
+            HAL_TRY(CudaStatus(cudaMemsetAsync(dDT.p, 0, bytes, s), "cudaMemset(dD)"));
             HAL_TRY(CudaStatus(cudaMemsetAsync(dS.p, 0, bytes, s), "cudaMemset(dS)"));
             cudaEvent_t e0, e1;
             HAL_TRY(CudaStatus(cudaEventCreate(&e0), "cudaEventCreate"));
@@ -688,7 +767,7 @@ namespace halcuda
                     BwdY<<<g.xDim, ty, smy, s>>>(g, first ? kBwdFirst : kBwdNext, D.p, static_cast<float>(decay),
                                                  b1.p, gCur, fNext, segF[b].p + k * n, segV[b].p + k * n, gNext,
                                                  b2.p, dD.p, dS.p, acc.p + 1);
-                    BwdX<<<g.yDim, tx, smx, s>>>(g, D.p, b2.p, segW[b].p + k * n, b1.p, dD.p);
+                    BwdX<<<g.yDim, tx, smx, s>>>(g, DT.p, b2.p, segW[b].p + k * n, b1.p, dDT.p);
                     CountLaunch(2);
                     r = LaunchStatus("adjoint backward step");
                     std::swap(gCur, gNext);
@@ -765,7 +844,7 @@ namespace halcuda
                     }
                     else
                     {
-                        rc = LaunchFwd(fCur, work[c ^ 1].p, b1.p, nullptr, srcp, negDecay, s);
+                        rc = LaunchFwd(fCur, work[c ^ 1].p, nullptr, nullptr, srcp, negDecay, s);
                         c ^= 1;
                         fCur = work[c].p;
                     }
@@ -850,6 +929,14 @@ namespace halcuda
                                              dS.p, acc.p + 1);
                 CountLaunch();
                 rc = LaunchStatus("adjoint backward tail");
+            }
+            if (rc == HAL_CUDA_OK)
+            {
+                // the x-faces' part of dL/dD, accumulated line by line
+                AddTransposed<<<dim3((g.xDim + 31) / 32, (g.yDim + 31) / 32), dim3(32, 8), 0, s>>>(dD.p, dDT.p,
+                                                                                               g.xDim, g.yDim);
+                CountLaunch();
+                rc = LaunchStatus("adjoint dD");
             }
             cudaEventRecord(e1, s);
             double h[2] = {0, 0};
