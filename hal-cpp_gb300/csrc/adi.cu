@@ -33,6 +33,7 @@
 #include "common.cuh"
 #include "adi_plan.h"
 #include "adi_sweep.h"
+#include "adi64.h"
 
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -1504,6 +1505,10 @@ namespace halcuda
         bool hasGhost = false;
         DevBuf<double> f64, d64;
         DevBuf<float> g32;       // ghost table of the FP64 interface call, in float
+        // the interface calls on lines longer than the FP32 partitioned solve
+        // takes: the FP64 Thomas solve per line, with its ghost table in FP64
+        std::unique_ptr<Adi64> adi64;
+        DevBuf<double> g64;
         DevBuf<int32_t> err;
         // set once a bounded device wait has given up: the sweep that gave
         // up left its lines undefined, so the handle takes no further ticks
@@ -1839,12 +1844,6 @@ extern "C" int hal_cuda_adi_create(int32_t xDim, int32_t yDim, hal_cuda_adi **ou
     HAL_REQUIRE(xDim > 0 && yDim > 0, "hal_cuda_adi_create: dimensions must be positive");
     HAL_REQUIRE(static_cast<int64_t>(xDim) * yDim < (int64_t(1) << 31),
                 "hal_cuda_adi_create: xDim*yDim exceeds int32");
-    if (xDim > HAL_CUDA_ADI_MAX_LINE || yDim > HAL_CUDA_ADI_MAX_LINE)
-    {
-        halcuda::SetError("hal_cuda_adi_create: ADI lines are limited to %d cells (got %d x %d)",
-                          HAL_CUDA_ADI_MAX_LINE, xDim, yDim);
-        return HAL_CUDA_ENOTSUP;
-    }
     hal_cuda_adi *h = new (std::nothrow) hal_cuda_adi();
     if (h == nullptr)
     {
@@ -1887,6 +1886,40 @@ namespace
             HAL_TRY(h->g32.Alloc(2 * (static_cast<size_t>(h->xDim) + h->yDim), "cudaMalloc(ghost)"));
         }
         cudaStream_t s = h->stream.Get();
+        if (h->xDim > HAL_CUDA_ADI_MAX_LINE || h->yDim > HAL_CUDA_ADI_MAX_LINE)
+        {
+            // lines beyond the FP32 partitioned solve: the FP64 Thomas solve
+            // per line, in the CPU backend's operation order (bit-exact)
+            if (h->adi64 == nullptr)
+            {
+                h->adi64.reset(new (std::nothrow) Adi64());
+                if (h->adi64 == nullptr)
+                {
+                    SetError("%s: out of host memory", who);
+                    return HAL_CUDA_ENOMEM;
+                }
+            }
+            const double *g = nullptr;
+            if (ghost != nullptr)
+            {
+                const size_t ng = 2 * (static_cast<size_t>(h->xDim) + h->yDim);
+                if (h->g64.p == nullptr)
+                {
+                    HAL_TRY(h->g64.Alloc(ng, "cudaMalloc(ghost)"));
+                }
+                HAL_TRY(CudaStatus(cudaMemcpyAsync(h->g64.p, ghost, ng * sizeof(double), cudaMemcpyHostToDevice, s),
+                                   "cudaMemcpy(ghost)"));
+                g = h->g64.p;
+            }
+            HAL_TRY(CudaStatus(cudaMemcpyAsync(h->f64.p, field, n * sizeof(double), cudaMemcpyHostToDevice, s),
+                               "cudaMemcpy(field)"));
+            HAL_TRY(CudaStatus(cudaMemcpyAsync(h->d64.p, deltas, n * sizeof(double), cudaMemcpyHostToDevice, s),
+                               "cudaMemcpy(deltas)"));
+            HAL_TRY(h->adi64->Run(h->f64.p, h->d64.p, h->xDim, h->yDim, wrapX, wrapY, r, g, s));
+            HAL_TRY(CudaStatus(cudaMemcpyAsync(deltas, h->d64.p, n * sizeof(double), cudaMemcpyDeviceToHost, s),
+                               "cudaMemcpy(deltas)"));
+            return CudaStatus(cudaStreamSynchronize(s), who);
+        }
         const float *g = nullptr;
         if (ghost != nullptr)
         {

@@ -22,6 +22,7 @@
 //     y-sweep reads coalesced too, and the y-sweep's result is transposed
 //     back while it is added into the deltas.
 #include "common.cuh"
+#include "adi64.h"
 #include "stencil64.cuh"
 #include "agents_wells.h"
 
@@ -634,7 +635,7 @@ namespace halcuda
         int device = 0;
         StreamSlot stream;
         DevBuf<double> f, d;
-        DevBuf<double> wA, wB, vB, dS;   // ADI scratch (allocated on first use)
+        Adi64 adi64;                     // DiffusionADI (plans and scratch)
         DevBuf<double> a0, a1, a2;       // uploaded per-cell arrays (rates, velocities)
         DevBuf<double> g0, g1, g2;       // uploaded ghost tables
         DevBuf<RedPartial> red;
@@ -642,7 +643,6 @@ namespace halcuda
         DevBuf<int32_t> ic0, ic1;        // uploaded index lists
         DevBuf<int8_t> iops;
         DevBuf<double> ivals, iout, iout2;
-        std::map<std::string, std::unique_ptr<PlanBuf64>> plans;
         cudaEvent_t evA = nullptr, evB = nullptr;
 
         int64_t Length() const
@@ -722,6 +722,37 @@ namespace halcuda
             return HAL_CUDA_OK;
         }
 
+        // Internal::Diffusion2DADI (ADIequations.h:306-337, Dirichlet
+        // :339-378): deltas += v - f.
+        int Adi(double r, const double *ghostHost)
+        {
+            const double *g = nullptr;
+            HAL_TRY(GhostTable(ghostHost, g0, &g));
+            return adi64.Run(f.p, d.p, xDim, yDim, wrapX, wrapY, r, g, stream.Get());
+        }
+
+        int Sync(const char *who)
+        {
+            return CudaStatus(cudaStreamSynchronize(stream.Get()), who);
+        }
+    };
+
+    // ---- Adi64 -------------------------------------------------------------
+    struct Adi64::Impl
+    {
+        DevBuf<double> wA, wB, vB, dS;  // scratch (grown on first use)
+        std::map<std::string, std::unique_ptr<PlanBuf64>> plans;
+
+        int Ensure(DevBuf<double> &b, size_t n, cudaStream_t s, const char *what)
+        {
+            if (b.n < n || b.p == nullptr)
+            {
+                HAL_TRY(CudaStatus(cudaStreamSynchronize(s), what));
+                HAL_TRY(b.Alloc(n, what));
+            }
+            return HAL_CUDA_OK;
+        }
+
         int Plan(int32_t L, double r, bool wrap, bool dirichlet, LinePlan64Dev *out)
         {
             char key[96];
@@ -753,38 +784,36 @@ namespace halcuda
             *out = it->second->dev;
             return HAL_CUDA_OK;
         }
-
-        // Internal::Diffusion2DADI (ADIequations.h:306-337, Dirichlet
-        // :339-378): deltas += v - f.
-        int Adi(double r, const double *ghostHost)
-        {
-            cudaStream_t s = stream.Get();
-            const size_t n = static_cast<size_t>(Length());
-            HAL_TRY(Ensure(wA, n, "cudaMalloc(ADI scratch)"));
-            HAL_TRY(Ensure(wB, n, "cudaMalloc(ADI scratch)"));
-            HAL_TRY(Ensure(vB, n, "cudaMalloc(ADI scratch)"));
-            HAL_TRY(Ensure(dS, n, "cudaMalloc(ADI scratch)"));
-            const double *g = nullptr;
-            HAL_TRY(GhostTable(ghostHost, g0, &g));
-            LinePlan64Dev px, py;
-            HAL_TRY(Plan(xDim, r, wrapX != 0, g != nullptr, &px));
-            HAL_TRY(Plan(yDim, r, wrapY != 0, g != nullptr, &py));
-            const int T = 32;  // one warp per block: the lines spread over the most SMs
-            AdiSweepX64<<<Blocks(yDim, T), T, 0, s>>>(f.p, dS.p, wA.p, px, xDim, yDim, wrapX, wrapY, g, r);
-            const dim3 tb(32, 8);
-            Transpose64<false><<<dim3((yDim + 31) / 32, (xDim + 31) / 32), tb, 0, s>>>(wA.p, wB.p, xDim, yDim,
-                                                                                        nullptr);
-            AdiSweepY64<<<Blocks(xDim, T), T, 0, s>>>(wB.p, dS.p, vB.p, py, xDim, yDim, wrapX, wrapY, g, r);
-            Transpose64<true><<<dim3((xDim + 31) / 32, (yDim + 31) / 32), tb, 0, s>>>(vB.p, d.p, yDim, xDim, f.p);
-            CountLaunch(4);
-            return LaunchStatus("pdegrid DiffusionADI");
-        }
-
-        int Sync(const char *who)
-        {
-            return CudaStatus(cudaStreamSynchronize(stream.Get()), who);
-        }
     };
+
+    Adi64::Adi64() : m_impl(new Impl())
+    {
+    }
+
+    Adi64::~Adi64() = default;
+
+    int Adi64::Run(const double *f, double *deltas, int32_t xDim, int32_t yDim, int32_t wrapX, int32_t wrapY,
+                   double r, const double *g, cudaStream_t s)
+    {
+        Impl &m = *m_impl;
+        const size_t n = static_cast<size_t>(xDim) * static_cast<size_t>(yDim);
+        HAL_TRY(m.Ensure(m.wA, n, s, "cudaMalloc(ADI scratch)"));
+        HAL_TRY(m.Ensure(m.wB, n, s, "cudaMalloc(ADI scratch)"));
+        HAL_TRY(m.Ensure(m.vB, n, s, "cudaMalloc(ADI scratch)"));
+        HAL_TRY(m.Ensure(m.dS, n, s, "cudaMalloc(ADI scratch)"));
+        LinePlan64Dev px, py;
+        HAL_TRY(m.Plan(xDim, r, wrapX != 0, g != nullptr, &px));
+        HAL_TRY(m.Plan(yDim, r, wrapY != 0, g != nullptr, &py));
+        const int T = 32;  // one warp per block: the lines spread over the most SMs
+        AdiSweepX64<<<Blocks(yDim, T), T, 0, s>>>(f, m.dS.p, m.wA.p, px, xDim, yDim, wrapX, wrapY, g, r);
+        const dim3 tb(32, 8);
+        Transpose64<false><<<dim3((yDim + 31) / 32, (xDim + 31) / 32), tb, 0, s>>>(m.wA.p, m.wB.p, xDim, yDim,
+                                                                                    nullptr);
+        AdiSweepY64<<<Blocks(xDim, T), T, 0, s>>>(m.wB.p, m.dS.p, m.vB.p, py, xDim, yDim, wrapX, wrapY, g, r);
+        Transpose64<true><<<dim3((xDim + 31) / 32, (yDim + 31) / 32), tb, 0, s>>>(m.vB.p, deltas, yDim, xDim, f);
+        CountLaunch(4);
+        return LaunchStatus("DiffusionADI (FP64)");
+    }
 }
 
 struct hal_cuda_pdegrid : public halcuda::PdeGrid

@@ -56,8 +56,11 @@ extern "C" {
 #define HAL_CUDA_ETIMEOUT 4 /* a bounded device-side wait gave up */
 #define HAL_CUDA_ENOTSUP 5  /* a size or mode this build does not handle */
 
-/* Longest line the ADI sweeps solve (the Vulkan AdiKernel2D caps lines at
- * kMaxLine = 1024, AdiKernel2D.h:41). */
+/* Longest line the FP32 partitioned ADI sweeps solve (the Vulkan AdiKernel2D
+ * caps lines at kMaxLine = 1024, AdiKernel2D.h:41).  The resident ADI ticks
+ * take lines up to this length; the interface calls (hal_cuda_diffuse_adi,
+ * _adi_bc) take any length, solving longer lines in FP64 as the CPU backend
+ * does. */
 #define HAL_CUDA_ADI_MAX_LINE 4096
 
 typedef struct hal_cuda_diffusion hal_cuda_diffusion; /* explicit stencil */
@@ -188,15 +191,19 @@ int hal_cuda_diffusion_set_stream(hal_cuda_diffusion *h, void *stream);
 /* ---- ADI: IAdiDiffusionBackend2D --------------------------------------- */
 
 /* GpuAdiDiffusionBackend2D(ComputeContext&, xDim, yDim)
- * (include/Hal/Gpu/GpuAdiDiffusionBackend2D.h); ENOTSUP if a side exceeds
- * HAL_CUDA_ADI_MAX_LINE. */
+ * (include/Hal/Gpu/GpuAdiDiffusionBackend2D.h).  Any size whose cell count
+ * fits int32; with a side above HAL_CUDA_ADI_MAX_LINE the resident ticks
+ * (run_ticks, profile) return EINVAL and only the interface calls run. */
 int hal_cuda_adi_create(int32_t xDim, int32_t yDim, hal_cuda_adi **out);
 int hal_cuda_adi_destroy(hal_cuda_adi *h);
 
 /* IAdiDiffusionBackend2D::DiffuseADI (IAdiDiffusionBackend2D.h:25-31):
  * deltas[i] += v[i] - field[i], v = one ADI step of field
  * (Internal::Diffusion2DADI, ADIequations.h:306-337).  Host double arrays;
- * size checks as hal_cuda_diffuse. */
+ * size checks as hal_cuda_diffuse.  Sides up to HAL_CUDA_ADI_MAX_LINE run the
+ * FP32 partitioned solve (max error 2e-6 (1 + r) of the field); with a longer
+ * side the step is the FP64 Thomas solve per line, bit-exact to the CPU
+ * backend. */
 int hal_cuda_diffuse_adi(hal_cuda_adi *h, const double *field, int64_t fieldLen,
                          double *deltas, int64_t deltasLen, double diffRate, int32_t xDim,
                          int32_t yDim, int32_t wrapX, int32_t wrapY);

@@ -227,9 +227,30 @@ def test_line_lengths_against_oracle(hal, oracle, L):
                 assert err <= TOL(r), (xd, yd, r, wx, wy, gh is None, err)
 
 
+@pytest.mark.parametrize("xd,yd,wx,wy,dirichlet", [(5000, 24, True, False, False), (17, 4100, False, True, True),
+                                                   (4097, 9, False, False, True)])
+def test_lines_above_max_through_the_interface(hal, oracle, xd, yd, wx, wy, dirichlet):
+    """A side above HAL_CUDA_ADI_MAX_LINE: DiffuseADI (and its Dirichlet
+    form) solves the step in FP64, Thomas per line in the CPU backend's order,
+    so the deltas equal the CPU's bit for bit; the resident FP32 ticks refuse
+    such a grid."""
+    rng = np.random.default_rng(xd + yd)
+    f = rng.random(xd * yd)
+    d = (rng.random(xd * yd) - 0.5) * 0.1
+    ghost = rng.random(2 * (xd + yd)) if dirichlet else None
+    with hal.Adi(xd, yd) as a:
+        if dirichlet:
+            got = a.diffuse_adi_bc(f, d.copy(), 3.0, wx, wy, ghost)
+        else:
+            got = a.diffuse_adi(f, d.copy(), 3.0, xd, yd, wx, wy)
+        exp = oracle.diffuse_adi(f, d, 3.0, xd, yd, wx, wy, ghost=ghost)
+        assert np.array_equal(got, exp)
+        assert np.abs(got - d).max() > 0
+        with pytest.raises(RuntimeError, match="ADI line length"):
+            a.run_ticks(1, 3.0, 0.0)
+
+
 def test_rejects_bad_sizes(hal):
-    with pytest.raises(RuntimeError):
-        hal.Adi(hal.ADI_MAX_LINE + 1, 8)
     with hal.Adi(4, 4) as a:
         with pytest.raises(ValueError):
             a.run_steps(np.zeros(15, np.float32), 1, 0.1)
