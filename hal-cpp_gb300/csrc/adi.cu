@@ -507,11 +507,24 @@ namespace halcuda
                                 "l"(src + kc * M), "r"(static_cast<uint32_t>(n) * 4u), "r"(bar)
                                 : "memory");
                         }
+                        else if (src != nullptr)
+                        {
+                            // a line the bulk copy cannot take (unaligned or
+                            // ragged): 4-byte asynchronous copies, all of the
+                            // chunk in flight at once; the thread waits for
+                            // its own copies below
+                            for (int i = 0; i < n; i++)
+                            {
+                                asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(SmemAddr(dst + i)),
+                                             "l"(src + kc * M + i)
+                                             : "memory");
+                            }
+                        }
                         else
                         {
                             for (int i = 0; i < n; i++)
                             {
-                                dst[i] = (src != nullptr) ? __ldg(src + kc * M + i) : 0.0f;
+                                dst[i] = 0.0f;
                             }
                         }
                         for (int i = n; i < M; i++)
@@ -519,6 +532,7 @@ namespace halcuda
                             dst[i] = 0.0f;  // padding past the line end (disjoint from the copy)
                         }
                     }
+                    asm volatile("cp.async.wait_all;" ::: "memory");
                 }
             }
             if (tmaBytes > 0)
