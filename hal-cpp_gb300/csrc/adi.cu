@@ -377,7 +377,8 @@ namespace halcuda
                 asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dynBytes));
                 const int64_t need = 4 * (static_cast<int64_t>(R + 2) * p.LS + kCoefSmemFloats +
                                           2 * static_cast<int64_t>(R) * P + kGbandSmem);
-                if (R < 1 || R > kMaxR || (R / kNL) * P > nthreads || need > static_cast<int64_t>(dynBytes))
+                if (R < 1 || R > kMaxR || (R / kNL) * P > nthreads || need > static_cast<int64_t>(dynBytes) ||
+                    p.inStride < p.L || p.outStride < p.Nlines)
                 {
                     if (tid == 0)
                     {
@@ -388,6 +389,10 @@ namespace halcuda
             }
             const int32_t L = p.L;
             const bool vecL = (L & 3) == 0;
+            // lines padded to a multiple of 4 floats: whole 16-byte copies,
+            // the padding (zeros) included
+            const int32_t L4 = (L + 3) & ~3;
+            const bool inPadded = p.inStride >= L4 && (p.inStride & 3) == 0;
 
             // ---- 1. stage lines x0-1 .. x0+R --------------------------------
             __shared__ const float *sSrc[kMaxR + 2];
@@ -443,15 +448,18 @@ namespace halcuda
                     // lines further out (a CTA past the last line) are never read
                     const int32_t line = x0 - 1 + rs;
                     const float *src = nullptr;
+                    bool padded = false;  // the line's stride pads it to a multiple of 4 floats
                     if (line >= 0 && line < p.Nlines)
                     {
-                        src = p.in + static_cast<int64_t>(line) * L;
+                        src = p.in + static_cast<int64_t>(line) * p.inStride;
+                        padded = inPadded;
                     }
                     else if (line == -1 || line == p.Nlines)
                     {
                         if (p.wrapLines)
                         {
-                            src = p.in + static_cast<int64_t>((line < 0) ? p.Nlines - 1 : 0) * L;
+                            src = p.in + static_cast<int64_t>((line < 0) ? p.Nlines - 1 : 0) * p.inStride;
+                            padded = inPadded;
                         }
                         else
                         {
@@ -459,7 +467,7 @@ namespace halcuda
                         }
                     }
                     sSrc[rs] = src;
-                    sTma[rs] = (src != nullptr) && vecL && ((reinterpret_cast<uintptr_t>(src) & 15) == 0);
+                    sTma[rs] = (src != nullptr) && (vecL || padded) && ((reinterpret_cast<uintptr_t>(src) & 15) == 0);
                 }
                 for (int q = tid; q < kCoefFloats / 4; q += nthreads)
                 {
@@ -479,7 +487,7 @@ namespace halcuda
                 {
                     for (int rr = 0; rr < nStaged; rr++)
                     {
-                        tmaBytes += sTma[rr] ? static_cast<uint32_t>(L) * 4u : 0u;
+                        tmaBytes += sTma[rr] ? static_cast<uint32_t>(L4) * 4u : 0u;
                     }
                     if (tmaBytes > 0)
                     {
@@ -495,16 +503,21 @@ namespace halcuda
                     const int kc = tid % P;
                     const int rstride = nthreads / P;
                     const int32_t n = min(M, L - kc * M);  // elements of this chunk inside the line
+                    const int32_t n4 = (n + 3) & ~3;          // the same in whole 16-byte units
                     for (int rr = tid / P; rr < nStaged && tid < rstride * P; rr += rstride)
                     {
                         const float *src = sSrc[rr];
                         float *dst = sLines + rr * p.LS + kc * kChunkStride;
+                        int32_t filled = n;  // elements the copies write
                         if (sTma[rr])
                         {
+                            // a padded line's last chunk takes its padding
+                            // (zeros) along, to a whole 16-byte unit
+                            filled = n4;
                             asm volatile(
                                 "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                                     SmemAddr(dst)),
-                                "l"(src + kc * M), "r"(static_cast<uint32_t>(n) * 4u), "r"(bar)
+                                "l"(src + kc * M), "r"(static_cast<uint32_t>(n4) * 4u), "r"(bar)
                                 : "memory");
                         }
                         else if (src != nullptr)
@@ -527,7 +540,7 @@ namespace halcuda
                                 dst[i] = 0.0f;
                             }
                         }
-                        for (int i = n; i < M; i++)
+                        for (int i = filled; i < M; i++)
                         {
                             dst[i] = 0.0f;  // padding past the line end (disjoint from the copy)
                         }
@@ -560,6 +573,7 @@ namespace halcuda
                     {
                         continue;
                     }
+                    // (the tensor-staged form runs dense lines only: inStride == L)
                     const float *src = p.wrapLines ? p.in + static_cast<int64_t>((side == 0) ? p.Nlines - 1 : 0) * L
                                                    : ((side == 0) ? p.ghostLo : p.ghostHi);
                     if (src == nullptr)
@@ -769,14 +783,22 @@ namespace halcuda
             const int uStart = tid / Q;
             const int32_t line0 = x0 + 4 * qd;
             const int step = nthreads / Q;
-            const bool vecOut = (p.Nlines & 3) == 0;
+            // 16-byte output rows; with a padded output stride the last quad
+            // of the last tile may reach into the padding, which takes zeros
+            // (the tensor-staged form runs dense rows only: outStride == Nlines)
+            const int32_t outRow = SWZ ? p.Nlines : p.outStride;
+            const bool vecOut = (outRow & 3) == 0;
             const bool quadOk = line0 < p.Nlines;
-            const int32_t nU = L >> 2;
+            const int32_t quadLines = p.Nlines - line0;  // lines of the quad inside the grid (4 or more: all)
+            // units of 4 positions; the chunked form also writes a last,
+            // partial unit (positions past L skipped), the tensor-staged one
+            // has L % 256 == 0
+            const int32_t nU = SWZ ? (L >> 2) : ((L + 3) >> 2);
             // units per write-out batch: the y-sweep's commit loads two units
             // ahead of the barrier; the x-sweep only stores (1: 21.18 against
             // 21.23 us per 2048^2 tick with 2, 21.56 with 4)
             constexpr int kUB = (MODE == kSweepTick) ? 2 : 1;
-            const int64_t nl = p.Nlines;
+            const int64_t nl = outRow;
             // the commit's f and src of this thread's first write-out units,
             // loaded before the barrier so that their latency overlaps it
             // (the tensor-staged form; the register budget of the chunked
@@ -868,7 +890,7 @@ namespace halcuda
             }
             else
             {
-                if (vecOut && vecL)
+                if (vecOut && (vecL || !SWZ))
                 {
                     // 16-byte units: 4 positions x 4 lines move as a 4x4 block
                     // (4 LDS.128, a register transpose, 4 STG.128).  UPT: the
@@ -927,6 +949,10 @@ namespace halcuda
 #pragma unroll
                                         for (int i = 0; i < 4; i++)
                                         {
+                                            if (!SWZ && !vecL && 4 * u + i >= L)
+                                            {
+                                                continue;  // past the line end: no output row
+                                            }
                                             fv[b][i] = __ldg(reinterpret_cast<const float4 *>(p.f + g0 + i * nl));
                                             if (hasSrc)
                                             {
@@ -976,6 +1002,20 @@ namespace halcuda
                                         w4.y = commit(w4.y, fv[b][i].y, sv[b][i].y, n1);
                                         w4.z = commit(w4.z, fv[b][i].z, sv[b][i].z, n2);
                                         w4.w = commit(w4.w, fv[b][i].w, sv[b][i].w, n3);
+                                    }
+                                    if constexpr (!SWZ)
+                                    {
+                                        if (!vecL && 4 * u + i >= L)
+                                        {
+                                            continue;  // past the line end: no output row
+                                        }
+                                        if (quadLines < 4)
+                                        {
+                                            // lines past the grid: the row's padding, zeros
+                                            w4.y = (quadLines > 1) ? w4.y : 0.0f;
+                                            w4.z = (quadLines > 2) ? w4.z : 0.0f;
+                                            w4.w = 0.0f;
+                                        }
                                     }
                                     St4(out + i * nl, w4);
                                 }
@@ -1094,7 +1134,7 @@ namespace halcuda
                                                sLines[SolPos<SWZ>(4 * qd + 3, pos, P, p.LS)]);
                             if constexpr (MODE == kSweepTick)
                             {
-                                const int64_t gi = static_cast<int64_t>(pos) * p.Nlines + line0;
+                                const int64_t gi = static_cast<int64_t>(pos) * outRow + line0;
                                 if (vecOut)
                                 {
                                     fv[b] = __ldg(reinterpret_cast<const float4 *>(p.f + gi));
@@ -1156,7 +1196,7 @@ namespace halcuda
                             o.z = commit(v[b].z, fv[b].z, sv[b].z, nn[b][2]);
                             o.w = commit(v[b].w, fv[b].w, sv[b].w, nn[b][3]);
                         }
-                        const int64_t gi = static_cast<int64_t>(pos) * p.Nlines + line0;
+                        const int64_t gi = static_cast<int64_t>(pos) * outRow + line0;
                         if (vecOut)
                         {
                             St4(p.out + gi, o);
@@ -1197,7 +1237,8 @@ namespace halcuda
 
         // out[c][r] = in[r][c] for an rows x cols matrix (32x32 tiles).
         template <typename TIn>
-        __global__ void Transpose(const TIn *__restrict__ in, float *__restrict__ out, int32_t rows, int32_t cols)
+        __global__ void Transpose(const TIn *__restrict__ in, float *__restrict__ out, int32_t rows, int32_t cols,
+                                  int32_t inStride, int32_t outStride)
         {
             __shared__ float tile[32][33];
             const int32_t c0 = blockIdx.x * 32;
@@ -1208,7 +1249,7 @@ namespace halcuda
                 const int32_t c = c0 + threadIdx.x;
                 if (r < rows && c < cols)
                 {
-                    tile[j][threadIdx.x] = static_cast<float>(in[static_cast<int64_t>(r) * cols + c]);
+                    tile[j][threadIdx.x] = static_cast<float>(in[static_cast<int64_t>(r) * inStride + c]);
                 }
             }
             __syncthreads();
@@ -1218,7 +1259,7 @@ namespace halcuda
                 const int32_t r = r0 + threadIdx.x;
                 if (r < rows && c < cols)
                 {
-                    out[static_cast<int64_t>(c) * rows + r] = tile[threadIdx.x][j];
+                    out[static_cast<int64_t>(c) * outStride + r] = tile[threadIdx.x][j];
                 }
             }
         }
@@ -1465,9 +1506,15 @@ namespace halcuda
 
     int LaunchTranspose(const float *in, float *out, int32_t rows, int32_t cols, cudaStream_t s)
     {
+        return LaunchTransposeStrided(in, cols, out, rows, rows, cols, s);
+    }
+
+    int LaunchTransposeStrided(const float *in, int32_t inStride, float *out, int32_t outStride, int32_t rows,
+                               int32_t cols, cudaStream_t s)
+    {
         dim3 block(32, 8);
         dim3 grid((cols + 31) / 32, (rows + 31) / 32);
-        Transpose<float><<<grid, block, 0, s>>>(in, out, rows, cols);
+        Transpose<float><<<grid, block, 0, s>>>(in, out, rows, cols, inStride, outStride);
         CountLaunch();
         return LaunchStatus("Transpose launch");
     }
@@ -1632,7 +1679,7 @@ namespace halcuda
         {
             dim3 block(32, 8);
             dim3 grid((cols + 31) / 32, (rows + 31) / 32);
-            Transpose<TIn><<<grid, block, 0, s>>>(in, out, rows, cols);
+            Transpose<TIn><<<grid, block, 0, s>>>(in, out, rows, cols, cols, rows);
             CountLaunch();
             return LaunchStatus("Transpose launch");
         }
@@ -1641,6 +1688,9 @@ namespace halcuda
         int LaunchSweep(SweepParams &p, cudaStream_t s, const CUtensorMap *tmap)
         {
             const bool swz = (tmap != nullptr);
+            // the single grid's lines and output rows are dense
+            p.inStride = p.L;
+            p.outStride = p.Nlines;
             SweepShape sh = ShapeFor(p.plan.P, p.Nlines, swz);
             p.R = sh.R;
             p.LS = sh.LS;

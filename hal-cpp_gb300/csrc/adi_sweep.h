@@ -49,6 +49,13 @@ namespace halcuda
         const double *f64;        // kSweepDeltas: field (line-major)
         double *deltas;           // kSweepDeltas: deltas (line-major)
         int32_t *err;             // set to 1 if a bounded wait gave up
+        // Floats between consecutive input lines (>= L) and between
+        // consecutive output rows (>= Nlines).  A stride above the length
+        // pads each line or row to a multiple of 4 floats: the padding of the
+        // input lines must hold zeros, and the sweep writes zeros into the
+        // padding of its output rows, so that the next sweep can stage every
+        // line with 16-byte copies and write whole 16-byte units.
+        int32_t inStride, outStride;
     };
 
     // Device copy of the line plan (adi_plan.h) of lines of length L at rate
@@ -73,6 +80,11 @@ namespace halcuda
 
     // out[c][r] = in[r][c] for a rows x cols FP32 matrix.
     int LaunchTranspose(const float *in, float *out, int32_t rows, int32_t cols, cudaStream_t s);
+
+    // The same with row strides: out[c * outStride + r] = in[r * inStride + c]
+    // (inStride >= cols, outStride >= rows); padding is left untouched.
+    int LaunchTransposeStrided(const float *in, int32_t inStride, float *out, int32_t outStride, int32_t rows,
+                               int32_t cols, cudaStream_t s);
 
     // ---- batched sweeps (many independent grids in one launch) ------------
     //

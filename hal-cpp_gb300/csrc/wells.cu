@@ -62,6 +62,12 @@ namespace halcuda
         std::vector<hal_cuda_well_desc> desc;
         DevBuf<float> arena;
         std::vector<size_t> offF0, offF1, offSrc, offW;
+        // ADI wells keep their rows padded to multiples of 4 floats: the
+        // field and source (layout B, yDim rows) with stride strideF >= xDim,
+        // the x-sweep's w (layout A, xDim rows) with stride strideW >= yDim.
+        // The padding holds zeros (the arena starts zeroed and the sweeps
+        // write zeros there), so every line stages by 16-byte copies.
+        std::vector<int32_t> strideF, strideW;
         std::vector<uint8_t> hasSrc;
         int cur = 0;
 
@@ -157,18 +163,24 @@ namespace halcuda
             adiIdx.assign(nw, -1);
             cellBase.assign(nw, -1);
             counts.assign(nw, 0);
+            strideF.assign(nw, 0);
+            strideW.assign(nw, 0);
             size_t total = 0;
             for (int32_t w = 0; w < n; w++)
             {
-                const size_t c = RoundUp(Cells(w));
+                const bool adi = desc[w].kind == HAL_CUDA_WELL_ADI;
+                strideF[w] = adi ? (desc[w].xDim + 3) & ~3 : desc[w].xDim;
+                strideW[w] = adi ? (desc[w].yDim + 3) & ~3 : desc[w].yDim;
+                const size_t c = adi ? RoundUp(static_cast<size_t>(desc[w].yDim) * static_cast<size_t>(strideF[w]))
+                                     : RoundUp(Cells(w));
                 offF0[w] = total;
                 offF1[w] = total + c;
                 offSrc[w] = total + 2 * c;
                 total += 3 * c;
-                if (desc[w].kind == HAL_CUDA_WELL_ADI)
+                if (adi)
                 {
                     offW[w] = total;
-                    total += c;
+                    total += RoundUp(static_cast<size_t>(desc[w].xDim) * static_cast<size_t>(strideW[w]));
                     adiIdx[w] = static_cast<int32_t>(adiWell.size());
                     adiWell.push_back(w);
                 }
@@ -385,6 +397,8 @@ namespace halcuda
                     p.LS = shx.LS;
                     p.out = W(w);
                     p.err = err.p;
+                    p.inStride = strideF[w];
+                    p.outStride = strideW[w];
                     sx[a] = p;
 
                     SweepParams q;
@@ -404,6 +418,8 @@ namespace halcuda
                     q.src = hasSrc[w] ? Src(w) : nullptr;
                     q.negDecay = static_cast<float>(-d.decay);
                     q.err = err.p;
+                    q.inStride = strideW[w];
+                    q.outStride = strideF[w];
                     sy[a] = q;
                 }
                 cudaStream_t s = stream.Get();
@@ -845,8 +861,9 @@ extern "C" int hal_cuda_wells_set_field(hal_cuda_wells *h, int32_t well, const f
     const size_t bytes = static_cast<size_t>(len) * sizeof(float);
     if (d.kind == HAL_CUDA_WELL_ADI)
     {
+        // dense through the x-sweep scratch, then into the padded rows
         HAL_TRY(CudaStatus(cudaMemcpyAsync(h->W(well), field, bytes, cudaMemcpyHostToDevice, s), "cudaMemcpy(field)"));
-        HAL_TRY(LaunchTranspose(h->W(well), h->F(well, h->cur), d.xDim, d.yDim, s));
+        HAL_TRY(LaunchTransposeStrided(h->W(well), d.yDim, h->F(well, h->cur), h->strideF[well], d.xDim, d.yDim, s));
     }
     else
     {
@@ -869,7 +886,7 @@ extern "C" int hal_cuda_wells_get_field(hal_cuda_wells *h, int32_t well, float *
     const float *from = h->F(well, h->cur);
     if (d.kind == HAL_CUDA_WELL_ADI)
     {
-        HAL_TRY(LaunchTranspose(from, h->W(well), d.yDim, d.xDim, s));
+        HAL_TRY(LaunchTransposeStrided(from, h->strideF[well], h->W(well), d.yDim, d.yDim, d.xDim, s));
         from = h->W(well);
     }
     HAL_TRY(CudaStatus(cudaMemcpyAsync(field, from, bytes, cudaMemcpyDeviceToHost, s), "cudaMemcpy(field)"));
@@ -896,7 +913,7 @@ extern "C" int hal_cuda_wells_set_source(hal_cuda_wells *h, int32_t well, const 
     {
         // through the x-sweep scratch, which holds nothing between ticks
         HAL_TRY(CudaStatus(cudaMemcpyAsync(h->W(well), dense, bytes, cudaMemcpyHostToDevice, s), "cudaMemcpy(source)"));
-        HAL_TRY(LaunchTranspose(h->W(well), h->Src(well), d.xDim, d.yDim, s));
+        HAL_TRY(LaunchTransposeStrided(h->W(well), d.yDim, h->Src(well), h->strideF[well], d.xDim, d.yDim, s));
     }
     else
     {
