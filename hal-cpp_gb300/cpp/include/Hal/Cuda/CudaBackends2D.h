@@ -95,7 +95,8 @@ namespace Hal::Cuda
                             const std::vector<double> &ghostXVel = {},
                             const std::vector<double> &ghostYVel = {});
 
-        // Device-resident PDEGrid2D tick: f' = f + r L(f) - decay f + src.
+        // Device-resident PDEGrid2D tick:
+        // f' = f + r L(f) - decay f + src - uptake * (agents in the cell) * f.
         void SetField(const std::vector<float> &field);
         void GetField(std::vector<float> &field);
         void SetSource(const std::vector<float> &dense);
@@ -103,6 +104,9 @@ namespace Hal::Cuda
         void SetDirichlet(const std::vector<float> &ghost);
         // PDEGrid2D::Advection(xVel, yVel) in every following tick (upwind).
         void SetVelocity(double xVel, double yVel);
+        // PDEGrid2D::Mul(cell, -uptake) once per agent of pAgents' last
+        // binning, every following tick (nullptr removes the coupling).
+        void SetUptake(CudaAgentForceBackend2D *pAgents, double uptake);
         void RunTicks(int32_t ticks, double diffRate, double decay, bool wrapX, bool wrapY);
         void Sync();
 

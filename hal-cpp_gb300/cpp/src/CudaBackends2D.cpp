@@ -139,6 +139,12 @@ namespace Hal::Cuda
         Check(hal_cuda_diffusion_set_velocity(m_pHandle, xVel, yVel), "CudaDiffusionBackend2D::SetVelocity");
     }
 
+    void CudaDiffusionBackend2D::SetUptake(CudaAgentForceBackend2D *pAgents, double uptake)
+    {
+        Check(hal_cuda_diffusion_set_uptake(m_pHandle, pAgents ? pAgents->Handle() : nullptr, uptake),
+              "CudaDiffusionBackend2D::SetUptake");
+    }
+
     void CudaDiffusionBackend2D::SetField(const std::vector<float> &field)
     {
         Check(hal_cuda_diffusion_set_field(m_pHandle, field.data(), static_cast<int64_t>(field.size())),

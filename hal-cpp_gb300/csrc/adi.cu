@@ -1545,13 +1545,8 @@ namespace halcuda
     }
 }
 
-struct hal_cuda_agents;  // agents.cu
-
 namespace halcuda
 {
-    // Device cell offsets of an agent handle's last dispatch and its grid.
-    const int32_t *AgentsCellOffsets(const hal_cuda_agents *a, int32_t *xDim, int32_t *yDim);
-
     struct Adi
     {
         int32_t xDim = 0, yDim = 0;

@@ -13,7 +13,8 @@
 //
 // Every line has its own tridiagonal matrix, so the line solves are parallel
 // cyclic reduction in shared memory (one CTA per line, one row per thread);
-// a wrapped line of a power-of-two length needs no Sherman-Morrison step.
+// a wrapped line of a power-of-two length reduces cyclically, any other
+// wrapped line by a Sherman-Morrison split (PcrSolveSM).
 //
 // Gradient of loss = 1/2 |f_T - target|^2.  I - L/2 and I + L/2 are
 // symmetric, so with gbar the adjoint of a step's output:
@@ -169,11 +170,112 @@ namespace halcuda
             return 0.0f;
         }
 
+        // A wrapped line whose length is not a power of two: the cyclic
+        // system A x = d is split as A = T + u v^T (TdmaSolver::TDMAperiodic's
+        // form, include/Hal/Pde/TdmaSolver.h:68-120: gamma = -b_0, T's
+        // diagonal b_0 - gamma and b_{n-1} - a_0 c_{n-1} / gamma, u = (gamma,
+        // 0, .., 0, c_{n-1}), v = (1, 0, .., 0, a_0 / gamma)); T y = d and
+        // T z = u are solved together by non-wrapped parallel cyclic reduction
+        // (the reductions of T are shared), then x = y - (v.y / (1 + v.z)) z.
+        // sm holds 4 * blockDim.x floats, sm2 blockDim.x + 4.
+        __device__ float PcrSolveSM(const float *sD, float d, int32_t j, int32_t n, float *sm, float *sm2)
+        {
+            float *sa = sm, *sb = sm + blockDim.x, *sc = sb + blockDim.x, *sd = sc + blockDim.x;
+            float *sd2 = sm2, *sx = sm2 + blockDim.x;
+            float eL0, eR0, eLn, eRn;
+            Faces(sD, 0, n, true, eL0, eR0);
+            Faces(sD, n - 1, n, true, eLn, eRn);
+            const float a0 = -0.5f * eL0;                 // row 0's coefficient of x_{n-1}
+            const float cn = -0.5f * eRn;                 // row n-1's coefficient of x_0
+            const float gam = -(1.0f + 0.5f * (eL0 + eR0));  // -b_0
+            float a = 0.0f, b = 1.0f, c = 0.0f, d2 = 0.0f;
+            if (j < n)
+            {
+                float eL, eR;
+                Faces(sD, j, n, true, eL, eR);
+                a = (j > 0) ? -0.5f * eL : 0.0f;
+                c = (j < n - 1) ? -0.5f * eR : 0.0f;
+                b = 1.0f + 0.5f * (eL + eR);
+                if (j == 0)
+                {
+                    b -= gam;
+                    d2 = gam;
+                }
+                if (j == n - 1)
+                {
+                    b -= a0 * cn / gam;
+                    d2 = cn;
+                }
+            }
+            for (int32_t delta = 1; delta < n; delta <<= 1)
+            {
+                if (j < n)
+                {
+                    sa[j] = a;
+                    sb[j] = b;
+                    sc[j] = c;
+                    sd[j] = d;
+                    sd2[j] = d2;
+                }
+                __syncthreads();
+                if (j < n)
+                {
+                    float al = 0.0f, bl = 1.0f, cl = 0.0f, dl = 0.0f, dl2 = 0.0f;
+                    float ar = 0.0f, br = 1.0f, cr = 0.0f, dr = 0.0f, dr2 = 0.0f;
+                    const int32_t il = j - delta, ir = j + delta;
+                    if (il >= 0)
+                    {
+                        al = sa[il];
+                        bl = sb[il];
+                        cl = sc[il];
+                        dl = sd[il];
+                        dl2 = sd2[il];
+                    }
+                    if (ir < n)
+                    {
+                        ar = sa[ir];
+                        br = sb[ir];
+                        cr = sc[ir];
+                        dr = sd[ir];
+                        dr2 = sd2[ir];
+                    }
+                    const float alpha = -__fdividef(a, bl);
+                    const float beta = -__fdividef(c, br);
+                    b = b + alpha * cl + beta * ar;
+                    d = d + alpha * dl + beta * dr;
+                    d2 = d2 + alpha * dl2 + beta * dr2;
+                    a = alpha * al;
+                    c = beta * cr;
+                }
+                __syncthreads();
+            }
+            const float y = d / b, z = d2 / b;
+            if (j == 0)
+            {
+                sx[0] = y;
+                sx[2] = z;
+            }
+            if (j == n - 1)
+            {
+                sx[1] = y;
+                sx[3] = z;
+            }
+            __syncthreads();
+            const float bog = a0 / gam;
+            const float fct = (sx[0] + bog * sx[1]) / (1.0f + (sx[2] + bog * sx[3]));
+            return y - fct * z;
+        }
+
         // Solves (I - L/2) x = d along the line by parallel cyclic reduction;
-        // thread j holds row j (j < n); sm holds 4 * blockDim.x floats.  A
-        // wrapped line must have a power-of-two length.
+        // thread j holds row j (j < n); sm holds 4 * blockDim.x floats, and a
+        // wrapped line whose length is not a power of two uses blockDim.x + 4
+        // more after the four line arrays (PcrSolveSM).
         __device__ float PcrSolve(const float *sD, float d, int32_t j, int32_t n, bool wrap, float *sm)
         {
+            if (wrap && n > 2 && (n & (n - 1)) != 0)
+            {
+                return PcrSolveSM(sD, d, j, n, sm, sm + 8 * blockDim.x);  // uniform across the CTA
+            }
             float *sa = sm, *sb = sm + blockDim.x, *sc = sb + blockDim.x, *sd = sc + blockDim.x;
             float a = 0.0f, b = 1.0f, c = 0.0f;
             if (j < n)
@@ -259,10 +361,12 @@ namespace halcuda
             return t;
         }
 
-        // Shared memory of the line kernels: 4 PCR arrays + 4 line arrays.
+        // Shared memory of the line kernels: 4 PCR arrays + 4 line arrays,
+        // then the second right-hand side and the broadcast values of the
+        // Sherman-Morrison solve (PcrSolveSM).
         __host__ __device__ constexpr size_t LineSmemFloats(int threads)
         {
-            return 8 * static_cast<size_t>(threads);
+            return 9 * static_cast<size_t>(threads) + 4;
         }
 
         // x-sweep: w = (I - Lx/2)^-1 (I + Ly/2) f, one CTA per line y, in
@@ -971,14 +1075,6 @@ namespace halcuda
             return rc;
         }
     };
-
-    namespace
-    {
-        bool PowerOfTwo(int32_t v)
-        {
-            return v > 0 && (v & (v - 1)) == 0;
-        }
-    }
 }
 
 using halcuda::Adjoint;
@@ -994,10 +1090,6 @@ extern "C" int hal_cuda_adjoint_create(int32_t xDim, int32_t yDim, int32_t wrapX
     *out = nullptr;
     HAL_REQUIRE(xDim >= 1 && yDim >= 1 && xDim <= halcuda::kMaxAdjLine && yDim <= halcuda::kMaxAdjLine,
                 "hal_cuda_adjoint_create: grid %d x %d, sides must be in [1, %d]", xDim, yDim, halcuda::kMaxAdjLine);
-    HAL_REQUIRE(!wrapX || halcuda::PowerOfTwo(xDim), "hal_cuda_adjoint_create: a wrapped x axis needs a power-of-two "
-                                                     "xDim (%d)", xDim);
-    HAL_REQUIRE(!wrapY || halcuda::PowerOfTwo(yDim), "hal_cuda_adjoint_create: a wrapped y axis needs a power-of-two "
-                                                     "yDim (%d)", yDim);
     hal_cuda_adjoint *h = new (std::nothrow) hal_cuda_adjoint();
     if (h == nullptr)
     {

@@ -34,6 +34,10 @@ namespace halcuda
     void DiffusionDims(const hal_cuda_diffusion *h, int32_t *xDim, int32_t *yDim);
     void AdiDims(const hal_cuda_adi *h, int32_t *xDim, int32_t *yDim);
 
+    // Device cell offsets of an agent handle's last dispatch (agents.cu) and
+    // its grid: the agent count of cell i is offsets[i + 1] - offsets[i].
+    const int32_t *AgentsCellOffsets(const hal_cuda_agents *a, int32_t *xDim, int32_t *yDim);
+
     // Maps a CUDA error to a status, recording the message.
     inline int CudaStatus(cudaError_t e, const char *what)
     {

@@ -105,7 +105,9 @@ namespace halcuda
         // or zero-flux cases, so every difference weight is 1.  The
         // arithmetic is the general path's with those weights (x * 1 and
         // fmaf(x, 1, y) round as x and x + y), so results are bit-identical.
-        template <bool ADV>
+        // UPT: the commit also multiplies each cell by negUptake once per
+        // agent binned in it (TickParams::cellOffsets).
+        template <bool ADV, bool UPT>
         __device__ __forceinline__ void TickInterior(const TickParams &p, const int32_t bx, const int32_t by,
                                                      const int32_t y0, const int32_t xs)
         {
@@ -171,6 +173,19 @@ namespace halcuda
                     o[k] = d + sv[k];
                 }
                 const int32_t x = xs + t;
+                if constexpr (UPT)
+                {
+                    // agent counts of the four cells: five consecutive offsets
+                    const int32_t *oc = p.cellOffsets + x * yD + y0;
+                    const int4 o4 = __ldg(reinterpret_cast<const int4 *>(oc));
+                    const int32_t o5 = __ldg(oc + 4);
+                    const int32_t nc[4] = {o4.y - o4.x, o4.z - o4.y, o4.w - o4.z, o5 - o4.w};
+#pragma unroll
+                    for (int k = 0; k < 4; k++)
+                    {
+                        o[k] = fmaf(cur[k], p.negUptake * static_cast<float>(nc[k]), o[k]);
+                    }
+                }
                 for (int32_t q = ptBeg; q < ptEnd; q++)
                 {
                     if (__ldg(p.ptRow + q) == x)
@@ -192,7 +207,7 @@ namespace halcuda
             }
         }
 
-        template <int VEC, bool ADV = false>
+        template <int VEC, bool ADV = false, bool UPT = false>
         __device__ __forceinline__ void TickTile(const TickParams &p, const int32_t bx, const int32_t by)
         {
             constexpr int T = kTickRowsPerThread;
@@ -208,7 +223,7 @@ namespace halcuda
             {
                 if (xs >= 1 && xs + T < p.xDim && y0 >= 1 && y0 + 4 < p.yDim)
                 {
-                    TickInterior<ADV>(p, bx, by, y0, xs);
+                    TickInterior<ADV, UPT>(p, bx, by, y0, xs);
                     return;
                 }
             }
@@ -363,6 +378,19 @@ namespace halcuda
                     }
                     o[k] = d + srcv[t][k];
                 }
+                if constexpr (UPT)
+                {
+                    const int32_t *oc = p.cellOffsets + static_cast<int64_t>(x) * p.yDim + y0;
+#pragma unroll
+                    for (int k = 0; k < VEC; k++)
+                    {
+                        if (k < nValid)
+                        {
+                            const int32_t nc = __ldg(oc + k + 1) - __ldg(oc + k);
+                            o[k] = fmaf(cur[k], p.negUptake * static_cast<float>(nc), o[k]);
+                        }
+                    }
+                }
                 for (int32_t q = ptBeg; q < ptEnd; q++)
                 {
                     if (__ldg(p.ptRow + q) == x)
@@ -405,7 +433,7 @@ namespace halcuda
 
         // Four CTAs per SM (64 registers) measured fastest for the plain tick
         // (6.68 vs 6.78 us at 2048^2); the advective tick is fastest unbounded.
-        template <int VEC, bool ADV>
+        template <int VEC, bool ADV, bool UPT = false>
         __global__ void __launch_bounds__(32 * kTickWarps, ADV ? 1 : 4)
             TickKernel(TickParams p)
         {
@@ -416,7 +444,7 @@ namespace halcuda
             // field (a no-op when launched without the attribute).
             asm volatile("griddepcontrol.launch_dependents;");
             asm volatile("griddepcontrol.wait;" ::: "memory");
-            TickTile<VEC, ADV>(p, static_cast<int32_t>(blockIdx.x), static_cast<int32_t>(blockIdx.y));
+            TickTile<VEC, ADV, UPT>(p, static_cast<int32_t>(blockIdx.x), static_cast<int32_t>(blockIdx.y));
         }
 
         // Batched form: CTA b runs tile tiles[b] = (grid, CTA column, CTA row).
@@ -481,6 +509,10 @@ namespace halcuda
         DevBuf<float> ptVal;
         bool hasPoints = false;
         double xVel = 0.0, yVel = 0.0;  // uniform advection of every tick (PDEGrid2D::Advection)
+        // agent uptake coupling (hal_cuda_diffusion_set_uptake): the agent
+        // handle whose last binning gives each cell's agent count
+        const hal_cuda_agents *agents = nullptr;
+        double uptake = 0.0;
         int32_t nPoints = 0;
         // Temporal blocking: ticks per launch 1 or 2 (0 = automatic, which
         // is 1).  The two-tick kernel stages tiles with a tensor map per field
@@ -536,9 +568,11 @@ namespace halcuda
             return HAL_CUDA_OK;
         }
 
+        // (the two-tick kernel has no uptake term: coupled ticks run one per
+        // launch)
         bool UseBlocked(int32_t ticks) const
         {
-            return tmapOk && ticks >= 2 && blockMode == 2;
+            return tmapOk && ticks >= 2 && blockMode == 2 && agents == nullptr;
         }
 
         // The dense source plus the point sources as one array (null if
@@ -623,6 +657,14 @@ namespace halcuda
             p.kDn = static_cast<float>(r + std::max(-vx, 0.0));
             p.kYm = static_cast<float>(r + std::max(vy, 0.0));
             p.kYp = static_cast<float>(r + std::max(-vy, 0.0));
+            p.cellOffsets = nullptr;
+            p.negUptake = 0.0f;
+            if (useExtras && agents != nullptr)
+            {
+                int32_t ax = 0, ay = 0;
+                p.cellOffsets = AgentsCellOffsets(agents, &ax, &ay);
+                p.negUptake = static_cast<float>(-uptake);
+            }
             return p;
         }
 
@@ -642,7 +684,18 @@ namespace halcuda
             at[0].val.programmaticStreamSerializationAllowed = 1;
             cfg.attrs = at;
             cfg.numAttrs = 1;
-            if (vec4)
+            if (p.cellOffsets != nullptr)
+            {
+                if (vec4)
+                {
+                    cudaLaunchKernelEx(&cfg, adv ? TickKernel<4, true, true> : TickKernel<4, false, true>, p);
+                }
+                else
+                {
+                    cudaLaunchKernelEx(&cfg, adv ? TickKernel<1, true, true> : TickKernel<1, false, true>, p);
+                }
+            }
+            else if (vec4)
             {
                 if (adv)
                 {
@@ -687,9 +740,9 @@ namespace halcuda
             // for an odd count); each launch flips the buffers
             const int32_t launches = blocked ? ticks / 2 + (ticks & 1) : ticks;
             char key[256];
-            snprintf(key, sizeof(key), "%d|%a|%a|%d|%d|%d|%d|%d|%d|%a|%a|%d|%p", ticks, r, decay, wrapX, wrapY,
-                     extras ? 1 : 0, hasSrc, hasPoints, hasGhost, xVel, yVel, blocked ? 1 : 0,
-                     static_cast<void *>(s));
+            snprintf(key, sizeof(key), "%d|%a|%a|%d|%d|%d|%d|%d|%d|%a|%a|%d|%p|%p|%a", ticks, r, decay, wrapX,
+                     wrapY, extras ? 1 : 0, hasSrc, hasPoints, hasGhost, xVel, yVel, blocked ? 1 : 0,
+                     static_cast<void *>(s), static_cast<const void *>(agents), uptake);
             GraphCache &graph = this->graph[cur];
             if (graph.exec == nullptr || graph.key != key)
             {
@@ -1140,6 +1193,26 @@ extern "C" int hal_cuda_diffusion_set_point_sources(hal_cuda_diffusion *h, int32
                                 "cudaMemcpy(points)"));
     h->hasPoints = true;
     h->nPoints = nPoints;
+    return HAL_CUDA_OK;
+}
+
+extern "C" int hal_cuda_diffusion_set_uptake(hal_cuda_diffusion *h, hal_cuda_agents *agents, double uptake)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_diffusion_set_uptake: handle is NULL");
+    if (agents == nullptr)
+    {
+        h->agents = nullptr;
+        h->uptake = 0.0;
+        return HAL_CUDA_OK;
+    }
+    HAL_REQUIRE(std::isfinite(uptake), "hal_cuda_diffusion_set_uptake: uptake must be finite");
+    int32_t ax = 0, ay = 0;
+    halcuda::AgentsCellOffsets(agents, &ax, &ay);
+    HAL_REQUIRE(ax == h->xDim && ay == h->yDim,
+                "hal_cuda_diffusion_set_uptake: agent grid %dx%d differs from the field %dx%d", ax, ay, h->xDim,
+                h->yDim);
+    h->agents = agents;
+    h->uptake = uptake;
     return HAL_CUDA_OK;
 }
 

@@ -72,6 +72,7 @@ SIGNATURES = {
     "hal_cuda_adi_set_source": (_I, [_vp, _vp, _i64]),
     "hal_cuda_adi_set_dirichlet": (_I, [_vp, _vp]),
     "hal_cuda_adi_set_uptake": (_I, [_vp, _vp, _f64]),
+    "hal_cuda_diffusion_set_uptake": (_I, [_vp, _vp, _f64]),
     "hal_cuda_adi_run_ticks": (_I, [_vp, _i32, _f64, _f64, _i32, _i32]),
     "hal_cuda_adi_run_steps": (_I, [_vp, _vp, _i64, _i32, _f64, _i32, _i32]),
     "hal_cuda_adi_run_ticks_host": (_I, [_vp, _vp, _vp, _i64, _i32, _f64, _f64, _i32, _i32]),
@@ -417,6 +418,12 @@ class Diffusion(_Handle):
     def set_velocity(self, xVel, yVel):
         """Uniform upwind advection of every following tick (PDEGrid2D::Advection)."""
         _check(lib().hal_cuda_diffusion_set_velocity(self._h, float(xVel), float(yVel)), "set_velocity")
+
+    def set_uptake(self, agents, uptake):
+        """Each agent of ``agents`` (its last binning) multiplies its cell by
+        -uptake every following tick; ``agents`` None removes the coupling."""
+        _check(lib().hal_cuda_diffusion_set_uptake(self._h, None if agents is None else agents.handle,
+                                                   uptake), "set_uptake")
 
     def run_ticks(self, ticks, diffRate, decay=0.0, wrapX=False, wrapY=False):
         _check(lib().hal_cuda_diffusion_run_ticks(self._h, ticks, diffRate, decay, int(wrapX),

@@ -148,6 +148,14 @@ int hal_cuda_diffusion_set_point_sources(hal_cuda_diffusion *h, int32_t nPoints,
                                          const int32_t *cells, const float *values);
 int hal_cuda_diffusion_set_dirichlet(hal_cuda_diffusion *h, const float *ghost);
 
+/* Agent uptake coupling of the explicit tick: every agent of `agents`
+ * (binned by its last dispatch or step) multiplies its cell by -uptake each
+ * tick, as a model's PDEGrid2D::Mul(cell, -uptake) per agent
+ * (PDEGrid2D.h:126-130, examples/CompetitiveRelease.cpp:147) before
+ * Update.  The agent handle's grid must match; agents NULL removes the
+ * coupling.  Coupled ticks run one per launch. */
+int hal_cuda_diffusion_set_uptake(hal_cuda_diffusion *h, hal_cuda_agents *agents, double uptake);
+
 /* Ticks per launch of the resident explicit tick: 1, 2 (temporal blocking:
  * a CTA stages its tile with a 2-cell halo by TMA and computes two ticks in
  * shared memory, so a pair of ticks reads and writes the field once), or 0
@@ -168,7 +176,8 @@ int hal_cuda_diffusion_set_velocity(hal_cuda_diffusion *h, double xVel, double y
 
 /* `ticks` fused ticks on the resident field, each
  *   f' = f + diffRate*L_bc(f) [+ advection] - decay*f + src + points
- * (PDEGrid2D::Diffusion + MulAll(-decay) + Add + Update).  EINVAL if
+ *        - uptake*count*f
+ * (PDEGrid2D::Diffusion + MulAll(-decay) + Add + Mul + Update).  EINVAL if
  * diffRate > 0.25 (PDEGrid2D::CheckDiffusionStable, PDEGrid2D.h:436-442).
  * Asynchronous on the handle's stream; a run of ticks is replayed from a
  * CUDA graph. */
@@ -595,7 +604,9 @@ int hal_cuda_wells_set_stream(hal_cuda_wells *h, void *stream);
  * loss = 1/2 |f_T - target|^2 with respect to D, decay and src comes from
  * adjoint kernels (transposed stencils and transposed line solves in reverse
  * sweep order) over states recomputed from checkpoints.  Sides up to
- * HAL_CUDA_ADJOINT_MAX_SIDE; a wrapped axis needs a power-of-two side. */
+ * HAL_CUDA_ADJOINT_MAX_SIDE, wrapped or zero-flux at any length (a wrapped
+ * line that is not a power of two long is solved with a Sherman-Morrison
+ * split, as TdmaSolver::TDMAperiodic does). */
 #define HAL_CUDA_ADJOINT_MAX_SIDE 1024
 
 typedef struct hal_cuda_adjoint hal_cuda_adjoint;

@@ -365,3 +365,66 @@ def test_explicit_2048_full_size(hal, oracle):
         out = d.get_field()
     assert rel_l2(out, exp) <= 1e-6
     assert max_rel(out, exp) <= 1e-5
+
+
+@pytest.mark.parametrize("xd,yd,wrapX,wrapY,dirichlet,vel", [
+    (300, 256, False, False, False, None),   # float4 strips, interior fast path
+    (257, 130, True, False, True, None),     # scalar strips, wrapped x, Dirichlet
+    (128, 200, False, True, False, (0.1, -0.2)),  # advective tick
+])
+def test_explicit_tick_uptake_against_oracle(hal, oracle, xd, yd, wrapX, wrapY, dirichlet, vel):
+    """Agent uptake on the explicit tick: every agent of the agent handle's
+    last binning multiplies its cell by -uptake each tick (a model's
+    PDEGrid2D::Mul(cell, -uptake) per agent), with decay, a dense source,
+    point sources and every boundary kind, against the FP64 oracle tick with
+    the same per-cell counts.  Removing the coupling gives the plain tick."""
+    rng = np.random.default_rng(xd * 7 + yd)
+    n = xd * yd
+    f0 = rng.random(n).astype(np.float32)
+    src = (rng.random(n) * 1e-3).astype(np.float32)
+    ghost = rng.random(2 * (xd + yd)).astype(np.float32) if dirichlet else None
+    pidx = rng.choice(n, 40, replace=False).astype(np.int32)
+    pval = (rng.random(40) * 0.05).astype(np.float32)
+    r, decay, uptake, ticks = 0.2, 1e-3, 4e-3, 25
+    nAgents = 3 * n // 2
+    pos = np.empty(2 * nAgents, np.float32)
+    pos[0::2] = rng.random(nAgents) * xd
+    pos[1::2] = np.clip(yd * 0.5 + rng.normal(0.0, yd * 0.15, nAgents), 0, yd - 1e-3)
+    with hal.Agents(xd, yd, nAgents) as ag, hal.Diffusion(xd, yd) as d:
+        ag.upload(pos, np.full(nAgents, 0.5, np.float32))
+        ag.dispatch(1.0, 0.1)
+        ag.sync()
+        off, _ = ag.get_bins()
+        counts = np.diff(off).astype(np.int32)
+        assert counts.sum() == nAgents and counts.max() >= 3
+        d.set_field(f0)
+        d.set_source(src)
+        d.set_point_sources(pidx, pval)
+        if ghost is not None:
+            d.set_dirichlet(ghost)
+        if vel is not None:
+            d.set_velocity(*vel)
+        d.set_uptake(ag, uptake)
+        d.run_ticks(ticks, r, decay, wrapX, wrapY)
+        out = d.get_field()
+        d.set_uptake(None, 0.0)
+        d.set_field(f0)
+        d.run_ticks(ticks, r, decay, wrapX, wrapY)
+        plain = d.get_field()
+    g64 = None if ghost is None else ghost.astype(np.float64)
+    vx, vy = vel if vel is not None else (0.0, 0.0)
+    exp = oracle.run_ticks(0, f0.astype(np.float64), xd, yd, r, wrapX, wrapY, g64, decay,
+                           src_dense=src.astype(np.float64), src_idx=pidx, src_val=pval.astype(np.float64),
+                           uptake_count=counts, uptake=uptake, ticks=ticks, xVel=vx, yVel=vy)
+    exp_plain = oracle.run_ticks(0, f0.astype(np.float64), xd, yd, r, wrapX, wrapY, g64, decay,
+                                 src_dense=src.astype(np.float64), src_idx=pidx, src_val=pval.astype(np.float64),
+                                 ticks=ticks, xVel=vx, yVel=vy)
+    assert max_rel(exp, exp_plain) > 1e-3  # the coupling changes the field
+    assert max_rel(out, exp) <= 1e-5, max_rel(out, exp)
+    assert max_rel(plain, exp_plain) <= 1e-5, max_rel(plain, exp_plain)
+
+
+def test_explicit_uptake_rejects_other_grid(hal):
+    with hal.Agents(32, 16, 10) as ag, hal.Diffusion(16, 32) as d:
+        with pytest.raises(ValueError, match="differs"):
+            d.set_uptake(ag, 1e-3)

@@ -8,6 +8,8 @@ CPU oracle within the usual tolerances:
   <= 2e-6 (1 + r) per tick (ADI);
 * agent forces: bit-identical to hal.Agents dispatch; bins per well follow
   the CPU's order, so the FP32 forces equal the single-grid ones exactly.
+  They are also compared directly with the FP64 oracle's forces (max-rel
+  <= 1e-4), as are the fields of a sample of the 512-well workload.
 """
 from __future__ import annotations
 
@@ -60,6 +62,15 @@ def _alone(hal, w, field, src, ticks):
         return h.get_field()
 
 
+FORCE_TOL = 1e-4
+
+
+def _oracle_forces(oracle, w, pos, rad):
+    v, _, _ = oracle.accumulate_forces(pos.astype(np.float64), rad.astype(np.float64), R, K, w["xDim"],
+                                       w["yDim"], w.get("wrapX", False), w.get("wrapY", False))
+    return v
+
+
 def _alone_forces(hal, w, pos, rad):
     with hal.Agents(w["xDim"], w["yDim"], max(len(rad), 1)) as ag:
         ag.upload(pos, rad)
@@ -99,6 +110,7 @@ def test_wells_equal_single_grid_handles(hal, oracle):
         at += n
         if n:
             assert np.array_equal(v, _alone_forces(hal, w, pos[i], rad[i])), (i, w)
+            assert max_rel(v, _oracle_forces(oracle, w, pos[i], rad[i])) <= FORCE_TOL, (i, w)
 
 
 def test_wells_bin_sizes_equal_single_grid_forces(hal):
@@ -237,9 +249,10 @@ def test_wells_reject_bad_input(hal):
             b.run_ticks(1, -1.0, 0.1)
 
 
-def test_wells_batched_workload_sample(hal):
+def test_wells_batched_workload_sample(hal, oracle):
     """512 wells of the batched workload (109M cells, 5.2M agents): two
-    ticks, and a sample of wells against the single-grid handles."""
+    ticks, and a sample of wells against the single-grid handles and the
+    FP64 oracle (fields and forces)."""
     from halcuda import workloads
 
     w = workloads.wells_inputs()
@@ -257,7 +270,14 @@ def test_wells_batched_workload_sample(hal):
         wd = w["wells"][i]
         wd = dict(wd, wrapX=False, wrapY=False)
         assert np.array_equal(got[i], _alone(hal, wd, w["fields"][i], None, 2)), i
+        mode = 1 if wd["kind"] == "adi" else 0
+        ref = oracle.run_ticks(mode, w["fields"][i].astype(np.float64), wd["xDim"], wd["yDim"], wd["diffRate"],
+                               decay=wd["decay"], ticks=2, threads=8)
+        tol = 2e-6 * (1 + wd["diffRate"]) * 2 if mode == 1 else 1e-5
+        assert max_rel(got[i], ref) <= tol, i
         a, e = int(starts[i]), int(starts[i + 1])
         if e > a:
-            exp = _alone_forces(hal, wd, w["positions"][2 * a: 2 * e], w["radii"][a:e])
+            p, rd = w["positions"][2 * a: 2 * e], w["radii"][a:e]
+            exp = _alone_forces(hal, wd, p, rd)
             assert np.array_equal(forces[2 * a: 2 * e], exp), i
+            assert max_rel(forces[2 * a: 2 * e], _oracle_forces(oracle, wd, p, rd)) <= FORCE_TOL, i
