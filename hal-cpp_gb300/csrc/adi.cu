@@ -334,7 +334,45 @@ namespace halcuda
 
         // One CTA's tile of a sweep: lines x0 .. x0+R-1 of the grid p.  tmap
         // is the grid's line tensor map (SWZ) or null.
-        template <int MODE, bool SWZ>
+        // Agent counts of write-out unit u: nc[e][i] = agents binned in cell
+        // (line0 + e, 4u + i), i.e. offsets[c + 1] - offsets[c] at c = (line0
+        // + e) * L + 4u + i (cells in layout A); 0 for the quad's lines at or
+        // past quadLines (outside the grid).  With L % 4 == 0 each line's five
+        // offsets are one 16-byte load and one 4-byte load.
+        __device__ __forceinline__ void UnitCounts(const int32_t *__restrict__ off, int32_t line0, int32_t quadLines,
+                                                   int32_t u, int32_t L, bool vecL, int32_t (&nc)[4][4])
+        {
+#pragma unroll
+            for (int e = 0; e < 4; e++)
+            {
+                const int32_t *oc = off + static_cast<int64_t>(line0 + e) * L + 4 * u;
+                if (e >= quadLines)
+                {
+                    nc[e][0] = nc[e][1] = nc[e][2] = nc[e][3] = 0;
+                }
+                else if (vecL)
+                {
+                    const int4 a = __ldg(reinterpret_cast<const int4 *>(oc));
+                    const int32_t b = __ldg(oc + 4);
+                    nc[e][0] = a.y - a.x;
+                    nc[e][1] = a.z - a.y;
+                    nc[e][2] = a.w - a.z;
+                    nc[e][3] = b - a.w;
+                }
+                else
+                {
+#pragma unroll
+                    for (int i = 0; i < 4; i++)
+                    {
+                        nc[e][i] = (4 * u + i < L) ? __ldg(oc + i + 1) - __ldg(oc + i) : 0;
+                    }
+                }
+            }
+        }
+
+        // UPT: the y-sweep's commit has the agent uptake term (a separate
+        // instantiation, so that the uncoupled tick keeps its registers).
+        template <int MODE, bool SWZ, bool UPT = false>
         __device__ __forceinline__ void SweepTile(const SweepParams &p, const CUtensorMap *tmap, const int32_t x0)
         {
             extern __shared__ __align__(1024) float smem[];
@@ -894,11 +932,10 @@ namespace halcuda
                 {
                     // 16-byte units: 4 positions x 4 lines move as a 4x4 block
                     // (4 LDS.128, a register transpose, 4 STG.128).  UPT: the
-                    // commit has an uptake term (agents coupled); without it
-                    // the commit skips the count loads and that product.
-                    auto writeVec = [&](auto uptTag) {
-                        constexpr bool UPT = decltype(uptTag)::value;
-                        (void)UPT;
+                    // commit has an uptake term (agents coupled), with the
+                    // unit's counts loaded line by line (UnitCounts); without
+                    // it the commit skips the count loads and that product.
+                    auto writeVec = [&]() {
                         const bool hasSrc = (p.src != nullptr);
                         (void)hasSrc;  // read by the commit of MODE kSweepTick only
                         // unit u of solution line 4qd+e sits at
@@ -971,22 +1008,20 @@ namespace halcuda
                                     continue;
                                 }
                                 float *out = p.out + static_cast<int64_t>(4 * u) * nl + line0;
+                                // per-agent uptake counts of the unit's 4 lines x 4 positions
+                                int32_t nc[4][4] = {};
+                                (void)nc;  // read by the commit of MODE kSweepTick only
+                                if constexpr (UPT)
+                                {
+                                    UnitCounts(p.cellOffsets, line0, quadLines, u, L, vecL, nc);
+                                }
 #pragma unroll
                                 for (int i = 0; i < 4; i++)
                                 {
                                     float4 w4 = o[b][i];
                                     if constexpr (MODE == kSweepTick)
                                     {
-                                        // per-agent uptake counts of the 4 lines at position 4u+i
-                                        int32_t n0 = 0, n1 = 0, n2 = 0, n3 = 0;
-                                        if constexpr (UPT)
-                                        {
-                                            const int64_t ci = static_cast<int64_t>(line0) * L + 4 * u + i;
-                                            n0 = __ldg(p.cellOffsets + ci + 1) - __ldg(p.cellOffsets + ci);
-                                            n1 = __ldg(p.cellOffsets + ci + L + 1) - __ldg(p.cellOffsets + ci + L);
-                                            n2 = __ldg(p.cellOffsets + ci + 2 * L + 1) - __ldg(p.cellOffsets + ci + 2 * L);
-                                            n3 = __ldg(p.cellOffsets + ci + 3 * L + 1) - __ldg(p.cellOffsets + ci + 3 * L);
-                                        }
+                                        const int32_t n0 = nc[0][i], n1 = nc[1][i], n2 = nc[2][i], n3 = nc[3][i];
                                         // f' = f + ((v - f) - decay f + src - uptake n f)
                                         auto commit = [&](float vv, float f0, float s0, int32_t nv) {
                                             float d = vv - f0;
@@ -1051,18 +1086,15 @@ namespace halcuda
                                                          make_float4(a[0].z, a[1].z, a[2].z, a[3].z),
                                                          make_float4(a[0].w, a[1].w, a[2].w, a[3].w)};
                                     float *out = p.out + static_cast<int64_t>(4 * u) * nl + line0;
+                                    int32_t nc[4][4] = {};
+                                    if constexpr (UPT)
+                                    {
+                                        UnitCounts(p.cellOffsets, line0, quadLines, u, L, vecL, nc);
+                                    }
 #pragma unroll
                                     for (int i = 0; i < 4; i++)
                                     {
-                                        int32_t n0 = 0, n1 = 0, n2 = 0, n3 = 0;
-                                        if constexpr (UPT)
-                                        {
-                                            const int64_t ci = static_cast<int64_t>(line0) * L + 4 * u + i;
-                                            n0 = __ldg(p.cellOffsets + ci + 1) - __ldg(p.cellOffsets + ci);
-                                            n1 = __ldg(p.cellOffsets + ci + L + 1) - __ldg(p.cellOffsets + ci + L);
-                                            n2 = __ldg(p.cellOffsets + ci + 2 * L + 1) - __ldg(p.cellOffsets + ci + 2 * L);
-                                            n3 = __ldg(p.cellOffsets + ci + 3 * L + 1) - __ldg(p.cellOffsets + ci + 3 * L);
-                                        }
+                                        const int32_t n0 = nc[0][i], n1 = nc[1][i], n2 = nc[2][i], n3 = nc[3][i];
                                         auto commit = [&](float vv, float f0, float s0, int32_t nv) {
                                             float d = vv - f0;
                                             d = fmaf(f0, p.negDecay, d);
@@ -1105,14 +1137,7 @@ namespace halcuda
                             block(u0, std::false_type{});
                         }
                     };
-                    if (MODE == kSweepTick && p.cellOffsets != nullptr)
-                    {
-                        writeVec(std::true_type{});
-                    }
-                    else
-                    {
-                        writeVec(std::false_type{});
-                    }
+                    writeVec();
                     return;
                 }
                 constexpr int kBatch = 2;
@@ -1218,11 +1243,11 @@ namespace halcuda
             }
         }
 
-        template <int MODE, bool SWZ>
+        template <int MODE, bool SWZ, bool UPT = false>
         __global__ void __launch_bounds__(kMaxThreads)
             AdiSweep(SweepParams p, const __grid_constant__ CUtensorMap tmap)
         {
-            SweepTile<MODE, SWZ>(p, &tmap, static_cast<int32_t>(blockIdx.x) * p.R);
+            SweepTile<MODE, SWZ, UPT>(p, &tmap, static_cast<int32_t>(blockIdx.x) * p.R);
         }
 
         // Batched form: CTA b runs tile tiles[b] = (grid, first line) of the
@@ -1344,18 +1369,24 @@ namespace halcuda
             return s;
         }
 
-        template <int MODE, bool SWZ>
+        template <int MODE, bool SWZ, bool UPT = false>
         int EnableSweepSmem(size_t bytes)
         {
             static SmemLimit s_limit;
-            return s_limit.Ensure(AdiSweep<MODE, SWZ>, bytes, "cudaFuncSetAttribute(AdiSweep)");
+            return s_limit.Ensure(AdiSweep<MODE, SWZ, UPT>, bytes, "cudaFuncSetAttribute(AdiSweep)");
         }
 
         template <int MODE>
         int EnableSweepSmemBoth(int32_t P, int32_t Nlines)
         {
             HAL_TRY((EnableSweepSmem<MODE, true>(ShapeFor(P, Nlines, true).smem)));
-            return EnableSweepSmem<MODE, false>(ShapeFor(P, Nlines, false).smem);
+            HAL_TRY((EnableSweepSmem<MODE, false>(ShapeFor(P, Nlines, false).smem)));
+            if constexpr (MODE == kSweepTick)
+            {
+                HAL_TRY((EnableSweepSmem<MODE, true, true>(ShapeFor(P, Nlines, true).smem)));
+                HAL_TRY((EnableSweepSmem<MODE, false, true>(ShapeFor(P, Nlines, false).smem)));
+            }
+            return HAL_CUDA_OK;
         }
 
         // cuTensorMapEncodeTiled through the runtime's driver entry point.
@@ -1690,17 +1721,36 @@ namespace halcuda
             p.R = sh.R;
             p.LS = sh.LS;
             unsigned blocks = static_cast<unsigned>((p.Nlines + sh.R - 1) / sh.R);
-            if (swz)
+            auto launch = [&](auto uptTag) -> int {
+                constexpr bool UPT = decltype(uptTag)::value;
+                if (swz)
+                {
+                    HAL_TRY((EnableSweepSmem<MODE, true, UPT>(sh.smem)));
+                    AdiSweep<MODE, true, UPT><<<blocks, sh.threads, sh.smem, s>>>(p, *tmap);
+                }
+                else
+                {
+                    CUtensorMap none;
+                    std::memset(&none, 0, sizeof(none));
+                    HAL_TRY((EnableSweepSmem<MODE, false, UPT>(sh.smem)));
+                    AdiSweep<MODE, false, UPT><<<blocks, sh.threads, sh.smem, s>>>(p, none);
+                }
+                return HAL_CUDA_OK;
+            };
+            if constexpr (MODE == kSweepTick)
             {
-                HAL_TRY((EnableSweepSmem<MODE, true>(sh.smem)));
-                AdiSweep<MODE, true><<<blocks, sh.threads, sh.smem, s>>>(p, *tmap);
+                if (p.cellOffsets != nullptr)
+                {
+                    HAL_TRY(launch(std::true_type{}));
+                }
+                else
+                {
+                    HAL_TRY(launch(std::false_type{}));
+                }
             }
             else
             {
-                CUtensorMap none;
-                std::memset(&none, 0, sizeof(none));
-                HAL_TRY((EnableSweepSmem<MODE, false>(sh.smem)));
-                AdiSweep<MODE, false><<<blocks, sh.threads, sh.smem, s>>>(p, none);
+                HAL_TRY(launch(std::false_type{}));
             }
             CountLaunch();
             return LaunchStatus("AdiSweep launch");
