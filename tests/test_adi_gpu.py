@@ -203,6 +203,37 @@ def test_ragged_last_tile_tick_against_oracle(hal, oracle, wrapX, wrapY, dirichl
     assert rel_l2(last, exp.reshape(xd, yd)[:, 1936:]) <= 1e-5
 
 
+@pytest.mark.parametrize("xd,yd,wrapX,wrapY,dirichlet", [
+    (2048, 2048, False, False, True),   # both sweeps tensor-staged: ghost lines, implicit ends
+    (2048, 2048, True, False, False),   # periodic x-lines, wrapped cross lines of the y-sweep
+    (2048, 1920, False, True, False),   # wrapped cross lines of the x-sweep, 120 tiles
+    (1024, 4096, False, False, True),   # x-lines of 1024 over 4096 lines
+    (4096, 1024, True, False, False),   # y-lines of 1024 over 4096 lines, wrapped cross lines
+])
+def test_large_tensor_staged_grids_against_oracle(hal, oracle, xd, yd, wrapX, wrapY, dirichlet):
+    """Full-size grids whose sweeps run the tensor-staged tiles over many
+    CTAs: every boundary kind of the cross axis, Dirichlet ends, decay and a
+    dense source, against the FP64 oracle."""
+    rng = np.random.default_rng(xd + 13 * yd + 7 * wrapX)
+    n = xd * yd
+    f0 = rng.random(n).astype(np.float32)
+    src = (rng.random(n) * 1e-3).astype(np.float32)
+    ghost = rng.random(2 * (xd + yd)).astype(np.float32) if dirichlet else None
+    r, decay, ticks = 5.0, 1e-2, 3
+    with hal.Adi(xd, yd) as a:
+        a.set_field(f0)
+        a.set_source(src)
+        if ghost is not None:
+            a.set_dirichlet(ghost)
+        a.run_ticks(ticks, r, decay, wrapX, wrapY)
+        out = a.get_field()
+    exp = oracle.run_ticks(1, f0.astype(np.float64), xd, yd, r, wrapX, wrapY,
+                           None if ghost is None else ghost.astype(np.float64), decay,
+                           src_dense=src.astype(np.float64), ticks=ticks, threads=16)
+    assert rel_l2(out, exp) <= 1e-5, rel_l2(out, exp)
+    assert max_rel(out, exp) <= 2e-6 * (1 + r) * ticks, max_rel(out, exp)
+
+
 LINES = [1, 2, 3, 31, 32, 33, 63, 64, 65, 100, 257, 1000, 2048, 4096]
 
 
