@@ -915,13 +915,18 @@ namespace halcuda
         // Forces of the resident step with the move fused in: the slot's
         // agent adds its delta to its velocity and moves.  Positions are read
         // from the cell-sorted copy, so writing the agent-order positions
-        // here races with no other thread.
+        // here races with no other thread.  With counts set, the moved agent
+        // is also counted into its new cell, BinCount's work for the next
+        // tick (cell, arrival rank): this tick's scan cleared the counts, and
+        // its scatter has read the previous cells and ranks.
         template <int LAW = kLawLinear, bool SUM = false>
         __global__ void ForcesMove(const int32_t *__restrict__ bucket, const int32_t *__restrict__ offsets,
                                    const float2 *__restrict__ sPos, const float *__restrict__ sRad, int32_t n,
                                    double interactionRad, float R, LawParams<float> lp, int32_t xDim, int32_t yDim,
                                    MoveParams mp, float *__restrict__ deltas, float2 *__restrict__ pos,
-                                   float2 *__restrict__ velocity, float *__restrict__ sums)
+                                   float2 *__restrict__ velocity, float *__restrict__ sums,
+                                   int32_t *__restrict__ cellOf, int32_t *__restrict__ arrival,
+                                   int32_t *__restrict__ counts)
         {
             ChainEntry();
             const int32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
@@ -945,6 +950,12 @@ namespace halcuda
             MoveAgent(mp, p, v);
             pos[i] = p;
             velocity[i] = v;
+            if (counts != nullptr)
+            {
+                const int32_t c = CellCoord(p.x, xDim) * yDim + CellCoord(p.y, yDim);
+                cellOf[i] = c;
+                arrival[i] = atomicAdd(counts + c, 1);
+            }
         }
 
         // ---- many independent wells in one pass ------------------------------
@@ -1247,6 +1258,21 @@ namespace halcuda
         bool sumsValid = false;  // sums32 holds the last dispatch's or step's sums
         int32_t nTiles = 0;
         bool countsDirty = true;  // counts not known to be zero (cleared by each scan)
+        // counts, cellOf and arrival hold the binning of the current pos32,
+        // counted by the last resident step's force kernel as it moved the
+        // agents: the next FP32 binning skips its count pass
+        bool binsPrecounted = false;
+
+        // pos32 changed by other means than the resident step: the precounted
+        // bins are stale and the counts must be cleared before a binning
+        void DropPrecount()
+        {
+            if (binsPrecounted)
+            {
+                binsPrecounted = false;
+                countsDirty = true;
+            }
+        }
 
         int Init(int32_t x, int32_t y, int32_t maxN)
         {
@@ -1288,7 +1314,14 @@ namespace halcuda
         template <typename TP, typename TR>
         int Bin(const TP *pos, const TR *rad, TR *sRad, cudaStream_t s, cudaEvent_t *ev = nullptr)
         {
-            if (countsDirty)
+            // the resident step's force kernel already counted these positions
+            const bool pre = binsPrecounted && static_cast<const void *>(pos) == static_cast<const void *>(pos32.p);
+            if (!pre)
+            {
+                DropPrecount();
+            }
+            binsPrecounted = false;
+            if (countsDirty && !pre)
             {
                 // a previous binning stopped before its scan cleared the counts
                 HAL_TRY(CudaStatus(cudaMemsetAsync(counts.p, 0, static_cast<size_t>(C) * sizeof(int32_t), s),
@@ -1297,7 +1330,7 @@ namespace halcuda
             countsDirty = true;
             const int T = 256;
             unsigned ablocks = static_cast<unsigned>((n + T - 1) / T);
-            if (n > 0)
+            if (n > 0 && !pre)
             {
                 LaunchChained(BinCount<TP>, ablocks, T, s, pos, n, xDim, yDim, static_cast<V2<TP> *>(nullptr),
                               cellOf.p, arrival.p, counts.p);
@@ -1436,10 +1469,13 @@ namespace
         LawParams<float> lp;
         lp.scale = static_cast<float>(law.scale);
         lp.exponent = static_cast<float>(law.exponent);
+        // the force kernel counts the moved agents into their new cells (the
+        // next binning's count pass); this binning's scan cleared the counts
         auto go = [&](auto kernel) {
             LaunchChained(kernel, blocks, T, s, a.bucket.p, a.offsets.p, a.sPos.p, a.sRad32.p, a.n, R,
                           static_cast<float>(R), lp, a.xDim, a.yDim, mp, a.vel32.p,
-                          reinterpret_cast<float2 *>(a.pos32.p), a.velState.p, sums);
+                          reinterpret_cast<float2 *>(a.pos32.p), a.velState.p, sums, a.cellOf.p, a.arrival.p,
+                          a.counts.p);
         };
         switch (law.kind * 2 + (law.sums ? 1 : 0))
         {
@@ -1451,7 +1487,10 @@ namespace
         default: go(ForcesMove<kLawPower, true>); break;
         }
         CountLaunch();
-        return LaunchStatus("agent forces and move");
+        const int rc = LaunchStatus("agent forces and move");
+        a.binsPrecounted = (rc == HAL_CUDA_OK);
+        a.countsDirty = (rc != HAL_CUDA_OK);
+        return rc;
     }
 }
 
@@ -1677,6 +1716,7 @@ extern "C" int hal_cuda_agents_upload(hal_cuda_agents *h, const float *positions
     using namespace halcuda;
     HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
     cudaStream_t s = h->stream.Get();
+    h->DropPrecount();
     h->n = n;
     if (n > 0)
     {
