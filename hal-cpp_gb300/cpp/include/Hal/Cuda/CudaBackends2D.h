@@ -152,6 +152,12 @@ namespace Hal::Cuda
         void SetSource(const std::vector<float> &dense);
         void SetDirichlet(const std::vector<float> &ghost);
         void SetUptake(CudaAgentForceBackend2D *pAgents, double uptake);
+        // `ticks` coupled ticks (the agents' resident step, then this field's
+        // tick with their uptake) as one graph; agents must be the coupled
+        // backend (SetUptake).  Equal to alternating agents.Step(1, ...) and
+        // RunTicks(1, ...).
+        void RunCoupled(CudaAgentForceBackend2D &agents, int32_t ticks, double diffRate, double decay, bool wrapX,
+                        bool wrapY, double interactionRad, double springConstant, double friction, double maxVel);
         void RunTicks(int32_t ticks, double diffRate, double decay, bool wrapX, bool wrapY);
         void Sync();
 

@@ -264,6 +264,15 @@ namespace Hal::Cuda
               "CudaAdiDiffusionBackend2D::SetUptake");
     }
 
+    void CudaAdiDiffusionBackend2D::RunCoupled(CudaAgentForceBackend2D &agents, int32_t ticks, double diffRate,
+                                               double decay, bool wrapX, bool wrapY, double interactionRad,
+                                               double springConstant, double friction, double maxVel)
+    {
+        Check(hal_cuda_adi_run_coupled(m_pHandle, agents.Handle(), ticks, diffRate, decay, wrapX ? 1 : 0,
+                                       wrapY ? 1 : 0, interactionRad, springConstant, friction, maxVel),
+              "CudaAdiDiffusionBackend2D::RunCoupled");
+    }
+
     void CudaAdiDiffusionBackend2D::RunTicks(int32_t ticks, double diffRate, double decay, bool wrapX, bool wrapY)
     {
         Check(hal_cuda_adi_run_ticks(m_pHandle, ticks, diffRate, decay, wrapX, wrapY),

@@ -1604,6 +1604,8 @@ namespace halcuda
         double uptake = 0.0;
         std::map<std::string, std::unique_ptr<LinePlanBuf>> plans;
         GraphCache graph[2];  // by the parity of the starting buffer
+        GraphCache coupled[2];          // coupled agent + ADI ticks, by parity
+        int64_t coupledLaunches[2] = {0, 0};  // kernel launches per replay
         // TMA tensor maps of the staged lines: x-sweep input field[0] /
         // field[1] (lines along x), y-sweep input w (lines along y)
         CUtensorMap tmapX[2];
@@ -1614,6 +1616,8 @@ namespace halcuda
         {
             graph[0].Reset();
             graph[1].Reset();
+            coupled[0].Reset();
+            coupled[1].Reset();
         }
 
         int Init(int32_t x, int32_t y)
@@ -1903,6 +1907,76 @@ namespace halcuda
             return HAL_CUDA_OK;
         }
 
+        // `ticks` coupled ticks on the handle's stream, each the agents'
+        // resident step (bins, forces, move) and then the ADI tick whose
+        // commit takes up the field per agent of those bins; replayed from a
+        // CUDA graph cached per buffer parity.  Every replay starts from the
+        // agents' precounted bins (CoupledStepBegin) and leaves them so.
+        int RunCoupled(hal_cuda_agents *ag, int32_t ticks, double r, double decay, bool wrapX, bool wrapY,
+                       const CoupledStep &st)
+        {
+            HAL_TRY(Usable("ADI coupled ticks"));
+            if (ticks <= 0)
+            {
+                return HAL_CUDA_OK;
+            }
+            cudaStream_t s = stream.Get();
+            const float *g = hasGhost ? ghost.p : nullptr;
+            HAL_TRY(PrepareShapes(r, wrapX, wrapY, g));
+            HAL_TRY(CoupledStepBegin(ag, st, s));
+            char key[384];
+            snprintf(key, sizeof(key), "%d|%a|%a|%d|%d|%d|%d|%p|%p|%a|%d|%a|%a|%a|%a", ticks, r, decay, wrapX, wrapY,
+                     hasSrc, hasGhost, static_cast<void *>(s), static_cast<const void *>(ag), uptake,
+                     CoupledAgentCount(ag), st.interactionRad, st.springConstant, st.friction, st.maxVel);
+            GraphCache &gc = coupled[cur];
+            if (gc.exec == nullptr || gc.key != key)
+            {
+                gc.Reset();
+                const int64_t l0 = g_launches.load();
+                cudaGraph_t gr = nullptr;
+                HAL_TRY(CudaStatus(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal),
+                                   "cudaStreamBeginCapture"));
+                int c = cur;
+                int rc = HAL_CUDA_OK;
+                for (int32_t t = 0; t < ticks && rc == HAL_CUDA_OK; t++)
+                {
+                    rc = CoupledStepOnce(ag, st, wrapX, wrapY, s);
+                    if (rc == HAL_CUDA_OK)
+                    {
+                        rc = EnqueueTick(c, r, decay, wrapX, wrapY, false, s);
+                    }
+                    c ^= 1;
+                }
+                cudaError_t e = cudaStreamEndCapture(s, &gr);
+                if (rc == HAL_CUDA_OK && !CoupledBinsPrecounted(ag))
+                {
+                    SetError("hal_cuda_adi_run_coupled: the agent steps did not leave their bins counted");
+                    rc = HAL_CUDA_EDEVICE;
+                }
+                if (rc != HAL_CUDA_OK)
+                {
+                    if (gr != nullptr)
+                    {
+                        cudaGraphDestroy(gr);
+                    }
+                    return rc;
+                }
+                HAL_TRY(CudaStatus(e, "cudaStreamEndCapture"));
+                e = cudaGraphInstantiate(&gc.exec, gr, 0);
+                cudaGraphDestroy(gr);
+                HAL_TRY(CudaStatus(e, "cudaGraphInstantiate"));
+                gc.key = key;
+                coupledLaunches[cur] = g_launches.load() - l0;  // counted at capture for this first launch
+            }
+            else
+            {
+                CountLaunch(coupledLaunches[cur]);
+            }
+            HAL_TRY(CudaStatus(cudaGraphLaunch(gc.exec, s), "cudaGraphLaunch"));
+            cur ^= (ticks & 1);
+            return CoupledStepEnd(ag, s);
+        }
+
         // Host field (layout A) -> field[cur] (layout B).
         int Upload(const float *host, cudaStream_t s)
         {
@@ -2161,6 +2235,23 @@ extern "C" int hal_cuda_adi_run_ticks(hal_cuda_adi *h, int32_t ticks, double dif
     HAL_REQUIRE(ticks >= 0, "hal_cuda_adi_run_ticks: negative tick count");
     HAL_TRY(halcuda::CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
     return h->RunTicks(ticks, diffRate, decay, wrapX != 0, wrapY != 0, false);
+}
+
+extern "C" int hal_cuda_adi_run_coupled(hal_cuda_adi *h, hal_cuda_agents *agents, int32_t ticks, double diffRate,
+                                        double decay, int32_t wrapX, int32_t wrapY, double interactionRad,
+                                        double springConstant, double friction, double maxVel)
+{
+    HAL_REQUIRE(h != nullptr && agents != nullptr, "hal_cuda_adi_run_coupled: handle is NULL");
+    HAL_REQUIRE(ticks >= 0, "hal_cuda_adi_run_coupled: negative tick count");
+    HAL_REQUIRE(h->agents == agents,
+                "hal_cuda_adi_run_coupled: the agent handle is not the one coupled by hal_cuda_adi_set_uptake");
+    HAL_TRY(halcuda::CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+    halcuda::CoupledStep st;
+    st.interactionRad = interactionRad;
+    st.springConstant = springConstant;
+    st.friction = friction;
+    st.maxVel = maxVel;
+    return h->RunCoupled(agents, ticks, diffRate, decay, wrapX != 0, wrapY != 0, st);
 }
 
 extern "C" int hal_cuda_adi_run_steps(hal_cuda_adi *h, float *field, int64_t len, int32_t steps, double diffRate,

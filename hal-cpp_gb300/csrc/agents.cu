@@ -1769,6 +1769,97 @@ extern "C" int hal_cuda_agents_get_state(hal_cuda_agents *h, float *positions, f
     return CudaStatus(cudaStreamSynchronize(s), "hal_cuda_agents_get_state");
 }
 
+namespace halcuda
+{
+    // ---- resident steps inside another handle's run (hal_cuda_adi_run_coupled)
+
+    int CoupledStepBegin(hal_cuda_agents *h, const CoupledStep &st, cudaStream_t s)
+    {
+        HAL_REQUIRE(h != nullptr, "hal_cuda_adi_run_coupled: agent handle is NULL");
+        HAL_REQUIRE(RadiusOk(st.interactionRad), "hal_cuda_adi_run_coupled: interactionRad %g outside [0, %g]",
+                    st.interactionRad, kMaxInteractionRad);
+        HAL_REQUIRE(std::isfinite(st.springConstant), "hal_cuda_adi_run_coupled: springConstant must be finite");
+        HAL_REQUIRE(std::isfinite(st.friction), "hal_cuda_adi_run_coupled: friction must be finite");
+        HAL_REQUIRE(!std::isnan(st.maxVel), "hal_cuda_adi_run_coupled: maxVel is NaN");
+        HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+        // the agent handle's own queued work comes first
+        cudaStream_t own = h->stream.Get();
+        if (own != s)
+        {
+            cudaEvent_t ev = nullptr;
+            HAL_TRY(CudaStatus(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate"));
+            cudaError_t e = cudaEventRecord(ev, own);
+            if (e == cudaSuccess)
+            {
+                e = cudaStreamWaitEvent(s, ev, 0);
+            }
+            cudaEventDestroy(ev);
+            HAL_TRY(CudaStatus(e, "hal_cuda_adi_run_coupled: stream order"));
+        }
+        // every replayed tick starts from counts that hold the current
+        // positions' binning (the previous tick's force kernel counted them)
+        if (!h->binsPrecounted && h->n > 0)
+        {
+            if (h->countsDirty)
+            {
+                HAL_TRY(CudaStatus(cudaMemsetAsync(h->counts.p, 0, static_cast<size_t>(h->C) * sizeof(int32_t), s),
+                                   "cudaMemsetAsync(counts)"));
+            }
+            const int T = 256;
+            BinCount<float><<<static_cast<unsigned>((h->n + T - 1) / T), T, 0, s>>>(
+                h->pos32.p, h->n, h->xDim, h->yDim, static_cast<float2 *>(nullptr), h->cellOf.p, h->arrival.p,
+                h->counts.p);
+            CountLaunch();
+            HAL_TRY(LaunchStatus("agent binning"));
+            h->binsPrecounted = true;
+            h->countsDirty = false;
+        }
+        h->sumsValid = false;
+        return HAL_CUDA_OK;
+    }
+
+    int CoupledStepOnce(hal_cuda_agents *h, const CoupledStep &st, int32_t wrapX, int32_t wrapY, cudaStream_t s)
+    {
+        MoveParams mp;
+        mp.friction = static_cast<float>(st.friction);
+        mp.maxVel = (st.maxVel < 0 || std::isinf(st.maxVel)) ? -1.0f : static_cast<float>(st.maxVel);
+        mp.xDimF = static_cast<float>(h->xDim);
+        mp.yDimF = static_cast<float>(h->yDim);
+        mp.wrapX = wrapX != 0;
+        mp.wrapY = wrapY != 0;
+        return StepOnce(*h, st.interactionRad, ForceLawSpec::Linear(st.springConstant), mp, s);
+    }
+
+    int CoupledStepEnd(hal_cuda_agents *h, cudaStream_t s)
+    {
+        // the agent handle's later work waits for the run
+        cudaStream_t own = h->stream.Get();
+        if (own == s)
+        {
+            return HAL_CUDA_OK;
+        }
+        cudaEvent_t ev = nullptr;
+        HAL_TRY(CudaStatus(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate"));
+        cudaError_t e = cudaEventRecord(ev, s);
+        if (e == cudaSuccess)
+        {
+            e = cudaStreamWaitEvent(own, ev, 0);
+        }
+        cudaEventDestroy(ev);
+        return CudaStatus(e, "hal_cuda_adi_run_coupled: stream order");
+    }
+
+    int32_t CoupledAgentCount(const hal_cuda_agents *h)
+    {
+        return h->n;
+    }
+
+    bool CoupledBinsPrecounted(const hal_cuda_agents *h)
+    {
+        return h->binsPrecounted;
+    }
+}
+
 namespace
 {
     int StepCommon(hal_cuda_agents *h, int32_t ticks, double interactionRad, const halcuda::ForceLawSpec &law,

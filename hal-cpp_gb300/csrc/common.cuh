@@ -38,6 +38,21 @@ namespace halcuda
     // its grid: the agent count of cell i is offsets[i + 1] - offsets[i].
     const int32_t *AgentsCellOffsets(const hal_cuda_agents *a, int32_t *xDim, int32_t *yDim);
 
+    // Resident agent steps enqueued by another handle on its stream (agents.cu;
+    // hal_cuda_adi_run_coupled): Begin orders the agent handle's queued work
+    // first and counts the current positions when the last step did not;
+    // StepOnce is one hal_cuda_agents_step tick with the linear law; End
+    // orders the agent handle's later work after the run.
+    struct CoupledStep
+    {
+        double interactionRad, springConstant, friction, maxVel;
+    };
+    int CoupledStepBegin(hal_cuda_agents *a, const CoupledStep &st, cudaStream_t s);
+    int CoupledStepOnce(hal_cuda_agents *a, const CoupledStep &st, int32_t wrapX, int32_t wrapY, cudaStream_t s);
+    int CoupledStepEnd(hal_cuda_agents *a, cudaStream_t s);
+    int32_t CoupledAgentCount(const hal_cuda_agents *a);
+    bool CoupledBinsPrecounted(const hal_cuda_agents *a);
+
     // Maps a CUDA error to a status, recording the message.
     inline int CudaStatus(cudaError_t e, const char *what)
     {

@@ -74,6 +74,7 @@ SIGNATURES = {
     "hal_cuda_adi_set_uptake": (_I, [_vp, _vp, _f64]),
     "hal_cuda_diffusion_set_uptake": (_I, [_vp, _vp, _f64]),
     "hal_cuda_adi_run_ticks": (_I, [_vp, _i32, _f64, _f64, _i32, _i32]),
+    "hal_cuda_adi_run_coupled": (_I, [_vp, _vp, _i32, _f64, _f64, _i32, _i32, _f64, _f64, _f64, _f64]),
     "hal_cuda_adi_run_steps": (_I, [_vp, _vp, _i64, _i32, _f64, _i32, _i32]),
     "hal_cuda_adi_run_ticks_host": (_I, [_vp, _vp, _vp, _i64, _i32, _f64, _f64, _i32, _i32]),
     "hal_cuda_adi_profile_graph": (_I, [_vp, _i32, _f64, _f64, _i32, _i32, _vp]),
@@ -504,6 +505,13 @@ class Adi(_Handle):
     def run_ticks(self, ticks, diffRate, decay=0.0, wrapX=False, wrapY=False):
         _check(lib().hal_cuda_adi_run_ticks(self._h, ticks, diffRate, decay, int(wrapX),
                                             int(wrapY)), "run_ticks")
+
+    def run_coupled(self, agents, ticks, diffRate, decay=0.0, wrapX=False, wrapY=False, interactionRad=1.0,
+                    springConstant=0.1, friction=1.0, maxVel=-1.0):
+        """`ticks` ticks of agents.step(1, ...) then run_ticks(1, ...), as one
+        graph on this handle's stream (agents coupled by set_uptake)."""
+        _check(lib().hal_cuda_adi_run_coupled(self._h, agents.handle, ticks, diffRate, decay, int(wrapX), int(wrapY),
+                                              interactionRad, springConstant, friction, maxVel), "run_coupled")
 
     def run_steps(self, field, steps, diffRate, wrapX=False, wrapY=False):
         f = np.array(field, dtype=np.float32, copy=True)

@@ -241,6 +241,20 @@ int hal_cuda_adi_set_uptake(hal_cuda_adi *h, hal_cuda_agents *agents, double upt
 int hal_cuda_adi_run_ticks(hal_cuda_adi *h, int32_t ticks, double diffRate, double decay,
                            int32_t wrapX, int32_t wrapY);
 
+/* `ticks` coupled ticks of a model like examples/CompetitiveRelease.cpp:
+ * each tick is one resident step of `agents` (hal_cuda_agents_step with the
+ * linear law: bins, forces, SphericalAgent2D's move) followed by one
+ * hal_cuda_adi_run_ticks tick whose commit takes up -uptake*count*f with
+ * the counts of that step's bins.  `agents` must be the handle coupled by
+ * hal_cuda_adi_set_uptake (same grid); its axes wrap as the field's.  The
+ * results equal alternating hal_cuda_agents_step(agents, 1, ...) and
+ * hal_cuda_adi_run_ticks(h, 1, ...) calls bit for bit; here the ticks run
+ * on the ADI handle's stream as one cached CUDA graph, ordered after the
+ * agent handle's queued work and before its later work.  Asynchronous. */
+int hal_cuda_adi_run_coupled(hal_cuda_adi *h, hal_cuda_agents *agents, int32_t ticks, double diffRate,
+                             double decay, int32_t wrapX, int32_t wrapY, double interactionRad,
+                             double springConstant, double friction, double maxVel);
+
 /* AdiKernel2D::RunSteps(field, steps, diffRate, wrapX, wrapY)
  * (src/Gpu/AdiKernel2D.cpp:296-364): upload, `steps` ADI steps, download. */
 int hal_cuda_adi_run_steps(hal_cuda_adi *h, float *field, int64_t len, int32_t steps,

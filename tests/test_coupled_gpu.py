@@ -77,3 +77,68 @@ def test_coupled_agents_and_adi_field_100_ticks(hal, oracle):
     assert moved, "the agents never moved"
     err = rel_l2(out, f64)
     assert err <= 1e-5, err
+
+
+@pytest.mark.parametrize("wrap", [(False, False), (True, False)])
+def test_run_coupled_equals_alternating_calls(hal, wrap):
+    """hal_cuda_adi_run_coupled (each tick: the agents' resident step, then the
+    ADI tick with their uptake, all ticks as one cached graph on the field's
+    stream) equals alternating agents.step(1) / run_ticks(1) calls bit for bit:
+    the field, the positions and the velocities, over runs of both buffer
+    parities and a cached-graph replay, with the agent handle on its own
+    stream; a dispatch after the run and a new upload are ordered after it."""
+    from halcuda import workloads
+
+    n_side, n_agents = 384, 40000
+    ag_in = workloads.agent_inputs(n_agents, n_side, seed=5)
+    fd_in = workloads.adi_inputs(n_side, seed=6, blobs=20)
+    pos0, rad = ag_in["positions"], ag_in["radii"]
+    f32 = fd_in["field"].astype(np.float32)
+    s32 = fd_in["src"].astype(np.float32)
+    wx, wy = wrap
+    runs = (3, 4, 3, 5)
+
+    def fresh(ag, a):
+        ag.upload(pos0, rad)
+        a.set_field(f32)
+        a.set_source(s32)
+        a.set_uptake(ag, UPTAKE)
+
+    with hal.Agents(n_side, n_side, n_agents) as ag, hal.Adi(n_side, n_side) as a:
+        ag.set_stream(a.stream())
+        fresh(ag, a)
+        for k in runs:
+            for _ in range(k):
+                ag.step(1, R, K, wx, wy, friction=FRICTION, maxVel=MAXVEL)
+                a.run_ticks(1, RATE, DECAY, wx, wy)
+        exp_f = a.get_field()
+        exp_p, exp_v = ag.get_state()
+        ag.dispatch(R, K, wx, wy)
+        exp_d = ag.download()
+        ag.set_stream(None)
+    with hal.Agents(n_side, n_side, n_agents) as ag, hal.Adi(n_side, n_side) as a:
+        fresh(ag, a)  # the agent handle keeps its own stream
+        for k in runs:
+            a.run_coupled(ag, k, RATE, DECAY, wx, wy, R, K, FRICTION, MAXVEL)
+        got_f = a.get_field()
+        got_p, got_v = ag.get_state()
+        ag.dispatch(R, K, wx, wy)
+        got_d = ag.download()
+        # an upload resets the agents: the next run bins them afresh
+        fresh(ag, a)
+        a.run_coupled(ag, 3, RATE, DECAY, wx, wy, R, K, FRICTION, MAXVEL)
+        again = a.get_field()
+        with pytest.raises(ValueError, match="coupled"):
+            with hal.Agents(n_side, n_side, 10) as other:
+                a.run_coupled(other, 1, RATE, DECAY, wx, wy, R, K, FRICTION, MAXVEL)
+    assert np.array_equal(got_f, exp_f)
+    assert np.array_equal(got_p, exp_p) and np.array_equal(got_v, exp_v)
+    assert np.array_equal(got_d, exp_d)
+    with hal.Agents(n_side, n_side, n_agents) as ag, hal.Adi(n_side, n_side) as a:
+        ag.set_stream(a.stream())
+        fresh(ag, a)
+        for _ in range(3):
+            ag.step(1, R, K, wx, wy, friction=FRICTION, maxVel=MAXVEL)
+            a.run_ticks(1, RATE, DECAY, wx, wy)
+        assert np.array_equal(again, a.get_field())
+        ag.set_stream(None)
