@@ -820,7 +820,10 @@ namespace halcuda
         // sum starts from the agent's velocity (SumForces adds to xVel/yVel),
         // otherwise from zero (the interface's velocity deltas); with SUM the
         // agent's sum of positive forces goes to sums.
-        template <typename T, typename TV, int LAW = kLawLinear, bool SUM = false, bool GRID = false>
+        // WALLS: neither axis wraps (a compile-time 0 for both wrap flags, so
+        // the displacement's wrap test leaves the per-candidate code).
+        template <typename T, typename TV, int LAW = kLawLinear, bool SUM = false, bool GRID = false,
+                  bool WALLS = false>
         __global__ void Forces(const int32_t *__restrict__ bucket, const int32_t *__restrict__ offsets,
                                const V2<T> *__restrict__ sPos, const T *__restrict__ sRad, int32_t n,
                                double interactionRad, T R, LawParams<T> lp, int32_t xDim, int32_t yDim,
@@ -840,7 +843,8 @@ namespace halcuda
                                    static_cast<T>(velIn[2 * static_cast<int64_t>(i) + 1]));
             }
             const ForceAcc<T> acc = ForceSlotLaw<T, LAW, SUM, GRID>(slot, offsets, sPos, sRad, interactionRad, R, lp,
-                                                                    xDim, yDim, wrapX, wrapY, v0);
+                                                                    xDim, yDim, WALLS ? 0 : wrapX, WALLS ? 0 : wrapY,
+                                                                    v0);
             StoreDelta(vel, i, acc.v);
             if constexpr (SUM)
             {
@@ -919,7 +923,7 @@ namespace halcuda
         // is also counted into its new cell, BinCount's work for the next
         // tick (cell, arrival rank): this tick's scan cleared the counts, and
         // its scatter has read the previous cells and ranks.
-        template <int LAW = kLawLinear, bool SUM = false>
+        template <int LAW = kLawLinear, bool SUM = false, bool WALLS = false>
         __global__ void ForcesMove(const int32_t *__restrict__ bucket, const int32_t *__restrict__ offsets,
                                    const float2 *__restrict__ sPos, const float *__restrict__ sRad, int32_t n,
                                    double interactionRad, float R, LawParams<float> lp, int32_t xDim, int32_t yDim,
@@ -936,7 +940,8 @@ namespace halcuda
             }
             const int32_t i = bucket[slot];
             const ForceAcc<float> acc = ForceSlotLaw<float, LAW, SUM, false>(
-                slot, offsets, sPos, sRad, interactionRad, R, lp, xDim, yDim, mp.wrapX, mp.wrapY, make_float2(0.f, 0.f));
+                slot, offsets, sPos, sRad, interactionRad, R, lp, xDim, yDim, WALLS ? 0 : mp.wrapX,
+                WALLS ? 0 : mp.wrapY, make_float2(0.f, 0.f));
             const V2<float> d = acc.v;
             StoreDelta(deltas, i, d);
             if constexpr (SUM)
@@ -1407,7 +1412,18 @@ namespace halcuda
             const bool grid = std::is_same<T, double>::value && law.grid;
             switch (law.kind * 4 + (law.sums ? 2 : 0) + (grid ? 1 : 0))
             {
-            case 0: go(Forces<T, TV, kLawLinear, false, false>); break;
+            case 0:
+                // the interface's law on a grid with walls: the wrap tests compiled out
+                if constexpr (std::is_same<T, float>::value)
+                {
+                    if (!wrapX && !wrapY)
+                    {
+                        go(Forces<T, TV, kLawLinear, false, false, true>);
+                        break;
+                    }
+                }
+                go(Forces<T, TV, kLawLinear, false, false>);
+                break;
             case 1: go(Forces<T, TV, kLawLinear, false, true>); break;
             case 2: go(Forces<T, TV, kLawLinear, true, false>); break;
             case 3: go(Forces<T, TV, kLawLinear, true, true>); break;
@@ -1479,7 +1495,16 @@ namespace
         };
         switch (law.kind * 2 + (law.sums ? 1 : 0))
         {
-        case 0: go(ForcesMove<kLawLinear, false>); break;
+        case 0:
+            if (!mp.wrapX && !mp.wrapY)
+            {
+                go(ForcesMove<kLawLinear, false, true>);  // walls: the wrap tests compiled out
+            }
+            else
+            {
+                go(ForcesMove<kLawLinear, false>);
+            }
+            break;
         case 1: go(ForcesMove<kLawLinear, true>); break;
         case 2: go(ForcesMove<kLawClamped, false>); break;
         case 3: go(ForcesMove<kLawClamped, true>); break;
