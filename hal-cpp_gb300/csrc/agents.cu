@@ -32,9 +32,14 @@ namespace halcuda
 {
     namespace
     {
-        constexpr int kScanThreads = 1024;
-        constexpr int kScanItems = 4;
+        // Scan tiles of 4096 cells: 256 threads, each with 16 cells in four
+        // 16-byte groups, so every thread has four loads in flight.
+        constexpr int kScanThreads = 256;
+        constexpr int kScanGroups = 4;
+        constexpr int kScanItems = 4 * kScanGroups;
         constexpr int kScanTile = kScanThreads * kScanItems;
+        // tiles whose prefix ScanApplySum forms itself (4.19M cells)
+        constexpr int kScanSumTiles = 1024;
 
         // Position pairs in the precision of the path: float2 on the FP32
         // resident path, double2 on the FP64 interface path.
@@ -171,18 +176,15 @@ namespace halcuda
         }
 
         // Pass 1 of the scan: per-tile sums.
-        // A thread's kScanItems consecutive cells [base, base + 4): one
-        // 16-byte access when the four are in range and aligned (each warp
-        // then touches every 32-byte sector once), element by element
-        // otherwise.
-        static_assert(kScanItems == 4, "the vector path moves 4 cells");
+        // Four consecutive cells [base, base + 4): one 16-byte access when the
+        // four are in range and aligned, element by element otherwise.
         __device__ __forceinline__ bool Vec4Ok(const int32_t *p, int64_t base, int64_t C)
         {
             return base + 4 <= C && ((reinterpret_cast<uintptr_t>(p + base) & 15u) == 0u);
         }
 
         __device__ __forceinline__ void LoadItems(const int32_t *__restrict__ p, int64_t base, int64_t C,
-                                                  int32_t (&v)[kScanItems])
+                                                  int32_t *v)
         {
             if (Vec4Ok(p, base, C))
             {
@@ -194,14 +196,13 @@ namespace halcuda
                 return;
             }
 #pragma unroll
-            for (int q = 0; q < kScanItems; q++)
+            for (int q = 0; q < 4; q++)
             {
                 v[q] = (base + q < C) ? p[base + q] : 0;
             }
         }
 
-        __device__ __forceinline__ void StoreItems(int32_t *__restrict__ p, int64_t base, int64_t C,
-                                                   const int32_t (&v)[kScanItems])
+        __device__ __forceinline__ void StoreItems(int32_t *__restrict__ p, int64_t base, int64_t C, const int32_t *v)
         {
             if (Vec4Ok(p, base, C))
             {
@@ -209,7 +210,7 @@ namespace halcuda
                 return;
             }
 #pragma unroll
-            for (int q = 0; q < kScanItems; q++)
+            for (int q = 0; q < 4; q++)
             {
                 if (base + q < C)
                 {
@@ -218,13 +219,19 @@ namespace halcuda
             }
         }
 
+        // The tile sum needs no order: group g of a thread is cells tile +
+        // g * 1024 + 4 * thread, so each warp's loads are contiguous.
         __global__ void __launch_bounds__(kScanThreads) ScanReduce(const int32_t *__restrict__ counts, int64_t C,
                                                                    int32_t *__restrict__ tileSums)
         {
             ChainEntry();
-            int64_t base = static_cast<int64_t>(blockIdx.x) * kScanTile + threadIdx.x * kScanItems;
+            const int64_t tile0 = static_cast<int64_t>(blockIdx.x) * kScanTile;
             int32_t v[kScanItems];
-            LoadItems(counts, base, C, v);
+#pragma unroll
+            for (int g = 0; g < kScanGroups; g++)
+            {
+                LoadItems(counts, tile0 + g * (4 * kScanThreads) + 4 * threadIdx.x, C, v + 4 * g);
+            }
             int32_t s = 0;
 #pragma unroll
             for (int q = 0; q < kScanItems; q++)
@@ -269,6 +276,52 @@ namespace halcuda
         // agents: agent pass 0.818 -> 0.772 ms).
         constexpr int64_t kClearInScanCells = int64_t(1) << 40;
 
+        // The cells of a thread of passes 3: kScanItems consecutive cells
+        // from tile + thread * kScanItems (in order, for the exclusive scan),
+        // loaded as four 16-byte groups.  With `clear` the groups holding a
+        // count are written back as zeros (most cells are empty, and an empty
+        // group is already cleared).
+        __device__ __forceinline__ void LoadThreadCells(int32_t *__restrict__ counts, int64_t base, int64_t C,
+                                                        bool clear, int32_t (&v)[kScanItems])
+        {
+#pragma unroll
+            for (int g = 0; g < kScanGroups; g++)
+            {
+                LoadItems(counts, base + 4 * g, C, v + 4 * g);
+            }
+            if (clear)
+            {
+#pragma unroll
+                for (int g = 0; g < kScanGroups; g++)
+                {
+                    if ((v[4 * g] | v[4 * g + 1] | v[4 * g + 2] | v[4 * g + 3]) != 0)
+                    {
+                        const int32_t zeros[4] = {0, 0, 0, 0};
+                        StoreItems(counts, base + 4 * g, C, zeros);
+                    }
+                }
+            }
+        }
+
+        // The thread's exclusive offsets from its first one, stored as four
+        // 16-byte groups.
+        __device__ __forceinline__ void StoreThreadOffsets(int32_t *__restrict__ offsets, int64_t base, int64_t C,
+                                                           int32_t first, const int32_t (&v)[kScanItems])
+        {
+            int32_t o[kScanItems];
+            o[0] = first;
+#pragma unroll
+            for (int q = 1; q < kScanItems; q++)
+            {
+                o[q] = o[q - 1] + v[q - 1];
+            }
+#pragma unroll
+            for (int g = 0; g < kScanGroups; g++)
+            {
+                StoreItems(offsets, base + 4 * g, C, o + 4 * g);
+            }
+        }
+
         // Pass 3: tile-local exclusive scan plus the tile prefix -> offsets.
         // With CLEAR it also zeroes the counts it has read (only the groups
         // holding one), so the next binning starts from zero without a memset.
@@ -278,25 +331,9 @@ namespace halcuda
                                                                   int32_t *__restrict__ offsets, int32_t n)
         {
             ChainEntry();
-            int64_t base = static_cast<int64_t>(blockIdx.x) * kScanTile + threadIdx.x * kScanItems;
+            const int64_t base = static_cast<int64_t>(blockIdx.x) * kScanTile + threadIdx.x * kScanItems;
             int32_t v[kScanItems];
-            LoadItems(counts, base, C, v);
-            if constexpr (CLEAR)
-            {
-                // only groups holding a count are written: most cells are
-                // empty, and an empty group is already cleared
-                int32_t any = 0;
-#pragma unroll
-                for (int q = 0; q < kScanItems; q++)
-                {
-                    any |= v[q];
-                }
-                if (any != 0)
-                {
-                    const int32_t zeros[kScanItems] = {0, 0, 0, 0};
-                    StoreItems(counts, base, C, zeros);
-                }
-            }
+            LoadThreadCells(counts, base, C, CLEAR, v);
             int32_t s = 0;
 #pragma unroll
             for (int q = 0; q < kScanItems; q++)
@@ -305,22 +342,15 @@ namespace halcuda
             }
             int32_t excl;
             BlockExclusiveScan(s, excl);
-            int32_t o[kScanItems];
-            o[0] = tilePrefix[blockIdx.x] + excl;
-#pragma unroll
-            for (int q = 1; q < kScanItems; q++)
-            {
-                o[q] = o[q - 1] + v[q - 1];
-            }
-            StoreItems(offsets, base, C, o);
+            StoreThreadOffsets(offsets, base, C, tilePrefix[blockIdx.x] + excl, v);
             if (blockIdx.x == 0 && threadIdx.x == 0)
             {
                 offsets[C] = n;
             }
         }
 
-        // Passes 2 and 3 in one launch, for grids of at most kScanThreads
-        // tiles: each CTA reduces the tile sums before its own (one per
+        // Passes 2 and 3 in one launch, for grids of at most kScanSumTiles
+        // tiles: each CTA reduces the tile sums before its own (a few per
         // thread) into its tile's prefix, then runs ScanApply<true>'s tile
         // scan.  This saves the single-CTA ScanTiles launch between them.
         __global__ void __launch_bounds__(kScanThreads) ScanApplySum(int32_t *__restrict__ counts, int64_t C,
@@ -328,25 +358,17 @@ namespace halcuda
                                                                      int32_t *__restrict__ offsets, int32_t n)
         {
             ChainEntry();
-            const int32_t before = (static_cast<int32_t>(threadIdx.x) < static_cast<int32_t>(blockIdx.x))
-                                       ? tileSums[threadIdx.x]
-                                       : 0;
+            int32_t before = 0;
+            for (int32_t t = static_cast<int32_t>(threadIdx.x); t < static_cast<int32_t>(blockIdx.x);
+                 t += kScanThreads)
+            {
+                before += tileSums[t];
+            }
             int32_t unused;
             const int32_t prefix = BlockExclusiveScan(before, unused);  // the block total
             const int64_t base = static_cast<int64_t>(blockIdx.x) * kScanTile + threadIdx.x * kScanItems;
             int32_t v[kScanItems];
-            LoadItems(counts, base, C, v);
-            int32_t any = 0;
-#pragma unroll
-            for (int q = 0; q < kScanItems; q++)
-            {
-                any |= v[q];
-            }
-            if (any != 0)
-            {
-                const int32_t zeros[kScanItems] = {0, 0, 0, 0};
-                StoreItems(counts, base, C, zeros);
-            }
+            LoadThreadCells(counts, base, C, true, v);
             int32_t sum = 0;
 #pragma unroll
             for (int q = 0; q < kScanItems; q++)
@@ -355,14 +377,7 @@ namespace halcuda
             }
             int32_t excl;
             BlockExclusiveScan(sum, excl);
-            int32_t o[kScanItems];
-            o[0] = prefix + excl;
-#pragma unroll
-            for (int q = 1; q < kScanItems; q++)
-            {
-                o[q] = o[q - 1] + v[q - 1];
-            }
-            StoreItems(offsets, base, C, o);
+            StoreThreadOffsets(offsets, base, C, prefix + excl, v);
             if (blockIdx.x == 0 && threadIdx.x == 0)
             {
                 offsets[C] = n;
@@ -1346,7 +1361,7 @@ namespace halcuda
                 cudaEventRecord(ev[0], s);
             }
             LaunchChained(ScanReduce, nTiles, kScanThreads, s, counts.p, C, tileSums.p);
-            if (nTiles <= kScanThreads)
+            if (nTiles <= kScanSumTiles)
             {
                 LaunchChained(ScanApplySum, nTiles, kScanThreads, s, counts.p, C, tileSums.p, offsets.p, n);
                 CountLaunch(2);
