@@ -267,14 +267,18 @@ namespace halcuda
         }
 
         // Solves (I - L/2) x = d along the line by parallel cyclic reduction;
-        // thread j holds row j (j < n); sm holds 4 * blockDim.x floats, and a
-        // wrapped line whose length is not a power of two uses blockDim.x + 4
-        // more after the four line arrays (PcrSolveSM).
-        __device__ float PcrSolve(const float *sD, float d, int32_t j, int32_t n, bool wrap, float *sm)
+        // thread j holds row j (j < n); sm holds 4 * blockDim.x floats.  SMW:
+        // the line wraps and its length is not a power of two (PcrSolveSM,
+        // which uses blockDim.x + 4 more floats after the four line arrays);
+        // a separate instantiation, so that the other line kernels keep their
+        // registers (32 against 38 with both forms in one kernel, and four
+        // 512-thread CTAs per SM).
+        template <bool SMW>
+        __device__ __forceinline__ float PcrSolve(const float *sD, float d, int32_t j, int32_t n, bool wrap, float *sm)
         {
-            if (wrap && n > 2 && (n & (n - 1)) != 0)
+            if constexpr (SMW)
             {
-                return PcrSolveSM(sD, d, j, n, sm, sm + 8 * blockDim.x);  // uniform across the CTA
+                return PcrSolveSM(sD, d, j, n, sm, sm + 8 * blockDim.x);
             }
             float *sa = sm, *sb = sm + blockDim.x, *sc = sb + blockDim.x, *sd = sc + blockDim.x;
             float a = 0.0f, b = 1.0f, c = 0.0f;
@@ -361,12 +365,19 @@ namespace halcuda
             return t;
         }
 
-        // Shared memory of the line kernels: 4 PCR arrays + 4 line arrays,
-        // then the second right-hand side and the broadcast values of the
-        // Sherman-Morrison solve (PcrSolveSM).
-        __host__ __device__ constexpr size_t LineSmemFloats(int threads)
+        // A wrapped line of length n that is not a power of two: its solve is
+        // the Sherman-Morrison form (the line kernels' SMW instantiation).
+        __host__ __device__ constexpr bool SmLine(int32_t n, bool wrap)
         {
-            return 9 * static_cast<size_t>(threads) + 4;
+            return wrap && n > 2 && (n & (n - 1)) != 0;
+        }
+
+        // Shared memory of the line kernels: 4 PCR arrays + 4 line arrays,
+        // and for an SmLine the second right-hand side and the broadcast
+        // values of PcrSolveSM.
+        __host__ __device__ constexpr size_t LineSmemFloats(int threads, int32_t n, bool wrap)
+        {
+            return SmLine(n, wrap) ? 9 * static_cast<size_t>(threads) + 4 : 8 * static_cast<size_t>(threads);
         }
 
         // x-sweep: w = (I - Lx/2)^-1 (I + Ly/2) f, one CTA per line y, in
@@ -376,6 +387,7 @@ namespace halcuda
         // written in HAL's layout for the y-sweep, and, when wB is set, also
         // line by line (wB[y * xDim + x]) as the state the backward x-kernel
         // reads along the same lines.
+        template <bool SMW>
         __global__ void FwdX(Grid g, const float *__restrict__ f, const float *__restrict__ DT, float *__restrict__ w,
                              float *__restrict__ wB)
         {
@@ -399,7 +411,7 @@ namespace halcuda
             {
                 lap += LapAlong(su, sD, j, n, g.wrapX != 0);
             }
-            const float e = PcrSolve(sD, 0.5f * lap, j, n, g.wrapX != 0, sm);
+            const float e = PcrSolve<SMW>(sD, 0.5f * lap, j, n, g.wrapX != 0, sm);
             if (j < n)
             {
                 w[Idx<kDirX>(g, line, j)] = c + e;
@@ -412,6 +424,7 @@ namespace halcuda
 
         // y-sweep and commit: v = (I - Ly/2)^-1 (I + Lx/2) w,
         // f' = f + (((v - f) + f*(-decay)) + src); v is kept when vOut != null.
+        template <bool SMW>
         __global__ void FwdY(Grid g, const float *__restrict__ w, const float *__restrict__ f,
                              const float *__restrict__ D, const float *__restrict__ src, float negDecay,
                              float *__restrict__ fOut, float *__restrict__ vOut)
@@ -437,7 +450,7 @@ namespace halcuda
                 lap += LapAlong(su, sD, j, n, g.wrapY != 0);
             }
             // residual form: v = w + (I - Ly/2)^-1 (Lx + Ly) w / 2
-            const float e = PcrSolve(sD, 0.5f * lap, j, n, g.wrapY != 0, sm);
+            const float e = PcrSolve<SMW>(sD, 0.5f * lap, j, n, g.wrapY != 0, sm);
             if (j < n)
             {
                 const int64_t i = Idx<kDirY>(g, line, j);
@@ -489,6 +502,7 @@ namespace halcuda
         };
 
         // Backward along y for step t: [gbar from step t+1] then the y-solve.
+        template <bool SMW>
         __global__ void BwdY(Grid g, int mode, const float *__restrict__ D, float decay,
                              const float *__restrict__ b1bar,     // step t+1's x-solve adjoint (kBwdNext/Tail)
                              const float *__restrict__ gPrev,     // adjoint of f_t+2 (kBwdNext/Tail), or gbar (kBwdFirst)
@@ -560,7 +574,7 @@ namespace halcuda
             }
             __syncthreads();
             const float lapg = (j < n) ? LapAlong(sq, sD, j, n, wrap) : 0.0f;
-            const float x = gbar + PcrSolve(sD, 0.5f * lapg, j, n, wrap, sm);
+            const float x = gbar + PcrSolve<SMW>(sD, 0.5f * lapg, j, n, wrap, sm);
             if (j < n)
             {
                 sp[j] = x;
@@ -579,6 +593,7 @@ namespace halcuda
         // The rates DT, the state wB and the x-face gradient dDT are all
         // line by line (y * xDim + x), contiguous along the CTA's line; only
         // b2bar and b1bar, which the y-kernels read and write, are strided.
+        template <bool SMW>
         __global__ void BwdX(Grid g, const float *__restrict__ DT, const float *__restrict__ b2bar,
                              const float *__restrict__ wB, float *__restrict__ b1bar, float *__restrict__ dDT)
         {
@@ -616,7 +631,7 @@ namespace halcuda
             __syncthreads();
             const float lapw = (j < n) ? lapb + 0.5f * LapAlong(sl, sD, j, n, wrap) : 0.0f;
             __syncthreads();
-            const float x = wbar + PcrSolve(sD, 0.5f * lapw, j, n, wrap, sm);
+            const float x = wbar + PcrSolve<SMW>(sD, 0.5f * lapw, j, n, wrap, sm);
             if (j < n)
             {
                 sp[j] = x;
@@ -732,8 +747,11 @@ namespace halcuda
                       cudaStream_t s)
         {
             const int tx = Threads(g.xDim), ty = Threads(g.yDim);
-            FwdX<<<g.yDim, tx, LineSmemFloats(tx) * sizeof(float), s>>>(g, fIn, DT.p, wA.p, wKeep);
-            FwdY<<<g.xDim, ty, LineSmemFloats(ty) * sizeof(float), s>>>(g, wA.p, fIn, D.p, srcp, negDecay, fOut,
+            const auto fwdX = SmLine(g.xDim, g.wrapX != 0) ? FwdX<true> : FwdX<false>;
+            const auto fwdY = SmLine(g.yDim, g.wrapY != 0) ? FwdY<true> : FwdY<false>;
+            fwdX<<<g.yDim, tx, LineSmemFloats(tx, g.xDim, g.wrapX != 0) * sizeof(float), s>>>(g, fIn, DT.p, wA.p, wKeep);
+            fwdY<<<g.xDim, ty, LineSmemFloats(ty, g.yDim, g.wrapY != 0) * sizeof(float), s>>>(g, wA.p, fIn, D.p,
+                                                                                               srcp, negDecay, fOut,
                                                                          vOut);
             CountLaunch(2);
             return LaunchStatus("adjoint forward step");
@@ -846,7 +864,10 @@ namespace halcuda
             int rc = HAL_CUDA_OK;
             float *gCur = gA.p, *gNext = gB.p;  // gCur: adjoint of the latest output handled
             const int tx = Threads(g.xDim), ty = Threads(g.yDim);
-            const size_t smx = LineSmemFloats(tx) * sizeof(float), smy = LineSmemFloats(ty) * sizeof(float);
+            const size_t smx = LineSmemFloats(tx, g.xDim, g.wrapX != 0) * sizeof(float);
+            const size_t smy = LineSmemFloats(ty, g.yDim, g.wrapY != 0) * sizeof(float);
+            const auto bwdX = SmLine(g.xDim, g.wrapX != 0) ? BwdX<true> : BwdX<false>;
+            const auto bwdY = SmLine(g.yDim, g.wrapY != 0) ? BwdY<true> : BwdY<false>;
             bool first = true;
             // states f_t0..f_t1, w and v of one segment into buffer b, from
             // the field at t0, on stream rs
@@ -868,10 +889,10 @@ namespace halcuda
                 {
                     const size_t k = static_cast<size_t>(t - t0);
                     const float *fNext = segF[b].p + (k + 1) * n;
-                    BwdY<<<g.xDim, ty, smy, s>>>(g, first ? kBwdFirst : kBwdNext, D.p, static_cast<float>(decay),
+                    bwdY<<<g.xDim, ty, smy, s>>>(g, first ? kBwdFirst : kBwdNext, D.p, static_cast<float>(decay),
                                                  b1.p, gCur, fNext, segF[b].p + k * n, segV[b].p + k * n, gNext,
                                                  b2.p, dD.p, dS.p, acc.p + 1);
-                    BwdX<<<g.yDim, tx, smx, s>>>(g, DT.p, b2.p, segW[b].p + k * n, b1.p, dDT.p);
+                    bwdX<<<g.yDim, tx, smx, s>>>(g, DT.p, b2.p, segW[b].p + k * n, b1.p, dDT.p);
                     CountLaunch(2);
                     r = LaunchStatus("adjoint backward step");
                     std::swap(gCur, gNext);
@@ -1028,7 +1049,7 @@ namespace halcuda
             if (rc == HAL_CUDA_OK && steps > 0)
             {
                 // the y-stencil part of step 0's (I + Ly/2) b1bar: its D terms
-                BwdY<<<g.xDim, ty, smy, s>>>(g, kBwdTail, D.p, static_cast<float>(decay), b1.p, gCur,
+                bwdY<<<g.xDim, ty, smy, s>>>(g, kBwdTail, D.p, static_cast<float>(decay), b1.p, gCur,
                                              segF[lastBuf].p, segF[lastBuf].p, segV[lastBuf].p, gNext, b2.p, dD.p,
                                              dS.p, acc.p + 1);
                 CountLaunch();

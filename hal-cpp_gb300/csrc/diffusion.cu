@@ -105,11 +105,11 @@ namespace halcuda
         // or zero-flux cases, so every difference weight is 1.  The
         // arithmetic is the general path's with those weights (x * 1 and
         // fmaf(x, 1, y) round as x and x + y), so results are bit-identical.
-        // UPT: the commit also multiplies each cell by negUptake once per
-        // agent binned in it (TickParams::cellOffsets).
+        // UPT: the commit also multiplies each cell by upt.negUptake once per
+        // agent binned in it (TickUptake).
         template <bool ADV, bool UPT>
-        __device__ __forceinline__ void TickInterior(const TickParams &p, const int32_t bx, const int32_t by,
-                                                     const int32_t y0, const int32_t xs)
+        __device__ __forceinline__ void TickInterior(const TickParams &p, const TickUptake &upt, const int32_t bx,
+                                                     const int32_t by, const int32_t y0, const int32_t xs)
         {
             constexpr int T = kTickRowsPerThread;
             const int64_t yD = p.yDim;
@@ -176,14 +176,14 @@ namespace halcuda
                 if constexpr (UPT)
                 {
                     // agent counts of the four cells: five consecutive offsets
-                    const int32_t *oc = p.cellOffsets + x * yD + y0;
+                    const int32_t *oc = upt.cellOffsets + x * yD + y0;
                     const int4 o4 = __ldg(reinterpret_cast<const int4 *>(oc));
                     const int32_t o5 = __ldg(oc + 4);
                     const int32_t nc[4] = {o4.y - o4.x, o4.z - o4.y, o4.w - o4.z, o5 - o4.w};
 #pragma unroll
                     for (int k = 0; k < 4; k++)
                     {
-                        o[k] = fmaf(cur[k], p.negUptake * static_cast<float>(nc[k]), o[k]);
+                        o[k] = fmaf(cur[k], upt.negUptake * static_cast<float>(nc[k]), o[k]);
                     }
                 }
                 for (int32_t q = ptBeg; q < ptEnd; q++)
@@ -208,7 +208,8 @@ namespace halcuda
         }
 
         template <int VEC, bool ADV = false, bool UPT = false>
-        __device__ __forceinline__ void TickTile(const TickParams &p, const int32_t bx, const int32_t by)
+        __device__ __forceinline__ void TickTile(const TickParams &p, const int32_t bx, const int32_t by,
+                                                 const TickUptake &upt = TickUptake{nullptr, 0.0f})
         {
             constexpr int T = kTickRowsPerThread;
             const int lane = threadIdx.x;
@@ -223,7 +224,7 @@ namespace halcuda
             {
                 if (xs >= 1 && xs + T < p.xDim && y0 >= 1 && y0 + 4 < p.yDim)
                 {
-                    TickInterior<ADV, UPT>(p, bx, by, y0, xs);
+                    TickInterior<ADV, UPT>(p, upt, bx, by, y0, xs);
                     return;
                 }
             }
@@ -380,14 +381,14 @@ namespace halcuda
                 }
                 if constexpr (UPT)
                 {
-                    const int32_t *oc = p.cellOffsets + static_cast<int64_t>(x) * p.yDim + y0;
+                    const int32_t *oc = upt.cellOffsets + static_cast<int64_t>(x) * p.yDim + y0;
 #pragma unroll
                     for (int k = 0; k < VEC; k++)
                     {
                         if (k < nValid)
                         {
                             const int32_t nc = __ldg(oc + k + 1) - __ldg(oc + k);
-                            o[k] = fmaf(cur[k], p.negUptake * static_cast<float>(nc), o[k]);
+                            o[k] = fmaf(cur[k], upt.negUptake * static_cast<float>(nc), o[k]);
                         }
                     }
                 }
@@ -433,7 +434,7 @@ namespace halcuda
 
         // Four CTAs per SM (64 registers) measured fastest for the plain tick
         // (6.68 vs 6.78 us at 2048^2); the advective tick is fastest unbounded.
-        template <int VEC, bool ADV, bool UPT = false>
+        template <int VEC, bool ADV>
         __global__ void __launch_bounds__(32 * kTickWarps, ADV ? 1 : 4)
             TickKernel(TickParams p)
         {
@@ -444,7 +445,17 @@ namespace halcuda
             // field (a no-op when launched without the attribute).
             asm volatile("griddepcontrol.launch_dependents;");
             asm volatile("griddepcontrol.wait;" ::: "memory");
-            TickTile<VEC, ADV, UPT>(p, static_cast<int32_t>(blockIdx.x), static_cast<int32_t>(blockIdx.y));
+            TickTile<VEC, ADV>(p, static_cast<int32_t>(blockIdx.x), static_cast<int32_t>(blockIdx.y));
+        }
+
+        // The tick with the agents' uptake term (hal_cuda_diffusion_set_uptake).
+        template <int VEC, bool ADV>
+        __global__ void __launch_bounds__(32 * kTickWarps, ADV ? 1 : 4)
+            TickKernelUptake(TickParams p, TickUptake up)
+        {
+            asm volatile("griddepcontrol.launch_dependents;");
+            asm volatile("griddepcontrol.wait;" ::: "memory");
+            TickTile<VEC, ADV, true>(p, static_cast<int32_t>(blockIdx.x), static_cast<int32_t>(blockIdx.y), up);
         }
 
         // Batched form: CTA b runs tile tiles[b] = (grid, CTA column, CTA row).
@@ -657,21 +668,26 @@ namespace halcuda
             p.kDn = static_cast<float>(r + std::max(-vx, 0.0));
             p.kYm = static_cast<float>(r + std::max(vy, 0.0));
             p.kYp = static_cast<float>(r + std::max(-vy, 0.0));
-            p.cellOffsets = nullptr;
-            p.negUptake = 0.0f;
+            return p;
+        }
+
+        // The uptake of a tick with extras (cellOffsets null: none).
+        TickUptake Uptake(bool useExtras) const
+        {
+            TickUptake u{nullptr, 0.0f};
             if (useExtras && agents != nullptr)
             {
                 int32_t ax = 0, ay = 0;
-                p.cellOffsets = AgentsCellOffsets(agents, &ax, &ay);
-                p.negUptake = static_cast<float>(-uptake);
+                u.cellOffsets = AgentsCellOffsets(agents, &ax, &ay);
+                u.negUptake = static_cast<float>(-uptake);
             }
-            return p;
+            return u;
         }
 
         // One tick, launched with programmatic stream serialization (the
         // kernel's griddepcontrol.wait keeps the ticks ordered): 6.55 against
         // 6.70 us per 2048^2 tick in a graph, bit-identical fields.
-        void LaunchTick(const TickParams &p, cudaStream_t s) const
+        void LaunchTick(const TickParams &p, const TickUptake &up, cudaStream_t s) const
         {
             const bool adv = p.kUp != p.r || p.kDn != p.r || p.kYm != p.r || p.kYp != p.r;
             cudaLaunchConfig_t cfg = {};
@@ -684,15 +700,15 @@ namespace halcuda
             at[0].val.programmaticStreamSerializationAllowed = 1;
             cfg.attrs = at;
             cfg.numAttrs = 1;
-            if (p.cellOffsets != nullptr)
+            if (up.cellOffsets != nullptr)
             {
                 if (vec4)
                 {
-                    cudaLaunchKernelEx(&cfg, adv ? TickKernel<4, true, true> : TickKernel<4, false, true>, p);
+                    cudaLaunchKernelEx(&cfg, adv ? TickKernelUptake<4, true> : TickKernelUptake<4, false>, p, up);
                 }
                 else
                 {
-                    cudaLaunchKernelEx(&cfg, adv ? TickKernel<1, true, true> : TickKernel<1, false, true>, p);
+                    cudaLaunchKernelEx(&cfg, adv ? TickKernelUptake<1, true> : TickKernelUptake<1, false>, p, up);
                 }
             }
             else if (vec4)
@@ -764,7 +780,7 @@ namespace halcuda
                 for (; t < ticks; t++)
                 {
                     TickParams p = Params(field[c].p, field[c ^ 1].p, r, decay, wrapX, wrapY, extras);
-                    LaunchTick(p, s);
+                    LaunchTick(p, Uptake(extras), s);
                     c ^= 1;
                 }
                 cudaError_t e = cudaStreamEndCapture(s, &g);
@@ -1325,7 +1341,7 @@ extern "C" int hal_cuda_diffusion_profile(hal_cuda_diffusion *h, int32_t iters, 
         int c = h->cur;
         TickParams p = h->Params(h->field[c].p, h->field[c ^ 1].p, diffRate, decay, wrapX != 0, wrapY != 0, true);
         cudaEventRecord(e0, s);
-        h->LaunchTick(p, s);
+        h->LaunchTick(p, h->Uptake(true), s);
         CountLaunch();
         cudaEventRecord(e1, s);
         rc = LaunchStatus("TickKernel launch");

@@ -27,12 +27,17 @@ namespace halcuda
         // r + max(-xVel, 0), y-1: r + max(yVel, 0), y+1: r + max(-yVel, 0).
         // Read only by the advective variant of the tick.
         float kUp, kDn, kYm, kYp;
-        // Agent uptake (the uptake variant of the single-grid tick): every
-        // agent binned in a cell multiplies it by negUptake, as a model's
-        // PDEGrid2D::Mul(cell, -uptake) per agent; the agent count of cell i
-        // is cellOffsets[i + 1] - cellOffsets[i] (layout x*yDim + y).
-        const int32_t *cellOffsets = nullptr;
-        float negUptake = 0.0f;
+    };
+
+    // Agent uptake of the single-grid tick's uptake variant (a second kernel
+    // parameter, so that the other ticks keep their parameters): every agent
+    // binned in a cell multiplies it by negUptake, as a model's
+    // PDEGrid2D::Mul(cell, -uptake) per agent; the agent count of cell i is
+    // cellOffsets[i + 1] - cellOffsets[i] (layout x*yDim + y).
+    struct TickUptake
+    {
+        const int32_t *cellOffsets;
+        float negUptake;
     };
 
     // Geometry of the tick's CTAs: 32 lanes x kTickWarps warps; a lane owns
