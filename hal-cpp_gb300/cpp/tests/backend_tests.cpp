@@ -487,6 +487,97 @@ namespace
         return "";
     }
 
+    // A CompetitiveRelease-style model tick through the classes: the coupled
+    // call equals alternating Step(1) / RunTicks(1) calls bit for bit, and the
+    // explicit field's uptake equals the oracle tick with the bins' counts.
+    std::string CoupledModel()
+    {
+        const int32_t nx = 48, ny = 64, n = 2500;
+        oracle_rand rng;
+        oracle_rand_init(&rng, 91);
+        std::vector<float> pos(2 * n), rad(n, 0.5f), f0(static_cast<size_t>(nx) * ny),
+            s0(static_cast<size_t>(nx) * ny);
+        for (int32_t i = 0; i < n; i++)
+        {
+            pos[2 * i] = static_cast<float>(oracle_rand_double(&rng) * nx * 0.999);
+            pos[2 * i + 1] = static_cast<float>(ny * 0.5 + (oracle_rand_double(&rng) - 0.5) * ny * 0.4);
+        }
+        for (size_t c = 0; c < f0.size(); c++)
+        {
+            f0[c] = static_cast<float>(oracle_rand_double(&rng));
+            s0[c] = static_cast<float>(0.01 * oracle_rand_double(&rng));
+        }
+        const double uptake = 0.002, r = 3.0, decay = 0.01;
+        std::vector<float> expF, expP, expV, gotF, gotP, gotV;
+        {
+            Hal::Cuda::CudaAgentForceBackend2D ag(nx, ny, n);
+            Hal::Cuda::CudaAdiDiffusionBackend2D adi(nx, ny);
+            ag.Upload(pos, rad);
+            adi.SetField(f0);
+            adi.SetSource(s0);
+            adi.SetUptake(&ag, uptake);
+            for (int t = 0; t < 9; t++)
+            {
+                // the handles' streams differ: the tick reads this step's bins,
+                // and the next step rebins after the tick has read them
+                ag.Step(1, 1.0, 0.1, false, false, 0.5, -1.0);
+                hal_cuda_agents_sync(ag.Handle());
+                adi.RunTicks(1, r, decay, false, false);
+                adi.Sync();
+            }
+            adi.GetField(expF);
+            ag.GetState(expP, expV);
+        }
+        {
+            Hal::Cuda::CudaAgentForceBackend2D ag(nx, ny, n);
+            Hal::Cuda::CudaAdiDiffusionBackend2D adi(nx, ny);
+            ag.Upload(pos, rad);
+            adi.SetField(f0);
+            adi.SetSource(s0);
+            adi.SetUptake(&ag, uptake);
+            adi.RunCoupled(ag, 4, r, decay, false, false, 1.0, 0.1, 0.5, -1.0);
+            adi.RunCoupled(ag, 5, r, decay, false, false, 1.0, 0.1, 0.5, -1.0);
+            adi.GetField(gotF);
+            ag.GetState(gotP, gotV);
+        }
+        if (gotF != expF || gotP != expP || gotV != expV)
+        {
+            return "RunCoupled differs from alternating Step / RunTicks calls";
+        }
+        // explicit uptake: one dispatch's bins, 20 ticks, against the oracle
+        Hal::Cuda::CudaAgentForceBackend2D ag(nx, ny, n);
+        Hal::Cuda::CudaDiffusionBackend2D diff(nx, ny);
+        ag.Upload(pos, rad);
+        ag.Dispatch(1.0, 0.1, false, false);
+        std::vector<int32_t> off, bucket;
+        ag.GetBins(off, bucket);
+        std::vector<int32_t> counts(f0.size());
+        for (size_t c = 0; c < counts.size(); c++)
+        {
+            counts[c] = off[c + 1] - off[c];
+        }
+        diff.SetField(f0);
+        diff.SetSource(s0);
+        diff.SetUptake(&ag, uptake);
+        diff.RunTicks(20, 0.2, decay, false, false);
+        diff.GetField(gotF);
+        const size_t cells = f0.size();
+        std::vector<double> exp(f0.begin(), f0.end()), deltas(cells, 0.0), scratch(cells),
+            src64(s0.begin(), s0.end());
+        for (int t = 0; t < 20; t++)
+        {
+            oracle_tick(0, exp.data(), deltas.data(), scratch.data(), nx, ny, 0.2, 0, 0, nullptr, decay, src64.data(),
+                        0, nullptr, nullptr, counts.data(), uptake, 1);
+        }
+        std::vector<double> got64(gotF.begin(), gotF.end());
+        const double err = MaxAbsDiff(got64, exp) / MaxAbs(exp);
+        if (err > 1e-5)
+        {
+            return Fmt("explicit ticks with uptake differ from the oracle: %.3e", err);
+        }
+        return "";
+    }
+
     double RelL2(const std::vector<float> &a, const std::vector<double> &b)
     {
         double num = 0.0, den = 0.0;
@@ -698,6 +789,7 @@ int main()
     Run("resident_agent_step_bit_exact", [&] { return AgentStep(agents64); });
     Run("batched_wells_equal_single_grids", [&] { return Wells(); });
     Run("adjoint_forward_backward_api", [&] { return Adjoint(); });
+    Run("coupled_model_ticks", [&] { return CoupledModel(); });
 
     std::printf("backend_tests: %d passed, %d failed\n", g_passed, g_failed);
     return g_failed == 0 ? 0 : 1;
