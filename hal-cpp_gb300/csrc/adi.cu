@@ -2137,6 +2137,7 @@ extern "C" int hal_cuda_diffuse_adi(hal_cuda_adi *h, const double *field, int64_
                                     int64_t deltasLen, double diffRate, int32_t xDim, int32_t yDim,
                                     int32_t wrapX, int32_t wrapY)
 {
+    HAL_TRACE();
     HAL_REQUIRE(h != nullptr, "hal_cuda_diffuse_adi: handle is NULL");
     int64_t length = static_cast<int64_t>(xDim) * yDim;
     HAL_REQUIRE(xDim > 0 && yDim > 0 && fieldLen == length && deltasLen == length,
@@ -2150,6 +2151,7 @@ extern "C" int hal_cuda_diffuse_adi(hal_cuda_adi *h, const double *field, int64_
 extern "C" int hal_cuda_diffuse_adi_bc(hal_cuda_adi *h, const double *field, double *deltas, double diffRate,
                                        int32_t wrapX, int32_t wrapY, const double *ghost)
 {
+    HAL_TRACE();
     HAL_REQUIRE(h != nullptr && field != nullptr && deltas != nullptr, "hal_cuda_diffuse_adi_bc: NULL argument");
     return DiffuseAdiCommon(h, field, deltas, diffRate, wrapX, wrapY, ghost, "hal_cuda_diffuse_adi_bc");
 }
@@ -2231,6 +2233,7 @@ extern "C" int hal_cuda_adi_set_uptake(hal_cuda_adi *h, hal_cuda_agents *agents,
 extern "C" int hal_cuda_adi_run_ticks(hal_cuda_adi *h, int32_t ticks, double diffRate, double decay, int32_t wrapX,
                                       int32_t wrapY)
 {
+    HAL_TRACE();
     HAL_REQUIRE(h != nullptr, "hal_cuda_adi_run_ticks: handle is NULL");
     HAL_REQUIRE(ticks >= 0, "hal_cuda_adi_run_ticks: negative tick count");
     HAL_TRY(halcuda::CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
@@ -2241,6 +2244,7 @@ extern "C" int hal_cuda_adi_run_coupled(hal_cuda_adi *h, hal_cuda_agents *agents
                                         double decay, int32_t wrapX, int32_t wrapY, double interactionRad,
                                         double springConstant, double friction, double maxVel)
 {
+    HAL_TRACE();
     HAL_REQUIRE(h != nullptr && agents != nullptr, "hal_cuda_adi_run_coupled: handle is NULL");
     HAL_REQUIRE(ticks >= 0, "hal_cuda_adi_run_coupled: negative tick count");
     HAL_REQUIRE(h->agents == agents,
@@ -2257,6 +2261,7 @@ extern "C" int hal_cuda_adi_run_coupled(hal_cuda_adi *h, hal_cuda_agents *agents
 extern "C" int hal_cuda_adi_run_steps(hal_cuda_adi *h, float *field, int64_t len, int32_t steps, double diffRate,
                                       int32_t wrapX, int32_t wrapY)
 {
+    HAL_TRACE();
     HAL_REQUIRE(h != nullptr && field != nullptr, "hal_cuda_adi_run_steps: NULL argument");
     HAL_REQUIRE(len == static_cast<int64_t>(h->Length()), "AdiKernel2D::RunSteps: field must hold xDim*yDim values");
     HAL_REQUIRE(steps >= 0, "hal_cuda_adi_run_steps: negative step count");
@@ -2269,6 +2274,7 @@ extern "C" int hal_cuda_adi_run_ticks_host(hal_cuda_adi *h, float *field, const 
                                            int32_t ticks, double diffRate, double decay, int32_t wrapX,
                                            int32_t wrapY)
 {
+    HAL_TRACE();
     HAL_REQUIRE(h != nullptr && field != nullptr, "hal_cuda_adi_run_ticks_host: NULL argument");
     HAL_REQUIRE(len == static_cast<int64_t>(h->Length()),
                 "hal_cuda_adi_run_ticks_host: field must hold xDim*yDim values");

@@ -1184,6 +1184,7 @@ extern "C" int hal_cuda_adjoint_set_problem(hal_cuda_adjoint *h, const float *f0
 extern "C" int hal_cuda_adjoint_forward(hal_cuda_adjoint *h, const float *D, double decay, const float *src,
                                         double *loss, float *fT)
 {
+    HAL_TRACE();
     HAL_REQUIRE(h != nullptr && D != nullptr && loss != nullptr, "hal_cuda_adjoint_forward: NULL argument");
     HAL_REQUIRE(h->hasProblem, "hal_cuda_adjoint_forward: call hal_cuda_adjoint_set_problem first");
     HAL_REQUIRE(std::isfinite(decay), "hal_cuda_adjoint_forward: decay %g", decay);
@@ -1194,6 +1195,7 @@ extern "C" int hal_cuda_adjoint_forward(hal_cuda_adjoint *h, const float *D, dou
 extern "C" int hal_cuda_adjoint_gradient(hal_cuda_adjoint *h, const float *D, double decay, const float *src,
                                          double *loss, float *gradD, double *gradDecay, float *gradSrc)
 {
+    HAL_TRACE();
     HAL_REQUIRE(h != nullptr && D != nullptr && loss != nullptr, "hal_cuda_adjoint_gradient: NULL argument");
     HAL_REQUIRE(h->hasProblem, "hal_cuda_adjoint_gradient: call hal_cuda_adjoint_set_problem first");
     HAL_REQUIRE(std::isfinite(decay), "hal_cuda_adjoint_gradient: decay %g", decay);

@@ -1652,6 +1652,7 @@ extern "C" int hal_cuda_accumulate_forces(hal_cuda_agents *h, const double *posi
                                           double interactionRad, double springConstant, int32_t xDim, int32_t yDim,
                                           int32_t wrapX, int32_t wrapY)
 {
+    HAL_TRACE();
     HAL_REQUIRE(h != nullptr, "hal_cuda_accumulate_forces: handle is NULL");
     HAL_REQUIRE(xDim == h->xDim && yDim == h->yDim,
                 "CudaAgentForceBackend2D::AccumulateForces called with dimensions differing from construction");
@@ -1691,6 +1692,7 @@ extern "C" int hal_cuda_sum_forces(hal_cuda_agents *h, const double *positions, 
                                    double interactionRad, const hal_cuda_force_law *law, int32_t order,
                                    int32_t xDim, int32_t yDim, int32_t wrapX, int32_t wrapY)
 {
+    HAL_TRACE();
     const char *who = "hal_cuda_sum_forces";
     HAL_REQUIRE(h != nullptr, "%s: handle is NULL", who);
     HAL_REQUIRE(xDim == h->xDim && yDim == h->yDim,
@@ -1956,6 +1958,7 @@ namespace
 extern "C" int hal_cuda_agents_step(hal_cuda_agents *h, int32_t ticks, double interactionRad, double springConstant,
                                     int32_t wrapX, int32_t wrapY, double friction, double maxVel)
 {
+    HAL_TRACE();
     return StepCommon(h, ticks, interactionRad, halcuda::ForceLawSpec::Linear(springConstant), wrapX, wrapY, friction,
                       maxVel, "hal_cuda_agents_step");
 }
@@ -1964,6 +1967,7 @@ extern "C" int hal_cuda_agents_step_law(hal_cuda_agents *h, int32_t ticks, doubl
                                         const hal_cuda_force_law *law, int32_t withSums, int32_t wrapX,
                                         int32_t wrapY, double friction, double maxVel)
 {
+    HAL_TRACE();
     halcuda::ForceLawSpec spec;
     HAL_TRY(LawFrom(law, withSums != 0, "hal_cuda_agents_step_law", &spec));
     return StepCommon(h, ticks, interactionRad, spec, wrapX, wrapY, friction, maxVel, "hal_cuda_agents_step_law");
@@ -1972,6 +1976,7 @@ extern "C" int hal_cuda_agents_step_law(hal_cuda_agents *h, int32_t ticks, doubl
 extern "C" int hal_cuda_agents_dispatch(hal_cuda_agents *h, double interactionRad, double springConstant,
                                         int32_t wrapX, int32_t wrapY)
 {
+    HAL_TRACE();
     return DispatchCommon(h, interactionRad, halcuda::ForceLawSpec::Linear(springConstant), wrapX, wrapY,
                           "hal_cuda_agents_dispatch");
 }
@@ -1979,6 +1984,7 @@ extern "C" int hal_cuda_agents_dispatch(hal_cuda_agents *h, double interactionRa
 extern "C" int hal_cuda_agents_dispatch_law(hal_cuda_agents *h, double interactionRad, const hal_cuda_force_law *law,
                                             int32_t withSums, int32_t wrapX, int32_t wrapY)
 {
+    HAL_TRACE();
     halcuda::ForceLawSpec spec;
     HAL_TRY(LawFrom(law, withSums != 0, "hal_cuda_agents_dispatch_law", &spec));
     return DispatchCommon(h, interactionRad, spec, wrapX, wrapY, "hal_cuda_agents_dispatch_law");

@@ -12,6 +12,8 @@
 #include <vector>
 
 #include "hal_cuda.h"
+
+#include <nvtx3/nvToolsExt.h>
 #include "hal_cuda_measure.h"
 
 namespace halcuda
@@ -19,6 +21,34 @@ namespace halcuda
     // Thread-local message of the last failed call (hal_cuda_last_error).
     void SetError(const char *fmt, ...);
     void ClearError();
+
+    // NVTX range over one library call, in the domain "hal_cuda" (HAL_TRACE at
+    // the top of the hot-path entry points): Nsight tools show the calls on
+    // the timeline and can filter kernels by call, e.g. ncu --nvtx
+    // --nvtx-include "hal_cuda@hal_cuda_adi_run_ticks/".  Without a tool
+    // attached a range costs a call through a no-op stub.
+    inline nvtxDomainHandle_t TraceDomain()
+    {
+        static const nvtxDomainHandle_t s_domain = nvtxDomainCreateA("hal_cuda");
+        return s_domain;
+    }
+
+    class TraceRange
+    {
+    public:
+        explicit TraceRange(const char *name)
+        {
+            nvtxEventAttributes_t a = {};
+            a.version = NVTX_VERSION;
+            a.size = NVTX_EVENT_ATTRIB_STRUCT_SIZE;
+            a.messageType = NVTX_MESSAGE_TYPE_ASCII;
+            a.message.ascii = name;
+            nvtxDomainRangePushEx(TraceDomain(), &a);
+        }
+        ~TraceRange() { nvtxDomainRangePop(TraceDomain()); }
+        TraceRange(const TraceRange &) = delete;
+        TraceRange &operator=(const TraceRange &) = delete;
+    };
 
     // Counts every kernel launch issued by the library (hal_cuda_launch_count).
     extern std::atomic<int64_t> g_launches;
@@ -301,3 +331,6 @@ namespace halcuda
             return HAL_CUDA_EINVAL;           \
         }                                     \
     } while (0)
+
+// Opens a TraceRange named after the enclosing entry point until it returns.
+#define HAL_TRACE() ::halcuda::TraceRange halTraceRange_(__func__)

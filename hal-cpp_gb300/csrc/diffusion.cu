@@ -980,6 +980,7 @@ namespace
 extern "C" int hal_cuda_diffuse_var(hal_cuda_diffusion *h, const double *field, double *deltas,
                                     const double *ratesX, const double *ratesY, int32_t wrapX, int32_t wrapY)
 {
+    HAL_TRACE();
     HAL_REQUIRE(h != nullptr && field != nullptr && deltas != nullptr && ratesX != nullptr && ratesY != nullptr,
                 "hal_cuda_diffuse_var: NULL argument");
     return Stencil64Common(h, kVarDiffusion, field, deltas, ratesX, ratesY, 0.0, 0.0, wrapX, wrapY, nullptr, nullptr,
@@ -989,6 +990,7 @@ extern "C" int hal_cuda_diffuse_var(hal_cuda_diffusion *h, const double *field, 
 extern "C" int hal_cuda_advect(hal_cuda_diffusion *h, const double *field, double *deltas, double xVel, double yVel,
                                int32_t wrapX, int32_t wrapY)
 {
+    HAL_TRACE();
     HAL_REQUIRE(h != nullptr && field != nullptr && deltas != nullptr, "hal_cuda_advect: NULL argument");
     return Stencil64Common(h, kAdvection, field, deltas, nullptr, nullptr, xVel, yVel, wrapX, wrapY, nullptr, nullptr,
                            nullptr, "hal_cuda_advect");
@@ -997,6 +999,7 @@ extern "C" int hal_cuda_advect(hal_cuda_diffusion *h, const double *field, doubl
 extern "C" int hal_cuda_advect_bc(hal_cuda_diffusion *h, const double *field, double *deltas, double xVel,
                                   double yVel, int32_t wrapX, int32_t wrapY, const double *ghost)
 {
+    HAL_TRACE();
     HAL_REQUIRE(h != nullptr && field != nullptr && deltas != nullptr, "hal_cuda_advect_bc: NULL argument");
     return Stencil64Common(h, kAdvection, field, deltas, nullptr, nullptr, xVel, yVel, wrapX, wrapY, ghost, nullptr,
                            nullptr, "hal_cuda_advect_bc");
@@ -1005,6 +1008,7 @@ extern "C" int hal_cuda_advect_bc(hal_cuda_diffusion *h, const double *field, do
 extern "C" int hal_cuda_advect_var(hal_cuda_diffusion *h, const double *field, double *deltas, const double *xVels,
                                    const double *yVels, int32_t wrapX, int32_t wrapY)
 {
+    HAL_TRACE();
     HAL_REQUIRE(h != nullptr && field != nullptr && deltas != nullptr && xVels != nullptr && yVels != nullptr,
                 "hal_cuda_advect_var: NULL argument");
     return Stencil64Common(h, kVarAdvection, field, deltas, xVels, yVels, 0.0, 0.0, wrapX, wrapY, nullptr, nullptr,
@@ -1015,6 +1019,7 @@ extern "C" int hal_cuda_advect_var_bc(hal_cuda_diffusion *h, const double *field
                                       const double *xVels, const double *yVels, int32_t wrapX, int32_t wrapY,
                                       const double *ghost, const double *ghostXVel, const double *ghostYVel)
 {
+    HAL_TRACE();
     HAL_REQUIRE(h != nullptr && field != nullptr && deltas != nullptr && xVels != nullptr && yVels != nullptr,
                 "hal_cuda_advect_var_bc: NULL argument");
     return Stencil64Common(h, kVarAdvection, field, deltas, xVels, yVels, 0.0, 0.0, wrapX, wrapY, ghost, ghostXVel,
@@ -1067,6 +1072,7 @@ extern "C" int hal_cuda_diffuse(hal_cuda_diffusion *h, const double *field, int6
                                 double *deltas, int64_t deltasLen, double diffRate, int32_t xDim,
                                 int32_t yDim, int32_t wrapX, int32_t wrapY)
 {
+    HAL_TRACE();
     HAL_REQUIRE(h != nullptr, "hal_cuda_diffuse: handle is NULL");
     int64_t length = static_cast<int64_t>(xDim) * yDim;
     HAL_REQUIRE(xDim > 0 && yDim > 0 && fieldLen == length && deltasLen == length,
@@ -1080,6 +1086,7 @@ extern "C" int hal_cuda_diffuse(hal_cuda_diffusion *h, const double *field, int6
 extern "C" int hal_cuda_diffuse_bc(hal_cuda_diffusion *h, const double *field, double *deltas,
                                    double diffRate, int32_t wrapX, int32_t wrapY, const double *ghost)
 {
+    HAL_TRACE();
     HAL_REQUIRE(h != nullptr && field != nullptr && deltas != nullptr, "hal_cuda_diffuse_bc: NULL argument");
     return DiffuseCommon(h, field, deltas, diffRate, wrapX, wrapY, ghost, "hal_cuda_diffuse_bc");
 }
@@ -1283,6 +1290,7 @@ extern "C" int hal_cuda_diffusion_set_dirichlet(hal_cuda_diffusion *h, const flo
 extern "C" int hal_cuda_diffusion_run_ticks(hal_cuda_diffusion *h, int32_t ticks, double diffRate,
                                             double decay, int32_t wrapX, int32_t wrapY)
 {
+    HAL_TRACE();
     HAL_REQUIRE(h != nullptr, "hal_cuda_diffusion_run_ticks: handle is NULL");
     HAL_REQUIRE(ticks >= 0, "hal_cuda_diffusion_run_ticks: negative tick count");
     HAL_REQUIRE(!(diffRate > 0.25), "Diffusion rate above stable maximum value of 0.25");
@@ -1293,6 +1301,7 @@ extern "C" int hal_cuda_diffusion_run_ticks(hal_cuda_diffusion *h, int32_t ticks
 extern "C" int hal_cuda_diffusion_run_steps(hal_cuda_diffusion *h, float *field, int64_t len, int32_t steps,
                                             double diffRate, int32_t wrapX, int32_t wrapY)
 {
+    HAL_TRACE();
     HAL_REQUIRE(h != nullptr && field != nullptr, "hal_cuda_diffusion_run_steps: NULL argument");
     HAL_REQUIRE(len == static_cast<int64_t>(h->Length()),
                 "DiffusionKernel2D::RunSteps: field must hold xDim*yDim values");

@@ -1025,6 +1025,7 @@ extern "C" int hal_cuda_wells_get_agents(hal_cuda_wells *h, float *positions, fl
 extern "C" int hal_cuda_wells_run_ticks(hal_cuda_wells *h, int32_t ticks, double interactionRad,
                                         double springConstant)
 {
+    HAL_TRACE();
     HAL_REQUIRE(h != nullptr, "hal_cuda_wells_run_ticks: handle is NULL");
     HAL_REQUIRE(ticks >= 0, "hal_cuda_wells_run_ticks: negative tick count");
     HAL_REQUIRE(std::isfinite(interactionRad) && interactionRad >= 0.0 && interactionRad <= halcuda::kMaxInteractionRad,
