@@ -538,6 +538,8 @@ namespace halcuda
         bool combDirty = true;
         DevBuf<int32_t> blockErr;
         bool stopped = false;  // a two-tick launch gave up waiting: no further ticks
+        // failure-detection test hook (hal_cuda_diffusion_test_stall)
+        uint32_t testExtraTx = 0, testWaitUs = 0;
 
         DevBuf<double> f64, d64, g64;
         DevBuf<double> a64, b64;  // per-cell rates or velocities of the FP64 stencil calls
@@ -636,6 +638,8 @@ namespace halcuda
             b.kYp = t.kYp;
             b.adv = (t.kUp != t.r || t.kDn != t.r || t.kYm != t.r || t.kYp != t.r) ? 1 : 0;
             b.err = blockErr.p;
+            b.extraTx = testExtraTx;
+            b.waitLimitUs = testWaitUs;
             return b;
         }
 
@@ -756,9 +760,9 @@ namespace halcuda
             // for an odd count); each launch flips the buffers
             const int32_t launches = blocked ? ticks / 2 + (ticks & 1) : ticks;
             char key[256];
-            snprintf(key, sizeof(key), "%d|%a|%a|%d|%d|%d|%d|%d|%d|%a|%a|%d|%p|%p|%a", ticks, r, decay, wrapX,
+            snprintf(key, sizeof(key), "%d|%a|%a|%d|%d|%d|%d|%d|%d|%a|%a|%d|%p|%p|%a|%u|%u", ticks, r, decay, wrapX,
                      wrapY, extras ? 1 : 0, hasSrc, hasPoints, hasGhost, xVel, yVel, blocked ? 1 : 0,
-                     static_cast<void *>(s), static_cast<const void *>(agents), uptake);
+                     static_cast<void *>(s), static_cast<const void *>(agents), uptake, testExtraTx, testWaitUs);
             GraphCache &graph = this->graph[cur];
             if (graph.exec == nullptr || graph.key != key)
             {
@@ -1236,6 +1240,18 @@ extern "C" int hal_cuda_diffusion_set_uptake(hal_cuda_diffusion *h, hal_cuda_age
                 h->yDim);
     h->agents = agents;
     h->uptake = uptake;
+    return HAL_CUDA_OK;
+}
+
+extern "C" int hal_cuda_diffusion_test_stall(hal_cuda_diffusion *h, int32_t stall, double waitSeconds)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_diffusion_test_stall: handle is NULL");
+    HAL_REQUIRE(waitSeconds >= 0.0 && waitSeconds <= 2.0, "hal_cuda_diffusion_test_stall: wait %g s outside [0, 2]",
+                waitSeconds);
+    // 16 bytes more than the copy brings: the mbarrier's phase never
+    // completes, and the bounded wait runs out
+    h->testExtraTx = stall ? 16u : 0u;
+    h->testWaitUs = static_cast<uint32_t>(waitSeconds * 1e6);
     return HAL_CUDA_OK;
 }
 

@@ -138,7 +138,8 @@ namespace halcuda
                 s_fail = 0;
                 asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
                 asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                             "r"(bytes + p.extraTx)
                              : "memory");
                 asm volatile(
                     "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
@@ -150,10 +151,12 @@ namespace halcuda
             // bounded wait for the tile; one that gives up records the
             // failure and waits once more (bounded again), so that the copy
             // is not still writing into shared memory when the CTA exits
-            if (!MbarWaitBounded(bar, kWaitLimitNs))
+            const unsigned long long limitNs =
+                (p.waitLimitUs != 0) ? 1000ull * static_cast<unsigned long long>(p.waitLimitUs) : kWaitLimitNs;
+            if (!MbarWaitBounded(bar, limitNs))
             {
                 s_fail = 1;
-                MbarWaitBounded(bar, kWaitLimitNs);
+                MbarWaitBounded(bar, limitNs);
             }
             __syncthreads();
             if (s_fail)

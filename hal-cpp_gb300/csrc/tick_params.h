@@ -67,6 +67,11 @@ namespace halcuda
         float kUp, kDn, kYm, kYp;  // per-side weights when advecting (see TickParams)
         int32_t adv;
         int32_t *err;              // set to 1 if a staging wait gave up
+        // failure-detection test hook (hal_cuda_diffusion_test_stall):
+        // bytes the staged copy's mbarrier expects beyond the copy, so that
+        // its wait runs out, and the wait's limit in us (0: the default)
+        uint32_t extraTx;
+        uint32_t waitLimitUs;
     };
 
     // Opaque 128-byte tensor map (a CUtensorMap) over one field buffer.

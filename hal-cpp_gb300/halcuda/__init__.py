@@ -48,6 +48,7 @@ SIGNATURES = {
     "hal_cuda_diffusion_set_source": (_I, [_vp, _vp, _i64]),
     "hal_cuda_diffusion_set_point_sources": (_I, [_vp, _i32, _vp, _vp]),
     "hal_cuda_diffusion_set_blocking": (_I, [_vp, _i32]),
+    "hal_cuda_diffusion_test_stall": (_I, [_vp, _i32, _f64]),
     "hal_cuda_diffusion_set_velocity": (_I, [_vp, _f64, _f64]),
     "hal_cuda_diffusion_set_dirichlet": (_I, [_vp, _vp]),
     "hal_cuda_diffusion_run_ticks": (_I, [_vp, _i32, _f64, _f64, _i32, _i32]),
@@ -415,6 +416,11 @@ class Diffusion(_Handle):
     def set_blocking(self, ticksPerLaunch):
         """Ticks per launch: 1, 2 (temporal blocking) or 0 (by grid size)."""
         _check(lib().hal_cuda_diffusion_set_blocking(self._h, int(ticksPerLaunch)), "set_blocking")
+
+    def test_stall(self, stall, waitSeconds=0.0):
+        """Failure-detection test hook: the two-tick kernel's staging waits run
+        out (see include/hal_cuda_measure.h)."""
+        _check(lib().hal_cuda_diffusion_test_stall(self._h, int(stall), float(waitSeconds)), "test_stall")
 
     def set_velocity(self, xVel, yVel):
         """Uniform upwind advection of every following tick (PDEGrid2D::Advection)."""

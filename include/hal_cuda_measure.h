@@ -40,6 +40,18 @@ int hal_cuda_fp64_issue_rate(double *opsPerSecond);
 int hal_cuda_stencil64_profile(hal_cuda_diffusion *h, int32_t kind, int32_t iters, double xVel,
                                double yVel, int32_t wrapX, int32_t wrapY, float *ms);
 
+/* Failure-detection test hook of the two-tick kernel
+ * (hal_cuda_diffusion_set_blocking(h, 2)): with stall set, every staged
+ * tile's mbarrier expects 16 bytes more than its tensor copy brings, so the
+ * kernel's bounded wait runs out -- no fault, no hang: each CTA waits
+ * waitSeconds (0: the 2 s default) twice, records the failure in the handle's
+ * device error word and returns without writing its tile.  The next
+ * synchronising call (hal_cuda_diffusion_get_field) then returns
+ * HAL_CUDA_ETIMEOUT, and the handle refuses every later tick, as after a real
+ * staging failure.  stall 0 restores normal launches (of a handle that has not
+ * stopped). */
+int hal_cuda_diffusion_test_stall(hal_cuda_diffusion *h, int32_t stall, double waitSeconds);
+
 /* Profiling: average device time (ms) of one fused-tick launch over `iters`
  * individually timed ticks (CUDA events, no graph).  The field advances. */
 int hal_cuda_diffusion_profile(hal_cuda_diffusion *h, int32_t iters, double diffRate,
