@@ -481,8 +481,13 @@ class Adi(_Handle):
         f = _f32(field)
         _check(lib().hal_cuda_adi_set_field(self._h, _p(f), f.size), "set_field")
 
-    def get_field(self):
-        out = np.empty(self.xDim * self.yDim, dtype=np.float32)
+    def get_field(self, out=None):
+        """The resident field in HAL's layout, into `out` (a float32 array of
+        xDim*yDim values, e.g. pinned pages) when given."""
+        if out is None:
+            out = np.empty(self.xDim * self.yDim, dtype=np.float32)
+        elif out.dtype != np.float32 or out.size != self.xDim * self.yDim or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous float32 array of xDim*yDim values")
         _check(lib().hal_cuda_adi_get_field(self._h, _p(out), out.size), "get_field")
         return out
 
