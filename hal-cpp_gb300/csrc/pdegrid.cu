@@ -300,14 +300,17 @@ namespace halcuda
         // The line-independent part of one sweep's Thomas solve.
         struct LinePlan64Dev
         {
-            const double *ws;  // elimination multipliers (index 0 unused)
-            const double *bs;  // modified diagonal
-            const double *zs;  // periodic: the Sherman-Morrison solution
-            double off;        // the off-diagonal -r/2
-            double vEnd;       // periodic: beta / gamma
-            double onePlusVz;  // periodic: 1 + (zs[0] + zs[L-1] * vEnd)
+            const double *ws;    // elimination multipliers (index 0 unused)
+            const double *bs;    // modified diagonal
+            const double *zs;    // periodic: the Sherman-Morrison solution
+            const double *rcHi;  // RN(1 / bs[i])
+            const double *rcLo;  // RN(1 / bs[i] - rcHi[i])
+            double off;          // the off-diagonal -r/2
+            double vEnd;         // periodic: beta / gamma
+            double onePlusVz;    // periodic: 1 + (zs[0] + zs[L-1] * vEnd)
             int32_t L;
             int32_t periodic;
+            int32_t fastDiv;     // every bs[i] in [2^-20, 2^20]: DivByPlan is exact
         };
 
         // ExplicitDiffusionY2ADI / X2ADI (src/Pde/ADIequations.cpp:19-47 and
@@ -347,110 +350,253 @@ namespace halcuda
             return DeltaTerm64(v, c, n, dim, wrap, base, stride, ghost, gi);
         }
 
-        // Back substitution of one line (thread) whose forward-eliminated
-        // right-hand side is in dS (element i at dS[i * lines + line]); the
-        // solution goes to out[i * lines + line].
-        __device__ __forceinline__ void BackSolve(const LinePlan64Dev &pl, const double *__restrict__ dS,
-                                                  double last, double *__restrict__ out, int32_t line, int32_t lines)
+        // n / b rounded to nearest, bit-equal to __ddiv_rn(n, b) for every n
+        // that PlanDivisionOutOfRange accepts, from the plan's reciprocal of
+        // b as a double-word: yHi = RN(1/b), yLo = RN(1/b - yHi).  q =
+        // RN(n*yHi + RN(n*yLo)) is within 1e-31 relative of n*(yHi + yLo)
+        // before its rounding, so it is one of the two doubles around n/b
+        // (faithful); its remainder n - b*q is then exact under an FMA, and
+        // RN(q + rem*yHi) is the correctly rounded quotient by Markstein's
+        // theorem (P. Markstein, "Computation of elementary functions on the
+        // IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990: y
+        // within half an ulp of 1/b, q within one ulp of n/b).  The argument
+        // needs no intermediate to underflow or overflow: the plan allows b
+        // in [2^-20, 2^20] only (fastDiv), and n must lie in [2^-900, 2^900)
+        // in magnitude.  n = +0 gives +0 (q = +0, rem = +0, for b > 0); n = -0
+        // would give +0 too, so PlanDivisionOutOfRange refuses it.  Four
+        // dependent FP64 operations instead of a division's longer sequence;
+        // hal_cuda_check_plan_division compares the two.
+        __device__ __forceinline__ double DivByPlan(double n, double b, double yHi, double yLo)
         {
-            const int32_t L = pl.L;
-            double x = __ddiv_rn(last, pl.bs[L - 1]);
-            out[static_cast<int64_t>(L - 1) * lines + line] = x;
-#pragma unroll 4
-            for (int32_t i = L - 2; i >= 0; i--)
+            const double t = __dmul_rn(n, yLo);
+            const double q = __fma_rn(n, yHi, t);
+            const double rem = __fma_rn(-b, q, n);
+            return __fma_rn(rem, yHi, q);
+        }
+
+        // Nonzero when DivByPlan may not be exact for the numerator n: -0,
+        // subnormal, nonzero below 2^-900 or from 2^900 in magnitude, inf or
+        // NaN.  Integer operations only, off the FP64 chain.
+        __device__ __forceinline__ uint32_t PlanDivisionOutOfRange(double n)
+        {
+            const uint32_t hi = static_cast<uint32_t>(__double2hiint(n));
+            const uint32_t e = (hi >> 20) & 0x7ffu;
+            const bool plusZero = (hi | static_cast<uint32_t>(__double2loint(n))) == 0u;
+            return ((e - 123u) > (1922u - 123u) && !plusZero) ? 1u : 0u;
+        }
+
+        // Right-hand side of one sweep at every cell (i, line) of lines laid
+        // out v[i * lines + line], one thread per cell: for the x-sweep
+        // ExplicitDiffusionY2ADI (ADIequations.h:316-324, Dirichlet :351-362),
+        // for the y-sweep ExplicitDiffusionX2ADI (ADIequations.h:325-336,
+        // Dirichlet :363-377) -- the cell plus half the rate times its two
+        // cross-axis differences, to line + 1 then line - 1 -- plus, with a
+        // ghost table, ImplicitBoundarySource along the line.  crossGhost[L +
+        // i] / crossGhost[i] are the ghosts beyond line lines-1 / line 0 of
+        // row i; alongLo[line] / alongLo[lines + line] those before element 0
+        // / after element L-1 of a line (null: zero-flux).
+        __global__ void AdiRhs64(const double *__restrict__ v, double *__restrict__ rhs, int32_t L, int32_t lines,
+                                 int32_t wrapCross, int32_t wrapAlong, const double *__restrict__ crossGhost,
+                                 const double *__restrict__ alongLo, double r)
+        {
+            const int32_t line = blockIdx.x * blockDim.x + threadIdx.x;
+            if (line >= lines)
             {
-                x = __ddiv_rn(__dsub_rn(dS[static_cast<int64_t>(i) * lines + line], __dmul_rn(pl.off, x)), pl.bs[i]);
-                out[static_cast<int64_t>(i) * lines + line] = x;
+                return;
+            }
+            for (int32_t i = blockIdx.y; i < L; i += gridDim.y)
+            {
+                const int64_t row = static_cast<int64_t>(i) * lines;
+                const double c = v[row + line];
+                double s = HalfStep(c, CrossDelta(v, c, line + 1, lines, wrapCross != 0, row, 1, crossGhost, L + i),
+                                    CrossDelta(v, c, line - 1, lines, wrapCross != 0, row, 1, crossGhost, i), r);
+                if (alongLo != nullptr)
+                {
+                    s = __dadd_rn(s, ImplicitSource(i, L, wrapAlong != 0, r, alongLo[line], alongLo[lines + line]));
+                }
+                rhs[row + line] = s;
+            }
+        }
+
+        constexpr int kChainFwd = 16;  // elements loaded ahead in the elimination
+        constexpr int kChainBwd = 8;   // ... and in the back substitution
+
+        // Thomas solve of one line per thread, TdmaSolver::TDMA
+        // (TdmaSolver.h:26-66) in its operations and order, over the
+        // right-hand sides in d (element i of a line at d[i * lines + line]):
+        // elimination in place, d[i] = d[i] - ws[i] * d[i - 1], then back
+        // substitution x[i] = (d[i] - off * x[i + 1]) / bs[i] into out.
+        // A warp's FP64 instruction costs tens of cycles on this part however
+        // many lanes it runs, and a line is one dependent chain, so the chain
+        // is all a thread does: AdiRhs64 computes the right-hand sides, the
+        // transposes apply the periodic correction, each loop loads the next
+        // batch of elements while it works on the current one, and the
+        // divisions use the plan's reciprocals (DivByPlan, FAST).  A periodic
+        // line (TDMAperiodic, TdmaSolver.h:96-119) leaves its factor (y0 +
+        // yL * vEnd) / (1 + vz) in factor[line].
+        template <bool FAST>
+        __global__ void __launch_bounds__(32) AdiChain64(double *__restrict__ d, double *__restrict__ out,
+                                                          LinePlan64Dev pl, int32_t lines,
+                                                          double *__restrict__ factor)
+        {
+            const int32_t line = blockIdx.x * blockDim.x + threadIdx.x;
+            if (line >= lines)
+            {
+                return;
+            }
+            const int32_t L = pl.L;
+            auto at = [&](int32_t i) { return static_cast<int64_t>(i) * lines + line; };
+
+            double rc[kChainFwd], wc[kChainFwd];
+#pragma unroll
+            for (int k = 0; k < kChainFwd; k++)
+            {
+                const int32_t i = min(k, L - 1);
+                rc[k] = __ldcg(d + at(i));
+                wc[k] = __ldg(pl.ws + i);
+            }
+            double prev = 0.0;
+            for (int32_t i0 = 0; i0 < L; i0 += kChainFwd)
+            {
+                double rn[kChainFwd], wn[kChainFwd];
+#pragma unroll
+                for (int k = 0; k < kChainFwd; k++)
+                {
+                    const int32_t i = min(i0 + kChainFwd + k, L - 1);
+                    rn[k] = __ldcg(d + at(i));
+                    wn[k] = __ldg(pl.ws + i);
+                }
+#pragma unroll
+                for (int k = 0; k < kChainFwd; k++)
+                {
+                    const int32_t i = i0 + k;
+                    if (i < L)
+                    {
+                        prev = (i == 0) ? rc[k] : __dsub_rn(rc[k], __dmul_rn(wc[k], prev));
+                        d[at(i)] = prev;
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < kChainFwd; k++)
+                {
+                    rc[k] = rn[k];
+                    wc[k] = wn[k];
+                }
+            }
+
+            // FAST: a numerator outside DivByPlan's range is only recorded
+            // here, and the line is solved again with IEEE divisions below
+            // (a test in the loop would put its branch on the chain)
+            uint32_t redo = 0;
+            double x = FAST ? DivByPlan(prev, pl.bs[L - 1], pl.rcHi[L - 1], pl.rcLo[L - 1])
+                            : __ddiv_rn(prev, pl.bs[L - 1]);
+            if (FAST)
+            {
+                redo |= PlanDivisionOutOfRange(prev);
+            }
+            out[at(L - 1)] = x;
+            double xLast = x;
+            double dc[kChainBwd], bc[kChainBwd], hc[kChainBwd], lc[kChainBwd];
+#pragma unroll
+            for (int k = 0; k < kChainBwd; k++)
+            {
+                const int32_t i = max(L - 2 - k, 0);
+                dc[k] = __ldcg(d + at(i));
+                bc[k] = __ldg(pl.bs + i);
+                hc[k] = FAST ? __ldg(pl.rcHi + i) : 0.0;
+                lc[k] = FAST ? __ldg(pl.rcLo + i) : 0.0;
+            }
+            for (int32_t i0 = L - 2; i0 >= 0; i0 -= kChainBwd)
+            {
+                double dn[kChainBwd], bn[kChainBwd], hn[kChainBwd], ln[kChainBwd];
+#pragma unroll
+                for (int k = 0; k < kChainBwd; k++)
+                {
+                    const int32_t i = max(i0 - kChainBwd - k, 0);
+                    dn[k] = __ldcg(d + at(i));
+                    bn[k] = __ldg(pl.bs + i);
+                    hn[k] = FAST ? __ldg(pl.rcHi + i) : 0.0;
+                    ln[k] = FAST ? __ldg(pl.rcLo + i) : 0.0;
+                }
+#pragma unroll
+                for (int k = 0; k < kChainBwd; k++)
+                {
+                    const int32_t i = i0 - k;
+                    if (i >= 0)
+                    {
+                        const double num = __dsub_rn(dc[k], __dmul_rn(pl.off, x));
+                        x = FAST ? DivByPlan(num, bc[k], hc[k], lc[k]) : __ddiv_rn(num, bc[k]);
+                        if (FAST)
+                        {
+                            redo |= PlanDivisionOutOfRange(num);
+                        }
+                        out[at(i)] = x;
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < kChainBwd; k++)
+                {
+                    dc[k] = dn[k];
+                    bc[k] = bn[k];
+                    hc[k] = hn[k];
+                    lc[k] = ln[k];
+                }
+            }
+            if (FAST && redo != 0)
+            {
+                x = __ddiv_rn(prev, pl.bs[L - 1]);
+                out[at(L - 1)] = x;
+                xLast = x;
+                for (int32_t i = L - 2; i >= 0; i--)
+                {
+                    x = __ddiv_rn(__dsub_rn(__ldcg(d + at(i)), __dmul_rn(pl.off, x)), pl.bs[i]);
+                    out[at(i)] = x;
+                }
             }
             if (pl.periodic)
             {
-                // TDMAperiodic (TdmaSolver.h:96-119): out = ys - factor * zs
-                const double y0 = out[line];
-                const double yL = out[static_cast<int64_t>(L - 1) * lines + line];
-                const double vy = __dadd_rn(y0, __dmul_rn(yL, pl.vEnd));
-                const double factor = __ddiv_rn(vy, pl.onePlusVz);
-                for (int32_t i = 0; i < L; i++)
-                {
-                    const int64_t k = static_cast<int64_t>(i) * lines + line;
-                    out[k] = __dsub_rn(out[k], __dmul_rn(factor, pl.zs[i]));
-                }
+                // x is now y0 (element 0), xLast yL (element L - 1)
+                const double vy = __dadd_rn(x, __dmul_rn(xLast, pl.vEnd));
+                factor[line] = __ddiv_rn(vy, pl.onePlusVz);
             }
         }
 
-        // x-sweep (ADIequations.h:316-324, Dirichlet :351-362): one thread per
-        // line y; element i of the line is the cell (i, y).  The right-hand
-        // side is ExplicitDiffusionY2ADI (+ the implicit boundary source);
-        // the solution goes to w in layout A (w[i * yDim + y]).
-        __global__ void AdiSweepX64(const double *__restrict__ f, double *__restrict__ dS, double *__restrict__ w,
-                                    LinePlan64Dev pl, int32_t xDim, int32_t yDim, int32_t wrapX, int32_t wrapY,
-                                    const double *__restrict__ ghost, double r)
+        // The sweeps' division (DivByPlan, or __ddiv_rn where
+        // PlanDivisionOutOfRange says so) against __ddiv_rn for every num[i]
+        // and den[j] (hi / lo: den's plan reciprocals); the count of
+        // differing bit patterns goes to *bad.
+        __global__ void CheckPlanDivision(const double *__restrict__ num, int64_t nNum, const double *__restrict__ den,
+                                          const double *__restrict__ hi, const double *__restrict__ lo, int32_t nDen,
+                                          unsigned long long *bad)
         {
-            const int32_t y = blockIdx.x * blockDim.x + threadIdx.x;
-            if (y >= yDim)
+            for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < nNum;
+                 i += static_cast<int64_t>(gridDim.x) * blockDim.x)
             {
-                return;
-            }
-            const double *gy = ghost ? ghost + 2 * yDim : nullptr;
-            const double lo = ghost ? ghost[y] : 0.0, hi = ghost ? ghost[yDim + y] : 0.0;
-            double prev = 0.0;
-#pragma unroll 4
-            for (int32_t i = 0; i < xDim; i++)
-            {
-                const int64_t row = static_cast<int64_t>(i) * yDim;
-                const double c = f[row + y];
-                double rhs = HalfStep(c, CrossDelta(f, c, y + 1, yDim, wrapY != 0, row, 1, gy, xDim + i),
-                                      CrossDelta(f, c, y - 1, yDim, wrapY != 0, row, 1, gy, i), r);
-                if (ghost != nullptr)
+                const double n = num[i];
+                unsigned long long c = 0;
+                for (int32_t j = 0; j < nDen; j++)
                 {
-                    rhs = __dadd_rn(rhs, ImplicitSource(i, xDim, wrapX != 0, r, lo, hi));
+                    const double a = __ddiv_rn(n, den[j]);
+                    const double b = PlanDivisionOutOfRange(n) ? __ddiv_rn(n, den[j]) : DivByPlan(n, den[j], hi[j], lo[j]);
+                    c += (__double_as_longlong(a) != __double_as_longlong(b)) ? 1ull : 0ull;
                 }
-                prev = (i == 0) ? rhs : __dsub_rn(rhs, __dmul_rn(pl.ws[i], prev));
-                dS[row + y] = prev;
-            }
-            BackSolve(pl, dS, prev, w, y, yDim);
-        }
-
-        // y-sweep (ADIequations.h:325-336, Dirichlet :363-377): one thread per
-        // line x over wB = w transposed (wB[i * xDim + x] = w(x, i)); the
-        // right-hand side is ExplicitDiffusionX2ADI of w (+ the implicit
-        // boundary source); the solution goes to vB[i * xDim + x].
-        __global__ void AdiSweepY64(const double *__restrict__ wB, double *__restrict__ dS, double *__restrict__ vB,
-                                    LinePlan64Dev pl, int32_t xDim, int32_t yDim, int32_t wrapX, int32_t wrapY,
-                                    const double *__restrict__ ghost, double r)
-        {
-            const int32_t x = blockIdx.x * blockDim.x + threadIdx.x;
-            if (x >= xDim)
-            {
-                return;
-            }
-            const double lo = ghost ? ghost[2 * yDim + x] : 0.0, hi = ghost ? ghost[2 * yDim + xDim + x] : 0.0;
-            double prev = 0.0;
-#pragma unroll 4
-            for (int32_t i = 0; i < yDim; i++)
-            {
-                const int64_t row = static_cast<int64_t>(i) * xDim;
-                const double c = wB[row + x];
-                // neighbours x+1 then x-1; ghost(x, y=i): bc(-1, i) at [i],
-                // bc(xDim, i) at [yDim + i]
-                double rhs = HalfStep(c, CrossDelta(wB, c, x + 1, xDim, wrapX != 0, row, 1, ghost, yDim + i),
-                                      CrossDelta(wB, c, x - 1, xDim, wrapX != 0, row, 1, ghost, i), r);
-                if (ghost != nullptr)
+                if (c != 0)
                 {
-                    rhs = __dadd_rn(rhs, ImplicitSource(i, yDim, wrapY != 0, r, lo, hi));
+                    atomicAdd(bad, c);
                 }
-                prev = (i == 0) ? rhs : __dsub_rn(rhs, __dmul_rn(pl.ws[i], prev));
-                dS[row + x] = prev;
             }
-            BackSolve(pl, dS, prev, vB, x, xDim);
         }
 
         // Tiled transpose of a rows x cols FP64 array: out[c * rows + r] =
         // in[r * cols + c].  With deltas, instead deltas[c * rows + r] +=
         // in[r * cols + c] - f[c * rows + r] (the y-sweep's commit into the
-        // deltas, ADIequations.h:331-335).
+        // deltas, ADIequations.h:331-335).  With fac, each input first takes
+        // the periodic correction of its line c at element r, in - fac[c] *
+        // zs[r] (TDMAperiodic's ys - factor * zs, TdmaSolver.h:115-118).
         template <bool COMMIT>
         __global__ void Transpose64(const double *__restrict__ in, double *__restrict__ out, int32_t rows,
-                                    int32_t cols, const double *__restrict__ f)
+                                    int32_t cols, const double *__restrict__ f, const double *__restrict__ fac,
+                                    const double *__restrict__ zs)
         {
             __shared__ double tile[32][33];
             const int32_t c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
@@ -459,7 +605,12 @@ namespace halcuda
                 const int32_t r = r0 + j, c = c0 + threadIdx.x;
                 if (r < rows && c < cols)
                 {
-                    tile[j][threadIdx.x] = in[static_cast<int64_t>(r) * cols + c];
+                    double v = in[static_cast<int64_t>(r) * cols + c];
+                    if (fac != nullptr)
+                    {
+                        v = __dsub_rn(v, __dmul_rn(fac[c], zs[r]));
+                    }
+                    tile[j][threadIdx.x] = v;
                 }
             }
             __syncthreads();
@@ -503,10 +654,47 @@ namespace halcuda
         // host, so each operation rounds as the reference's does.
         struct LinePlan64Host
         {
-            std::vector<double> ws, bs, zs;
+            std::vector<double> ws, bs, zs, rcHi, rcLo;
             double off = 0, vEnd = 0, onePlusVz = 0;
             bool periodic = false;
+            bool fastDiv = false;
         };
+
+        // 1/b as a double-word for DivByPlan: hi = RN(1/b); 1 - b*hi is
+        // exact under an FMA, so lo = RN((1 - b*hi) / b) = RN(1/b - hi).
+        void PlanReciprocal(double b, double *hi, double *lo)
+        {
+            *hi = 1.0 / b;
+            *lo = std::fma(-b, *hi, 1.0) / b;
+        }
+
+        // b in [2^-20, 2^20], where DivByPlan is exact for every n that
+        // PlanDivisionOutOfRange accepts (the matrices of a diffusion rate
+        // r >= 0 have diagonals of at least 1).
+        bool PlanDivisorInRange(double b)
+        {
+            return b >= 0x1p-20 && b <= 0x1p20;
+        }
+
+        // Reciprocals of the modified diagonal and whether DivByPlan may
+        // replace the back substitution's divisions.
+        void AddReciprocals(LinePlan64Host &p)
+        {
+            const size_t n = p.bs.size();
+            p.rcHi.assign(n, 0.0);
+            p.rcLo.assign(n, 0.0);
+            p.fastDiv = true;
+            for (size_t i = 0; i < n; i++)
+            {
+                p.fastDiv = p.fastDiv && PlanDivisorInRange(p.bs[i]);
+                PlanReciprocal(p.bs[i], &p.rcHi[i], &p.rcLo[i]);
+            }
+            if (!p.fastDiv)
+            {
+                std::fill(p.rcHi.begin(), p.rcHi.end(), 0.0);
+                std::fill(p.rcLo.begin(), p.rcLo.end(), 0.0);
+            }
+        }
 
         struct PlanCoeffs
         {
@@ -612,11 +800,13 @@ namespace halcuda
                 const double vz = p.zs[0] + p.zs[len - 1] * p.vEnd;
                 p.onePlusVz = 1 + vz;
                 p.periodic = true;
+                AddReciprocals(p);
                 return p;
             }
             k.endAdjust = dirichlet ? 1.0 : -1.0;
             Eliminate(k, p.ws, p.bs);
             p.zs.assign(static_cast<size_t>(len), 0.0);
+            AddReciprocals(p);
             return p;
         }
 
@@ -741,6 +931,7 @@ namespace halcuda
     struct Adi64::Impl
     {
         DevBuf<double> wA, wB, vB, dS;  // scratch (grown on first use)
+        DevBuf<double> fac;             // periodic factors of the current sweep's lines
         std::map<std::string, std::unique_ptr<PlanBuf64>> plans;
 
         int Ensure(DevBuf<double> &b, size_t n, cudaStream_t s, const char *what)
@@ -763,10 +954,12 @@ namespace halcuda
                 const LinePlan64Host h = BuildPlan64(L, r, wrap, dirichlet);
                 auto pb = std::make_unique<PlanBuf64>();
                 std::vector<double> all;
-                all.reserve(3 * static_cast<size_t>(L));
+                all.reserve(5 * static_cast<size_t>(L));
                 all.insert(all.end(), h.ws.begin(), h.ws.end());
                 all.insert(all.end(), h.bs.begin(), h.bs.end());
                 all.insert(all.end(), h.zs.begin(), h.zs.end());
+                all.insert(all.end(), h.rcHi.begin(), h.rcHi.end());
+                all.insert(all.end(), h.rcLo.begin(), h.rcLo.end());
                 HAL_TRY(pb->buf.Alloc(all.size(), "cudaMalloc(ADI plan)"));
                 HAL_TRY(CudaStatus(cudaMemcpy(pb->buf.p, all.data(), all.size() * sizeof(double),
                                               cudaMemcpyHostToDevice),
@@ -774,6 +967,9 @@ namespace halcuda
                 pb->dev.ws = pb->buf.p;
                 pb->dev.bs = pb->buf.p + L;
                 pb->dev.zs = pb->buf.p + 2 * static_cast<size_t>(L);
+                pb->dev.rcHi = pb->buf.p + 3 * static_cast<size_t>(L);
+                pb->dev.rcLo = pb->buf.p + 4 * static_cast<size_t>(L);
+                pb->dev.fastDiv = h.fastDiv ? 1 : 0;
                 pb->dev.off = h.off;
                 pb->dev.vEnd = h.vEnd;
                 pb->dev.onePlusVz = h.onePlusVz;
@@ -804,14 +1000,37 @@ namespace halcuda
         LinePlan64Dev px, py;
         HAL_TRY(m.Plan(xDim, r, wrapX != 0, g != nullptr, &px));
         HAL_TRY(m.Plan(yDim, r, wrapY != 0, g != nullptr, &py));
-        const int T = 32;  // one warp per block: the lines spread over the most SMs
-        AdiSweepX64<<<Blocks(yDim, T), T, 0, s>>>(f, m.dS.p, m.wA.p, px, xDim, yDim, wrapX, wrapY, g, r);
+        // per sweep: the right-hand sides on every SM, the chains one line
+        // per thread and one warp per block (the lines spread over the most
+        // SMs), then the transpose that applies the periodic correction
+        const size_t nFac = static_cast<size_t>(std::max(xDim, yDim));
+        HAL_TRY(m.Ensure(m.fac, nFac, s, "cudaMalloc(ADI scratch)"));
+        const int T = 32;
         const dim3 tb(32, 8);
-        Transpose64<false><<<dim3((yDim + 31) / 32, (xDim + 31) / 32), tb, 0, s>>>(m.wA.p, m.wB.p, xDim, yDim,
-                                                                                    nullptr);
-        AdiSweepY64<<<Blocks(xDim, T), T, 0, s>>>(m.wB.p, m.dS.p, m.vB.p, py, xDim, yDim, wrapX, wrapY, g, r);
-        Transpose64<true><<<dim3((xDim + 31) / 32, (yDim + 31) / 32), tb, 0, s>>>(m.vB.p, deltas, yDim, xDim, f);
-        CountLaunch(4);
+        const auto rhsGrid = [](int32_t lines, int32_t L) {
+            return dim3(Blocks(lines, 256), static_cast<unsigned>(std::min<int32_t>(std::max<int32_t>(L, 1), 65535)));
+        };
+        const auto chain = [&](const LinePlan64Dev &pl, int32_t lines, double *out) {
+            if (pl.fastDiv)
+            {
+                AdiChain64<true><<<Blocks(lines, T), T, 0, s>>>(m.dS.p, out, pl, lines, m.fac.p);
+            }
+            else
+            {
+                AdiChain64<false><<<Blocks(lines, T), T, 0, s>>>(m.dS.p, out, pl, lines, m.fac.p);
+            }
+        };
+        AdiRhs64<<<rhsGrid(yDim, xDim), 256, 0, s>>>(f, m.dS.p, xDim, yDim, wrapY, wrapX,
+                                                        g ? g + 2 * static_cast<size_t>(yDim) : nullptr, g, r);
+        chain(px, yDim, m.wA.p);
+        Transpose64<false><<<dim3((yDim + 31) / 32, (xDim + 31) / 32), tb, 0, s>>>(
+            m.wA.p, m.wB.p, xDim, yDim, nullptr, px.periodic ? m.fac.p : nullptr, px.zs);
+        AdiRhs64<<<rhsGrid(xDim, yDim), 256, 0, s>>>(m.wB.p, m.dS.p, yDim, xDim, wrapX, wrapY, g,
+                                                        g ? g + 2 * static_cast<size_t>(yDim) : nullptr, r);
+        chain(py, xDim, m.vB.p);
+        Transpose64<true><<<dim3((xDim + 31) / 32, (yDim + 31) / 32), tb, 0, s>>>(
+            m.vB.p, deltas, yDim, xDim, f, py.periodic ? m.fac.p : nullptr, py.zs);
+        CountLaunch(6);
         return LaunchStatus("DiffusionADI (FP64)");
     }
 }
@@ -1252,5 +1471,43 @@ extern "C" int hal_cuda_pdegrid_dims(hal_cuda_pdegrid *h, int32_t *dims)
     dims[2] = h->wrapX;
     dims[3] = h->wrapY;
     dims[4] = h->updateCt;
+    return HAL_CUDA_OK;
+}
+
+extern "C" int hal_cuda_check_plan_division(const double *num, int64_t nNum, const double *den, int32_t nDen,
+                                            int64_t *mismatches)
+{
+    using namespace halcuda;
+    HAL_REQUIRE(num != nullptr && den != nullptr && mismatches != nullptr,
+                "hal_cuda_check_plan_division: NULL argument");
+    HAL_REQUIRE(nNum >= 0 && nDen >= 0, "hal_cuda_check_plan_division: negative count");
+    std::vector<double> host(3 * static_cast<size_t>(nDen));
+    for (int32_t j = 0; j < nDen; j++)
+    {
+        HAL_REQUIRE(PlanDivisorInRange(den[j]),
+                    "hal_cuda_check_plan_division: divisor %d (%g) outside [2^-20, 2^20]", j, den[j]);
+        host[j] = den[j];
+        PlanReciprocal(den[j], &host[nDen + j], &host[2 * static_cast<size_t>(nDen) + j]);
+    }
+    HAL_TRY(CudaStatus(cudaSetDevice(CurrentDevice()), "cudaSetDevice"));
+    DevBuf<double> dNum, dDen;
+    DevBuf<unsigned long long> dBad;
+    HAL_TRY(dNum.Alloc(static_cast<size_t>(std::max<int64_t>(nNum, 1)), "cudaMalloc(division check)"));
+    HAL_TRY(dDen.Alloc(std::max<size_t>(host.size(), 1), "cudaMalloc(division check)"));
+    HAL_TRY(dBad.Alloc(1, "cudaMalloc(division check)"));
+    HAL_TRY(CudaStatus(cudaMemcpy(dNum.p, num, sizeof(double) * nNum, cudaMemcpyHostToDevice), "cudaMemcpy"));
+    HAL_TRY(CudaStatus(cudaMemcpy(dDen.p, host.data(), sizeof(double) * host.size(), cudaMemcpyHostToDevice),
+                       "cudaMemcpy"));
+    HAL_TRY(CudaStatus(cudaMemset(dBad.p, 0, sizeof(unsigned long long)), "cudaMemset"));
+    if (nNum > 0 && nDen > 0)
+    {
+        CheckPlanDivision<<<StrideBlocks(nNum), 256>>>(dNum.p, nNum, dDen.p, dDen.p + nDen,
+                                                       dDen.p + 2 * static_cast<size_t>(nDen), nDen, dBad.p);
+        CountLaunch();
+        HAL_TRY(LaunchStatus("CheckPlanDivision"));
+    }
+    unsigned long long bad = 0;
+    HAL_TRY(CudaStatus(cudaMemcpy(&bad, dBad.p, sizeof(bad), cudaMemcpyDeviceToHost), "cudaMemcpy"));
+    *mismatches = static_cast<int64_t>(bad);
     return HAL_CUDA_OK;
 }

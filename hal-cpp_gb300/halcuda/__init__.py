@@ -43,6 +43,7 @@ SIGNATURES = {
     "hal_cuda_advect_var_bc": (_I, [_vp, _vp, _vp, _vp, _vp, _i32, _i32, _vp, _vp, _vp]),
     "hal_cuda_stencil64_profile": (_I, [_vp, _i32, _i32, _f64, _f64, _i32, _i32, _vp]),
     "hal_cuda_fp64_issue_rate": (_I, [_vp]),
+    "hal_cuda_check_plan_division": (_I, [_vp, _i64, _vp, _i32, _vp]),
     "hal_cuda_diffusion_set_field": (_I, [_vp, _vp, _i64]),
     "hal_cuda_diffusion_get_field": (_I, [_vp, _vp, _i64]),
     "hal_cuda_diffusion_set_source": (_I, [_vp, _vp, _i64]),
@@ -231,6 +232,18 @@ def fp64_issue_rate() -> float:
     """Measured FP64 add issue rate of the current device (ops/s)."""
     v = ctypes.c_double()
     _check(lib().hal_cuda_fp64_issue_rate(ctypes.byref(v)), "fp64_issue_rate")
+    return v.value
+
+
+def check_plan_division(num, den) -> int:
+    """Pairs (num[i], den[j]) whose quotient by the FP64 ADI's division (a
+    double-word reciprocal and one Markstein correction) differs in any bit
+    from IEEE division on the device; every |den| must lie in [2^-20, 2^20]."""
+    n = np.ascontiguousarray(num, np.float64)
+    d = np.ascontiguousarray(den, np.float64)
+    v = ctypes.c_int64()
+    _check(lib().hal_cuda_check_plan_division(n.ctypes.data, n.size, d.ctypes.data, d.size, ctypes.byref(v)),
+           "check_plan_division")
     return v.value
 
 

@@ -29,6 +29,18 @@ int64_t hal_cuda_launch_count(void);
  * use it as their roofline. */
 int hal_cuda_fp64_issue_rate(double *opsPerSecond);
 
+/* Check of the FP64 ADI's division (DiffusionADI's back substitution,
+ * hal_cuda_pdegrid_diffusion_adi and the exact hal_cuda_adi calls): for every
+ * num[i] and den[j] the device divides once by IEEE division (__ddiv_rn) and
+ * once as the sweeps do -- from den's reciprocal as a double-word with one
+ * Markstein correction, with IEEE division for a numerator that is -0,
+ * subnormal, nonzero below 2^-900 or from 2^900 in magnitude, inf or NaN --
+ * and *mismatches receives the number of pairs whose bit patterns differ.
+ * Every den[j] must lie in [2^-20, 2^20], the range in which the sweeps use
+ * that division; host arrays. */
+int hal_cuda_check_plan_division(const double *num, int64_t nNum, const double *den, int32_t nDen,
+                                 int64_t *mismatches);
+
 /* ---- explicit diffusion -------------------------------------------------- */
 
 /* Profiling of the FP64 stencils above (zero-flux forms): average device time

@@ -171,6 +171,79 @@ def test_pdegrid_adi_1024_bit_exact(hal, oracle, wx, wy, dirichlet):
     assert np.abs(d).max() > 0
 
 
+def _plan_diagonals(r, n=64, end_adjust=-1.0):
+    """TdmaSolver::TDMA's modified diagonal of a line's ADI matrix
+    (off-diagonal -r/2, diagonal 1 - w * off, w = 2 + end_adjust at the
+    ends), in its operations."""
+    off = -r / 2.0
+    b = np.empty(n)
+    for i in range(n):
+        w = 2.0 + (end_adjust if i == 0 else 0.0) + (end_adjust if i == n - 1 else 0.0)
+        b[i] = 1 - w * off
+        if i > 0:
+            b[i] = b[i] - (off / b[i - 1]) * off
+    return b
+
+
+def test_adi_plan_division_matches_ieee(hal):
+    """The FP64 ADI's back substitution divides through the diagonal's
+    reciprocal (a double-word and one Markstein correction).  Its quotients
+    must equal IEEE division bit for bit: for numerators in the sweeps'
+    ranges, random bit patterns, signed zeros, subnormals, huge values,
+    infinities and NaN (for -0 and nonzero numerators outside [2^-900,
+    2^900) the sweeps solve the line again with IEEE divisions), and for
+    divisors from the plans' diagonals and across [2^-20, 2^20]."""
+    rng = np.random.default_rng(11)
+    m = 1 << 17
+    special = np.array([0.0, -0.0, 5e-324, -5e-324, 2.2250738585072014e-308, np.inf, -np.inf, np.nan,
+                        1.7976931348623157e308, -1.7976931348623157e308, np.ldexp(1.0, -900),
+                        np.ldexp(1.0, -900) * (1 - 2.0 ** -53), np.ldexp(1.0, 900), np.ldexp(1.0, 900) * (1 - 2.0 ** -53)])
+    num = np.concatenate([
+        rng.random(m) - 0.5,
+        rng.random(m) * 10.0,
+        np.ldexp(rng.random(m) + 0.5, rng.integers(-1000, 1000, m)) * rng.choice([-1.0, 1.0], m),
+        rng.integers(0, np.iinfo(np.uint64).max, m, dtype=np.uint64, endpoint=True).view(np.float64),
+        special,
+    ])
+    den = np.concatenate([
+        _plan_diagonals(0.1), _plan_diagonals(5.0), _plan_diagonals(5.0, end_adjust=1.0), _plan_diagonals(300.0),
+        np.ldexp(rng.random(32) + 1.0, rng.integers(-20, 20, 32)),
+        [1.0, 2.0 ** -20, 2.0 ** 20, 3.0, 1.0 + 2.0 ** -52],
+    ])
+    assert hal.check_plan_division(num, den) == 0
+    for bad in (2.0 ** 21, -1.0, 0.0):
+        with pytest.raises(ValueError):
+            hal.check_plan_division(num[:4], np.array([bad]))
+
+
+@pytest.mark.parametrize("wx,wy,dirichlet", [(0, 0, False), (1, 0, False), (0, 1, True)])
+def test_pdegrid_adi_extreme_values_bit_exact(hal, oracle, wx, wy, dirichlet):
+    """DiffusionADI on a field with a zero region, negative zeros, values
+    below 2^-900 and above 2^900 (the sweeps' fast division does not cover
+    those numerators; their lines are solved again with IEEE divisions)
+    equals the CPU's bit for bit, signs of zero included."""
+    from pyoracle import PDEScript
+
+    xd, yd = 300, 200
+    rng = np.random.default_rng(21 + wx + 2 * wy)
+    f0 = rng.random((xd, yd))
+    f0[:, :60] = 0.0
+    f0[100:140, 60:80] = -0.0
+    f0[150:170, :] = rng.random((20, yd)) * 1e-300
+    f0[200:205, 100:150] = 1e280
+    f0 = f0.ravel()
+    ghost = np.where(rng.random(2 * (xd + yd)) < 0.5, 0.0, rng.random(2 * (xd + yd))) if dirichlet else None
+    sc = PDEScript(xd, yd, wx, wy)
+    sc.add("adi_bc" if dirichlet else "adi", d0=3.0, arrays=[ghost] if dirichlet else None)
+    ef, ed, _, _ = oracle.pdegrid_script(sc, f0)
+    with hal.PDEGrid(xd, yd, wx, wy) as grid:
+        grid.set_state(f0)
+        grid.diffusion_adi(3.0, ghost=ghost)
+        f, d, _ = grid.get_state()
+    assert np.array_equal(f.view(np.uint64), ef.view(np.uint64))
+    assert np.array_equal(d.view(np.uint64), ed.view(np.uint64))
+
+
 def test_pdegrid_agent_operations(hal, oracle):
     """Each agent's Mul(Isq(), -uptake) from the agent handle's binning,
     and per-agent Add values, equal the same operations as a list in agent
