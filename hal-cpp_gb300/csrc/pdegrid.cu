@@ -28,6 +28,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <limits>
 #include <map>
 #include <memory>
@@ -303,8 +304,8 @@ namespace halcuda
             const double *ws;    // elimination multipliers (index 0 unused)
             const double *bs;    // modified diagonal
             const double *zs;    // periodic: the Sherman-Morrison solution
-            const double *rcHi;  // RN(1 / bs[i])
-            const double *rcLo;  // RN(1 / bs[i] - rcHi[i])
+            const double2 *bh;   // (bs[i], RN(1 / bs[i])): DivByPlan's b and yHi
+            const int2 *lo;      // RN(1 / bs[i]) - yHi as (FP32 mantissa bits, exponent)
             double off;          // the off-diagonal -r/2
             double vEnd;         // periodic: beta / gamma
             double onePlusVz;    // periodic: 1 + (zs[0] + zs[L-1] * vEnd)
@@ -350,28 +351,47 @@ namespace halcuda
             return DeltaTerm64(v, c, n, dim, wrap, base, stride, ghost, gi);
         }
 
+        // An approximation of n * yLo, for DivByPlan, without FP64
+        // instructions: yLo = mLo * 2^eLo with mLo an FP32 value in +-[1, 2]
+        // (0 for yLo = 0, with eLo very negative); n's top 20 mantissa bits
+        // times mLo in FP32, the exponents added as integers.  Within 1e-5
+        // of n * yLo relative, or 0 where n is +-0 or subnormal or the
+        // product is below 2^-1022.
+        __device__ __forceinline__ double ApproxTimesLo(double n, float mLo, int32_t eLo)
+        {
+            const uint32_t hi = static_cast<uint32_t>(__double2hiint(n));
+            const int32_t en = static_cast<int32_t>((hi >> 20) & 0x7ffu);
+            const float fn = __uint_as_float(0x3f800000u | ((hi & 0xfffffu) << 3));
+            const uint32_t pb = __float_as_uint(fn * mLo);
+            const int32_t te = en + eLo + static_cast<int32_t>((pb >> 23) & 0xffu) - 127;
+            const uint32_t tHi = ((hi ^ pb) & 0x80000000u) | (static_cast<uint32_t>(te) << 20) | ((pb & 0x7fffffu) >> 3);
+            const bool ok = te > 0 && en != 0;
+            return __hiloint2double(ok ? static_cast<int32_t>(tHi) : 0, ok ? static_cast<int32_t>(pb << 29) : 0);
+        }
+
         // n / b rounded to nearest, bit-equal to __ddiv_rn(n, b) for every n
         // that PlanDivisionOutOfRange accepts, from the plan's reciprocal of
-        // b as a double-word: yHi = RN(1/b), yLo = RN(1/b - yHi).  q =
-        // RN(n*yHi + RN(n*yLo)) is within 1e-31 relative of n*(yHi + yLo)
-        // before its rounding, so it is one of the two doubles around n/b
-        // (faithful); its remainder n - b*q is then exact under an FMA, and
-        // RN(q + rem*yHi) is the correctly rounded quotient by Markstein's
-        // theorem (P. Markstein, "Computation of elementary functions on the
-        // IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990: y
-        // within half an ulp of 1/b, q within one ulp of n/b).  The argument
-        // needs no intermediate to underflow or overflow: the plan allows b
-        // in [2^-20, 2^20] only (fastDiv), and n must lie in [2^-900, 2^900)
-        // in magnitude.  n = +0 gives +0 (q = +0, rem = +0, for b > 0); n = -0
-        // would give +0 too, so PlanDivisionOutOfRange refuses it.  Four
-        // dependent FP64 operations instead of a division's longer sequence;
-        // hal_cuda_check_plan_division compares the two.
-        __device__ __forceinline__ double DivByPlan(double n, double b, double yHi, double yLo)
+        // b as a double-word: yHi = RN(1/b) and yLo = RN(1/b - yHi) (|yLo| <=
+        // 2^-53 |yHi|).  With t within half of n*yLo (ApproxTimesLo's is
+        // within 1e-5), n*yHi + t is within 2^-54 |n/b| of n/b, so q =
+        // RN(n*yHi + t) is one of the two doubles around n/b (faithful); its
+        // remainder n - b*q is then exact under an FMA, and RN(q + rem*yHi)
+        // is the correctly rounded quotient by Markstein's theorem (P.
+        // Markstein, "Computation of elementary functions on the IBM RISC
+        // System/6000 processor", IBM J. Res. Dev. 34(1), 1990: y within half
+        // an ulp of 1/b, q within one ulp of n/b).  The argument needs no
+        // intermediate to underflow or overflow: the plan allows b in
+        // [2^-20, 2^20] only (fastDiv), and n must lie in [2^-900, 2^900) in
+        // magnitude.  n = +0 gives +0 (t = 0, q = +0, rem = +0, for b > 0);
+        // n = -0 would give +0 too, so PlanDivisionOutOfRange refuses it.
+        // Three dependent FP64 operations instead of a division's longer
+        // sequence; hal_cuda_check_plan_division compares the two.
+        __device__ __forceinline__ double DivByPlan(double n, double2 bh, int2 lo)
         {
-            const double t = __dmul_rn(n, yLo);
-            const double q = __fma_rn(n, yHi, t);
-            const double rem = __fma_rn(-b, q, n);
-            return __fma_rn(rem, yHi, q);
+            const double t = ApproxTimesLo(n, __int_as_float(lo.x), lo.y);
+            const double q = __fma_rn(n, bh.y, t);
+            const double rem = __fma_rn(-bh.x, q, n);
+            return __fma_rn(rem, bh.y, q);
         }
 
         // Nonzero when DivByPlan may not be exact for the numerator n: -0,
@@ -488,35 +508,36 @@ namespace halcuda
             // here, and the line is solved again with IEEE divisions below
             // (a test in the loop would put its branch on the chain)
             uint32_t redo = 0;
-            double x = FAST ? DivByPlan(prev, pl.bs[L - 1], pl.rcHi[L - 1], pl.rcLo[L - 1])
-                            : __ddiv_rn(prev, pl.bs[L - 1]);
+            double x = FAST ? DivByPlan(prev, pl.bh[L - 1], pl.lo[L - 1]) : __ddiv_rn(prev, pl.bs[L - 1]);
             if (FAST)
             {
                 redo |= PlanDivisionOutOfRange(prev);
             }
             out[at(L - 1)] = x;
             double xLast = x;
-            double dc[kChainBwd], bc[kChainBwd], hc[kChainBwd], lc[kChainBwd];
+            double dc[kChainBwd];
+            double2 bc[kChainBwd];
+            int2 lc[kChainBwd];
 #pragma unroll
             for (int k = 0; k < kChainBwd; k++)
             {
                 const int32_t i = max(L - 2 - k, 0);
                 dc[k] = __ldcg(d + at(i));
-                bc[k] = __ldg(pl.bs + i);
-                hc[k] = FAST ? __ldg(pl.rcHi + i) : 0.0;
-                lc[k] = FAST ? __ldg(pl.rcLo + i) : 0.0;
+                bc[k] = FAST ? __ldg(pl.bh + i) : make_double2(__ldg(pl.bs + i), 0.0);
+                lc[k] = FAST ? __ldg(pl.lo + i) : make_int2(0, 0);
             }
             for (int32_t i0 = L - 2; i0 >= 0; i0 -= kChainBwd)
             {
-                double dn[kChainBwd], bn[kChainBwd], hn[kChainBwd], ln[kChainBwd];
+                double dn[kChainBwd];
+                double2 bn[kChainBwd];
+                int2 ln[kChainBwd];
 #pragma unroll
                 for (int k = 0; k < kChainBwd; k++)
                 {
                     const int32_t i = max(i0 - kChainBwd - k, 0);
                     dn[k] = __ldcg(d + at(i));
-                    bn[k] = __ldg(pl.bs + i);
-                    hn[k] = FAST ? __ldg(pl.rcHi + i) : 0.0;
-                    ln[k] = FAST ? __ldg(pl.rcLo + i) : 0.0;
+                    bn[k] = FAST ? __ldg(pl.bh + i) : make_double2(__ldg(pl.bs + i), 0.0);
+                    ln[k] = FAST ? __ldg(pl.lo + i) : make_int2(0, 0);
                 }
 #pragma unroll
                 for (int k = 0; k < kChainBwd; k++)
@@ -525,7 +546,7 @@ namespace halcuda
                     if (i >= 0)
                     {
                         const double num = __dsub_rn(dc[k], __dmul_rn(pl.off, x));
-                        x = FAST ? DivByPlan(num, bc[k], hc[k], lc[k]) : __ddiv_rn(num, bc[k]);
+                        x = FAST ? DivByPlan(num, bc[k], lc[k]) : __ddiv_rn(num, bc[k].x);
                         if (FAST)
                         {
                             redo |= PlanDivisionOutOfRange(num);
@@ -538,7 +559,6 @@ namespace halcuda
                 {
                     dc[k] = dn[k];
                     bc[k] = bn[k];
-                    hc[k] = hn[k];
                     lc[k] = ln[k];
                 }
             }
@@ -563,11 +583,10 @@ namespace halcuda
 
         // The sweeps' division (DivByPlan, or __ddiv_rn where
         // PlanDivisionOutOfRange says so) against __ddiv_rn for every num[i]
-        // and den[j] (hi / lo: den's plan reciprocals); the count of
+        // and divisor j (bh[j], lo[j]: its plan entries); the count of
         // differing bit patterns goes to *bad.
-        __global__ void CheckPlanDivision(const double *__restrict__ num, int64_t nNum, const double *__restrict__ den,
-                                          const double *__restrict__ hi, const double *__restrict__ lo, int32_t nDen,
-                                          unsigned long long *bad)
+        __global__ void CheckPlanDivision(const double *__restrict__ num, int64_t nNum, const double2 *__restrict__ bh,
+                                          const int2 *__restrict__ lo, int32_t nDen, unsigned long long *bad)
         {
             for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < nNum;
                  i += static_cast<int64_t>(gridDim.x) * blockDim.x)
@@ -576,8 +595,8 @@ namespace halcuda
                 unsigned long long c = 0;
                 for (int32_t j = 0; j < nDen; j++)
                 {
-                    const double a = __ddiv_rn(n, den[j]);
-                    const double b = PlanDivisionOutOfRange(n) ? __ddiv_rn(n, den[j]) : DivByPlan(n, den[j], hi[j], lo[j]);
+                    const double a = __ddiv_rn(n, bh[j].x);
+                    const double b = PlanDivisionOutOfRange(n) ? __ddiv_rn(n, bh[j].x) : DivByPlan(n, bh[j], lo[j]);
                     c += (__double_as_longlong(a) != __double_as_longlong(b)) ? 1ull : 0ull;
                 }
                 if (c != 0)
@@ -654,18 +673,34 @@ namespace halcuda
         // host, so each operation rounds as the reference's does.
         struct LinePlan64Host
         {
-            std::vector<double> ws, bs, zs, rcHi, rcLo;
+            std::vector<double> ws, bs, zs;
+            std::vector<double2> bh;
+            std::vector<int2> lo;
             double off = 0, vEnd = 0, onePlusVz = 0;
             bool periodic = false;
             bool fastDiv = false;
         };
 
-        // 1/b as a double-word for DivByPlan: hi = RN(1/b); 1 - b*hi is
-        // exact under an FMA, so lo = RN((1 - b*hi) / b) = RN(1/b - hi).
-        void PlanReciprocal(double b, double *hi, double *lo)
+        // DivByPlan's entries for the divisor b: (b, hi) with hi = RN(1/b),
+        // and lo = RN(1/b - hi) as an FP32 mantissa in +-[1, 2) (its bits)
+        // and an exponent; 1 - b*hi is exact under an FMA, so lo = RN((1 -
+        // b*hi) / b).  A lo below 2^-200 |hi| counts as 0 (its product with
+        // any n is far below half an ulp of n/b).
+        void PlanReciprocal(double b, double2 *bh, int2 *lo)
         {
-            *hi = 1.0 / b;
-            *lo = std::fma(-b, *hi, 1.0) / b;
+            const double hi = 1.0 / b;
+            const double l = std::fma(-b, hi, 1.0) / b;
+            *bh = make_double2(b, hi);
+            *lo = make_int2(0, -4096);
+            if (l != 0.0 && std::fabs(l) >= std::ldexp(std::fabs(hi), -200))
+            {
+                int e = 0;
+                const double fr = std::frexp(l, &e);  // l = fr * 2^e, |fr| in [0.5, 1)
+                const float m = static_cast<float>(fr * 2.0);
+                int32_t bits = 0;
+                std::memcpy(&bits, &m, sizeof(bits));
+                *lo = make_int2(bits, e - 1);
+            }
         }
 
         // b in [2^-20, 2^20], where DivByPlan is exact for every n that
@@ -681,18 +716,16 @@ namespace halcuda
         void AddReciprocals(LinePlan64Host &p)
         {
             const size_t n = p.bs.size();
-            p.rcHi.assign(n, 0.0);
-            p.rcLo.assign(n, 0.0);
+            p.bh.assign(n, make_double2(0.0, 0.0));
+            p.lo.assign(n, make_int2(0, 0));
             p.fastDiv = true;
             for (size_t i = 0; i < n; i++)
             {
                 p.fastDiv = p.fastDiv && PlanDivisorInRange(p.bs[i]);
-                PlanReciprocal(p.bs[i], &p.rcHi[i], &p.rcLo[i]);
             }
-            if (!p.fastDiv)
+            for (size_t i = 0; p.fastDiv && i < n; i++)
             {
-                std::fill(p.rcHi.begin(), p.rcHi.end(), 0.0);
-                std::fill(p.rcLo.begin(), p.rcLo.end(), 0.0);
+                PlanReciprocal(p.bs[i], &p.bh[i], &p.lo[i]);
             }
         }
 
@@ -953,22 +986,23 @@ namespace halcuda
             {
                 const LinePlan64Host h = BuildPlan64(L, r, wrap, dirichlet);
                 auto pb = std::make_unique<PlanBuf64>();
-                std::vector<double> all;
-                all.reserve(5 * static_cast<size_t>(L));
-                all.insert(all.end(), h.ws.begin(), h.ws.end());
-                all.insert(all.end(), h.bs.begin(), h.bs.end());
-                all.insert(all.end(), h.zs.begin(), h.zs.end());
-                all.insert(all.end(), h.rcHi.begin(), h.rcHi.end());
-                all.insert(all.end(), h.rcLo.begin(), h.rcLo.end());
+                // layout (in doubles): bh [2L], lo [L], ws [L], bs [L], zs [L]
+                const size_t Ls = static_cast<size_t>(L);
+                std::vector<double> all(6 * Ls, 0.0);
+                std::memcpy(all.data(), h.bh.data(), sizeof(double2) * Ls);
+                std::memcpy(all.data() + 2 * Ls, h.lo.data(), sizeof(int2) * Ls);
+                std::copy(h.ws.begin(), h.ws.end(), all.begin() + 3 * Ls);
+                std::copy(h.bs.begin(), h.bs.end(), all.begin() + 4 * Ls);
+                std::copy(h.zs.begin(), h.zs.end(), all.begin() + 5 * Ls);
                 HAL_TRY(pb->buf.Alloc(all.size(), "cudaMalloc(ADI plan)"));
                 HAL_TRY(CudaStatus(cudaMemcpy(pb->buf.p, all.data(), all.size() * sizeof(double),
                                               cudaMemcpyHostToDevice),
                                    "cudaMemcpy(ADI plan)"));
-                pb->dev.ws = pb->buf.p;
-                pb->dev.bs = pb->buf.p + L;
-                pb->dev.zs = pb->buf.p + 2 * static_cast<size_t>(L);
-                pb->dev.rcHi = pb->buf.p + 3 * static_cast<size_t>(L);
-                pb->dev.rcLo = pb->buf.p + 4 * static_cast<size_t>(L);
+                pb->dev.bh = reinterpret_cast<const double2 *>(pb->buf.p);
+                pb->dev.lo = reinterpret_cast<const int2 *>(pb->buf.p + 2 * Ls);
+                pb->dev.ws = pb->buf.p + 3 * Ls;
+                pb->dev.bs = pb->buf.p + 4 * Ls;
+                pb->dev.zs = pb->buf.p + 5 * Ls;
                 pb->dev.fastDiv = h.fastDiv ? 1 : 0;
                 pb->dev.off = h.off;
                 pb->dev.vEnd = h.vEnd;
@@ -1481,28 +1515,32 @@ extern "C" int hal_cuda_check_plan_division(const double *num, int64_t nNum, con
     HAL_REQUIRE(num != nullptr && den != nullptr && mismatches != nullptr,
                 "hal_cuda_check_plan_division: NULL argument");
     HAL_REQUIRE(nNum >= 0 && nDen >= 0, "hal_cuda_check_plan_division: negative count");
-    std::vector<double> host(3 * static_cast<size_t>(nDen));
+    std::vector<double2> bh(static_cast<size_t>(nDen));
+    std::vector<int2> lo(static_cast<size_t>(nDen));
     for (int32_t j = 0; j < nDen; j++)
     {
         HAL_REQUIRE(PlanDivisorInRange(den[j]),
                     "hal_cuda_check_plan_division: divisor %d (%g) outside [2^-20, 2^20]", j, den[j]);
-        host[j] = den[j];
-        PlanReciprocal(den[j], &host[nDen + j], &host[2 * static_cast<size_t>(nDen) + j]);
+        PlanReciprocal(den[j], &bh[j], &lo[j]);
     }
     HAL_TRY(CudaStatus(cudaSetDevice(CurrentDevice()), "cudaSetDevice"));
-    DevBuf<double> dNum, dDen;
+    DevBuf<double> dNum;
+    DevBuf<double2> dBh;
+    DevBuf<int2> dLo;
     DevBuf<unsigned long long> dBad;
     HAL_TRY(dNum.Alloc(static_cast<size_t>(std::max<int64_t>(nNum, 1)), "cudaMalloc(division check)"));
-    HAL_TRY(dDen.Alloc(std::max<size_t>(host.size(), 1), "cudaMalloc(division check)"));
+    HAL_TRY(dBh.Alloc(static_cast<size_t>(std::max<int32_t>(nDen, 1)), "cudaMalloc(division check)"));
+    HAL_TRY(dLo.Alloc(static_cast<size_t>(std::max<int32_t>(nDen, 1)), "cudaMalloc(division check)"));
     HAL_TRY(dBad.Alloc(1, "cudaMalloc(division check)"));
     HAL_TRY(CudaStatus(cudaMemcpy(dNum.p, num, sizeof(double) * nNum, cudaMemcpyHostToDevice), "cudaMemcpy"));
-    HAL_TRY(CudaStatus(cudaMemcpy(dDen.p, host.data(), sizeof(double) * host.size(), cudaMemcpyHostToDevice),
+    HAL_TRY(CudaStatus(cudaMemcpy(dBh.p, bh.data(), sizeof(double2) * bh.size(), cudaMemcpyHostToDevice),
+                       "cudaMemcpy"));
+    HAL_TRY(CudaStatus(cudaMemcpy(dLo.p, lo.data(), sizeof(int2) * lo.size(), cudaMemcpyHostToDevice),
                        "cudaMemcpy"));
     HAL_TRY(CudaStatus(cudaMemset(dBad.p, 0, sizeof(unsigned long long)), "cudaMemset"));
     if (nNum > 0 && nDen > 0)
     {
-        CheckPlanDivision<<<StrideBlocks(nNum), 256>>>(dNum.p, nNum, dDen.p, dDen.p + nDen,
-                                                       dDen.p + 2 * static_cast<size_t>(nDen), nDen, dBad.p);
+        CheckPlanDivision<<<StrideBlocks(nNum), 256>>>(dNum.p, nNum, dBh.p, dLo.p, nDen, dBad.p);
         CountLaunch();
         HAL_TRY(LaunchStatus("CheckPlanDivision"));
     }
