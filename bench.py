@@ -615,6 +615,55 @@ def secondary_stencil64(hal, torch, stream, iters=20):
                     "(wall clock, copies in and out); cpu = the oracle, 1 thread"}
 
 
+def secondary_pdegrid_adi(hal, torch, stream, warm=2, iters=10):
+    """The FP64 DiffusionADI tick of the device-resident PDEGrid2D
+    (DiffusionADI + MulAll + Update, bit-identical to the reference's
+    PDEGrid2D) on a 2048^2 zero-flux grid, beside the CPU oracle's FP64 ADI
+    step on the same field.  Each line's Thomas solve is one dependent FP64
+    chain, and a warp's FP64 instruction takes 64 cycles on GB300, so the
+    chains are bound by L x 7 FP64 instructions x 64 cycles per sweep."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    pyoracle.build(ref=False)
+    rng = np.random.default_rng(14)
+    f0 = rng.random(CELLS)
+    with hal.PDEGrid(N, N) as g:
+        g.set_stream(stream.cuda_stream)
+        g.set_state(f0)
+
+        def tick():
+            g.diffusion_adi(5.0)
+            g.apply_all(2, -0.01)  # HAL_CUDA_CELL_MUL
+            g.update()
+
+        for _ in range(warm):
+            tick()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record()
+            for _ in range(iters):
+                tick()
+            e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / iters
+    t0 = time.perf_counter()
+    pyoracle.Oracle.diffuse_adi(f0, np.zeros(CELLS), 5.0, N, N, False, False)
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    sm_hz = 2.07e9
+    chain_floor_ms = 2 * N * 7 * 64 / sm_hz * 1e3
+    return {"workload": "pdegrid-fp64-adi-2048x2048-r5-zeroflux (DiffusionADI + MulAll + Update)",
+            "ms_per_tick": ms, "value": CELLS / (ms * 1e-3), "unit": "cell-updates/s",
+            "cpu_oracle_adi_ms": cpu_ms, "cpu_cores": 1,
+            "speedup_vs_cpu_adi_step": cpu_ms / ms,
+            "chain_bound": {"bound": "fp64 issue of one warp (64 cycles per instruction)",
+                            "fp64_instructions_per_element": 7, "floor_ms_per_tick_at_2070_mhz": chain_floor_ms,
+                            "frac_of_tick": chain_floor_ms / ms},
+            "note": "FP64, bit-identical to the reference's PDEGrid2D; the CPU figure is the oracle's "
+                    "DiffusionADI step alone (1 thread)"}
+
+
 def secondary_interface_calls(timeout=600):
     """Per-call times of Diffuse, DiffuseADI and AccumulateForces through the
     C++ backend classes on host std::vector<double> data (upload, kernels and
@@ -775,6 +824,7 @@ def profile_case(case, n, iters):
         wells 0 K      K batched ticks of the 512 wells
         adjoint N K    one gradient of K steps, checkpoints every 10
         coupled N K    K coupled ticks (agent step + ADI tick with uptake)
+        pdegrid_adi N K  K FP64 PDEGrid2D ticks (DiffusionADI + MulAll + Update)
     """
     import halcuda as hal
     from halcuda import workloads
@@ -884,6 +934,16 @@ def profile_case(case, n, iters):
             a.sync()
             ag.set_stream(None)
         print(f"coupled {agents} agents in {n}^2: {iters + 1} ticks")
+    elif case == "pdegrid_adi":
+        rng = np.random.default_rng(14)
+        with hal.PDEGrid(n, n) as g:
+            g.set_state(rng.random(n * n))
+            for _ in range(iters + 1):
+                g.diffusion_adi(5.0)
+                g.apply_all(2, -0.01)  # HAL_CUDA_CELL_MUL
+                g.update()
+            g.get_state()
+        print(f"pdegrid FP64 ADI {n}^2: {iters + 1} ticks")
     else:
         raise SystemExit(f"unknown profile case {case}")
     return 0
@@ -899,7 +959,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-case", default=None,
                     help="run one small fixed case for an ncu capture instead of the benchmark "
-                         "(adi, explicit, agents, stencil64, wells, adjoint, coupled)")
+                         "(adi, explicit, agents, stencil64, wells, adjoint, coupled, pdegrid_adi)")
     ap.add_argument("--profile-size", type=int, default=2048, help="grid side of the profile case")
     ap.add_argument("--profile-iters", type=int, default=3, help="launch iterations of the profile case")
     args = ap.parse_args()
@@ -1027,6 +1087,7 @@ def main():
                      "wells": secondary_wells(hal, torch, stream),
                      "adjoint": secondary_adjoint(hal),
                      "stencil64": secondary_stencil64(hal, torch, stream),
+                     "pdegrid_adi": secondary_pdegrid_adi(hal, torch, stream),
                      "interface_calls": secondary_interface_calls()}
 
     cpu = None
