@@ -145,6 +145,11 @@ namespace Hal::Cuda
                                  bool                       wrapY,
                                  const std::vector<double> &ghost);
 
+        // exact: DiffuseADI and DiffuseADIDirichlet solve every size in
+        // FP64, bit-exact to CpuAdiDiffusionBackend2D (default false: FP32
+        // for sides up to HAL_CUDA_ADI_MAX_LINE).
+        void SetExact(bool exact);
+
         // Device-resident PDEGrid2D::DiffusionADI tick:
         // f' = ADI(f) - decay f + src - uptake * (agents in the cell) * f.
         void SetField(const std::vector<float> &field);

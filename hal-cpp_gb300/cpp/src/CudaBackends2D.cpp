@@ -245,6 +245,11 @@ namespace Hal::Cuda
               "CudaAdiDiffusionBackend2D::GetField");
     }
 
+    void CudaAdiDiffusionBackend2D::SetExact(bool exact)
+    {
+        Check(hal_cuda_adi_set_exact(m_pHandle, exact ? 1 : 0), "CudaAdiDiffusionBackend2D::SetExact");
+    }
+
     void CudaAdiDiffusionBackend2D::SetSource(const std::vector<float> &dense)
     {
         Check(hal_cuda_adi_set_source(m_pHandle, dense.empty() ? nullptr : dense.data(),

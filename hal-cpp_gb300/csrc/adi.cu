@@ -1596,6 +1596,7 @@ namespace halcuda
         // takes: the FP64 Thomas solve per line, with its ghost table in FP64
         std::unique_ptr<Adi64> adi64;
         DevBuf<double> g64;
+        bool exact = false;      // hal_cuda_adi_set_exact: the FP64 solve at every size
         DevBuf<int32_t> err;
         // set once a bounded device wait has given up: the sweep that gave
         // up left its lines undefined, so the handle takes no further ticks
@@ -2100,10 +2101,11 @@ namespace
             HAL_TRY(h->g32.Alloc(2 * (static_cast<size_t>(h->xDim) + h->yDim), "cudaMalloc(ghost)"));
         }
         cudaStream_t s = h->stream.Get();
-        if (h->xDim > HAL_CUDA_ADI_MAX_LINE || h->yDim > HAL_CUDA_ADI_MAX_LINE)
+        if (h->exact || h->xDim > HAL_CUDA_ADI_MAX_LINE || h->yDim > HAL_CUDA_ADI_MAX_LINE)
         {
-            // lines beyond the FP32 partitioned solve: the FP64 Thomas solve
-            // per line, in the CPU backend's operation order (bit-exact)
+            // exact mode, or lines beyond the FP32 partitioned solve: the
+            // FP64 Thomas solve per line, in the CPU backend's operation
+            // order (bit-exact)
             if (h->adi64 == nullptr)
             {
                 h->adi64.reset(new (std::nothrow) Adi64());
@@ -2336,6 +2338,13 @@ extern "C" int hal_cuda_adi_sync(hal_cuda_adi *h)
 extern "C" void *hal_cuda_adi_stream(hal_cuda_adi *h)
 {
     return h ? static_cast<void *>(h->stream.Get()) : nullptr;
+}
+
+extern "C" int hal_cuda_adi_set_exact(hal_cuda_adi *h, int32_t exact)
+{
+    HAL_REQUIRE(h != nullptr, "hal_cuda_adi_set_exact: handle is NULL");
+    h->exact = exact != 0;
+    return HAL_CUDA_OK;
 }
 
 extern "C" int hal_cuda_adi_set_stream(hal_cuda_adi *h, void *stream)

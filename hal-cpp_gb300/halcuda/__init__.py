@@ -83,6 +83,7 @@ SIGNATURES = {
     "hal_cuda_adi_profile": (_I, [_vp, _i32, _f64, _f64, _i32, _i32, _vp]),
     "hal_cuda_adi_sync": (_I, [_vp]),
     "hal_cuda_adi_stream": (_vp, [_vp]),
+    "hal_cuda_adi_set_exact": (_I, [_vp, _i32]),
     "hal_cuda_adi_set_stream": (_I, [_vp, _vp]),
     "hal_cuda_agents_create": (_I, [_i32, _i32, _i32, _vp]),
     "hal_cuda_agents_destroy": (_I, [_vp]),
@@ -481,6 +482,12 @@ class Adi(_Handle):
         _check(lib().hal_cuda_diffuse_adi(self._h, _p(f), f.size, _p(d), d.size, diffRate, xDim,
                                           yDim, int(wrapX), int(wrapY)), "diffuse_adi")
         return d
+
+    def set_exact(self, exact=True):
+        """Interface calls (diffuse_adi, diffuse_adi_bc) in FP64 at every
+        size, bit-exact to the CPU backend (default: FP32 up to
+        HAL_CUDA_ADI_MAX_LINE)."""
+        _check(lib().hal_cuda_adi_set_exact(self._h, int(bool(exact))), "adi_set_exact")
 
     def diffuse_adi_bc(self, field, deltas, diffRate, wrapX, wrapY, ghost):
         f = _f64(field)

@@ -222,6 +222,14 @@ int hal_cuda_diffuse_adi(hal_cuda_adi *h, const double *field, int64_t fieldLen,
 int hal_cuda_diffuse_adi_bc(hal_cuda_adi *h, const double *field, double *deltas,
                             double diffRate, int32_t wrapX, int32_t wrapY, const double *ghost);
 
+/* Exact mode of the two interface calls above (no reference counterpart: a
+ * choice of this backend).  With exact nonzero, hal_cuda_diffuse_adi and
+ * _adi_bc solve every size with the FP64 Thomas solve per line, bit-exact to
+ * the CPU backend (CpuAdiDiffusionBackend2D); 0, the default, keeps the FP32
+ * partitioned solve for sides up to HAL_CUDA_ADI_MAX_LINE.  The resident
+ * ticks are not affected. */
+int hal_cuda_adi_set_exact(hal_cuda_adi *h, int32_t exact);
+
 /* Resident field and per-tick terms, as for the explicit handle. */
 int hal_cuda_adi_set_field(hal_cuda_adi *h, const float *field, int64_t len);
 int hal_cuda_adi_get_field(hal_cuda_adi *h, float *field, int64_t len);

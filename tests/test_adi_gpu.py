@@ -281,6 +281,33 @@ def test_lines_above_max_through_the_interface(hal, oracle, xd, yd, wx, wy, diri
             a.run_ticks(1, 3.0, 0.0)
 
 
+@pytest.mark.parametrize("xd,yd,wx,wy,dirichlet", [(512, 384, False, False, False), (300, 257, True, True, False),
+                                                   (640, 96, False, True, True), (129, 1024, True, False, True)])
+def test_exact_mode_interface_bit_exact(hal, oracle, xd, yd, wx, wy, dirichlet):
+    """With set_exact, DiffuseADI and its Dirichlet form solve every size in
+    FP64, Thomas per line in the CPU backend's order: the deltas equal the
+    CPU's bit for bit (without it these sizes take the FP32 solve)."""
+    rng = np.random.default_rng(xd * 3 + yd)
+    f = rng.random(xd * yd)
+    d = (rng.random(xd * yd) - 0.5) * 0.1
+    ghost = rng.random(2 * (xd + yd)) if dirichlet else None
+    with hal.Adi(xd, yd) as a:
+        a.set_exact(True)
+        if dirichlet:
+            got = a.diffuse_adi_bc(f, d.copy(), 4.0, wx, wy, ghost)
+        else:
+            got = a.diffuse_adi(f, d.copy(), 4.0, xd, yd, wx, wy)
+        exp = oracle.diffuse_adi(f, d, 4.0, xd, yd, wx, wy, ghost=ghost)
+        assert np.array_equal(got.view(np.uint64), exp.view(np.uint64))
+        a.set_exact(False)
+        if dirichlet:
+            fp32 = a.diffuse_adi_bc(f, d.copy(), 4.0, wx, wy, ghost)
+        else:
+            fp32 = a.diffuse_adi(f, d.copy(), 4.0, xd, yd, wx, wy)
+        assert not np.array_equal(fp32, exp)
+        assert _step_err(fp32, exp, f) <= TOL(4.0)
+
+
 def test_rejects_bad_sizes(hal):
     with hal.Adi(4, 4) as a:
         with pytest.raises(ValueError):
