@@ -83,6 +83,10 @@ int main()
             [&] { oracle_adi2(f.data(), scratch.data(), dc.data(), 0.8, n, n, 1, 1, nullptr); }, reps);
         std::snprintf(size, sizeof(size), "%dx%d", n, n);
         Line("DiffuseADI", size, tc, tg, "cell_updates", static_cast<double>(n) * n);
+        // the same call in exact mode (FP64 Thomas per line, bit-exact)
+        gpu.SetExact(true);
+        const double te = Seconds([&] { gpu.DiffuseADI(f, dg, 0.8, n, n, true, true); }, reps);
+        Line("DiffuseADI (exact)", size, tc, te, "cell_updates", static_cast<double>(n) * n);
     }
     for (int32_t agents : {1000, 10000, 50000, 200000})
     {
