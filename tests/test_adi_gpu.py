@@ -282,7 +282,10 @@ def test_lines_above_max_through_the_interface(hal, oracle, xd, yd, wx, wy, diri
 
 
 @pytest.mark.parametrize("xd,yd,wx,wy,dirichlet", [(512, 384, False, False, False), (300, 257, True, True, False),
-                                                   (640, 96, False, True, True), (129, 1024, True, False, True)])
+                                                   (640, 96, False, True, True), (129, 1024, True, False, True),
+                                                   (1, 7, False, False, False), (7, 1, True, True, False),
+                                                   (2, 3, True, True, False), (3, 2, False, False, True),
+                                                   (1, 1, False, False, True), (17, 33, True, False, False)])
 def test_exact_mode_interface_bit_exact(hal, oracle, xd, yd, wx, wy, dirichlet):
     """With set_exact, DiffuseADI and its Dirichlet form solve every size in
     FP64, Thomas per line in the CPU backend's order: the deltas equal the
@@ -299,6 +302,8 @@ def test_exact_mode_interface_bit_exact(hal, oracle, xd, yd, wx, wy, dirichlet):
             got = a.diffuse_adi(f, d.copy(), 4.0, xd, yd, wx, wy)
         exp = oracle.diffuse_adi(f, d, 4.0, xd, yd, wx, wy, ghost=ghost)
         assert np.array_equal(got.view(np.uint64), exp.view(np.uint64))
+        if xd * yd < 4096:
+            return
         a.set_exact(False)
         if dirichlet:
             fp32 = a.diffuse_adi_bc(f, d.copy(), 4.0, wx, wy, ghost)
