@@ -137,6 +137,23 @@ namespace halcuda
             }
         }
 
+        // A value-form SetAll / AddAll / MulAll deferred to the Update right
+        // after it, in one pass: deltas = op(deltas, field, value), then
+        // field += deltas and deltas = 0, the two kernels' operations in
+        // their order.
+        __global__ void ApplyAllCommit(int op, double value, int64_t n, double *__restrict__ f,
+                                       double *__restrict__ deltas)
+        {
+            for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+                 i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+            {
+                const double fi = f[i];
+                const double d = ApplyOp(op, deltas[i], fi, value);
+                f[i] = __dadd_rn(fi, d);
+                deltas[i] = 0.0;
+            }
+        }
+
         // SetNonNegative (PDEGrid2D.h:244-255): Set(i, 0) where f + d < 0.
         __global__ void NonNegative(int64_t n, const double *__restrict__ f, double *__restrict__ deltas)
         {
@@ -855,6 +872,10 @@ namespace halcuda
         int32_t xDim = 0, yDim = 0;
         int32_t wrapX = 0, wrapY = 0;
         int32_t updateCt = 0;
+        // a value-form *All call not yet run (see Prepare)
+        bool pendingAll = false;
+        int32_t pendingOp = 0;
+        double pendingValue = 0.0;
         int device = 0;
         StreamSlot stream;
         DevBuf<double> f, d;
@@ -1078,10 +1099,23 @@ namespace
     using halcuda::CudaStatus;
     using halcuda::LaunchStatus;
 
-    int Prepare(hal_cuda_pdegrid *h, const char *who)
+    // Every entry point starts here.  A pending value-form *All call
+    // (hal_cuda_pdegrid_apply_all) runs first, unless the caller is the
+    // Update that takes it over (flush false).
+    int Prepare(hal_cuda_pdegrid *h, const char *who, bool flush = true)
     {
         HAL_REQUIRE(h != nullptr, "%s: handle is NULL", who);
-        return CudaStatus(cudaSetDevice(h->device), "cudaSetDevice");
+        HAL_TRY(CudaStatus(cudaSetDevice(h->device), "cudaSetDevice"));
+        if (flush && h->pendingAll)
+        {
+            h->pendingAll = false;
+            const int64_t n = h->Length();
+            halcuda::ApplyAll<<<halcuda::StrideBlocks(n), 256, 0, h->stream.Get()>>>(
+                h->pendingOp, h->pendingValue, nullptr, n, h->f.p, h->d.p);
+            halcuda::CountLaunch();
+            HAL_TRY(LaunchStatus(who));
+        }
+        return HAL_CUDA_OK;
     }
 }
 
@@ -1258,23 +1292,37 @@ extern "C" int hal_cuda_pdegrid_apply_all(hal_cuda_pdegrid *h, int32_t op, doubl
     HAL_REQUIRE(op >= HAL_CUDA_CELL_SET && op <= HAL_CUDA_CELL_SCALE, "%s: unknown operation %d", who, op);
     cudaStream_t s = h->stream.Get();
     const int64_t n = h->Length();
-    const double *pc = nullptr;
-    if (perCell != nullptr)
+    if (perCell == nullptr)
     {
-        HAL_TRY(h->Upload(h->a0, perCell, static_cast<size_t>(n), "cudaMemcpy(values)"));
-        pc = h->a0.p;
+        // deferred: the next call runs it first, and an Update right after
+        // it runs it in its own pass (ApplyAllCommit)
+        h->pendingAll = true;
+        h->pendingOp = op;
+        h->pendingValue = value;
+        return HAL_CUDA_OK;
     }
+    HAL_TRY(h->Upload(h->a0, perCell, static_cast<size_t>(n), "cudaMemcpy(values)"));
+    const double *pc = h->a0.p;
     halcuda::ApplyAll<<<halcuda::StrideBlocks(n), 256, 0, s>>>(op, value, pc, n, h->f.p, h->d.p);
     halcuda::CountLaunch();
     HAL_TRY(LaunchStatus(who));
-    return perCell != nullptr ? h->Sync(who) : HAL_CUDA_OK;
+    return h->Sync(who);
 }
 
 extern "C" int hal_cuda_pdegrid_update(hal_cuda_pdegrid *h)
 {
-    HAL_TRY(Prepare(h, "hal_cuda_pdegrid_update"));
+    HAL_TRY(Prepare(h, "hal_cuda_pdegrid_update", false));
     const int64_t n = h->Length();
-    halcuda::Commit<<<halcuda::StrideBlocks(n), 256, 0, h->stream.Get()>>>(n, h->f.p, h->d.p);
+    if (h->pendingAll)
+    {
+        h->pendingAll = false;
+        halcuda::ApplyAllCommit<<<halcuda::StrideBlocks(n), 256, 0, h->stream.Get()>>>(
+            h->pendingOp, h->pendingValue, n, h->f.p, h->d.p);
+    }
+    else
+    {
+        halcuda::Commit<<<halcuda::StrideBlocks(n), 256, 0, h->stream.Get()>>>(n, h->f.p, h->d.p);
+    }
     halcuda::CountLaunch();
     h->updateCt++;
     return LaunchStatus("hal_cuda_pdegrid_update");
@@ -1492,7 +1540,7 @@ extern "C" void *hal_cuda_pdegrid_stream(hal_cuda_pdegrid *h)
 
 extern "C" int hal_cuda_pdegrid_set_stream(hal_cuda_pdegrid *h, void *stream)
 {
-    HAL_REQUIRE(h != nullptr, "hal_cuda_pdegrid_set_stream: handle is NULL");
+    HAL_TRY(Prepare(h, "hal_cuda_pdegrid_set_stream"));  // a pending *All runs on the old stream
     h->stream.Set(stream);
     return HAL_CUDA_OK;
 }

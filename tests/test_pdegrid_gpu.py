@@ -171,6 +171,39 @@ def test_pdegrid_adi_1024_bit_exact(hal, oracle, wx, wy, dirichlet):
     assert np.abs(d).max() > 0
 
 
+@pytest.mark.parametrize("batch", [False, True])
+def test_pdegrid_deferred_all_calls(hal, oracle, batch):
+    """A value-form SetAll / AddAll / MulAll runs inside the next Update's
+    pass, or before any other call: sequences that follow it with another
+    *All, a per-cell list, a query of the deltas, an operator, a per-cell
+    *All, a stream change or the Update itself equal the reference's calls
+    one by one."""
+    from pyoracle import PDEScript
+
+    xd, yd = 97, 130
+    rng = np.random.default_rng(31)
+    f0 = rng.random(xd * yd)
+    sc = PDEScript(xd, yd)
+    sc.add("mul_all", d0=-0.01).add("update")
+    sc.add("mul_all", d0=-0.02).add("add_all", d0=0.003).add("update")
+    sc.add("add_all", d0=0.01).add("max_delta").add("max_delta_scaled", d0=0.5).add("update")
+    sc.add("set_all", d0=0.25).add("get", i=17).add("set", i=5, d0=0.9).add("update")
+    sc.add("mul_all", d0=-0.05).add("diffusion", d0=0.1).add("update")
+    sc.add("mul_all", d0=-0.03).add("set_all_values", arrays=[rng.random(xd * yd)]).add("update")
+    sc.add("mul_all", d0=-0.04).add("adi", d0=2.0).add("mul_all", d0=0.5).add("update").add("max").add("avg")
+    ef, ed, euc, erec = oracle.pdegrid_script(sc, f0)
+    with hal.PDEGrid(xd, yd) as grid:
+        grid.set_state(f0)
+        rec = run_on_device(hal, grid, sc, batch)
+        grid.apply_all(2, -0.07)
+        grid.set_stream(None)
+        f1, d1, _ = grid.get_state()
+        f, d, uc = grid.get_state()
+    # the trailing MulAll is pending until get_state runs it
+    assert np.array_equal(f, ef) and np.array_equal(d1, ed + ef * -0.07) and uc == euc
+    _check_records(rec, erec, sc)
+
+
 def _plan_diagonals(r, n=64, end_adjust=-1.0):
     """TdmaSolver::TDMA's modified diagonal of a line's ADI matrix
     (off-diagonal -r/2, diagonal 1 - w * off, w = 2 + end_adjust at the
