@@ -462,7 +462,11 @@ int hal_cuda_pdegrid_apply_agents(hal_cuda_pdegrid *h, hal_cuda_agents *agents, 
                                   double value, const double *perAgent);
 
 /* SetAll / AddAll / MulAll (PDEGrid2D.h:188-217): the operation at every
- * cell; perCell (xDim*yDim, may be NULL) replaces value (SetAll(pVals)). */
+ * cell; perCell (xDim*yDim, may be NULL) replaces value (SetAll(pVals)).
+ * The value form (perCell NULL) is recorded and runs at the start of the next
+ * call on the handle, or, when that call is hal_cuda_pdegrid_update, inside
+ * its pass; results are the same as running it at once, and a launch failure
+ * is reported by that next call. */
 int hal_cuda_pdegrid_apply_all(hal_cuda_pdegrid *h, int32_t op, double value, const double *perCell);
 
 /* Update (PDEGrid2D.h:178-186) and SetNonNegative (:244-255). */
